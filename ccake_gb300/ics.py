@@ -1,0 +1,165 @@
+"""Synthetic initial conditions and run configurations for the SPH hot path.
+
+Every workload here is generated in memory with a seeded generator; no dataset
+is read. Units are the reference's internal ones: positions in fm (eta is
+dimensionless), energy density in fm^-4 (GeV/fm^3 divided by hbar*c),
+charge densities in fm^-3, temperatures in fm^-1.
+
+Workloads
+---------
+gubser_2d       ideal 2+1-D Gubser flow, conformal EoS (the analytic-oracle case)
+hotspots_2d     viscous 2+1-D BSQ run, 30 Gaussian hot spots, conformal-diagonal EoS
+hotspots_3d     viscous 3+1-D Milne run, tabulated EoS (see ``eos_table``)
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+
+import numpy as np
+
+HBARC_GEVFM = 0.1973269804   # include/constants.h:16 of the reference
+HBARC_MEVFM = 197.3269804
+
+# Reference conformal constant: c = pi^2 (2 (Nc^2 - 1) + 3.5 Nc Nf) / 90 with
+# Nc = 3, Nf = 2.5 (src/eos_initialization.cpp:226-229); p = c T^4.
+C_REFERENCE = math.pi ** 2 * (2.0 * (3.0 * 3.0 - 1.0) + 3.5 * 3.0 * 2.5) / 90.0
+
+
+@dataclasses.dataclass
+class RunConfig:
+    """Mirror of the C ``ccake_config`` (and of the oracle's ``Config``)."""
+    dim: int = 2
+    coord: int = 0                 # 0 Milne ("hyperbolic"), 1 Cartesian
+    eos_kind: int = 0              # 0 conformal, 1 conformal_diagonal, 2 table
+    using_shear: int = 0
+    using_vorticity: int = 0
+    shear_relax_mode: int = 0      # 0 default max(5 eta/w, 0.005), 1 "Gubser" 5 eta/w
+    zeta_mode: int = 1             # 0 default, 1 constant, 2 cs2-dependent, 3 peaked
+    factorized_kernel: int = 0
+    input_as_entropy: int = 0
+    modulate_zeta_with_tanh: int = 0
+    thermo_mode: int = 0           # 0 reference derivative chain, 1 exact Hessian inverse
+    hT: float = 0.1
+    hEta: float = 0.1
+    t0: float = 1.0
+    dt: float = 0.001
+    eos_c: float = C_REFERENCE
+    eos_T0: float = 1.0
+    eos_muB0: float = 1.0
+    eos_muQ0: float = 1.0
+    eos_muS0: float = 1.0
+    eta_over_s: float = 0.0
+    zeta_over_s: float = 0.0
+    zeta_cs2_A: float = 1.67552
+    zeta_cs2_p: float = 2.0
+    zeta_peak_T: float = 0.16 / HBARC_GEVFM
+    zeta_peak_width: float = 0.02 / HBARC_GEVFM
+    xmin: float = -5.0
+    ymin: float = -5.0
+    etamin: float = -0.1
+    freeze_out_T: float = 150.0 / HBARC_MEVFM
+
+
+@dataclasses.dataclass
+class Particles:
+    """Host struct-of-arrays input (the reference's ccake IC columns)."""
+    x: np.ndarray
+    y: np.ndarray
+    eta: np.ndarray
+    e: np.ndarray          # energy density, fm^-4 (or entropy density when input_as_entropy)
+    rhoB: np.ndarray
+    rhoS: np.ndarray
+    rhoQ: np.ndarray
+    ux: np.ndarray
+    uy: np.ndarray
+    ueta: np.ndarray
+
+    @property
+    def n(self) -> int:
+        return int(self.x.shape[0])
+
+    def take(self, idx) -> "Particles":
+        return Particles(*(getattr(self, f.name)[idx] for f in dataclasses.fields(self)))
+
+
+def lattice_2d(nx: int, ny: int, dx: float, xmin: float, ymin: float):
+    """Lattice points x_i = xmin + i*dx in FP64 (row-major, x fastest)."""
+    i = np.arange(nx, dtype=np.float64)
+    j = np.arange(ny, dtype=np.float64)
+    xs = xmin + i * dx
+    ys = ymin + j * dx
+    X, Y = np.meshgrid(xs, ys, indexing="xy")
+    return X.ravel().copy(), Y.ravel().copy()
+
+
+def gubser_temperature(tau, r, q=1.0, That0=1.2):
+    """Ideal Gubser temperature (fm^-1), BASELINE config 1 formula."""
+    num = (That0 / tau ** (1.0 / 3.0)) * (2.0 * q) ** (2.0 / 3.0)
+    den = (1.0 + 2.0 * q * q * (tau * tau + r * r) + q ** 4 * (tau * tau - r * r) ** 2) ** (1.0 / 3.0)
+    return num / den
+
+
+def gubser_ur(tau, r, q=1.0):
+    """Radial spatial four-velocity u^r = sinh(kappa), tanh(kappa) = v^r
+    (utilities/ideal_gubser_ic_generator.py:31-36 of the reference)."""
+    kap = np.arctanh(2.0 * q * q * tau * r / (1.0 + q * q * tau * tau + q * q * r * r))
+    return np.sinh(kap)
+
+
+def gubser_2d(n_side=200, dx=0.05, h=0.1, tau0=1.0, dt=0.001, c_e=15.6269, q=1.0, That0=1.2):
+    """Config 1: ideal Gubser flow on an n_side^2 lattice over [-5, 5)^2.
+
+    ``c_e`` is the coefficient of e = c_e T^4; the conformal EoS is set to
+    p = (c_e/3) T^4 so the analytic solution applies. Pass ``c_e = 3*C_REFERENCE``
+    for the reference's own constant.
+    """
+    xmin = -0.5 * n_side * dx
+    x, y = lattice_2d(n_side, n_side, dx, xmin, xmin)
+    r = np.sqrt(x * x + y * y)
+    T = gubser_temperature(tau0, r, q, That0)
+    e = c_e * T ** 4
+    ur = gubser_ur(tau0, r, q)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        ux = np.where(r > 0, ur * x / np.where(r > 0, r, 1.0), 0.0)
+        uy = np.where(r > 0, ur * y / np.where(r > 0, r, 1.0), 0.0)
+    z = np.zeros_like(x)
+    p = Particles(x, y, z.copy(), e, z.copy(), z.copy(), z.copy(), ux, uy, z.copy())
+    cfg = RunConfig(dim=2, eos_kind=0, using_shear=0, hT=h, t0=tau0, dt=dt,
+                    eos_c=c_e / 3.0, xmin=xmin, ymin=xmin, etamin=-0.1, zeta_mode=1,
+                    zeta_over_s=0.0, eta_over_s=0.0)
+    return p, cfg
+
+
+def hotspots_2d(n_side=400, dx=0.05, h=0.1, n_hot=30, sigma=0.4, seed=20251203, tau0=1.0,
+                dt=0.001, eta_over_s=0.08, floor_GeV=0.01, peak_range=(5.0, 50.0)):
+    """Config 2: 30 Gaussian hot spots (sigma 0.4 fm), centres ~ N(0, 3 fm),
+    peaks ~ U[5, 50] GeV/fm^3, plus a uniform floor of ``floor_GeV`` GeV/fm^3
+    so that every lattice particle carries matter. rhoB = e[GeV/fm^3]/20 fm^-3,
+    rhoS = 0, rhoQ = 0.4 rhoB. Conformal-diagonal EoS with the reference
+    constants, eta/s = 0.08 with tau_pi = 5 eta/w ("Gubser"), zeta = 0, u = 0.
+    Generator: numpy PCG64 with the given seed.
+
+    The enthalpy derivatives use the exact inverse of the susceptibility
+    matrix (``thermo_mode=1``): with two non-zero charges the reference's
+    Schur-complement chain divides by its 1e-25 cross-susceptibility
+    placeholders for this EoS and returns dw/drho_B ~ -1e20, after which the
+    evolution is not finite.
+    """
+    rng = np.random.Generator(np.random.PCG64(seed))
+    cx = rng.normal(0.0, 3.0, n_hot)
+    cy = rng.normal(0.0, 3.0, n_hot)
+    amp = rng.uniform(peak_range[0], peak_range[1], n_hot)
+    xmin = -0.5 * n_side * dx
+    x, y = lattice_2d(n_side, n_side, dx, xmin, xmin)
+    eG = np.full_like(x, floor_GeV)
+    for k in range(n_hot):
+        eG += amp[k] * np.exp(-((x - cx[k]) ** 2 + (y - cy[k]) ** 2) / (2.0 * sigma * sigma))
+    rhoB = eG / 20.0
+    rhoQ = 0.4 * rhoB
+    z = np.zeros_like(x)
+    p = Particles(x, y, z.copy(), eG / HBARC_GEVFM, rhoB, z.copy(), rhoQ, z.copy(), z.copy(), z.copy())
+    cfg = RunConfig(dim=2, eos_kind=1, using_shear=1 if eta_over_s > 1e-10 else 0,
+                    shear_relax_mode=1, thermo_mode=1, zeta_mode=1, zeta_over_s=0.0, eta_over_s=eta_over_s,
+                    hT=h, t0=tau0, dt=dt, xmin=xmin, ymin=xmin, etamin=-0.1)
+    return p, cfg

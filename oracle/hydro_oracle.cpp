@@ -1,0 +1,696 @@
+// CPU oracle: transport coefficients, shear-tensor constraints, the MRF
+// equations of motion (ideal + shear + bulk, Milne coordinates), the midpoint
+// RK2 evolver, conservation sums and initialisation.
+// TEST INFRASTRUCTURE ONLY (see oracle.hpp).
+#include "oracle.hpp"
+#include "table_oracle.hpp"
+
+#include <algorithm>
+#include <cmath>
+
+namespace orc {
+
+namespace {
+
+// Milne index helpers (include/milne.hpp). Vector<D>::make_covariant flips the
+// sign of every component and, except in 2-D, multiplies the last one by t^2
+// (:92-96, 2-D specialisation :354); make_contravariant is the inverse (:103-107).
+inline void cov_D(int D, double* v, double t2) {
+  if (D == 2) { v[0] = -v[0]; v[1] = -v[1]; return; }
+  for (int i = 0; i < D - 1; i++) v[i] = -v[i];
+  v[D - 1] *= -t2;
+}
+inline void contra_D(int D, double* v, double t2) {
+  if (D == 2) { v[0] = -v[0]; v[1] = -v[1]; return; }
+  for (int i = 0; i < D - 1; i++) v[i] = -v[i];
+  v[D - 1] *= -1. / t2;
+}
+// delta_i_eta<D> (:1095-1110). In 2-D the reference also reads index 2 of a
+// two-element vector (out of bounds); that read is taken as zero here.
+inline double dEta(int D, int i) { return (D == 3 && i == 2) ? 1.0 : 0.0; }
+
+struct Coefs {
+  double eta, tau_pi, zeta, tau_Pi, delta_PiPi, delta_pipi, lambda_piPi, lambda_Pipi, phi1, phi3,
+      phi6, phi7, tau_pipi;
+};
+
+// src/transport_coefficients.cpp:620-900
+double eta_of(const Config& c, double T, double w) {
+  if (T <= 0.0) return 0.0;
+  return c.eta_over_s * (w / T);
+}
+double tau_pi_of(const Config& c, double eta, double w) {
+  if (c.shear_relax_mode == kTauPiGubser) return (5.0 * eta) / w;
+  if (c.shear_relax_mode == kTauPiMinval) return std::max((5.0 * eta) / w, 0.001);
+  return std::max(5.0 * eta / w, 0.005);
+}
+double zeta_of(const Config& c, double T, double w, double cs2) {
+  switch (c.zeta_mode) {
+    case kZetaConstant: return c.zeta_over_s * (w / T);
+    case kZetaCs2: {
+      double factor = 1.0;
+      if (c.modulate_zeta_with_tanh) {
+        const double Ttr = 150.0 / kHbarcMeVfm, Tsc = 10.0 / kHbarcMeVfm;
+        double th = std::tanh((T - Ttr) / Tsc), xp = std::pow(T / Ttr, c.zeta_cs2_p);
+        factor = 0.5 * (1.0 + xp) + 0.5 * (1.0 - xp) * th;
+      }
+      double zs = c.zeta_cs2_A * factor * std::pow((1.0 / 3.0) - std::min(cs2, 1.0), c.zeta_cs2_p);
+      return zs * w / T;
+    }
+    case kZetaPeaked: {
+      // zeta/s peaked at T = zeta_peak_T (Gaussian of width zeta_peak_width),
+      // height zeta_over_s: the bulk mode requested for the 3+1-D run.
+      double x = (T - c.zeta_peak_T) / c.zeta_peak_width;
+      return c.zeta_over_s * std::exp(-0.5 * x * x) * (w / T);
+    }
+    default: return 0.005 * (w / T);
+  }
+}
+double tau_Pi_of(const Config& c, double zeta, double w, double cs2) {
+  const double p = c.zeta_cs2_p;
+  const double cc = cs2 > 1 ? 1 : cs2;
+  if (std::pow((1.0 / 3.0 - cc), p) < 1e-10) return 1e10;
+  return std::max(5.0 * zeta / (std::pow((1.0 / 3.0 - cc), p) * w), 0.1);
+}
+
+Coefs coefs(const Config& c, const double* th) {
+  Coefs k;
+  const double T = th[kT], w = th[kW], cs2 = th[kCs2], p = th[kP];
+  k.eta = eta_of(c, T, w);
+  k.tau_pi = tau_pi_of(c, k.eta, w);
+  k.zeta = zeta_of(c, T, w, cs2);
+  k.tau_Pi = tau_Pi_of(c, k.zeta, w, cs2);
+  k.delta_PiPi = 2. * k.tau_Pi / 3.0;
+  k.delta_pipi = 4. * k.tau_pi / 3.0;
+  k.lambda_piPi = 6. / 5. * k.tau_pi;
+  const double cc = cs2 > 1 ? 1 : cs2;
+  k.lambda_Pipi = 8. * (1. / 3. - cc) * k.tau_Pi / 5.;
+  k.phi1 = 0.0;
+  k.phi3 = 0.0;
+  k.phi6 = 0.0;
+  k.phi7 = 9. / (70. * p);
+  k.tau_pipi = 10. * k.tau_pi / 7.0;
+  return k;
+}
+
+inline double gamma_of(int D, const double* u, double t2) {
+  double uc[3] = {u[0], u[1], u[2]};
+  cov_D(D, uc, t2);
+  double c = 0;
+  for (int i = 0; i < D; i++) c += uc[i] * u[i];
+  return std::sqrt(1 - c);
+}
+
+// inverse of a D x D matrix by cofactors (include/milne.hpp:788-834)
+void inverse(int D, const double* A, double* Ai) {
+  if (D == 1) { Ai[0] = 1. / A[0]; return; }
+  if (D == 2) {
+    double det = A[0] * A[3] - A[1] * A[2];
+    Ai[0] = A[3] / det; Ai[1] = -A[1] / det; Ai[2] = -A[2] / det; Ai[3] = A[0] / det;
+    return;
+  }
+#define M(i, j) A[(i) * 3 + (j)]
+  double det = M(0, 0) * M(1, 1) * M(2, 2) + M(0, 1) * M(1, 2) * M(2, 0) + M(0, 2) * M(1, 0) * M(2, 1) -
+               M(0, 2) * M(1, 1) * M(2, 0) - M(0, 1) * M(1, 0) * M(2, 2) - M(0, 0) * M(1, 2) * M(2, 1);
+  Ai[0] = (M(1, 1) * M(2, 2) - M(1, 2) * M(2, 1)) / det;
+  Ai[1] = (M(0, 2) * M(2, 1) - M(0, 1) * M(2, 2)) / det;
+  Ai[2] = (M(0, 1) * M(1, 2) - M(0, 2) * M(1, 1)) / det;
+  Ai[3] = (M(1, 2) * M(2, 0) - M(1, 0) * M(2, 2)) / det;
+  Ai[4] = (M(0, 0) * M(2, 2) - M(0, 2) * M(2, 0)) / det;
+  Ai[5] = (M(0, 2) * M(1, 0) - M(0, 0) * M(1, 2)) / det;
+  Ai[6] = (M(1, 0) * M(2, 1) - M(1, 1) * M(2, 0)) / det;
+  Ai[7] = (M(0, 1) * M(2, 0) - M(0, 0) * M(2, 1)) / det;
+  Ai[8] = (M(0, 0) * M(1, 1) - M(0, 1) * M(1, 0)) / det;
+#undef M
+}
+
+// Per-particle output of the shear MRF assembly.
+struct ShearMRF {
+  double M0i[9], F0i[3], Mnab[3], Fnab;
+  double Mext[2][3][3], Fext[2][3];
+};
+
+// src/eom_default.cpp:882-1412 (calculate_MRF_shear) for one particle.
+void shear_mrf(const System& s, int a, double t, bool use_vort, ShearMRF& o) {
+  const int D = s.cfg.dim;
+  const double t2 = t * t;
+  const double cmd[4] = {1.0, -1.0, -1.0, -1.0 / t / t};
+  const double sigma = s.sigma[a], g = s.gamma[a];
+  const double eta = s.eta_pi[a], phi6 = s.phi6[a], phi7 = s.phi7[a], lpP = s.lambda_piPi[a];
+  const double tpp = s.tau_pipi[a], dpp = s.delta_pipi[a], tpi = s.tau_pi[a];
+  const double tdelta = dpp - tpi;
+  const double Pi = s.bulk[a];
+  double u[3] = {0, 0, 0}, uc[3], v[3] = {0, 0, 0}, fu[3] = {0, 0, 0}, fuc[3];
+  for (int i = 0; i < D; i++) { u[i] = s.u[i][a]; v[i] = s.v[i][a]; fu[i] = u[i]; }
+  for (int i = 0; i < 3; i++) { uc[i] = u[i]; fuc[i] = fu[i]; }
+  cov_D(D, uc, t2);
+  fuc[0] = -fuc[0]; fuc[1] = -fuc[1]; fuc[2] *= -t2;  // Vector<3> make_covariant
+  double pi[4][4], hy[4][4], pc[4][4];
+  for (int i = 0; i < 4; i++) for (int j = 0; j < 4; j++) pi[i][j] = s.shv[i * 4 + j][a];
+  // shv_hybrid = pi^mu_nu (Matrix<4,4>::make_covariant slot 1), shv_cov slot 0 on top
+  for (int i = 0; i < 4; i++) for (int j = 0; j < 4; j++) {
+      double f = (j == 1 || j == 2) ? -1.0 : (j == 3 ? -t2 : 1.0);
+      hy[i][j] = pi[i][j] * f;
+    }
+  for (int i = 0; i < 4; i++) for (int j = 0; j < 4; j++) {
+      double f = (i == 1 || i == 2) ? -1.0 : (i == 3 ? -t2 : 1.0);
+      pc[i][j] = hy[i][j] * f;
+    }
+  const double geo = dEta(D, D - 1) * u[D - 1] * u[D - 1] * t / g;
+  double gV[3][3] = {{0}}, divV = 0;
+  for (int i = 0; i < D; i++) {
+    divV += s.gradV[i * D + i][a];
+    for (int j = 0; j < D; j++) gV[i][j] = s.gradV[i * D + j][a];
+  }
+  double gu[3][3] = {{0}}, gu0[3] = {0, 0, 0};
+  for (int i = 0; i < D; i++)
+    for (int j = 0; j < D; j++) {
+      gu[i][j] = g * gV[i][j];
+      for (int k = 0; k < D; k++) gu[i][j] += -g * u[j] * uc[k] * gV[i][k];
+    }
+  for (int i = 0; i < D; i++) {
+    double acc = 0;
+    for (int j = 0; j < D; j++) acc += gu[i][j] * uc[j];
+    gu0[i] = -1. * acc / g;
+  }
+  double gu0c[3] = {gu0[0], gu0[1], gu0[2]};
+  contra_D(D, gu0c, t2);
+  double cgu[3][3] = {{0}};  // contravariant first index, zero padded to 3x3
+  for (int i = 0; i < D; i++)
+    for (int j = 0; j < D; j++) {
+      double f = (D == 2) ? -1.0 : (i < D - 1 ? -1.0 : -1.0 / t2);
+      cgu[i][j] = gu[i][j] * f;
+    }
+  double gu3[3][3] = {{0}};
+  for (int i = 0; i < D; i++) for (int j = 0; j < D; j++) gu3[i][j] = gu[i][j];
+
+  double guv[3] = {0, 0, 0};  // contract(grad_uj, v, FirstIndex)
+  for (int j = 0; j < D; j++) for (int k = 0; k < D; k++) guv[j] += gu[k][j] * v[k];
+  double gu0v = 0;
+  for (int k = 0; k < D; k++) gu0v += gu0[k] * v[k];
+
+  double v_gradu_shv[3], gugs[3], sgu[3], vsgu[3];
+  for (int i = 0; i < D; i++) {
+    v_gradu_shv[i] = 0.0;
+    for (int j = 0; j < D; j++) v_gradu_shv[i] += guv[j] * hy[i + 1][j + 1];
+    v_gradu_shv[i] += gu0v * hy[i + 1][0];
+    gugs[i] = 0.0;
+    for (int j = 0; j < D; j++) gugs[i] += cgu[i][j] * hy[0][j + 1];
+    gugs[i] += cmd[i + 1] * gu0[i] * hy[0][0];
+    sgu[i] = 0.0;
+    for (int j = 0; j < D; j++) sgu[i] += pi[j + 1][0] * gu[j][i] + pi[j + 1][i + 1] * gu0[j];
+    vsgu[i] = 0.0;
+    for (int j = 0; j < D; j++) vsgu[i] += v[j] * pi[0][0] * gu[j][i] + v[j] * pi[0][i + 1] * gu0[j];
+  }
+  double sgu_s = 0.0;
+  for (int i = 0; i < D; i++) {
+    for (int j = 0; j < D; j++) sgu_s += (hy[i + 1][j + 1] - v[i] * hy[0][j + 1]) * gu[i][j];
+    sgu_s += (hy[i + 1][0] - v[i] * hy[0][0]) * gu0[i];
+  }
+  double ss = 0.0;
+  for (int i = 0; i < 4; i++) for (int j = 0; j < 4; j++) ss += pi[i][j] * pc[i][j];
+  double sl0[3];
+  for (int i = 0; i < D; i++) {
+    sl0[i] = 0.0;
+    for (int j = 0; j < 4; j++) sl0[i] += (pi[0][j] * hy[i + 1][j] + pi[i + 1][j] * hy[0][j]) / 2.;
+  }
+  const double uD = u[D - 1];
+  const double expn = geo + g / t + g * divV;
+  double Fs[3], FD[3], Fds[3], Fdo[3], Fdd[3], Ms[3][3], MD[3][3], Mds[3][3], Mdo[3][3], Mdd[3][3];
+  for (int i = 0; i < D; i++) {
+    const double di = dEta(D, i);
+    Fs[i] = -(guv[i] - gu0c[i]) / 2. + u[i] * g * (geo + g / t + g * divV) / 3. - g * geo * u[i] / 2.;
+    FD[i] = g * (u[i] * hy[0][0] + g * hy[i + 1][0]) * geo + t * uD * pi[3][i + 1] * di;
+    Fds[i] = -(v_gradu_shv[i] - gugs[i] - 4. * g * u[i] * sgu_s / 3. - sgu[i] + vsgu[i]) / 4. +
+             (hy[i + 1][0] - g * g * hy[i + 1][0] - g * u[i] * hy[0][0] + pi[0][i + 1] +
+              4. * u[i] * g * hy[0][0] / 3.) * geo / 4. +
+             (g * cmd[i + 1] * hy[0][3] * di / t + g * pi[3][0] * di / t +
+              4. * g * u[i] * (g * hy[3][3] / t) / 3.) / 4. -
+             pi[0][i + 1] * (g / t + geo + g * divV) / 3.;
+    Fdo[i] = -(v_gradu_shv[i] - gugs[i] + sgu[i] - vsgu[i]) / 4. +
+             (hy[i + 1][0] - g * g * hy[i + 1][0] - g * u[i] * hy[0][0] - pi[0][i + 1]) * geo / 4. +
+             (g * cmd[i + 1] * hy[0][3] * di / t - g * pi[3][0] * di / t) / 4.;
+    Fdd[i] = pi[i + 1][0] * expn;
+    for (int j = 0; j < D; j++) {
+      Ms[i][j] = u[i] * uc[j] / (2. * 3.);
+      MD[i][j] = g * u[i] * (hy[0][j + 1] - hy[0][0] * uc[j] / g) + g * g * (hy[i + 1][j + 1] - hy[i + 1][0] * uc[j] / g);
+      Mds[i][j] = (hy[i + 1][j + 1] - hy[i + 1][0] * uc[j] / g - g * g * hy[i + 1][j + 1] - g * u[i] * hy[0][j + 1] +
+                   uc[j] * g * hy[i + 1][0] + uc[j] * u[i] * hy[0][0] +
+                   4. * g * u[i] * (hy[0][j + 1] - hy[0][0] * uc[j] / g) / 3. +
+                   (-pi[0][i + 1] + 4. * pi[0][i + 1] / 3.) * uc[j] / g) / 4.;
+      Mdo[i][j] = (hy[i + 1][j + 1] - hy[i + 1][0] * uc[j] / g - g * g * hy[i + 1][j + 1] - g * u[i] * hy[0][j + 1] +
+                   uc[j] * g * hy[i + 1][0] + uc[j] * u[i] * hy[0][0] + pi[0][i + 1] * uc[j] / g) / 4.;
+      Mdd[i][j] = -pi[i + 1][0] * uc[j] / g;
+    }
+    Ms[i][i] += (1. - g * g) / 2.;
+    Mdo[i][i] += -pi[0][0] / 4.;
+    Mds[i][i] += +pi[0][0] / 4.;
+    Fs[i] += di * (-(-uD * t - uD / t + g * uD * uD * t + 2. * g * g * uD / t) / 2.);
+    FD[i] += di * (uD * pi[0][0] / t + g * pi[3][0] / t);
+    if (D != 2) {
+      Fds[i] += (t * uD * di * cmd[i + 1] * hy[0][0] + uD * hy[i + 1][3] * g / t / 4. + hy[i + 1][3] * t * uD +
+                 pi[0][0] * di * uD / t + t * uD * uD * (g * hy[i + 1][0] + u[i] * hy[0][0]) +
+                 2. * g * uD * (g * hy[i + 1][3] + u[i] * pi[0][3]) / t) / 4. +
+                g * u[i] * (hy[3][0] * uD * t + uD * hy[0][3] / t) / 3.;
+      Fdo[i] += (t * uD * di * cmd[i + 1] * hy[0][0] + uD * hy[i + 1][3] * g / t - hy[3][i + 1] * t * uD -
+                 pi[0][0] * di * uD / t + t * uD * uD * (g * hy[i + 1][0] + u[i] * hy[0][0]) +
+                 2. * g * uD * (g * hy[i + 1][3] + u[i] * pi[0][3]) / t) / 4.;
+    }
+  }
+  double Fnab = 0.0;
+  for (int i = 0; i < D; i++) {
+    o.Mnab[i] = hy[0][i + 1] - hy[0][0] * uc[i] / g;
+    for (int j = 0; j < D; j++) Fnab += (hy[i + 1][j + 1] - v[i] * hy[0][j + 1]) * gu[i][j];
+    Fnab += (hy[i + 1][0] - v[i] * hy[0][0]) * gu0[i];
+  }
+  Fnab += +hy[3][3] * g / t + hy[0][0] * geo + (t * hy[3][0] + hy[0][3] / t) * uD * dEta(D, D - 1);
+  o.Fnab = Fnab;
+  const double uv = use_vort ? 1.0 : 0.0;
+  for (int i = 0; i < D; i++) {
+    o.F0i[i] = (-pi[i + 1][0] - tpi * FD[i] - dpp * Fdd[i] + 2. * tpi * Fdo[i] * uv - tpp * Fds[i] +
+                (2. * eta + lpP * Pi) * Fs[i] + phi6 * Pi * pi[i + 1][0] + phi7 * (sl0[i] + g * u[i] * ss / 3.)) /
+               (tpi * g);
+    for (int j = 0; j < D; j++)
+      o.M0i[i * D + j] = (-tpi * MD[i][j] - dpp * Mdd[i][j] + 2. * tpi * Mdo[i][j] * uv - tpp * Mds[i][j] +
+                          (2. * eta + lpP * Pi) * Ms[i][j]) / (tpi * g);
+  }
+  // shear-tensor evolution (2x3 upper block, i <= j)
+  double gugjs[2][3], sigu[2][3], vsig[2][3], sml[2][3];
+  for (int i = 0; i < 2; i++)
+    for (int j = i; j < 3; j++) {
+      gugjs[i][j] = sigu[i][j] = vsig[i][j] = sml[i][j] = 0.0;
+      for (int k = 0; k < D; k++) {
+        gugjs[i][j] += cgu[i][k] * hy[j + 1][k + 1] + cgu[j][k] * hy[i + 1][k + 1];
+        sigu[i][j] += pi[k + 1][i + 1] * gu3[k][j] + pi[k + 1][j + 1] * gu3[k][i];
+        vsig[i][j] += v[k] * pi[0][i + 1] * gu3[k][j] + v[k] * pi[0][j + 1] * gu3[k][i];
+      }
+      for (int k = 0; k < 4; k++) sml[i][j] += (pi[i + 1][k] * hy[j + 1][k] + pi[j + 1][k] * hy[i + 1][k]) / 2.;
+    }
+  double FD2[2][3] = {{0}}, Fsg[2][3] = {{0}}, Fdl[2][3] = {{0}}, Fdo2[2][3] = {{0}}, Fds2[2][3] = {{0}};
+  double MD2[2][3][3] = {{{0}}}, Msg[2][3][3] = {{{0}}}, Mdl[2][3][3] = {{{0}}}, Mdo2[2][3][3] = {{{0}}},
+         Mds2[2][3][3] = {{{0}}};
+  const double f2 = fu[2];
+  for (int i = 0; i < 2; i++) {
+    for (int j = i; j < 3; j++) {
+      const double di = dEta(D, i), dj = dEta(D, j);
+      FD2[i][j] = g * geo * (fu[i] * hy[j + 1][0] + fu[j] * hy[i + 1][0]);
+      Fsg[i][j] = cgu[i][j] / 2. + cgu[j][i] / 2. + fu[i] * fu[j] * expn / 3.;
+      Fdl[i][j] = pi[i + 1][j + 1] * expn;
+      const double common =
+          t * f2 * (cmd[i + 1] * hy[j + 1][0] * di + cmd[j + 1] * hy[i + 1][0] * dj) +
+          g * (cmd[i + 1] * hy[j + 1][3] * di + cmd[j + 1] * hy[i + 1][3] * dj) / t +
+          f2 * f2 * t * (fu[i] * hy[j + 1][0] + fu[j] * hy[i + 1][0]) +
+          2. * g * f2 * (fu[i] * hy[j + 1][3] + fu[j] * hy[i + 1][3]) / t;
+      const double cross = g * (pi[3][i + 1] * dj + pi[3][j + 1] * di) / t +
+                           f2 * (pi[0][i + 1] * dj + pi[0][j + 1] * di) / t;
+      Fdo2[i][j] = -(-gugjs[i][j] + sigu[i][j] - vsig[i][j]) / 4. +
+                   (-fu[i] * g * hy[j + 1][0] - fu[j] * g * hy[i + 1][0]) * geo / 4. + (common - cross) / 4.;
+      Fds2[i][j] = -(-gugjs[i][j] - sigu[i][j] + vsig[i][j] - 4. * (fu[i] * fu[j]) * sgu_s / 3.) / 4. +
+                   (-fu[i] * g * hy[j + 1][0] - fu[j] * g * hy[i + 1][0] + 4. * fu[i] * fu[j] * hy[0][0] / 3.) * geo / 4. +
+                   (common + cross +
+                    4. * fu[i] * fu[j] * (hy[3][0] * f2 * t + g * hy[3][3] / t + f2 * hy[0][3] / t) / 3.) / 4. -
+                   pi[i + 1][j + 1] * (g / t + geo + g * divV) / 3.;
+      for (int k = 0; k < D; k++) {
+        MD2[i][j][k] = g * (fu[i] * hy[j + 1][k + 1] - fu[i] * hy[j + 1][0] * fuc[k] / g + fu[j] * hy[i + 1][k + 1] -
+                            fu[j] * hy[i + 1][0] * fuc[k] / g);
+        Msg[i][j][k] = -fu[i] * fu[j] * fuc[k] / (3. * g);
+        Mdl[i][j][k] = -pi[i + 1][j + 1] * fuc[k] / g;
+        Mdo2[i][j][k] = (-fu[i] * hy[j + 1][k + 1] * g - fu[j] * hy[i + 1][k + 1] * g + fuc[k] * fu[i] * hy[j + 1][0] +
+                         fuc[k] * fu[j] * hy[i + 1][0]) / 4.;
+        Mds2[i][j][k] = (-fu[i] * hy[j + 1][k + 1] * g - fu[j] * hy[i + 1][k + 1] * g + fuc[k] * fu[i] * hy[j + 1][0] +
+                         fuc[k] * fu[j] * hy[i + 1][0] +
+                         4. * fu[i] * fu[j] * (hy[0][k + 1] - hy[0][0] * fuc[k] / g) / 3. +
+                         4. * pi[i + 1][j + 1] * fuc[k] / 3. / g) / 4.;
+      }
+      Mds2[i][j][i] += pi[0][j + 1] / 4.;
+      Mdo2[i][j][i] += -pi[0][j + 1] / 4.;
+      Msg[i][j][i] += -g * fu[j] / 2.;
+    }
+    for (int j = i; j < D; j++) {
+      Msg[i][j][j] += -g * fu[i] / 2.;
+      Mds2[i][j][j] += pi[0][i + 1] / 4.;
+      Mdo2[i][j][j] += -pi[0][i + 1] / 4.;
+    }
+    for (int k = 0; k < D; k++) {
+      Msg[i][i][k] += cmd[i + 1] * fuc[k] / (g * 3.);
+      Mds2[i][i][k] += -cmd[i + 1] * (hy[0][k + 1] - hy[0][0] * fuc[k] / g) / 3.;
+    }
+    FD2[i][2] += g * pi[3][i + 1] / t + f2 * pi[0][i + 1] / t;
+    Fsg[i][i] += -cmd[i + 1] * expn / 3.;
+    Fsg[i][2] += -fu[i] * f2 * f2 * t / 2. - fu[i] * f2 * g / t;
+    Fds2[i][i] += -cmd[i + 1] * sgu_s / 3. - cmd[i + 1] * hy[0][0] * geo / 3. -
+                  cmd[i + 1] * (hy[3][0] * f2 * t + g * hy[3][3] / t + f2 * hy[0][3] / t) / 3.;
+  }
+  for (int i = 0; i < 2; i++) {
+    for (int j = i; j < 3; j++) {
+      o.Fext[i][j] = (-pi[i + 1][j + 1] - tdelta * Fdl[i][j] - tpi * FD2[i][j] + 2. * tpi * Fdo2[i][j] * uv -
+                      tpp * Fds2[i][j] + (2. * eta + lpP * Pi) * Fsg[i][j] + phi6 * Pi * pi[i + 1][j + 1] +
+                      phi7 * (sml[i][j] + fu[i] * fu[j] * ss / 3.)) / (sigma * tpi * g);
+      for (int k = 0; k < D; k++)
+        o.Mext[i][j][k] = (-tpi * MD2[i][j][k] - tdelta * Mdl[i][j][k] + 2. * tpi * Mdo2[i][j][k] * uv -
+                           tpp * Mds2[i][j][k] + (2. * eta + lpP * Pi) * Msg[i][j][k]) / (sigma * tpi * g);
+    }
+    o.Fext[i][i] += phi7 * (-cmd[i + 1] * ss) / (3. * tpi * g * sigma);
+  }
+}
+
+}  // namespace
+
+// src/eom_default.cpp:17-38 (update_velocity)
+void update_velocity(System& s) {
+  const int D = s.cfg.dim;
+  const double t2 = s.t * s.t;
+#pragma omp parallel for
+  for (int a = 0; a < s.n; a++) {
+    double u[3] = {s.u[0][a], s.u[1][a], s.u[2][a]};
+    double g = gamma_of(D, u, t2);
+    s.gamma[a] = g;
+    for (int i = 0; i < D; i++) s.v[i][a] = u[i] / g;
+  }
+}
+
+// src/eom_default.cpp:56-172 (reset_pi_tensor), diffusion part omitted.
+void reset_pi_tensor(System& s) {
+  const int D = s.cfg.dim;
+  const double t2 = s.t * s.t;
+#pragma omp parallel for
+  for (int a = 0; a < s.n; a++) {
+    const double g = s.gamma[a], sig = s.sigma[a];
+    double fu[3] = {0, 0, 0};
+    for (int i = 0; i < D; i++) fu[i] = s.u[i][a];
+    double fc[3] = {-fu[0], -fu[1], -t2 * fu[2]};
+    s.bulk[a] = s.ext_bulk[a] * sig;
+    double p[4][4] = {{0}};
+    const int map[2][3] = {{0, 1, 2}, {-1, 3, 4}};
+    for (int i = 0; i < 2; i++)
+      for (int j = i; j < 3; j++) p[i + 1][j + 1] = s.ext_shv[map[i][j]][a] * sig;
+    for (int i = 1; i < 4; i++) for (int j = i + 1; j < 4; j++) p[j][i] = p[i][j];
+    p[0][0] = (fc[0] * fc[0] * p[1][1] + fc[1] * fc[1] * p[2][2] + 2. * fc[1] * fc[0] * p[2][1] +
+               2. * fc[2] * fc[0] * p[3][1] + 2. * fc[2] * fc[1] * p[3][2] - fc[2] * fc[2] * (p[1][1] + p[2][2]) / t2) /
+              (g * g - fc[2] * fc[2] / (t2));
+    p[3][3] = (p[0][0] - p[1][1] - p[2][2]) / t2;
+    for (int i = 0; i < 3; i++) {
+      double acc = 0.;
+      for (int j = 0; j < 3; j++) acc += -p[i + 1][j + 1] * fc[j] / g;
+      p[0][i + 1] = acc;
+    }
+    for (int i = 1; i < 4; i++) p[i][0] = p[0][i];
+    for (int i = 0; i < 4; i++) for (int j = 0; j < 4; j++) s.shv[i * 4 + j][a] = p[i][j];
+  }
+}
+
+// src/sph_workstation.cpp:1622-1699 (update_all_particle_viscosities)
+void update_viscosities(System& s) {
+#pragma omp parallel for
+  for (int a = 0; a < s.n; a++) {
+    double th[16];
+    for (int k = 0; k < 16; k++) th[k] = s.th[k][a];
+    Coefs k = coefs(s.cfg, th);
+    s.eta_pi[a] = k.eta; s.tau_pi[a] = k.tau_pi; s.zeta_Pi[a] = k.zeta; s.tau_Pi[a] = k.tau_Pi;
+    s.delta_PiPi[a] = k.delta_PiPi; s.delta_pipi[a] = k.delta_pipi; s.lambda_piPi[a] = k.lambda_piPi;
+    s.lambda_Pipi[a] = k.lambda_Pipi; s.phi1[a] = k.phi1; s.phi3[a] = k.phi3; s.phi6[a] = k.phi6;
+    s.phi7[a] = k.phi7; s.tau_pipi[a] = k.tau_pipi;
+  }
+}
+
+// src/sph_workstation.cpp:1713-1772 -> :658-741 (locate_phase_diagram_point_sBSQ):
+// previous (T, mu) and EoS as the seed; thermo set from the solution.
+int update_thermodynamics(System& s) {
+  int failures = 0;
+#pragma omp parallel for reduction(+ : failures)
+  for (int a = 0; a < s.n; a++) {
+    double x[4] = {s.th[kT][a], s.th[kMuB][a], s.th[kMuQ][a], s.th[kMuS][a]};
+    double tgt[4] = {s.th[kS][a], s.th[kRhoB][a], s.th[kRhoS][a], s.th[kRhoQ][a]};
+    int it = 0;
+    int k = eos_invert(s.cfg, s.table, 1, tgt, s.eos_id[a], x, &it);
+    if (k < 0) { s.eos_status[a] = -1; failures++; continue; }
+    double th[16];
+    eos_set_thermo(s.cfg, s.table, k, x, th);
+    for (int j = 0; j < 16; j++) s.th[j][a] = th[j];
+    s.eos_id[a] = k;
+    s.eos_status[a] = it;
+  }
+  return failures;
+}
+
+// src/eom_default.cpp:211-869 (evaluate_time_derivatives) without sources and
+// without the diffusion sector (dN/dt is then zero).
+void evaluate_time_derivatives(System& s) {
+  const int D = s.cfg.dim;
+  const double t = s.t, t2 = t * t;
+  const bool shear = s.cfg.using_shear;
+#pragma omp parallel for
+  for (int a = 0; a < s.n; a++) {
+    ShearMRF sm{};
+    if (shear) shear_mrf(s, a, t, s.cfg.using_vorticity, sm);
+    const double g = s.gamma[a], sig = s.sigma[a];
+    const double dwds = s.th[kDwds][a], T = s.th[kT][a], w = s.th[kW][a], sden = s.th[kS][a];
+    const double rho[3] = {s.th[kRhoB][a], s.th[kRhoS][a], s.th[kRhoQ][a]};
+    const double dwdr[3] = {s.th[kDwdB][a], s.th[kDwdS][a], s.th[kDwdQ][a]};
+    const double mu[3] = {s.th[kMuB][a], s.th[kMuS][a], s.th[kMuQ][a]};
+    const double Pi = s.bulk[a], zeta = s.zeta_Pi[a], tPi = s.tau_Pi[a], dPP = s.delta_PiPi[a];
+    const double phi1 = s.phi1[a], phi3 = s.phi3[a], lPp = s.lambda_Pipi[a];
+    const double ztil = zeta + (dPP - tPi) * Pi;
+    double u[3] = {0, 0, 0}, uc[3];
+    for (int i = 0; i < D; i++) u[i] = s.u[i][a];
+    for (int i = 0; i < 3; i++) uc[i] = u[i];
+    cov_D(D, uc, t2);
+    double pi[4][4], pc[4][4];
+    for (int i = 0; i < 4; i++) for (int j = 0; j < 4; j++) pi[i][j] = s.shv[i * 4 + j][a];
+    for (int i = 0; i < 4; i++) for (int j = 0; j < 4; j++) {
+        double fj = (j == 1 || j == 2) ? -1.0 : (j == 3 ? -t2 : 1.0);
+        double fi = (i == 1 || i == 2) ? -1.0 : (i == 3 ? -t2 : 1.0);
+        pc[i][j] = pi[i][j] * fj * fi;
+      }
+    double divV = 0;
+    for (int i = 0; i < D; i++) divV += s.gradV[i * D + i][a];
+    const double geo = dEta(D, D - 1) * u[D - 1] * u[D - 1] * t / g;
+    const double expn = g * divV + g / t + geo;
+    // fill_auxiliary_variables (:229-362)
+    double Mb[3], Ms[3];
+    for (int i = 0; i < D; i++) {
+      Mb[i] = (ztil * uc[i] / g) / (sig * g * tPi);
+      Ms[i] = (Pi * uc[i] / g) / (sig * g * T);
+    }
+    // R_extensive_entropy = -mu/T multiplies dN/dt, which is zero without the
+    // diffusion sector and sources
+    (void)mu;
+    double Fb = -(ztil * (g * divV + g / t + geo) + Pi - phi1 * Pi * Pi) / (sig * g * tPi);
+    double Fs = (-Pi * (g * divV + g / t + geo)) / (sig * g * T);
+    double Fnab = 0, Mnab[3] = {0, 0, 0};
+    if (shear) {
+      Fnab = sm.Fnab;
+      Fs += Fnab / (sig * g * T);
+      double pp = 0;
+      for (int i = 0; i < 4; i++) for (int j = 0; j < 4; j++) pp += pc[i][j] * pi[i][j];
+      Fb += -(lPp * Fnab - phi3 * pp) / (sig * g * tPi);
+      for (int i = 0; i < D; i++) {
+        Mnab[i] = sm.Mnab[i];
+        Mb[i] += -lPp * Mnab[i] / (sig * g * tPi);
+        Ms[i] += Mnab[i] / (sig * g * T);
+      }
+    }
+    // compute_velocity_derivative (:456-618)
+    double gP[3], gB[3];
+    for (int i = 0; i < D; i++) { gP[i] = s.gradP[i][a]; gB[i] = s.gradBulk[i][a]; }
+    contra_D(D, gP, t2);
+    contra_D(D, gB, t2);
+    const double X = sden * dwds / g + (rho[0] * dwdr[0] + rho[1] * dwdr[1] + rho[2] * dwdr[2]) / g;
+    double Mw[3];
+    for (int i = 0; i < D; i++) Mw[i] = X * uc[i] / g + sig * dwds * Ms[i];
+    const double Fw = -X * (geo + g / t + g * divV) + sig * dwds * Fs;
+    const double Fbulk = sig * Fb - Pi * (g * divV + g / t + geo) / g;
+    double Mu[9], Fu[3];
+    for (int i = 0; i < D; i++) {
+      for (int j = 0; j < D; j++) Mu[i * D + j] = u[i] * g * (Mb[j] + Mw[j]) - u[i] * uc[j] * (w + Pi) / g;
+      Mu[i * D + i] += g * (w + Pi);
+      Fu[i] = (gP[i] + gB[i]) - g * (Fw + Fbulk) * u[i] - (w + Pi) * expn * u[i] -
+              2. * (w + Pi) * g * u[D - 1] * dEta(D, i) / t;
+    }
+    if (shear) {
+      for (int i = 0; i < D; i++) {
+        Fu[i] += -pi[i + 1][0] / t - 2. * dEta(D, i) * pi[0][3] / t - s.divshear[i][a] + s.gradshear[i][a] - sm.F0i[i];
+        for (int j = 0; j < D; j++) Mu[i * D + j] += sm.M0i[i * D + j];
+      }
+    }
+    double MI[9], du[3];
+    inverse(D, Mu, MI);
+    for (int i = 0; i < D; i++) {
+      du[i] = 0;
+      for (int j = 0; j < D; j++) du[i] += MI[i * D + j] * Fu[j];
+    }
+    // compute_derivatives (:622-826)
+    // contractions with du/dt first, then the F terms, as in the reference
+    double m1 = 0, m2 = 0, m3 = 0, c1 = 0;
+    for (int i = 0; i < D; i++) { m1 += Ms[i] * du[i]; m2 += Mb[i] * du[i]; m3 += Mnab[i] * du[i]; c1 += uc[i] * du[i]; }
+    const double dS = m1 + Fs, dB = m2 + Fb, snu = m3 + Fnab;
+    const double th = -1. * c1 / g + g * divV + g / t + geo;
+    for (int i = 0; i < D; i++) s.du_dt[i][a] = du[i];
+    s.d_ext[0][a] = dS;
+    s.d_ext[1][a] = s.d_ext[2][a] = s.d_ext[3][a] = 0.0;
+    s.d_ext_bulk[a] = dB;
+    s.theta[a] = th;
+    s.shv_nabla_u[a] = snu;
+    if (shear) {
+      const int map[2][3] = {{0, 1, 2}, {-1, 3, 4}};
+      for (int i = 0; i < 2; i++)
+        for (int j = i; j < 3; j++) {
+          double acc = 0.;
+          for (int k = 0; k < D; k++) acc += sm.Mext[i][j][k] * du[k];
+          s.d_ext_shv[map[i][j]][a] = acc + sm.Fext[i][j];
+        }
+    } else {
+      for (int k = 0; k < 6; k++) s.d_ext_shv[k][a] = 0.0;
+    }
+    // compute_Ez_derivative (:827-862)
+    const double u3 = (D == 3) ? u[2] : 0.0;
+    const double e = s.th[kE][a], p = s.th[kP][a];
+    s.dEz[a] = ((e + p + Pi) * u3 * u3 + (p + Pi) / t2 + pi[3][3]) * s.mass[0][a] * t2 / s.sigma_lab[a];
+  }
+}
+
+// src/sph_workstation.cpp:1509-1612 (get_time_derivatives), phases 01-10.
+void get_time_derivatives(System& s, NbrList& nl) {
+  build_neighbours(s, nl);        // 01_neighbour_list
+  update_velocity(s);             // 02_gamma_velocity
+  smooth_fields(s, nl);           // 03_smooth_fields
+  update_thermodynamics(s);       // 04_thermodynamics
+  reset_pi_tensor(s);             // 05_reset_pi_tensor
+  update_viscosities(s);          // 08_viscosities
+  smooth_gradients(s, nl);        // 09_smooth_gradients
+  evaluate_time_derivatives(s);   // 10_time_derivatives
+}
+
+// src/evolver.cpp:124-168 (fill_cache), :344-486 (step_rk), :493-517 (rk2).
+static void step_rk(System& s, NbrList& nl, double dt, double t0) {
+  get_time_derivatives(s, nl);
+  const int D = s.cfg.dim;
+#pragma omp parallel for
+  for (int a = 0; a < s.n; a++) {
+    double es = s.ext0[0][a] + dt * s.d_ext[0][a];
+    s.ext_bulk[a] = s.ext_bulk0[a] + dt * s.d_ext_bulk[a];
+    for (int k = 1; k < 4; k++) s.ext[k][a] = s.ext0[k][a] + dt * s.d_ext[k][a];
+    s.Ez[a] = s.Ez0[a] + dt * s.dEz[a];
+    for (int i = 0; i < D; i++) {
+      s.r[i][a] = s.r0[i][a] + dt * s.v[i][a];
+      s.u[i][a] = s.u0[i][a] + dt * s.du_dt[i][a];
+    }
+    for (int k = 0; k < 5; k++) s.ext_shv[k][a] = s.ext_shv0[k][a] + dt * s.d_ext_shv[k][a];
+    if (es < 0.0 && s.freeze[a] > 3) es = 1.e-3;
+    else if (es < 0.0) s.eos_status[a] = -2;  // negative entropy: fatal in the reference
+    s.ext[0][a] = es;
+    for (int i = D; i < 3; i++) { s.r[i][a] = 0.0; s.u[i][a] = 0.0; }
+  }
+  s.t = t0 + dt;
+}
+
+void rk2_step(System& s, NbrList& nl) {
+  for (int a = 0; a < s.n; a++) {
+    for (int i = 0; i < 3; i++) { s.r0[i][a] = s.r[i][a]; s.u0[i][a] = s.u[i][a]; }
+    for (int k = 0; k < 4; k++) s.ext0[k][a] = s.ext[k][a];
+    s.ext_bulk0[a] = s.ext_bulk[a];
+    for (int k = 0; k < 6; k++) s.ext_shv0[k][a] = s.ext_shv[k][a];
+    s.Ez0[a] = s.Ez[a];
+  }
+  const double t0 = s.t, dt = s.cfg.dt;
+  step_rk(s, nl, .5 * dt, t0);
+  step_rk(s, nl, dt, t0);
+}
+
+// src/system_state.cpp:738-885 (entropy, BSQ, energy totals) without the
+// diffusion q^0 terms (zero here).
+Totals conservation(const System& s) {
+  Totals T{0, 0, 0, 0, 0, 0};
+  const double sqrtg = s.cfg.coord == 0 ? s.t : 1.0;
+  for (int a = 0; a < s.n; a++) {
+    T.S += s.ext[0][a] * s.mass[0][a];
+    T.B += s.ext[1][a] * s.mass[1][a];
+    T.Sq += s.ext[2][a] * s.mass[2][a];
+    T.Q += s.ext[3][a] * s.mass[3][a];
+    const double g = s.gamma[a];
+    const double C = s.th[kW][a] + s.bulk[a];
+    T.E += (C * g * g - s.th[kP][a] - s.bulk[a] + s.shv[0][a]) * s.mass[0][a] * sqrtg / s.sigma_lab[a];
+    T.Ez += s.Ez[a];
+  }
+  return T;
+}
+
+// src/BSQHydro.cpp:568-646 (initialize_hydrodynamics) with
+// src/sph_workstation.cpp:1228-1340 (process_initial_conditions),
+// :252-375 (initialize_entropy_and_charge_densities) and :394-457
+// (initial_smoothing); no freeze-in, sources or jets.
+void initialize(System& s, NbrList& nl) {
+  const int D = s.cfg.dim;
+  s.t = s.cfg.t0;
+  const double t2 = s.t * s.t;
+  const double T_seed = 580.0 / kHbarcMeVfm;
+  for (int a = 0; a < s.n; a++) {
+    double u[3] = {s.u[0][a], s.u[1][a], s.u[2][a]};
+    s.gamma[a] = gamma_of(D, u, t2);
+    for (int k = 0; k < 4; k++) { s.ext[k][a] = 1.0; s.mass[k][a] = 1.0; }
+    s.th[kT][a] = T_seed;
+    s.th[kMuB][a] = s.th[kMuS][a] = s.th[kMuQ][a] = 0.0;
+    s.eos_id[a] = 0;
+    s.freeze[a] = 0;
+    s.btrack[a] = 0;
+    s.Ez[a] = 0.0;
+  }
+  build_neighbours(s, nl);
+  // freeze-out energy density: e(T_FO, 0, 0, 0) of the default EoS
+  double efc = 0;
+  {
+    double x[4] = {s.cfg.freeze_out_T, 0, 0, 0}, o[17];
+    eos_full_thermo(s.cfg, s.table, 0, x, o);
+    efc = o[5];
+  }
+  int bad = 0;
+#pragma omp parallel for reduction(+ : bad)
+  for (int a = 0; a < s.n; a++) {
+    double x[4] = {s.th[kT][a], 0, 0, 0};
+    int it = 0, k;
+    if (s.cfg.input_as_entropy) {
+      double tgt[4] = {s.in_s[a], s.in_rho[0][a], s.in_rho[1][a], s.in_rho[2][a]};
+      k = eos_invert(s.cfg, s.table, 1, tgt, 0, x, &it);
+    } else {
+      double tgt[4] = {s.in_e[a], s.in_rho[0][a], s.in_rho[1][a], s.in_rho[2][a]};
+      k = eos_invert(s.cfg, s.table, 0, tgt, 0, x, &it);
+      if (k < 0) {
+        s.freeze[a] = 4;
+        double tz[4] = {s.in_e[a], 0, 0, 0};
+        x[0] = s.th[kT][a]; x[1] = x[2] = x[3] = 0;
+        k = eos_invert(s.cfg, s.table, 0, tz, 0, x, &it);
+      }
+    }
+    if (k < 0) { s.eos_status[a] = -1; bad++; continue; }
+    double th[16];
+    eos_set_thermo(s.cfg, s.table, k, x, th);
+    for (int j = 0; j < 16; j++) s.th[j][a] = th[j];
+    s.eos_id[a] = k;
+    s.eos_status[a] = it;
+    if (s.cfg.input_as_entropy) s.in_e[a] = th[kE]; else s.in_s[a] = th[kS];
+    if (!(s.in_e[a] > efc && s.freeze[a] != 4)) s.freeze[a] = 4;
+  }
+  calculate_initial_sigma(s, nl, s.cfg.t0);
+  for (int a = 0; a < s.n; a++) {
+    const double sg = s.sigma[a];
+    for (int k = 0; k < 4; k++) s.mass[k][a] = 1;
+    s.ext[0][a] = s.in_s[a] / sg;
+    for (int k = 1; k < 4; k++) s.ext[k][a] = s.in_rho[k - 1][a] / sg;
+    if (s.in_s[a] < 0.0) s.freeze[a] = 4;
+  }
+  update_velocity(s);
+  // initial_smoothing
+  update_velocity(s);
+  smooth_fields(s, nl);
+  for (int a = 0; a < s.n; a++) {  // calculate_extensive_shv (no initial shear), set_bulk_Pi
+    for (int k = 0; k < 6; k++) s.ext_shv[k][a] = 0.0;
+    for (int k = 0; k < 16; k++) s.shv[k][a] = 0.0;
+    s.ext_bulk[a] = 0.0;
+    s.bulk[a] = 0.0;
+  }
+  reset_pi_tensor(s);
+  update_thermodynamics(s);
+  (void)bad;
+}
+
+}  // namespace orc

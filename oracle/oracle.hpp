@@ -1,0 +1,137 @@
+// CPU FP64 oracle for the CCAKE per-timestep SPH hot path.
+//
+// TEST INFRASTRUCTURE ONLY. This library is the checker that the CUDA path is
+// compared against; it is never linked into, loaded by, or called from the
+// product library. Only the tests, the smoke check and the CPU-baseline leg of
+// the benchmark load it.
+//
+// It restates, in plain C++17 (+OpenMP over particles), the algorithms of the
+// reference (the-nuclear-confectionery/CCAKE). Each routine cites the reference
+// file:line it follows. The reference itself cannot be built here (Kokkos,
+// Cabana, GSL, HDF5 and yaml-cpp are absent), so parity is pinned against the
+// reference's own unit-test golden values (kernel, smoothing, gradient, RK2,
+// multilinear interpolation) and against the analytic ideal Gubser flow.
+//
+// Units follow the reference: T, mu in fm^-1; e, p in fm^-4; s, rho in fm^-3.
+#pragma once
+#include <cstdint>
+#include <vector>
+#include <string>
+
+namespace orc {
+
+constexpr double kHbarcGeVfm = 0.1973269804;   // include/constants.h:16
+constexpr double kHbarcMeVfm = 197.3269804;    // include/constants.h:17
+constexpr double kTiny = 1e-25;                // include/eos_header.h:16
+constexpr double kTbqsInf = 1e10;              // include/eos_header.h:17
+
+enum EosKind : int32_t { kConformal = 0, kConformalDiagonal = 1, kTable = 2 };
+enum ShearRelax : int32_t { kTauPiDefault = 0, kTauPiGubser = 1, kTauPiMinval = 2 };
+enum ZetaMode : int32_t { kZetaDefault = 0, kZetaConstant = 1, kZetaCs2 = 2, kZetaPeaked = 3 };
+
+// Run configuration (the subset of the reference Settings the hot path reads).
+// Layout is mirrored by a ctypes Structure in the tests.
+struct Config {
+  int32_t dim;               // 2 or 3 (spatial dimensions)
+  int32_t coord;             // 0 = Milne ("hyperbolic", EoM_default); 1 = Cartesian
+  int32_t eos_kind;          // EosKind
+  int32_t using_shear;       // settings.h:263-270 (eta/s > 1e-10)
+  int32_t using_vorticity;
+  int32_t shear_relax_mode;  // ShearRelax
+  int32_t zeta_mode;         // ZetaMode
+  int32_t factorized_kernel; // D=3 W2D(r_perp)*W1D(deta) kernel
+  int32_t input_as_entropy;
+  int32_t modulate_zeta_with_tanh;
+  int32_t thermo_mode;       // 0 = reference Schur-complement chain, 1 = exact Hessian inverse
+  int32_t pad1;
+  double hT, hEta, t0, dt;
+  double eos_c, eos_T0, eos_muB0, eos_muQ0, eos_muS0;
+  double eta_over_s, zeta_over_s, zeta_cs2_A, zeta_cs2_p;
+  double zeta_peak_T, zeta_peak_width;   // peaked zeta/s mode (config 4)
+  double xmin, ymin, etamin;              // lower corner of the IC grid
+  double freeze_out_T;                    // fm^-1
+};
+
+// Per-particle state, struct of arrays.
+struct System {
+  Config cfg;
+  int n = 0;
+  double t = 0;
+  // evolved state
+  std::vector<double> r[3], u[3];
+  std::vector<double> ext[4];       // extensive s, rhoB, rhoS, rhoQ (per sph mass)
+  std::vector<double> mass[4];      // sph_mass (1 after init)
+  std::vector<double> ext_bulk;
+  std::vector<double> ext_shv[6];   // (0,0),(0,1),(0,2),(1,1),(1,2) of the 2x3 block; [5] unused
+  std::vector<double> Ez;           // contribution_to_total_Ez
+  std::vector<int32_t> freeze, btrack;
+  // input
+  std::vector<double> in_e, in_s, in_rho[3], in_bulk;
+  std::vector<double> in_shv[6];    // pi^{xx},xy,xeta,yy,yeta,etaeta (fm^-4..)
+  // derived
+  std::vector<double> gamma, v[3], sigma_lab, sigma, smoothed[4];
+  // thermo: T, muB, muS, muQ, p, s, rhoB, rhoS, rhoQ, e, w, cs2, dwds, dwdB, dwdS, dwdQ
+  std::vector<double> th[16];
+  std::vector<int32_t> eos_id;      // index into the EoS chain of the last solution
+  std::vector<int32_t> eos_status;  // 0 ok, >0 number of failed attempts, <0 no solution
+  std::vector<double> bulk;
+  std::vector<double> shv[16];      // 4x4 pi^{mu nu}
+  // transport
+  std::vector<double> eta_pi, tau_pi, zeta_Pi, tau_Pi, delta_PiPi, delta_pipi,
+      lambda_piPi, lambda_Pipi, phi1, phi3, phi6, phi7, tau_pipi;
+  // gradients
+  std::vector<double> gradP[3], gradE[3], gradBulk[3], gradshear[3], divshear[3], gradV[9];
+  // time derivatives
+  std::vector<double> du_dt[3], d_ext[4], d_ext_bulk, d_ext_shv[6], dEz, theta, shv_nabla_u;
+  // evolver cache
+  std::vector<double> r0[3], u0[3], ext0[4], ext_bulk0, ext_shv0[6], Ez0;
+  // table EoS (optional)
+  struct Table* table = nullptr;
+};
+
+enum ThermoIdx { kT = 0, kMuB, kMuS, kMuQ, kP, kS, kRhoB, kRhoS, kRhoQ, kE, kW, kCs2,
+                 kDwds, kDwdB, kDwdS, kDwdQ };
+
+// --- SPH kernel (src/kernel.cpp) ---------------------------------------------
+double kernel_W(int D, double r, double h);
+void kernel_gradW(int D, const double* rel, double r, double h, double* grad);
+double kernel_W_factorized(const double* r1, const double* r2, double hT, double hEta);
+void kernel_gradW_factorized(const double* rel, double hT, double hEta, double* grad);
+
+// --- neighbours --------------------------------------------------------------
+// Full neighbour list, CSR, predicate dx^2+dy^2+dz^2 <= (2h)^2, self excluded.
+void neighbours_bruteforce(const System& s, std::vector<int32_t>& off, std::vector<int32_t>& idx);
+void neighbours_celllist(const System& s, std::vector<int32_t>& off, std::vector<int32_t>& idx);
+
+// --- the step pieces ----------------------------------------------------------
+struct NbrList { std::vector<int32_t> off, idx; };
+void build_neighbours(System& s, NbrList& nl);
+void update_velocity(System& s);
+void smooth_fields(System& s, const NbrList& nl);
+void calculate_initial_sigma(System& s, const NbrList& nl, double t);
+int update_thermodynamics(System& s);
+void reset_pi_tensor(System& s);
+void update_viscosities(System& s);
+void smooth_gradients(System& s, const NbrList& nl);
+void evaluate_time_derivatives(System& s);
+void get_time_derivatives(System& s, NbrList& nl);
+void rk2_step(System& s, NbrList& nl);
+void initialize(System& s, NbrList& nl);
+
+struct Totals { double S, B, Sq, Q, E, Ez; };
+Totals conservation(const System& s);
+
+// --- equation of state ---------------------------------------------------------
+struct Table;
+// 17-field thermo at (T, muB, muQ, muS): p s B S Q e cs2 chiBB chiQQ chiSS chiBQ
+// chiBS chiQS chiTB chiTQ chiTS chiTT (include/eos_base.h get_full_thermo order)
+void eos_full_thermo(const Config& c, const Table* tab, int model, const double tbqs[4], double out[17]);
+// Invert (e or s, B, S, Q) -> (T, muB, muQ, muS) with the reference's seed chain.
+// Returns the chain index of the model used, or -1 when no solution was found.
+int eos_invert(const Config& c, const Table* tab, int mode_entropy, const double target[4],
+               int start_model, double tbqs_inout[4], int* iterations);
+// Derived thermodynamics after a solution (include/eos.h:121-175 set_thermo subset).
+void eos_set_thermo(const Config& c, const Table* tab, int model, const double tbqs[4], double th16[16]);
+int eos_chain_length(const Config& c);
+
+}  // namespace orc
