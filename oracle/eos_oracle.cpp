@@ -151,13 +151,15 @@ void solve4(double A[4][4], double* b, double* xout) {
 }
 
 // One solver attempt from a seed (replaces GSL hybrids in src/rootfinder.cpp:206-416).
-// Stopping rule: max |F_i| < 1e-10 (the reference's gsl_multiroot_test_residual
-// tolerance, include/rootfinder.h:36-37), then one Newton polish step. At most
-// 100 iterations; leaving the model's (T, mu) box fails the attempt.
+// Stopping rule: the reference's max |F_i| < 1e-10 (gsl_multiroot_test_residual,
+// include/rootfinder.h:36-37); once it holds, full Newton steps continue (at
+// most 8) until the largest relative step is below 1e-12, so the answer does
+// not depend on where the absolute rule happened to trigger. At most 100
+// iterations; leaving the model's (T, mu) box fails the attempt.
 bool newton_attempt(const Config& c, const Table* tab, int model, int entropy,
                     const double* tgt, const double* lo, const double* hi, double* x, int* iters) {
   const double tol = 1e-10;
-  bool conv = false;
+  int extra = -1;
   for (int it = 0; it < 100; it++) {
     double f[4], J[4][4];
     densities_and_jacobian(c, tab, model, entropy, x, f, J);
@@ -165,16 +167,20 @@ bool newton_attempt(const Config& c, const Table* tab, int model, int entropy,
     double fmax = 0;
     for (int i = 0; i < 4; i++) fmax = std::max(fmax, std::fabs(F[i]));
     if (!(fmax == fmax)) return false;  // NaN
+    if (extra < 0 && fmax < tol) extra = 0;
     double rhs[4] = {-F[0], -F[1], -F[2], -F[3]}, dx[4];
     solve4(J, rhs, dx);
-    if (conv) {  // polish step after convergence
-      double y[4];
-      for (int i = 0; i < 4; i++) y[i] = x[i] + dx[i];
+    if (extra >= 0) {
+      double y[4], rel = 0;
+      for (int i = 0; i < 4; i++) {
+        y[i] = x[i] + dx[i];
+        rel = std::max(rel, std::fabs(dx[i]) / std::max(std::fabs(x[i]), 1e-300));
+      }
       if (y[0] > 0 && std::isfinite(y[0])) for (int i = 0; i < 4; i++) x[i] = y[i];
-      *iters += it;
-      return true;
+      extra++;
+      if (rel < 1e-12 || extra >= 8) { *iters += it + 1; return true; }
+      continue;
     }
-    if (fmax < tol) { conv = true; continue; }
     // damped step: halve while the residual grows (at most 6 halvings)
     double lam = 1.0;
     double y[4];
