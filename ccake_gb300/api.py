@@ -1,0 +1,200 @@
+"""ctypes binding of libccake_gpu.so (the C ABI in include/ccake_gpu.h).
+
+This is the Python-side caller used by the tests and the benchmark. The
+library must have been built (``python -m ccake_gb300.build``); loading fails
+loudly otherwise -- there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_i32, _i64, _f64 = ctypes.c_int32, ctypes.c_int64, ctypes.c_double
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int32)
+
+
+class CcakeConfig(ctypes.Structure):
+    _fields_ = [(n, _i32) for n in (
+        "dim", "coord", "eos_kind", "using_shear", "using_vorticity", "shear_relax_mode", "zeta_mode",
+        "factorized_kernel", "input_as_entropy", "modulate_zeta_with_tanh", "thermo_mode", "precision")] + \
+        [(n, _f64) for n in (
+            "hT", "hEta", "t0", "dt", "eos_c", "eos_T0", "eos_muB0", "eos_muQ0", "eos_muS0", "eta_over_s",
+            "zeta_over_s", "zeta_cs2_A", "zeta_cs2_p", "zeta_peak_T", "zeta_peak_width", "xmin", "ymin",
+            "etamin", "freeze_out_T")]
+
+
+class ParticlesSoA(ctypes.Structure):
+    _fields_ = [("n", _i64)] + [(k, _dp) for k in ("x", "y", "eta", "e_or_s", "rhoB", "rhoS", "rhoQ", "ux",
+                                                    "uy", "ueta")]
+
+
+class Totals(ctypes.Structure):
+    _fields_ = [(k, _f64) for k in ("S", "B", "Sq", "Q", "E", "Ez")]
+
+
+STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "EoS inversion failed", 4: "negative entropy",
+          5: "buffer too small", 6: "call out of order", 7: "out of device memory", 8: "non-finite state"}
+
+
+class CcakeError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def lib():
+    """Loads libccake_gpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        path = library_path()
+        if not os.path.exists(path):
+            raise RuntimeError(f"{path} is missing: run `python -m ccake_gb300.build` first")
+        L = ctypes.CDLL(path)
+        P = ctypes.c_void_p
+        L.ccake_status_string.restype = ctypes.c_char_p
+        L.ccake_status_string.argtypes = [_i32]
+        L.ccake_last_error.restype = ctypes.c_char_p
+        L.ccake_last_error.argtypes = [P]
+        L.ccake_ctx_create.argtypes = [ctypes.POINTER(CcakeConfig), ctypes.POINTER(P)]
+        L.ccake_ctx_destroy.argtypes = [P]
+        L.ccake_load_particles.argtypes = [P, ctypes.POINTER(ParticlesSoA)]
+        for name in ("ccake_initialize", "ccake_build_neighbours", "ccake_smooth_fields", "ccake_update_thermo",
+                     "ccake_update_viscosities", "ccake_smooth_gradients", "ccake_time_derivatives"):
+            getattr(L, name).argtypes = [P]
+        L.ccake_step.argtypes = [P, _i32]
+        L.ccake_get_time.argtypes = [P, _dp]
+        L.ccake_get_count.argtypes = [P, ctypes.POINTER(_i64)]
+        L.ccake_conservation.argtypes = [P, ctypes.POINTER(Totals)]
+        L.ccake_copy_out.argtypes = [P, ctypes.c_char_p, _dp]
+        L.ccake_copy_out_int.argtypes = [P, ctypes.c_char_p, _ip]
+        L.ccake_get_neighbours.argtypes = [P, _ip, _ip, _i64, ctypes.POINTER(_i64)]
+        L.ccake_eos_invert_batch.argtypes = [P, _i32, _i64, _dp, _dp, _dp, _ip, _ip]
+        _lib = L
+    return _lib
+
+
+def make_config(rc) -> CcakeConfig:
+    c = CcakeConfig()
+    for name, _ in CcakeConfig._fields_:
+        if hasattr(rc, name):
+            setattr(c, name, getattr(rc, name))
+    return c
+
+
+def _d(a):
+    return a.ctypes.data_as(_dp) if a is not None else None
+
+
+def _i(a):
+    return a.ctypes.data_as(_ip) if a is not None else None
+
+
+class GpuHydro:
+    """One event resident on the GPU, driven through the C ABI."""
+
+    def __init__(self, rc):
+        L = lib()
+        self.rc = rc
+        self.cfg = make_config(rc)
+        self.h = ctypes.c_void_p()
+        self._check(L.ccake_ctx_create(ctypes.byref(self.cfg), ctypes.byref(self.h)), "create")
+        self.n = 0
+
+    def _check(self, code, what):
+        if code != 0:
+            msg = lib().ccake_last_error(self.h).decode() if self.h else ""
+            raise CcakeError(code, f"{what}: {msg}")
+
+    def close(self):
+        if self.h:
+            lib().ccake_ctx_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def load(self, particles):
+        arrs = {k: np.ascontiguousarray(getattr(particles, k), dtype=np.float64)
+                for k in ("x", "y", "eta", "e", "rhoB", "rhoS", "rhoQ", "ux", "uy", "ueta")}
+        self._keep = arrs
+        soa = ParticlesSoA(particles.n, _d(arrs["x"]), _d(arrs["y"]), _d(arrs["eta"]), _d(arrs["e"]),
+                           _d(arrs["rhoB"]), _d(arrs["rhoS"]), _d(arrs["rhoQ"]), _d(arrs["ux"]),
+                           _d(arrs["uy"]), _d(arrs["ueta"]))
+        self._check(lib().ccake_load_particles(self.h, ctypes.byref(soa)), "load")
+        self.n = particles.n
+
+    def initialize(self):
+        self._check(lib().ccake_initialize(self.h), "initialize")
+
+    def step(self, n=1):
+        self._check(lib().ccake_step(self.h, int(n)), "step")
+
+    def phase(self, name):
+        self._check(getattr(lib(), "ccake_" + name)(self.h), name)
+
+    @property
+    def t(self):
+        v = ctypes.c_double()
+        self._check(lib().ccake_get_time(self.h, ctypes.byref(v)), "time")
+        return v.value
+
+    def get(self, name):
+        out = np.empty(self.n, dtype=np.float64)
+        self._check(lib().ccake_copy_out(self.h, name.encode(), _d(out)), f"copy_out {name}")
+        return out
+
+    def get_int(self, name):
+        out = np.empty(self.n, dtype=np.int32)
+        self._check(lib().ccake_copy_out_int(self.h, name.encode(), _i(out)), f"copy_out_int {name}")
+        return out
+
+    def totals(self):
+        t = Totals()
+        self._check(lib().ccake_conservation(self.h, ctypes.byref(t)), "conservation")
+        return {k: getattr(t, k) for k, _ in Totals._fields_}
+
+    def neighbours(self):
+        off = np.zeros(self.n + 1, dtype=np.int32)
+        cnt = ctypes.c_int64()
+        code = lib().ccake_get_neighbours(self.h, _i(off), None, 0, ctypes.byref(cnt))
+        if code not in (0, 5):
+            self._check(code, "neighbours")
+        idx = np.zeros(max(cnt.value, 1), dtype=np.int32)
+        self._check(lib().ccake_get_neighbours(self.h, _i(off), _i(idx), cnt.value, ctypes.byref(cnt)),
+                    "neighbours")
+        return off, idx[:cnt.value]
+
+    def eos_invert(self, entropy, targets, seeds):
+        t = np.ascontiguousarray(targets, dtype=np.float64)
+        x = np.ascontiguousarray(seeds, dtype=np.float64).copy()
+        n = t.shape[0]
+        th = np.zeros((n, 16))
+        st = np.zeros(n, dtype=np.int32)
+        it = np.zeros(n, dtype=np.int32)
+        self._check(lib().ccake_eos_invert_batch(self.h, int(entropy), n, _d(t), _d(x), _d(th), _i(st), _i(it)),
+                    "eos_invert_batch")
+        return x, th, st, it
+
+
+def exported_symbols():
+    """Names declared in include/ccake_gpu.h."""
+    import re
+    hdr = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "ccake_gpu.h")
+    src = open(hdr).read()
+    return sorted(set(re.findall(r"\b(ccake_[a-z_0-9]+)\s*\(", src)))

@@ -1,0 +1,510 @@
+// Host side of libccake_gpu.so: the C ABI declared in include/ccake_gpu.h.
+// Owns device memory, orders particles by neighbour cell, sequences the
+// kernels of a derivative evaluation and captures one RK2 step in a CUDA
+// graph that ccake_step replays.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "ccake_gpu.h"
+#include "kernels.cuh"
+
+using namespace ccake;
+
+struct ccake_ctx {
+  ccake_config cfg{};
+  RunConst rc{};
+  EosDev eos{};
+  Ptrs p{};
+  int64_t n = 0;
+  std::vector<int32_t> perm;   // storage slot -> caller's index
+  cudaStream_t stream = nullptr;
+  bool loaded = false, initialized = false;
+  double t = 0.0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  std::string err;
+  double* dbuf = nullptr;
+  int32_t* ibuf = nullptr;
+  double* d_table = nullptr;
+};
+
+namespace {
+
+ccake_status_t fail(ccake_ctx* c, ccake_status_t s, const std::string& msg) {
+  if (c) c->err = msg;
+  return s;
+}
+
+#define CK(call)                                                                                   \
+  do {                                                                                             \
+    cudaError_t e_ = (call);                                                                       \
+    if (e_ != cudaSuccess) return fail(ctx, CCAKE_ERR_CUDA, std::string(#call ": ") + cudaGetErrorString(e_)); \
+  } while (0)
+
+void free_buffers(ccake_ctx* ctx) {
+  if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+  if (ctx->graph) cudaGraphDestroy(ctx->graph);
+  ctx->graph_exec = nullptr;
+  ctx->graph = nullptr;
+  if (ctx->dbuf) cudaFree(ctx->dbuf);
+  if (ctx->ibuf) cudaFree(ctx->ibuf);
+  ctx->dbuf = nullptr;
+  ctx->ibuf = nullptr;
+}
+
+// Neighbour-cell grid: the reference's box (twice the IC lower corner,
+// mirrored; src/system_state.cpp:656-692), widened to hold every particle,
+// cell edge >= 2h.
+Grid make_grid(const ccake_config& cfg, const ccake_particles_soa* h) {
+  Grid g{};
+  const double cut = 2.0 * cfg.hT;
+  const double corner[3] = {cfg.xmin, cfg.ymin, cfg.etamin};
+  const double* xs[3] = {h->x, h->y, h->eta};
+  for (int k = 0; k < 3; k++) {
+    if (k >= cfg.dim) { g.lo[k] = -cfg.hT; g.nc[k] = 1; g.inv_cs[k] = 1.0 / (2.0 * cfg.hT); continue; }
+    double lo = 2.0 * corner[k], hi = -2.0 * corner[k];
+    double mn = 1e300, mx = -1e300;
+    for (int64_t i = 0; i < h->n; i++) { mn = std::min(mn, xs[k][i]); mx = std::max(mx, xs[k][i]); }
+    lo = std::min(lo, mn - cut);
+    hi = std::max(hi, mx + cut);
+    int nc = (int)std::floor((hi - lo) / cut);
+    nc = std::max(1, std::min(nc, 1 << 14));
+    g.lo[k] = lo;
+    g.nc[k] = nc;
+    g.inv_cs[k] = nc / (hi - lo);
+  }
+  g.ncell = g.nc[0] * g.nc[1] * g.nc[2];
+  return g;
+}
+
+int host_cell(const Grid& g, int k, double x) {
+  int c = (int)std::floor((x - g.lo[k]) * g.inv_cs[k]);
+  return c < 0 ? 0 : (c >= g.nc[k] ? g.nc[k] - 1 : c);
+}
+
+ccake_status_t check_errors(ccake_ctx* ctx) {
+  int32_t e[NERR];
+  CK(cudaMemcpyAsync(e, ctx->p.err, sizeof(e), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaGetLastError());
+  if (e[E_EOS]) return fail(ctx, CCAKE_ERR_EOS, std::to_string(e[E_EOS]) + " particles without an EoS solution");
+  if (e[E_NEGS]) return fail(ctx, CCAKE_ERR_NEG_ENTROPY, std::to_string(e[E_NEGS]) + " particles with negative entropy");
+  if (e[E_NONFINITE]) return fail(ctx, CCAKE_ERR_NONFINITE, std::to_string(e[E_NONFINITE]) + " non-finite particles");
+  return CCAKE_OK;
+}
+
+ccake_status_t reset_errors(ccake_ctx* ctx) {
+  CK(cudaMemsetAsync(ctx->p.err, 0, sizeof(int32_t) * NERR, ctx->stream));
+  return CCAKE_OK;
+}
+
+void enqueue_substep(ccake_ctx* ctx, int sub) {
+  const double dt = ctx->cfg.dt;
+  launch_build_cells(ctx->rc, ctx->p, ctx->stream);
+  launch_passA(ctx->rc, ctx->eos, ctx->p, A_WITH_THERMO, ctx->stream);
+  int mode = B_EOM | B_UPDATE | (sub == 2 ? B_WRITE_Y0 : 0);
+  launch_passB(ctx->rc, ctx->p, mode, sub == 1 ? 0.5 * dt : dt, ctx->stream);
+  launch_clock(ctx->p, sub, dt, ctx->stream);
+}
+
+struct FieldRef {
+  const double* base;
+  bool ok;
+};
+
+FieldRef field_ref(ccake_ctx* ctx, const std::string& k) {
+  const Ptrs& p = ctx->p;
+  const int64_t n = ctx->n;
+  auto Y = [&](int s) { return FieldRef{p.y + s * n, true}; };
+  static const char* thn[NTH] = {"T", "muB", "muS", "muQ", "p", "s", "rhoB", "rhoS", "rhoQ", "e", "w", "cs2",
+                                 "dwds", "dwdB", "dwdS", "dwdQ"};
+  for (int q = 0; q < NTH; q++) if (k == thn[q]) return FieldRef{p.th + q * n, true};
+  if (k == "x") return Y(Y_X0);
+  if (k == "y") return Y(Y_X1);
+  if (k == "eta") return Y(Y_X2);
+  if (k == "ext_s") return Y(Y_ES);
+  if (k == "ext_B") return Y(Y_EB);
+  if (k == "ext_S") return Y(Y_ESS);
+  if (k == "ext_Q") return Y(Y_EQ);
+  if (k == "ext_bulk") return Y(Y_EBULK);
+  if (k == "Ez") return Y(Y_EZ);
+  for (int q = 0; q < 3; q++) {
+    const std::string d = std::to_string(q);
+    if (k == "u" + d) return Y(Y_U0 + q);
+    if (k == "v" + d) return FieldRef{p.v + q * n, true};
+    if (k == "gradP" + d) return FieldRef{p.grads + (G_P + q) * n, true};
+    if (k == "gradE" + d) return FieldRef{p.grads + (G_E + q) * n, true};
+    if (k == "gradBulk" + d) return FieldRef{p.grads + (G_B + q) * n, true};
+    if (k == "gradshear" + d) return FieldRef{p.grads + (G_SH + q) * n, true};
+    if (k == "divshear" + d) return FieldRef{p.grads + (G_DS + q) * n, true};
+    if (k == "du_dt" + d) return FieldRef{p.derivs + (D_DU0 + q) * n, true};
+  }
+  for (int q = 0; q < 5; q++) {
+    if (k == "ext_shv" + std::to_string(q)) return Y(Y_SHV0 + q);
+    if (k == "d_ext_shv" + std::to_string(q)) return FieldRef{p.derivs + (D_DSHV0 + q) * n, true};
+  }
+  for (int q = 0; q < 9; q++) if (k == "gradV" + std::to_string(q)) return FieldRef{p.grads + (G_V + q) * n, true};
+  for (int a = 0; a < 4; a++)
+    for (int b = 0; b < 4; b++)
+      if (k == "shv" + std::to_string(a) + std::to_string(b)) return FieldRef{p.pi + pi_slot(a, b) * n, true};
+  if (k == "gamma") return FieldRef{p.gam, true};
+  if (k == "sigma_lab") return FieldRef{p.slab, true};
+  if (k == "sigma") return FieldRef{p.sig, true};
+  if (k == "bulk") return FieldRef{p.bulk, true};
+  if (k == "d_ext_s") return FieldRef{p.derivs + D_DS * n, true};
+  if (k == "d_ext_bulk") return FieldRef{p.derivs + D_DBULK * n, true};
+  if (k == "dEz") return FieldRef{p.derivs + D_DEZ * n, true};
+  if (k == "eta_pi") return FieldRef{p.derivs + D_ETA * n, true};
+  if (k == "tau_pi") return FieldRef{p.derivs + D_TAUPI * n, true};
+  if (k == "zeta_Pi") return FieldRef{p.derivs + D_ZETA * n, true};
+  if (k == "tau_Pi") return FieldRef{p.derivs + D_TAUBULK * n, true};
+  if (k == "in_s") return FieldRef{p.in_s, true};
+  return FieldRef{nullptr, false};
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* ccake_status_string(ccake_status_t s) {
+  switch (s) {
+    case CCAKE_OK: return "ok";
+    case CCAKE_ERR_INVALID: return "invalid argument";
+    case CCAKE_ERR_CUDA: return "CUDA error";
+    case CCAKE_ERR_EOS: return "EoS inversion failed";
+    case CCAKE_ERR_NEG_ENTROPY: return "negative entropy";
+    case CCAKE_ERR_CAPACITY: return "buffer too small";
+    case CCAKE_ERR_STATE: return "call out of order";
+    case CCAKE_ERR_NOMEM: return "out of device memory";
+    case CCAKE_ERR_NONFINITE: return "non-finite state";
+  }
+  return "unknown";
+}
+
+const char* ccake_last_error(const ccake_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+ccake_status_t ccake_ctx_create(const ccake_config* cfg, ccake_ctx** out) {
+  if (!cfg || !out) return CCAKE_ERR_INVALID;
+  *out = nullptr;
+  if (cfg->dim != 2 && cfg->dim != 3) return CCAKE_ERR_INVALID;
+  if (cfg->coord != 0) return CCAKE_ERR_INVALID;
+  if (cfg->eos_kind != 0 && cfg->eos_kind != 1) return CCAKE_ERR_INVALID;
+  if (!(cfg->hT > 0) || !(cfg->t0 > 0) || !(cfg->dt > 0)) return CCAKE_ERR_INVALID;
+  if (cfg->dim == 3 && cfg->factorized_kernel) return CCAKE_ERR_INVALID;
+  ccake_ctx* ctx = new ccake_ctx;
+  ctx->cfg = *cfg;
+  if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete ctx;
+    return CCAKE_ERR_CUDA;
+  }
+  RunConst& rc = ctx->rc;
+  rc.cfg = *cfg;
+  const int D = cfg->dim;
+  const double h = cfg->hT;
+  rc.cut2 = (2.0 * h) * (2.0 * h);
+  rc.inv_h = 1.0 / h;
+  rc.wn = knorm(D) / std::pow(h, D);
+  rc.wn2 = knorm2(D) / std::pow(h, D);
+  rc.gn = kgrad(D) / std::pow(h, D + 1);
+  rc.gn2 = kgrad2(D) / std::pow(h, D + 1);
+  rc.k0 = rc.wn;   // W(0)
+  EosDev& e = ctx->eos;
+  e.kind = cfg->eos_kind;
+  e.thermo_mode = cfg->thermo_mode;
+  e.own = {cfg->eos_c, cfg->eos_T0, cfg->eos_muB0, cfg->eos_muQ0, cfg->eos_muS0};
+  e.conf = e.cdiag = e.own;
+  double x4[4] = {cfg->freeze_out_T, 0, 0, 0}, o[17];
+  model_thermo(e, chain_model(e.kind, 0), x4, o);
+  rc.efreeze = o[5];
+  *out = ctx;
+  return CCAKE_OK;
+}
+
+ccake_status_t ccake_ctx_destroy(ccake_ctx* ctx) {
+  if (!ctx) return CCAKE_ERR_INVALID;
+  free_buffers(ctx);
+  if (ctx->d_table) cudaFree(ctx->d_table);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return CCAKE_OK;
+}
+
+ccake_status_t ccake_load_particles(ccake_ctx* ctx, const ccake_particles_soa* h) {
+  if (!ctx || !h || h->n <= 0 || !h->x || !h->y || !h->e_or_s || !h->ux || !h->uy) return CCAKE_ERR_INVALID;
+  if (ctx->cfg.dim == 3 && (!h->eta || !h->ueta)) return fail(ctx, CCAKE_ERR_INVALID, "dim 3 needs eta and ueta");
+  if (h->n > (int64_t)0x3fffffff) return fail(ctx, CCAKE_ERR_INVALID, "too many particles");
+  free_buffers(ctx);
+  const int64_t n = h->n;
+  ctx->n = n;
+  ctx->rc.grid = make_grid(ctx->cfg, h);
+  const Grid& g = ctx->rc.grid;
+  // storage order: by neighbour cell, then by input index
+  std::vector<int64_t> key(n);
+  for (int64_t i = 0; i < n; i++) {
+    int64_t c = host_cell(g, 0, h->x[i]) + (int64_t)g.nc[0] * host_cell(g, 1, h->y[i]);
+    if (ctx->cfg.dim == 3) c += (int64_t)g.nc[0] * g.nc[1] * host_cell(g, 2, h->eta[i]);
+    key[i] = c;
+  }
+  ctx->perm.resize(n);
+  std::iota(ctx->perm.begin(), ctx->perm.end(), 0);
+  std::stable_sort(ctx->perm.begin(), ctx->perm.end(), [&](int32_t a, int32_t b) { return key[a] < key[b]; });
+  // device memory: one double slab, one int slab
+  const size_t nd = (size_t)n * (2 * NY + 1 + NTH + 1 + 3 + 1 + 1 + 1 + NPI + RA + RB + NGRAD + NDER + 1 + 1 + 3) +
+                    (size_t)kTotBlocks * 6 + 8;
+  const size_t ni = (size_t)n * 7 + (size_t)g.ncell * 2 + 1 + NERR + 8;
+  if (cudaMalloc(&ctx->dbuf, nd * sizeof(double)) != cudaSuccess) return fail(ctx, CCAKE_ERR_NOMEM, "device allocation");
+  if (cudaMalloc(&ctx->ibuf, ni * sizeof(int32_t)) != cudaSuccess) return fail(ctx, CCAKE_ERR_NOMEM, "device allocation");
+  CK(cudaMemsetAsync(ctx->dbuf, 0, nd * sizeof(double), ctx->stream));
+  CK(cudaMemsetAsync(ctx->ibuf, 0, ni * sizeof(int32_t), ctx->stream));
+  Ptrs& p = ctx->p;
+  p.n = (int)n;
+  double* d = ctx->dbuf;
+  auto take = [&](size_t k) { double* r = d; d += k * n; return r; };
+  // the records come first: their slabs are multiples of 64 bytes, so the
+  // 16-byte vector loads stay aligned for any n
+  p.recA = take(RA); p.recB = take(RB);
+  p.y = take(NY); p.y0 = take(NY); p.m = take(1); p.th = take(NTH); p.gam = take(1); p.v = take(3);
+  p.slab = take(1); p.sig = take(1); p.bulk = take(1); p.pi = take(NPI);
+  p.grads = take(NGRAD); p.derivs = take(NDER); p.in_e = take(1); p.in_s = take(1); p.in_rho = take(3);
+  p.partials = d;
+  d += (size_t)kTotBlocks * 6;
+  p.clock = reinterpret_cast<Clock*>(d);
+  int32_t* ip = ctx->ibuf;
+  auto itake = [&](size_t k) { int32_t* r = ip; ip += k; return r; };
+  p.eos_id = itake(n); p.eos_iters = itake(n); p.btrack = itake(n); p.freeze = itake(n);
+  p.cell_of = itake(n); p.cell_rank = itake(n); p.cell_idx = itake(n);
+  p.cell_count = itake(g.ncell); p.cell_start = itake(g.ncell + 1); p.err = itake(NERR);
+  // upload permuted inputs
+  std::vector<double> tmp((size_t)n);
+  auto up = [&](const double* src, double* dst) -> ccake_status_t {
+    for (int64_t k = 0; k < n; k++) tmp[k] = src ? src[ctx->perm[k]] : 0.0;
+    CK(cudaMemcpyAsync(dst, tmp.data(), n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return CCAKE_OK;
+  };
+  ccake_status_t s;
+  if ((s = up(h->x, p.y + Y_X0 * n)) || (s = up(h->y, p.y + Y_X1 * n)) ||
+      (s = up(ctx->cfg.dim == 3 ? h->eta : nullptr, p.y + Y_X2 * n)) || (s = up(h->ux, p.y + Y_U0 * n)) ||
+      (s = up(h->uy, p.y + Y_U1 * n)) || (s = up(ctx->cfg.dim == 3 ? h->ueta : nullptr, p.y + Y_U2 * n)) ||
+      (s = up(h->e_or_s, p.in_e)) || (s = up(h->rhoB, p.in_rho)) || (s = up(h->rhoS, p.in_rho + n)) ||
+      (s = up(h->rhoQ, p.in_rho + 2 * n)))
+    return s;
+  ctx->loaded = true;
+  ctx->initialized = false;
+  return CCAKE_OK;
+}
+
+ccake_status_t ccake_initialize(ccake_ctx* ctx) {
+  if (!ctx) return CCAKE_ERR_INVALID;
+  if (!ctx->loaded) return fail(ctx, CCAKE_ERR_STATE, "load particles first");
+  Clock c{ctx->cfg.t0, ctx->cfg.t0};
+  CK(cudaMemcpyAsync(ctx->p.clock, &c, sizeof(Clock), cudaMemcpyHostToDevice, ctx->stream));
+  ccake_status_t s = reset_errors(ctx);
+  if (s) return s;
+  launch_init_state(ctx->rc, ctx->p, ctx->stream);
+  launch_init_invert(ctx->rc, ctx->eos, ctx->p, ctx->stream);
+  launch_build_cells(ctx->rc, ctx->p, ctx->stream);
+  launch_passA(ctx->rc, ctx->eos, ctx->p, A_SMOOTH_ONLY, ctx->stream);   // initial sigma
+  launch_init_ext(ctx->rc, ctx->p, ctx->stream);
+  launch_passA(ctx->rc, ctx->eos, ctx->p, A_WITH_THERMO, ctx->stream);   // initial smoothing
+  const int64_t n = ctx->n;
+  CK(cudaMemcpyAsync(ctx->p.y0, ctx->p.y, NY * n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+  s = check_errors(ctx);
+  if (s) return s;
+  ctx->t = ctx->cfg.t0;
+  ctx->initialized = true;
+  return CCAKE_OK;
+}
+
+ccake_status_t ccake_step(ccake_ctx* ctx, int32_t n_steps) {
+  if (!ctx || n_steps < 0) return CCAKE_ERR_INVALID;
+  if (!ctx->initialized) return fail(ctx, CCAKE_ERR_STATE, "initialize first");
+  ccake_status_t s = reset_errors(ctx);
+  if (s) return s;
+  if (!ctx->graph_exec) {
+    CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    enqueue_substep(ctx, 1);
+    enqueue_substep(ctx, 2);
+    CK(cudaStreamEndCapture(ctx->stream, &ctx->graph));
+    CK(cudaGraphInstantiate(&ctx->graph_exec, ctx->graph, 0));
+  }
+  for (int k = 0; k < n_steps; k++) CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
+  s = check_errors(ctx);
+  Clock c;
+  CK(cudaMemcpy(&c, ctx->p.clock, sizeof(Clock), cudaMemcpyDeviceToHost));
+  ctx->t = c.t;
+  return s;
+}
+
+ccake_status_t ccake_build_neighbours(ccake_ctx* ctx) {
+  if (!ctx) return CCAKE_ERR_INVALID;
+  if (!ctx->loaded) return fail(ctx, CCAKE_ERR_STATE, "load particles first");
+  launch_build_cells(ctx->rc, ctx->p, ctx->stream);
+  return check_errors(ctx);
+}
+
+ccake_status_t ccake_smooth_fields(ccake_ctx* ctx) {
+  if (!ctx) return CCAKE_ERR_INVALID;
+  if (!ctx->initialized) return fail(ctx, CCAKE_ERR_STATE, "initialize first");
+  launch_build_cells(ctx->rc, ctx->p, ctx->stream);
+  launch_passA(ctx->rc, ctx->eos, ctx->p, A_SMOOTH_ONLY, ctx->stream);
+  return check_errors(ctx);
+}
+
+ccake_status_t ccake_update_thermo(ccake_ctx* ctx) {
+  if (!ctx) return CCAKE_ERR_INVALID;
+  if (!ctx->initialized) return fail(ctx, CCAKE_ERR_STATE, "initialize first");
+  ccake_status_t s = reset_errors(ctx);
+  if (s) return s;
+  launch_thermo(ctx->rc, ctx->eos, ctx->p, ctx->stream);
+  return check_errors(ctx);
+}
+
+ccake_status_t ccake_update_viscosities(ccake_ctx* ctx) {
+  if (!ctx) return CCAKE_ERR_INVALID;
+  if (!ctx->initialized) return fail(ctx, CCAKE_ERR_STATE, "initialize first");
+  launch_visc(ctx->rc, ctx->p, ctx->stream);
+  return check_errors(ctx);
+}
+
+ccake_status_t ccake_smooth_gradients(ccake_ctx* ctx) {
+  if (!ctx) return CCAKE_ERR_INVALID;
+  if (!ctx->initialized) return fail(ctx, CCAKE_ERR_STATE, "initialize first");
+  launch_passB(ctx->rc, ctx->p, B_GRADS, 0.0, ctx->stream);
+  return check_errors(ctx);
+}
+
+ccake_status_t ccake_time_derivatives(ccake_ctx* ctx) {
+  if (!ctx) return CCAKE_ERR_INVALID;
+  if (!ctx->initialized) return fail(ctx, CCAKE_ERR_STATE, "initialize first");
+  launch_passB(ctx->rc, ctx->p, B_GRADS | B_EOM | B_DERIVS, 0.0, ctx->stream);
+  return check_errors(ctx);
+}
+
+ccake_status_t ccake_get_time(const ccake_ctx* ctx, double* t) {
+  if (!ctx || !t) return CCAKE_ERR_INVALID;
+  *t = ctx->t;
+  return CCAKE_OK;
+}
+
+ccake_status_t ccake_get_count(const ccake_ctx* ctx, int64_t* n) {
+  if (!ctx || !n) return CCAKE_ERR_INVALID;
+  *n = ctx->n;
+  return CCAKE_OK;
+}
+
+ccake_status_t ccake_conservation(ccake_ctx* ctx, ccake_totals* out) {
+  if (!ctx || !out) return CCAKE_ERR_INVALID;
+  if (!ctx->initialized) return fail(ctx, CCAKE_ERR_STATE, "initialize first");
+  launch_totals(ctx->rc, ctx->p, kTotBlocks, ctx->stream);
+  std::vector<double> part((size_t)kTotBlocks * 6);
+  CK(cudaMemcpyAsync(part.data(), ctx->p.partials, part.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  double acc[6] = {0, 0, 0, 0, 0, 0};
+  for (int b = 0; b < kTotBlocks; b++)
+    for (int q = 0; q < 6; q++) acc[q] += part[b * 6 + q];
+  *out = ccake_totals{acc[0], acc[1], acc[2], acc[3], acc[4], acc[5]};
+  return CCAKE_OK;
+}
+
+ccake_status_t ccake_copy_out(ccake_ctx* ctx, const char* field, double* host_out) {
+  if (!ctx || !field || !host_out) return CCAKE_ERR_INVALID;
+  if (!ctx->loaded) return fail(ctx, CCAKE_ERR_STATE, "load particles first");
+  FieldRef f = field_ref(ctx, field);
+  if (!f.ok) return fail(ctx, CCAKE_ERR_INVALID, std::string("unknown field ") + field);
+  std::vector<double> tmp((size_t)ctx->n);
+  CK(cudaMemcpyAsync(tmp.data(), f.base, ctx->n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  for (int64_t k = 0; k < ctx->n; k++) host_out[ctx->perm[k]] = tmp[k];
+  return CCAKE_OK;
+}
+
+ccake_status_t ccake_copy_out_int(ccake_ctx* ctx, const char* field, int32_t* host_out) {
+  if (!ctx || !field || !host_out) return CCAKE_ERR_INVALID;
+  if (!ctx->loaded) return fail(ctx, CCAKE_ERR_STATE, "load particles first");
+  const std::string k(field);
+  const int32_t* base = k == "btrack" ? ctx->p.btrack : k == "eos_id" ? ctx->p.eos_id
+                      : k == "eos_iters" ? ctx->p.eos_iters : k == "freeze" ? ctx->p.freeze : nullptr;
+  if (!base) return fail(ctx, CCAKE_ERR_INVALID, "unknown field " + k);
+  std::vector<int32_t> tmp((size_t)ctx->n);
+  CK(cudaMemcpyAsync(tmp.data(), base, ctx->n * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  for (int64_t q = 0; q < ctx->n; q++) host_out[ctx->perm[q]] = tmp[q];
+  return CCAKE_OK;
+}
+
+ccake_status_t ccake_get_neighbours(ccake_ctx* ctx, int32_t* offsets, int32_t* idx, int64_t idx_cap, int64_t* count) {
+  if (!ctx || !offsets || !count) return CCAKE_ERR_INVALID;
+  if (!ctx->loaded) return fail(ctx, CCAKE_ERR_STATE, "load particles first");
+  const int64_t n = ctx->n;
+  int32_t* d_cnt = nullptr;
+  CK(cudaMalloc(&d_cnt, (n + 1) * sizeof(int32_t)));
+  launch_build_cells(ctx->rc, ctx->p, ctx->stream);
+  launch_neighbour_counts(ctx->rc, ctx->p, d_cnt, ctx->stream);
+  std::vector<int32_t> cnt(n), off(n + 1, 0);
+  cudaError_t e = cudaMemcpyAsync(cnt.data(), d_cnt, n * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream);
+  cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) { cudaFree(d_cnt); return fail(ctx, CCAKE_ERR_CUDA, cudaGetErrorString(e)); }
+  for (int64_t k = 0; k < n; k++) off[k + 1] = off[k] + cnt[k];
+  const int64_t m = off[n];
+  *count = m;
+  // offsets in the caller's order
+  std::vector<int32_t> inv(n);
+  for (int64_t k = 0; k < n; k++) inv[ctx->perm[k]] = (int32_t)k;
+  offsets[0] = 0;
+  for (int64_t i = 0; i < n; i++) offsets[i + 1] = offsets[i] + cnt[inv[i]];
+  if (!idx || idx_cap < m) { cudaFree(d_cnt); return fail(ctx, CCAKE_ERR_CAPACITY, "idx_cap too small"); }
+  int32_t *d_off = nullptr, *d_idx = nullptr;
+  CK(cudaMalloc(&d_off, (n + 1) * sizeof(int32_t)));
+  CK(cudaMalloc(&d_idx, std::max<int64_t>(m, 1) * sizeof(int32_t)));
+  CK(cudaMemcpyAsync(d_off, off.data(), (n + 1) * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
+  launch_neighbour_fill(ctx->rc, ctx->p, d_off, d_idx, ctx->stream);
+  std::vector<int32_t> all(m);
+  CK(cudaMemcpyAsync(all.data(), d_idx, m * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  cudaFree(d_cnt);
+  cudaFree(d_off);
+  cudaFree(d_idx);
+  for (int64_t i = 0; i < n; i++) {
+    const int32_t k = inv[i];
+    int32_t* row = idx + offsets[i];
+    for (int32_t j = 0; j < cnt[k]; j++) row[j] = ctx->perm[all[off[k] + j]];
+    std::sort(row, row + cnt[k]);
+  }
+  return check_errors(ctx);
+}
+
+ccake_status_t ccake_eos_invert_batch(ccake_ctx* ctx, int32_t entropy_mode, int64_t n, const double* in4,
+                                      double* tbqs, double* th16, int32_t* status, int32_t* iters) {
+  if (!ctx || n < 0 || !in4 || !tbqs || !status) return CCAKE_ERR_INVALID;
+  if (n == 0) return CCAKE_OK;
+  double *d_in = nullptr, *d_x = nullptr, *d_th = nullptr;
+  int32_t *d_st = nullptr, *d_it = nullptr;
+  CK(cudaMalloc(&d_in, n * 4 * sizeof(double)));
+  CK(cudaMalloc(&d_x, n * 4 * sizeof(double)));
+  if (th16) CK(cudaMalloc(&d_th, n * 16 * sizeof(double)));
+  CK(cudaMalloc(&d_st, n * sizeof(int32_t)));
+  if (iters) CK(cudaMalloc(&d_it, n * sizeof(int32_t)));
+  CK(cudaMemcpyAsync(d_in, in4, n * 4 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(d_x, tbqs, n * 4 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  launch_eos_batch(ctx->eos, entropy_mode, n, d_in, d_x, d_th, d_st, d_it, ctx->stream);
+  CK(cudaMemcpyAsync(tbqs, d_x, n * 4 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  if (th16) CK(cudaMemcpyAsync(th16, d_th, n * 16 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(status, d_st, n * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+  if (iters) CK(cudaMemcpyAsync(iters, d_it, n * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  cudaFree(d_in);
+  cudaFree(d_x);
+  if (d_th) cudaFree(d_th);
+  cudaFree(d_st);
+  if (d_it) cudaFree(d_it);
+  CK(cudaGetLastError());
+  return CCAKE_OK;
+}
+
+}  // extern "C"

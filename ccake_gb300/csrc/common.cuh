@@ -1,0 +1,106 @@
+// Shared device definitions for the GB300 SPH hot path: state layout in HBM,
+// the cubic-spline kernel, the neighbour-cell grid and run constants.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "ccake_gpu.h"
+
+namespace ccake {
+
+constexpr double kHbarcGeVfm = 0.1973269804;   // reference include/constants.h:16
+constexpr double kHbarcMeVfm = 197.3269804;    // reference include/constants.h:17
+constexpr double kTiny = 1e-25;                // reference include/eos_header.h:16
+constexpr double kTbqsInf = 1e10;              // reference include/eos_header.h:17
+
+// Evolved per-particle state (struct of arrays, one n-long slab per slot).
+// The same layout is used for the current state Y and the step-start cache Y0.
+enum YSlot : int {
+  Y_X0 = 0, Y_X1, Y_X2,          // position (x, y, eta)
+  Y_U0, Y_U1, Y_U2,              // spatial four-velocity u^i
+  Y_ES, Y_EB, Y_ESS, Y_EQ,       // extensive s, rhoB, rhoS, rhoQ
+  Y_EBULK,                       // extensive bulk pressure
+  Y_SHV0, Y_SHV1, Y_SHV2, Y_SHV3, Y_SHV4,  // extensive pi^{ij}: (1,1)(1,2)(1,3)(2,2)(2,3)
+  Y_EZ,                          // contribution_to_total_Ez
+  NY
+};
+
+// Thermodynamic slots (the reference's thermo_info subset the path reads).
+enum ThSlot : int { T_T = 0, T_MUB, T_MUS, T_MUQ, T_P, T_S, T_RB, T_RS, T_RQ, T_E, T_W, T_CS2,
+                    T_DWDS, T_DWDB, T_DWDSS, T_DWDQ, NTH };  // dw/ds, dw/drhoB, dw/drhoS, dw/drhoQ
+
+// Shear tensor pi^{mu nu} slots (upper triangle of the symmetric 4x4).
+enum PiSlot : int { P00 = 0, P01, P02, P03, P11, P12, P13, P22, P23, P33, NPI };
+__host__ __device__ constexpr int pi_slot(int i, int j) {
+  return (i > j) ? pi_slot(j, i)
+                 : (i == 0 ? j : (i == 1 ? 3 + j : (i == 2 ? 5 + j : 9)));
+}
+
+// Gradient slots written only when a caller asks for gradients.
+enum GradSlot : int { G_P = 0, G_E = 3, G_B = 6, G_SH = 9, G_DS = 12, G_V = 15, NGRAD = 24 };
+
+// Derivative slots written only when a caller asks for them.
+enum DerivSlot : int { D_DU0 = 0, D_DU1, D_DU2, D_DS, D_DBULK, D_DSHV0, D_DSHV1, D_DSHV2, D_DSHV3,
+                       D_DSHV4, D_DEZ, D_ETA, D_TAUPI, D_ZETA, D_TAUBULK, NDER };
+
+// Neighbour-record strides (doubles). Record A feeds the smoothing pass,
+// record B the gradient pass; both are rewritten once per substep.
+//   A: x0 x1 x2 m | m*ext_s m*ext_B m*ext_S m*ext_Q
+//   B: x0 x1 x2 m | m*p/sl^2 m*e m*Pi/sl^2 0 | m*v^i (3) 0 | m*pi^{0i}/sl^2 (3) 0 |
+//      m*pi^{ij}/sl^2 (11 12 13 22 23 33) 0 0
+constexpr int RA = 8;
+constexpr int RB = 24;
+enum RecB : int { B_X0 = 0, B_X1, B_X2, B_M, B_P, B_E, B_PI, B_V0 = 8, B_PI0 = 12, B_PIJ = 16 };
+
+// Neighbour-cell grid over a fixed box; cell edge >= 2h, indices clamped.
+struct Grid {
+  double lo[3];
+  double inv_cs[3];
+  int nc[3];
+  int ncell;
+};
+
+// Run constants passed by value to every kernel.
+struct RunConst {
+  ccake_config cfg;
+  Grid grid;
+  double cut2;           // (2h)^2
+  double inv_h;
+  double wn, wn2;        // W normalisations knorm/h^D, knorm2/h^D
+  double gn, gn2;        // grad W normalisations kgrad/h^(D+1), kgrad2/h^(D+1)
+  double k0;             // W(0)
+  double efreeze;        // e(T_FO, 0, 0, 0)
+};
+
+// Device-side clock: tau at the start of the RK2 step and the current tau.
+struct Clock {
+  double t0;
+  double t;
+};
+
+// Error counters raised by the kernels (read back by the host after a call).
+enum ErrSlot : int { E_EOS = 0, E_NEGS = 1, E_NONFINITE = 2, NERR = 4 };
+
+// Kernel normalisations of the reference, src/kernel.cpp:11-26.
+__host__ __device__ inline double knorm(int D) { return D == 1 ? 2. / 3. : D == 2 ? 10. / (7 * M_PI) : 1. / M_PI; }
+__host__ __device__ inline double knorm2(int D) { return D == 1 ? 1. / 6. : D == 2 ? 5. / (14. * M_PI) : 1. / (4 * M_PI); }
+__host__ __device__ inline double kgrad(int D) { return D == 1 ? -1. / 2. : D == 2 ? -15. / (14. * M_PI) : -3. / (4. * M_PI); }
+__host__ __device__ inline double kgrad2(int D) { return D == 1 ? 1. : D == 2 ? 15. / (7. * M_PI) : 3. / (2. * M_PI); }
+
+// Exact squared distance of the neighbour predicate (reference Cabana
+// VerletList, cutoff 2h): products and sums rounded separately, no FMA.
+template <int D>
+__device__ __forceinline__ double dist2_exact(const double* d) {
+  double s = __dmul_rn(d[0], d[0]);
+  s = __dadd_rn(s, __dmul_rn(d[1], d[1]));
+  if (D == 3) s = __dadd_rn(s, __dmul_rn(d[2], d[2]));
+  return s;
+}
+
+// Cell coordinate of a position along one axis, clamped to the grid.
+__device__ __forceinline__ int cell_coord(const Grid& g, int k, double x) {
+  int c = (int)floor((x - g.lo[k]) * g.inv_cs[k]);
+  return c < 0 ? 0 : (c >= g.nc[k] ? g.nc[k] - 1 : c);
+}
+
+}  // namespace ccake

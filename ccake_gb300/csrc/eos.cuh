@@ -1,0 +1,508 @@
+// Device equation of state: analytic conformal / conformal-diagonal models,
+// the tabulated 4-D EoS with multilinear lookup, the (e|s, B, S, Q) ->
+// (T, muB, muQ, muS) Newton root finder with the reference's seed chain, and
+// the enthalpy derivatives dw/ds, dw/drho. Everything is FP64.
+#pragma once
+#include "common.cuh"
+
+namespace ccake {
+
+struct Scales { double c, T0, muB0, muQ0, muS0; };
+
+// Tabulated EoS in device memory: uniform (T, muB, muQ, muS) grid, muS
+// fastest, 17 fields per node (p s B S Q e cs2 chiBB chiQQ chiSS chiBQ chiBS
+// chiQS chiTB chiTQ chiTS chiTT), layout of reference src/eos_table.cpp:31-35.
+struct TableView {
+  const double* f = nullptr;
+  int n[4] = {1, 1, 1, 1};
+  double lo[4] = {0, 0, 0, 0};
+  double d[4] = {0, 0, 0, 0};
+};
+
+struct EosDev {
+  int kind;                 // ccake_config::eos_kind
+  int thermo_mode;          // 0 reference chain, 1 exact Hessian inverse
+  Scales own;               // scales of the analytic default model
+  Scales conf, cdiag;       // fallback scales behind a table
+  TableView tab;
+};
+
+enum Model : int { M_CONF = 0, M_CDIAG = 1, M_TABLE = 2 };
+
+// Chains of the reference (src/eos_initialization.cpp:216-501):
+// conformal -> [conformal, conformal_diagonal]; conformal_diagonal -> [itself];
+// table -> [table, conformal, conformal_diagonal].
+__host__ __device__ inline int chain_len(int kind) { return kind == 0 ? 2 : (kind == 1 ? 1 : 3); }
+__host__ __device__ inline int chain_model(int kind, int k) {
+  if (kind == 0) return k == 0 ? M_CONF : M_CDIAG;
+  if (kind == 1) return M_CDIAG;
+  return k == 0 ? M_TABLE : (k == 1 ? M_CONF : M_CDIAG);
+}
+__host__ __device__ inline Scales model_scales(const EosDev& e, int model) {
+  if (e.kind == 2 && model != M_TABLE) return model == M_CONF ? e.conf : e.cdiag;
+  return e.own;
+}
+
+// p = c T0^4 x^2, x = (T/T0)^2 + sum (mu/mu0)^2 (reference include/eos_conformal.h:33-194).
+__host__ __device__ inline void conformal_thermo(const Scales& k, const double* x4, double* o) {
+  const double T = x4[0], mB = x4[1], mQ = x4[2], mS = x4[3];
+  const double iT = 1.0 / k.T0, iB = 1.0 / k.muB0, iQ = 1.0 / k.muQ0, iS = 1.0 / k.muS0;
+  const double iT2 = iT * iT, iB2 = iB * iB, iQ2 = iQ * iQ, iS2 = iS * iS;
+  const double x = T * T * iT2 + mB * mB * iB2 + mS * mS * iS2 + mQ * mQ * iQ2;
+  const double cp = k.c * k.T0 * k.T0 * k.T0 * k.T0;
+  const double p = cp * x * x;
+  const double s = 4.0 * cp * T * x * iT2;
+  const double B = 4.0 * cp * mB * x * iB2;
+  const double S = 4.0 * cp * mS * x * iS2;
+  const double Q = 4.0 * cp * mQ * x * iQ2;
+  o[0] = p; o[1] = s; o[2] = B; o[3] = S; o[4] = Q;
+  o[5] = (s * T + mB * B + mQ * Q + mS * S) - p;
+  o[6] = 1.0 / 3.0;
+  o[7] = cp * (8.0 * mB * mB * iB2 * iB2 + 4.0 * x * iB2);
+  o[8] = cp * (8.0 * mQ * mQ * iQ2 * iQ2 + 4.0 * x * iQ2);
+  o[9] = cp * (8.0 * mS * mS * iS2 * iS2 + 4.0 * x * iS2);
+  o[10] = 8.0 * cp * mB * mQ * iB2 * iQ2;
+  o[11] = 8.0 * cp * mB * mS * iB2 * iS2;
+  o[12] = 8.0 * cp * mS * mQ * iS2 * iQ2;
+  o[13] = 8.0 * cp * T * mB * iT2 * iB2;
+  o[14] = 8.0 * cp * T * mQ * iT2 * iQ2;
+  o[15] = 8.0 * cp * T * mS * iT2 * iS2;
+  o[16] = cp * (8.0 * T * T * iT2 * iT2 + 4.0 * x * iT2);
+}
+
+// p = c T0^4 [(T/T0)^4 + sum (mu/mu0)^4]; cross susceptibilities are the
+// TINY placeholders of the reference (include/eos_conformal_diagonal.h:78-205).
+__host__ __device__ inline void confdiag_thermo(const Scales& k, const double* x4, double* o) {
+  const double T = x4[0], mB = x4[1], mQ = x4[2], mS = x4[3];
+  const double cp = k.c * k.T0 * k.T0 * k.T0 * k.T0;
+  const double rT = T / k.T0, rB = mB / k.muB0, rQ = mQ / k.muQ0, rS = mS / k.muS0;
+  const double p = cp * (rT * rT * rT * rT + rB * rB * rB * rB + rS * rS * rS * rS + rQ * rQ * rQ * rQ);
+  const double s = 4.0 * cp * rT * rT * rT / k.T0;
+  const double B = 4.0 * cp * rB * rB * rB / k.muB0;
+  const double S = 4.0 * cp * rS * rS * rS / k.muS0;
+  const double Q = 4.0 * cp * rQ * rQ * rQ / k.muQ0;
+  o[0] = p; o[1] = s; o[2] = B; o[3] = S; o[4] = Q;
+  o[5] = (s * T + mB * B + mQ * Q + mS * S) - p;
+  o[6] = 1.0 / 3.0;
+  o[7] = 12.0 * cp * rB * rB / (k.muB0 * k.muB0);
+  o[8] = 12.0 * cp * rQ * rQ / (k.muQ0 * k.muQ0);
+  o[9] = 12.0 * cp * rS * rS / (k.muS0 * k.muS0);
+  for (int i = 10; i < 16; i++) o[i] = kTiny;
+  o[16] = 12.0 * cp * rT * rT / (k.T0 * k.T0);
+}
+
+// Multilinear lookup with the reference's index rule (src/interpolatorND.cpp:250-317):
+// integer part by truncation toward zero, last cell reused at the upper edge,
+// NaN outside.
+__host__ __device__ inline void table_thermo(const TableView& t, const double* x, double* o) {
+  int ind[4];
+  double fr[4];
+  for (int k = 0; k < 4; k++) {
+    if (isnan(x[k])) { for (int i = 0; i < 17; i++) o[i] = NAN; return; }
+    if (t.n[k] <= 1 || fabs(t.d[k]) < 1e-30) { ind[k] = 0; fr[k] = 1.0; continue; }
+    const double q = (x[k] - t.lo[k]) / t.d[k];
+    const double ip = trunc(q);
+    fr[k] = 1.0 - (q - ip);
+    ind[k] = (int)ip;
+    if (ind[k] + 1 == t.n[k]) { fr[k] = 1.0 - fr[k]; ind[k]--; }
+    if (ind[k] < 0 || ind[k] >= t.n[k] || !(fabs(q) < 2e9)) { for (int i = 0; i < 17; i++) o[i] = NAN; return; }
+  }
+  for (int i = 0; i < 17; i++) o[i] = 0.0;
+  for (int h = 0; h < 16; h++) {
+    const int b[4] = {(h >> 3) & 1, (h >> 2) & 1, (h >> 1) & 1, h & 1};
+    double w = 1.0;
+    long idx = 0;
+    for (int k = 0; k < 4; k++) {
+      w *= (fr[k] + b[k] - 2.0 * b[k] * fr[k]);
+      const int c = (t.n[k] <= 1) ? 0 : ind[k] + b[k];
+      idx = idx * t.n[k] + c;
+    }
+    const double* node = t.f + (size_t)idx * 17;
+    for (int i = 0; i < 17; i++) o[i] += w * node[i];
+  }
+}
+
+__host__ __device__ inline void model_thermo(const EosDev& e, int model, const double* x4, double* o) {
+  if (model == M_TABLE) { table_thermo(e.tab, x4, o); return; }
+  const Scales k = model_scales(e, model);
+  if (model == M_CONF) conformal_thermo(k, x4, o); else confdiag_thermo(k, x4, o);
+}
+
+__host__ __device__ inline void model_box(const EosDev& e, int model, double* lo, double* hi) {
+  if (model == M_TABLE) {
+    for (int k = 0; k < 4; k++) { lo[k] = e.tab.lo[k]; hi[k] = e.tab.lo[k] + e.tab.d[k] * (e.tab.n[k] - 1); }
+    return;
+  }
+  lo[0] = 0.0; hi[0] = kTbqsInf;
+  for (int i = 1; i < 4; i++) { lo[i] = -kTbqsInf; hi[i] = kTbqsInf; }
+}
+
+// Densities (e|s, B, Q, S) at x = (T, muB, muQ, muS) and their Jacobian: the
+// Hessian of p (exactly diagonal for the conformal-diagonal model).
+__host__ __device__ inline void dens_jac(const EosDev& e, int model, int entropy, const double* x, double* f,
+                                         double J[4][4]) {
+  double o[17];
+  model_thermo(e, model, x, o);
+  double H[4][4];
+  if (model == M_CDIAG) {
+    for (int i = 0; i < 4; i++) for (int j = 0; j < 4; j++) H[i][j] = 0.0;
+    H[0][0] = o[16]; H[1][1] = o[7]; H[2][2] = o[8]; H[3][3] = o[9];
+  } else {
+    H[0][0] = o[16]; H[0][1] = H[1][0] = o[13]; H[0][2] = H[2][0] = o[14]; H[0][3] = H[3][0] = o[15];
+    H[1][1] = o[7]; H[1][2] = H[2][1] = o[10]; H[1][3] = H[3][1] = o[11];
+    H[2][2] = o[8]; H[2][3] = H[3][2] = o[12]; H[3][3] = o[9];
+  }
+  f[0] = entropy ? o[1] : o[5];
+  f[1] = o[2];
+  f[2] = o[4];
+  f[3] = o[3];
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    J[1][j] = H[1][j];
+    J[2][j] = H[2][j];
+    J[3][j] = H[3][j];
+    J[0][j] = entropy ? H[0][j] : x[0] * H[0][j] + x[1] * H[1][j] + x[2] * H[2][j] + x[3] * H[3][j];
+  }
+}
+
+// 4x4 solve, partial pivoting; a zero pivot leaves its unknown unchanged.
+__host__ __device__ inline void solve4(double A[4][4], double* b, double* x) {
+  bool dead[4] = {false, false, false, false};
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    int p = k;
+    double best = fabs(A[k][k]);
+    for (int i = k + 1; i < 4; i++)
+      if (fabs(A[i][k]) > best) { best = fabs(A[i][k]); p = i; }
+    if (p != k) {
+      for (int j = 0; j < 4; j++) { double tmp = A[k][j]; A[k][j] = A[p][j]; A[p][j] = tmp; }
+      double tb = b[k]; b[k] = b[p]; b[p] = tb;
+    }
+    if (A[k][k] == 0.0) { dead[k] = true; continue; }
+    for (int i = k + 1; i < 4; i++) {
+      if (A[i][k] == 0.0) continue;
+      const double m = A[i][k] / A[k][k];
+      for (int j = k; j < 4; j++) A[i][j] -= m * A[k][j];
+      b[i] -= m * b[k];
+    }
+  }
+#pragma unroll
+  for (int k = 3; k >= 0; k--) {
+    if (dead[k]) { x[k] = 0.0; continue; }
+    double acc = b[k];
+    for (int j = k + 1; j < 4; j++) acc -= A[k][j] * x[j];
+    x[k] = acc / A[k][k];
+  }
+}
+
+// One Newton attempt from a seed. Stopping rule: the reference's max|F| < 1e-10
+// (include/rootfinder.h:36-37); then full steps (at most 8) until the largest
+// relative step is below 1e-12. 100 iterations at most; damped by residual
+// halving; leaving the model box fails.
+__host__ __device__ inline bool newton_attempt(const EosDev& e, int model, int entropy, const double* tgt,
+                                               const double* lo, const double* hi, double* x, int* iters) {
+  int extra = -1;
+  for (int it = 0; it < 100; it++) {
+    double f[4], J[4][4];
+    dens_jac(e, model, entropy, x, f, J);
+    double F[4], fres = 0.0;
+    for (int i = 0; i < 4; i++) { F[i] = f[i] - tgt[i]; fres = fres > fabs(F[i]) ? fres : fabs(F[i]); }
+    if (!(fres == fres)) return false;
+    if (extra < 0 && fres < 1e-10) extra = 0;
+    double rhs[4] = {-F[0], -F[1], -F[2], -F[3]}, dx[4];
+    solve4(J, rhs, dx);
+    if (extra >= 0) {
+      double y[4], rel = 0.0;
+      for (int i = 0; i < 4; i++) {
+        y[i] = x[i] + dx[i];
+        const double r = fabs(dx[i]) / fmax(fabs(x[i]), 1e-300);
+        rel = rel > r ? rel : r;
+      }
+      if (y[0] > 0 && isfinite(y[0])) for (int i = 0; i < 4; i++) x[i] = y[i];
+      extra++;
+      if (rel < 1e-12 || extra >= 8) { *iters += it + 1; return true; }
+      continue;
+    }
+    double lam = 1.0, y[4];
+    for (int h = 0; h < 7; h++) {
+      for (int i = 0; i < 4; i++) y[i] = x[i] + lam * dx[i];
+      if (y[0] > 0) {
+        double fy[4], Jy[4][4];
+        dens_jac(e, model, entropy, y, fy, Jy);
+        double gmax = 0.0;
+        for (int i = 0; i < 4; i++) { const double r = fabs(fy[i] - tgt[i]); gmax = gmax > r ? gmax : r; }
+        if (gmax <= fres || h == 6) break;
+      }
+      lam *= 0.5;
+    }
+    if (!(y[0] > 0)) y[0] = 0.5 * x[0];
+    for (int i = 0; i < 4; i++) x[i] = y[i];
+    for (int i = 0; i < 4; i++)
+      if (!(x[i] >= lo[i] && x[i] <= hi[i])) return false;
+  }
+  return false;
+}
+
+__host__ __device__ inline double sgnd(double v) { return (0.0 < v) - (v < 0.0); }
+
+// Seed sanitising and the perturbed-restart ladder of the reference
+// (src/rootfinder.cpp:421-715).
+__host__ __device__ inline bool find_root(const EosDev& e, int model, int entropy, const double* tgt, double* x,
+                                          int* iters) {
+  double lo[4], hi[4];
+  model_box(e, model, lo, hi);
+  double pos[4] = {x[0], x[1], x[2], x[3]};
+  const double sg[4] = {1.0, sgnd(tgt[1]), sgnd(tgt[2]), sgnd(tgt[3])};
+  for (int i = 0; i < 4; i++)
+    if (pos[i] * pos[i] < 1e-10) pos[i] = fmin(0.5 * hi[i], 1.0) * sg[i];
+  const double t0 = pos[0], b0 = pos[1], q0 = pos[2], s0 = pos[3];
+  double seeds[10][4];
+  const double tp = t0 + 0.2 * t0 > hi[0] ? hi[0] - 1 : t0 + 0.2 * t0;
+  const double tm = t0 - 0.2 * t0 < lo[0] ? lo[0] + 1 : t0 - 0.2 * t0;
+  const double bp = b0 + 0.2 * b0 > hi[1] ? hi[1] - 1 : b0 + 0.2 * b0;
+  const double bm = b0 - 0.2 * b0 < lo[1] ? lo[1] + 1 : b0 - 0.2 * b0;
+  const double sp = s0 + 0.2 * s0 > hi[3] ? hi[3] - 1 : s0 + 0.2 * s0;
+  const double sm = s0 - 0.2 * s0 < lo[3] ? lo[3] + 1 : s0 - 0.2 * s0;
+  const double qp = q0 + 0.2 * q0 > hi[2] ? hi[2] - 1 : q0 + 0.2 * q0;
+  const double qm = q0 - 0.2 * q0 < lo[2] ? lo[2] + 1 : q0 - 0.2 * q0;
+  auto clampT = [&](double v) { return (v < lo[0] || v > hi[0]) ? t0 : v; };
+  const double list[10][4] = {{t0, b0, q0, s0},         {clampT(tp), b0, q0, s0}, {clampT(tm), b0, q0, s0},
+                              {t0, bp, q0, s0},         {t0, bm, q0, s0},         {t0, b0, q0, sp},
+                              {t0, b0, q0, sm},         {t0, b0, qp, s0},         {t0, b0, qm, s0},
+                              {t0, fmin(0.5 * hi[1], 1.0) * sg[1], fmin(0.5 * hi[2], 1.0) * sg[2],
+                               fmin(0.5 * hi[3], 1.0) * sg[3]}};
+  (void)seeds;
+  for (int a = 0; a < 10; a++) {
+    double y[4] = {list[a][0], list[a][1], list[a][2], list[a][3]};
+    if (newton_attempt(e, model, entropy, tgt, lo, hi, y, iters)) {
+      for (int i = 0; i < 4; i++) x[i] = y[i];
+      return true;
+    }
+  }
+  return false;
+}
+
+// Exact inverses of the conformal-diagonal model, the reference's last seed
+// (include/eos_conformal_diagonal.h:49-76).
+__host__ __device__ inline void confdiag_seed(const Scales& k, int entropy, const double* target, double* x) {
+  const double den = 1.5874010519681994748 * cbrt(k.c);
+  const double e0 = target[0], B = target[1], S = target[2], Q = target[3];
+  if (entropy) {
+    x[0] = cbrt(k.T0 * k.T0 * k.T0 * k.T0 * e0) / den;
+  } else {
+    const double ft = 4.0 / 3.0;
+    const double disc = e0 - 3.0 * (pow(k.muB0 * fabs(B), ft) + pow(k.muS0 * fabs(S), ft) + pow(k.muQ0 * fabs(Q), ft)) /
+                                 (4.0 * den);
+    x[0] = k.T0 * pow(disc / (3.0 * k.c), 0.25);
+  }
+  x[1] = sgnd(B) * cbrt(k.muB0 * k.muB0 * k.muB0 * k.muB0 * fabs(B)) / den;
+  x[2] = sgnd(Q) * cbrt(k.muQ0 * k.muQ0 * k.muQ0 * k.muQ0 * fabs(Q)) / den;
+  x[3] = sgnd(S) * cbrt(k.muS0 * k.muS0 * k.muS0 * k.muS0 * fabs(S)) / den;
+}
+
+// (e|s, B, S, Q) -> (T, muB, muQ, muS) through the EoS chain with the
+// reference's seeds (src/eos.cpp:629-804 entropy mode, :813-975 energy mode).
+// Returns the chain index used, or -1.
+__host__ __device__ inline int eos_invert(const EosDev& e, int entropy, const double* target, int start, double* x,
+                                          int* iters) {
+  const double tgt[4] = {target[0], target[1], target[3], target[2]};  // (e|s, B, Q, S)
+  const int n = chain_len(e.kind);
+  const Scales cdk = model_scales(e, M_CDIAG);
+  const double prev[4] = {x[0], x[1], x[2], x[3]};
+  int it = 0;
+  for (int k = entropy ? (start > 0 ? start : 0) : 0; k < n; k++) {
+    const int model = chain_model(e.kind, k);
+    double y[4];
+    bool ok;
+    if (entropy) {
+      for (int i = 0; i < 4; i++) y[i] = prev[i];
+      ok = find_root(e, model, 1, tgt, y, &it);
+      if (!ok) { y[0] = prev[0]; y[1] = y[2] = y[3] = 0.0; ok = find_root(e, model, 1, tgt, y, &it); }
+      if (!ok) {
+        y[0] = 580.0 / kHbarcMeVfm; y[1] = sgnd(tgt[1]); y[2] = sgnd(tgt[2]); y[3] = sgnd(tgt[3]);
+        ok = find_root(e, model, 1, tgt, y, &it);
+      }
+      if (!ok) { confdiag_seed(cdk, 1, target, y); ok = find_root(e, model, 1, tgt, y, &it); }
+    } else {
+      y[0] = 580.0 / kHbarcMeVfm; y[1] = sgnd(tgt[1]); y[2] = sgnd(tgt[2]); y[3] = sgnd(tgt[3]);
+      ok = find_root(e, model, 0, tgt, y, &it);
+      if (!ok) { confdiag_seed(cdk, 0, target, y); ok = find_root(e, model, 0, tgt, y, &it); }
+    }
+    if (ok) {
+      double o[17];
+      model_thermo(e, model, y, o);
+      if (o[6] < 0.0 || o[6] > 1.0) continue;   // prohibit unstable / acausal cs2
+      for (int i = 0; i < 4; i++) x[i] = y[i];
+      *iters = it;
+      return k;
+    }
+  }
+  *iters = it;
+  return -1;
+}
+
+// a^T m^-1 b with the reference's guard on m11, m22 (src/eos_derivatives.cpp:457-560).
+__host__ __device__ inline double aTmb(const double* a, double m[3][3], const double* b) {
+  const double EPS = 1e-3;
+  if (fabs(m[1][1]) < EPS) m[1][1] = (m[1][1] >= 0.0 ? EPS : -EPS);
+  if (fabs(m[2][2]) < EPS) m[2][2] = (m[2][2] >= 0.0 ? EPS : -EPS);
+  double y[3] = {b[0], b[1], b[2]};
+  for (int k = 0; k < 3; k++) {
+    int p = k;
+    for (int i = k + 1; i < 3; i++) if (fabs(m[i][k]) > fabs(m[p][k])) p = i;
+    if (p != k) {
+      for (int j = 0; j < 3; j++) { double t = m[k][j]; m[k][j] = m[p][j]; m[p][j] = t; }
+      double t = y[k]; y[k] = y[p]; y[p] = t;
+    }
+    for (int i = k + 1; i < 3; i++) {
+      const double f = m[i][k] / m[k][k];
+      for (int j = k; j < 3; j++) m[i][j] -= f * m[k][j];
+      y[i] -= f * y[k];
+    }
+  }
+  double z[3];
+  for (int k = 2; k >= 0; k--) {
+    double acc = y[k];
+    for (int j = k + 1; j < 3; j++) acc -= m[k][j] * z[j];
+    z[k] = acc / m[k][k];
+  }
+  return a[0] * z[0] + a[1] * z[1] + a[2] * z[2];
+}
+
+struct Chi { double t2, tb, tq, ts, b2, q2, s2, bq, bs, sq; };
+
+// Schur-complement terms of the reference (src/eos_derivatives.cpp:33-455).
+// which: 0 term1; 1..3 term2(B,S,Q); 4..6 term3(B,S,Q); 7 + 3*j + i term4(j,i).
+__host__ __device__ inline double schur_term(const Chi& x, int which) {
+  double a[3], b[3], m[3][3], base;
+#define SET3(v, p, q, r) { v[0] = (p); v[1] = (q); v[2] = (r); }
+#define SETM(a0, a1, a2, b0, b1, b2, c0, c1, c2) \
+  { m[0][0] = a0; m[0][1] = a1; m[0][2] = a2; m[1][0] = b0; m[1][1] = b1; m[1][2] = b2; m[2][0] = c0; m[2][1] = c1; m[2][2] = c2; }
+  switch (which) {
+    case 0: SET3(a, x.tb, x.ts, x.tq); SET3(b, x.tb, x.ts, x.tq);
+      SETM(x.b2, x.bs, x.bq, x.bs, x.s2, x.sq, x.bq, x.sq, x.q2); base = x.t2; break;
+    case 1: SET3(a, x.t2, x.ts, x.tq); SET3(b, x.b2, x.bs, x.bq);
+      SETM(x.tb, x.bs, x.bq, x.ts, x.s2, x.sq, x.tq, x.sq, x.q2); base = x.tb; break;
+    case 2: SET3(a, x.t2, x.tb, x.tq); SET3(b, x.bs, x.s2, x.sq);
+      SETM(x.tb, x.b2, x.bq, x.ts, x.bs, x.sq, x.tq, x.bq, x.q2); base = x.ts; break;
+    case 3: SET3(a, x.t2, x.tb, x.ts); SET3(b, x.bq, x.sq, x.q2);
+      SETM(x.tb, x.b2, x.bs, x.ts, x.bs, x.s2, x.tq, x.bq, x.sq); base = x.tq; break;
+    case 4: SET3(a, x.b2, x.bs, x.bq); SET3(b, x.t2, x.ts, x.tq);
+      SETM(x.tb, x.ts, x.tq, x.bs, x.s2, x.sq, x.bq, x.sq, x.q2); base = x.tb; break;
+    case 5: SET3(a, x.bs, x.s2, x.sq); SET3(b, x.t2, x.tb, x.tq);
+      SETM(x.tb, x.ts, x.tq, x.b2, x.bs, x.bq, x.bq, x.sq, x.q2); base = x.ts; break;
+    case 6: SET3(a, x.bq, x.sq, x.q2); SET3(b, x.t2, x.tb, x.ts);
+      SETM(x.tb, x.ts, x.tq, x.b2, x.bs, x.bq, x.bs, x.s2, x.sq); base = x.tq; break;
+    // term4(j, i), j: charge of the density, i: charge of the potential (0 B, 1 S, 2 Q)
+    case 7 + 0 * 3 + 0: SET3(a, x.tb, x.bs, x.bq); SET3(b, x.tb, x.bs, x.bq);
+      SETM(x.t2, x.ts, x.tq, x.ts, x.s2, x.sq, x.tq, x.sq, x.q2); base = x.b2; break;
+    case 7 + 1 * 3 + 0: SET3(a, x.ts, x.s2, x.sq); SET3(b, x.tb, x.b2, x.bq);
+      SETM(x.t2, x.ts, x.tq, x.tb, x.bs, x.bq, x.tq, x.sq, x.q2); base = x.bs; break;
+    case 7 + 2 * 3 + 0: SET3(a, x.tq, x.sq, x.q2); SET3(b, x.tb, x.b2, x.bs);
+      SETM(x.t2, x.ts, x.tq, x.tb, x.bs, x.bq, x.ts, x.s2, x.sq); base = x.bq; break;
+    case 7 + 0 * 3 + 1: SET3(a, x.tb, x.b2, x.bq); SET3(b, x.ts, x.s2, x.sq);
+      SETM(x.t2, x.tb, x.tq, x.ts, x.bs, x.sq, x.tq, x.bq, x.q2); base = x.bs; break;
+    case 7 + 1 * 3 + 1: SET3(a, x.ts, x.bs, x.sq); SET3(b, x.ts, x.bs, x.sq);
+      SETM(x.t2, x.tb, x.tq, x.tb, x.b2, x.bq, x.tq, x.bq, x.q2); base = x.s2; break;
+    case 7 + 2 * 3 + 1: SET3(a, x.tq, x.bq, x.q2); SET3(b, x.ts, x.bs, x.s2);
+      SETM(x.t2, x.tb, x.tq, x.tb, x.b2, x.bq, x.ts, x.bs, x.sq); base = x.sq; break;
+    case 7 + 0 * 3 + 2: SET3(a, x.tb, x.b2, x.bs); SET3(b, x.tq, x.sq, x.q2);
+      SETM(x.t2, x.tb, x.ts, x.ts, x.bs, x.s2, x.tq, x.bq, x.sq); base = x.bq; break;
+    case 7 + 1 * 3 + 2: SET3(a, x.ts, x.bs, x.s2); SET3(b, x.tq, x.bq, x.q2);
+      SETM(x.t2, x.tb, x.ts, x.tb, x.b2, x.bs, x.tq, x.bq, x.sq); base = x.sq; break;
+    default: SET3(a, x.tq, x.bq, x.sq); SET3(b, x.tq, x.bq, x.sq);
+      SETM(x.t2, x.tb, x.ts, x.tb, x.b2, x.bs, x.ts, x.bs, x.s2); base = x.q2; break;
+  }
+#undef SET3
+#undef SETM
+  return base - aTmb(a, m, b);
+}
+
+// Derived thermodynamics at a solution: T mu p s rho e w cs2 and dw/ds, dw/drho
+// (reference include/eos.h:121-175, src/eos.cpp:276-344). th must hold NTH doubles.
+__host__ __device__ inline void set_thermo(const EosDev& e, int k, const double* x, double* th) {
+  const int model = chain_model(e.kind, k);
+  double o[17];
+  model_thermo(e, model, x, o);
+  const double T = x[0], mB = x[1], mQ = x[2], mS = x[3];
+  const double s = o[1], B = o[2], S = o[3], Q = o[4];
+  th[T_T] = T; th[T_MUB] = mB; th[T_MUS] = mS; th[T_MUQ] = mQ;
+  th[T_P] = o[0]; th[T_S] = s; th[T_RB] = B; th[T_RS] = S; th[T_RQ] = Q; th[T_E] = o[5];
+  th[T_W] = o[5] + o[0]; th[T_CS2] = o[6];
+  const Chi X{o[16], o[13], o[14], o[15], o[7], o[8], o[9], o[10], o[11], o[12]};
+  const bool hB = fabs(B) > kTiny, hS = fabs(S) > kTiny, hQ = fabs(Q) > kTiny;
+  if (e.thermo_mode == 1) {
+    // exact: G = H^-1 over the Hessian rows that are not identically zero
+    double H[4][4] = {{X.t2, X.tb, X.ts, X.tq}, {X.tb, X.b2, X.bs, X.bq}, {X.ts, X.bs, X.s2, X.sq},
+                      {X.tq, X.bq, X.sq, X.q2}};
+    if (model == M_CDIAG)
+      for (int i = 0; i < 4; i++) for (int j = 0; j < 4; j++) if (i != j) H[i][j] = 0.0;
+    int keep[4], m = 0;
+    for (int i = 0; i < 4; i++) {
+      bool zero = true;
+      for (int j = 0; j < 4; j++) zero = zero && (H[i][j] == 0.0);
+      if (!zero) keep[m++] = i;
+    }
+    double A[4][8];
+    for (int i = 0; i < 4; i++) for (int j = 0; j < 8; j++) A[i][j] = 0.0;
+    for (int i = 0; i < m; i++) {
+      for (int j = 0; j < m; j++) A[i][j] = H[keep[i]][keep[j]];
+      A[i][m + i] = 1.0;
+    }
+    for (int col = 0; col < m; col++) {
+      int p = col;
+      for (int r = col + 1; r < m; r++) if (fabs(A[r][col]) > fabs(A[p][col])) p = r;
+      if (p != col) for (int j = 0; j < 2 * m; j++) { double t = A[col][j]; A[col][j] = A[p][j]; A[p][j] = t; }
+      const double piv = A[col][col];
+      for (int j = 0; j < 2 * m; j++) A[col][j] /= piv;
+      for (int r = 0; r < m; r++) {
+        if (r == col || A[r][col] == 0.0) continue;
+        const double f = A[r][col];
+        for (int j = 0; j < 2 * m; j++) A[r][j] -= f * A[col][j];
+      }
+    }
+    double G[4][4];
+    for (int i = 0; i < 4; i++) for (int j = 0; j < 4; j++) G[i][j] = 0.0;
+    for (int i = 0; i < m; i++) for (int j = 0; j < m; j++) G[keep[i]][keep[j]] = A[i][m + j];
+    const double rho[4] = {0.0, B, S, Q};
+    const bool act[4] = {true, hB, hS, hQ};
+    const double mu[4] = {T, mB, mS, mQ};
+    for (int a = 0; a < 4; a++) {
+      double acc = mu[a];
+      if (a == 0 || act[a]) {
+        acc += s * G[0][a];
+        for (int b = 1; b < 4; b++) if (act[b]) acc += rho[b] * G[b][a];
+      }
+      th[T_DWDS + a] = acc;
+    }
+    return;
+  }
+  double ct = 0.0;
+  if (hB) ct += B / schur_term(X, 1);
+  if (hQ) ct += Q / schur_term(X, 3);
+  if (hS) ct += S / schur_term(X, 2);
+  th[T_DWDS] = T + s / schur_term(X, 0) + ct;
+  ct = 0.0;
+  if (hB) {
+    ct += s / schur_term(X, 4) + B / schur_term(X, 7 + 0);
+    if (hQ) ct += Q / schur_term(X, 7 + 0 * 3 + 2);
+    if (hS) ct += S / schur_term(X, 7 + 0 * 3 + 1);
+  }
+  th[T_DWDB] = mB + ct;
+  ct = 0.0;
+  if (hS) {
+    ct += s / schur_term(X, 5) + S / schur_term(X, 7 + 1 * 3 + 1);
+    if (hB) ct += B / schur_term(X, 7 + 1 * 3 + 0);
+    if (hQ) ct += Q / schur_term(X, 7 + 1 * 3 + 2);
+  }
+  th[T_DWDSS] = mS + ct;
+  ct = 0.0;
+  if (hQ) {
+    ct += s / schur_term(X, 6) + Q / schur_term(X, 7 + 2 * 3 + 2);
+    if (hB) ct += B / schur_term(X, 7 + 2 * 3 + 0);
+    if (hS) ct += S / schur_term(X, 7 + 2 * 3 + 1);
+  }
+  th[T_DWDQ] = mQ + ct;
+}
+
+}  // namespace ccake

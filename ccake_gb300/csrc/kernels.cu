@@ -1,0 +1,676 @@
+// Kernels of the GB300 SPH hot path.
+//
+// One RK2 substep is four small cell-list kernels plus two fused passes:
+//   pass A  (per particle a): smoothing sums over the 3^D neighbour cells,
+//           LRF densities, EoS Newton inversion, pi^{mu nu} constraints;
+//           writes neighbour record B.
+//   pass B  (per particle a): gradient sums in separable form, the MRF
+//           equations of motion and the RK2 update of the state; writes
+//           neighbour record A for the next substep.
+// Each particle's sums are accumulated in registers by the thread that owns
+// it (gather, no atomics), in a fixed cell/index order, so results are
+// reproducible run to run.
+#include <cstdio>
+
+#include "kernels.cuh"
+#include "physics.cuh"
+
+namespace ccake {
+
+namespace {
+
+constexpr int kBlock = 128;
+
+// ---------------------------------------------------------------------------
+// neighbour cells: count, scan, scatter, in-cell sort
+// ---------------------------------------------------------------------------
+template <int D>
+__global__ void k_bin(RunConst rc, Ptrs p) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.n) return;
+  const Grid& g = rc.grid;
+  int c = cell_coord(g, 0, p.y[Y_X0 * p.n + i]);
+  c += g.nc[0] * cell_coord(g, 1, p.y[Y_X1 * p.n + i]);
+  if (D == 3) c += g.nc[0] * g.nc[1] * cell_coord(g, 2, p.y[Y_X2 * p.n + i]);
+  p.cell_of[i] = c;
+  p.cell_rank[i] = atomicAdd(&p.cell_count[c], 1);
+}
+
+// Exclusive scan of the cell counts by one CTA (each thread owns a chunk).
+__global__ void k_scan(const int32_t* __restrict__ cnt, int32_t* __restrict__ start, int ncell) {
+  __shared__ int32_t warp_tot[32];
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int chunk = (ncell + nt - 1) / nt;
+  const int b = tid * chunk, e = min(ncell, b + chunk);
+  int32_t local = 0;
+  for (int c = b; c < e; c++) local += cnt[c];
+  // block exclusive scan of `local`
+  const int lane = tid & 31, wid = tid >> 5;
+  int32_t x = local;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_tot[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    int32_t w = (lane < (nt >> 5)) ? warp_tot[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int32_t y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    warp_tot[lane] = w;
+  }
+  __syncthreads();
+  int32_t run = x - local + (wid > 0 ? warp_tot[wid - 1] : 0);
+  for (int c = b; c < e; c++) {
+    start[c] = run;
+    run += cnt[c];
+  }
+  if (tid == nt - 1) start[ncell] = run;
+}
+
+__global__ void k_scatter(Ptrs p) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.n) return;
+  p.cell_idx[p.cell_start[p.cell_of[i]] + p.cell_rank[i]] = i;
+}
+
+// Sorts each cell's index list (insertion sort; cells hold tens of particles)
+// so the summation order does not depend on atomic arrival order.
+__global__ void k_sort_cells(Ptrs p, int ncell) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncell) return;
+  const int b = p.cell_start[c], e = p.cell_start[c + 1];
+  for (int j = b + 1; j < e; j++) {
+    const int32_t key = p.cell_idx[j];
+    int k = j - 1;
+    while (k >= b && p.cell_idx[k] > key) { p.cell_idx[k + 1] = p.cell_idx[k]; k--; }
+    p.cell_idx[k + 1] = key;
+  }
+}
+
+// Iterates the 3^D neighbour cells of a position; calls f(b) for every
+// particle b != a in them.
+template <int D, class F>
+__device__ __forceinline__ void for_candidates(const RunConst& rc, const Ptrs& p, int a, const double* xa, F&& f) {
+  const Grid& g = rc.grid;
+  const int cx = cell_coord(g, 0, xa[0]), cy = cell_coord(g, 1, xa[1]);
+  const int cz = (D == 3) ? cell_coord(g, 2, xa[2]) : 0;
+  const int zlo = (D == 3) ? max(cz - 1, 0) : 0, zhi = (D == 3) ? min(cz + 1, g.nc[2] - 1) : 0;
+  for (int z = zlo; z <= zhi; z++)
+    for (int y = max(cy - 1, 0); y <= min(cy + 1, g.nc[1] - 1); y++) {
+      const int row = (z * g.nc[1] + y) * g.nc[0];
+      const int c0 = row + max(cx - 1, 0), c1 = row + min(cx + 1, g.nc[0] - 1);
+      // cells c0..c1 are contiguous in the sorted list
+      const int jb = p.cell_start[c0], je = p.cell_start[c1 + 1];
+      for (int j = jb; j < je; j++) {
+        const int b = p.cell_idx[j];
+        if (b != a) f(b);
+      }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// pass A
+// ---------------------------------------------------------------------------
+template <int D>
+__device__ __forceinline__ void thermo_tail(const RunConst& rc, const EosDev& eos, const Ptrs& p, int i, double t) {
+  const int n = p.n;
+  const double t2 = t * t;
+  double th[NTH];
+  double x[4] = {p.th[T_T * n + i], p.th[T_MUB * n + i], p.th[T_MUQ * n + i], p.th[T_MUS * n + i]};
+  const double tgt[4] = {p.th[T_S * n + i], p.th[T_RB * n + i], p.th[T_RS * n + i], p.th[T_RQ * n + i]};
+  int iters = 0;
+  const int k = eos_invert(eos, 1, tgt, p.eos_id[i], x, &iters);
+  if (k < 0) {
+    atomicAdd(&p.err[E_EOS], 1);
+    return;
+  }
+  set_thermo(eos, k, x, th);
+#pragma unroll
+  for (int q = 0; q < NTH; q++) p.th[q * n + i] = th[q];
+  p.eos_id[i] = k;
+  p.eos_iters[i] = iters;
+  // pi^{mu nu} and Pi from the extensive forms
+  const double sig = p.sig[i], g = p.gam[i], slab = p.slab[i];
+  double u3[3] = {p.y[Y_U0 * n + i], p.y[Y_U1 * n + i], D == 3 ? p.y[Y_U2 * n + i] : 0.0};
+  double es[5];
+#pragma unroll
+  for (int q = 0; q < 5; q++) es[q] = p.y[(Y_SHV0 + q) * n + i];
+  double pi[NPI];
+  reset_pi(es, sig, g, u3, t2, pi);
+  const double Pi = p.y[Y_EBULK * n + i] * sig;
+  p.bulk[i] = Pi;
+#pragma unroll
+  for (int q = 0; q < NPI; q++) p.pi[q * n + i] = pi[q];
+  // neighbour record B
+  const double isl2 = 1.0 / (slab * slab);
+  double* rb = p.recB + (size_t)i * RB;
+  rb[B_X0] = p.y[Y_X0 * n + i];
+  rb[B_X1] = p.y[Y_X1 * n + i];
+  rb[B_X2] = D == 3 ? p.y[Y_X2 * n + i] : 0.0;
+  rb[B_M] = p.m[i];
+  rb[B_P] = th[T_P] * isl2;
+  rb[B_E] = th[T_E];
+  rb[B_PI] = Pi * isl2;
+#pragma unroll
+  for (int q = 0; q < 3; q++) {
+    rb[B_V0 + q] = p.v[q * n + i];
+    rb[B_PI0 + q] = pi[pi_slot(0, q + 1)] * isl2;
+  }
+  rb[B_PIJ + 0] = pi[P11] * isl2;
+  rb[B_PIJ + 1] = pi[P12] * isl2;
+  rb[B_PIJ + 2] = pi[P13] * isl2;
+  rb[B_PIJ + 3] = pi[P22] * isl2;
+  rb[B_PIJ + 4] = pi[P23] * isl2;
+  rb[B_PIJ + 5] = pi[P33] * isl2;
+}
+
+template <int D>
+__global__ void __launch_bounds__(kBlock) k_passA(RunConst rc, EosDev eos, Ptrs p, int mode) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.n) return;
+  const int n = p.n;
+  const double t = p.clock->t;
+  const double2* ra = reinterpret_cast<const double2*>(p.recA);
+  const double2 a01 = ra[(size_t)i * 4 + 0], a23 = ra[(size_t)i * 4 + 1];
+  const double2 a45 = ra[(size_t)i * 4 + 2], a67 = ra[(size_t)i * 4 + 3];
+  const double xa[3] = {a01.x, a01.y, a23.x};
+  const double k0 = rc.k0;
+  double sl = a23.y * k0, s0 = a45.x * k0, s1 = a45.y * k0, s2 = a67.x * k0, s3 = a67.y * k0;
+  int nn = 0;
+  const bool charges = true;
+  for_candidates<D>(rc, p, i, xa, [&](int b) {
+    const double2 b01 = __ldg(&ra[(size_t)b * 4 + 0]), b23 = __ldg(&ra[(size_t)b * 4 + 1]);
+    double d[3] = {xa[0] - b01.x, xa[1] - b01.y, xa[2] - b23.x};
+    const double d2 = dist2_exact<D>(d);
+    if (d2 <= rc.cut2) {
+      nn++;
+      const double r = sqrt(d2);
+      const double q = r * rc.inv_h;
+      double W;
+      if (q >= 2.0) W = 0.0;
+      else if (q >= 1.0) { const double z = 2.0 - q; W = rc.wn2 * z * z * z; }
+      else W = rc.wn * (1.0 - 1.5 * q * q + 0.75 * q * q * q);
+      const double2 b45 = __ldg(&ra[(size_t)b * 4 + 2]);
+      sl += b23.y * W;
+      s0 += b45.x * W;
+      if (charges) {
+        const double2 b67 = __ldg(&ra[(size_t)b * 4 + 3]);
+        s1 += b45.y * W;
+        s2 += b67.x * W;
+        s3 += b67.y * W;
+      }
+    }
+  });
+  // gamma and v from u (update_velocity), LRF densities (get_LRF = lab/(gamma t))
+  const double u3[3] = {p.y[Y_U0 * n + i], p.y[Y_U1 * n + i], D == 3 ? p.y[Y_U2 * n + i] : 0.0};
+  const double g = gamma_milne<D>(u3, t * t);
+  p.gam[i] = g;
+#pragma unroll
+  for (int q = 0; q < 3; q++) p.v[q * n + i] = (q < D) ? u3[q] / g : 0.0;
+  p.slab[i] = sl;
+  p.sig[i] = sl / g / t;
+  p.th[T_S * n + i] = s0 / g / t;
+  p.th[T_RB * n + i] = s1 / g / t;
+  p.th[T_RS * n + i] = s2 / g / t;
+  p.th[T_RQ * n + i] = s3 / g / t;
+  p.btrack[i] = nn;
+  if (mode == A_WITH_THERMO) thermo_tail<D>(rc, eos, p, i, t);
+}
+
+template <int D>
+__global__ void __launch_bounds__(kBlock) k_thermo(RunConst rc, EosDev eos, Ptrs p) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.n) return;
+  thermo_tail<D>(rc, eos, p, i, p.clock->t);
+}
+
+// ---------------------------------------------------------------------------
+// pass B
+// ---------------------------------------------------------------------------
+template <int D>
+__global__ void __launch_bounds__(kBlock) k_passB(RunConst rc, Ptrs p, int mode, double dt_sub) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.n) return;
+  const int n = p.n;
+  const double t = p.clock->t;
+  const bool shear = rc.cfg.using_shear;
+  const double* rbA = p.recB + (size_t)i * RB;
+  const double xa[3] = {rbA[B_X0], rbA[B_X1], rbA[B_X2]};
+  // separable accumulators: S1 = sum m grad W, SX = sum m X_b grad W, ...
+  double S1[D], SP[D], SE[D], SB[D], SV[D][D], S0[D][D], SD[D];
+#pragma unroll
+  for (int k = 0; k < D; k++) {
+    S1[k] = SP[k] = SE[k] = SB[k] = SD[k] = 0.0;
+#pragma unroll
+    for (int l = 0; l < D; l++) SV[k][l] = S0[k][l] = 0.0;
+  }
+  for_candidates<D>(rc, p, i, xa, [&](int b) {
+    const double* rb = p.recB + (size_t)b * RB;
+    const double2 b01 = __ldg(reinterpret_cast<const double2*>(rb));
+    const double2 b23 = __ldg(reinterpret_cast<const double2*>(rb + 2));
+    double d[3] = {xa[0] - b01.x, xa[1] - b01.y, xa[2] - b23.x};
+    const double d2 = dist2_exact<D>(d);
+    if (d2 <= rc.cut2) {
+      // grad_a W(r_a - r_b), reference src/kernel.cpp:95-118
+      const double r = sqrt(d2);
+      const double q = r * rc.inv_h;
+      double f;
+      if (q >= 2.0) f = 0.0;
+      else if (q >= 1.0) { const double z = 2.0 - q; f = (rc.gn / r) * z * z; }
+      else f = rc.gn2 * (1.5 * q - 2) * rc.inv_h;
+      const double mf = b23.y * f;   // m_b * (grad W)/rel
+      double gm[D];
+#pragma unroll
+      for (int k = 0; k < D; k++) gm[k] = mf * d[k];
+      const double2 b45 = __ldg(reinterpret_cast<const double2*>(rb + 4));
+      const double2 b67 = __ldg(reinterpret_cast<const double2*>(rb + 6));
+      const double2 v01 = __ldg(reinterpret_cast<const double2*>(rb + B_V0));
+      const double vb[3] = {v01.x, v01.y, D == 3 ? __ldg(rb + B_V0 + 2) : 0.0};
+#pragma unroll
+      for (int k = 0; k < D; k++) {
+        S1[k] += gm[k];
+        SP[k] += b45.x * gm[k];
+        SE[k] += b45.y * gm[k];
+        SB[k] += b67.x * gm[k];
+#pragma unroll
+        for (int l = 0; l < D; l++) SV[k][l] += vb[l] * gm[k];
+      }
+      if (shear) {
+        double p0[3], pij[6];
+#pragma unroll
+        for (int k = 0; k < D; k++) p0[k] = __ldg(rb + B_PI0 + k);
+#pragma unroll
+        for (int k = 0; k < 6; k++) pij[k] = (D == 3 || (k != 2 && k != 4 && k != 5)) ? __ldg(rb + B_PIJ + k) : 0.0;
+        // pi^{ij}/sl^2 with (11 12 13 22 23 33) packing
+        auto PJ = [&](int a_, int b_) {
+          const int lo = a_ < b_ ? a_ : b_, hi = a_ < b_ ? b_ : a_;
+          return pij[lo == 0 ? hi : (lo == 1 ? 2 + hi : 5)];
+        };
+#pragma unroll
+        for (int k = 0; k < D; k++) {
+#pragma unroll
+          for (int l = 0; l < D; l++) S0[k][l] += p0[l] * gm[k];
+          double acc = 0.0;
+#pragma unroll
+          for (int l = 0; l < D; l++) acc += PJ(k, l) * gm[l];
+          SD[k] += acc;
+        }
+      }
+    }
+  });
+  // own values
+  const double sla = p.slab[i];
+  const double ea = rbA[B_E], Pa = rbA[B_P], Pia = rbA[B_PI];
+  double va[3] = {rbA[B_V0], rbA[B_V0 + 1], D == 3 ? rbA[B_V0 + 2] : 0.0};
+  double gP[3] = {0, 0, 0}, gE[3] = {0, 0, 0}, gB[3] = {0, 0, 0}, gS[3] = {0, 0, 0}, dS[3] = {0, 0, 0};
+  double gV[9] = {0};
+  double vS1 = 0.0;
+#pragma unroll
+  for (int k = 0; k < D; k++) vS1 += va[k] * S1[k];
+#pragma unroll
+  for (int k = 0; k < D; k++) {
+    gP[k] = sla * (SP[k] + Pa * S1[k]);
+    gE[k] = (SE[k] - ea * S1[k]) / sla;
+    gB[k] = sla * (SB[k] + Pia * S1[k]);
+#pragma unroll
+    for (int l = 0; l < D; l++) gV[k * D + l] = (SV[k][l] - va[l] * S1[k]) / sla;
+    if (shear) {
+      double acc = 0.0;
+#pragma unroll
+      for (int l = 0; l < D; l++) acc += va[l] * S0[l][k];
+      gS[k] = sla * (acc + rbA[B_PI0 + k] * vS1);
+      double acc2 = SD[k];
+#pragma unroll
+      for (int l = 0; l < D; l++) {
+        const int lo = k < l ? k : l, hi = k < l ? l : k;
+        acc2 += rbA[B_PIJ + (lo == 0 ? hi : (lo == 1 ? 2 + hi : 5))] * S1[l];
+      }
+      dS[k] = sla * acc2;
+    }
+  }
+  if (mode & B_GRADS) {
+#pragma unroll
+    for (int k = 0; k < D; k++) {
+      p.grads[(G_P + k) * n + i] = gP[k];
+      p.grads[(G_E + k) * n + i] = gE[k];
+      p.grads[(G_B + k) * n + i] = gB[k];
+      p.grads[(G_SH + k) * n + i] = gS[k];
+      p.grads[(G_DS + k) * n + i] = dS[k];
+    }
+#pragma unroll
+    for (int k = 0; k < D * D; k++) p.grads[(G_V + k) * n + i] = gV[k];
+  }
+  if (!(mode & B_EOM)) return;
+  // equations of motion for particle i
+  double th[NTH];
+#pragma unroll
+  for (int q = 0; q < NTH; q++) th[q] = p.th[q * n + i];
+  EomIn<D> in;
+  in.th = th;
+#pragma unroll
+  for (int q = 0; q < 3; q++) {
+    in.u[q] = (q < D) ? p.y[(Y_U0 + q) * n + i] : 0.0;
+    in.v[q] = va[q];
+    in.gradP[q] = gP[q];
+    in.gradBulk[q] = gB[q];
+    in.gradshear[q] = gS[q];
+    in.divshear[q] = dS[q];
+  }
+#pragma unroll
+  for (int q = 0; q < 9; q++) in.gradV[q] = gV[q];
+  in.g = p.gam[i];
+  in.sigma = p.sig[i];
+  in.sigma_lab = sla;
+  in.m = p.m[i];
+  in.Pi = p.bulk[i];
+#pragma unroll
+  for (int q = 0; q < NPI; q++) in.pi[q] = p.pi[q * n + i];
+  const Transport k = transport(rc.cfg, th);
+  EomOut o;
+  eom<D>(rc.cfg, k, in, t, o);
+  if (mode & B_DERIVS) {
+#pragma unroll
+    for (int q = 0; q < 3; q++) p.derivs[(D_DU0 + q) * n + i] = (q < D) ? o.du[q] : 0.0;
+    p.derivs[D_DS * n + i] = o.dS;
+    p.derivs[D_DBULK * n + i] = o.dBulk;
+#pragma unroll
+    for (int q = 0; q < 5; q++) p.derivs[(D_DSHV0 + q) * n + i] = o.dShv[q];
+    p.derivs[D_DEZ * n + i] = o.dEz;
+    p.derivs[D_ETA * n + i] = k.eta;
+    p.derivs[D_TAUPI * n + i] = k.tau_pi;
+    p.derivs[D_ZETA * n + i] = k.zeta;
+    p.derivs[D_TAUBULK * n + i] = k.tau_Pi;
+  }
+  if (!(mode & B_UPDATE)) return;
+  // midpoint RK2 update from the step-start cache (reference src/evolver.cpp:344-486)
+  const double* y0 = p.y0;
+  double ynew[NY];
+#pragma unroll
+  for (int q = 0; q < NY; q++) ynew[q] = y0[q * n + i];
+#pragma unroll
+  for (int q = 0; q < D; q++) {
+    ynew[Y_X0 + q] += dt_sub * va[q];
+    ynew[Y_U0 + q] += dt_sub * o.du[q];
+  }
+  double es = ynew[Y_ES] + dt_sub * o.dS;
+  ynew[Y_EBULK] += dt_sub * o.dBulk;
+#pragma unroll
+  for (int q = 0; q < 5; q++) ynew[Y_SHV0 + q] += dt_sub * o.dShv[q];
+  ynew[Y_EZ] += dt_sub * o.dEz;
+  if (es < 0.0) {
+    if (p.freeze[i] > 3) es = 1.e-3;
+    else atomicAdd(&p.err[E_NEGS], 1);
+  }
+  ynew[Y_ES] = es;
+  bool finite = true;
+#pragma unroll
+  for (int q = 0; q < NY; q++) finite = finite && isfinite(ynew[q]);
+  if (!finite) atomicAdd(&p.err[E_NONFINITE], 1);
+#pragma unroll
+  for (int q = 0; q < NY; q++) p.y[q * n + i] = ynew[q];
+  if (mode & B_WRITE_Y0) {
+#pragma unroll
+    for (int q = 0; q < NY; q++) p.y0[q * n + i] = ynew[q];
+  }
+  // neighbour record A for the next substep
+  const double m = p.m[i];
+  double2* ra = reinterpret_cast<double2*>(p.recA) + (size_t)i * 4;
+  ra[0] = make_double2(ynew[Y_X0], ynew[Y_X1]);
+  ra[1] = make_double2(D == 3 ? ynew[Y_X2] : 0.0, m);
+  ra[2] = make_double2(m * ynew[Y_ES], m * ynew[Y_EB]);
+  ra[3] = make_double2(m * ynew[Y_ESS], m * ynew[Y_EQ]);
+}
+
+__global__ void k_visc(RunConst rc, Ptrs p) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.n) return;
+  const int n = p.n;
+  double th[NTH];
+  for (int q = 0; q < NTH; q++) th[q] = p.th[q * n + i];
+  const Transport k = transport(rc.cfg, th);
+  p.derivs[D_ETA * n + i] = k.eta;
+  p.derivs[D_TAUPI * n + i] = k.tau_pi;
+  p.derivs[D_ZETA * n + i] = k.zeta;
+  p.derivs[D_TAUBULK * n + i] = k.tau_Pi;
+}
+
+__global__ void k_clock(Clock* c, int substep, double dt) {
+  if (substep == 1) c->t = c->t0 + 0.5 * dt;
+  else { c->t = c->t0 + dt; c->t0 = c->t; }
+}
+
+// ---------------------------------------------------------------------------
+// initialisation (reference src/sph_workstation.cpp:252-375, :1228-1340)
+// ---------------------------------------------------------------------------
+template <int D>
+__global__ void k_init_state(RunConst rc, Ptrs p) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.n) return;
+  const int n = p.n;
+  const double t = p.clock->t;
+  const double u3[3] = {p.y[Y_U0 * n + i], p.y[Y_U1 * n + i], D == 3 ? p.y[Y_U2 * n + i] : 0.0};
+  const double g = gamma_milne<D>(u3, t * t);
+  p.gam[i] = g;
+  for (int q = 0; q < 3; q++) p.v[q * n + i] = (q < D) ? u3[q] / g : 0.0;
+  p.m[i] = 1.0;
+  for (int q = Y_ES; q <= Y_EQ; q++) p.y[q * n + i] = 1.0;
+  p.y[Y_EBULK * n + i] = 0.0;
+  for (int q = 0; q < 5; q++) p.y[(Y_SHV0 + q) * n + i] = 0.0;
+  p.y[Y_EZ * n + i] = 0.0;
+  p.th[T_T * n + i] = 580.0 / kHbarcMeVfm;
+  p.th[T_MUB * n + i] = p.th[T_MUS * n + i] = p.th[T_MUQ * n + i] = 0.0;
+  p.eos_id[i] = 0;
+  p.freeze[i] = 0;
+  double2* ra = reinterpret_cast<double2*>(p.recA) + (size_t)i * 4;
+  ra[0] = make_double2(p.y[Y_X0 * n + i], p.y[Y_X1 * n + i]);
+  ra[1] = make_double2(D == 3 ? p.y[Y_X2 * n + i] : 0.0, 1.0);
+  ra[2] = make_double2(1.0, 1.0);
+  ra[3] = make_double2(1.0, 1.0);
+}
+
+__global__ void k_init_invert(RunConst rc, EosDev eos, Ptrs p) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.n) return;
+  const int n = p.n;
+  const int entropy = rc.cfg.input_as_entropy;
+  double x[4] = {p.th[T_T * n + i], 0.0, 0.0, 0.0};
+  double tgt[4] = {p.in_e[i], p.in_rho[i], p.in_rho[n + i], p.in_rho[2 * n + i]};
+  int iters = 0;
+  int k = eos_invert(eos, entropy, tgt, 0, x, &iters);
+  if (k < 0 && !entropy) {
+    // freeze the particle and retry at zero charge (src/sph_workstation.cpp:1825-1848)
+    p.freeze[i] = 4;
+    x[0] = p.th[T_T * n + i]; x[1] = x[2] = x[3] = 0.0;
+    const double tz[4] = {tgt[0], 0.0, 0.0, 0.0};
+    k = eos_invert(eos, 0, tz, 0, x, &iters);
+  }
+  if (k < 0) { atomicAdd(&p.err[E_EOS], 1); return; }
+  double th[NTH];
+  set_thermo(eos, k, x, th);
+  for (int q = 0; q < NTH; q++) p.th[q * n + i] = th[q];
+  p.eos_id[i] = k;
+  p.eos_iters[i] = iters;
+  if (entropy) { p.in_s[i] = p.in_e[i]; p.in_e[i] = th[T_E]; }
+  else p.in_s[i] = th[T_S];
+  if (!(p.in_e[i] > rc.efreeze && p.freeze[i] != 4)) p.freeze[i] = 4;
+}
+
+// ext = input/sigma after the initial sigma (src/sph_workstation.cpp:338-364)
+template <int D>
+__global__ void k_init_ext(RunConst rc, Ptrs p) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.n) return;
+  const int n = p.n;
+  const double sg = p.sig[i];
+  const double es = p.in_s[i] / sg;
+  p.y[Y_ES * n + i] = es;
+  p.y[Y_EB * n + i] = p.in_rho[i] / sg;
+  p.y[Y_ESS * n + i] = p.in_rho[n + i] / sg;
+  p.y[Y_EQ * n + i] = p.in_rho[2 * n + i] / sg;
+  if (p.in_s[i] < 0.0) p.freeze[i] = 4;
+  const double m = p.m[i];
+  double2* ra = reinterpret_cast<double2*>(p.recA) + (size_t)i * 4;
+  ra[2] = make_double2(m * es, m * p.y[Y_EB * n + i]);
+  ra[3] = make_double2(m * p.y[Y_ESS * n + i], m * p.y[Y_EQ * n + i]);
+}
+
+// ---------------------------------------------------------------------------
+// conservation sums (src/system_state.cpp:738-885): per-block partials in a
+// fixed order, summed on the host
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_totals(RunConst rc, Ptrs p) {
+  __shared__ double sh[6][256];
+  const int n = p.n;
+  const double t = p.clock->t;
+  const double sqrtg = rc.cfg.coord == 0 ? t : 1.0;
+  double acc[6] = {0, 0, 0, 0, 0, 0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double m = p.m[i];
+    acc[0] += p.y[Y_ES * n + i] * m;
+    acc[1] += p.y[Y_EB * n + i] * m;
+    acc[2] += p.y[Y_ESS * n + i] * m;
+    acc[3] += p.y[Y_EQ * n + i] * m;
+    const double g = p.gam[i];
+    const double C = p.th[T_W * n + i] + p.bulk[i];
+    acc[4] += (C * g * g - p.th[T_P * n + i] - p.bulk[i] + p.pi[P00 * n + i]) * m * sqrtg / p.slab[i];
+    acc[5] += p.y[Y_EZ * n + i];
+  }
+  for (int q = 0; q < 6; q++) sh[q][threadIdx.x] = acc[q];
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s)
+      for (int q = 0; q < 6; q++) sh[q][threadIdx.x] += sh[q][threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int q = 0; q < 6; q++) p.partials[blockIdx.x * 6 + q] = sh[q][0];
+}
+
+// ---------------------------------------------------------------------------
+// explicit neighbour list (parity checks only)
+// ---------------------------------------------------------------------------
+template <int D>
+__global__ void k_nbr_count(RunConst rc, Ptrs p, int32_t* counts) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.n) return;
+  const double xa[3] = {p.y[Y_X0 * p.n + i], p.y[Y_X1 * p.n + i], D == 3 ? p.y[Y_X2 * p.n + i] : 0.0};
+  int c = 0;
+  for_candidates<D>(rc, p, i, xa, [&](int b) {
+    double d[3] = {xa[0] - p.y[Y_X0 * p.n + b], xa[1] - p.y[Y_X1 * p.n + b],
+                   D == 3 ? xa[2] - p.y[Y_X2 * p.n + b] : 0.0};
+    if (dist2_exact<D>(d) <= rc.cut2) c++;
+  });
+  counts[i] = c;
+}
+
+template <int D>
+__global__ void k_nbr_fill(RunConst rc, Ptrs p, const int32_t* off, int32_t* idx) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.n) return;
+  const double xa[3] = {p.y[Y_X0 * p.n + i], p.y[Y_X1 * p.n + i], D == 3 ? p.y[Y_X2 * p.n + i] : 0.0};
+  int c = off[i];
+  for_candidates<D>(rc, p, i, xa, [&](int b) {
+    double d[3] = {xa[0] - p.y[Y_X0 * p.n + b], xa[1] - p.y[Y_X1 * p.n + b],
+                   D == 3 ? xa[2] - p.y[Y_X2 * p.n + b] : 0.0};
+    if (dist2_exact<D>(d) <= rc.cut2) idx[c++] = b;
+  });
+}
+
+__global__ void k_eos_batch(EosDev eos, int entropy, int64_t n, const double* in4, double* tbqs, double* th16,
+                            int32_t* status, int32_t* iters) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double x[4] = {tbqs[4 * i], tbqs[4 * i + 1], tbqs[4 * i + 2], tbqs[4 * i + 3]};
+  int it = 0;
+  const int k = eos_invert(eos, entropy, in4 + 4 * i, 0, x, &it);
+  status[i] = k;
+  if (iters) iters[i] = it;
+  if (k >= 0) {
+    for (int q = 0; q < 4; q++) tbqs[4 * i + q] = x[q];
+    if (th16) set_thermo(eos, k, x, th16 + 16 * i);
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+void launch_build_cells(const RunConst& rc, const Ptrs& p, cudaStream_t s) {
+  const int nb = (p.n + kBlock - 1) / kBlock;
+  cudaMemsetAsync(p.cell_count, 0, sizeof(int32_t) * rc.grid.ncell, s);
+  if (rc.cfg.dim == 3) k_bin<3><<<nb, kBlock, 0, s>>>(rc, p);
+  else k_bin<2><<<nb, kBlock, 0, s>>>(rc, p);
+  k_scan<<<1, 1024, 0, s>>>(p.cell_count, p.cell_start, rc.grid.ncell);
+  k_scatter<<<nb, kBlock, 0, s>>>(p);
+  k_sort_cells<<<(rc.grid.ncell + 255) / 256, 256, 0, s>>>(p, rc.grid.ncell);
+}
+
+void launch_passA(const RunConst& rc, const EosDev& eos, const Ptrs& p, int mode, cudaStream_t s) {
+  const int nb = (p.n + kBlock - 1) / kBlock;
+  if (rc.cfg.dim == 3) k_passA<3><<<nb, kBlock, 0, s>>>(rc, eos, p, mode);
+  else k_passA<2><<<nb, kBlock, 0, s>>>(rc, eos, p, mode);
+}
+
+void launch_thermo(const RunConst& rc, const EosDev& eos, const Ptrs& p, cudaStream_t s) {
+  const int nb = (p.n + kBlock - 1) / kBlock;
+  if (rc.cfg.dim == 3) k_thermo<3><<<nb, kBlock, 0, s>>>(rc, eos, p);
+  else k_thermo<2><<<nb, kBlock, 0, s>>>(rc, eos, p);
+}
+
+void launch_passB(const RunConst& rc, const Ptrs& p, int mode, double dt_sub, cudaStream_t s) {
+  const int nb = (p.n + kBlock - 1) / kBlock;
+  if (rc.cfg.dim == 3) k_passB<3><<<nb, kBlock, 0, s>>>(rc, p, mode, dt_sub);
+  else k_passB<2><<<nb, kBlock, 0, s>>>(rc, p, mode, dt_sub);
+}
+
+void launch_visc(const RunConst& rc, const Ptrs& p, cudaStream_t s) {
+  k_visc<<<(p.n + kBlock - 1) / kBlock, kBlock, 0, s>>>(rc, p);
+}
+
+void launch_clock(const Ptrs& p, int substep, double dt, cudaStream_t s) { k_clock<<<1, 1, 0, s>>>(p.clock, substep, dt); }
+
+void launch_init_state(const RunConst& rc, const Ptrs& p, cudaStream_t s) {
+  const int nb = (p.n + kBlock - 1) / kBlock;
+  if (rc.cfg.dim == 3) k_init_state<3><<<nb, kBlock, 0, s>>>(rc, p);
+  else k_init_state<2><<<nb, kBlock, 0, s>>>(rc, p);
+}
+
+void launch_init_invert(const RunConst& rc, const EosDev& eos, const Ptrs& p, cudaStream_t s) {
+  k_init_invert<<<(p.n + kBlock - 1) / kBlock, kBlock, 0, s>>>(rc, eos, p);
+}
+
+void launch_init_ext(const RunConst& rc, const Ptrs& p, cudaStream_t s) {
+  const int nb = (p.n + kBlock - 1) / kBlock;
+  if (rc.cfg.dim == 3) k_init_ext<3><<<nb, kBlock, 0, s>>>(rc, p);
+  else k_init_ext<2><<<nb, kBlock, 0, s>>>(rc, p);
+}
+
+void launch_totals(const RunConst& rc, const Ptrs& p, int nblocks, cudaStream_t s) {
+  k_totals<<<nblocks, 256, 0, s>>>(rc, p);
+}
+
+void launch_neighbour_counts(const RunConst& rc, const Ptrs& p, int32_t* counts, cudaStream_t s) {
+  const int nb = (p.n + kBlock - 1) / kBlock;
+  if (rc.cfg.dim == 3) k_nbr_count<3><<<nb, kBlock, 0, s>>>(rc, p, counts);
+  else k_nbr_count<2><<<nb, kBlock, 0, s>>>(rc, p, counts);
+}
+
+void launch_neighbour_fill(const RunConst& rc, const Ptrs& p, const int32_t* offsets, int32_t* idx, cudaStream_t s) {
+  const int nb = (p.n + kBlock - 1) / kBlock;
+  if (rc.cfg.dim == 3) k_nbr_fill<3><<<nb, kBlock, 0, s>>>(rc, p, offsets, idx);
+  else k_nbr_fill<2><<<nb, kBlock, 0, s>>>(rc, p, offsets, idx);
+}
+
+void launch_eos_batch(const EosDev& eos, int entropy, int64_t n, const double* in4, double* tbqs, double* th16,
+                      int32_t* status, int32_t* iters, cudaStream_t s) {
+  const int nb = (int)((n + kBlock - 1) / kBlock);
+  k_eos_batch<<<nb, kBlock, 0, s>>>(eos, entropy, n, in4, tbqs, th16, status, iters);
+}
+
+}  // namespace ccake

@@ -1,0 +1,65 @@
+// Device buffers and kernel launchers of the SPH hot path.
+#pragma once
+#include "common.cuh"
+#include "eos.cuh"
+
+namespace ccake {
+
+// Device pointers of one event (struct-of-arrays slabs of length n).
+struct Ptrs {
+  int n;
+  double* y;        // NY * n   current state
+  double* y0;       // NY * n   state at the start of the RK2 step
+  double* m;        // n        sph mass
+  double* th;       // NTH * n  thermodynamics (LRF densities before the EoS, solution after)
+  double* gam;      // n
+  double* v;        // 3 * n
+  double* slab;     // n        sigma_lab
+  double* sig;      // n        sigma (local rest frame)
+  double* bulk;     // n        Pi
+  double* pi;       // NPI * n  pi^{mu nu}
+  double* recA;     // RA * n   neighbour record of the smoothing pass
+  double* recB;     // RB * n   neighbour record of the gradient pass
+  double* grads;    // NGRAD * n (parity checks)
+  double* derivs;   // NDER * n  (parity checks)
+  double* in_e;     // n  input energy (or entropy) density
+  double* in_s;     // n  entropy density found at initialisation
+  double* in_rho;   // 3 * n input charge densities
+  int32_t* eos_id;
+  int32_t* eos_iters;
+  int32_t* btrack;
+  int32_t* freeze;
+  int32_t* cell_of;
+  int32_t* cell_rank;
+  int32_t* cell_count;
+  int32_t* cell_start;   // ncell + 1
+  int32_t* cell_idx;     // n
+  int32_t* err;          // NERR
+  Clock* clock;
+  double* partials;      // reduction scratch
+};
+
+// Pass A modes
+enum : int { A_SMOOTH_ONLY = 0, A_WITH_THERMO = 1 };
+// Pass B mode bits
+enum : int { B_GRADS = 1, B_EOM = 2, B_DERIVS = 4, B_UPDATE = 8, B_WRITE_Y0 = 16 };
+
+void launch_build_cells(const RunConst& rc, const Ptrs& p, cudaStream_t s);
+void launch_passA(const RunConst& rc, const EosDev& eos, const Ptrs& p, int mode, cudaStream_t s);
+void launch_thermo(const RunConst& rc, const EosDev& eos, const Ptrs& p, cudaStream_t s);
+void launch_passB(const RunConst& rc, const Ptrs& p, int mode, double dt_sub, cudaStream_t s);
+void launch_visc(const RunConst& rc, const Ptrs& p, cudaStream_t s);
+void launch_clock(const Ptrs& p, int substep, double dt, cudaStream_t s);
+void launch_init_state(const RunConst& rc, const Ptrs& p, cudaStream_t s);
+void launch_init_invert(const RunConst& rc, const EosDev& eos, const Ptrs& p, cudaStream_t s);
+void launch_init_ext(const RunConst& rc, const Ptrs& p, cudaStream_t s);
+void launch_totals(const RunConst& rc, const Ptrs& p, int nblocks, cudaStream_t s);
+void launch_neighbour_counts(const RunConst& rc, const Ptrs& p, int32_t* counts, cudaStream_t s);
+void launch_neighbour_fill(const RunConst& rc, const Ptrs& p, const int32_t* offsets, int32_t* idx,
+                           cudaStream_t s);
+void launch_eos_batch(const EosDev& eos, int entropy, int64_t n, const double* in4, double* tbqs, double* th16,
+                      int32_t* status, int32_t* iters, cudaStream_t s);
+
+constexpr int kTotBlocks = 608;   // 4 x 152 SMs; fixed so the sums are reproducible
+
+}  // namespace ccake

@@ -1,0 +1,411 @@
+// Device per-particle physics of the hot path: transport coefficients, the
+// pi^{mu nu} constraints, and the MRF equations of motion (ideal + shear +
+// bulk, Milne coordinates) for one particle. FP64, templated on dimension.
+#pragma once
+#include "common.cuh"
+
+namespace ccake {
+
+struct Transport {
+  double eta, tau_pi, zeta, tau_Pi, delta_PiPi, delta_pipi, lambda_piPi, lambda_Pipi, phi1, phi3, phi6, phi7,
+      tau_pipi;
+};
+
+// Reference src/transport_coefficients.cpp:620-900 (modes used by the hot path).
+__device__ inline Transport transport(const ccake_config& c, const double* th) {
+  Transport k;
+  const double T = th[T_T], w = th[T_W], cs2 = th[T_CS2], p = th[T_P];
+  k.eta = (T <= 0.0) ? 0.0 : c.eta_over_s * (w / T);
+  if (c.shear_relax_mode == 1) k.tau_pi = (5.0 * k.eta) / w;
+  else if (c.shear_relax_mode == 2) k.tau_pi = fmax((5.0 * k.eta) / w, 0.001);
+  else k.tau_pi = fmax(5.0 * k.eta / w, 0.005);
+  switch (c.zeta_mode) {
+    case 1: k.zeta = c.zeta_over_s * (w / T); break;
+    case 2: {
+      double factor = 1.0;
+      if (c.modulate_zeta_with_tanh) {
+        const double Ttr = 150.0 / kHbarcMeVfm, Tsc = 10.0 / kHbarcMeVfm;
+        const double thx = tanh((T - Ttr) / Tsc), xp = pow(T / Ttr, c.zeta_cs2_p);
+        factor = 0.5 * (1.0 + xp) + 0.5 * (1.0 - xp) * thx;
+      }
+      k.zeta = c.zeta_cs2_A * factor * pow((1.0 / 3.0) - fmin(cs2, 1.0), c.zeta_cs2_p) * w / T;
+      break;
+    }
+    case 3: {
+      const double x = (T - c.zeta_peak_T) / c.zeta_peak_width;
+      k.zeta = c.zeta_over_s * exp(-0.5 * x * x) * (w / T);
+      break;
+    }
+    default: k.zeta = 0.005 * (w / T);
+  }
+  const double cc = cs2 > 1 ? 1 : cs2;
+  const double pw = pow((1.0 / 3.0 - cc), c.zeta_cs2_p);
+  k.tau_Pi = (pw < 1e-10) ? 1e10 : fmax(5.0 * k.zeta / (pw * w), 0.1);
+  k.delta_PiPi = 2. * k.tau_Pi / 3.0;
+  k.delta_pipi = 4. * k.tau_pi / 3.0;
+  k.lambda_piPi = 6. / 5. * k.tau_pi;
+  k.lambda_Pipi = 8. * (1. / 3. - cc) * k.tau_Pi / 5.;
+  k.phi1 = 0.0;
+  k.phi3 = 0.0;
+  k.phi6 = 0.0;
+  k.phi7 = 9. / (70. * p);
+  k.tau_pipi = 10. * k.tau_pi / 7.0;
+  return k;
+}
+
+// gamma = sqrt(1 - u_i u^i) in Milne coordinates (reference src/eom_default.cpp:17-38,
+// include/milne.hpp:92-96 and :354).
+template <int D>
+__device__ __forceinline__ double gamma_milne(const double* u, double t2) {
+  double c = u[0] * u[0] + u[1] * u[1];
+  if (D == 3) c += t2 * u[2] * u[2];
+  return sqrt(1.0 + c);
+}
+
+// pi^{mu nu} from the extensive spatial components, tracelessness and
+// orthogonality (reference src/eom_default.cpp:56-172). pi[] uses PiSlot.
+__device__ inline void reset_pi(const double* ext_shv, double sigma, double g, const double* u3, double t2,
+                                double* pi) {
+  const double f0 = -u3[0], f1 = -u3[1], f2 = -t2 * u3[2];   // covariant u_i
+  const double p11 = ext_shv[0] * sigma, p12 = ext_shv[1] * sigma, p13 = ext_shv[2] * sigma;
+  const double p22 = ext_shv[3] * sigma, p23 = ext_shv[4] * sigma;
+  const double p00 = (f0 * f0 * p11 + f1 * f1 * p22 + 2. * f1 * f0 * p12 + 2. * f2 * f0 * p13 + 2. * f2 * f1 * p23 -
+                      f2 * f2 * (p11 + p22) / t2) / (g * g - f2 * f2 / t2);
+  const double p33 = (p00 - p11 - p22) / t2;
+  pi[P00] = p00; pi[P11] = p11; pi[P12] = p12; pi[P13] = p13; pi[P22] = p22; pi[P23] = p23; pi[P33] = p33;
+  pi[P01] = -(p11 * f0 + p12 * f1 + p13 * f2) / g;
+  pi[P02] = -(p12 * f0 + p22 * f1 + p23 * f2) / g;
+  pi[P03] = -(p13 * f0 + p23 * f1 + p33 * f2) / g;
+}
+
+// Inputs of the equations of motion for one particle.
+template <int D>
+struct EomIn {
+  double u[3], v[3];
+  double g, sigma, sigma_lab, m;
+  const double* th;          // NTH thermo values
+  double Pi;                 // bulk pressure
+  double pi[NPI];            // pi^{mu nu}
+  double gradP[3], gradBulk[3], gradshear[3], divshear[3], gradV[9];
+};
+
+struct EomOut {
+  double du[3], dS, dBulk, dShv[5], dEz;
+};
+
+// Reference src/eom_default.cpp:211-869 (evaluate_time_derivatives) and
+// :882-1412 (calculate_MRF_shear), without sources and without the diffusion
+// sector, for one particle at time t.
+template <int D>
+__device__ inline void eom(const ccake_config& cfg, const Transport& k, const EomIn<D>& in, double t, EomOut& o) {
+  const double t2 = t * t;
+  const double g = in.g, sig = in.sigma;
+  const double* th = in.th;
+  const double T = th[T_T], w = th[T_W], sden = th[T_S], dwds = th[T_DWDS];
+  const double rho[3] = {th[T_RB], th[T_RS], th[T_RQ]};
+  const double dwdr[3] = {th[T_DWDB], th[T_DWDSS], th[T_DWDQ]};
+  const double Pi = in.Pi;
+  auto P = [&](int i, int j) { return in.pi[pi_slot(i, j)]; };
+  // covariant spatial velocity (Vector<D>::make_covariant)
+  double u[3] = {in.u[0], in.u[1], D == 3 ? in.u[2] : 0.0};
+  double uc[3] = {-u[0], -u[1], D == 3 ? -t2 * u[2] : 0.0};
+  double divV = 0.0;
+#pragma unroll
+  for (int i = 0; i < D; i++) divV += in.gradV[i * D + i];
+  const double uD = u[D - 1];
+  const double geo = (D == 3) ? uD * uD * t / g : 0.0;
+  const double expn = g * divV + g / t + geo;
+  auto dEta = [](int i) { return (D == 3 && i == 2) ? 1.0 : 0.0; };
+
+  // ---- shear MRFs --------------------------------------------------------
+  double M0i[9] = {0}, F0i[3] = {0}, Mnab[3] = {0}, Fnab = 0.0;
+  double Mext[5][3] = {{0}}, Fext[5] = {0};
+  double ss = 0.0;   // pi^{mu nu} pi_{mu nu}
+  if (cfg.using_shear) {
+    const double cmd[4] = {1.0, -1.0, -1.0, -1.0 / t / t};
+    const double eta = k.eta, phi6 = k.phi6, phi7 = k.phi7, lpP = k.lambda_piPi;
+    const double tpp = k.tau_pipi, dpp = k.delta_pipi, tpi = k.tau_pi;
+    const double tdelta = dpp - tpi;
+    const double v[3] = {in.v[0], in.v[1], D == 3 ? in.v[2] : 0.0};
+    const double fu[3] = {u[0], u[1], u[2]};
+    const double fuc[3] = {-u[0], -u[1], -t2 * u[2]};
+    double pi[4][4], hy[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        pi[i][j] = P(i, j);
+        hy[i][j] = pi[i][j] * ((j == 1 || j == 2) ? -1.0 : (j == 3 ? -t2 : 1.0));   // pi^mu_nu
+      }
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+      for (int j = 0; j < 4; j++) ss += pi[i][j] * hy[i][j] * ((i == 1 || i == 2) ? -1.0 : (i == 3 ? -t2 : 1.0));
+    double gu[3][3] = {{0}}, gu0[3] = {0}, cgu[3][3] = {{0}};
+#pragma unroll
+    for (int i = 0; i < D; i++)
+#pragma unroll
+      for (int j = 0; j < D; j++) {
+        double acc = g * in.gradV[i * D + j];
+#pragma unroll
+        for (int kk = 0; kk < D; kk++) acc += -g * u[j] * uc[kk] * in.gradV[i * D + kk];
+        gu[i][j] = acc;
+      }
+#pragma unroll
+    for (int i = 0; i < D; i++) {
+      double acc = 0;
+#pragma unroll
+      for (int j = 0; j < D; j++) acc += gu[i][j] * uc[j];
+      gu0[i] = -1. * acc / g;
+#pragma unroll
+      for (int j = 0; j < D; j++) cgu[i][j] = gu[i][j] * ((D == 2 || i < D - 1) ? -1.0 : -1.0 / t2);
+    }
+    double gu0c[3] = {-gu0[0], -gu0[1], D == 3 ? -gu0[2] / t2 : 0.0};
+    double guv[3] = {0, 0, 0}, gu0v = 0.0;
+#pragma unroll
+    for (int j = 0; j < D; j++) {
+#pragma unroll
+      for (int kk = 0; kk < D; kk++) guv[j] += gu[kk][j] * v[kk];
+      gu0v += gu0[j] * v[j];
+    }
+    double vgs[3], ggs[3], sgu[3], vsg[3], sl0[3];
+    double sgu_s = 0.0;
+#pragma unroll
+    for (int i = 0; i < D; i++) {
+      double a1 = 0, a2 = 0, a3 = 0, a4 = 0, a5 = 0;
+#pragma unroll
+      for (int j = 0; j < D; j++) {
+        a1 += guv[j] * hy[i + 1][j + 1];
+        a2 += cgu[i][j] * hy[0][j + 1];
+        a3 += pi[j + 1][0] * gu[j][i] + pi[j + 1][i + 1] * gu0[j];
+        a4 += v[j] * pi[0][0] * gu[j][i] + v[j] * pi[0][i + 1] * gu0[j];
+        sgu_s += (hy[i + 1][j + 1] - v[i] * hy[0][j + 1]) * gu[i][j];
+      }
+      sgu_s += (hy[i + 1][0] - v[i] * hy[0][0]) * gu0[i];
+      vgs[i] = a1 + gu0v * hy[i + 1][0];
+      ggs[i] = a2 + cmd[i + 1] * gu0[i] * hy[0][0];
+      sgu[i] = a3;
+      vsg[i] = a4;
+#pragma unroll
+      for (int j = 0; j < 4; j++) a5 += (pi[0][j] * hy[i + 1][j] + pi[i + 1][j] * hy[0][j]) / 2.;
+      sl0[i] = a5;
+    }
+    // four-acceleration MRFs
+    const double uv = cfg.using_vorticity ? 1.0 : 0.0;
+#pragma unroll
+    for (int i = 0; i < D; i++) {
+      const double di = dEta(i);
+      double Fs = -(guv[i] - gu0c[i]) / 2. + u[i] * g * expn / 3. - g * geo * u[i] / 2.;
+      double FD = g * (u[i] * hy[0][0] + g * hy[i + 1][0]) * geo + t * uD * pi[3][i + 1] * di;
+      double Fds = -(vgs[i] - ggs[i] - 4. * g * u[i] * sgu_s / 3. - sgu[i] + vsg[i]) / 4. +
+                   (hy[i + 1][0] - g * g * hy[i + 1][0] - g * u[i] * hy[0][0] + pi[0][i + 1] +
+                    4. * u[i] * g * hy[0][0] / 3.) * geo / 4. +
+                   (g * cmd[i + 1] * hy[0][3] * di / t + g * pi[3][0] * di / t + 4. * g * u[i] * (g * hy[3][3] / t) / 3.) / 4. -
+                   pi[0][i + 1] * (g / t + geo + g * divV) / 3.;
+      double Fdo = -(vgs[i] - ggs[i] + sgu[i] - vsg[i]) / 4. +
+                   (hy[i + 1][0] - g * g * hy[i + 1][0] - g * u[i] * hy[0][0] - pi[0][i + 1]) * geo / 4. +
+                   (g * cmd[i + 1] * hy[0][3] * di / t - g * pi[3][0] * di / t) / 4.;
+      const double Fdd = pi[i + 1][0] * expn;
+      Fs += di * (-(-uD * t - uD / t + g * uD * uD * t + 2. * g * g * uD / t) / 2.);
+      FD += di * (uD * pi[0][0] / t + g * pi[3][0] / t);
+      if (D == 3) {
+        Fds += (t * uD * di * cmd[i + 1] * hy[0][0] + uD * hy[i + 1][3] * g / t / 4. + hy[i + 1][3] * t * uD +
+                pi[0][0] * di * uD / t + t * uD * uD * (g * hy[i + 1][0] + u[i] * hy[0][0]) +
+                2. * g * uD * (g * hy[i + 1][3] + u[i] * pi[0][3]) / t) / 4. +
+               g * u[i] * (hy[3][0] * uD * t + uD * hy[0][3] / t) / 3.;
+        Fdo += (t * uD * di * cmd[i + 1] * hy[0][0] + uD * hy[i + 1][3] * g / t - hy[3][i + 1] * t * uD -
+                pi[0][0] * di * uD / t + t * uD * uD * (g * hy[i + 1][0] + u[i] * hy[0][0]) +
+                2. * g * uD * (g * hy[i + 1][3] + u[i] * pi[0][3]) / t) / 4.;
+      }
+      F0i[i] = (-pi[i + 1][0] - tpi * FD - dpp * Fdd + 2. * tpi * Fdo * uv - tpp * Fds + (2. * eta + lpP * Pi) * Fs +
+                phi6 * Pi * pi[i + 1][0] + phi7 * (sl0[i] + g * u[i] * ss / 3.)) / (tpi * g);
+#pragma unroll
+      for (int j = 0; j < D; j++) {
+        double Ms = u[i] * uc[j] / (2. * 3.);
+        const double MD = g * u[i] * (hy[0][j + 1] - hy[0][0] * uc[j] / g) + g * g * (hy[i + 1][j + 1] - hy[i + 1][0] * uc[j] / g);
+        double Mds = (hy[i + 1][j + 1] - hy[i + 1][0] * uc[j] / g - g * g * hy[i + 1][j + 1] - g * u[i] * hy[0][j + 1] +
+                      uc[j] * g * hy[i + 1][0] + uc[j] * u[i] * hy[0][0] +
+                      4. * g * u[i] * (hy[0][j + 1] - hy[0][0] * uc[j] / g) / 3. +
+                      (-pi[0][i + 1] + 4. * pi[0][i + 1] / 3.) * uc[j] / g) / 4.;
+        double Mdo = (hy[i + 1][j + 1] - hy[i + 1][0] * uc[j] / g - g * g * hy[i + 1][j + 1] - g * u[i] * hy[0][j + 1] +
+                      uc[j] * g * hy[i + 1][0] + uc[j] * u[i] * hy[0][0] + pi[0][i + 1] * uc[j] / g) / 4.;
+        const double Mdd = -pi[i + 1][0] * uc[j] / g;
+        if (i == j) {
+          Ms += (1. - g * g) / 2.;
+          Mdo += -pi[0][0] / 4.;
+          Mds += +pi[0][0] / 4.;
+        }
+        M0i[i * D + j] = (-tpi * MD - dpp * Mdd + 2. * tpi * Mdo * uv - tpp * Mds + (2. * eta + lpP * Pi) * Ms) / (tpi * g);
+      }
+    }
+    // pi^{ij} nabla_i u_j MRF
+#pragma unroll
+    for (int i = 0; i < D; i++) {
+      Mnab[i] = hy[0][i + 1] - hy[0][0] * uc[i] / g;
+#pragma unroll
+      for (int j = 0; j < D; j++) Fnab += (hy[i + 1][j + 1] - v[i] * hy[0][j + 1]) * gu[i][j];
+      Fnab += (hy[i + 1][0] - v[i] * hy[0][0]) * gu0[i];
+    }
+    Fnab += +hy[3][3] * g / t + hy[0][0] * geo + (t * hy[3][0] + hy[0][3] / t) * uD * dEta(D - 1);
+    // shear-tensor evolution MRFs on the (i <= j) entries of the 2x3 block
+    const double f2 = fu[2];
+#pragma unroll
+    for (int i = 0; i < 2; i++) {
+#pragma unroll
+      for (int j = i; j < 3; j++) {
+        const int slot = (i == 0) ? j : 2 + j;   // (0,0)(0,1)(0,2)(1,1)(1,2) -> 0..4
+        const double di = dEta(i), dj = dEta(j);
+        double gugjs = 0, sigu = 0, vsig = 0, sml = 0;
+#pragma unroll
+        for (int kk = 0; kk < D; kk++) {
+          const double cg_i = (i < D) ? cgu[i][kk] : 0.0, cg_j = (j < D) ? cgu[j][kk] : 0.0;
+          const double g3_j = (kk < D && j < D) ? gu[kk][j] : 0.0, g3_i = (i < D) ? gu[kk][i] : 0.0;
+          gugjs += cg_i * hy[j + 1][kk + 1] + cg_j * hy[i + 1][kk + 1];
+          sigu += pi[kk + 1][i + 1] * g3_j + pi[kk + 1][j + 1] * g3_i;
+          vsig += v[kk] * pi[0][i + 1] * g3_j + v[kk] * pi[0][j + 1] * g3_i;
+        }
+#pragma unroll
+        for (int kk = 0; kk < 4; kk++) sml += (pi[i + 1][kk] * hy[j + 1][kk] + pi[j + 1][kk] * hy[i + 1][kk]) / 2.;
+        double FD2 = g * geo * (fu[i] * hy[j + 1][0] + fu[j] * hy[i + 1][0]);
+        const double cg_ij = (i < D && j < D) ? cgu[i][j] : 0.0, cg_ji = (i < D && j < D) ? cgu[j][i] : 0.0;
+        double Fsg = cg_ij / 2. + cg_ji / 2. + fu[i] * fu[j] * expn / 3.;
+        const double Fdl = pi[i + 1][j + 1] * expn;
+        const double common = t * f2 * (cmd[i + 1] * hy[j + 1][0] * di + cmd[j + 1] * hy[i + 1][0] * dj) +
+                              g * (cmd[i + 1] * hy[j + 1][3] * di + cmd[j + 1] * hy[i + 1][3] * dj) / t +
+                              f2 * f2 * t * (fu[i] * hy[j + 1][0] + fu[j] * hy[i + 1][0]) +
+                              2. * g * f2 * (fu[i] * hy[j + 1][3] + fu[j] * hy[i + 1][3]) / t;
+        const double cross = g * (pi[3][i + 1] * dj + pi[3][j + 1] * di) / t + f2 * (pi[0][i + 1] * dj + pi[0][j + 1] * di) / t;
+        const double Fdo2 = -(-gugjs + sigu - vsig) / 4. + (-fu[i] * g * hy[j + 1][0] - fu[j] * g * hy[i + 1][0]) * geo / 4. +
+                            (common - cross) / 4.;
+        double Fds2 = -(-gugjs - sigu + vsig - 4. * (fu[i] * fu[j]) * sgu_s / 3.) / 4. +
+                      (-fu[i] * g * hy[j + 1][0] - fu[j] * g * hy[i + 1][0] + 4. * fu[i] * fu[j] * hy[0][0] / 3.) * geo / 4. +
+                      (common + cross + 4. * fu[i] * fu[j] * (hy[3][0] * f2 * t + g * hy[3][3] / t + f2 * hy[0][3] / t) / 3.) / 4. -
+                      pi[i + 1][j + 1] * (g / t + geo + g * divV) / 3.;
+        if (j == 2) {
+          FD2 += g * pi[3][i + 1] / t + f2 * pi[0][i + 1] / t;
+          Fsg += -fu[i] * f2 * f2 * t / 2. - fu[i] * f2 * g / t;
+        }
+        if (i == j) {
+          Fsg += -cmd[i + 1] * expn / 3.;
+          Fds2 += -cmd[i + 1] * sgu_s / 3. - cmd[i + 1] * hy[0][0] * geo / 3. -
+                  cmd[i + 1] * (hy[3][0] * f2 * t + g * hy[3][3] / t + f2 * hy[0][3] / t) / 3.;
+        }
+        double F = (-pi[i + 1][j + 1] - tdelta * Fdl - tpi * FD2 + 2. * tpi * Fdo2 * uv - tpp * Fds2 +
+                    (2. * eta + lpP * Pi) * Fsg + phi6 * Pi * pi[i + 1][j + 1] + phi7 * (sml + fu[i] * fu[j] * ss / 3.)) /
+                   (sig * tpi * g);
+        if (i == j) F += phi7 * (-cmd[i + 1] * ss) / (3. * tpi * g * sig);
+        Fext[slot] = F;
+#pragma unroll
+        for (int kk = 0; kk < D; kk++) {
+          const double MD2 = g * (fu[i] * hy[j + 1][kk + 1] - fu[i] * hy[j + 1][0] * fuc[kk] / g + fu[j] * hy[i + 1][kk + 1] -
+                                  fu[j] * hy[i + 1][0] * fuc[kk] / g);
+          double Msg = -fu[i] * fu[j] * fuc[kk] / (3. * g);
+          const double Mdl = -pi[i + 1][j + 1] * fuc[kk] / g;
+          double Mdo2 = (-fu[i] * hy[j + 1][kk + 1] * g - fu[j] * hy[i + 1][kk + 1] * g + fuc[kk] * fu[i] * hy[j + 1][0] +
+                         fuc[kk] * fu[j] * hy[i + 1][0]) / 4.;
+          double Mds2 = (-fu[i] * hy[j + 1][kk + 1] * g - fu[j] * hy[i + 1][kk + 1] * g + fuc[kk] * fu[i] * hy[j + 1][0] +
+                         fuc[kk] * fu[j] * hy[i + 1][0] + 4. * fu[i] * fu[j] * (hy[0][kk + 1] - hy[0][0] * fuc[kk] / g) / 3. +
+                         4. * pi[i + 1][j + 1] * fuc[kk] / 3. / g) / 4.;
+          if (kk == i) {            // i = k terms
+            Mds2 += pi[0][j + 1] / 4.;
+            Mdo2 += -pi[0][j + 1] / 4.;
+            Msg += -g * fu[j] / 2.;
+          }
+          if (kk == j && j < D) {   // j = k terms
+            Msg += -g * fu[i] / 2.;
+            Mds2 += pi[0][i + 1] / 4.;
+            Mdo2 += -pi[0][i + 1] / 4.;
+          }
+          if (i == j) {             // i = j terms
+            Msg += cmd[i + 1] * fuc[kk] / (g * 3.);
+            Mds2 += -cmd[i + 1] * (hy[0][kk + 1] - hy[0][0] * fuc[kk] / g) / 3.;
+          }
+          Mext[slot][kk] = (-tpi * MD2 - tdelta * Mdl + 2. * tpi * Mdo2 * uv - tpp * Mds2 + (2. * eta + lpP * Pi) * Msg) /
+                           (sig * tpi * g);
+        }
+      }
+    }
+  }
+
+  // ---- auxiliary bulk and entropy MRFs (reference :229-362) ---------------
+  const double ztil = k.zeta + (k.delta_PiPi - k.tau_Pi) * Pi;
+  double Mb[3], Ms[3];
+#pragma unroll
+  for (int i = 0; i < D; i++) {
+    Mb[i] = (ztil * uc[i] / g) / (sig * g * k.tau_Pi);
+    Ms[i] = (Pi * uc[i] / g) / (sig * g * T);
+  }
+  double Fb = -(ztil * expn + Pi - k.phi1 * Pi * Pi) / (sig * g * k.tau_Pi);
+  double Fs = (-Pi * expn) / (sig * g * T);
+  if (cfg.using_shear) {
+    Fs += Fnab / (sig * g * T);
+    Fb += -(k.lambda_Pipi * Fnab - k.phi3 * ss) / (sig * g * k.tau_Pi);
+#pragma unroll
+    for (int i = 0; i < D; i++) {
+      Mb[i] += -k.lambda_Pipi * Mnab[i] / (sig * g * k.tau_Pi);
+      Ms[i] += Mnab[i] / (sig * g * T);
+    }
+  }
+  // ---- four-acceleration (reference :456-618); dN/dt = 0 without diffusion --
+  double gP[3], gB[3];
+#pragma unroll
+  for (int i = 0; i < D; i++) {
+    const double f = (D == 2 || i < D - 1) ? -1.0 : -1.0 / t2;   // make_contravariant
+    gP[i] = in.gradP[i] * f;
+    gB[i] = in.gradBulk[i] * f;
+  }
+  const double X = sden * dwds / g + (rho[0] * dwdr[0] + rho[1] * dwdr[1] + rho[2] * dwdr[2]) / g;
+  double Mw[3];
+#pragma unroll
+  for (int i = 0; i < D; i++) Mw[i] = X * uc[i] / g + sig * dwds * Ms[i];
+  const double Fw = -X * (geo + g / t + g * divV) + sig * dwds * Fs;
+  const double Fbulk = sig * Fb - Pi * (g * divV + g / t + geo) / g;
+  double Mu[9], Fu[3];
+#pragma unroll
+  for (int i = 0; i < D; i++) {
+#pragma unroll
+    for (int j = 0; j < D; j++) Mu[i * D + j] = u[i] * g * (Mb[j] + Mw[j]) - u[i] * uc[j] * (w + Pi) / g + M0i[i * D + j];
+    Mu[i * D + i] += g * (w + Pi);
+    Fu[i] = (gP[i] + gB[i]) - g * (Fw + Fbulk) * u[i] - (w + Pi) * expn * u[i] - 2. * (w + Pi) * g * uD * dEta(i) / t;
+    if (cfg.using_shear)
+      Fu[i] += -P(i + 1, 0) / t - 2. * dEta(i) * P(0, 3) / t - in.divshear[i] + in.gradshear[i] - F0i[i];
+  }
+  // du/dt = M^-1 F by cofactors (include/milne.hpp:788-834)
+  double du[3];
+  if (D == 2) {
+    const double det = Mu[0] * Mu[3] - Mu[1] * Mu[2];
+    du[0] = (Mu[3] / det) * Fu[0] + (-Mu[1] / det) * Fu[1];
+    du[1] = (-Mu[2] / det) * Fu[0] + (Mu[0] / det) * Fu[1];
+    du[2] = 0.0;
+  } else {
+#define A(i, j) Mu[(i) * 3 + (j)]
+    const double det = A(0, 0) * A(1, 1) * A(2, 2) + A(0, 1) * A(1, 2) * A(2, 0) + A(0, 2) * A(1, 0) * A(2, 1) -
+                       A(0, 2) * A(1, 1) * A(2, 0) - A(0, 1) * A(1, 0) * A(2, 2) - A(0, 0) * A(1, 2) * A(2, 1);
+    const double inv[9] = {(A(1, 1) * A(2, 2) - A(1, 2) * A(2, 1)) / det, (A(0, 2) * A(2, 1) - A(0, 1) * A(2, 2)) / det,
+                           (A(0, 1) * A(1, 2) - A(0, 2) * A(1, 1)) / det, (A(1, 2) * A(2, 0) - A(1, 0) * A(2, 2)) / det,
+                           (A(0, 0) * A(2, 2) - A(0, 2) * A(2, 0)) / det, (A(0, 2) * A(1, 0) - A(0, 0) * A(1, 2)) / det,
+                           (A(1, 0) * A(2, 1) - A(1, 1) * A(2, 0)) / det, (A(0, 1) * A(2, 0) - A(0, 0) * A(2, 1)) / det,
+                           (A(0, 0) * A(1, 1) - A(0, 1) * A(1, 0)) / det};
+#undef A
+#pragma unroll
+    for (int i = 0; i < 3; i++) du[i] = inv[i * 3 + 0] * Fu[0] + inv[i * 3 + 1] * Fu[1] + inv[i * 3 + 2] * Fu[2];
+  }
+  // ---- derivatives (reference :622-826) -------------------------------------
+  double m1 = 0, m2 = 0;
+#pragma unroll
+  for (int i = 0; i < D; i++) { m1 += Ms[i] * du[i]; m2 += Mb[i] * du[i]; o.du[i] = du[i]; }
+  o.dS = m1 + Fs;
+  o.dBulk = m2 + Fb;
+#pragma unroll
+  for (int sl = 0; sl < 5; sl++) {
+    double acc = 0.0;
+#pragma unroll
+    for (int kk = 0; kk < D; kk++) acc += Mext[sl][kk] * du[kk];
+    o.dShv[sl] = cfg.using_shear ? acc + Fext[sl] : 0.0;
+  }
+  // ---- dEz (reference :827-862) ---------------------------------------------
+  const double u3 = (D == 3) ? u[2] : 0.0;
+  o.dEz = ((th[T_E] + th[T_P] + Pi) * u3 * u3 + (th[T_P] + Pi) / t2 + P(3, 3)) * in.m * t2 / in.sigma_lab;
+}
+
+}  // namespace ccake

@@ -1,0 +1,159 @@
+/*
+ * ccake_gpu.h -- C ABI of the GB300-native CCAKE SPH hot path (libccake_gpu.so).
+ *
+ * One context holds one hydro event resident in the device memory of the
+ * current CUDA device: particle state, neighbour cell lists, EoS seeds.
+ * Plain C, no exceptions cross this boundary, every call returns a
+ * ccake_status_t. A context is used by one host thread at a time.
+ *
+ * The reference (the-nuclear-confectionery/CCAKE) exposes this path only as
+ * C++ templates; each entry below names the reference member function it
+ * replaces (paths are within the reference project).
+ *
+ * Units are the reference's internal units: positions fm (eta dimensionless),
+ * energy density fm^-4, entropy and charge densities fm^-3, T and mu fm^-1.
+ */
+#ifndef CCAKE_GPU_H
+#define CCAKE_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum ccake_status {
+  CCAKE_OK = 0,
+  CCAKE_ERR_INVALID = 1,        /* bad argument or unsupported configuration */
+  CCAKE_ERR_CUDA = 2,           /* a CUDA runtime call failed */
+  CCAKE_ERR_EOS = 3,            /* the EoS root finder found no solution (src/eos.cpp:790-801) */
+  CCAKE_ERR_NEG_ENTROPY = 4,    /* negative extensive entropy (src/evolver.cpp:437-450) */
+  CCAKE_ERR_CAPACITY = 5,       /* an output buffer is too small */
+  CCAKE_ERR_STATE = 6,          /* call out of order (e.g. step before initialize) */
+  CCAKE_ERR_NOMEM = 7,          /* device allocation failed */
+  CCAKE_ERR_NONFINITE = 8       /* a non-finite value appeared in the evolved state */
+} ccake_status_t;
+
+/* Run configuration: the subset of the reference Settings
+ * (include/settings.h:23-287) that the hot path reads. */
+typedef struct ccake_config {
+  int32_t dim;               /* spatial dimensions: 2 or 3 */
+  int32_t coord;             /* 0 Milne ("hyperbolic", EoM_default); Cartesian not supported */
+  int32_t eos_kind;          /* 0 conformal, 1 conformal_diagonal, 2 table */
+  int32_t using_shear;       /* include/settings.h:263-270 */
+  int32_t using_vorticity;
+  int32_t shear_relax_mode;  /* 0 default max(5 eta/w, 0.005), 1 "Gubser" 5 eta/w, 2 minVal */
+  int32_t zeta_mode;         /* 0 default 0.005 w/T, 1 constant, 2 cs2-dependent, 3 peaked */
+  int32_t factorized_kernel; /* D=3 W2D(r_perp)*W1D(deta) (src/kernel.cpp:130-170) */
+  int32_t input_as_entropy;  /* input column is s instead of e */
+  int32_t modulate_zeta_with_tanh;
+  int32_t thermo_mode;       /* 0 reference dw/ds chain (src/eos.cpp:276-344), 1 exact Hessian inverse */
+  int32_t precision;         /* 0 FP64 throughout; 1 FP32-compensated pair sums */
+  double hT, hEta, t0, dt;
+  double eos_c, eos_T0, eos_muB0, eos_muQ0, eos_muS0;
+  double eta_over_s, zeta_over_s, zeta_cs2_A, zeta_cs2_p;
+  double zeta_peak_T, zeta_peak_width;
+  double xmin, ymin, etamin;  /* lower corner of the IC grid (IC header, src/BSQHydro.cpp:241-249) */
+  double freeze_out_T;        /* fm^-1 */
+} ccake_config;
+
+/* Host struct-of-arrays particle input, the columns of the reference's
+ * "ccake" IC format (src/BSQHydro.cpp:206-330) already in internal units.
+ * eta/ueta may be NULL for dim = 2; rhoB/rhoS/rhoQ may be NULL (zero). */
+typedef struct ccake_particles_soa {
+  int64_t n;
+  const double *x, *y, *eta;
+  const double *e_or_s;
+  const double *rhoB, *rhoS, *rhoQ;
+  const double *ux, *uy, *ueta;
+} ccake_particles_soa;
+
+/* Conserved totals, src/system_state.cpp:738-885. */
+typedef struct ccake_totals {
+  double S, B, Sq, Q, E, Ez;
+} ccake_totals;
+
+typedef struct ccake_ctx ccake_ctx;
+
+/* Human-readable name of a status code. */
+const char* ccake_status_string(ccake_status_t s);
+
+/* Last error message of a context (never NULL). */
+const char* ccake_last_error(const ccake_ctx* ctx);
+
+/* Creates a context on the current CUDA device.
+ * Replaces BSQHydro<D,TEOM>::BSQHydro and SPHWorkstation::initialize
+ * (include/BSQHydro.h:48-54, src/sph_workstation.cpp:37-84). */
+ccake_status_t ccake_ctx_create(const ccake_config* cfg, ccake_ctx** out);
+ccake_status_t ccake_ctx_destroy(ccake_ctx* ctx);
+
+/* Copies host particles into device memory, reordered by neighbour cell.
+ * Replaces SPHWorkstation::process_initial_conditions and
+ * SystemState::allocate_cabana_particles (src/sph_workstation.cpp:1228-1340,
+ * src/system_state.cpp:57-326). */
+ccake_status_t ccake_load_particles(ccake_ctx* ctx, const ccake_particles_soa* host);
+
+/* e -> s inversion, initial sigma, extensive densities and initial smoothing.
+ * Replaces BSQHydro::initialize_hydrodynamics (src/BSQHydro.cpp:568-646). */
+ccake_status_t ccake_initialize(ccake_ctx* ctx);
+
+/* Step building blocks, each runnable alone on the current state for parity
+ * checks; together they are one derivative evaluation
+ * (SPHWorkstation::get_time_derivatives, src/sph_workstation.cpp:1509-1612). */
+/* SystemState::reset_neighbour_list (src/system_state.cpp:650-719) */
+ccake_status_t ccake_build_neighbours(ccake_ctx* ctx);
+/* SPHWorkstation::smooth_all_particle_fields (src/sph_workstation.cpp:494-578),
+ * preceded by TEOM::update_velocity (src/eom_default.cpp:17-38) */
+ccake_status_t ccake_smooth_fields(ccake_ctx* ctx);
+/* SPHWorkstation::update_all_particle_thermodynamics (src/sph_workstation.cpp:1713-1772)
+ * followed by TEOM::reset_pi_tensor (src/eom_default.cpp:56-172) */
+ccake_status_t ccake_update_thermo(ccake_ctx* ctx);
+/* SPHWorkstation::update_all_particle_viscosities (src/sph_workstation.cpp:1622-1699) */
+ccake_status_t ccake_update_viscosities(ccake_ctx* ctx);
+/* SPHWorkstation::smooth_all_particle_gradients (src/sph_workstation.cpp:796-986) */
+ccake_status_t ccake_smooth_gradients(ccake_ctx* ctx);
+/* TEOM::evaluate_time_derivatives (src/eom_default.cpp:211-869) */
+ccake_status_t ccake_time_derivatives(ccake_ctx* ctx);
+
+/* Advances n_steps midpoint-RK2 steps with the fused device path (graph
+ * captured). Replaces SPHWorkstation::advance_timestep ->
+ * Evolver::execute_timestep (src/sph_workstation.cpp:2042-2073,
+ * src/evolver.cpp:97-117, :344-517). */
+ccake_status_t ccake_step(ccake_ctx* ctx, int32_t n_steps);
+
+/* Current time tau (fm/c) and particle count. */
+ccake_status_t ccake_get_time(const ccake_ctx* ctx, double* t);
+ccake_status_t ccake_get_count(const ccake_ctx* ctx, int64_t* n);
+
+/* Conservation sums (src/system_state.cpp:738-885). */
+ccake_status_t ccake_conservation(ccake_ctx* ctx, ccake_totals* out);
+
+/* Copies one named per-particle field, in the caller's input order, to host
+ * memory (n doubles). Names: x y eta u0 u1 u2 v0.. ext_s ext_B ext_S ext_Q
+ * ext_bulk ext_shv0..4 Ez gamma sigma_lab sigma T muB muS muQ p s rhoB rhoS
+ * rhoQ e w cs2 dwds dwdB dwdS dwdQ bulk shvIJ (I,J in 0..3) gradP0.. gradE0..
+ * gradBulk0.. gradshear0.. divshear0.. gradV0..8 du_dt0.. d_ext_s d_ext_bulk
+ * d_ext_shv0..4 dEz eta_pi tau_pi zeta_Pi tau_Pi. */
+ccake_status_t ccake_copy_out(ccake_ctx* ctx, const char* field, double* host_out);
+/* Integer fields: btrack eos_id eos_iters freeze. */
+ccake_status_t ccake_copy_out_int(ccake_ctx* ctx, const char* field, int32_t* host_out);
+
+/* Neighbour list of the current positions in CSR form, input order, each row
+ * sorted by index (parity checks only). offsets has n+1 entries; returns
+ * CCAKE_ERR_CAPACITY with *count set when idx_cap is too small. */
+ccake_status_t ccake_get_neighbours(ccake_ctx* ctx, int32_t* offsets, int32_t* idx, int64_t idx_cap,
+                                    int64_t* count);
+
+/* Batch EoS inversion on host arrays: in4 rows (e|s, rhoB, rhoS, rhoQ);
+ * tbqs rows (T, muB, muQ, muS) hold the seeds on entry and the solution on
+ * exit; th16 rows receive T muB muS muQ p s rhoB rhoS rhoQ e w cs2 dwds dwdB
+ * dwdS dwdQ (may be NULL); status = EoS chain index used or -1.
+ * Replaces EquationOfState::update_s / s_out (src/eos.cpp:574-975). */
+ccake_status_t ccake_eos_invert_batch(ccake_ctx* ctx, int32_t entropy_mode, int64_t n, const double* in4,
+                                      double* tbqs, double* th16, int32_t* status, int32_t* iters);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CCAKE_GPU_H */

@@ -1,0 +1,163 @@
+"""CUDA path against the CPU oracle, through the C ABI.
+
+Tolerances: neighbour sets bit-exact; fields within 1e-10 relative per
+comparison (the spec FP64 bar), measured as |gpu - oracle| /
+(|oracle| + 1e-6 * max|oracle|) so that fields crossing zero are judged
+against their own scale.
+"""
+import dataclasses
+
+import numpy as np
+import pytest
+
+from ccake_gb300 import api, ics
+import oracle_py as O
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-10
+
+
+def relerr(a, b):
+    scale = np.abs(b) + 1e-6 * np.max(np.abs(b)) + 1e-300
+    return float(np.max(np.abs(a - b) / scale))
+
+
+def cases():
+    g, grc = ics.gubser_2d(n_side=40)
+    h, hrc = ics.hotspots_2d(n_side=48, n_hot=6, seed=7)
+    return {"gubser": (g, grc), "hotspots": (h, hrc)}
+
+
+def pair(name):
+    p, rc = cases()[name]
+    gpu = api.GpuHydro(rc)
+    gpu.load(p)
+    orc = O.OracleRun(p, rc)
+    return p, rc, gpu, orc
+
+
+def csr_rows(off, idx):
+    return [tuple(idx[off[i]:off[i + 1]]) for i in range(len(off) - 1)]
+
+
+@pytest.mark.parametrize("name", ["gubser", "hotspots"])
+def test_neighbour_sets_bit_exact(name):
+    p, rc, gpu, orc = pair(name)
+    go, gi = gpu.neighbours()
+    oo, oi = orc.neighbours()
+    assert np.array_equal(go, oo)
+    assert csr_rows(go, gi) == csr_rows(oo, oi)
+    # 2h pairs of the lattice are included (4 per interior particle)
+    assert np.median(np.diff(go)) == 48
+
+
+@pytest.mark.parametrize("name", ["gubser", "hotspots"])
+def test_initialize_parity(name):
+    p, rc, gpu, orc = pair(name)
+    gpu.initialize()
+    assert orc.initialize() == 0
+    for f in ("sigma_lab", "sigma", "gamma", "T", "muB", "muQ", "p", "e", "s", "w", "dwds", "dwdB",
+              "ext_s", "ext_B", "ext_Q", "rhoB"):
+        assert relerr(gpu.get(f), orc.get(f)) < RTOL, f
+
+
+@pytest.mark.parametrize("name", ["gubser", "hotspots"])
+def test_derivative_parity(name):
+    p, rc, gpu, orc = pair(name)
+    gpu.initialize()
+    orc.initialize()
+    gpu.step(2)
+    orc.step(2)
+    gpu.phase("time_derivatives")
+    orc.phase("derivatives")
+    fields = ["gradP0", "gradP1", "gradE0", "gradE1", "gradBulk0", "gradV0", "gradV1", "gradV2", "gradV3",
+              "du_dt0", "du_dt1", "d_ext_s", "dEz"]
+    if rc.using_shear:
+        fields += ["gradshear0", "gradshear1", "divshear0", "divshear1", "d_ext_shv0", "d_ext_shv1",
+                   "d_ext_shv3", "d_ext_bulk"]
+    for f in fields:
+        assert relerr(gpu.get(f), orc.get(f)) < RTOL, f
+
+
+@pytest.mark.parametrize("name", ["gubser", "hotspots"])
+def test_ten_steps_parity(name):
+    p, rc, gpu, orc = pair(name)
+    gpu.initialize()
+    orc.initialize()
+    gpu.step(10)
+    assert orc.step(10) == 0
+    assert abs(gpu.t - orc.t) < 1e-14
+    fields = ["x", "y", "u0", "u1", "ext_s", "ext_B", "T", "e", "p", "sigma_lab", "Ez"]
+    if rc.using_shear:
+        fields += ["ext_shv0", "ext_shv1", "ext_shv3", "shv00", "shv11"]
+    for f in fields:
+        assert relerr(gpu.get(f), orc.get(f)) < RTOL, f
+    tg, to = gpu.totals(), orc.totals()
+    for k in ("S", "B", "Q", "E", "Ez"):
+        assert abs(tg[k] - to[k]) <= 1e-10 * (abs(to[k]) + 1e-30), k
+
+
+def test_neighbours_after_motion_bit_exact():
+    p, rc, gpu, orc = pair("gubser")
+    gpu.initialize()
+    gpu.step(5)
+    # feed the GPU positions to the oracle: identical inputs, identical sets
+    orc.set("x", gpu.get("x"))
+    orc.set("y", gpu.get("y"))
+    go, gi = gpu.neighbours()
+    oo, oi = orc.neighbours()
+    assert csr_rows(go, gi) == csr_rows(oo, oi)
+
+
+def test_runs_are_bitwise_reproducible():
+    p, rc = cases()["hotspots"]
+    outs = []
+    for _ in range(2):
+        g = api.GpuHydro(rc)
+        g.load(p)
+        g.initialize()
+        g.step(3)
+        outs.append(np.concatenate([g.get("u0"), g.get("ext_shv0"), g.get("T")]))
+    assert np.array_equal(outs[0], outs[1])
+
+
+@pytest.mark.parametrize("eos_kind,entropy,thermo_mode", [(0, 1, 0), (0, 0, 0), (1, 1, 1), (1, 0, 1)])
+def test_eos_batch_inversion_parity(eos_kind, entropy, thermo_mode):
+    import ctypes
+    rng = np.random.default_rng(11)
+    n = 2000
+    T = rng.uniform(0.3, 2.5, n)
+    mu = rng.uniform(-0.4, 0.4, (n, 3))
+    mu[: n // 4] = 0.0                       # zero-charge rows take the decoupled path
+    rc = ics.RunConfig(eos_kind=eos_kind, thermo_mode=thermo_mode)
+    cfg = O.make_config(rc)
+    tgt = np.zeros((n, 4))
+    for i in range(n):
+        x = np.array([T[i], *mu[i]])
+        o = np.zeros(17)
+        O.lib().orc_eos_full_thermo(ctypes.byref(cfg), None, 0, O._dp(x), O._dp(o))
+        tgt[i] = [o[1] if entropy else o[5], o[2], o[3], o[4]]
+    seeds = np.tile([580 / 197.3269804, 0, 0, 0], (n, 1))
+    xo, tho, sto, _ = O.eos_invert_batch(rc, entropy, tgt, seeds=seeds)
+    gpu = api.GpuHydro(rc)
+    xg, thg, stg, _ = gpu.eos_invert(entropy, tgt, seeds)
+    assert np.array_equal(stg, sto)
+    assert relerr(xg[:, 0], xo[:, 0]) < 1e-12
+    assert np.max(np.abs(xg[:, 1:] - xo[:, 1:])) < 1e-12
+    for c in (4, 5, 9, 10, 12):
+        assert relerr(thg[:, c], tho[:, c]) < 1e-11, c
+
+
+def test_gubser_flow_matches_analytic_on_gpu():
+    p, rc = ics.gubser_2d(n_side=200)
+    gpu = api.GpuHydro(rc)
+    gpu.load(p)
+    gpu.initialize()
+    gpu.step(100)
+    x, y, T = gpu.get("x"), gpu.get("y"), gpu.get("T")
+    r = np.sqrt(x * x + y * y)
+    m = r < 2.0
+    Ta = ics.gubser_temperature(gpu.t, r)
+    assert abs(gpu.t - 1.1) < 1e-12
+    assert np.max(np.abs(T[m] / Ta[m] - 1)) < 5e-3
