@@ -1,0 +1,310 @@
+"""Benchmark of the SPH hot path: particle-steps/s on the viscous 2+1-D BSQ event.
+
+Workload (one GPU): 400 x 400 = 160,000 particles, dx = 0.05 fm, h = 0.1 fm,
+30 Gaussian hot spots (seeded), conformal-diagonal EoS with B and Q charge,
+eta/s = 0.08 with tau_pi = 5 eta/w, midpoint RK2 at dt = 0.001 fm/c, plain
+FP64. One "step" is one RK2 step (two derivative evaluations) of every
+particle. Synthetic data generated in memory.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+N > 1 runs under torchrun: every rank advances its own independent event
+(replicas; the path has no cross-event exchange), the slowest rank's time is
+reported and value counts the particles of all ranks.
+
+--impl reference times the reference algorithm on the host cores: the
+reference itself (Kokkos/Cabana/GSL/HDF5/yaml-cpp) cannot be built here, so
+its CPU restatement in oracle/ (C++17/OpenMP, all host threads) is timed.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s (plain FP64, viscous BSQ 2+1-D hot-spot event)"
+UNIT = "particle-steps/s"
+
+
+def workload(n_side=400):
+    from ccake_gb300 import ics
+    return ics.hotspots_2d(n_side=n_side)
+
+
+def config_dict(n, extra=None):
+    d = {"workload": "viscous 2+1-D BSQ, 30 hot spots, 400x400 lattice (160k particles), dx=0.05 fm, h=0.1 fm, "
+                     "conformal-diagonal EoS, eta/s=0.08, RK2 dt=0.001 fm/c",
+         "particles_per_gpu": n, "precision": "fp64",
+         "l2": "resident event state larger than the 129 MB L2 (no flush)"}
+    if extra:
+        d.update(extra)
+    return d
+
+
+# -- clocks during the timed region ----------------------------------------------------------
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self, gpu_index=0):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                if int(f[0]) != gpu_index:
+                    continue
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+def fp64_peak_tflops():
+    """FP64 DGEMM throughput of this GPU (torch/cuBLAS, 8192^3), the FP64 pipe ceiling."""
+    import torch
+    n = 8192
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 1e30
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    del a, b
+    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+
+
+def read_traffic(kernel):
+    """DRAM bytes per launch from the committed ncu summary, or None."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        parts = line.split()
+        if len(parts) >= 2 and parts[0] == kernel:
+            try:
+                return float(parts[1])
+            except ValueError:
+                return None
+    return None
+
+
+# -- the reference arm ---------------------------------------------------------------------------
+def cpu_reference(p, rc, steps, warmup=1):
+    """Times the oracle (CPU restatement of the reference) with all host threads."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_py as O
+    O.build()
+    r = O.OracleRun(p, rc)
+    r.initialize()
+    if warmup:
+        r.step(warmup)
+    t0 = time.perf_counter()
+    r.step(steps)
+    dt = time.perf_counter() - t0
+    return p.n * steps / dt, dt
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    p, rc = workload()
+    steps = max(1, min(args.steps, args.ref_steps))
+    value, dt = cpu_reference(p, rc, steps, warmup=min(args.warmup, 1))
+    cores = os.cpu_count()
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": config_dict(p.n, {"host": "cpu"}),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{steps} of the event's RK2 steps, all {p.n} particles, OMP threads={cores}"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "the reference's Kokkos/Cabana build needs dependencies absent here; its CPU restatement "
+                    "(oracle/, same algorithms) is timed"}
+    print(json.dumps(line))
+
+
+# -- our arm ---------------------------------------------------------------------------------
+def run_ours(args, world, rank):
+    import torch
+    from ccake_gb300 import api, build
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    build.build()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    p, rc = workload()
+    n = p.n
+    gpu = api.GpuHydro(rc)
+    gpu.load(p)
+    gpu.initialize()
+    for _ in range(args.warmup):
+        gpu.step(1)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = ClockSampler()
+    if rank == 0:
+        clocks.start()
+        time.sleep(0.3)
+    ms = gpu.step_timed(args.steps)
+    torch.cuda.synchronize()
+    clk = clocks.stop(local) if rank == 0 else None
+    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+    if dist:
+        dist.barrier()
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t.item())
+    value = world * n * args.steps / (ms_max * 1e-3)
+    # per-kernel device times (events on the library's stream), kernel by kernel
+    prof = gpu.profile_phases(max(2, min(10, args.steps)))
+    # end to end through the C ABI with host buffers (upload, initialise, K steps, download)
+    e2e = run_e2e(p, rc, args.steps)
+    if dist:
+        dist.destroy_process_group()
+    if rank != 0:
+        return
+    hbm_peak, peak_kind = measured_peaks()
+    # algorithmic bytes per particle (FP64 scalars x 8): pass B reads positions,
+    # velocity, p, e, sigma_lab, Pi, pi (3), thermo (14), state (12), step cache (12)
+    # and writes the state (12): 60 scalars; pass A 28; cell kernels 3.
+    alg = {"cells": 3 * 8 * n, "passA": 28 * 8 * n, "passB": 60 * 8 * n}
+    names = ["cells", "passA", "passB"]
+    dom = int(np.argmax(prof))
+    kname = names[dom]
+    achieved = alg[kname] / (prof[dom] * 1e-3) / 1e9
+    fp64 = None
+    try:
+        fp64 = fp64_peak_tflops()
+    except Exception:
+        pass
+    # FP64 operations per particle per launch counted from the kernels' arithmetic (48 neighbours):
+    # pass A ~ 48 x 22 + EoS/thermo ~ 1.4k; pass B ~ 48 x 40 + EoM ~ 3.4k
+    flops = {"cells": 0.0, "passA": (48 * 22 + 1400) * n, "passB": (48 * 40 + 3400) * n}
+    fp64_ach = flops[kname] / (prof[dom] * 1e-3) / 1e12
+    traffic = read_traffic(kname)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": config_dict(n, {"parallelism": f"replicas{world}", "device_bytes": gpu.device_bytes()}),
+        "clocks": clk,
+        "gpu_launches": 14 * args.steps,
+        "e2e": e2e,
+        "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "peak_kind": peak_kind,
+                     "traffic": traffic,
+                     "algorithmic_bytes_per_launch": alg[kname], "avg_launch_ms": prof[dom],
+                     "phase_ms": dict(zip(names, [float(x) for x in prof])),
+                     "fp64": {"achieved_tflops": fp64_ach, "peak_tflops": fp64,
+                              "frac": (fp64_ach / fp64) if fp64 else None,
+                              "peak_kind": "measured DGEMM on this GPU (torch/cuBLAS 8192^3)"}},
+    }
+    if not args.no_cpu:
+        ref_steps = max(1, args.ref_steps)
+        cv, cdt = cpu_reference(p, rc, ref_steps, warmup=0)
+        line["cpu_baseline"] = {"value": cv, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                                "sample": f"{ref_steps} RK2 steps of the same 160k-particle event on the host "
+                                          f"(oracle/, OpenMP, {os.cpu_count()} threads)"}
+    print(json.dumps(line))
+
+
+def run_e2e(p, rc, steps):
+    """Same metric through the C ABI with host buffers: load (H2D), initialise,
+    K steps, copy the evolved state back (D2H), all inside the timed region."""
+    from ccake_gb300 import api
+    out_fields = ["x", "y", "u0", "u1", "ext_s", "ext_bulk", "ext_shv0", "ext_shv1", "ext_shv3", "T", "e"]
+    t0 = time.perf_counter()
+    g = api.GpuHydro(rc)
+    g.load(p)
+    g.initialize()
+    g.step(steps)
+    outs = [g.get(f) for f in out_fields]
+    dt = time.perf_counter() - t0
+    g.close()
+    n = p.n
+    h2d = 10 * 8 * n
+    d2h = sum(o.nbytes for o in outs)
+    return {"value": n * steps / dt, "unit": UNIT, "h2d_bytes_per_step": h2d / steps,
+            "d2h_bytes_per_step": d2h / steps, "wall_s": dt,
+            "what": "ccake_load_particles + ccake_initialize + ccake_step(K) + ccake_copy_out of 11 fields"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--ref-steps", type=int, default=4, help="RK2 steps timed on the CPU")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank)
+
+
+if __name__ == "__main__":
+    main()

@@ -75,6 +75,9 @@ def lib():
                      "ccake_update_viscosities", "ccake_smooth_gradients", "ccake_time_derivatives"):
             getattr(L, name).argtypes = [P]
         L.ccake_step.argtypes = [P, _i32]
+        L.ccake_step_timed.argtypes = [P, _i32, ctypes.POINTER(ctypes.c_float)]
+        L.ccake_profile_phases.argtypes = [P, _i32, _dp]
+        L.ccake_device_bytes.argtypes = [P, ctypes.POINTER(_i64)]
         L.ccake_get_time.argtypes = [P, _dp]
         L.ccake_get_count.argtypes = [P, ctypes.POINTER(_i64)]
         L.ccake_conservation.argtypes = [P, ctypes.POINTER(Totals)]
@@ -144,6 +147,23 @@ class GpuHydro:
 
     def step(self, n=1):
         self._check(lib().ccake_step(self.h, int(n)), "step")
+
+    def step_timed(self, n):
+        """Advances n steps; returns the device time (ms) measured on the library's stream."""
+        ms = ctypes.c_float()
+        self._check(lib().ccake_step_timed(self.h, int(n), ctypes.byref(ms)), "step_timed")
+        return float(ms.value)
+
+    def profile_phases(self, n):
+        """Average device ms per launch: (cell-list kernels, pass A, pass B)."""
+        out = np.zeros(3)
+        self._check(lib().ccake_profile_phases(self.h, int(n), _d(out)), "profile_phases")
+        return out
+
+    def device_bytes(self):
+        v = ctypes.c_int64()
+        self._check(lib().ccake_device_bytes(self.h, ctypes.byref(v)), "device_bytes")
+        return int(v.value)
 
     def phase(self, name):
         self._check(getattr(lib(), "ccake_" + name)(self.h), name)

@@ -341,6 +341,74 @@ ccake_status_t ccake_step(ccake_ctx* ctx, int32_t n_steps) {
   return s;
 }
 
+ccake_status_t ccake_step_timed(ccake_ctx* ctx, int32_t n_steps, float* device_ms) {
+  if (!ctx || n_steps < 0 || !device_ms) return CCAKE_ERR_INVALID;
+  if (!ctx->initialized) return fail(ctx, CCAKE_ERR_STATE, "initialize first");
+  ccake_status_t s = ccake_step(ctx, 0);   // builds the graph, clears errors
+  if (s) return s;
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  CK(cudaEventRecord(e0, ctx->stream));
+  for (int k = 0; k < n_steps; k++) CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
+  CK(cudaEventRecord(e1, ctx->stream));
+  CK(cudaEventSynchronize(e1));
+  CK(cudaEventElapsedTime(device_ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  s = check_errors(ctx);
+  Clock c;
+  CK(cudaMemcpy(&c, ctx->p.clock, sizeof(Clock), cudaMemcpyDeviceToHost));
+  ctx->t = c.t;
+  return s;
+}
+
+ccake_status_t ccake_profile_phases(ccake_ctx* ctx, int32_t n_steps, double* ms3) {
+  if (!ctx || n_steps <= 0 || !ms3) return CCAKE_ERR_INVALID;
+  if (!ctx->initialized) return fail(ctx, CCAKE_ERR_STATE, "initialize first");
+  ccake_status_t s = reset_errors(ctx);
+  if (s) return s;
+  cudaEvent_t ev[4];
+  for (int q = 0; q < 4; q++) CK(cudaEventCreate(&ev[q]));
+  double acc[3] = {0, 0, 0};
+  const double dt = ctx->cfg.dt;
+  for (int k = 0; k < n_steps; k++) {
+    for (int sub = 1; sub <= 2; sub++) {
+      CK(cudaEventRecord(ev[0], ctx->stream));
+      launch_build_cells(ctx->rc, ctx->p, ctx->stream);
+      CK(cudaEventRecord(ev[1], ctx->stream));
+      launch_passA(ctx->rc, ctx->eos, ctx->p, A_WITH_THERMO, ctx->stream);
+      CK(cudaEventRecord(ev[2], ctx->stream));
+      launch_passB(ctx->rc, ctx->p, B_EOM | B_UPDATE | (sub == 2 ? B_WRITE_Y0 : 0), sub == 1 ? 0.5 * dt : dt,
+                   ctx->stream);
+      CK(cudaEventRecord(ev[3], ctx->stream));
+      launch_clock(ctx->p, sub, dt, ctx->stream);
+      CK(cudaEventSynchronize(ev[3]));
+      float m;
+      for (int q = 0; q < 3; q++) {
+        CK(cudaEventElapsedTime(&m, ev[q], ev[q + 1]));
+        acc[q] += m;
+      }
+    }
+  }
+  for (int q = 0; q < 4; q++) cudaEventDestroy(ev[q]);
+  for (int q = 0; q < 3; q++) ms3[q] = acc[q] / (2.0 * n_steps);
+  s = check_errors(ctx);
+  Clock c;
+  CK(cudaMemcpy(&c, ctx->p.clock, sizeof(Clock), cudaMemcpyDeviceToHost));
+  ctx->t = c.t;
+  return s;
+}
+
+ccake_status_t ccake_device_bytes(const ccake_ctx* ctx, int64_t* bytes) {
+  if (!ctx || !bytes) return CCAKE_ERR_INVALID;
+  const int64_t n = ctx->n;
+  const int64_t nd = n * (2 * NY + 1 + NTH + 1 + 3 + 1 + 1 + 1 + NPI + RA + RB + NGRAD + NDER + 1 + 1 + 3);
+  const int64_t ni = n * 7 + (int64_t)ctx->rc.grid.ncell * 2;
+  *bytes = nd * 8 + ni * 4;
+  return CCAKE_OK;
+}
+
 ccake_status_t ccake_build_neighbours(ccake_ctx* ctx) {
   if (!ctx) return CCAKE_ERR_INVALID;
   if (!ctx->loaded) return fail(ctx, CCAKE_ERR_STATE, "load particles first");

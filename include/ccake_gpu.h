@@ -121,6 +121,21 @@ ccake_status_t ccake_time_derivatives(ccake_ctx* ctx);
  * src/evolver.cpp:97-117, :344-517). */
 ccake_status_t ccake_step(ccake_ctx* ctx, int32_t n_steps);
 
+/* ccake_step with its device time: CUDA events recorded on the context's
+ * stream around the n_steps graph launches (milliseconds in *device_ms).
+ * Measurement entry point; no reference counterpart. */
+ccake_status_t ccake_step_timed(ccake_ctx* ctx, int32_t n_steps, float* device_ms);
+
+/* Runs n_steps RK2 steps kernel by kernel (no graph) with CUDA events between
+ * the launches and returns the average device time per launch, in ms, of:
+ * ms[0] the four cell-list kernels together, ms[1] the smoothing+EoS pass,
+ * ms[2] the gradient+EoM+RK2 pass. Measurement entry point; no reference
+ * counterpart (the reference's phase timers are src/sph_workstation.cpp:1543-1583). */
+ccake_status_t ccake_profile_phases(ccake_ctx* ctx, int32_t n_steps, double* ms3);
+
+/* Bytes of device memory the context holds. */
+ccake_status_t ccake_device_bytes(const ccake_ctx* ctx, int64_t* bytes);
+
 /* Current time tau (fm/c) and particle count. */
 ccake_status_t ccake_get_time(const ccake_ctx* ctx, double* t);
 ccake_status_t ccake_get_count(const ccake_ctx* ctx, int64_t* n);
