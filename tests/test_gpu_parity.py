@@ -18,9 +18,15 @@ pytestmark = pytest.mark.gpu
 RTOL = 1e-10
 
 
-def relerr(a, b):
-    scale = np.abs(b) + 1e-6 * np.max(np.abs(b)) + 1e-300
+def relerr(a, b, floor=1e-6):
+    scale = np.abs(b) + floor * np.max(np.abs(b)) + 1e-300
     return float(np.max(np.abs(a - b) / scale))
+
+
+# Gradients are sums whose terms cancel (sum_b m_b grad W ~ 0 on a lattice);
+# they are compared against 1e-4 of their own range, where their rounding
+# (~1e-16 of the summands) is visible.
+GRAD_FLOOR = 1e-4
 
 
 def cases():
@@ -96,7 +102,7 @@ def test_derivative_parity(name):
         fields += ["gradshear0", "gradshear1", "divshear0", "divshear1", "d_ext_shv0", "d_ext_shv1",
                    "d_ext_shv3", "d_ext_bulk"]
     for f in fields:
-        assert relerr(gpu.get(f), orc.get(f)) < RTOL, f
+        assert relerr(gpu.get(f), orc.get(f), GRAD_FLOOR) < RTOL, f
 
 
 @pytest.mark.parametrize("name", ["gubser", "hotspots"])
