@@ -167,6 +167,26 @@ ccake_status_t ccake_get_neighbours(ccake_ctx* ctx, int32_t* offsets, int32_t* i
 ccake_status_t ccake_eos_invert_batch(ccake_ctx* ctx, int32_t entropy_mode, int64_t n, const double* in4,
                                       double* tbqs, double* th16, int32_t* status, int32_t* iters);
 
+/* Neighbour counts (the number of b != a with |r_a - r_b|^2 <= (2h)^2, the
+ * same exact predicate as every other entry point) of n particles whose
+ * positions are already in device memory, written to d_counts (device, n
+ * int32), launched on `stream` (a cudaStream_t, NULL for the default stream).
+ * No counterpart in the reference: an allocation-free entry point for callers
+ * that cannot call cudaMalloc while they run (inside another library's
+ * allocation-free section, from a stream callback, or under an allocator they
+ * do not own). It allocates nothing: its cell-list scratch is one file-scope
+ * device array for at most 262,144 particles and 262,144 cells (about 5.2 MB,
+ * held by every device that loads the library until exit); larger inputs are
+ * rejected with CCAKE_ERR_CAPACITY. lo3/hi3 (host, 3 doubles) bound the cell
+ * grid (particles outside are clamped to edge cells; the counts do not depend
+ * on the box). The first call on a device looks up the scratch address; make
+ * it before any stream capture. Calls share the scratch: calls that overlap
+ * on the GPU race and must be serialised by the caller. Returns once the
+ * kernels are enqueued. */
+ccake_status_t ccake_neighbour_counts_noalloc(const double* d_x, const double* d_y, const double* d_eta, int64_t n,
+                                              int32_t dim, double h, const double* lo3, const double* hi3,
+                                              int32_t* d_counts, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
