@@ -46,11 +46,24 @@ ccake_status_t fail(ccake_ctx* c, ccake_status_t s, const std::string& msg) {
     if (e_ != cudaSuccess) return fail(ctx, CCAKE_ERR_CUDA, std::string(#call ": ") + cudaGetErrorString(e_)); \
   } while (0)
 
-void free_buffers(ccake_ctx* ctx) {
+void drop_graph(ccake_ctx* ctx) {
   if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
   if (ctx->graph) cudaGraphDestroy(ctx->graph);
   ctx->graph_exec = nullptr;
   ctx->graph = nullptr;
+}
+
+void free_lists(ccake_ctx* ctx) {
+  if (ctx->p.nbr_idx) cudaFree(ctx->p.nbr_idx);
+  if (ctx->p.nbr_f) cudaFree(ctx->p.nbr_f);
+  ctx->p.nbr_idx = nullptr;
+  ctx->p.nbr_f = nullptr;
+  ctx->p.K = 0;
+}
+
+void free_buffers(ccake_ctx* ctx) {
+  drop_graph(ctx);
+  free_lists(ctx);
   if (ctx->dbuf) cudaFree(ctx->dbuf);
   if (ctx->ibuf) cudaFree(ctx->ibuf);
   ctx->dbuf = nullptr;
@@ -95,6 +108,9 @@ ccake_status_t check_errors(ccake_ctx* ctx) {
   if (e[E_EOS]) return fail(ctx, CCAKE_ERR_EOS, std::to_string(e[E_EOS]) + " particles without an EoS solution");
   if (e[E_NEGS]) return fail(ctx, CCAKE_ERR_NEG_ENTROPY, std::to_string(e[E_NEGS]) + " particles with negative entropy");
   if (e[E_NONFINITE]) return fail(ctx, CCAKE_ERR_NONFINITE, std::to_string(e[E_NONFINITE]) + " non-finite particles");
+  if (e[E_NBR_OVERFLOW])
+    return fail(ctx, CCAKE_ERR_CAPACITY, std::to_string(e[E_NBR_OVERFLOW]) + " particles exceed the neighbour-list capacity " +
+                                             std::to_string(ctx->p.K) + " (re-initialise to resize)");
   return CCAKE_OK;
 }
 
@@ -216,7 +232,7 @@ ccake_status_t ccake_ctx_create(const ccake_config* cfg, ccake_ctx** out) {
   EosDev& e = ctx->eos;
   e.kind = cfg->eos_kind;
   e.thermo_mode = cfg->thermo_mode;
-  e.own = {cfg->eos_c, cfg->eos_T0, cfg->eos_muB0, cfg->eos_muQ0, cfg->eos_muS0};
+  e.own = make_scales(cfg->eos_c, cfg->eos_T0, cfg->eos_muB0, cfg->eos_muQ0, cfg->eos_muS0);
   e.conf = e.cdiag = e.own;
   double x4[4] = {cfg->freeze_out_T, 0, 0, 0}, o[17];
   model_thermo(e, chain_model(e.kind, 0), x4, o);
@@ -254,7 +270,7 @@ ccake_status_t ccake_load_particles(ccake_ctx* ctx, const ccake_particles_soa* h
   std::iota(ctx->perm.begin(), ctx->perm.end(), 0);
   std::stable_sort(ctx->perm.begin(), ctx->perm.end(), [&](int32_t a, int32_t b) { return key[a] < key[b]; });
   // device memory: one double slab, one int slab
-  const size_t nd = (size_t)n * (2 * NY + 1 + NTH + 1 + 3 + 1 + 1 + 1 + NPI + RA + RB + NGRAD + NDER + 1 + 1 + 3) +
+  const size_t nd = (size_t)n * (2 + 2 * NY + 1 + NTH + 1 + 3 + 1 + 1 + 1 + NPI + RA + RB + NGRAD + NDER + 1 + 1 + 3) +
                     (size_t)kTotBlocks * 6 + 8;
   const size_t ni = (size_t)n * 7 + (size_t)g.ncell * 2 + 1 + NERR + 8;
   if (cudaMalloc(&ctx->dbuf, nd * sizeof(double)) != cudaSuccess) return fail(ctx, CCAKE_ERR_NOMEM, "device allocation");
@@ -268,6 +284,7 @@ ccake_status_t ccake_load_particles(ccake_ctx* ctx, const ccake_particles_soa* h
   // the records come first: their slabs are multiples of 64 bytes, so the
   // 16-byte vector loads stay aligned for any n
   p.recA = take(RA); p.recB = take(RB);
+  p.posf = reinterpret_cast<float4*>(take(2));
   p.y = take(NY); p.y0 = take(NY); p.m = take(1); p.th = take(NTH); p.gam = take(1); p.v = take(3);
   p.slab = take(1); p.sig = take(1); p.bulk = take(1); p.pi = take(NPI);
   p.grads = take(NGRAD); p.derivs = take(NDER); p.in_e = take(1); p.in_s = take(1); p.in_rho = take(3);
@@ -306,6 +323,25 @@ ccake_status_t ccake_initialize(ccake_ctx* ctx) {
   CK(cudaMemcpyAsync(ctx->p.clock, &c, sizeof(Clock), cudaMemcpyHostToDevice, ctx->stream));
   ccake_status_t s = reset_errors(ctx);
   if (s) return s;
+  // neighbour-list capacity: 1.5x the largest initial neighbour count + 16
+  // (pass A flags an overflow, reported as CCAKE_ERR_CAPACITY)
+  {
+    launch_build_cells(ctx->rc, ctx->p, ctx->stream);
+    launch_neighbour_counts(ctx->rc, ctx->p, ctx->p.btrack, ctx->stream);
+    std::vector<int32_t> cnt((size_t)ctx->n);
+    CK(cudaMemcpyAsync(cnt.data(), ctx->p.btrack, ctx->n * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    const int mx = *std::max_element(cnt.begin(), cnt.end());
+    const int K = ((mx * 3 / 2 + 16) + 15) / 16 * 16;
+    if (K != ctx->p.K) {
+      drop_graph(ctx);
+      free_lists(ctx);
+      if (cudaMalloc(&ctx->p.nbr_idx, (size_t)K * ctx->n * sizeof(int32_t)) != cudaSuccess ||
+          cudaMalloc(&ctx->p.nbr_f, (size_t)K * ctx->n * sizeof(double)) != cudaSuccess)
+        return fail(ctx, CCAKE_ERR_NOMEM, "neighbour list allocation");
+      ctx->p.K = K;
+    }
+  }
   launch_init_state(ctx->rc, ctx->p, ctx->stream);
   launch_init_invert(ctx->rc, ctx->eos, ctx->p, ctx->stream);
   launch_build_cells(ctx->rc, ctx->p, ctx->stream);
@@ -403,9 +439,9 @@ ccake_status_t ccake_profile_phases(ccake_ctx* ctx, int32_t n_steps, double* ms3
 ccake_status_t ccake_device_bytes(const ccake_ctx* ctx, int64_t* bytes) {
   if (!ctx || !bytes) return CCAKE_ERR_INVALID;
   const int64_t n = ctx->n;
-  const int64_t nd = n * (2 * NY + 1 + NTH + 1 + 3 + 1 + 1 + 1 + NPI + RA + RB + NGRAD + NDER + 1 + 1 + 3);
+  const int64_t nd = n * (2 + 2 * NY + 1 + NTH + 1 + 3 + 1 + 1 + 1 + NPI + RA + RB + NGRAD + NDER + 1 + 1 + 3);
   const int64_t ni = n * 7 + (int64_t)ctx->rc.grid.ncell * 2;
-  *bytes = nd * 8 + ni * 4;
+  *bytes = nd * 8 + ni * 4 + (int64_t)ctx->p.K * n * 12;
   return CCAKE_OK;
 }
 

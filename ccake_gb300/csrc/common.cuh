@@ -79,7 +79,7 @@ struct Clock {
 };
 
 // Error counters raised by the kernels (read back by the host after a call).
-enum ErrSlot : int { E_EOS = 0, E_NEGS = 1, E_NONFINITE = 2, NERR = 4 };
+enum ErrSlot : int { E_EOS = 0, E_NEGS = 1, E_NONFINITE = 2, E_NBR_OVERFLOW = 3, NERR = 4 };
 
 // Kernel normalisations of the reference, src/kernel.cpp:11-26.
 __host__ __device__ inline double knorm(int D) { return D == 1 ? 2. / 3. : D == 2 ? 10. / (7 * M_PI) : 1. / M_PI; }

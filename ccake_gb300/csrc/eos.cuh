@@ -7,7 +7,15 @@
 
 namespace ccake {
 
-struct Scales { double c, T0, muB0, muQ0, muS0; };
+// Model scales with their reciprocals (the FP64 pipe is the bottleneck, so
+// the models multiply by 1/T0 instead of dividing by T0).
+struct Scales {
+  double c, T0, muB0, muQ0, muS0;
+  double iT0, iB0, iQ0, iS0;
+};
+__host__ __device__ inline Scales make_scales(double c, double T0, double muB0, double muQ0, double muS0) {
+  return Scales{c, T0, muB0, muQ0, muS0, 1.0 / T0, 1.0 / muB0, 1.0 / muQ0, 1.0 / muS0};
+}
 
 // Tabulated EoS in device memory: uniform (T, muB, muQ, muS) grid, muS
 // fastest, 17 fields per node (p s B S Q e cs2 chiBB chiQQ chiSS chiBQ chiBS
@@ -46,7 +54,7 @@ __host__ __device__ inline Scales model_scales(const EosDev& e, int model) {
 // p = c T0^4 x^2, x = (T/T0)^2 + sum (mu/mu0)^2 (reference include/eos_conformal.h:33-194).
 __host__ __device__ inline void conformal_thermo(const Scales& k, const double* x4, double* o) {
   const double T = x4[0], mB = x4[1], mQ = x4[2], mS = x4[3];
-  const double iT = 1.0 / k.T0, iB = 1.0 / k.muB0, iQ = 1.0 / k.muQ0, iS = 1.0 / k.muS0;
+  const double iT = k.iT0, iB = k.iB0, iQ = k.iQ0, iS = k.iS0;
   const double iT2 = iT * iT, iB2 = iB * iB, iQ2 = iQ * iQ, iS2 = iS * iS;
   const double x = T * T * iT2 + mB * mB * iB2 + mS * mS * iS2 + mQ * mQ * iQ2;
   const double cp = k.c * k.T0 * k.T0 * k.T0 * k.T0;
@@ -75,20 +83,20 @@ __host__ __device__ inline void conformal_thermo(const Scales& k, const double* 
 __host__ __device__ inline void confdiag_thermo(const Scales& k, const double* x4, double* o) {
   const double T = x4[0], mB = x4[1], mQ = x4[2], mS = x4[3];
   const double cp = k.c * k.T0 * k.T0 * k.T0 * k.T0;
-  const double rT = T / k.T0, rB = mB / k.muB0, rQ = mQ / k.muQ0, rS = mS / k.muS0;
+  const double rT = T * k.iT0, rB = mB * k.iB0, rQ = mQ * k.iQ0, rS = mS * k.iS0;
   const double p = cp * (rT * rT * rT * rT + rB * rB * rB * rB + rS * rS * rS * rS + rQ * rQ * rQ * rQ);
-  const double s = 4.0 * cp * rT * rT * rT / k.T0;
-  const double B = 4.0 * cp * rB * rB * rB / k.muB0;
-  const double S = 4.0 * cp * rS * rS * rS / k.muS0;
-  const double Q = 4.0 * cp * rQ * rQ * rQ / k.muQ0;
+  const double s = 4.0 * cp * rT * rT * rT * k.iT0;
+  const double B = 4.0 * cp * rB * rB * rB * k.iB0;
+  const double S = 4.0 * cp * rS * rS * rS * k.iS0;
+  const double Q = 4.0 * cp * rQ * rQ * rQ * k.iQ0;
   o[0] = p; o[1] = s; o[2] = B; o[3] = S; o[4] = Q;
   o[5] = (s * T + mB * B + mQ * Q + mS * S) - p;
   o[6] = 1.0 / 3.0;
-  o[7] = 12.0 * cp * rB * rB / (k.muB0 * k.muB0);
-  o[8] = 12.0 * cp * rQ * rQ / (k.muQ0 * k.muQ0);
-  o[9] = 12.0 * cp * rS * rS / (k.muS0 * k.muS0);
+  o[7] = 12.0 * cp * rB * rB * (k.iB0 * k.iB0);
+  o[8] = 12.0 * cp * rQ * rQ * (k.iQ0 * k.iQ0);
+  o[9] = 12.0 * cp * rS * rS * (k.iS0 * k.iS0);
   for (int i = 10; i < 16; i++) o[i] = kTiny;
-  o[16] = 12.0 * cp * rT * rT / (k.T0 * k.T0);
+  o[16] = 12.0 * cp * rT * rT * (k.iT0 * k.iT0);
 }
 
 // Multilinear lookup with the reference's index rule (src/interpolatorND.cpp:250-317):
@@ -201,16 +209,29 @@ __host__ __device__ inline void solve4(double A[4][4], double* b, double* x) {
 // halving; leaving the model box fails.
 __host__ __device__ inline bool newton_attempt(const EosDev& e, int model, int entropy, const double* tgt,
                                                const double* lo, const double* hi, double* x, int* iters) {
+  // f, J at the current x are carried over from the accepted trial point of
+  // the previous iteration (the same values a fresh evaluation would give),
+  // so an undamped iteration costs one density/Jacobian evaluation.
   int extra = -1;
+  double f[4], J[4][4];
+  bool have = false;
+  const bool diag = (model == M_CDIAG);
   for (int it = 0; it < 100; it++) {
-    double f[4], J[4][4];
-    dens_jac(e, model, entropy, x, f, J);
+    if (!have) dens_jac(e, model, entropy, x, f, J);
+    have = false;
     double F[4], fres = 0.0;
     for (int i = 0; i < 4; i++) { F[i] = f[i] - tgt[i]; fres = fres > fabs(F[i]) ? fres : fabs(F[i]); }
     if (!(fres == fres)) return false;
     if (extra < 0 && fres < 1e-10) extra = 0;
-    double rhs[4] = {-F[0], -F[1], -F[2], -F[3]}, dx[4];
-    solve4(J, rhs, dx);
+    double dx[4];
+    if (diag) {
+      // the conformal-diagonal Jacobian is diagonal: the 4x4 elimination
+      // reduces to these divisions (a zero pivot leaves its unknown unchanged)
+      for (int i = 0; i < 4; i++) dx[i] = (J[i][i] == 0.0) ? 0.0 : (-F[i]) / J[i][i];
+    } else {
+      double rhs[4] = {-F[0], -F[1], -F[2], -F[3]};
+      solve4(J, rhs, dx);
+    }
     if (extra >= 0) {
       double y[4], rel = 0.0;
       for (int i = 0; i < 4; i++) {
@@ -227,15 +248,14 @@ __host__ __device__ inline bool newton_attempt(const EosDev& e, int model, int e
     for (int h = 0; h < 7; h++) {
       for (int i = 0; i < 4; i++) y[i] = x[i] + lam * dx[i];
       if (y[0] > 0) {
-        double fy[4], Jy[4][4];
-        dens_jac(e, model, entropy, y, fy, Jy);
+        dens_jac(e, model, entropy, y, f, J);
         double gmax = 0.0;
-        for (int i = 0; i < 4; i++) { const double r = fabs(fy[i] - tgt[i]); gmax = gmax > r ? gmax : r; }
-        if (gmax <= fres || h == 6) break;
+        for (int i = 0; i < 4; i++) { const double r = fabs(f[i] - tgt[i]); gmax = gmax > r ? gmax : r; }
+        if (gmax <= fres || h == 6) { have = true; break; }
       }
       lam *= 0.5;
     }
-    if (!(y[0] > 0)) y[0] = 0.5 * x[0];
+    if (!(y[0] > 0)) { y[0] = 0.5 * x[0]; have = false; }
     for (int i = 0; i < 4; i++) x[i] = y[i];
     for (int i = 0; i < 4; i++)
       if (!(x[i] >= lo[i] && x[i] <= hi[i])) return false;
@@ -453,8 +473,8 @@ __host__ __device__ inline void set_thermo(const EosDev& e, int k, const double*
       int p = col;
       for (int r = col + 1; r < m; r++) if (fabs(A[r][col]) > fabs(A[p][col])) p = r;
       if (p != col) for (int j = 0; j < 2 * m; j++) { double t = A[col][j]; A[col][j] = A[p][j]; A[p][j] = t; }
-      const double piv = A[col][col];
-      for (int j = 0; j < 2 * m; j++) A[col][j] /= piv;
+      const double ipiv = 1.0 / A[col][col];
+      for (int j = 0; j < 2 * m; j++) A[col][j] *= ipiv;
       for (int r = 0; r < m; r++) {
         if (r == col || A[r][col] == 0.0) continue;
         const double f = A[r][col];

@@ -113,6 +113,48 @@ __device__ __forceinline__ void for_candidates(const RunConst& rc, const Ptrs& p
     }
 }
 
+// Iterates the 3^D neighbour cells of particle a and calls f(b, d, d2) for
+// every b != a with d2 = |r_a - r_b|^2 <= (2h)^2 (exact FP64 predicate).
+// Candidates are first screened in FP32 from the float copies of the
+// positions: a candidate is skipped only when its FP32 squared distance
+// exceeds (2h)^2 by more than a bound on the FP32 error (per axis
+// 2^-22 (|x_a| + |x_b| + |dx|) before squaring, 4e-7 relative after), so the
+// exact predicate sees every pair that can be a neighbour and the set is the
+// FP64 one. GB300's FP64 pipe is the bottleneck; this keeps the ~2/3 of the
+// candidates that are rejected off it.
+template <int D, class F>
+__device__ __forceinline__ void for_neighbours(const RunConst& rc, const Ptrs& p, int a, const double* xa, F&& f) {
+  const Grid& g = rc.grid;
+  const float4 pa = p.posf[a];
+  const float cut2f = (float)rc.cut2 * 1.000001f;
+  const int cx = cell_coord(g, 0, xa[0]), cy = cell_coord(g, 1, xa[1]);
+  const int cz = (D == 3) ? cell_coord(g, 2, xa[2]) : 0;
+  const int zlo = (D == 3) ? max(cz - 1, 0) : 0, zhi = (D == 3) ? min(cz + 1, g.nc[2] - 1) : 0;
+  const double2* ra = reinterpret_cast<const double2*>(p.recA);
+  for (int z = zlo; z <= zhi; z++)
+    for (int y = max(cy - 1, 0); y <= min(cy + 1, g.nc[1] - 1); y++) {
+      const int row = (z * g.nc[1] + y) * g.nc[0];
+      const int jb = p.cell_start[row + max(cx - 1, 0)], je = p.cell_start[row + min(cx + 1, g.nc[0] - 1) + 1];
+      for (int j = jb; j < je; j++) {
+        const int b = p.cell_idx[j];
+        if (b == a) continue;
+        const float4 pb = __ldg(&p.posf[b]);
+        const float dxf = pa.x - pb.x, dyf = pa.y - pb.y, dzf = (D == 3) ? pa.z - pb.z : 0.0f;
+        const float ex = 2.4e-7f * (fabsf(pa.x) + fabsf(pb.x) + fabsf(dxf)) + 1e-30f;
+        const float ey = 2.4e-7f * (fabsf(pa.y) + fabsf(pb.y) + fabsf(dyf)) + 1e-30f;
+        const float ez = (D == 3) ? 2.4e-7f * (fabsf(pa.z) + fabsf(pb.z) + fabsf(dzf)) + 1e-30f : 0.0f;
+        const float d2f = dxf * dxf + dyf * dyf + dzf * dzf;
+        const float bound = ex * (2.0f * fabsf(dxf) + ex) + ey * (2.0f * fabsf(dyf) + ey) +
+                            ez * (2.0f * fabsf(dzf) + ez) + 4e-7f * d2f;
+        if (d2f - bound > cut2f) continue;
+        const double2 b01 = __ldg(&ra[(size_t)b * 4 + 0]), b23 = __ldg(&ra[(size_t)b * 4 + 1]);
+        double d[3] = {xa[0] - b01.x, xa[1] - b01.y, (D == 3) ? xa[2] - b23.x : 0.0};
+        const double d2 = dist2_exact<D>(d);
+        if (d2 <= rc.cut2) f(b, d, d2, b23.y);
+      }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // pass A
 // ---------------------------------------------------------------------------
@@ -182,30 +224,32 @@ __global__ void __launch_bounds__(kBlock) k_passA(RunConst rc, EosDev eos, Ptrs 
   const double k0 = rc.k0;
   double sl = a23.y * k0, s0 = a45.x * k0, s1 = a45.y * k0, s2 = a67.x * k0, s3 = a67.y * k0;
   int nn = 0;
-  const bool charges = true;
-  for_candidates<D>(rc, p, i, xa, [&](int b) {
-    const double2 b01 = __ldg(&ra[(size_t)b * 4 + 0]), b23 = __ldg(&ra[(size_t)b * 4 + 1]);
-    double d[3] = {xa[0] - b01.x, xa[1] - b01.y, xa[2] - b23.x};
-    const double d2 = dist2_exact<D>(d);
-    if (d2 <= rc.cut2) {
-      nn++;
-      const double r = sqrt(d2);
-      const double q = r * rc.inv_h;
-      double W;
-      if (q >= 2.0) W = 0.0;
-      else if (q >= 1.0) { const double z = 2.0 - q; W = rc.wn2 * z * z * z; }
-      else W = rc.wn * (1.0 - 1.5 * q * q + 0.75 * q * q * q);
-      const double2 b45 = __ldg(&ra[(size_t)b * 4 + 2]);
-      sl += b23.y * W;
-      s0 += b45.x * W;
-      if (charges) {
-        const double2 b67 = __ldg(&ra[(size_t)b * 4 + 3]);
-        s1 += b45.y * W;
-        s2 += b67.x * W;
-        s3 += b67.y * W;
-      }
+  const int K = p.K;
+  for_neighbours<D>(rc, p, i, xa, [&](int b, const double* d, double d2, double mb) {
+    // W (src/kernel.cpp:34-48) and the radial factor of grad W (:95-118):
+    // grad_a W = f * (r_a - r_b), f = kgrad/h^(D+1) (2-q)^2 / r for 1 <= q < 2,
+    // kgrad2/h^(D+1) (1.5 q - 2) / h for q < 1. One rsqrt gives r and 1/r.
+    const double rs = d2 > 0.0 ? rsqrt(d2) : 0.0;
+    const double r = d2 * rs;
+    const double q = r * rc.inv_h;
+    double W, fg;
+    if (q >= 2.0) { W = 0.0; fg = 0.0; }
+    else if (q >= 1.0) { const double z = 2.0 - q; W = rc.wn2 * z * z * z; fg = rc.gn * rs * z * z; }
+    else { W = rc.wn * (1.0 - 1.5 * q * q + 0.75 * q * q * q); fg = rc.gn2 * (1.5 * q - 2) * rc.inv_h; }
+    if (nn < K) {
+      p.nbr_idx[(size_t)nn * n + i] = b;
+      p.nbr_f[(size_t)nn * n + i] = fg;
     }
+    nn++;
+    const double2 b45 = __ldg(&ra[(size_t)b * 4 + 2]);
+    const double2 b67 = __ldg(&ra[(size_t)b * 4 + 3]);
+    sl += mb * W;
+    s0 += b45.x * W;
+    s1 += b45.y * W;
+    s2 += b67.x * W;
+    s3 += b67.y * W;
   });
+  if (nn > K) atomicAdd(&p.err[E_NBR_OVERFLOW], 1);
   // gamma and v from u (update_velocity), LRF densities (get_LRF = lab/(gamma t))
   const double u3[3] = {p.y[Y_U0 * n + i], p.y[Y_U1 * n + i], D == 3 ? p.y[Y_U2 * n + i] : 0.0};
   const double g = gamma_milne<D>(u3, t * t);
@@ -249,21 +293,18 @@ __global__ void __launch_bounds__(kBlock) k_passB(RunConst rc, Ptrs p, int mode,
 #pragma unroll
     for (int l = 0; l < D; l++) SV[k][l] = S0[k][l] = 0.0;
   }
-  for_candidates<D>(rc, p, i, xa, [&](int b) {
+  // the neighbours and grad-W factors pass A listed for this substep
+  const int cnt = min(p.btrack[i], p.K);
+  for (int kk = 0; kk < cnt; kk++) {
+    const int b = p.nbr_idx[(size_t)kk * n + i];
+    const double fg = p.nbr_f[(size_t)kk * n + i];
     const double* rb = p.recB + (size_t)b * RB;
     const double2 b01 = __ldg(reinterpret_cast<const double2*>(rb));
     const double2 b23 = __ldg(reinterpret_cast<const double2*>(rb + 2));
     double d[3] = {xa[0] - b01.x, xa[1] - b01.y, xa[2] - b23.x};
-    const double d2 = dist2_exact<D>(d);
-    if (d2 <= rc.cut2) {
-      // grad_a W(r_a - r_b), reference src/kernel.cpp:95-118
-      const double r = sqrt(d2);
-      const double q = r * rc.inv_h;
-      double f;
-      if (q >= 2.0) f = 0.0;
-      else if (q >= 1.0) { const double z = 2.0 - q; f = (rc.gn / r) * z * z; }
-      else f = rc.gn2 * (1.5 * q - 2) * rc.inv_h;
-      const double mf = b23.y * f;   // m_b * (grad W)/rel
+    {
+      // grad_a W(r_a - r_b) = fg * d, reference src/kernel.cpp:95-118
+      const double mf = b23.y * fg;   // m_b * (grad W)/rel
       double gm[D];
 #pragma unroll
       for (int k = 0; k < D; k++) gm[k] = mf * d[k];
@@ -302,7 +343,7 @@ __global__ void __launch_bounds__(kBlock) k_passB(RunConst rc, Ptrs p, int mode,
         }
       }
     }
-  });
+  }
   // own values
   const double sla = p.slab[i];
   const double ea = rbA[B_E], Pa = rbA[B_P], Pia = rbA[B_PI];
@@ -421,6 +462,7 @@ __global__ void __launch_bounds__(kBlock) k_passB(RunConst rc, Ptrs p, int mode,
   const double m = p.m[i];
   double2* ra = reinterpret_cast<double2*>(p.recA) + (size_t)i * 4;
   ra[0] = make_double2(ynew[Y_X0], ynew[Y_X1]);
+  p.posf[i] = make_float4((float)ynew[Y_X0], (float)ynew[Y_X1], D == 3 ? (float)ynew[Y_X2] : 0.0f, 0.0f);
   ra[1] = make_double2(D == 3 ? ynew[Y_X2] : 0.0, m);
   ra[2] = make_double2(m * ynew[Y_ES], m * ynew[Y_EB]);
   ra[3] = make_double2(m * ynew[Y_ESS], m * ynew[Y_EQ]);
@@ -469,6 +511,8 @@ __global__ void k_init_state(RunConst rc, Ptrs p) {
   double2* ra = reinterpret_cast<double2*>(p.recA) + (size_t)i * 4;
   ra[0] = make_double2(p.y[Y_X0 * n + i], p.y[Y_X1 * n + i]);
   ra[1] = make_double2(D == 3 ? p.y[Y_X2 * n + i] : 0.0, 1.0);
+  p.posf[i] = make_float4((float)p.y[Y_X0 * n + i], (float)p.y[Y_X1 * n + i],
+                          D == 3 ? (float)p.y[Y_X2 * n + i] : 0.0f, 0.0f);
   ra[2] = make_double2(1.0, 1.0);
   ra[3] = make_double2(1.0, 1.0);
 }

@@ -37,6 +37,12 @@ struct Ptrs {
   int32_t* err;          // NERR
   Clock* clock;
   double* partials;      // reduction scratch
+  // per-substep neighbour list written by pass A, read by pass B (k-major:
+  // entry k of particle i at k * n + i); nbr_f is the radial factor of grad W
+  float4* posf;          // FP32 copy of the positions (candidate prefilter)
+  int32_t* nbr_idx;      // K * n
+  double* nbr_f;         // K * n
+  int K;                 // list capacity per particle
 };
 
 // Pass A modes

@@ -100,6 +100,10 @@ template <int D>
 __device__ inline void eom(const ccake_config& cfg, const Transport& k, const EomIn<D>& in, double t, EomOut& o) {
   const double t2 = t * t;
   const double g = in.g, sig = in.sigma;
+  // reciprocals: FP64 division is a long instruction sequence on the scarce
+  // FP64 pipe, so each divisor is inverted once
+  const double ig = 1.0 / g, it = 1.0 / t, it2 = 1.0 / t2;
+  const double k13 = 1.0 / 3.0, k16 = 1.0 / 6.0;
   const double* th = in.th;
   const double T = th[T_T], w = th[T_W], sden = th[T_S], dwds = th[T_DWDS];
   const double rho[3] = {th[T_RB], th[T_RS], th[T_RQ]};
@@ -113,8 +117,8 @@ __device__ inline void eom(const ccake_config& cfg, const Transport& k, const Eo
 #pragma unroll
   for (int i = 0; i < D; i++) divV += in.gradV[i * D + i];
   const double uD = u[D - 1];
-  const double geo = (D == 3) ? uD * uD * t / g : 0.0;
-  const double expn = g * divV + g / t + geo;
+  const double geo = (D == 3) ? uD * uD * t * ig : 0.0;
+  const double expn = g * divV + g * it + geo;
   auto dEta = [](int i) { return (D == 3 && i == 2) ? 1.0 : 0.0; };
 
   // ---- shear MRFs --------------------------------------------------------
@@ -122,10 +126,11 @@ __device__ inline void eom(const ccake_config& cfg, const Transport& k, const Eo
   double Mext[5][3] = {{0}}, Fext[5] = {0};
   double ss = 0.0;   // pi^{mu nu} pi_{mu nu}
   if (cfg.using_shear) {
-    const double cmd[4] = {1.0, -1.0, -1.0, -1.0 / t / t};
+    const double cmd[4] = {1.0, -1.0, -1.0, -1.0 * it * it};
     const double eta = k.eta, phi6 = k.phi6, phi7 = k.phi7, lpP = k.lambda_piPi;
     const double tpp = k.tau_pipi, dpp = k.delta_pipi, tpi = k.tau_pi;
     const double tdelta = dpp - tpi;
+    const double itg = 1.0 / (tpi * g), istg = 1.0 / (sig * tpi * g);
     const double v[3] = {in.v[0], in.v[1], D == 3 ? in.v[2] : 0.0};
     const double fu[3] = {u[0], u[1], u[2]};
     const double fuc[3] = {-u[0], -u[1], -t2 * u[2]};
@@ -156,11 +161,11 @@ __device__ inline void eom(const ccake_config& cfg, const Transport& k, const Eo
       double acc = 0;
 #pragma unroll
       for (int j = 0; j < D; j++) acc += gu[i][j] * uc[j];
-      gu0[i] = -1. * acc / g;
+      gu0[i] = -1. * acc * ig;
 #pragma unroll
-      for (int j = 0; j < D; j++) cgu[i][j] = gu[i][j] * ((D == 2 || i < D - 1) ? -1.0 : -1.0 / t2);
+      for (int j = 0; j < D; j++) cgu[i][j] = gu[i][j] * ((D == 2 || i < D - 1) ? -1.0 : -1.0 * it2);
     }
-    double gu0c[3] = {-gu0[0], -gu0[1], D == 3 ? -gu0[2] / t2 : 0.0};
+    double gu0c[3] = {-gu0[0], -gu0[1], D == 3 ? -gu0[2] * it2 : 0.0};
     double guv[3] = {0, 0, 0}, gu0v = 0.0;
 #pragma unroll
     for (int j = 0; j < D; j++) {
@@ -195,58 +200,58 @@ __device__ inline void eom(const ccake_config& cfg, const Transport& k, const Eo
 #pragma unroll
     for (int i = 0; i < D; i++) {
       const double di = dEta(i);
-      double Fs = -(guv[i] - gu0c[i]) / 2. + u[i] * g * expn / 3. - g * geo * u[i] / 2.;
+      double Fs = -(guv[i] - gu0c[i]) / 2. + u[i] * g * expn * k13 - g * geo * u[i] / 2.;
       double FD = g * (u[i] * hy[0][0] + g * hy[i + 1][0]) * geo + t * uD * pi[3][i + 1] * di;
-      double Fds = -(vgs[i] - ggs[i] - 4. * g * u[i] * sgu_s / 3. - sgu[i] + vsg[i]) / 4. +
+      double Fds = -(vgs[i] - ggs[i] - 4. * g * u[i] * sgu_s * k13 - sgu[i] + vsg[i]) / 4. +
                    (hy[i + 1][0] - g * g * hy[i + 1][0] - g * u[i] * hy[0][0] + pi[0][i + 1] +
-                    4. * u[i] * g * hy[0][0] / 3.) * geo / 4. +
-                   (g * cmd[i + 1] * hy[0][3] * di / t + g * pi[3][0] * di / t + 4. * g * u[i] * (g * hy[3][3] / t) / 3.) / 4. -
-                   pi[0][i + 1] * (g / t + geo + g * divV) / 3.;
+                    4. * u[i] * g * hy[0][0] * k13) * geo / 4. +
+                   (g * cmd[i + 1] * hy[0][3] * di * it + g * pi[3][0] * di * it + 4. * g * u[i] * (g * hy[3][3] * it) * k13) / 4. -
+                   pi[0][i + 1] * (g * it + geo + g * divV) * k13;
       double Fdo = -(vgs[i] - ggs[i] + sgu[i] - vsg[i]) / 4. +
                    (hy[i + 1][0] - g * g * hy[i + 1][0] - g * u[i] * hy[0][0] - pi[0][i + 1]) * geo / 4. +
-                   (g * cmd[i + 1] * hy[0][3] * di / t - g * pi[3][0] * di / t) / 4.;
+                   (g * cmd[i + 1] * hy[0][3] * di * it - g * pi[3][0] * di * it) / 4.;
       const double Fdd = pi[i + 1][0] * expn;
-      Fs += di * (-(-uD * t - uD / t + g * uD * uD * t + 2. * g * g * uD / t) / 2.);
-      FD += di * (uD * pi[0][0] / t + g * pi[3][0] / t);
+      Fs += di * (-(-uD * t - uD * it + g * uD * uD * t + 2. * g * g * uD * it) / 2.);
+      FD += di * (uD * pi[0][0] * it + g * pi[3][0] * it);
       if (D == 3) {
-        Fds += (t * uD * di * cmd[i + 1] * hy[0][0] + uD * hy[i + 1][3] * g / t / 4. + hy[i + 1][3] * t * uD +
-                pi[0][0] * di * uD / t + t * uD * uD * (g * hy[i + 1][0] + u[i] * hy[0][0]) +
-                2. * g * uD * (g * hy[i + 1][3] + u[i] * pi[0][3]) / t) / 4. +
-               g * u[i] * (hy[3][0] * uD * t + uD * hy[0][3] / t) / 3.;
-        Fdo += (t * uD * di * cmd[i + 1] * hy[0][0] + uD * hy[i + 1][3] * g / t - hy[3][i + 1] * t * uD -
-                pi[0][0] * di * uD / t + t * uD * uD * (g * hy[i + 1][0] + u[i] * hy[0][0]) +
-                2. * g * uD * (g * hy[i + 1][3] + u[i] * pi[0][3]) / t) / 4.;
+        Fds += (t * uD * di * cmd[i + 1] * hy[0][0] + uD * hy[i + 1][3] * g * it / 4. + hy[i + 1][3] * t * uD +
+                pi[0][0] * di * uD * it + t * uD * uD * (g * hy[i + 1][0] + u[i] * hy[0][0]) +
+                2. * g * uD * (g * hy[i + 1][3] + u[i] * pi[0][3]) * it) / 4. +
+               g * u[i] * (hy[3][0] * uD * t + uD * hy[0][3] * it) * k13;
+        Fdo += (t * uD * di * cmd[i + 1] * hy[0][0] + uD * hy[i + 1][3] * g * it - hy[3][i + 1] * t * uD -
+                pi[0][0] * di * uD * it + t * uD * uD * (g * hy[i + 1][0] + u[i] * hy[0][0]) +
+                2. * g * uD * (g * hy[i + 1][3] + u[i] * pi[0][3]) * it) / 4.;
       }
       F0i[i] = (-pi[i + 1][0] - tpi * FD - dpp * Fdd + 2. * tpi * Fdo * uv - tpp * Fds + (2. * eta + lpP * Pi) * Fs +
-                phi6 * Pi * pi[i + 1][0] + phi7 * (sl0[i] + g * u[i] * ss / 3.)) / (tpi * g);
+                phi6 * Pi * pi[i + 1][0] + phi7 * (sl0[i] + g * u[i] * ss * k13)) * itg;
 #pragma unroll
       for (int j = 0; j < D; j++) {
-        double Ms = u[i] * uc[j] / (2. * 3.);
-        const double MD = g * u[i] * (hy[0][j + 1] - hy[0][0] * uc[j] / g) + g * g * (hy[i + 1][j + 1] - hy[i + 1][0] * uc[j] / g);
-        double Mds = (hy[i + 1][j + 1] - hy[i + 1][0] * uc[j] / g - g * g * hy[i + 1][j + 1] - g * u[i] * hy[0][j + 1] +
+        double Ms = u[i] * uc[j] * k16;
+        const double MD = g * u[i] * (hy[0][j + 1] - hy[0][0] * uc[j] * ig) + g * g * (hy[i + 1][j + 1] - hy[i + 1][0] * uc[j] * ig);
+        double Mds = (hy[i + 1][j + 1] - hy[i + 1][0] * uc[j] * ig - g * g * hy[i + 1][j + 1] - g * u[i] * hy[0][j + 1] +
                       uc[j] * g * hy[i + 1][0] + uc[j] * u[i] * hy[0][0] +
-                      4. * g * u[i] * (hy[0][j + 1] - hy[0][0] * uc[j] / g) / 3. +
-                      (-pi[0][i + 1] + 4. * pi[0][i + 1] / 3.) * uc[j] / g) / 4.;
-        double Mdo = (hy[i + 1][j + 1] - hy[i + 1][0] * uc[j] / g - g * g * hy[i + 1][j + 1] - g * u[i] * hy[0][j + 1] +
-                      uc[j] * g * hy[i + 1][0] + uc[j] * u[i] * hy[0][0] + pi[0][i + 1] * uc[j] / g) / 4.;
-        const double Mdd = -pi[i + 1][0] * uc[j] / g;
+                      4. * g * u[i] * (hy[0][j + 1] - hy[0][0] * uc[j] * ig) * k13 +
+                      (-pi[0][i + 1] + 4. * pi[0][i + 1] * k13) * uc[j] * ig) / 4.;
+        double Mdo = (hy[i + 1][j + 1] - hy[i + 1][0] * uc[j] * ig - g * g * hy[i + 1][j + 1] - g * u[i] * hy[0][j + 1] +
+                      uc[j] * g * hy[i + 1][0] + uc[j] * u[i] * hy[0][0] + pi[0][i + 1] * uc[j] * ig) / 4.;
+        const double Mdd = -pi[i + 1][0] * uc[j] * ig;
         if (i == j) {
           Ms += (1. - g * g) / 2.;
           Mdo += -pi[0][0] / 4.;
           Mds += +pi[0][0] / 4.;
         }
-        M0i[i * D + j] = (-tpi * MD - dpp * Mdd + 2. * tpi * Mdo * uv - tpp * Mds + (2. * eta + lpP * Pi) * Ms) / (tpi * g);
+        M0i[i * D + j] = (-tpi * MD - dpp * Mdd + 2. * tpi * Mdo * uv - tpp * Mds + (2. * eta + lpP * Pi) * Ms) * itg;
       }
     }
     // pi^{ij} nabla_i u_j MRF
 #pragma unroll
     for (int i = 0; i < D; i++) {
-      Mnab[i] = hy[0][i + 1] - hy[0][0] * uc[i] / g;
+      Mnab[i] = hy[0][i + 1] - hy[0][0] * uc[i] * ig;
 #pragma unroll
       for (int j = 0; j < D; j++) Fnab += (hy[i + 1][j + 1] - v[i] * hy[0][j + 1]) * gu[i][j];
       Fnab += (hy[i + 1][0] - v[i] * hy[0][0]) * gu0[i];
     }
-    Fnab += +hy[3][3] * g / t + hy[0][0] * geo + (t * hy[3][0] + hy[0][3] / t) * uD * dEta(D - 1);
+    Fnab += +hy[3][3] * g * it + hy[0][0] * geo + (t * hy[3][0] + hy[0][3] * it) * uD * dEta(D - 1);
     // shear-tensor evolution MRFs on the (i <= j) entries of the 2x3 block
     const double f2 = fu[2];
 #pragma unroll
@@ -268,44 +273,44 @@ __device__ inline void eom(const ccake_config& cfg, const Transport& k, const Eo
         for (int kk = 0; kk < 4; kk++) sml += (pi[i + 1][kk] * hy[j + 1][kk] + pi[j + 1][kk] * hy[i + 1][kk]) / 2.;
         double FD2 = g * geo * (fu[i] * hy[j + 1][0] + fu[j] * hy[i + 1][0]);
         const double cg_ij = (i < D && j < D) ? cgu[i][j] : 0.0, cg_ji = (i < D && j < D) ? cgu[j][i] : 0.0;
-        double Fsg = cg_ij / 2. + cg_ji / 2. + fu[i] * fu[j] * expn / 3.;
+        double Fsg = cg_ij / 2. + cg_ji / 2. + fu[i] * fu[j] * expn * k13;
         const double Fdl = pi[i + 1][j + 1] * expn;
         const double common = t * f2 * (cmd[i + 1] * hy[j + 1][0] * di + cmd[j + 1] * hy[i + 1][0] * dj) +
-                              g * (cmd[i + 1] * hy[j + 1][3] * di + cmd[j + 1] * hy[i + 1][3] * dj) / t +
+                              g * (cmd[i + 1] * hy[j + 1][3] * di + cmd[j + 1] * hy[i + 1][3] * dj) * it +
                               f2 * f2 * t * (fu[i] * hy[j + 1][0] + fu[j] * hy[i + 1][0]) +
-                              2. * g * f2 * (fu[i] * hy[j + 1][3] + fu[j] * hy[i + 1][3]) / t;
-        const double cross = g * (pi[3][i + 1] * dj + pi[3][j + 1] * di) / t + f2 * (pi[0][i + 1] * dj + pi[0][j + 1] * di) / t;
+                              2. * g * f2 * (fu[i] * hy[j + 1][3] + fu[j] * hy[i + 1][3]) * it;
+        const double cross = g * (pi[3][i + 1] * dj + pi[3][j + 1] * di) * it + f2 * (pi[0][i + 1] * dj + pi[0][j + 1] * di) * it;
         const double Fdo2 = -(-gugjs + sigu - vsig) / 4. + (-fu[i] * g * hy[j + 1][0] - fu[j] * g * hy[i + 1][0]) * geo / 4. +
                             (common - cross) / 4.;
-        double Fds2 = -(-gugjs - sigu + vsig - 4. * (fu[i] * fu[j]) * sgu_s / 3.) / 4. +
-                      (-fu[i] * g * hy[j + 1][0] - fu[j] * g * hy[i + 1][0] + 4. * fu[i] * fu[j] * hy[0][0] / 3.) * geo / 4. +
-                      (common + cross + 4. * fu[i] * fu[j] * (hy[3][0] * f2 * t + g * hy[3][3] / t + f2 * hy[0][3] / t) / 3.) / 4. -
-                      pi[i + 1][j + 1] * (g / t + geo + g * divV) / 3.;
+        double Fds2 = -(-gugjs - sigu + vsig - 4. * (fu[i] * fu[j]) * sgu_s * k13) / 4. +
+                      (-fu[i] * g * hy[j + 1][0] - fu[j] * g * hy[i + 1][0] + 4. * fu[i] * fu[j] * hy[0][0] * k13) * geo / 4. +
+                      (common + cross + 4. * fu[i] * fu[j] * (hy[3][0] * f2 * t + g * hy[3][3] * it + f2 * hy[0][3] * it) * k13) / 4. -
+                      pi[i + 1][j + 1] * (g * it + geo + g * divV) * k13;
         if (j == 2) {
-          FD2 += g * pi[3][i + 1] / t + f2 * pi[0][i + 1] / t;
-          Fsg += -fu[i] * f2 * f2 * t / 2. - fu[i] * f2 * g / t;
+          FD2 += g * pi[3][i + 1] * it + f2 * pi[0][i + 1] * it;
+          Fsg += -fu[i] * f2 * f2 * t / 2. - fu[i] * f2 * g * it;
         }
         if (i == j) {
-          Fsg += -cmd[i + 1] * expn / 3.;
-          Fds2 += -cmd[i + 1] * sgu_s / 3. - cmd[i + 1] * hy[0][0] * geo / 3. -
-                  cmd[i + 1] * (hy[3][0] * f2 * t + g * hy[3][3] / t + f2 * hy[0][3] / t) / 3.;
+          Fsg += -cmd[i + 1] * expn * k13;
+          Fds2 += -cmd[i + 1] * sgu_s * k13 - cmd[i + 1] * hy[0][0] * geo * k13 -
+                  cmd[i + 1] * (hy[3][0] * f2 * t + g * hy[3][3] * it + f2 * hy[0][3] * it) * k13;
         }
         double F = (-pi[i + 1][j + 1] - tdelta * Fdl - tpi * FD2 + 2. * tpi * Fdo2 * uv - tpp * Fds2 +
-                    (2. * eta + lpP * Pi) * Fsg + phi6 * Pi * pi[i + 1][j + 1] + phi7 * (sml + fu[i] * fu[j] * ss / 3.)) /
-                   (sig * tpi * g);
-        if (i == j) F += phi7 * (-cmd[i + 1] * ss) / (3. * tpi * g * sig);
+                    (2. * eta + lpP * Pi) * Fsg + phi6 * Pi * pi[i + 1][j + 1] + phi7 * (sml + fu[i] * fu[j] * ss * k13)) *
+                   istg;
+        if (i == j) F += phi7 * (-cmd[i + 1] * ss) * (k13 * istg);
         Fext[slot] = F;
 #pragma unroll
         for (int kk = 0; kk < D; kk++) {
-          const double MD2 = g * (fu[i] * hy[j + 1][kk + 1] - fu[i] * hy[j + 1][0] * fuc[kk] / g + fu[j] * hy[i + 1][kk + 1] -
-                                  fu[j] * hy[i + 1][0] * fuc[kk] / g);
-          double Msg = -fu[i] * fu[j] * fuc[kk] / (3. * g);
-          const double Mdl = -pi[i + 1][j + 1] * fuc[kk] / g;
+          const double MD2 = g * (fu[i] * hy[j + 1][kk + 1] - fu[i] * hy[j + 1][0] * fuc[kk] * ig + fu[j] * hy[i + 1][kk + 1] -
+                                  fu[j] * hy[i + 1][0] * fuc[kk] * ig);
+          double Msg = -fu[i] * fu[j] * fuc[kk] * (k13 * ig);
+          const double Mdl = -pi[i + 1][j + 1] * fuc[kk] * ig;
           double Mdo2 = (-fu[i] * hy[j + 1][kk + 1] * g - fu[j] * hy[i + 1][kk + 1] * g + fuc[kk] * fu[i] * hy[j + 1][0] +
                          fuc[kk] * fu[j] * hy[i + 1][0]) / 4.;
           double Mds2 = (-fu[i] * hy[j + 1][kk + 1] * g - fu[j] * hy[i + 1][kk + 1] * g + fuc[kk] * fu[i] * hy[j + 1][0] +
-                         fuc[kk] * fu[j] * hy[i + 1][0] + 4. * fu[i] * fu[j] * (hy[0][kk + 1] - hy[0][0] * fuc[kk] / g) / 3. +
-                         4. * pi[i + 1][j + 1] * fuc[kk] / 3. / g) / 4.;
+                         fuc[kk] * fu[j] * hy[i + 1][0] + 4. * fu[i] * fu[j] * (hy[0][kk + 1] - hy[0][0] * fuc[kk] * ig) * k13 +
+                         4. * pi[i + 1][j + 1] * fuc[kk] * k13 * ig) / 4.;
           if (kk == i) {            // i = k terms
             Mds2 += pi[0][j + 1] / 4.;
             Mdo2 += -pi[0][j + 1] / 4.;
@@ -317,11 +322,11 @@ __device__ inline void eom(const ccake_config& cfg, const Transport& k, const Eo
             Mdo2 += -pi[0][i + 1] / 4.;
           }
           if (i == j) {             // i = j terms
-            Msg += cmd[i + 1] * fuc[kk] / (g * 3.);
-            Mds2 += -cmd[i + 1] * (hy[0][kk + 1] - hy[0][0] * fuc[kk] / g) / 3.;
+            Msg += cmd[i + 1] * fuc[kk] * (ig * k13);
+            Mds2 += -cmd[i + 1] * (hy[0][kk + 1] - hy[0][0] * fuc[kk] * ig) * k13;
           }
-          Mext[slot][kk] = (-tpi * MD2 - tdelta * Mdl + 2. * tpi * Mdo2 * uv - tpp * Mds2 + (2. * eta + lpP * Pi) * Msg) /
-                           (sig * tpi * g);
+          Mext[slot][kk] = (-tpi * MD2 - tdelta * Mdl + 2. * tpi * Mdo2 * uv - tpp * Mds2 + (2. * eta + lpP * Pi) * Msg) *
+                           istg;
         }
       }
     }
@@ -329,63 +334,65 @@ __device__ inline void eom(const ccake_config& cfg, const Transport& k, const Eo
 
   // ---- auxiliary bulk and entropy MRFs (reference :229-362) ---------------
   const double ztil = k.zeta + (k.delta_PiPi - k.tau_Pi) * Pi;
+  const double isgT = 1.0 / (sig * g * T), isgP = 1.0 / (sig * g * k.tau_Pi);
   double Mb[3], Ms[3];
 #pragma unroll
   for (int i = 0; i < D; i++) {
-    Mb[i] = (ztil * uc[i] / g) / (sig * g * k.tau_Pi);
-    Ms[i] = (Pi * uc[i] / g) / (sig * g * T);
+    Mb[i] = (ztil * uc[i] * ig) * isgP;
+    Ms[i] = (Pi * uc[i] * ig) * isgT;
   }
-  double Fb = -(ztil * expn + Pi - k.phi1 * Pi * Pi) / (sig * g * k.tau_Pi);
-  double Fs = (-Pi * expn) / (sig * g * T);
+  double Fb = -(ztil * expn + Pi - k.phi1 * Pi * Pi) * isgP;
+  double Fs = (-Pi * expn) * isgT;
   if (cfg.using_shear) {
-    Fs += Fnab / (sig * g * T);
-    Fb += -(k.lambda_Pipi * Fnab - k.phi3 * ss) / (sig * g * k.tau_Pi);
+    Fs += Fnab * isgT;
+    Fb += -(k.lambda_Pipi * Fnab - k.phi3 * ss) * isgP;
 #pragma unroll
     for (int i = 0; i < D; i++) {
-      Mb[i] += -k.lambda_Pipi * Mnab[i] / (sig * g * k.tau_Pi);
-      Ms[i] += Mnab[i] / (sig * g * T);
+      Mb[i] += -k.lambda_Pipi * Mnab[i] * isgP;
+      Ms[i] += Mnab[i] * isgT;
     }
   }
   // ---- four-acceleration (reference :456-618); dN/dt = 0 without diffusion --
   double gP[3], gB[3];
 #pragma unroll
   for (int i = 0; i < D; i++) {
-    const double f = (D == 2 || i < D - 1) ? -1.0 : -1.0 / t2;   // make_contravariant
+    const double f = (D == 2 || i < D - 1) ? -1.0 : -1.0 * it2;   // make_contravariant
     gP[i] = in.gradP[i] * f;
     gB[i] = in.gradBulk[i] * f;
   }
-  const double X = sden * dwds / g + (rho[0] * dwdr[0] + rho[1] * dwdr[1] + rho[2] * dwdr[2]) / g;
+  const double X = sden * dwds * ig + (rho[0] * dwdr[0] + rho[1] * dwdr[1] + rho[2] * dwdr[2]) * ig;
   double Mw[3];
 #pragma unroll
-  for (int i = 0; i < D; i++) Mw[i] = X * uc[i] / g + sig * dwds * Ms[i];
-  const double Fw = -X * (geo + g / t + g * divV) + sig * dwds * Fs;
-  const double Fbulk = sig * Fb - Pi * (g * divV + g / t + geo) / g;
+  for (int i = 0; i < D; i++) Mw[i] = X * uc[i] * ig + sig * dwds * Ms[i];
+  const double Fw = -X * (geo + g * it + g * divV) + sig * dwds * Fs;
+  const double Fbulk = sig * Fb - Pi * (g * divV + g * it + geo) * ig;
   double Mu[9], Fu[3];
 #pragma unroll
   for (int i = 0; i < D; i++) {
 #pragma unroll
-    for (int j = 0; j < D; j++) Mu[i * D + j] = u[i] * g * (Mb[j] + Mw[j]) - u[i] * uc[j] * (w + Pi) / g + M0i[i * D + j];
+    for (int j = 0; j < D; j++) Mu[i * D + j] = u[i] * g * (Mb[j] + Mw[j]) - u[i] * uc[j] * (w + Pi) * ig + M0i[i * D + j];
     Mu[i * D + i] += g * (w + Pi);
-    Fu[i] = (gP[i] + gB[i]) - g * (Fw + Fbulk) * u[i] - (w + Pi) * expn * u[i] - 2. * (w + Pi) * g * uD * dEta(i) / t;
+    Fu[i] = (gP[i] + gB[i]) - g * (Fw + Fbulk) * u[i] - (w + Pi) * expn * u[i] - 2. * (w + Pi) * g * uD * dEta(i) * it;
     if (cfg.using_shear)
-      Fu[i] += -P(i + 1, 0) / t - 2. * dEta(i) * P(0, 3) / t - in.divshear[i] + in.gradshear[i] - F0i[i];
+      Fu[i] += -P(i + 1, 0) * it - 2. * dEta(i) * P(0, 3) * it - in.divshear[i] + in.gradshear[i] - F0i[i];
   }
   // du/dt = M^-1 F by cofactors (include/milne.hpp:788-834)
   double du[3];
   if (D == 2) {
-    const double det = Mu[0] * Mu[3] - Mu[1] * Mu[2];
-    du[0] = (Mu[3] / det) * Fu[0] + (-Mu[1] / det) * Fu[1];
-    du[1] = (-Mu[2] / det) * Fu[0] + (Mu[0] / det) * Fu[1];
+    const double idet = 1.0 / (Mu[0] * Mu[3] - Mu[1] * Mu[2]);
+    du[0] = (Mu[3] * idet) * Fu[0] + (-Mu[1] * idet) * Fu[1];
+    du[1] = (-Mu[2] * idet) * Fu[0] + (Mu[0] * idet) * Fu[1];
     du[2] = 0.0;
   } else {
 #define A(i, j) Mu[(i) * 3 + (j)]
     const double det = A(0, 0) * A(1, 1) * A(2, 2) + A(0, 1) * A(1, 2) * A(2, 0) + A(0, 2) * A(1, 0) * A(2, 1) -
                        A(0, 2) * A(1, 1) * A(2, 0) - A(0, 1) * A(1, 0) * A(2, 2) - A(0, 0) * A(1, 2) * A(2, 1);
-    const double inv[9] = {(A(1, 1) * A(2, 2) - A(1, 2) * A(2, 1)) / det, (A(0, 2) * A(2, 1) - A(0, 1) * A(2, 2)) / det,
-                           (A(0, 1) * A(1, 2) - A(0, 2) * A(1, 1)) / det, (A(1, 2) * A(2, 0) - A(1, 0) * A(2, 2)) / det,
-                           (A(0, 0) * A(2, 2) - A(0, 2) * A(2, 0)) / det, (A(0, 2) * A(1, 0) - A(0, 0) * A(1, 2)) / det,
-                           (A(1, 0) * A(2, 1) - A(1, 1) * A(2, 0)) / det, (A(0, 1) * A(2, 0) - A(0, 0) * A(2, 1)) / det,
-                           (A(0, 0) * A(1, 1) - A(0, 1) * A(1, 0)) / det};
+    const double idet = 1.0 / det;
+    const double inv[9] = {(A(1, 1) * A(2, 2) - A(1, 2) * A(2, 1)) * idet, (A(0, 2) * A(2, 1) - A(0, 1) * A(2, 2)) * idet,
+                           (A(0, 1) * A(1, 2) - A(0, 2) * A(1, 1)) * idet, (A(1, 2) * A(2, 0) - A(1, 0) * A(2, 2)) * idet,
+                           (A(0, 0) * A(2, 2) - A(0, 2) * A(2, 0)) * idet, (A(0, 2) * A(1, 0) - A(0, 0) * A(1, 2)) * idet,
+                           (A(1, 0) * A(2, 1) - A(1, 1) * A(2, 0)) * idet, (A(0, 1) * A(2, 0) - A(0, 0) * A(2, 1)) * idet,
+                           (A(0, 0) * A(1, 1) - A(0, 1) * A(1, 0)) * idet};
 #undef A
 #pragma unroll
     for (int i = 0; i < 3; i++) du[i] = inv[i * 3 + 0] * Fu[0] + inv[i * 3 + 1] * Fu[1] + inv[i * 3 + 2] * Fu[2];
@@ -405,7 +412,7 @@ __device__ inline void eom(const ccake_config& cfg, const Transport& k, const Eo
   }
   // ---- dEz (reference :827-862) ---------------------------------------------
   const double u3 = (D == 3) ? u[2] : 0.0;
-  o.dEz = ((th[T_E] + th[T_P] + Pi) * u3 * u3 + (th[T_P] + Pi) / t2 + P(3, 3)) * in.m * t2 / in.sigma_lab;
+  o.dEz = ((th[T_E] + th[T_P] + Pi) * u3 * u3 + (th[T_P] + Pi) * it2 + P(3, 3)) * in.m * t2 / in.sigma_lab;   // one division per particle
 }
 
 }  // namespace ccake
