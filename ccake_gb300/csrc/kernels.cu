@@ -20,6 +20,7 @@ namespace ccake {
 namespace {
 
 constexpr int kBlock = 128;
+constexpr int kSurv = 64;   // candidate chunk kept per thread in shared memory (pass A)
 
 // ---------------------------------------------------------------------------
 // neighbour cells: count, scan, scatter, in-cell sort
@@ -113,48 +114,6 @@ __device__ __forceinline__ void for_candidates(const RunConst& rc, const Ptrs& p
     }
 }
 
-// Iterates the 3^D neighbour cells of particle a and calls f(b, d, d2) for
-// every b != a with d2 = |r_a - r_b|^2 <= (2h)^2 (exact FP64 predicate).
-// Candidates are first screened in FP32 from the float copies of the
-// positions: a candidate is skipped only when its FP32 squared distance
-// exceeds (2h)^2 by more than a bound on the FP32 error (per axis
-// 2^-22 (|x_a| + |x_b| + |dx|) before squaring, 4e-7 relative after), so the
-// exact predicate sees every pair that can be a neighbour and the set is the
-// FP64 one. GB300's FP64 pipe is the bottleneck; this keeps the ~2/3 of the
-// candidates that are rejected off it.
-template <int D, class F>
-__device__ __forceinline__ void for_neighbours(const RunConst& rc, const Ptrs& p, int a, const double* xa, F&& f) {
-  const Grid& g = rc.grid;
-  const float4 pa = p.posf[a];
-  const float cut2f = (float)rc.cut2 * 1.000001f;
-  const int cx = cell_coord(g, 0, xa[0]), cy = cell_coord(g, 1, xa[1]);
-  const int cz = (D == 3) ? cell_coord(g, 2, xa[2]) : 0;
-  const int zlo = (D == 3) ? max(cz - 1, 0) : 0, zhi = (D == 3) ? min(cz + 1, g.nc[2] - 1) : 0;
-  const double2* ra = reinterpret_cast<const double2*>(p.recA);
-  for (int z = zlo; z <= zhi; z++)
-    for (int y = max(cy - 1, 0); y <= min(cy + 1, g.nc[1] - 1); y++) {
-      const int row = (z * g.nc[1] + y) * g.nc[0];
-      const int jb = p.cell_start[row + max(cx - 1, 0)], je = p.cell_start[row + min(cx + 1, g.nc[0] - 1) + 1];
-      for (int j = jb; j < je; j++) {
-        const int b = p.cell_idx[j];
-        if (b == a) continue;
-        const float4 pb = __ldg(&p.posf[b]);
-        const float dxf = pa.x - pb.x, dyf = pa.y - pb.y, dzf = (D == 3) ? pa.z - pb.z : 0.0f;
-        const float ex = 2.4e-7f * (fabsf(pa.x) + fabsf(pb.x) + fabsf(dxf)) + 1e-30f;
-        const float ey = 2.4e-7f * (fabsf(pa.y) + fabsf(pb.y) + fabsf(dyf)) + 1e-30f;
-        const float ez = (D == 3) ? 2.4e-7f * (fabsf(pa.z) + fabsf(pb.z) + fabsf(dzf)) + 1e-30f : 0.0f;
-        const float d2f = dxf * dxf + dyf * dyf + dzf * dzf;
-        const float bound = ex * (2.0f * fabsf(dxf) + ex) + ey * (2.0f * fabsf(dyf) + ey) +
-                            ez * (2.0f * fabsf(dzf) + ez) + 4e-7f * d2f;
-        if (d2f - bound > cut2f) continue;
-        const double2 b01 = __ldg(&ra[(size_t)b * 4 + 0]), b23 = __ldg(&ra[(size_t)b * 4 + 1]);
-        double d[3] = {xa[0] - b01.x, xa[1] - b01.y, (D == 3) ? xa[2] - b23.x : 0.0};
-        const double d2 = dist2_exact<D>(d);
-        if (d2 <= rc.cut2) f(b, d, d2, b23.y);
-      }
-    }
-}
-
 // ---------------------------------------------------------------------------
 // pass A
 // ---------------------------------------------------------------------------
@@ -225,30 +184,83 @@ __global__ void __launch_bounds__(kBlock) k_passA(RunConst rc, EosDev eos, Ptrs 
   double sl = a23.y * k0, s0 = a45.x * k0, s1 = a45.y * k0, s2 = a67.x * k0, s3 = a67.y * k0;
   int nn = 0;
   const int K = p.K;
-  for_neighbours<D>(rc, p, i, xa, [&](int b, const double* d, double d2, double mb) {
-    // W (src/kernel.cpp:34-48) and the radial factor of grad W (:95-118):
-    // grad_a W = f * (r_a - r_b), f = kgrad/h^(D+1) (2-q)^2 / r for 1 <= q < 2,
-    // kgrad2/h^(D+1) (1.5 q - 2) / h for q < 1. One rsqrt gives r and 1/r.
-    const double rs = d2 > 0.0 ? rsqrt(d2) : 0.0;
-    const double r = d2 * rs;
-    const double q = r * rc.inv_h;
-    double W, fg;
-    if (q >= 2.0) { W = 0.0; fg = 0.0; }
-    else if (q >= 1.0) { const double z = 2.0 - q; W = rc.wn2 * z * z * z; fg = rc.gn * rs * z * z; }
-    else { W = rc.wn * (1.0 - 1.5 * q * q + 0.75 * q * q * q); fg = rc.gn2 * (1.5 * q - 2) * rc.inv_h; }
-    if (nn < K) {
-      p.nbr_idx[(size_t)nn * n + i] = b;
-      p.nbr_f[(size_t)nn * n + i] = fg;
+  // Two phases per chunk of candidates, so that the FP64 work runs with full
+  // warps (an FP64 warp instruction costs the same pipe time whatever its
+  // active-lane count): phase 1 screens candidates in FP32 and keeps the
+  // survivors in this thread's shared-memory column; phase 2 runs the exact
+  // FP64 predicate, W and the grad-W factor on the survivors.
+  __shared__ int32_t surv[kSurv][kBlock];
+  const int tid = threadIdx.x;
+  const Grid& gr = rc.grid;
+  const float4 pa = p.posf[i];
+  const float cut2f = (float)rc.cut2 * 1.000001f;
+  int rlo[D == 3 ? 9 : 3], rhi[D == 3 ? 9 : 3], nr = 0;
+  {
+    const int cx = cell_coord(gr, 0, xa[0]), cy = cell_coord(gr, 1, xa[1]);
+    const int cz = (D == 3) ? cell_coord(gr, 2, xa[2]) : 0;
+    const int zlo = (D == 3) ? max(cz - 1, 0) : 0, zhi = (D == 3) ? min(cz + 1, gr.nc[2] - 1) : 0;
+    for (int z = zlo; z <= zhi; z++)
+      for (int y = max(cy - 1, 0); y <= min(cy + 1, gr.nc[1] - 1); y++) {
+        const int row = (z * gr.nc[1] + y) * gr.nc[0];
+        rlo[nr] = p.cell_start[row + max(cx - 1, 0)];
+        rhi[nr] = p.cell_start[row + min(cx + 1, gr.nc[0] - 1) + 1];
+        nr++;
+      }
+  }
+  int r = 0, j = nr > 0 ? rlo[0] : 0;
+  while (r < nr) {
+    int ns = 0;
+    while (r < nr && ns < kSurv) {            // phase 1 (FP32)
+      if (j >= rhi[r]) { if (++r < nr) j = rlo[r]; continue; }
+      const int b = p.cell_idx[j++];
+      if (b == i) continue;
+      const float4 pb = __ldg(&p.posf[b]);
+      // skipped only when the FP32 squared distance exceeds (2h)^2 by more
+      // than a bound on its FP32 error (per axis 2^-22 (|x_a|+|x_b|+|dx|)
+      // before squaring, 4e-7 relative after): the exact predicate below
+      // sees every possible neighbour, so the set is the FP64 one
+      const float dxf = pa.x - pb.x, dyf = pa.y - pb.y, dzf = (D == 3) ? pa.z - pb.z : 0.0f;
+      const float ex = 2.4e-7f * (fabsf(pa.x) + fabsf(pb.x) + fabsf(dxf)) + 1e-30f;
+      const float ey = 2.4e-7f * (fabsf(pa.y) + fabsf(pb.y) + fabsf(dyf)) + 1e-30f;
+      const float ez = (D == 3) ? 2.4e-7f * (fabsf(pa.z) + fabsf(pb.z) + fabsf(dzf)) + 1e-30f : 0.0f;
+      const float d2f = dxf * dxf + dyf * dyf + dzf * dzf;
+      const float bound = ex * (2.0f * fabsf(dxf) + ex) + ey * (2.0f * fabsf(dyf) + ey) +
+                          ez * (2.0f * fabsf(dzf) + ez) + 4e-7f * d2f;
+      if (d2f - bound > cut2f) continue;
+      surv[ns++][tid] = b;
     }
-    nn++;
-    const double2 b45 = __ldg(&ra[(size_t)b * 4 + 2]);
-    const double2 b67 = __ldg(&ra[(size_t)b * 4 + 3]);
-    sl += mb * W;
-    s0 += b45.x * W;
-    s1 += b45.y * W;
-    s2 += b67.x * W;
-    s3 += b67.y * W;
-  });
+    for (int s = 0; s < ns; s++) {            // phase 2 (FP64)
+      const int b = surv[s][tid];
+      const double2 b01 = __ldg(&ra[(size_t)b * 4 + 0]), b23 = __ldg(&ra[(size_t)b * 4 + 1]);
+      double d[3] = {xa[0] - b01.x, xa[1] - b01.y, (D == 3) ? xa[2] - b23.x : 0.0};
+      const double d2 = dist2_exact<D>(d);
+      if (!(d2 <= rc.cut2)) continue;
+      // W (src/kernel.cpp:34-48) and the radial factor of grad W (:95-118):
+      // grad_a W = fg (r_a - r_b), fg = kgrad/h^(D+1) (2-q)^2 / r for
+      // 1 <= q < 2 and kgrad2/h^(D+1) (1.5 q - 2) / h for q < 1. One rsqrt
+      // gives r and 1/r; both branches are evaluated and selected.
+      const double rs = d2 > 0.0 ? rsqrt(d2) : 0.0;
+      const double rr = d2 * rs;
+      const double q = rr * rc.inv_h;
+      const double z = 2.0 - q, qq = q * q;
+      const double Win = rc.wn * (1.0 - 1.5 * qq + 0.75 * q * qq), Wout = rc.wn2 * z * z * z;
+      const double fin = rc.gn2 * (1.5 * q - 2) * rc.inv_h, fout = rc.gn * rs * z * z;
+      const double W = q < 1.0 ? Win : (q < 2.0 ? Wout : 0.0);
+      const double fg = q < 1.0 ? fin : (q < 2.0 ? fout : 0.0);
+      if (nn < K) {
+        p.nbr_idx[(size_t)nn * n + i] = b;
+        p.nbr_f[(size_t)nn * n + i] = fg;
+      }
+      nn++;
+      const double2 b45 = __ldg(&ra[(size_t)b * 4 + 2]);
+      const double2 b67 = __ldg(&ra[(size_t)b * 4 + 3]);
+      sl += b23.y * W;
+      s0 += b45.x * W;
+      s1 += b45.y * W;
+      s2 += b67.x * W;
+      s3 += b67.y * W;
+    }
+  }
   if (nn > K) atomicAdd(&p.err[E_NBR_OVERFLOW], 1);
   // gamma and v from u (update_velocity), LRF densities (get_LRF = lab/(gamma t))
   const double u3[3] = {p.y[Y_U0 * n + i], p.y[Y_U1 * n + i], D == 3 ? p.y[Y_U2 * n + i] : 0.0};
