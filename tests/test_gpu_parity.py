@@ -186,3 +186,21 @@ def test_gubser_flow_matches_analytic_on_gpu():
     Ta = ics.gubser_temperature(gpu.t, r)
     assert abs(gpu.t - 1.1) < 1e-12
     assert np.max(np.abs(T[m] / Ta[m] - 1)) < 5e-3
+
+
+def test_three_d_milne_parity():
+    # 3+1-D Milne lattice (x, y, eta_s): ~280 neighbours per particle
+    p, rc = ics.hotspots_3d(n_xy=16, n_eta=12, n_hot=4, seed=3)
+    gpu = api.GpuHydro(rc)
+    gpu.load(p)
+    orc = O.OracleRun(p, rc)
+    go, gi = gpu.neighbours()
+    oo, oi = orc.neighbours()
+    assert csr_rows(go, gi) == csr_rows(oo, oi)
+    gpu.initialize()
+    assert orc.initialize() == 0
+    gpu.step(3)
+    assert orc.step(3) == 0
+    for f in ("x", "y", "eta", "u0", "u1", "u2", "ext_s", "T", "e", "sigma_lab", "ext_shv0", "ext_shv2",
+              "ext_shv4", "shv33", "Ez"):
+        assert relerr(gpu.get(f), orc.get(f)) < RTOL, f
