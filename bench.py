@@ -219,6 +219,7 @@ def run_ours(args, world, rank):
     prof = gpu.profile_phases(max(2, min(10, args.steps)))
     # end to end through the C ABI with host buffers (upload, initialise, K steps, download)
     e2e = run_e2e(p, rc, args.steps)
+    mixed = run_mixed(p, rc, args, world, dist)
     if dist:
         dist.destroy_process_group()
     if rank != 0:
@@ -250,6 +251,7 @@ def run_ours(args, world, rank):
         "clocks": clk,
         "gpu_launches": 14 * args.steps,
         "e2e": e2e,
+        "mixed": mixed,
         "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "peak_kind": peak_kind,
                      "traffic": traffic,
@@ -266,6 +268,60 @@ def run_ours(args, world, rank):
                                 "sample": f"{ref_steps} RK2 steps of the same 160k-particle event on the host "
                                           f"(oracle/, OpenMP, {os.cpu_count()} threads)"}
     print(json.dumps(line))
+
+
+def run_mixed(p, rc, args, world, dist):
+    """The mixed-precision form (FP32 compensated pair sums, FP32 EoM, FP64
+    EoS/state) on the same event: throughput, and the per-particle error of
+    e and the charge densities after 100 steps against the FP64 form (which
+    matches the FP64 oracle to 1e-10 per field)."""
+    import dataclasses
+    import torch
+    from ccake_gb300 import api
+    mrc = dataclasses.replace(rc, precision=1)
+    g = api.GpuHydro(mrc)
+    g.load(p)
+    g.initialize()
+    for _ in range(args.warmup):
+        g.step(1)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ms = g.step_timed(args.steps)
+    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t.item())
+    prof = g.profile_phases(max(2, min(10, args.steps)))
+    g.close()
+    # accuracy: 100 steps of each form from the same initial state
+    steps_err = 100
+    runs = {}
+    for prec in (0, 1):
+        h = api.GpuHydro(dataclasses.replace(rc, precision=prec))
+        h.load(p)
+        h.initialize()
+        h.step(steps_err)
+        runs[prec] = {f: h.get(f) for f in ("e", "rhoB", "rhoQ", "s", "T", "u0", "u1")}
+        runs[prec]["totals"] = h.totals()
+        h.close()
+    err = {}
+    for f in ("e", "rhoB", "rhoQ", "s", "T"):
+        a, b = runs[1][f], runs[0][f]
+        err[f] = float(np.max(np.abs(a - b) / (np.abs(b) + 1e-300)))
+    for f in ("u0", "u1"):
+        a, b = runs[1][f], runs[0][f]
+        err[f + "_of_range"] = float(np.max(np.abs(a - b)) / (np.max(np.abs(b)) + 1e-300))
+    tot = {k: float(abs(runs[1]["totals"][k] - runs[0]["totals"][k]) / (abs(runs[0]["totals"][k]) + 1e-300))
+           for k in ("S", "B", "Q", "E")}
+    n = p.n
+    return {"value": world * n * args.steps / (ms_max * 1e-3), "unit": UNIT, "ms_per_step": ms_max / args.steps,
+            "phase_ms": dict(zip(["cells", "passA", "passB"], [float(x) for x in prof])),
+            "gpu_launches": 16 * args.steps,
+            "max_rel_err_after_100_steps": err, "totals_rel_diff_after_100_steps": tot,
+            "error_reference": "plain FP64 form on the GPU (equal to the FP64 oracle within 1e-10 per field)",
+            "what": "FP32 pair loops with Kahan sums and (hi, lo) float positions, FP32 EoM; FP64 EoS Newton, "
+                    "state, RK2 update and totals"}
 
 
 def run_e2e(p, rc, steps):
@@ -289,6 +345,25 @@ def run_e2e(p, rc, steps):
             "what": "ccake_load_particles + ccake_initialize + ccake_step(K) + ccake_copy_out of 11 fields"}
 
 
+def run_form_only(args, form):
+    """Only the timed step loop of one precision form (for profiler launch
+    lists); prints a partial line."""
+    import dataclasses
+    import torch
+    from ccake_gb300 import api, build
+    build.build()
+    p, rc = workload()
+    g = api.GpuHydro(dataclasses.replace(rc, precision=1 if form == "mixed" else 0))
+    g.load(p)
+    g.initialize()
+    for _ in range(args.warmup):
+        g.step(1)
+    torch.cuda.synchronize()
+    ms = g.step_timed(args.steps)
+    print(json.dumps({"partial": True, "form": form, "metric": METRIC, "unit": UNIT, "steps": args.steps,
+                      "ms_per_step": ms / args.steps, "value": p.n * args.steps / (ms * 1e-3)}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -297,11 +372,15 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--ref-steps", type=int, default=4, help="RK2 steps timed on the CPU")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--form", choices=["fp64", "mixed"], default=None,
+                    help="time only this form's step loop (profiler launch lists); partial output")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":
         run_reference(args, world, rank)
+    elif args.form:
+        run_form_only(args, args.form)
     else:
         run_ours(args, world, rank)
 

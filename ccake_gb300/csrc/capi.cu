@@ -31,6 +31,7 @@ struct ccake_ctx {
   double* dbuf = nullptr;
   int32_t* ibuf = nullptr;
   double* d_table = nullptr;
+  int records_form = 0;   // which smoothing record matches the state: 0 FP64, 1 mixed
 };
 
 namespace {
@@ -119,12 +120,35 @@ ccake_status_t reset_errors(ccake_ctx* ctx) {
   return CCAKE_OK;
 }
 
+// doubles per particle in the double slab (state, fields, records)
+constexpr int64_t kDoublesPerParticle =
+    RA + RB + 2 + RAF / 2 + RBF / 2 + 2 * NY + 1 + NTH + 1 + 3 + 1 + 1 + 1 + NPI + NGRAD + NDER + 1 + 1 + 3;
+
+// The smoothing record of each precision form is written by that form's
+// pass B; before a pass A of the other form runs, it is packed from the state.
+void ensure_records(ccake_ctx* ctx, int form) {
+  if (ctx->records_form == form) return;
+  if (form == 1) launch_pack_mixed(ctx->rc, ctx->p, ctx->stream);
+  else launch_pack_fp64(ctx->rc, ctx->p, ctx->stream);
+  ctx->records_form = form;
+}
+
+void enqueue_passA(ccake_ctx* ctx) {
+  if (ctx->cfg.precision == 1) launch_passA_mixed(ctx->rc, ctx->eos, ctx->p, ctx->stream);
+  else launch_passA(ctx->rc, ctx->eos, ctx->p, A_WITH_THERMO, ctx->stream);
+}
+
+void enqueue_passB(ccake_ctx* ctx, int mode, double dt_sub) {
+  if (ctx->cfg.precision == 1) launch_passB_mixed(ctx->rc, ctx->p, mode, dt_sub, ctx->stream);
+  else launch_passB(ctx->rc, ctx->p, mode, dt_sub, ctx->stream);
+}
+
 void enqueue_substep(ccake_ctx* ctx, int sub) {
   const double dt = ctx->cfg.dt;
   launch_build_cells(ctx->rc, ctx->p, ctx->stream);
-  launch_passA(ctx->rc, ctx->eos, ctx->p, A_WITH_THERMO, ctx->stream);
+  enqueue_passA(ctx);
   int mode = B_EOM | B_UPDATE | (sub == 2 ? B_WRITE_Y0 : 0);
-  launch_passB(ctx->rc, ctx->p, mode, sub == 1 ? 0.5 * dt : dt, ctx->stream);
+  enqueue_passB(ctx, mode, sub == 1 ? 0.5 * dt : dt);
   launch_clock(ctx->p, sub, dt, ctx->stream);
 }
 
@@ -210,6 +234,7 @@ ccake_status_t ccake_ctx_create(const ccake_config* cfg, ccake_ctx** out) {
   if (cfg->dim != 2 && cfg->dim != 3) return CCAKE_ERR_INVALID;
   if (cfg->coord != 0) return CCAKE_ERR_INVALID;
   if (cfg->eos_kind != 0 && cfg->eos_kind != 1) return CCAKE_ERR_INVALID;
+  if (cfg->precision != 0 && cfg->precision != 1) return CCAKE_ERR_INVALID;
   if (!(cfg->hT > 0) || !(cfg->t0 > 0) || !(cfg->dt > 0)) return CCAKE_ERR_INVALID;
   if (cfg->dim == 3 && cfg->factorized_kernel) return CCAKE_ERR_INVALID;
   ccake_ctx* ctx = new ccake_ctx;
@@ -270,9 +295,8 @@ ccake_status_t ccake_load_particles(ccake_ctx* ctx, const ccake_particles_soa* h
   std::iota(ctx->perm.begin(), ctx->perm.end(), 0);
   std::stable_sort(ctx->perm.begin(), ctx->perm.end(), [&](int32_t a, int32_t b) { return key[a] < key[b]; });
   // device memory: one double slab, one int slab
-  const size_t nd = (size_t)n * (2 + 2 * NY + 1 + NTH + 1 + 3 + 1 + 1 + 1 + NPI + RA + RB + NGRAD + NDER + 1 + 1 + 3) +
-                    (size_t)kTotBlocks * 6 + 8;
-  const size_t ni = (size_t)n * 7 + (size_t)g.ncell * 2 + 1 + NERR + 8;
+  const size_t nd = (size_t)n * kDoublesPerParticle + (size_t)kTotBlocks * 6 + 8;
+  const size_t ni = (size_t)n * 7 + (size_t)g.ncell * 2 + 1 + NERR + 2 * (size_t)scan_tiles(g.ncell) + 1 + 8;
   if (cudaMalloc(&ctx->dbuf, nd * sizeof(double)) != cudaSuccess) return fail(ctx, CCAKE_ERR_NOMEM, "device allocation");
   if (cudaMalloc(&ctx->ibuf, ni * sizeof(int32_t)) != cudaSuccess) return fail(ctx, CCAKE_ERR_NOMEM, "device allocation");
   CK(cudaMemsetAsync(ctx->dbuf, 0, nd * sizeof(double), ctx->stream));
@@ -285,6 +309,8 @@ ccake_status_t ccake_load_particles(ccake_ctx* ctx, const ccake_particles_soa* h
   // 16-byte vector loads stay aligned for any n
   p.recA = take(RA); p.recB = take(RB);
   p.posf = reinterpret_cast<float4*>(take(2));
+  p.recAf = reinterpret_cast<float*>(take(RAF / 2));
+  p.recBf = reinterpret_cast<float*>(take(RBF / 2));
   p.y = take(NY); p.y0 = take(NY); p.m = take(1); p.th = take(NTH); p.gam = take(1); p.v = take(3);
   p.slab = take(1); p.sig = take(1); p.bulk = take(1); p.pi = take(NPI);
   p.grads = take(NGRAD); p.derivs = take(NDER); p.in_e = take(1); p.in_s = take(1); p.in_rho = take(3);
@@ -296,6 +322,7 @@ ccake_status_t ccake_load_particles(ccake_ctx* ctx, const ccake_particles_soa* h
   p.eos_id = itake(n); p.eos_iters = itake(n); p.btrack = itake(n); p.freeze = itake(n);
   p.cell_of = itake(n); p.cell_rank = itake(n); p.cell_idx = itake(n);
   p.cell_count = itake(g.ncell); p.cell_start = itake(g.ncell + 1); p.err = itake(NERR);
+  p.scan_aux = itake(2 * (size_t)scan_tiles(g.ncell) + 1);
   // upload permuted inputs
   std::vector<double> tmp((size_t)n);
   auto up = [&](const double* src, double* dst) -> ccake_status_t {
@@ -352,6 +379,7 @@ ccake_status_t ccake_initialize(ccake_ctx* ctx) {
   CK(cudaMemcpyAsync(ctx->p.y0, ctx->p.y, NY * n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
   s = check_errors(ctx);
   if (s) return s;
+  ctx->records_form = 0;
   ctx->t = ctx->cfg.t0;
   ctx->initialized = true;
   return CCAKE_OK;
@@ -362,6 +390,7 @@ ccake_status_t ccake_step(ccake_ctx* ctx, int32_t n_steps) {
   if (!ctx->initialized) return fail(ctx, CCAKE_ERR_STATE, "initialize first");
   ccake_status_t s = reset_errors(ctx);
   if (s) return s;
+  ensure_records(ctx, ctx->cfg.precision);
   if (!ctx->graph_exec) {
     CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     enqueue_substep(ctx, 1);
@@ -404,6 +433,7 @@ ccake_status_t ccake_profile_phases(ccake_ctx* ctx, int32_t n_steps, double* ms3
   if (!ctx->initialized) return fail(ctx, CCAKE_ERR_STATE, "initialize first");
   ccake_status_t s = reset_errors(ctx);
   if (s) return s;
+  ensure_records(ctx, ctx->cfg.precision);
   cudaEvent_t ev[4];
   for (int q = 0; q < 4; q++) CK(cudaEventCreate(&ev[q]));
   double acc[3] = {0, 0, 0};
@@ -413,10 +443,9 @@ ccake_status_t ccake_profile_phases(ccake_ctx* ctx, int32_t n_steps, double* ms3
       CK(cudaEventRecord(ev[0], ctx->stream));
       launch_build_cells(ctx->rc, ctx->p, ctx->stream);
       CK(cudaEventRecord(ev[1], ctx->stream));
-      launch_passA(ctx->rc, ctx->eos, ctx->p, A_WITH_THERMO, ctx->stream);
+      enqueue_passA(ctx);
       CK(cudaEventRecord(ev[2], ctx->stream));
-      launch_passB(ctx->rc, ctx->p, B_EOM | B_UPDATE | (sub == 2 ? B_WRITE_Y0 : 0), sub == 1 ? 0.5 * dt : dt,
-                   ctx->stream);
+      enqueue_passB(ctx, B_EOM | B_UPDATE | (sub == 2 ? B_WRITE_Y0 : 0), sub == 1 ? 0.5 * dt : dt);
       CK(cudaEventRecord(ev[3], ctx->stream));
       launch_clock(ctx->p, sub, dt, ctx->stream);
       CK(cudaEventSynchronize(ev[3]));
@@ -439,8 +468,8 @@ ccake_status_t ccake_profile_phases(ccake_ctx* ctx, int32_t n_steps, double* ms3
 ccake_status_t ccake_device_bytes(const ccake_ctx* ctx, int64_t* bytes) {
   if (!ctx || !bytes) return CCAKE_ERR_INVALID;
   const int64_t n = ctx->n;
-  const int64_t nd = n * (2 + 2 * NY + 1 + NTH + 1 + 3 + 1 + 1 + 1 + NPI + RA + RB + NGRAD + NDER + 1 + 1 + 3);
-  const int64_t ni = n * 7 + (int64_t)ctx->rc.grid.ncell * 2;
+  const int64_t nd = n * kDoublesPerParticle;
+  const int64_t ni = n * 7 + (int64_t)ctx->rc.grid.ncell * 2 + 2 * (int64_t)scan_tiles(ctx->rc.grid.ncell);
   *bytes = nd * 8 + ni * 4 + (int64_t)ctx->p.K * n * 12;
   return CCAKE_OK;
 }
@@ -455,6 +484,7 @@ ccake_status_t ccake_build_neighbours(ccake_ctx* ctx) {
 ccake_status_t ccake_smooth_fields(ccake_ctx* ctx) {
   if (!ctx) return CCAKE_ERR_INVALID;
   if (!ctx->initialized) return fail(ctx, CCAKE_ERR_STATE, "initialize first");
+  ensure_records(ctx, 0);   // the phase entry points run the FP64 form
   launch_build_cells(ctx->rc, ctx->p, ctx->stream);
   launch_passA(ctx->rc, ctx->eos, ctx->p, A_SMOOTH_ONLY, ctx->stream);
   return check_errors(ctx);

@@ -320,11 +320,45 @@ __host__ __device__ inline void confdiag_seed(const Scales& k, int entropy, cons
   x[3] = sgnd(S) * cbrt(k.muS0 * k.muS0 * k.muS0 * k.muS0 * fabs(S)) / den;
 }
 
+// Exact inverse of an analytic model in entropy mode, (s, B, Q, S) ->
+// (T, muB, muQ, muS); false for the table.
+//   conformal-diagonal: p = c T0^4 sum_k (X_k/X0_k)^4, so each density
+//     d_k = 4 c T0^4 X_k^3 / X0_k^4 and X_k = cbrt(d_k X0_k^4 / (4 c T0^4));
+//   conformal: p = c T0^4 x^2 with x = sum_k (X_k/X0_k)^2, so
+//     d_k = 4 c T0^4 x X_k / X0_k^2; with a_k = X_k/X0_k and
+//     d'_k = d_k X0_k / (4 c T0^4) = a_k x, x^3 = sum_k d'_k^2 and a_k = d'_k / x.
+__host__ __device__ inline bool analytic_seed(const EosDev& e, int model, const double* tgt, double* y) {
+  if (model == M_TABLE) return false;
+  const Scales k = model_scales(e, model);
+  const double X0[4] = {k.T0, k.muB0, k.muQ0, k.muS0};
+  const double c4 = 4.0 * k.c * k.T0 * k.T0 * k.T0 * k.T0;
+  if (model == M_CDIAG) {
+    for (int i = 0; i < 4; i++) {
+      const double q = X0[i] * X0[i];
+      y[i] = cbrt(tgt[i] * q * q / c4);
+    }
+    return y[0] > 0.0;
+  }
+  double d[4], x3 = 0.0;
+  for (int i = 0; i < 4; i++) {
+    d[i] = tgt[i] * X0[i] / c4;
+    x3 += d[i] * d[i];
+  }
+  const double xx = cbrt(x3);
+  if (!(xx > 0.0)) return false;
+  const double ix = 1.0 / xx;
+  for (int i = 0; i < 4; i++) y[i] = d[i] * ix * X0[i];
+  return y[0] > 0.0;
+}
+
 // (e|s, B, S, Q) -> (T, muB, muQ, muS) through the EoS chain with the
 // reference's seeds (src/eos.cpp:629-804 entropy mode, :813-975 energy mode).
-// Returns the chain index used, or -1.
+// seed_mode 1 (entropy mode) first tries Newton from the analytic model's
+// exact inverse, then the reference's seeds. o_out, if given, receives the
+// model thermodynamics at the solution (17 values). Returns the chain index
+// used, or -1.
 __host__ __device__ inline int eos_invert(const EosDev& e, int entropy, const double* target, int start, double* x,
-                                          int* iters) {
+                                          int* iters, int seed_mode = 0, double* o_out = nullptr) {
   const double tgt[4] = {target[0], target[1], target[3], target[2]};  // (e|s, B, Q, S)
   const int n = chain_len(e.kind);
   const Scales cdk = model_scales(e, M_CDIAG);
@@ -333,8 +367,14 @@ __host__ __device__ inline int eos_invert(const EosDev& e, int entropy, const do
   for (int k = entropy ? (start > 0 ? start : 0) : 0; k < n; k++) {
     const int model = chain_model(e.kind, k);
     double y[4];
-    bool ok;
-    if (entropy) {
+    bool ok = false;
+    if (entropy && seed_mode == 1 && analytic_seed(e, model, tgt, y)) {
+      double lo[4], hi[4];
+      model_box(e, model, lo, hi);
+      ok = newton_attempt(e, model, 1, tgt, lo, hi, y, &it);
+    }
+    if (ok) {
+    } else if (entropy) {
       for (int i = 0; i < 4; i++) y[i] = prev[i];
       ok = find_root(e, model, 1, tgt, y, &it);
       if (!ok) { y[0] = prev[0]; y[1] = y[2] = y[3] = 0.0; ok = find_root(e, model, 1, tgt, y, &it); }
@@ -353,6 +393,8 @@ __host__ __device__ inline int eos_invert(const EosDev& e, int entropy, const do
       model_thermo(e, model, y, o);
       if (o[6] < 0.0 || o[6] > 1.0) continue;   // prohibit unstable / acausal cs2
       for (int i = 0; i < 4; i++) x[i] = y[i];
+      if (o_out)
+        for (int i = 0; i < 17; i++) o_out[i] = o[i];
       *iters = it;
       return k;
     }
@@ -440,10 +482,9 @@ __host__ __device__ inline double schur_term(const Chi& x, int which) {
 
 // Derived thermodynamics at a solution: T mu p s rho e w cs2 and dw/ds, dw/drho
 // (reference include/eos.h:121-175, src/eos.cpp:276-344). th must hold NTH doubles.
-__host__ __device__ inline void set_thermo(const EosDev& e, int k, const double* x, double* th) {
+// o: the model thermodynamics at x (model_thermo of the chain's model k).
+__host__ __device__ inline void set_thermo_o(const EosDev& e, int k, const double* x, const double* o, double* th) {
   const int model = chain_model(e.kind, k);
-  double o[17];
-  model_thermo(e, model, x, o);
   const double T = x[0], mB = x[1], mQ = x[2], mS = x[3];
   const double s = o[1], B = o[2], S = o[3], Q = o[4];
   th[T_T] = T; th[T_MUB] = mB; th[T_MUS] = mS; th[T_MUQ] = mQ;
@@ -455,8 +496,19 @@ __host__ __device__ inline void set_thermo(const EosDev& e, int k, const double*
     // exact: G = H^-1 over the Hessian rows that are not identically zero
     double H[4][4] = {{X.t2, X.tb, X.ts, X.tq}, {X.tb, X.b2, X.bs, X.bq}, {X.ts, X.bs, X.s2, X.sq},
                       {X.tq, X.bq, X.sq, X.q2}};
-    if (model == M_CDIAG)
-      for (int i = 0; i < 4; i++) for (int j = 0; j < 4; j++) if (i != j) H[i][j] = 0.0;
+    const double rho[4] = {0.0, B, S, Q};
+    const bool act[4] = {true, hB, hS, hQ};
+    const double mu[4] = {T, mB, mS, mQ};
+    if (model == M_CDIAG) {
+      // diagonal Hessian: G = diag(1/H_aa) over the non-zero rows (the
+      // elimination below gives the same reciprocals)
+      for (int a = 0; a < 4; a++) {
+        const double Haa = H[a][a];
+        const double G = Haa != 0.0 ? 1.0 / Haa : 0.0;
+        th[T_DWDS + a] = (a == 0 || act[a]) ? mu[a] + (a == 0 ? s : rho[a]) * G : mu[a];
+      }
+      return;
+    }
     int keep[4], m = 0;
     for (int i = 0; i < 4; i++) {
       bool zero = true;
@@ -484,9 +536,6 @@ __host__ __device__ inline void set_thermo(const EosDev& e, int k, const double*
     double G[4][4];
     for (int i = 0; i < 4; i++) for (int j = 0; j < 4; j++) G[i][j] = 0.0;
     for (int i = 0; i < m; i++) for (int j = 0; j < m; j++) G[keep[i]][keep[j]] = A[i][m + j];
-    const double rho[4] = {0.0, B, S, Q};
-    const bool act[4] = {true, hB, hS, hQ};
-    const double mu[4] = {T, mB, mS, mQ};
     for (int a = 0; a < 4; a++) {
       double acc = mu[a];
       if (a == 0 || act[a]) {
@@ -523,6 +572,12 @@ __host__ __device__ inline void set_thermo(const EosDev& e, int k, const double*
     if (hS) ct += S / schur_term(X, 7 + 2 * 3 + 1);
   }
   th[T_DWDQ] = mQ + ct;
+}
+
+__host__ __device__ inline void set_thermo(const EosDev& e, int k, const double* x, double* th) {
+  double o[17];
+  model_thermo(e, chain_model(e.kind, k), x, o);
+  set_thermo_o(e, k, x, o, th);
 }
 
 }  // namespace ccake

@@ -10,17 +10,18 @@
 // Each particle's sums are accumulated in registers by the thread that owns
 // it (gather, no atomics), in a fixed cell/index order, so results are
 // reproducible run to run.
+#include <climits>
 #include <cstdio>
 
 #include "kernels.cuh"
+#include "passes.cuh"
 #include "physics.cuh"
 
 namespace ccake {
 
 namespace {
 
-constexpr int kBlock = 128;
-constexpr int kSurv = 64;   // candidate chunk kept per thread in shared memory (pass A)
+using namespace passes;
 
 // ---------------------------------------------------------------------------
 // neighbour cells: count, scan, scatter, in-cell sort
@@ -37,40 +38,105 @@ __global__ void k_bin(RunConst rc, Ptrs p) {
   p.cell_rank[i] = atomicAdd(&p.cell_count[c], 1);
 }
 
-// Exclusive scan of the cell counts by one CTA (each thread owns a chunk).
-__global__ void k_scan(const int32_t* __restrict__ cnt, int32_t* __restrict__ start, int ncell) {
-  __shared__ int32_t warp_tot[32];
-  const int tid = threadIdx.x, nt = blockDim.x;
-  const int chunk = (ncell + nt - 1) / nt;
-  const int b = tid * chunk, e = min(ncell, b + chunk);
-  int32_t local = 0;
-  for (int c = b; c < e; c++) local += cnt[c];
-  // block exclusive scan of `local`
-  const int lane = tid & 31, wid = tid >> 5;
-  int32_t x = local;
+// Exclusive scan of the cell counts, multi-CTA: each CTA scans a tile of
+// kScanTile cells (coalesced through shared memory) into cell_start and
+// publishes the tile total; the last CTA to finish (atomic ticket, no
+// waiting) scans the tile totals into tile offsets; k_scan_add adds them.
+constexpr int kScanThreads = 256;
+constexpr int kScanPer = 4;
+constexpr int kScanTile = kScanThreads * kScanPer;
+
+__device__ __forceinline__ int32_t block_exclusive_scan(int32_t x, int32_t* warp_tot, int32_t* total) {
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
+  int32_t v = x;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
-    int32_t y = __shfl_up_sync(0xffffffffu, x, o);
-    if (lane >= o) x += y;
+    const int32_t y = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v += y;
   }
-  if (lane == 31) warp_tot[wid] = x;
+  if (lane == 31) warp_tot[wid] = v;
   __syncthreads();
   if (wid == 0) {
-    int32_t w = (lane < (nt >> 5)) ? warp_tot[lane] : 0;
+    int32_t w = (lane < nw) ? warp_tot[lane] : 0;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      int32_t y = __shfl_up_sync(0xffffffffu, w, o);
+      const int32_t y = __shfl_up_sync(0xffffffffu, w, o);
       if (lane >= o) w += y;
     }
-    warp_tot[lane] = w;
+    if (lane < nw) warp_tot[lane] = w;
   }
   __syncthreads();
-  int32_t run = x - local + (wid > 0 ? warp_tot[wid - 1] : 0);
-  for (int c = b; c < e; c++) {
-    start[c] = run;
-    run += cnt[c];
+  const int32_t excl = v - x + (wid > 0 ? warp_tot[wid - 1] : 0);
+  if (total) *total = warp_tot[nw - 1];
+  __syncthreads();
+  return excl;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const int32_t* __restrict__ cnt, int32_t* __restrict__ start,
+                                                             int32_t* __restrict__ aux, int ncell) {
+  __shared__ int32_t sh[kScanTile];
+  __shared__ int32_t warp_tot[32];
+  __shared__ int32_t tile_total;
+  __shared__ bool last;
+  const int tid = threadIdx.x;
+  const int base = blockIdx.x * kScanTile;
+#pragma unroll
+  for (int j = 0; j < kScanPer; j++) {
+    const int c = base + j * kScanThreads + tid;
+    sh[j * kScanThreads + tid] = c < ncell ? cnt[c] : 0;
   }
-  if (tid == nt - 1) start[ncell] = run;
+  __syncthreads();
+  int32_t v[kScanPer], sum = 0;
+#pragma unroll
+  for (int j = 0; j < kScanPer; j++) {
+    v[j] = sh[tid * kScanPer + j];
+    sum += v[j];
+  }
+  int32_t run = block_exclusive_scan(sum, warp_tot, &tile_total);
+#pragma unroll
+  for (int j = 0; j < kScanPer; j++) {
+    sh[tid * kScanPer + j] = run;
+    run += v[j];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < kScanPer; j++) {
+    const int c = base + j * kScanThreads + tid;
+    if (c < ncell) start[c] = sh[j * kScanThreads + tid];
+  }
+  // aux: [0, ntiles) tile totals, then tile offsets, then the ticket
+  const int ntiles = gridDim.x;
+  int32_t* tot = aux;
+  int32_t* off = aux + ntiles;
+  int32_t* ticket = aux + 2 * ntiles;
+  if (tid == 0) {
+    tot[blockIdx.x] = tile_total;
+    __threadfence();
+    last = (atomicAdd(ticket, 1) == ntiles - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  int32_t carry = 0;
+  for (int t0 = 0; t0 < ntiles; t0 += kScanThreads) {
+    const int t = t0 + tid;
+    const int32_t x = t < ntiles ? ((volatile int32_t*)tot)[t] : 0;
+    int32_t chunk;
+    const int32_t e = block_exclusive_scan(x, warp_tot, &chunk);
+    if (t < ntiles) off[t] = carry + e;
+    carry += chunk;
+  }
+  if (tid == 0) {
+    start[ncell] = carry;
+    *ticket = 0;
+  }
+}
+
+__global__ void k_scan_add(int32_t* __restrict__ start, const int32_t* __restrict__ aux, int ncell, int ntiles) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncell) return;
+  const int tile = c / kScanTile;
+  if (tile > 0) start[c] += aux[ntiles + tile];
 }
 
 __global__ void k_scatter(Ptrs p) {
@@ -79,17 +145,51 @@ __global__ void k_scatter(Ptrs p) {
   p.cell_idx[p.cell_start[p.cell_of[i]] + p.cell_rank[i]] = i;
 }
 
-// Sorts each cell's index list (insertion sort; cells hold tens of particles)
-// so the summation order does not depend on atomic arrival order.
+// Sorts each cell's index list (one warp a cell; rank of a value = number of
+// smaller values, by shuffles) so that the summation order does not depend on
+// the atomic arrival order. Cells of more than 32 kSortChunks particles fall
+// back to one lane's insertion sort.
+constexpr int kSortChunks = 8;
 __global__ void k_sort_cells(Ptrs p, int ncell) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= ncell) return;
-  const int b = p.cell_start[c], e = p.cell_start[c + 1];
-  for (int j = b + 1; j < e; j++) {
-    const int32_t key = p.cell_idx[j];
-    int k = j - 1;
-    while (k >= b && p.cell_idx[k] > key) { p.cell_idx[k + 1] = p.cell_idx[k]; k--; }
-    p.cell_idx[k + 1] = key;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= ncell) return;
+  const int b = p.cell_start[warp], e = p.cell_start[warp + 1];
+  const int m = e - b;
+  if (m <= 1) return;
+  if (m > 32 * kSortChunks) {
+    if (lane == 0)
+      for (int j = b + 1; j < e; j++) {
+        const int32_t key = p.cell_idx[j];
+        int k = j - 1;
+        while (k >= b && p.cell_idx[k] > key) { p.cell_idx[k + 1] = p.cell_idx[k]; k--; }
+        p.cell_idx[k + 1] = key;
+      }
+    return;
+  }
+  const int nch = (m + 31) >> 5;
+  int32_t v[kSortChunks];
+  int r[kSortChunks];
+#pragma unroll
+  for (int c = 0; c < kSortChunks; c++) {
+    const int j = c * 32 + lane;
+    v[c] = (c < nch && j < m) ? p.cell_idx[b + j] : INT_MAX;
+    r[c] = 0;
+  }
+#pragma unroll
+  for (int c2 = 0; c2 < kSortChunks; c2++) {
+    if (c2 >= nch) break;
+    for (int k = 0; k < 32; k++) {
+      const int32_t u = __shfl_sync(0xffffffffu, v[c2], k);
+#pragma unroll
+      for (int c = 0; c < kSortChunks; c++) r[c] += (u < v[c]) ? 1 : 0;
+    }
+  }
+  __syncwarp();
+#pragma unroll
+  for (int c = 0; c < kSortChunks; c++) {
+    const int j = c * 32 + lane;
+    if (c < nch && j < m) p.cell_idx[b + r[c]] = v[c];
   }
 }
 
@@ -118,59 +218,6 @@ __device__ __forceinline__ void for_candidates(const RunConst& rc, const Ptrs& p
 // pass A
 // ---------------------------------------------------------------------------
 template <int D>
-__device__ __forceinline__ void thermo_tail(const RunConst& rc, const EosDev& eos, const Ptrs& p, int i, double t) {
-  const int n = p.n;
-  const double t2 = t * t;
-  double th[NTH];
-  double x[4] = {p.th[T_T * n + i], p.th[T_MUB * n + i], p.th[T_MUQ * n + i], p.th[T_MUS * n + i]};
-  const double tgt[4] = {p.th[T_S * n + i], p.th[T_RB * n + i], p.th[T_RS * n + i], p.th[T_RQ * n + i]};
-  int iters = 0;
-  const int k = eos_invert(eos, 1, tgt, p.eos_id[i], x, &iters);
-  if (k < 0) {
-    atomicAdd(&p.err[E_EOS], 1);
-    return;
-  }
-  set_thermo(eos, k, x, th);
-#pragma unroll
-  for (int q = 0; q < NTH; q++) p.th[q * n + i] = th[q];
-  p.eos_id[i] = k;
-  p.eos_iters[i] = iters;
-  // pi^{mu nu} and Pi from the extensive forms
-  const double sig = p.sig[i], g = p.gam[i], slab = p.slab[i];
-  double u3[3] = {p.y[Y_U0 * n + i], p.y[Y_U1 * n + i], D == 3 ? p.y[Y_U2 * n + i] : 0.0};
-  double es[5];
-#pragma unroll
-  for (int q = 0; q < 5; q++) es[q] = p.y[(Y_SHV0 + q) * n + i];
-  double pi[NPI];
-  reset_pi(es, sig, g, u3, t2, pi);
-  const double Pi = p.y[Y_EBULK * n + i] * sig;
-  p.bulk[i] = Pi;
-#pragma unroll
-  for (int q = 0; q < NPI; q++) p.pi[q * n + i] = pi[q];
-  // neighbour record B
-  const double isl2 = 1.0 / (slab * slab);
-  double* rb = p.recB + (size_t)i * RB;
-  rb[B_X0] = p.y[Y_X0 * n + i];
-  rb[B_X1] = p.y[Y_X1 * n + i];
-  rb[B_X2] = D == 3 ? p.y[Y_X2 * n + i] : 0.0;
-  rb[B_M] = p.m[i];
-  rb[B_P] = th[T_P] * isl2;
-  rb[B_E] = th[T_E];
-  rb[B_PI] = Pi * isl2;
-#pragma unroll
-  for (int q = 0; q < 3; q++) {
-    rb[B_V0 + q] = p.v[q * n + i];
-    rb[B_PI0 + q] = pi[pi_slot(0, q + 1)] * isl2;
-  }
-  rb[B_PIJ + 0] = pi[P11] * isl2;
-  rb[B_PIJ + 1] = pi[P12] * isl2;
-  rb[B_PIJ + 2] = pi[P13] * isl2;
-  rb[B_PIJ + 3] = pi[P22] * isl2;
-  rb[B_PIJ + 4] = pi[P23] * isl2;
-  rb[B_PIJ + 5] = pi[P33] * isl2;
-}
-
-template <int D>
 __global__ void __launch_bounds__(kBlock) k_passA(RunConst rc, EosDev eos, Ptrs p, int mode) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= p.n) return;
@@ -194,19 +241,8 @@ __global__ void __launch_bounds__(kBlock) k_passA(RunConst rc, EosDev eos, Ptrs 
   const Grid& gr = rc.grid;
   const float4 pa = p.posf[i];
   const float cut2f = (float)rc.cut2 * 1.000001f;
-  int rlo[D == 3 ? 9 : 3], rhi[D == 3 ? 9 : 3], nr = 0;
-  {
-    const int cx = cell_coord(gr, 0, xa[0]), cy = cell_coord(gr, 1, xa[1]);
-    const int cz = (D == 3) ? cell_coord(gr, 2, xa[2]) : 0;
-    const int zlo = (D == 3) ? max(cz - 1, 0) : 0, zhi = (D == 3) ? min(cz + 1, gr.nc[2] - 1) : 0;
-    for (int z = zlo; z <= zhi; z++)
-      for (int y = max(cy - 1, 0); y <= min(cy + 1, gr.nc[1] - 1); y++) {
-        const int row = (z * gr.nc[1] + y) * gr.nc[0];
-        rlo[nr] = p.cell_start[row + max(cx - 1, 0)];
-        rhi[nr] = p.cell_start[row + min(cx + 1, gr.nc[0] - 1) + 1];
-        nr++;
-      }
-  }
+  int rlo[D == 3 ? 9 : 3], rhi[D == 3 ? 9 : 3];
+  const int nr = neighbour_ranges<D>(gr, p.cell_start, xa, rlo, rhi);
   int r = 0, j = nr > 0 ? rlo[0] : 0;
   while (r < nr) {
     int ns = 0;
@@ -215,18 +251,10 @@ __global__ void __launch_bounds__(kBlock) k_passA(RunConst rc, EosDev eos, Ptrs 
       const int b = p.cell_idx[j++];
       if (b == i) continue;
       const float4 pb = __ldg(&p.posf[b]);
-      // skipped only when the FP32 squared distance exceeds (2h)^2 by more
-      // than a bound on its FP32 error (per axis 2^-22 (|x_a|+|x_b|+|dx|)
-      // before squaring, 4e-7 relative after): the exact predicate below
-      // sees every possible neighbour, so the set is the FP64 one
-      const float dxf = pa.x - pb.x, dyf = pa.y - pb.y, dzf = (D == 3) ? pa.z - pb.z : 0.0f;
-      const float ex = 2.4e-7f * (fabsf(pa.x) + fabsf(pb.x) + fabsf(dxf)) + 1e-30f;
-      const float ey = 2.4e-7f * (fabsf(pa.y) + fabsf(pb.y) + fabsf(dyf)) + 1e-30f;
-      const float ez = (D == 3) ? 2.4e-7f * (fabsf(pa.z) + fabsf(pb.z) + fabsf(dzf)) + 1e-30f : 0.0f;
-      const float d2f = dxf * dxf + dyf * dyf + dzf * dzf;
-      const float bound = ex * (2.0f * fabsf(dxf) + ex) + ey * (2.0f * fabsf(dyf) + ey) +
-                          ez * (2.0f * fabsf(dzf) + ez) + 4e-7f * d2f;
-      if (d2f - bound > cut2f) continue;
+      // the screen never drops a pair the exact predicate below accepts, so
+      // the neighbour set is the FP64 one
+      float d2f, bound;
+      if (!maybe_neighbour<D>(pa, pb, cut2f, d2f, bound)) continue;
       surv[ns++][tid] = b;
     }
     for (int s = 0; s < ns; s++) {            // phase 2 (FP64)
@@ -275,14 +303,14 @@ __global__ void __launch_bounds__(kBlock) k_passA(RunConst rc, EosDev eos, Ptrs 
   p.th[T_RS * n + i] = s2 / g / t;
   p.th[T_RQ * n + i] = s3 / g / t;
   p.btrack[i] = nn;
-  if (mode == A_WITH_THERMO) thermo_tail<D>(rc, eos, p, i, t);
+  if (mode == A_WITH_THERMO) thermo_tail<D, false>(rc, eos, p, i, t);
 }
 
 template <int D>
 __global__ void __launch_bounds__(kBlock) k_thermo(RunConst rc, EosDev eos, Ptrs p) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= p.n) return;
-  thermo_tail<D>(rc, eos, p, i, p.clock->t);
+  thermo_tail<D, false>(rc, eos, p, i, p.clock->t);
 }
 
 // ---------------------------------------------------------------------------
@@ -386,98 +414,7 @@ __global__ void __launch_bounds__(kBlock) k_passB(RunConst rc, Ptrs p, int mode,
       dS[k] = sla * acc2;
     }
   }
-  if (mode & B_GRADS) {
-#pragma unroll
-    for (int k = 0; k < D; k++) {
-      p.grads[(G_P + k) * n + i] = gP[k];
-      p.grads[(G_E + k) * n + i] = gE[k];
-      p.grads[(G_B + k) * n + i] = gB[k];
-      p.grads[(G_SH + k) * n + i] = gS[k];
-      p.grads[(G_DS + k) * n + i] = dS[k];
-    }
-#pragma unroll
-    for (int k = 0; k < D * D; k++) p.grads[(G_V + k) * n + i] = gV[k];
-  }
-  if (!(mode & B_EOM)) return;
-  // equations of motion for particle i
-  double th[NTH];
-#pragma unroll
-  for (int q = 0; q < NTH; q++) th[q] = p.th[q * n + i];
-  EomIn<D> in;
-  in.th = th;
-#pragma unroll
-  for (int q = 0; q < 3; q++) {
-    in.u[q] = (q < D) ? p.y[(Y_U0 + q) * n + i] : 0.0;
-    in.v[q] = va[q];
-    in.gradP[q] = gP[q];
-    in.gradBulk[q] = gB[q];
-    in.gradshear[q] = gS[q];
-    in.divshear[q] = dS[q];
-  }
-#pragma unroll
-  for (int q = 0; q < 9; q++) in.gradV[q] = gV[q];
-  in.g = p.gam[i];
-  in.sigma = p.sig[i];
-  in.sigma_lab = sla;
-  in.m = p.m[i];
-  in.Pi = p.bulk[i];
-#pragma unroll
-  for (int q = 0; q < NPI; q++) in.pi[q] = p.pi[q * n + i];
-  const Transport k = transport(rc.cfg, th);
-  EomOut o;
-  eom<D>(rc.cfg, k, in, t, o);
-  if (mode & B_DERIVS) {
-#pragma unroll
-    for (int q = 0; q < 3; q++) p.derivs[(D_DU0 + q) * n + i] = (q < D) ? o.du[q] : 0.0;
-    p.derivs[D_DS * n + i] = o.dS;
-    p.derivs[D_DBULK * n + i] = o.dBulk;
-#pragma unroll
-    for (int q = 0; q < 5; q++) p.derivs[(D_DSHV0 + q) * n + i] = o.dShv[q];
-    p.derivs[D_DEZ * n + i] = o.dEz;
-    p.derivs[D_ETA * n + i] = k.eta;
-    p.derivs[D_TAUPI * n + i] = k.tau_pi;
-    p.derivs[D_ZETA * n + i] = k.zeta;
-    p.derivs[D_TAUBULK * n + i] = k.tau_Pi;
-  }
-  if (!(mode & B_UPDATE)) return;
-  // midpoint RK2 update from the step-start cache (reference src/evolver.cpp:344-486)
-  const double* y0 = p.y0;
-  double ynew[NY];
-#pragma unroll
-  for (int q = 0; q < NY; q++) ynew[q] = y0[q * n + i];
-#pragma unroll
-  for (int q = 0; q < D; q++) {
-    ynew[Y_X0 + q] += dt_sub * va[q];
-    ynew[Y_U0 + q] += dt_sub * o.du[q];
-  }
-  double es = ynew[Y_ES] + dt_sub * o.dS;
-  ynew[Y_EBULK] += dt_sub * o.dBulk;
-#pragma unroll
-  for (int q = 0; q < 5; q++) ynew[Y_SHV0 + q] += dt_sub * o.dShv[q];
-  ynew[Y_EZ] += dt_sub * o.dEz;
-  if (es < 0.0) {
-    if (p.freeze[i] > 3) es = 1.e-3;
-    else atomicAdd(&p.err[E_NEGS], 1);
-  }
-  ynew[Y_ES] = es;
-  bool finite = true;
-#pragma unroll
-  for (int q = 0; q < NY; q++) finite = finite && isfinite(ynew[q]);
-  if (!finite) atomicAdd(&p.err[E_NONFINITE], 1);
-#pragma unroll
-  for (int q = 0; q < NY; q++) p.y[q * n + i] = ynew[q];
-  if (mode & B_WRITE_Y0) {
-#pragma unroll
-    for (int q = 0; q < NY; q++) p.y0[q * n + i] = ynew[q];
-  }
-  // neighbour record A for the next substep
-  const double m = p.m[i];
-  double2* ra = reinterpret_cast<double2*>(p.recA) + (size_t)i * 4;
-  ra[0] = make_double2(ynew[Y_X0], ynew[Y_X1]);
-  p.posf[i] = make_float4((float)ynew[Y_X0], (float)ynew[Y_X1], D == 3 ? (float)ynew[Y_X2] : 0.0f, 0.0f);
-  ra[1] = make_double2(D == 3 ? ynew[Y_X2] : 0.0, m);
-  ra[2] = make_double2(m * ynew[Y_ES], m * ynew[Y_EB]);
-  ra[3] = make_double2(m * ynew[Y_ESS], m * ynew[Y_EQ]);
+  finish_particle<D, double, false>(rc, p, i, mode, t, dt_sub, va, gP, gE, gB, gS, dS, gV);
 }
 
 __global__ void k_visc(RunConst rc, Ptrs p) {
@@ -575,6 +512,17 @@ __global__ void k_init_ext(RunConst rc, Ptrs p) {
   ra[3] = make_double2(m * p.y[Y_ESS * n + i], m * p.y[Y_EQ * n + i]);
 }
 
+// FP64 smoothing record from the state (after mixed substeps moved the particles)
+template <int D>
+__global__ void k_pack_fp64(Ptrs p) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.n) return;
+  const int n = p.n;
+  const double x[3] = {p.y[Y_X0 * n + i], p.y[Y_X1 * n + i], D == 3 ? p.y[Y_X2 * n + i] : 0.0};
+  const double ext[4] = {p.y[Y_ES * n + i], p.y[Y_EB * n + i], p.y[Y_ESS * n + i], p.y[Y_EQ * n + i]};
+  write_recA<D>(p, i, x, p.m[i], ext);
+}
+
 // ---------------------------------------------------------------------------
 // conservation sums (src/system_state.cpp:738-885): per-block partials in a
 // fixed order, summed on the host
@@ -662,9 +610,12 @@ void launch_build_cells(const RunConst& rc, const Ptrs& p, cudaStream_t s) {
   cudaMemsetAsync(p.cell_count, 0, sizeof(int32_t) * rc.grid.ncell, s);
   if (rc.cfg.dim == 3) k_bin<3><<<nb, kBlock, 0, s>>>(rc, p);
   else k_bin<2><<<nb, kBlock, 0, s>>>(rc, p);
-  k_scan<<<1, 1024, 0, s>>>(p.cell_count, p.cell_start, rc.grid.ncell);
+  const int ncell = rc.grid.ncell;
+  const int ntiles = scan_tiles(ncell);
+  k_scan_tiles<<<ntiles, kScanThreads, 0, s>>>(p.cell_count, p.cell_start, p.scan_aux, ncell);
+  k_scan_add<<<(ncell + 255) / 256, 256, 0, s>>>(p.cell_start, p.scan_aux, ncell, ntiles);
   k_scatter<<<nb, kBlock, 0, s>>>(p);
-  k_sort_cells<<<(rc.grid.ncell + 255) / 256, 256, 0, s>>>(p, rc.grid.ncell);
+  k_sort_cells<<<(int)(((int64_t)ncell * 32 + 255) / 256), 256, 0, s>>>(p, ncell);
 }
 
 void launch_passA(const RunConst& rc, const EosDev& eos, const Ptrs& p, int mode, cudaStream_t s) {
@@ -705,6 +656,12 @@ void launch_init_ext(const RunConst& rc, const Ptrs& p, cudaStream_t s) {
   const int nb = (p.n + kBlock - 1) / kBlock;
   if (rc.cfg.dim == 3) k_init_ext<3><<<nb, kBlock, 0, s>>>(rc, p);
   else k_init_ext<2><<<nb, kBlock, 0, s>>>(rc, p);
+}
+
+void launch_pack_fp64(const RunConst& rc, const Ptrs& p, cudaStream_t s) {
+  const int nb = (p.n + kBlock - 1) / kBlock;
+  if (rc.cfg.dim == 3) k_pack_fp64<3><<<nb, kBlock, 0, s>>>(p);
+  else k_pack_fp64<2><<<nb, kBlock, 0, s>>>(p);
 }
 
 void launch_totals(const RunConst& rc, const Ptrs& p, int nblocks, cudaStream_t s) {

@@ -34,6 +34,7 @@ struct Ptrs {
   int32_t* cell_count;
   int32_t* cell_start;   // ncell + 1
   int32_t* cell_idx;     // n
+  int32_t* scan_aux;     // 2 * scan_tiles(ncell) + 1: tile totals, tile offsets, ticket (zeroed)
   int32_t* err;          // NERR
   Clock* clock;
   double* partials;      // reduction scratch
@@ -43,7 +44,20 @@ struct Ptrs {
   int32_t* nbr_idx;      // K * n
   double* nbr_f;         // K * n
   int K;                 // list capacity per particle
+  // mixed-precision form (precision = 1): FP32 neighbour records
+  float* recAf;          // RAF * n
+  float* recBf;          // RBF * n
 };
+
+// Mixed-precision neighbour records, float4-aligned per particle. A position
+// x is carried as the float pair (hi, lo), hi = fl(x), lo = fl(x - hi), so a
+// difference of nearby positions keeps full FP32 precision.
+//   A: xhi0 xhi1 xhi2 m | xlo0 xlo1 xlo2 0 | m*ext_s m*ext_B m*ext_S m*ext_Q
+//   B: xhi0 xhi1 xhi2 m | xlo0 xlo1 xlo2 p/sl^2 | e Pi/sl^2 v0 v1 |
+//      v2 pi01/sl^2 pi02/sl^2 pi03/sl^2 | pi11 pi12 pi13 pi22 | pi23 pi33 0 0
+//      (the pi^{ij} entries divided by sl^2 as well)
+constexpr int RAF = 12;
+constexpr int RBF = 24;
 
 // Pass A modes
 enum : int { A_SMOOTH_ONLY = 0, A_WITH_THERMO = 1 };
@@ -63,9 +77,16 @@ void launch_totals(const RunConst& rc, const Ptrs& p, int nblocks, cudaStream_t 
 void launch_neighbour_counts(const RunConst& rc, const Ptrs& p, int32_t* counts, cudaStream_t s);
 void launch_neighbour_fill(const RunConst& rc, const Ptrs& p, const int32_t* offsets, int32_t* idx,
                            cudaStream_t s);
+void launch_pack_fp64(const RunConst& rc, const Ptrs& p, cudaStream_t s);
+void launch_pack_mixed(const RunConst& rc, const Ptrs& p, cudaStream_t s);
+void launch_passA_mixed(const RunConst& rc, const EosDev& eos, const Ptrs& p, cudaStream_t s);
+void launch_passB_mixed(const RunConst& rc, const Ptrs& p, int mode, double dt_sub, cudaStream_t s);
 void launch_eos_batch(const EosDev& eos, int entropy, int64_t n, const double* in4, double* tbqs, double* th16,
                       int32_t* status, int32_t* iters, cudaStream_t s);
 
 constexpr int kTotBlocks = 608;   // 4 x 152 SMs; fixed so the sums are reproducible
+
+// CTAs of the cell-count scan (1024 cells each)
+inline int scan_tiles(int ncell) { return (ncell + 1023) / 1024; }
 
 }  // namespace ccake

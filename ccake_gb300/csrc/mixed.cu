@@ -1,0 +1,260 @@
+// Mixed-precision form of the two fused passes (ccake_config.precision = 1).
+//
+// The pair loops run in FP32: positions travel as (hi, lo) float pairs, so a
+// pair displacement (hi_a - hi_b) + (lo_a - lo_b) keeps FP32 precision even
+// where |x| >> |dx|; W, the grad-W factor and every pair sum are FP32, the sums
+// Kahan-compensated. The per-particle work that decides accuracy stays FP64:
+// the EoS Newton inversion, pi^{mu nu} reconstruction, the RK2 state update
+// and the conservation sums; the equations of motion run in FP32.
+//
+// FP64 on this part is a narrow pipe (one FP64 warp instruction costs as much
+// pipe time as 64 FP32 ones), so moving the pair loops off it removes the
+// bound the FP64 passes sit on. The neighbour set is decided by the FP32
+// predicate; pairs it classifies differently from the FP64 predicate lie at
+// |r_a - r_b| = 2h to FP32 rounding, where W and grad W vanish as (2 - q)^3
+// and (2 - q)^2.
+#include "kernels.cuh"
+#include "passes.cuh"
+#include "physics.cuh"
+
+namespace ccake {
+
+namespace {
+
+using namespace passes;
+
+// Packs the mixed smoothing record from the FP64 state (before the first
+// mixed substep, and whenever FP64 passes moved the particles last).
+template <int D>
+__global__ void k_pack_mixed(Ptrs p) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.n) return;
+  const int n = p.n;
+  const double x[3] = {p.y[Y_X0 * n + i], p.y[Y_X1 * n + i], D == 3 ? p.y[Y_X2 * n + i] : 0.0};
+  const double ext[4] = {p.y[Y_ES * n + i], p.y[Y_EB * n + i], p.y[Y_ESS * n + i], p.y[Y_EQ * n + i]};
+  write_recAf<D>(p, i, x, p.m[i], ext);
+}
+
+// Pass A, mixed form: smoothing sums (sigma_lab and the four extensive
+// densities, src/sph_workstation.cpp:495-578 of the reference), the
+// per-substep neighbour list with FP32 grad-W factors.
+template <int D>
+__global__ void __launch_bounds__(kBlock) k_passA_mixed(RunConst rc, Ptrs p) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.n) return;
+  const int n = p.n;
+  const double t = p.clock->t;
+  const float4* ra = reinterpret_cast<const float4*>(p.recAf);
+  constexpr int SA = RAF / 4;
+  const float4 ah = ra[(size_t)i * SA], al = ra[(size_t)i * SA + 1], ae = ra[(size_t)i * SA + 2];
+  const float k0 = (float)rc.k0;
+  KSum sl, s0, s1, s2, s3;
+  sl.init(ah.w * k0);
+  s0.init(ae.x * k0);
+  s1.init(ae.y * k0);
+  s2.init(ae.z * k0);
+  s3.init(ae.w * k0);
+  const float cut2 = (float)rc.cut2, ih = (float)rc.inv_h;
+  const float wn = (float)rc.wn, wn2 = (float)rc.wn2, gn = (float)rc.gn, gn2 = (float)rc.gn2;
+  const int K = p.K;
+  float* nf = reinterpret_cast<float*>(p.nbr_f);
+  const double xa[3] = {p.y[Y_X0 * n + i], p.y[Y_X1 * n + i], D == 3 ? p.y[Y_X2 * n + i] : 0.0};
+  int rlo[D == 3 ? 9 : 3], rhi[D == 3 ? 9 : 3];
+  const int nr = neighbour_ranges<D>(rc.grid, p.cell_start, xa, rlo, rhi);
+  int nn = 0;
+  for (int r = 0; r < nr; r++) {
+    for (int j = rlo[r]; j < rhi[r]; j++) {
+      const int b = p.cell_idx[j];
+      if (b == i) continue;
+      const float4 bh = __ldg(&ra[(size_t)b * SA]), bl = __ldg(&ra[(size_t)b * SA + 1]);
+      const float dx = (ah.x - bh.x) + (al.x - bl.x);
+      const float dy = (ah.y - bh.y) + (al.y - bl.y);
+      const float dz = (D == 3) ? (ah.z - bh.z) + (al.z - bl.z) : 0.0f;
+      const float d2 = dx * dx + dy * dy + dz * dz;
+      if (!(d2 <= cut2)) continue;
+      // W (src/kernel.cpp:34-48) and grad_a W = fg (r_a - r_b) (:95-118)
+      const float rs = d2 > 0.0f ? rsqrtf(d2) : 0.0f;
+      const float q = d2 * rs * ih;
+      const float z = fmaxf(2.0f - q, 0.0f), qq = q * q;
+      const float W = q < 1.0f ? wn * (1.0f - 1.5f * qq + 0.75f * q * qq) : wn2 * z * z * z;
+      const float fg = q < 1.0f ? gn2 * (1.5f * q - 2.0f) * ih : gn * rs * z * z;
+      if (nn < K) {
+        p.nbr_idx[(size_t)nn * n + i] = b;
+        nf[(size_t)nn * n + i] = fg;
+      }
+      nn++;
+      const float4 be = __ldg(&ra[(size_t)b * SA + 2]);
+      sl.add(bh.w * W);
+      s0.add(be.x * W);
+      s1.add(be.y * W);
+      s2.add(be.z * W);
+      s3.add(be.w * W);
+    }
+  }
+  if (nn > K) atomicAdd(&p.err[E_NBR_OVERFLOW], 1);
+  const double u3[3] = {p.y[Y_U0 * n + i], p.y[Y_U1 * n + i], D == 3 ? p.y[Y_U2 * n + i] : 0.0};
+  const double g = gamma_milne<D>(u3, t * t);
+  p.gam[i] = g;
+#pragma unroll
+  for (int q = 0; q < 3; q++) p.v[q * n + i] = (q < D) ? u3[q] / g : 0.0;
+  const double slab = sl.value64();
+  const double igt = 1.0 / (g * t);
+  p.slab[i] = slab;
+  p.sig[i] = slab * igt;
+  p.th[T_S * n + i] = s0.value64() * igt;
+  p.th[T_RB * n + i] = s1.value64() * igt;
+  p.th[T_RS * n + i] = s2.value64() * igt;
+  p.th[T_RQ * n + i] = s3.value64() * igt;
+  p.btrack[i] = nn;
+}
+
+// EoS inversion and the mixed gradient record, as a kernel of its own: the
+// FP64 Newton solve needs ~255 registers a thread, which would cap the
+// occupancy of the gather loop above at 8 warps an SM.
+template <int D>
+__global__ void __launch_bounds__(kBlock) k_thermo_mixed(RunConst rc, EosDev eos, Ptrs p) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.n) return;
+  thermo_tail<D, true>(rc, eos, p, i, p.clock->t);
+}
+
+// Pass B, mixed form: separable gradient sums over the list pass A wrote,
+// FP32 with Kahan compensation (the separable forms of
+// src/sph_workstation.cpp:797-986), then the FP32 equations of motion and the
+// FP64 RK2 update.
+template <int D>
+__global__ void __launch_bounds__(kBlock) k_passB_mixed(RunConst rc, Ptrs p, int mode, double dt_sub) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.n) return;
+  const int n = p.n;
+  const double t = p.clock->t;
+  const bool shear = rc.cfg.using_shear;
+  constexpr int SB = RBF / 4;
+  const float4* rbf = reinterpret_cast<const float4*>(p.recBf);
+  const float4 A0 = rbf[(size_t)i * SB], A1 = rbf[(size_t)i * SB + 1], A2 = rbf[(size_t)i * SB + 2];
+  const float4 A3 = rbf[(size_t)i * SB + 3], A4 = rbf[(size_t)i * SB + 4], A5 = rbf[(size_t)i * SB + 5];
+  KSum S1[D], SP[D], SE[D], SB_[D], SV[D][D], S0[D][D], SD[D];
+#pragma unroll
+  for (int k = 0; k < D; k++) {
+    S1[k].init(0.0f);
+    SP[k].init(0.0f);
+    SE[k].init(0.0f);
+    SB_[k].init(0.0f);
+    SD[k].init(0.0f);
+#pragma unroll
+    for (int l = 0; l < D; l++) {
+      SV[k][l].init(0.0f);
+      S0[k][l].init(0.0f);
+    }
+  }
+  const float* nf = reinterpret_cast<const float*>(p.nbr_f);
+  const int cnt = min(p.btrack[i], p.K);
+  for (int kk = 0; kk < cnt; kk++) {
+    const int b = p.nbr_idx[(size_t)kk * n + i];
+    const float fg = nf[(size_t)kk * n + i];
+    const float4* rb = rbf + (size_t)b * SB;
+    const float4 B0 = __ldg(rb), B1 = __ldg(rb + 1), B2 = __ldg(rb + 2);
+    const float d[3] = {(A0.x - B0.x) + (A1.x - B1.x), (A0.y - B0.y) + (A1.y - B1.y),
+                        (D == 3) ? (A0.z - B0.z) + (A1.z - B1.z) : 0.0f};
+    const float mf = B0.w * fg;
+    float gm[D];
+#pragma unroll
+    for (int k = 0; k < D; k++) gm[k] = mf * d[k];
+    float vb[3] = {B2.z, B2.w, 0.0f};
+    float4 B3 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (D == 3 || shear) B3 = __ldg(rb + 3);
+    if (D == 3) vb[2] = B3.x;
+#pragma unroll
+    for (int k = 0; k < D; k++) {
+      S1[k].add(gm[k]);
+      SP[k].add(B1.w * gm[k]);
+      SE[k].add(B2.x * gm[k]);
+      SB_[k].add(B2.y * gm[k]);
+#pragma unroll
+      for (int l = 0; l < D; l++) SV[k][l].add(vb[l] * gm[k]);
+    }
+    if (shear) {
+      const float4 B4 = __ldg(rb + 4);
+      const float4 B5 = (D == 3) ? __ldg(rb + 5) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      const float p0[3] = {B3.y, B3.z, B3.w};
+      // pi^{ij}/sl^2 packed (11 12 13 22 23 33)
+      const float pij[6] = {B4.x, B4.y, B4.z, B4.w, B5.x, B5.y};
+#pragma unroll
+      for (int k = 0; k < D; k++) {
+#pragma unroll
+        for (int l = 0; l < D; l++) S0[k][l].add(p0[l] * gm[k]);
+        float acc = 0.0f;
+#pragma unroll
+        for (int l = 0; l < D; l++) {
+          const int lo = k < l ? k : l, hi = k < l ? l : k;
+          acc += pij[lo == 0 ? hi : (lo == 1 ? 2 + hi : 5)] * gm[l];
+        }
+        SD[k].add(acc);
+      }
+    }
+  }
+  // own values from the same FP32 record as the neighbours', so that a
+  // uniform field gives a zero gradient up to the compensated sums' error
+  const float sla = (float)p.slab[i], isla = 1.0f / sla;
+  const float ea = A2.x, Pa = A1.w, Pia = A2.y;
+  const float va[3] = {A2.z, A2.w, D == 3 ? A3.x : 0.0f};
+  const float pi0a[3] = {A3.y, A3.z, A3.w};
+  const float pija[6] = {A4.x, A4.y, A4.z, A4.w, A5.x, A5.y};
+  float s1v[D];
+#pragma unroll
+  for (int k = 0; k < D; k++) s1v[k] = S1[k].value();
+  float gP[3] = {0, 0, 0}, gE[3] = {0, 0, 0}, gB[3] = {0, 0, 0}, gS[3] = {0, 0, 0}, dS[3] = {0, 0, 0};
+  float gV[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  float vS1 = 0.0f;
+#pragma unroll
+  for (int k = 0; k < D; k++) vS1 += va[k] * s1v[k];
+#pragma unroll
+  for (int k = 0; k < D; k++) {
+    gP[k] = sla * (SP[k].value() + Pa * s1v[k]);
+    gE[k] = (SE[k].value() - ea * s1v[k]) * isla;
+    gB[k] = sla * (SB_[k].value() + Pia * s1v[k]);
+#pragma unroll
+    for (int l = 0; l < D; l++) gV[k * D + l] = (SV[k][l].value() - va[l] * s1v[k]) * isla;
+    if (shear) {
+      float acc = 0.0f;
+#pragma unroll
+      for (int l = 0; l < D; l++) acc += va[l] * S0[l][k].value();
+      gS[k] = sla * (acc + pi0a[k] * vS1);
+      float acc2 = SD[k].value();
+#pragma unroll
+      for (int l = 0; l < D; l++) {
+        const int lo = k < l ? k : l, hi = k < l ? l : k;
+        acc2 += pija[lo == 0 ? hi : (lo == 1 ? 2 + hi : 5)] * s1v[l];
+      }
+      dS[k] = sla * acc2;
+    }
+  }
+  finish_particle<D, float, true>(rc, p, i, mode, t, dt_sub, va, gP, gE, gB, gS, dS, gV);
+}
+
+}  // namespace
+
+void launch_pack_mixed(const RunConst& rc, const Ptrs& p, cudaStream_t s) {
+  const int nb = (p.n + kBlock - 1) / kBlock;
+  if (rc.cfg.dim == 3) k_pack_mixed<3><<<nb, kBlock, 0, s>>>(p);
+  else k_pack_mixed<2><<<nb, kBlock, 0, s>>>(p);
+}
+
+void launch_passA_mixed(const RunConst& rc, const EosDev& eos, const Ptrs& p, cudaStream_t s) {
+  const int nb = (p.n + kBlock - 1) / kBlock;
+  if (rc.cfg.dim == 3) {
+    k_passA_mixed<3><<<nb, kBlock, 0, s>>>(rc, p);
+    k_thermo_mixed<3><<<nb, kBlock, 0, s>>>(rc, eos, p);
+  } else {
+    k_passA_mixed<2><<<nb, kBlock, 0, s>>>(rc, p);
+    k_thermo_mixed<2><<<nb, kBlock, 0, s>>>(rc, eos, p);
+  }
+}
+
+void launch_passB_mixed(const RunConst& rc, const Ptrs& p, int mode, double dt_sub, cudaStream_t s) {
+  const int nb = (p.n + kBlock - 1) / kBlock;
+  if (rc.cfg.dim == 3) k_passB_mixed<3><<<nb, kBlock, 0, s>>>(rc, p, mode, dt_sub);
+  else k_passB_mixed<2><<<nb, kBlock, 0, s>>>(rc, p, mode, dt_sub);
+}
+
+}  // namespace ccake

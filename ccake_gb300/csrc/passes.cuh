@@ -1,0 +1,263 @@
+// Device pieces shared by the FP64 and the mixed-precision passes.
+#pragma once
+#include "kernels.cuh"
+#include "physics.cuh"
+
+namespace ccake {
+namespace passes {
+
+constexpr int kBlock = 128;
+constexpr int kSurv = 64;   // candidate chunk kept per thread in shared memory (pass A)
+
+// Row ranges [lo, hi) of the sorted cell list covering the 3^D neighbour
+// cells of a position (the cells of one (y, z) row are contiguous).
+template <int D>
+__device__ __forceinline__ int neighbour_ranges(const Grid& gr, const int32_t* cell_start, const double* xa,
+                                                int* rlo, int* rhi) {
+  int nr = 0;
+  const int cx = cell_coord(gr, 0, xa[0]), cy = cell_coord(gr, 1, xa[1]);
+  const int cz = (D == 3) ? cell_coord(gr, 2, xa[2]) : 0;
+  const int zlo = (D == 3) ? max(cz - 1, 0) : 0, zhi = (D == 3) ? min(cz + 1, gr.nc[2] - 1) : 0;
+  for (int z = zlo; z <= zhi; z++)
+    for (int y = max(cy - 1, 0); y <= min(cy + 1, gr.nc[1] - 1); y++) {
+      const int row = (z * gr.nc[1] + y) * gr.nc[0];
+      rlo[nr] = cell_start[row + max(cx - 1, 0)];
+      rhi[nr] = cell_start[row + min(cx + 1, gr.nc[0] - 1) + 1];
+      nr++;
+    }
+  return nr;
+}
+
+// FP32 screen of a candidate pair: false only when the FP32 squared distance
+// exceeds (2h)^2 by more than a bound on its FP32 error (per axis
+// 2^-22 (|x_a| + |x_b| + |dx|) before squaring, 4e-7 relative after), so every
+// pair the exact FP64 predicate accepts survives. d2f returns the FP32
+// squared distance, bound its error bound.
+template <int D>
+__device__ __forceinline__ bool maybe_neighbour(const float4& pa, const float4& pb, float cut2f, float& d2f,
+                                                float& bound) {
+  const float dxf = pa.x - pb.x, dyf = pa.y - pb.y, dzf = (D == 3) ? pa.z - pb.z : 0.0f;
+  const float ex = 2.4e-7f * (fabsf(pa.x) + fabsf(pb.x) + fabsf(dxf)) + 1e-30f;
+  const float ey = 2.4e-7f * (fabsf(pa.y) + fabsf(pb.y) + fabsf(dyf)) + 1e-30f;
+  const float ez = (D == 3) ? 2.4e-7f * (fabsf(pa.z) + fabsf(pb.z) + fabsf(dzf)) + 1e-30f : 0.0f;
+  d2f = dxf * dxf + dyf * dyf + dzf * dzf;
+  bound = ex * (2.0f * fabsf(dxf) + ex) + ey * (2.0f * fabsf(dyf) + ey) + ez * (2.0f * fabsf(dzf) + ez) + 4e-7f * d2f;
+  return !(d2f - bound > cut2f);
+}
+
+// Compensated (Kahan) FP32 sum: s - c carries the sum to about FP32
+// precision of the sum itself rather than of the sum of magnitudes.
+struct KSum {
+  float s, c;
+  __device__ __forceinline__ void init(float x) { s = x; c = 0.0f; }
+  __device__ __forceinline__ void add(float x) {
+    const float y = x - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+  __device__ __forceinline__ float value() const { return s - c; }
+  __device__ __forceinline__ double value64() const { return (double)s - (double)c; }
+};
+
+// x = hi + lo with hi = fl32(x): the pair carries x to ~2^-48 relative.
+__device__ __forceinline__ void split2(double x, float& hi, float& lo) {
+  hi = (float)x;
+  lo = (float)(x - (double)hi);
+}
+
+// Smoothing record of particle i (FP64 form, plus the FP32 screen copy).
+template <int D>
+__device__ __forceinline__ void write_recA(const Ptrs& p, int i, const double* x, double m, const double* ext) {
+  double2* ra = reinterpret_cast<double2*>(p.recA) + (size_t)i * 4;
+  ra[0] = make_double2(x[0], x[1]);
+  ra[1] = make_double2(D == 3 ? x[2] : 0.0, m);
+  ra[2] = make_double2(m * ext[0], m * ext[1]);
+  ra[3] = make_double2(m * ext[2], m * ext[3]);
+  p.posf[i] = make_float4((float)x[0], (float)x[1], D == 3 ? (float)x[2] : 0.0f, 0.0f);
+}
+
+// Smoothing record of particle i (mixed form).
+template <int D>
+__device__ __forceinline__ void write_recAf(const Ptrs& p, int i, const double* x, double m, const double* ext) {
+  float hi[3], lo[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) split2(k < D ? x[k] : 0.0, hi[k], lo[k]);
+  float4* ra = reinterpret_cast<float4*>(p.recAf) + (size_t)i * (RAF / 4);
+  ra[0] = make_float4(hi[0], hi[1], hi[2], (float)m);
+  ra[1] = make_float4(lo[0], lo[1], lo[2], 0.0f);
+  ra[2] = make_float4((float)(m * ext[0]), (float)(m * ext[1]), (float)(m * ext[2]), (float)(m * ext[3]));
+}
+
+// EoS inversion of the smoothed densities of particle i, pi^{mu nu} and Pi
+// from the extensive forms, and its gradient record (FP64 or mixed form).
+template <int D, bool MIX>
+__device__ __forceinline__ void thermo_tail(const RunConst& rc, const EosDev& eos, const Ptrs& p, int i, double t) {
+  const int n = p.n;
+  const double t2 = t * t;
+  double th[NTH];
+  double x[4] = {p.th[T_T * n + i], p.th[T_MUB * n + i], p.th[T_MUQ * n + i], p.th[T_MUS * n + i]};
+  const double tgt[4] = {p.th[T_S * n + i], p.th[T_RB * n + i], p.th[T_RS * n + i], p.th[T_RQ * n + i]};
+  int iters = 0;
+  double o[17];
+  const int k = eos_invert(eos, 1, tgt, p.eos_id[i], x, &iters, MIX ? 1 : 0, o);
+  if (k < 0) {
+    atomicAdd(&p.err[E_EOS], 1);
+    return;
+  }
+  set_thermo_o(eos, k, x, o, th);
+#pragma unroll
+  for (int q = 0; q < NTH; q++) p.th[q * n + i] = th[q];
+  p.eos_id[i] = k;
+  p.eos_iters[i] = iters;
+  // pi^{mu nu} and Pi from the extensive forms
+  const double sig = p.sig[i], g = p.gam[i], slab = p.slab[i];
+  double u3[3] = {p.y[Y_U0 * n + i], p.y[Y_U1 * n + i], D == 3 ? p.y[Y_U2 * n + i] : 0.0};
+  double es[5];
+#pragma unroll
+  for (int q = 0; q < 5; q++) es[q] = p.y[(Y_SHV0 + q) * n + i];
+  double pi[NPI];
+  reset_pi(es, sig, g, u3, t2, pi);
+  const double Pi = p.y[Y_EBULK * n + i] * sig;
+  p.bulk[i] = Pi;
+#pragma unroll
+  for (int q = 0; q < NPI; q++) p.pi[q * n + i] = pi[q];
+  // neighbour record B
+  const double isl2 = 1.0 / (slab * slab);
+  if constexpr (MIX) {
+    float hi[3], lo[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) split2(k < D ? p.y[(Y_X0 + k) * n + i] : 0.0, hi[k], lo[k]);
+    const float f = (float)isl2;
+    float4* rb = reinterpret_cast<float4*>(p.recBf) + (size_t)i * (RBF / 4);
+    rb[0] = make_float4(hi[0], hi[1], hi[2], (float)p.m[i]);
+    rb[1] = make_float4(lo[0], lo[1], lo[2], (float)(th[T_P] * isl2));
+    rb[2] = make_float4((float)th[T_E], (float)(Pi * isl2), (float)p.v[i], (float)p.v[n + i]);
+    rb[3] = make_float4((float)p.v[2 * n + i], (float)pi[pi_slot(0, 1)] * f, (float)pi[pi_slot(0, 2)] * f,
+                        (float)pi[pi_slot(0, 3)] * f);
+    rb[4] = make_float4((float)pi[P11] * f, (float)pi[P12] * f, (float)pi[P13] * f, (float)pi[P22] * f);
+    rb[5] = make_float4((float)pi[P23] * f, (float)pi[P33] * f, 0.0f, 0.0f);
+  } else {
+    double* rb = p.recB + (size_t)i * RB;
+    rb[B_X0] = p.y[Y_X0 * n + i];
+    rb[B_X1] = p.y[Y_X1 * n + i];
+    rb[B_X2] = D == 3 ? p.y[Y_X2 * n + i] : 0.0;
+    rb[B_M] = p.m[i];
+    rb[B_P] = th[T_P] * isl2;
+    rb[B_E] = th[T_E];
+    rb[B_PI] = Pi * isl2;
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      rb[B_V0 + q] = p.v[q * n + i];
+      rb[B_PI0 + q] = pi[pi_slot(0, q + 1)] * isl2;
+    }
+    rb[B_PIJ + 0] = pi[P11] * isl2;
+    rb[B_PIJ + 1] = pi[P12] * isl2;
+    rb[B_PIJ + 2] = pi[P13] * isl2;
+    rb[B_PIJ + 3] = pi[P22] * isl2;
+    rb[B_PIJ + 4] = pi[P23] * isl2;
+    rb[B_PIJ + 5] = pi[P33] * isl2;
+  }
+}
+
+// Everything of pass B after the gradients, for particle i: optional export
+// of the gradients, the equations of motion (in type R), optional export of
+// the derivatives, the midpoint RK2 update of the FP64 state from the
+// step-start cache (reference src/evolver.cpp:344-486) and the smoothing
+// record for the next substep (FP64 or mixed form).
+template <int D, typename R, bool MIX>
+__device__ __forceinline__ void finish_particle(const RunConst& rc, const Ptrs& p, int i, int mode, double t,
+                                                double dt_sub, const R* va, const R* gP, const R* gE, const R* gB,
+                                                const R* gS, const R* dS, const R* gV) {
+  const int n = p.n;
+  if (mode & B_GRADS) {
+#pragma unroll
+    for (int k = 0; k < D; k++) {
+      p.grads[(G_P + k) * n + i] = gP[k];
+      p.grads[(G_E + k) * n + i] = gE[k];
+      p.grads[(G_B + k) * n + i] = gB[k];
+      p.grads[(G_SH + k) * n + i] = gS[k];
+      p.grads[(G_DS + k) * n + i] = dS[k];
+    }
+#pragma unroll
+    for (int k = 0; k < D * D; k++) p.grads[(G_V + k) * n + i] = gV[k];
+  }
+  if (!(mode & B_EOM)) return;
+  double th[NTH];
+#pragma unroll
+  for (int q = 0; q < NTH; q++) th[q] = p.th[q * n + i];
+  EomIn<D, R> in;
+  in.th = th;
+#pragma unroll
+  for (int q = 0; q < 3; q++) {
+    in.u[q] = (q < D) ? R(p.y[(Y_U0 + q) * n + i]) : R(0);
+    in.v[q] = va[q];
+    in.gradP[q] = gP[q];
+    in.gradBulk[q] = gB[q];
+    in.gradshear[q] = gS[q];
+    in.divshear[q] = dS[q];
+  }
+#pragma unroll
+  for (int q = 0; q < 9; q++) in.gradV[q] = gV[q];
+  in.g = R(p.gam[i]);
+  in.sigma = R(p.sig[i]);
+  in.sigma_lab = R(p.slab[i]);
+  in.m = R(p.m[i]);
+  in.Pi = R(p.bulk[i]);
+#pragma unroll
+  for (int q = 0; q < NPI; q++) in.pi[q] = R(p.pi[q * n + i]);
+  const Transport k = transport(rc.cfg, th);
+  EomOut<R> o;
+  eom<D, R>(rc.cfg, k, in, t, o);
+  if (mode & B_DERIVS) {
+#pragma unroll
+    for (int q = 0; q < 3; q++) p.derivs[(D_DU0 + q) * n + i] = (q < D) ? double(o.du[q]) : 0.0;
+    p.derivs[D_DS * n + i] = o.dS;
+    p.derivs[D_DBULK * n + i] = o.dBulk;
+#pragma unroll
+    for (int q = 0; q < 5; q++) p.derivs[(D_DSHV0 + q) * n + i] = o.dShv[q];
+    p.derivs[D_DEZ * n + i] = o.dEz;
+    p.derivs[D_ETA * n + i] = k.eta;
+    p.derivs[D_TAUPI * n + i] = k.tau_pi;
+    p.derivs[D_ZETA * n + i] = k.zeta;
+    p.derivs[D_TAUBULK * n + i] = k.tau_Pi;
+  }
+  if (!(mode & B_UPDATE)) return;
+  const double* y0 = p.y0;
+  double ynew[NY];
+#pragma unroll
+  for (int q = 0; q < NY; q++) ynew[q] = y0[q * n + i];
+#pragma unroll
+  for (int q = 0; q < D; q++) {
+    ynew[Y_X0 + q] += dt_sub * p.v[q * n + i];
+    ynew[Y_U0 + q] += dt_sub * double(o.du[q]);
+  }
+  double es = ynew[Y_ES] + dt_sub * double(o.dS);
+  ynew[Y_EBULK] += dt_sub * double(o.dBulk);
+#pragma unroll
+  for (int q = 0; q < 5; q++) ynew[Y_SHV0 + q] += dt_sub * double(o.dShv[q]);
+  ynew[Y_EZ] += dt_sub * double(o.dEz);
+  if (es < 0.0) {
+    if (p.freeze[i] > 3) es = 1.e-3;
+    else atomicAdd(&p.err[E_NEGS], 1);
+  }
+  ynew[Y_ES] = es;
+  bool finite = true;
+#pragma unroll
+  for (int q = 0; q < NY; q++) finite = finite && isfinite(ynew[q]);
+  if (!finite) atomicAdd(&p.err[E_NONFINITE], 1);
+#pragma unroll
+  for (int q = 0; q < NY; q++) p.y[q * n + i] = ynew[q];
+  if (mode & B_WRITE_Y0) {
+#pragma unroll
+    for (int q = 0; q < NY; q++) p.y0[q * n + i] = ynew[q];
+  }
+  const double x[3] = {ynew[Y_X0], ynew[Y_X1], D == 3 ? ynew[Y_X2] : 0.0};
+  const double ext[4] = {ynew[Y_ES], ynew[Y_EB], ynew[Y_ESS], ynew[Y_EQ]};
+  if constexpr (MIX) write_recAf<D>(p, i, x, p.m[i], ext);
+  else write_recA<D>(p, i, x, p.m[i], ext);
+}
+
+
+}  // namespace passes
+}  // namespace ccake

@@ -79,105 +79,114 @@ __device__ inline void reset_pi(const double* ext_shv, double sigma, double g, c
 }
 
 // Inputs of the equations of motion for one particle.
-template <int D>
+template <int D, typename R = double>
 struct EomIn {
-  double u[3], v[3];
-  double g, sigma, sigma_lab, m;
-  const double* th;          // NTH thermo values
-  double Pi;                 // bulk pressure
-  double pi[NPI];            // pi^{mu nu}
-  double gradP[3], gradBulk[3], gradshear[3], divshear[3], gradV[9];
+  R u[3], v[3];
+  R g, sigma, sigma_lab, m;
+  const double* th;          // NTH thermo values (FP64, from the EoS)
+  R Pi;                      // bulk pressure
+  R pi[NPI];                 // pi^{mu nu}
+  R gradP[3], gradBulk[3], gradshear[3], divshear[3], gradV[9];
 };
 
+template <typename R = double>
 struct EomOut {
-  double du[3], dS, dBulk, dShv[5], dEz;
+  R du[3], dS, dBulk, dShv[5], dEz;
 };
 
 // Reference src/eom_default.cpp:211-869 (evaluate_time_derivatives) and
 // :882-1412 (calculate_MRF_shear), without sources and without the diffusion
 // sector, for one particle at time t.
-template <int D>
-__device__ inline void eom(const ccake_config& cfg, const Transport& k, const EomIn<D>& in, double t, EomOut& o) {
-  const double t2 = t * t;
-  const double g = in.g, sig = in.sigma;
+// R = double is the plain FP64 form; R = float is the mixed form's EoM (the
+// state update it feeds stays FP64).
+template <int D, typename R = double>
+__device__ inline void eom(const ccake_config& cfg, const Transport& kd, const EomIn<D, R>& in, double td,
+                           EomOut<R>& o) {
+  const R t = R(td);
+  struct {
+    R eta, tau_pi, zeta, tau_Pi, delta_PiPi, delta_pipi, lambda_piPi, lambda_Pipi, phi1, phi3, phi6, phi7, tau_pipi;
+  } k{R(kd.eta), R(kd.tau_pi), R(kd.zeta), R(kd.tau_Pi), R(kd.delta_PiPi), R(kd.delta_pipi), R(kd.lambda_piPi),
+      R(kd.lambda_Pipi), R(kd.phi1), R(kd.phi3), R(kd.phi6), R(kd.phi7), R(kd.tau_pipi)};
+  const R t2 = t * t;
+  const R g = in.g, sig = in.sigma;
   // reciprocals: FP64 division is a long instruction sequence on the scarce
   // FP64 pipe, so each divisor is inverted once
-  const double ig = 1.0 / g, it = 1.0 / t, it2 = 1.0 / t2;
-  const double k13 = 1.0 / 3.0, k16 = 1.0 / 6.0;
+  const R ig = R(1.0) / g, it = R(1.0) / t, it2 = R(1.0) / t2;
+  const R k13 = R(1.0) / R(3.0), k16 = R(1.0) / R(6.0);
   const double* th = in.th;
-  const double T = th[T_T], w = th[T_W], sden = th[T_S], dwds = th[T_DWDS];
-  const double rho[3] = {th[T_RB], th[T_RS], th[T_RQ]};
-  const double dwdr[3] = {th[T_DWDB], th[T_DWDSS], th[T_DWDQ]};
-  const double Pi = in.Pi;
+  const R T = R(th[T_T]), w = R(th[T_W]), sden = R(th[T_S]), dwds = R(th[T_DWDS]);
+  const R rho[3] = {R(th[T_RB]), R(th[T_RS]), R(th[T_RQ])};
+  const R dwdr[3] = {R(th[T_DWDB]), R(th[T_DWDSS]), R(th[T_DWDQ])};
+  const R Pi = in.Pi;
   auto P = [&](int i, int j) { return in.pi[pi_slot(i, j)]; };
   // covariant spatial velocity (Vector<D>::make_covariant)
-  double u[3] = {in.u[0], in.u[1], D == 3 ? in.u[2] : 0.0};
-  double uc[3] = {-u[0], -u[1], D == 3 ? -t2 * u[2] : 0.0};
-  double divV = 0.0;
+  R u[3] = {in.u[0], in.u[1], D == 3 ? in.u[2] : R(0.0)};
+  R uc[3] = {-u[0], -u[1], D == 3 ? -t2 * u[2] : R(0.0)};
+  R divV = R(0.0);
 #pragma unroll
   for (int i = 0; i < D; i++) divV += in.gradV[i * D + i];
-  const double uD = u[D - 1];
-  const double geo = (D == 3) ? uD * uD * t * ig : 0.0;
-  const double expn = g * divV + g * it + geo;
-  auto dEta = [](int i) { return (D == 3 && i == 2) ? 1.0 : 0.0; };
+  const R uD = u[D - 1];
+  const R geo = (D == 3) ? uD * uD * t * ig : R(0.0);
+  const R expn = g * divV + g * it + geo;
+  auto dEta = [](int i) { return (D == 3 && i == 2) ? R(1.0) : R(0.0); };
 
   // ---- shear MRFs --------------------------------------------------------
-  double M0i[9] = {0}, F0i[3] = {0}, Mnab[3] = {0}, Fnab = 0.0;
-  double Mext[5][3] = {{0}}, Fext[5] = {0};
-  double ss = 0.0;   // pi^{mu nu} pi_{mu nu}
+  R M0i[9] = {0}, F0i[3] = {0}, Mnab[3] = {0}, Fnab = R(0.0);
+  R Mext[5][3] = {{0}}, Fext[5] = {0};
+  R ss = R(0.0);   // pi^{mu nu} pi_{mu nu}
   if (cfg.using_shear) {
-    const double cmd[4] = {1.0, -1.0, -1.0, -1.0 * it * it};
-    const double eta = k.eta, phi6 = k.phi6, phi7 = k.phi7, lpP = k.lambda_piPi;
-    const double tpp = k.tau_pipi, dpp = k.delta_pipi, tpi = k.tau_pi;
-    const double tdelta = dpp - tpi;
-    const double itg = 1.0 / (tpi * g), istg = 1.0 / (sig * tpi * g);
-    const double v[3] = {in.v[0], in.v[1], D == 3 ? in.v[2] : 0.0};
-    const double fu[3] = {u[0], u[1], u[2]};
-    const double fuc[3] = {-u[0], -u[1], -t2 * u[2]};
-    double pi[4][4], hy[4][4];
+    const R cmd[4] = {R(1.0), -R(1.0), -R(1.0), -R(1.0) * it * it};
+    const R eta = k.eta, phi6 = k.phi6, phi7 = k.phi7, lpP = k.lambda_piPi;
+    const R tpp = k.tau_pipi, dpp = k.delta_pipi, tpi = k.tau_pi;
+    const R tdelta = dpp - tpi;
+    const R itg = R(1.0) / (tpi * g), istg = R(1.0) / (sig * tpi * g);
+    const R v[3] = {in.v[0], in.v[1], D == 3 ? in.v[2] : R(0.0)};
+    const R fu[3] = {u[0], u[1], u[2]};
+    const R fuc[3] = {-u[0], -u[1], -t2 * u[2]};
+    R pi[4][4], hy[4][4];
 #pragma unroll
     for (int i = 0; i < 4; i++)
 #pragma unroll
       for (int j = 0; j < 4; j++) {
         pi[i][j] = P(i, j);
-        hy[i][j] = pi[i][j] * ((j == 1 || j == 2) ? -1.0 : (j == 3 ? -t2 : 1.0));   // pi^mu_nu
+        hy[i][j] = pi[i][j] * ((j == 1 || j == 2) ? -R(1.0) : (j == 3 ? -t2 : R(1.0)));   // pi^mu_nu
       }
 #pragma unroll
     for (int i = 0; i < 4; i++)
 #pragma unroll
-      for (int j = 0; j < 4; j++) ss += pi[i][j] * hy[i][j] * ((i == 1 || i == 2) ? -1.0 : (i == 3 ? -t2 : 1.0));
-    double gu[3][3] = {{0}}, gu0[3] = {0}, cgu[3][3] = {{0}};
+      for (int j = 0; j < 4; j++) ss += pi[i][j] * hy[i][j] * ((i == 1 || i == 2) ? -R(1.0) : (i == 3 ? -t2 : R(1.0)));
+    R gu[3][3] = {{0}}, gu0[3] = {0}, cgu[3][3] = {{0}};
 #pragma unroll
     for (int i = 0; i < D; i++)
 #pragma unroll
       for (int j = 0; j < D; j++) {
-        double acc = g * in.gradV[i * D + j];
+        R acc = g * in.gradV[i * D + j];
 #pragma unroll
         for (int kk = 0; kk < D; kk++) acc += -g * u[j] * uc[kk] * in.gradV[i * D + kk];
         gu[i][j] = acc;
       }
 #pragma unroll
     for (int i = 0; i < D; i++) {
-      double acc = 0;
+      R acc = 0;
 #pragma unroll
       for (int j = 0; j < D; j++) acc += gu[i][j] * uc[j];
-      gu0[i] = -1. * acc * ig;
+      gu0[i] = -R(1.) * acc * ig;
 #pragma unroll
-      for (int j = 0; j < D; j++) cgu[i][j] = gu[i][j] * ((D == 2 || i < D - 1) ? -1.0 : -1.0 * it2);
+      for (int j = 0; j < D; j++) cgu[i][j] = gu[i][j] * ((D == 2 || i < D - 1) ? -R(1.0) : -R(1.0) * it2);
     }
-    double gu0c[3] = {-gu0[0], -gu0[1], D == 3 ? -gu0[2] * it2 : 0.0};
-    double guv[3] = {0, 0, 0}, gu0v = 0.0;
+    R gu0c[3] = {-gu0[0], -gu0[1], D == 3 ? -gu0[2] * it2 : R(0.0)};
+    R guv[3] = {0, 0, 0}, gu0v = R(0.0);
 #pragma unroll
     for (int j = 0; j < D; j++) {
 #pragma unroll
       for (int kk = 0; kk < D; kk++) guv[j] += gu[kk][j] * v[kk];
       gu0v += gu0[j] * v[j];
     }
-    double vgs[3], ggs[3], sgu[3], vsg[3], sl0[3];
-    double sgu_s = 0.0;
+    R vgs[3], ggs[3], sgu[3], vsg[3], sl0[3];
+    R sgu_s = R(0.0);
 #pragma unroll
     for (int i = 0; i < D; i++) {
-      double a1 = 0, a2 = 0, a3 = 0, a4 = 0, a5 = 0;
+      R a1 = 0, a2 = 0, a3 = 0, a4 = 0, a5 = 0;
 #pragma unroll
       for (int j = 0; j < D; j++) {
         a1 += guv[j] * hy[i + 1][j + 1];
@@ -192,55 +201,55 @@ __device__ inline void eom(const ccake_config& cfg, const Transport& k, const Eo
       sgu[i] = a3;
       vsg[i] = a4;
 #pragma unroll
-      for (int j = 0; j < 4; j++) a5 += (pi[0][j] * hy[i + 1][j] + pi[i + 1][j] * hy[0][j]) / 2.;
+      for (int j = 0; j < 4; j++) a5 += (pi[0][j] * hy[i + 1][j] + pi[i + 1][j] * hy[0][j]) / R(2.);
       sl0[i] = a5;
     }
     // four-acceleration MRFs
-    const double uv = cfg.using_vorticity ? 1.0 : 0.0;
+    const R uv = cfg.using_vorticity ? R(1.0) : R(0.0);
 #pragma unroll
     for (int i = 0; i < D; i++) {
-      const double di = dEta(i);
-      double Fs = -(guv[i] - gu0c[i]) / 2. + u[i] * g * expn * k13 - g * geo * u[i] / 2.;
-      double FD = g * (u[i] * hy[0][0] + g * hy[i + 1][0]) * geo + t * uD * pi[3][i + 1] * di;
-      double Fds = -(vgs[i] - ggs[i] - 4. * g * u[i] * sgu_s * k13 - sgu[i] + vsg[i]) / 4. +
+      const R di = dEta(i);
+      R Fs = -(guv[i] - gu0c[i]) / R(2.) + u[i] * g * expn * k13 - g * geo * u[i] / R(2.);
+      R FD = g * (u[i] * hy[0][0] + g * hy[i + 1][0]) * geo + t * uD * pi[3][i + 1] * di;
+      R Fds = -(vgs[i] - ggs[i] - R(4.) * g * u[i] * sgu_s * k13 - sgu[i] + vsg[i]) / R(4.) +
                    (hy[i + 1][0] - g * g * hy[i + 1][0] - g * u[i] * hy[0][0] + pi[0][i + 1] +
-                    4. * u[i] * g * hy[0][0] * k13) * geo / 4. +
-                   (g * cmd[i + 1] * hy[0][3] * di * it + g * pi[3][0] * di * it + 4. * g * u[i] * (g * hy[3][3] * it) * k13) / 4. -
+                    R(4.) * u[i] * g * hy[0][0] * k13) * geo / R(4.) +
+                   (g * cmd[i + 1] * hy[0][3] * di * it + g * pi[3][0] * di * it + R(4.) * g * u[i] * (g * hy[3][3] * it) * k13) / R(4.) -
                    pi[0][i + 1] * (g * it + geo + g * divV) * k13;
-      double Fdo = -(vgs[i] - ggs[i] + sgu[i] - vsg[i]) / 4. +
-                   (hy[i + 1][0] - g * g * hy[i + 1][0] - g * u[i] * hy[0][0] - pi[0][i + 1]) * geo / 4. +
-                   (g * cmd[i + 1] * hy[0][3] * di * it - g * pi[3][0] * di * it) / 4.;
-      const double Fdd = pi[i + 1][0] * expn;
-      Fs += di * (-(-uD * t - uD * it + g * uD * uD * t + 2. * g * g * uD * it) / 2.);
+      R Fdo = -(vgs[i] - ggs[i] + sgu[i] - vsg[i]) / R(4.) +
+                   (hy[i + 1][0] - g * g * hy[i + 1][0] - g * u[i] * hy[0][0] - pi[0][i + 1]) * geo / R(4.) +
+                   (g * cmd[i + 1] * hy[0][3] * di * it - g * pi[3][0] * di * it) / R(4.);
+      const R Fdd = pi[i + 1][0] * expn;
+      Fs += di * (-(-uD * t - uD * it + g * uD * uD * t + R(2.) * g * g * uD * it) / R(2.));
       FD += di * (uD * pi[0][0] * it + g * pi[3][0] * it);
       if (D == 3) {
-        Fds += (t * uD * di * cmd[i + 1] * hy[0][0] + uD * hy[i + 1][3] * g * it / 4. + hy[i + 1][3] * t * uD +
+        Fds += (t * uD * di * cmd[i + 1] * hy[0][0] + uD * hy[i + 1][3] * g * it / R(4.) + hy[i + 1][3] * t * uD +
                 pi[0][0] * di * uD * it + t * uD * uD * (g * hy[i + 1][0] + u[i] * hy[0][0]) +
-                2. * g * uD * (g * hy[i + 1][3] + u[i] * pi[0][3]) * it) / 4. +
+                R(2.) * g * uD * (g * hy[i + 1][3] + u[i] * pi[0][3]) * it) / R(4.) +
                g * u[i] * (hy[3][0] * uD * t + uD * hy[0][3] * it) * k13;
         Fdo += (t * uD * di * cmd[i + 1] * hy[0][0] + uD * hy[i + 1][3] * g * it - hy[3][i + 1] * t * uD -
                 pi[0][0] * di * uD * it + t * uD * uD * (g * hy[i + 1][0] + u[i] * hy[0][0]) +
-                2. * g * uD * (g * hy[i + 1][3] + u[i] * pi[0][3]) * it) / 4.;
+                R(2.) * g * uD * (g * hy[i + 1][3] + u[i] * pi[0][3]) * it) / R(4.);
       }
-      F0i[i] = (-pi[i + 1][0] - tpi * FD - dpp * Fdd + 2. * tpi * Fdo * uv - tpp * Fds + (2. * eta + lpP * Pi) * Fs +
+      F0i[i] = (-pi[i + 1][0] - tpi * FD - dpp * Fdd + R(2.) * tpi * Fdo * uv - tpp * Fds + (R(2.) * eta + lpP * Pi) * Fs +
                 phi6 * Pi * pi[i + 1][0] + phi7 * (sl0[i] + g * u[i] * ss * k13)) * itg;
 #pragma unroll
       for (int j = 0; j < D; j++) {
-        double Ms = u[i] * uc[j] * k16;
-        const double MD = g * u[i] * (hy[0][j + 1] - hy[0][0] * uc[j] * ig) + g * g * (hy[i + 1][j + 1] - hy[i + 1][0] * uc[j] * ig);
-        double Mds = (hy[i + 1][j + 1] - hy[i + 1][0] * uc[j] * ig - g * g * hy[i + 1][j + 1] - g * u[i] * hy[0][j + 1] +
+        R Ms = u[i] * uc[j] * k16;
+        const R MD = g * u[i] * (hy[0][j + 1] - hy[0][0] * uc[j] * ig) + g * g * (hy[i + 1][j + 1] - hy[i + 1][0] * uc[j] * ig);
+        R Mds = (hy[i + 1][j + 1] - hy[i + 1][0] * uc[j] * ig - g * g * hy[i + 1][j + 1] - g * u[i] * hy[0][j + 1] +
                       uc[j] * g * hy[i + 1][0] + uc[j] * u[i] * hy[0][0] +
-                      4. * g * u[i] * (hy[0][j + 1] - hy[0][0] * uc[j] * ig) * k13 +
-                      (-pi[0][i + 1] + 4. * pi[0][i + 1] * k13) * uc[j] * ig) / 4.;
-        double Mdo = (hy[i + 1][j + 1] - hy[i + 1][0] * uc[j] * ig - g * g * hy[i + 1][j + 1] - g * u[i] * hy[0][j + 1] +
-                      uc[j] * g * hy[i + 1][0] + uc[j] * u[i] * hy[0][0] + pi[0][i + 1] * uc[j] * ig) / 4.;
-        const double Mdd = -pi[i + 1][0] * uc[j] * ig;
+                      R(4.) * g * u[i] * (hy[0][j + 1] - hy[0][0] * uc[j] * ig) * k13 +
+                      (-pi[0][i + 1] + R(4.) * pi[0][i + 1] * k13) * uc[j] * ig) / R(4.);
+        R Mdo = (hy[i + 1][j + 1] - hy[i + 1][0] * uc[j] * ig - g * g * hy[i + 1][j + 1] - g * u[i] * hy[0][j + 1] +
+                      uc[j] * g * hy[i + 1][0] + uc[j] * u[i] * hy[0][0] + pi[0][i + 1] * uc[j] * ig) / R(4.);
+        const R Mdd = -pi[i + 1][0] * uc[j] * ig;
         if (i == j) {
-          Ms += (1. - g * g) / 2.;
-          Mdo += -pi[0][0] / 4.;
-          Mds += +pi[0][0] / 4.;
+          Ms += (R(1.) - g * g) / R(2.);
+          Mdo += -pi[0][0] / R(4.);
+          Mds += +pi[0][0] / R(4.);
         }
-        M0i[i * D + j] = (-tpi * MD - dpp * Mdd + 2. * tpi * Mdo * uv - tpp * Mds + (2. * eta + lpP * Pi) * Ms) * itg;
+        M0i[i * D + j] = (-tpi * MD - dpp * Mdd + R(2.) * tpi * Mdo * uv - tpp * Mds + (R(2.) * eta + lpP * Pi) * Ms) * itg;
       }
     }
     // pi^{ij} nabla_i u_j MRF
@@ -253,79 +262,79 @@ __device__ inline void eom(const ccake_config& cfg, const Transport& k, const Eo
     }
     Fnab += +hy[3][3] * g * it + hy[0][0] * geo + (t * hy[3][0] + hy[0][3] * it) * uD * dEta(D - 1);
     // shear-tensor evolution MRFs on the (i <= j) entries of the 2x3 block
-    const double f2 = fu[2];
+    const R f2 = fu[2];
 #pragma unroll
     for (int i = 0; i < 2; i++) {
 #pragma unroll
       for (int j = i; j < 3; j++) {
         const int slot = (i == 0) ? j : 2 + j;   // (0,0)(0,1)(0,2)(1,1)(1,2) -> 0..4
-        const double di = dEta(i), dj = dEta(j);
-        double gugjs = 0, sigu = 0, vsig = 0, sml = 0;
+        const R di = dEta(i), dj = dEta(j);
+        R gugjs = 0, sigu = 0, vsig = 0, sml = 0;
 #pragma unroll
         for (int kk = 0; kk < D; kk++) {
-          const double cg_i = (i < D) ? cgu[i][kk] : 0.0, cg_j = (j < D) ? cgu[j][kk] : 0.0;
-          const double g3_j = (kk < D && j < D) ? gu[kk][j] : 0.0, g3_i = (i < D) ? gu[kk][i] : 0.0;
+          const R cg_i = (i < D) ? cgu[i][kk] : R(0.0), cg_j = (j < D) ? cgu[j][kk] : R(0.0);
+          const R g3_j = (kk < D && j < D) ? gu[kk][j] : R(0.0), g3_i = (i < D) ? gu[kk][i] : R(0.0);
           gugjs += cg_i * hy[j + 1][kk + 1] + cg_j * hy[i + 1][kk + 1];
           sigu += pi[kk + 1][i + 1] * g3_j + pi[kk + 1][j + 1] * g3_i;
           vsig += v[kk] * pi[0][i + 1] * g3_j + v[kk] * pi[0][j + 1] * g3_i;
         }
 #pragma unroll
-        for (int kk = 0; kk < 4; kk++) sml += (pi[i + 1][kk] * hy[j + 1][kk] + pi[j + 1][kk] * hy[i + 1][kk]) / 2.;
-        double FD2 = g * geo * (fu[i] * hy[j + 1][0] + fu[j] * hy[i + 1][0]);
-        const double cg_ij = (i < D && j < D) ? cgu[i][j] : 0.0, cg_ji = (i < D && j < D) ? cgu[j][i] : 0.0;
-        double Fsg = cg_ij / 2. + cg_ji / 2. + fu[i] * fu[j] * expn * k13;
-        const double Fdl = pi[i + 1][j + 1] * expn;
-        const double common = t * f2 * (cmd[i + 1] * hy[j + 1][0] * di + cmd[j + 1] * hy[i + 1][0] * dj) +
+        for (int kk = 0; kk < 4; kk++) sml += (pi[i + 1][kk] * hy[j + 1][kk] + pi[j + 1][kk] * hy[i + 1][kk]) / R(2.);
+        R FD2 = g * geo * (fu[i] * hy[j + 1][0] + fu[j] * hy[i + 1][0]);
+        const R cg_ij = (i < D && j < D) ? cgu[i][j] : R(0.0), cg_ji = (i < D && j < D) ? cgu[j][i] : R(0.0);
+        R Fsg = cg_ij / R(2.) + cg_ji / R(2.) + fu[i] * fu[j] * expn * k13;
+        const R Fdl = pi[i + 1][j + 1] * expn;
+        const R common = t * f2 * (cmd[i + 1] * hy[j + 1][0] * di + cmd[j + 1] * hy[i + 1][0] * dj) +
                               g * (cmd[i + 1] * hy[j + 1][3] * di + cmd[j + 1] * hy[i + 1][3] * dj) * it +
                               f2 * f2 * t * (fu[i] * hy[j + 1][0] + fu[j] * hy[i + 1][0]) +
-                              2. * g * f2 * (fu[i] * hy[j + 1][3] + fu[j] * hy[i + 1][3]) * it;
-        const double cross = g * (pi[3][i + 1] * dj + pi[3][j + 1] * di) * it + f2 * (pi[0][i + 1] * dj + pi[0][j + 1] * di) * it;
-        const double Fdo2 = -(-gugjs + sigu - vsig) / 4. + (-fu[i] * g * hy[j + 1][0] - fu[j] * g * hy[i + 1][0]) * geo / 4. +
-                            (common - cross) / 4.;
-        double Fds2 = -(-gugjs - sigu + vsig - 4. * (fu[i] * fu[j]) * sgu_s * k13) / 4. +
-                      (-fu[i] * g * hy[j + 1][0] - fu[j] * g * hy[i + 1][0] + 4. * fu[i] * fu[j] * hy[0][0] * k13) * geo / 4. +
-                      (common + cross + 4. * fu[i] * fu[j] * (hy[3][0] * f2 * t + g * hy[3][3] * it + f2 * hy[0][3] * it) * k13) / 4. -
+                              R(2.) * g * f2 * (fu[i] * hy[j + 1][3] + fu[j] * hy[i + 1][3]) * it;
+        const R cross = g * (pi[3][i + 1] * dj + pi[3][j + 1] * di) * it + f2 * (pi[0][i + 1] * dj + pi[0][j + 1] * di) * it;
+        const R Fdo2 = -(-gugjs + sigu - vsig) / R(4.) + (-fu[i] * g * hy[j + 1][0] - fu[j] * g * hy[i + 1][0]) * geo / R(4.) +
+                            (common - cross) / R(4.);
+        R Fds2 = -(-gugjs - sigu + vsig - R(4.) * (fu[i] * fu[j]) * sgu_s * k13) / R(4.) +
+                      (-fu[i] * g * hy[j + 1][0] - fu[j] * g * hy[i + 1][0] + R(4.) * fu[i] * fu[j] * hy[0][0] * k13) * geo / R(4.) +
+                      (common + cross + R(4.) * fu[i] * fu[j] * (hy[3][0] * f2 * t + g * hy[3][3] * it + f2 * hy[0][3] * it) * k13) / R(4.) -
                       pi[i + 1][j + 1] * (g * it + geo + g * divV) * k13;
         if (j == 2) {
           FD2 += g * pi[3][i + 1] * it + f2 * pi[0][i + 1] * it;
-          Fsg += -fu[i] * f2 * f2 * t / 2. - fu[i] * f2 * g * it;
+          Fsg += -fu[i] * f2 * f2 * t / R(2.) - fu[i] * f2 * g * it;
         }
         if (i == j) {
           Fsg += -cmd[i + 1] * expn * k13;
           Fds2 += -cmd[i + 1] * sgu_s * k13 - cmd[i + 1] * hy[0][0] * geo * k13 -
                   cmd[i + 1] * (hy[3][0] * f2 * t + g * hy[3][3] * it + f2 * hy[0][3] * it) * k13;
         }
-        double F = (-pi[i + 1][j + 1] - tdelta * Fdl - tpi * FD2 + 2. * tpi * Fdo2 * uv - tpp * Fds2 +
-                    (2. * eta + lpP * Pi) * Fsg + phi6 * Pi * pi[i + 1][j + 1] + phi7 * (sml + fu[i] * fu[j] * ss * k13)) *
+        R F = (-pi[i + 1][j + 1] - tdelta * Fdl - tpi * FD2 + R(2.) * tpi * Fdo2 * uv - tpp * Fds2 +
+                    (R(2.) * eta + lpP * Pi) * Fsg + phi6 * Pi * pi[i + 1][j + 1] + phi7 * (sml + fu[i] * fu[j] * ss * k13)) *
                    istg;
         if (i == j) F += phi7 * (-cmd[i + 1] * ss) * (k13 * istg);
         Fext[slot] = F;
 #pragma unroll
         for (int kk = 0; kk < D; kk++) {
-          const double MD2 = g * (fu[i] * hy[j + 1][kk + 1] - fu[i] * hy[j + 1][0] * fuc[kk] * ig + fu[j] * hy[i + 1][kk + 1] -
+          const R MD2 = g * (fu[i] * hy[j + 1][kk + 1] - fu[i] * hy[j + 1][0] * fuc[kk] * ig + fu[j] * hy[i + 1][kk + 1] -
                                   fu[j] * hy[i + 1][0] * fuc[kk] * ig);
-          double Msg = -fu[i] * fu[j] * fuc[kk] * (k13 * ig);
-          const double Mdl = -pi[i + 1][j + 1] * fuc[kk] * ig;
-          double Mdo2 = (-fu[i] * hy[j + 1][kk + 1] * g - fu[j] * hy[i + 1][kk + 1] * g + fuc[kk] * fu[i] * hy[j + 1][0] +
-                         fuc[kk] * fu[j] * hy[i + 1][0]) / 4.;
-          double Mds2 = (-fu[i] * hy[j + 1][kk + 1] * g - fu[j] * hy[i + 1][kk + 1] * g + fuc[kk] * fu[i] * hy[j + 1][0] +
-                         fuc[kk] * fu[j] * hy[i + 1][0] + 4. * fu[i] * fu[j] * (hy[0][kk + 1] - hy[0][0] * fuc[kk] * ig) * k13 +
-                         4. * pi[i + 1][j + 1] * fuc[kk] * k13 * ig) / 4.;
+          R Msg = -fu[i] * fu[j] * fuc[kk] * (k13 * ig);
+          const R Mdl = -pi[i + 1][j + 1] * fuc[kk] * ig;
+          R Mdo2 = (-fu[i] * hy[j + 1][kk + 1] * g - fu[j] * hy[i + 1][kk + 1] * g + fuc[kk] * fu[i] * hy[j + 1][0] +
+                         fuc[kk] * fu[j] * hy[i + 1][0]) / R(4.);
+          R Mds2 = (-fu[i] * hy[j + 1][kk + 1] * g - fu[j] * hy[i + 1][kk + 1] * g + fuc[kk] * fu[i] * hy[j + 1][0] +
+                         fuc[kk] * fu[j] * hy[i + 1][0] + R(4.) * fu[i] * fu[j] * (hy[0][kk + 1] - hy[0][0] * fuc[kk] * ig) * k13 +
+                         R(4.) * pi[i + 1][j + 1] * fuc[kk] * k13 * ig) / R(4.);
           if (kk == i) {            // i = k terms
-            Mds2 += pi[0][j + 1] / 4.;
-            Mdo2 += -pi[0][j + 1] / 4.;
-            Msg += -g * fu[j] / 2.;
+            Mds2 += pi[0][j + 1] / R(4.);
+            Mdo2 += -pi[0][j + 1] / R(4.);
+            Msg += -g * fu[j] / R(2.);
           }
           if (kk == j && j < D) {   // j = k terms
-            Msg += -g * fu[i] / 2.;
-            Mds2 += pi[0][i + 1] / 4.;
-            Mdo2 += -pi[0][i + 1] / 4.;
+            Msg += -g * fu[i] / R(2.);
+            Mds2 += pi[0][i + 1] / R(4.);
+            Mdo2 += -pi[0][i + 1] / R(4.);
           }
           if (i == j) {             // i = j terms
             Msg += cmd[i + 1] * fuc[kk] * (ig * k13);
             Mds2 += -cmd[i + 1] * (hy[0][kk + 1] - hy[0][0] * fuc[kk] * ig) * k13;
           }
-          Mext[slot][kk] = (-tpi * MD2 - tdelta * Mdl + 2. * tpi * Mdo2 * uv - tpp * Mds2 + (2. * eta + lpP * Pi) * Msg) *
+          Mext[slot][kk] = (-tpi * MD2 - tdelta * Mdl + R(2.) * tpi * Mdo2 * uv - tpp * Mds2 + (R(2.) * eta + lpP * Pi) * Msg) *
                            istg;
         }
       }
@@ -333,16 +342,16 @@ __device__ inline void eom(const ccake_config& cfg, const Transport& k, const Eo
   }
 
   // ---- auxiliary bulk and entropy MRFs (reference :229-362) ---------------
-  const double ztil = k.zeta + (k.delta_PiPi - k.tau_Pi) * Pi;
-  const double isgT = 1.0 / (sig * g * T), isgP = 1.0 / (sig * g * k.tau_Pi);
-  double Mb[3], Ms[3];
+  const R ztil = k.zeta + (k.delta_PiPi - k.tau_Pi) * Pi;
+  const R isgT = R(1.0) / (sig * g * T), isgP = R(1.0) / (sig * g * k.tau_Pi);
+  R Mb[3], Ms[3];
 #pragma unroll
   for (int i = 0; i < D; i++) {
     Mb[i] = (ztil * uc[i] * ig) * isgP;
     Ms[i] = (Pi * uc[i] * ig) * isgT;
   }
-  double Fb = -(ztil * expn + Pi - k.phi1 * Pi * Pi) * isgP;
-  double Fs = (-Pi * expn) * isgT;
+  R Fb = -(ztil * expn + Pi - k.phi1 * Pi * Pi) * isgP;
+  R Fs = (-Pi * expn) * isgT;
   if (cfg.using_shear) {
     Fs += Fnab * isgT;
     Fb += -(k.lambda_Pipi * Fnab - k.phi3 * ss) * isgP;
@@ -353,42 +362,42 @@ __device__ inline void eom(const ccake_config& cfg, const Transport& k, const Eo
     }
   }
   // ---- four-acceleration (reference :456-618); dN/dt = 0 without diffusion --
-  double gP[3], gB[3];
+  R gP[3], gB[3];
 #pragma unroll
   for (int i = 0; i < D; i++) {
-    const double f = (D == 2 || i < D - 1) ? -1.0 : -1.0 * it2;   // make_contravariant
+    const R f = (D == 2 || i < D - 1) ? -R(1.0) : -R(1.0) * it2;   // make_contravariant
     gP[i] = in.gradP[i] * f;
     gB[i] = in.gradBulk[i] * f;
   }
-  const double X = sden * dwds * ig + (rho[0] * dwdr[0] + rho[1] * dwdr[1] + rho[2] * dwdr[2]) * ig;
-  double Mw[3];
+  const R X = sden * dwds * ig + (rho[0] * dwdr[0] + rho[1] * dwdr[1] + rho[2] * dwdr[2]) * ig;
+  R Mw[3];
 #pragma unroll
   for (int i = 0; i < D; i++) Mw[i] = X * uc[i] * ig + sig * dwds * Ms[i];
-  const double Fw = -X * (geo + g * it + g * divV) + sig * dwds * Fs;
-  const double Fbulk = sig * Fb - Pi * (g * divV + g * it + geo) * ig;
-  double Mu[9], Fu[3];
+  const R Fw = -X * (geo + g * it + g * divV) + sig * dwds * Fs;
+  const R Fbulk = sig * Fb - Pi * (g * divV + g * it + geo) * ig;
+  R Mu[9], Fu[3];
 #pragma unroll
   for (int i = 0; i < D; i++) {
 #pragma unroll
     for (int j = 0; j < D; j++) Mu[i * D + j] = u[i] * g * (Mb[j] + Mw[j]) - u[i] * uc[j] * (w + Pi) * ig + M0i[i * D + j];
     Mu[i * D + i] += g * (w + Pi);
-    Fu[i] = (gP[i] + gB[i]) - g * (Fw + Fbulk) * u[i] - (w + Pi) * expn * u[i] - 2. * (w + Pi) * g * uD * dEta(i) * it;
+    Fu[i] = (gP[i] + gB[i]) - g * (Fw + Fbulk) * u[i] - (w + Pi) * expn * u[i] - R(2.) * (w + Pi) * g * uD * dEta(i) * it;
     if (cfg.using_shear)
-      Fu[i] += -P(i + 1, 0) * it - 2. * dEta(i) * P(0, 3) * it - in.divshear[i] + in.gradshear[i] - F0i[i];
+      Fu[i] += -P(i + 1, 0) * it - R(2.) * dEta(i) * P(0, 3) * it - in.divshear[i] + in.gradshear[i] - F0i[i];
   }
   // du/dt = M^-1 F by cofactors (include/milne.hpp:788-834)
-  double du[3];
+  R du[3];
   if (D == 2) {
-    const double idet = 1.0 / (Mu[0] * Mu[3] - Mu[1] * Mu[2]);
+    const R idet = R(1.0) / (Mu[0] * Mu[3] - Mu[1] * Mu[2]);
     du[0] = (Mu[3] * idet) * Fu[0] + (-Mu[1] * idet) * Fu[1];
     du[1] = (-Mu[2] * idet) * Fu[0] + (Mu[0] * idet) * Fu[1];
-    du[2] = 0.0;
+    du[2] = R(0.0);
   } else {
 #define A(i, j) Mu[(i) * 3 + (j)]
-    const double det = A(0, 0) * A(1, 1) * A(2, 2) + A(0, 1) * A(1, 2) * A(2, 0) + A(0, 2) * A(1, 0) * A(2, 1) -
+    const R det = A(0, 0) * A(1, 1) * A(2, 2) + A(0, 1) * A(1, 2) * A(2, 0) + A(0, 2) * A(1, 0) * A(2, 1) -
                        A(0, 2) * A(1, 1) * A(2, 0) - A(0, 1) * A(1, 0) * A(2, 2) - A(0, 0) * A(1, 2) * A(2, 1);
-    const double idet = 1.0 / det;
-    const double inv[9] = {(A(1, 1) * A(2, 2) - A(1, 2) * A(2, 1)) * idet, (A(0, 2) * A(2, 1) - A(0, 1) * A(2, 2)) * idet,
+    const R idet = R(1.0) / det;
+    const R inv[9] = {(A(1, 1) * A(2, 2) - A(1, 2) * A(2, 1)) * idet, (A(0, 2) * A(2, 1) - A(0, 1) * A(2, 2)) * idet,
                            (A(0, 1) * A(1, 2) - A(0, 2) * A(1, 1)) * idet, (A(1, 2) * A(2, 0) - A(1, 0) * A(2, 2)) * idet,
                            (A(0, 0) * A(2, 2) - A(0, 2) * A(2, 0)) * idet, (A(0, 2) * A(1, 0) - A(0, 0) * A(1, 2)) * idet,
                            (A(1, 0) * A(2, 1) - A(1, 1) * A(2, 0)) * idet, (A(0, 1) * A(2, 0) - A(0, 0) * A(2, 1)) * idet,
@@ -398,21 +407,21 @@ __device__ inline void eom(const ccake_config& cfg, const Transport& k, const Eo
     for (int i = 0; i < 3; i++) du[i] = inv[i * 3 + 0] * Fu[0] + inv[i * 3 + 1] * Fu[1] + inv[i * 3 + 2] * Fu[2];
   }
   // ---- derivatives (reference :622-826) -------------------------------------
-  double m1 = 0, m2 = 0;
+  R m1 = 0, m2 = 0;
 #pragma unroll
   for (int i = 0; i < D; i++) { m1 += Ms[i] * du[i]; m2 += Mb[i] * du[i]; o.du[i] = du[i]; }
   o.dS = m1 + Fs;
   o.dBulk = m2 + Fb;
 #pragma unroll
   for (int sl = 0; sl < 5; sl++) {
-    double acc = 0.0;
+    R acc = R(0.0);
 #pragma unroll
     for (int kk = 0; kk < D; kk++) acc += Mext[sl][kk] * du[kk];
-    o.dShv[sl] = cfg.using_shear ? acc + Fext[sl] : 0.0;
+    o.dShv[sl] = cfg.using_shear ? acc + Fext[sl] : R(0.0);
   }
   // ---- dEz (reference :827-862) ---------------------------------------------
-  const double u3 = (D == 3) ? u[2] : 0.0;
-  o.dEz = ((th[T_E] + th[T_P] + Pi) * u3 * u3 + (th[T_P] + Pi) * it2 + P(3, 3)) * in.m * t2 / in.sigma_lab;   // one division per particle
+  const R u3 = (D == 3) ? u[2] : R(0.0);
+  o.dEz = ((R(th[T_E]) + R(th[T_P]) + Pi) * u3 * u3 + (R(th[T_P]) + Pi) * it2 + P(3, 3)) * in.m * t2 / in.sigma_lab;
 }
 
 }  // namespace ccake

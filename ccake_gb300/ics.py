@@ -40,6 +40,7 @@ class RunConfig:
     input_as_entropy: int = 0
     modulate_zeta_with_tanh: int = 0
     thermo_mode: int = 0           # 0 reference derivative chain, 1 exact Hessian inverse
+    precision: int = 0             # 0 FP64 throughout, 1 FP32 compensated pair loops (GPU only)
     hT: float = 0.1
     hEta: float = 0.1
     t0: float = 1.0
