@@ -85,6 +85,7 @@ def lib():
         L.ccake_copy_out_int.argtypes = [P, ctypes.c_char_p, _ip]
         L.ccake_get_neighbours.argtypes = [P, _ip, _ip, _i64, ctypes.POINTER(_i64)]
         L.ccake_eos_invert_batch.argtypes = [P, _i32, _i64, _dp, _dp, _dp, _ip, _ip]
+        L.ccake_eos_invert_batch_ex.argtypes = [P, _i32, _i32, _i64, _dp, _dp, _dp, _ip, _ip]
         _lib = L
     return _lib
 
@@ -200,15 +201,16 @@ class GpuHydro:
                     "neighbours")
         return off, idx[:cnt.value]
 
-    def eos_invert(self, entropy, targets, seeds):
+    def eos_invert(self, entropy, targets, seeds, seed_mode=0):
+        """Batch inversion; seed_mode 0 reference seed chain, 1 analytic exact inverse first."""
         t = np.ascontiguousarray(targets, dtype=np.float64)
         x = np.ascontiguousarray(seeds, dtype=np.float64).copy()
         n = t.shape[0]
         th = np.zeros((n, 16))
         st = np.zeros(n, dtype=np.int32)
         it = np.zeros(n, dtype=np.int32)
-        self._check(lib().ccake_eos_invert_batch(self.h, int(entropy), n, _d(t), _d(x), _d(th), _i(st), _i(it)),
-                    "eos_invert_batch")
+        self._check(lib().ccake_eos_invert_batch_ex(self.h, int(entropy), int(seed_mode), n, _d(t), _d(x), _d(th),
+                                                    _i(st), _i(it)), "eos_invert_batch")
         return x, th, st, it
 
 

@@ -615,7 +615,14 @@ ccake_status_t ccake_get_neighbours(ccake_ctx* ctx, int32_t* offsets, int32_t* i
 
 ccake_status_t ccake_eos_invert_batch(ccake_ctx* ctx, int32_t entropy_mode, int64_t n, const double* in4,
                                       double* tbqs, double* th16, int32_t* status, int32_t* iters) {
+  return ccake_eos_invert_batch_ex(ctx, entropy_mode, CCAKE_SEED_REFERENCE, n, in4, tbqs, th16, status, iters);
+}
+
+ccake_status_t ccake_eos_invert_batch_ex(ccake_ctx* ctx, int32_t entropy_mode, int32_t seed_mode, int64_t n,
+                                         const double* in4, double* tbqs, double* th16, int32_t* status,
+                                         int32_t* iters) {
   if (!ctx || n < 0 || !in4 || !tbqs || !status) return CCAKE_ERR_INVALID;
+  if (seed_mode != CCAKE_SEED_REFERENCE && seed_mode != CCAKE_SEED_ANALYTIC) return CCAKE_ERR_INVALID;
   if (n == 0) return CCAKE_OK;
   double *d_in = nullptr, *d_x = nullptr, *d_th = nullptr;
   int32_t *d_st = nullptr, *d_it = nullptr;
@@ -626,7 +633,7 @@ ccake_status_t ccake_eos_invert_batch(ccake_ctx* ctx, int32_t entropy_mode, int6
   if (iters) CK(cudaMalloc(&d_it, n * sizeof(int32_t)));
   CK(cudaMemcpyAsync(d_in, in4, n * 4 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(d_x, tbqs, n * 4 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-  launch_eos_batch(ctx->eos, entropy_mode, n, d_in, d_x, d_th, d_st, d_it, ctx->stream);
+  launch_eos_batch(ctx->eos, entropy_mode, seed_mode, n, d_in, d_x, d_th, d_st, d_it, ctx->stream);
   CK(cudaMemcpyAsync(tbqs, d_x, n * 4 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   if (th16) CK(cudaMemcpyAsync(th16, d_th, n * 16 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaMemcpyAsync(status, d_st, n * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));

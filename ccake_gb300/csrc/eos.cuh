@@ -327,24 +327,36 @@ __host__ __device__ inline void confdiag_seed(const Scales& k, int entropy, cons
 //   conformal: p = c T0^4 x^2 with x = sum_k (X_k/X0_k)^2, so
 //     d_k = 4 c T0^4 x X_k / X0_k^2; with a_k = X_k/X0_k and
 //     d'_k = d_k X0_k / (4 c T0^4) = a_k x, x^3 = sum_k d'_k^2 and a_k = d'_k / x.
+// Real cube root: FP32 cbrtf seed, then one Halley step in FP64,
+// y <- y (y^3 + 2x) / (2 y^3 + x), which triples the seed's ~2^-23 relative
+// accuracy to beyond FP64 precision (Halley's method on y^3 - x = 0). Inputs
+// outside the FP32 normal range go to cbrt.
+__host__ __device__ inline double cbrt_halley(double x) {
+  const double ax = fabs(x);
+  if (!(ax > 1e-30 && ax < 1e30)) return cbrt(x);
+  const double y = (double)cbrtf((float)x);
+  const double y3 = y * y * y;
+  return y * (y3 + 2.0 * x) / (2.0 * y3 + x);
+}
+
 __host__ __device__ inline bool analytic_seed(const EosDev& e, int model, const double* tgt, double* y) {
   if (model == M_TABLE) return false;
   const Scales k = model_scales(e, model);
   const double X0[4] = {k.T0, k.muB0, k.muQ0, k.muS0};
-  const double c4 = 4.0 * k.c * k.T0 * k.T0 * k.T0 * k.T0;
+  const double ic4 = 1.0 / (4.0 * k.c * k.T0 * k.T0 * k.T0 * k.T0);
   if (model == M_CDIAG) {
     for (int i = 0; i < 4; i++) {
       const double q = X0[i] * X0[i];
-      y[i] = cbrt(tgt[i] * q * q / c4);
+      y[i] = cbrt_halley(tgt[i] * q * q * ic4);
     }
     return y[0] > 0.0;
   }
   double d[4], x3 = 0.0;
   for (int i = 0; i < 4; i++) {
-    d[i] = tgt[i] * X0[i] / c4;
+    d[i] = tgt[i] * X0[i] * ic4;
     x3 += d[i] * d[i];
   }
-  const double xx = cbrt(x3);
+  const double xx = cbrt_halley(x3);
   if (!(xx > 0.0)) return false;
   const double ix = 1.0 / xx;
   for (int i = 0; i < 4; i++) y[i] = d[i] * ix * X0[i];
@@ -369,6 +381,19 @@ __host__ __device__ inline int eos_invert(const EosDev& e, int entropy, const do
     double y[4];
     bool ok = false;
     if (entropy && seed_mode == 1 && analytic_seed(e, model, tgt, y)) {
+      // the exact inverse is accepted when it meets the reference's residual
+      // test (max |F| < 1e-10); otherwise Newton starts from it
+      double o[17];
+      model_thermo(e, model, y, o);
+      const double fres = fmax(fmax(fabs(o[1] - tgt[0]), fabs(o[2] - tgt[1])),
+                               fmax(fabs(o[4] - tgt[2]), fabs(o[3] - tgt[3])));
+      if (fres < 1e-10 && !(o[6] < 0.0 || o[6] > 1.0)) {
+        for (int i = 0; i < 4; i++) x[i] = y[i];
+        if (o_out)
+          for (int i = 0; i < 17; i++) o_out[i] = o[i];
+        *iters = it;
+        return k;
+      }
       double lo[4], hi[4];
       model_box(e, model, lo, hi);
       ok = newton_attempt(e, model, 1, tgt, lo, hi, y, &it);
@@ -483,7 +508,10 @@ __host__ __device__ inline double schur_term(const Chi& x, int which) {
 // Derived thermodynamics at a solution: T mu p s rho e w cs2 and dw/ds, dw/drho
 // (reference include/eos.h:121-175, src/eos.cpp:276-344). th must hold NTH doubles.
 // o: the model thermodynamics at x (model_thermo of the chain's model k).
-__host__ __device__ inline void set_thermo_o(const EosDev& e, int k, const double* x, const double* o, double* th) {
+// fp32_derivs: the conformal-diagonal enthalpy derivatives dw/ds, dw/drho in
+// FP32 arithmetic (they feed only FP32 equations of motion in the mixed form).
+__host__ __device__ inline void set_thermo_o(const EosDev& e, int k, const double* x, const double* o, double* th,
+                                             bool fp32_derivs = false) {
   const int model = chain_model(e.kind, k);
   const double T = x[0], mB = x[1], mQ = x[2], mS = x[3];
   const double s = o[1], B = o[2], S = o[3], Q = o[4];
@@ -504,8 +532,13 @@ __host__ __device__ inline void set_thermo_o(const EosDev& e, int k, const doubl
       // elimination below gives the same reciprocals)
       for (int a = 0; a < 4; a++) {
         const double Haa = H[a][a];
-        const double G = Haa != 0.0 ? 1.0 / Haa : 0.0;
-        th[T_DWDS + a] = (a == 0 || act[a]) ? mu[a] + (a == 0 ? s : rho[a]) * G : mu[a];
+        if (fp32_derivs) {
+          const float G = Haa != 0.0 ? 1.0f / (float)Haa : 0.0f;
+          th[T_DWDS + a] = (a == 0 || act[a]) ? (double)((float)mu[a] + (float)(a == 0 ? s : rho[a]) * G) : mu[a];
+        } else {
+          const double G = Haa != 0.0 ? 1.0 / Haa : 0.0;
+          th[T_DWDS + a] = (a == 0 || act[a]) ? mu[a] + (a == 0 ? s : rho[a]) * G : mu[a];
+        }
       }
       return;
     }

@@ -585,18 +585,19 @@ __global__ void k_nbr_fill(RunConst rc, Ptrs p, const int32_t* off, int32_t* idx
   });
 }
 
-__global__ void k_eos_batch(EosDev eos, int entropy, int64_t n, const double* in4, double* tbqs, double* th16,
-                            int32_t* status, int32_t* iters) {
+__global__ void k_eos_batch(EosDev eos, int entropy, int seed_mode, int64_t n, const double* in4, double* tbqs,
+                            double* th16, int32_t* status, int32_t* iters) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   double x[4] = {tbqs[4 * i], tbqs[4 * i + 1], tbqs[4 * i + 2], tbqs[4 * i + 3]};
   int it = 0;
-  const int k = eos_invert(eos, entropy, in4 + 4 * i, 0, x, &it);
+  double o[17];
+  const int k = eos_invert(eos, entropy, in4 + 4 * i, 0, x, &it, seed_mode, o);
   status[i] = k;
   if (iters) iters[i] = it;
   if (k >= 0) {
     for (int q = 0; q < 4; q++) tbqs[4 * i + q] = x[q];
-    if (th16) set_thermo(eos, k, x, th16 + 16 * i);
+    if (th16) set_thermo_o(eos, k, x, o, th16 + 16 * i);
   }
 }
 
@@ -680,10 +681,10 @@ void launch_neighbour_fill(const RunConst& rc, const Ptrs& p, const int32_t* off
   else k_nbr_fill<2><<<nb, kBlock, 0, s>>>(rc, p, offsets, idx);
 }
 
-void launch_eos_batch(const EosDev& eos, int entropy, int64_t n, const double* in4, double* tbqs, double* th16,
-                      int32_t* status, int32_t* iters, cudaStream_t s) {
+void launch_eos_batch(const EosDev& eos, int entropy, int seed_mode, int64_t n, const double* in4, double* tbqs,
+                      double* th16, int32_t* status, int32_t* iters, cudaStream_t s) {
   const int nb = (int)((n + kBlock - 1) / kBlock);
-  k_eos_batch<<<nb, kBlock, 0, s>>>(eos, entropy, n, in4, tbqs, th16, status, iters);
+  k_eos_batch<<<nb, kBlock, 0, s>>>(eos, entropy, seed_mode, n, in4, tbqs, th16, status, iters);
 }
 
 }  // namespace ccake

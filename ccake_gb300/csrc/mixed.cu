@@ -62,33 +62,56 @@ __global__ void __launch_bounds__(kBlock) k_passA_mixed(RunConst rc, Ptrs p) {
   int rlo[D == 3 ? 9 : 3], rhi[D == 3 ? 9 : 3];
   const int nr = neighbour_ranges<D>(rc.grid, p.cell_start, xa, rlo, rhi);
   int nn = 0;
+  // candidates in groups of four: the cell-list entries, then the records,
+  // then the energy records of the accepted ones are each loaded together so
+  // that their latencies overlap; accepted pairs are visited in candidate
+  // order, as a one-at-a-time loop would
+  constexpr int U = 4;
   for (int r = 0; r < nr; r++) {
-    for (int j = rlo[r]; j < rhi[r]; j++) {
-      const int b = p.cell_idx[j];
-      if (b == i) continue;
-      const float4 bh = __ldg(&ra[(size_t)b * SA]), bl = __ldg(&ra[(size_t)b * SA + 1]);
-      const float dx = (ah.x - bh.x) + (al.x - bl.x);
-      const float dy = (ah.y - bh.y) + (al.y - bl.y);
-      const float dz = (D == 3) ? (ah.z - bh.z) + (al.z - bl.z) : 0.0f;
-      const float d2 = dx * dx + dy * dy + dz * dz;
-      if (!(d2 <= cut2)) continue;
-      // W (src/kernel.cpp:34-48) and grad_a W = fg (r_a - r_b) (:95-118)
-      const float rs = d2 > 0.0f ? rsqrtf(d2) : 0.0f;
-      const float q = d2 * rs * ih;
-      const float z = fmaxf(2.0f - q, 0.0f), qq = q * q;
-      const float W = q < 1.0f ? wn * (1.0f - 1.5f * qq + 0.75f * q * qq) : wn2 * z * z * z;
-      const float fg = q < 1.0f ? gn2 * (1.5f * q - 2.0f) * ih : gn * rs * z * z;
-      if (nn < K) {
-        p.nbr_idx[(size_t)nn * n + i] = b;
-        nf[(size_t)nn * n + i] = fg;
+    const int je = rhi[r];
+    for (int j0 = rlo[r]; j0 < je; j0 += U) {
+      int bb[U];
+      float4 bh[U], bl[U], be[U];
+      float d2[U];
+      bool ok[U];
+#pragma unroll
+      for (int u = 0; u < U; u++) bb[u] = (j0 + u < je) ? p.cell_idx[j0 + u] : i;
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        bh[u] = __ldg(&ra[(size_t)bb[u] * SA]);
+        bl[u] = __ldg(&ra[(size_t)bb[u] * SA + 1]);
       }
-      nn++;
-      const float4 be = __ldg(&ra[(size_t)b * SA + 2]);
-      sl.add(bh.w * W);
-      s0.add(be.x * W);
-      s1.add(be.y * W);
-      s2.add(be.z * W);
-      s3.add(be.w * W);
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const float dx = (ah.x - bh[u].x) + (al.x - bl[u].x);
+        const float dy = (ah.y - bh[u].y) + (al.y - bl[u].y);
+        const float dz = (D == 3) ? (ah.z - bh[u].z) + (al.z - bl[u].z) : 0.0f;
+        d2[u] = dx * dx + dy * dy + dz * dz;
+        ok[u] = (d2[u] <= cut2) && bb[u] != i;
+      }
+#pragma unroll
+      for (int u = 0; u < U; u++)
+        if (ok[u]) be[u] = __ldg(&ra[(size_t)bb[u] * SA + 2]);
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        if (!ok[u]) continue;
+        // W (src/kernel.cpp:34-48) and grad_a W = fg (r_a - r_b) (:95-118)
+        const float rs = d2[u] > 0.0f ? rsqrtf(d2[u]) : 0.0f;
+        const float q = d2[u] * rs * ih;
+        const float z = fmaxf(2.0f - q, 0.0f), qq = q * q;
+        const float W = q < 1.0f ? wn * (1.0f - 1.5f * qq + 0.75f * q * qq) : wn2 * z * z * z;
+        const float fg = q < 1.0f ? gn2 * (1.5f * q - 2.0f) * ih : gn * rs * z * z;
+        if (nn < K) {
+          p.nbr_idx[(size_t)nn * n + i] = bb[u];
+          nf[(size_t)nn * n + i] = fg;
+        }
+        nn++;
+        sl.add(bh[u].w * W);
+        s0.add(be[u].x * W);
+        s1.add(be[u].y * W);
+        s2.add(be[u].z * W);
+        s3.add(be[u].w * W);
+      }
     }
   }
   if (nn > K) atomicAdd(&p.err[E_NBR_OVERFLOW], 1);
@@ -118,16 +141,18 @@ __global__ void __launch_bounds__(kBlock) k_thermo_mixed(RunConst rc, EosDev eos
   thermo_tail<D, true>(rc, eos, p, i, p.clock->t);
 }
 
-// Pass B, mixed form: separable gradient sums over the list pass A wrote,
-// FP32 with Kahan compensation (the separable forms of
-// src/sph_workstation.cpp:797-986), then the FP32 equations of motion and the
-// FP64 RK2 update.
+// Pass B, mixed form, part 1: separable gradient sums over the list pass A
+// wrote, FP32 with Kahan compensation (the separable forms of
+// src/sph_workstation.cpp:797-986), written to the float view of the gradient
+// slab (slot q of particle i at q * n + i, slots as GradSlot). The equations
+// of motion run in k_eom_mixed: kept apart, this gather loop needs ~70
+// registers a thread instead of ~170 and keeps enough warps in flight to
+// cover its gather latency.
 template <int D>
-__global__ void __launch_bounds__(kBlock) k_passB_mixed(RunConst rc, Ptrs p, int mode, double dt_sub) {
+__global__ void __launch_bounds__(kBlock) k_passB_mixed(RunConst rc, Ptrs p) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= p.n) return;
   const int n = p.n;
-  const double t = p.clock->t;
   const bool shear = rc.cfg.using_shear;
   constexpr int SB = RBF / 4;
   const float4* rbf = reinterpret_cast<const float4*>(p.recBf);
@@ -149,9 +174,20 @@ __global__ void __launch_bounds__(kBlock) k_passB_mixed(RunConst rc, Ptrs p, int
   }
   const float* nf = reinterpret_cast<const float*>(p.nbr_f);
   const int cnt = min(p.btrack[i], p.K);
+  // the list entries are streamed from memory two iterations ahead of use
+  int bq0 = 0, bq1 = 0;
+  float fq0 = 0.0f, fq1 = 0.0f;
+  if (cnt > 0) { bq0 = p.nbr_idx[i]; fq0 = nf[i]; }
+  if (cnt > 1) { bq1 = p.nbr_idx[(size_t)n + i]; fq1 = nf[(size_t)n + i]; }
   for (int kk = 0; kk < cnt; kk++) {
-    const int b = p.nbr_idx[(size_t)kk * n + i];
-    const float fg = nf[(size_t)kk * n + i];
+    const int b = bq0;
+    const float fg = fq0;
+    bq0 = bq1;
+    fq0 = fq1;
+    if (kk + 2 < cnt) {
+      bq1 = p.nbr_idx[(size_t)(kk + 2) * n + i];
+      fq1 = nf[(size_t)(kk + 2) * n + i];
+    }
     const float4* rb = rbf + (size_t)b * SB;
     const float4 B0 = __ldg(rb), B1 = __ldg(rb + 1), B2 = __ldg(rb + 2);
     const float d[3] = {(A0.x - B0.x) + (A1.x - B1.x), (A0.y - B0.y) + (A1.y - B1.y),
@@ -229,7 +265,42 @@ __global__ void __launch_bounds__(kBlock) k_passB_mixed(RunConst rc, Ptrs p, int
       dS[k] = sla * acc2;
     }
   }
-  finish_particle<D, float, true>(rc, p, i, mode, t, dt_sub, va, gP, gE, gB, gS, dS, gV);
+  float* gf = reinterpret_cast<float*>(p.grads);
+#pragma unroll
+  for (int k = 0; k < D; k++) {
+    gf[(G_P + k) * n + i] = gP[k];
+    gf[(G_E + k) * n + i] = gE[k];
+    gf[(G_B + k) * n + i] = gB[k];
+    gf[(G_SH + k) * n + i] = gS[k];
+    gf[(G_DS + k) * n + i] = dS[k];
+  }
+#pragma unroll
+  for (int k = 0; k < D * D; k++) gf[(G_V + k) * n + i] = gV[k];
+}
+
+// Pass B, mixed form, part 2: FP32 equations of motion from the gradients of
+// part 1, FP64 RK2 update, mixed smoothing record for the next substep.
+template <int D>
+__global__ void __launch_bounds__(kBlock) k_eom_mixed(RunConst rc, Ptrs p, int mode, double dt_sub) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.n) return;
+  const int n = p.n;
+  const float* gf = reinterpret_cast<const float*>(p.grads);
+  const float4 A2 = reinterpret_cast<const float4*>(p.recBf)[(size_t)i * (RBF / 4) + 2];
+  const float va[3] = {A2.z, A2.w, D == 3 ? p.recBf[(size_t)i * RBF + 12] : 0.0f};
+  float gP[3] = {0, 0, 0}, gE[3] = {0, 0, 0}, gB[3] = {0, 0, 0}, gS[3] = {0, 0, 0}, dS[3] = {0, 0, 0};
+  float gV[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+  for (int k = 0; k < D; k++) {
+    gP[k] = gf[(G_P + k) * n + i];
+    gE[k] = gf[(G_E + k) * n + i];
+    gB[k] = gf[(G_B + k) * n + i];
+    gS[k] = gf[(G_SH + k) * n + i];
+    dS[k] = gf[(G_DS + k) * n + i];
+  }
+#pragma unroll
+  for (int k = 0; k < D * D; k++) gV[k] = gf[(G_V + k) * n + i];
+  finish_particle<D, float, true>(rc, p, i, mode & ~B_GRADS, p.clock->t, dt_sub, va, gP, gE, gB, gS, dS, gV);
 }
 
 }  // namespace
@@ -253,8 +324,13 @@ void launch_passA_mixed(const RunConst& rc, const EosDev& eos, const Ptrs& p, cu
 
 void launch_passB_mixed(const RunConst& rc, const Ptrs& p, int mode, double dt_sub, cudaStream_t s) {
   const int nb = (p.n + kBlock - 1) / kBlock;
-  if (rc.cfg.dim == 3) k_passB_mixed<3><<<nb, kBlock, 0, s>>>(rc, p, mode, dt_sub);
-  else k_passB_mixed<2><<<nb, kBlock, 0, s>>>(rc, p, mode, dt_sub);
+  if (rc.cfg.dim == 3) {
+    k_passB_mixed<3><<<nb, kBlock, 0, s>>>(rc, p);
+    k_eom_mixed<3><<<nb, kBlock, 0, s>>>(rc, p, mode, dt_sub);
+  } else {
+    k_passB_mixed<2><<<nb, kBlock, 0, s>>>(rc, p);
+    k_eom_mixed<2><<<nb, kBlock, 0, s>>>(rc, p, mode, dt_sub);
+  }
 }
 
 }  // namespace ccake

@@ -105,7 +105,7 @@ __device__ __forceinline__ void thermo_tail(const RunConst& rc, const EosDev& eo
     atomicAdd(&p.err[E_EOS], 1);
     return;
   }
-  set_thermo_o(eos, k, x, o, th);
+  set_thermo_o(eos, k, x, o, th, MIX);
 #pragma unroll
   for (int q = 0; q < NTH; q++) p.th[q * n + i] = th[q];
   p.eos_id[i] = k;
@@ -206,7 +206,7 @@ __device__ __forceinline__ void finish_particle(const RunConst& rc, const Ptrs& 
   in.Pi = R(p.bulk[i]);
 #pragma unroll
   for (int q = 0; q < NPI; q++) in.pi[q] = R(p.pi[q * n + i]);
-  const Transport k = transport(rc.cfg, th);
+  const TransportT<R> k = transport<R>(rc.cfg, th);
   EomOut<R> o;
   eom<D, R>(rc.cfg, k, in, t, o);
   if (mode & B_DERIVS) {

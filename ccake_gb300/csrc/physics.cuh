@@ -6,50 +6,69 @@
 
 namespace ccake {
 
-struct Transport {
-  double eta, tau_pi, zeta, tau_Pi, delta_PiPi, delta_pipi, lambda_piPi, lambda_Pipi, phi1, phi3, phi6, phi7,
-      tau_pipi;
+template <typename R = double>
+struct TransportT {
+  R eta, tau_pi, zeta, tau_Pi, delta_PiPi, delta_pipi, lambda_piPi, lambda_Pipi, phi1, phi3, phi6, phi7, tau_pipi;
 };
+using Transport = TransportT<double>;
 
-// Reference src/transport_coefficients.cpp:620-900 (modes used by the hot path).
-__device__ inline Transport transport(const ccake_config& c, const double* th) {
-  Transport k;
-  const double T = th[T_T], w = th[T_W], cs2 = th[T_CS2], p = th[T_P];
-  k.eta = (T <= 0.0) ? 0.0 : c.eta_over_s * (w / T);
-  if (c.shear_relax_mode == 1) k.tau_pi = (5.0 * k.eta) / w;
-  else if (c.shear_relax_mode == 2) k.tau_pi = fmax((5.0 * k.eta) / w, 0.001);
-  else k.tau_pi = fmax(5.0 * k.eta / w, 0.005);
+// x^p; integer exponents 0..8 by repeated products (exact to rounding, and
+// a fraction of pow's instruction count), others by pow.
+template <typename R>
+__device__ __forceinline__ R powi_or_pow(R x, R p) {
+  if (p == R(2)) return x * x;
+  if (p >= R(0) && p <= R(8) && p == floor(p)) {
+    R r = R(1);
+    for (int k = 0; k < (int)p; k++) r *= x;
+    return r;
+  }
+  return pow(x, p);
+}
+
+// Reference src/transport_coefficients.cpp:620-900 (modes used by the hot
+// path). R = double for the plain form; R = float where the coefficients only
+// feed the mixed form's FP32 equations of motion.
+template <typename R = double>
+__device__ inline TransportT<R> transport(const ccake_config& c, const double* th) {
+  TransportT<R> k;
+  const R T = R(th[T_T]), w = R(th[T_W]), cs2 = R(th[T_CS2]), p = R(th[T_P]);
+  const R eos = R(c.eta_over_s), zos = R(c.zeta_over_s), zp = R(c.zeta_cs2_p);
+  const R k13 = R(1.0) / R(3.0);
+  k.eta = (T <= R(0)) ? R(0) : eos * (w / T);
+  if (c.shear_relax_mode == 1) k.tau_pi = (R(5) * k.eta) / w;
+  else if (c.shear_relax_mode == 2) k.tau_pi = fmax((R(5) * k.eta) / w, R(0.001));
+  else k.tau_pi = fmax(R(5) * k.eta / w, R(0.005));
   switch (c.zeta_mode) {
-    case 1: k.zeta = c.zeta_over_s * (w / T); break;
+    case 1: k.zeta = zos * (w / T); break;
     case 2: {
-      double factor = 1.0;
+      R factor = R(1);
       if (c.modulate_zeta_with_tanh) {
-        const double Ttr = 150.0 / kHbarcMeVfm, Tsc = 10.0 / kHbarcMeVfm;
-        const double thx = tanh((T - Ttr) / Tsc), xp = pow(T / Ttr, c.zeta_cs2_p);
-        factor = 0.5 * (1.0 + xp) + 0.5 * (1.0 - xp) * thx;
+        const R Ttr = R(150.0 / kHbarcMeVfm), Tsc = R(10.0 / kHbarcMeVfm);
+        const R thx = tanh((T - Ttr) / Tsc), xp = powi_or_pow<R>(T / Ttr, zp);
+        factor = R(0.5) * (R(1) + xp) + R(0.5) * (R(1) - xp) * thx;
       }
-      k.zeta = c.zeta_cs2_A * factor * pow((1.0 / 3.0) - fmin(cs2, 1.0), c.zeta_cs2_p) * w / T;
+      k.zeta = R(c.zeta_cs2_A) * factor * powi_or_pow<R>(k13 - fmin(cs2, R(1)), zp) * w / T;
       break;
     }
     case 3: {
-      const double x = (T - c.zeta_peak_T) / c.zeta_peak_width;
-      k.zeta = c.zeta_over_s * exp(-0.5 * x * x) * (w / T);
+      const R x = (T - R(c.zeta_peak_T)) / R(c.zeta_peak_width);
+      k.zeta = zos * exp(R(-0.5) * x * x) * (w / T);
       break;
     }
-    default: k.zeta = 0.005 * (w / T);
+    default: k.zeta = R(0.005) * (w / T);
   }
-  const double cc = cs2 > 1 ? 1 : cs2;
-  const double pw = pow((1.0 / 3.0 - cc), c.zeta_cs2_p);
-  k.tau_Pi = (pw < 1e-10) ? 1e10 : fmax(5.0 * k.zeta / (pw * w), 0.1);
-  k.delta_PiPi = 2. * k.tau_Pi / 3.0;
-  k.delta_pipi = 4. * k.tau_pi / 3.0;
-  k.lambda_piPi = 6. / 5. * k.tau_pi;
-  k.lambda_Pipi = 8. * (1. / 3. - cc) * k.tau_Pi / 5.;
-  k.phi1 = 0.0;
-  k.phi3 = 0.0;
-  k.phi6 = 0.0;
-  k.phi7 = 9. / (70. * p);
-  k.tau_pipi = 10. * k.tau_pi / 7.0;
+  const R cc = cs2 > R(1) ? R(1) : cs2;
+  const R pw = powi_or_pow<R>(k13 - cc, zp);
+  k.tau_Pi = (pw < R(1e-10)) ? R(1e10) : fmax(R(5) * k.zeta / (pw * w), R(0.1));
+  k.delta_PiPi = R(2) * k.tau_Pi / R(3);
+  k.delta_pipi = R(4) * k.tau_pi / R(3);
+  k.lambda_piPi = R(6) / R(5) * k.tau_pi;
+  k.lambda_Pipi = R(8) * (k13 - cc) * k.tau_Pi / R(5);
+  k.phi1 = R(0);
+  k.phi3 = R(0);
+  k.phi6 = R(0);
+  k.phi7 = R(9) / (R(70) * p);
+  k.tau_pipi = R(10) * k.tau_pi / R(7);
   return k;
 }
 
@@ -69,13 +88,15 @@ __device__ inline void reset_pi(const double* ext_shv, double sigma, double g, c
   const double f0 = -u3[0], f1 = -u3[1], f2 = -t2 * u3[2];   // covariant u_i
   const double p11 = ext_shv[0] * sigma, p12 = ext_shv[1] * sigma, p13 = ext_shv[2] * sigma;
   const double p22 = ext_shv[3] * sigma, p23 = ext_shv[4] * sigma;
+  // one division each for 1/t^2 and 1/g (FP64 division is a long sequence)
+  const double it2 = 1.0 / t2, ig = 1.0 / g;
   const double p00 = (f0 * f0 * p11 + f1 * f1 * p22 + 2. * f1 * f0 * p12 + 2. * f2 * f0 * p13 + 2. * f2 * f1 * p23 -
-                      f2 * f2 * (p11 + p22) / t2) / (g * g - f2 * f2 / t2);
-  const double p33 = (p00 - p11 - p22) / t2;
+                      f2 * f2 * (p11 + p22) * it2) / (g * g - f2 * f2 * it2);
+  const double p33 = (p00 - p11 - p22) * it2;
   pi[P00] = p00; pi[P11] = p11; pi[P12] = p12; pi[P13] = p13; pi[P22] = p22; pi[P23] = p23; pi[P33] = p33;
-  pi[P01] = -(p11 * f0 + p12 * f1 + p13 * f2) / g;
-  pi[P02] = -(p12 * f0 + p22 * f1 + p23 * f2) / g;
-  pi[P03] = -(p13 * f0 + p23 * f1 + p33 * f2) / g;
+  pi[P01] = -(p11 * f0 + p12 * f1 + p13 * f2) * ig;
+  pi[P02] = -(p12 * f0 + p22 * f1 + p23 * f2) * ig;
+  pi[P03] = -(p13 * f0 + p23 * f1 + p33 * f2) * ig;
 }
 
 // Inputs of the equations of motion for one particle.
@@ -100,13 +121,9 @@ struct EomOut {
 // R = double is the plain FP64 form; R = float is the mixed form's EoM (the
 // state update it feeds stays FP64).
 template <int D, typename R = double>
-__device__ inline void eom(const ccake_config& cfg, const Transport& kd, const EomIn<D, R>& in, double td,
+__device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, const EomIn<D, R>& in, double td,
                            EomOut<R>& o) {
   const R t = R(td);
-  struct {
-    R eta, tau_pi, zeta, tau_Pi, delta_PiPi, delta_pipi, lambda_piPi, lambda_Pipi, phi1, phi3, phi6, phi7, tau_pipi;
-  } k{R(kd.eta), R(kd.tau_pi), R(kd.zeta), R(kd.tau_Pi), R(kd.delta_PiPi), R(kd.delta_pipi), R(kd.lambda_piPi),
-      R(kd.lambda_Pipi), R(kd.phi1), R(kd.phi3), R(kd.phi6), R(kd.phi7), R(kd.tau_pipi)};
   const R t2 = t * t;
   const R g = in.g, sig = in.sigma;
   // reciprocals: FP64 division is a long instruction sequence on the scarce

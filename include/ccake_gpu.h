@@ -167,6 +167,20 @@ ccake_status_t ccake_get_neighbours(ccake_ctx* ctx, int32_t* offsets, int32_t* i
 ccake_status_t ccake_eos_invert_batch(ccake_ctx* ctx, int32_t entropy_mode, int64_t n, const double* in4,
                                       double* tbqs, double* th16, int32_t* status, int32_t* iters);
 
+/* Seed rules of the batch inversion (seed_mode of ccake_eos_invert_batch_ex). */
+enum {
+  CCAKE_SEED_REFERENCE = 0, /* the reference's seed chain from the tbqs rows */
+  CCAKE_SEED_ANALYTIC = 1   /* entropy mode, conformal models: the exact inverse,
+                               accepted when max|F| < 1e-10, else Newton from it,
+                               then the reference's seed chain */
+};
+
+/* ccake_eos_invert_batch with a seed rule. No reference counterpart: the
+ * reference always seeds from the previous solution. */
+ccake_status_t ccake_eos_invert_batch_ex(ccake_ctx* ctx, int32_t entropy_mode, int32_t seed_mode, int64_t n,
+                                         const double* in4, double* tbqs, double* th16, int32_t* status,
+                                         int32_t* iters);
+
 /* Neighbour counts (the number of b != a with |r_a - r_b|^2 <= (2h)^2, the
  * same exact predicate as every other entry point) of n particles whose
  * positions are already in device memory, written to d_counts (device, n

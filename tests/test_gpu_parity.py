@@ -174,6 +174,39 @@ def test_eos_batch_inversion_parity(eos_kind, entropy, thermo_mode):
         assert relerr(thg[:, c], tho[:, c]) < 1e-11, c
 
 
+@pytest.mark.parametrize("eos_kind,thermo_mode", [(0, 0), (1, 1)])
+def test_eos_batch_analytic_seed(eos_kind, thermo_mode):
+    # exact inverses of the conformal models (cube roots by an FP32 seed and
+    # one FP64 Halley step): accepted without Newton steps. They recover the
+    # states the targets were made from; the oracle's Newton (reference
+    # stopping rule, absolute residual 1e-10) can stop short on a potential
+    # whose density is below that residual, so the roots are compared with
+    # the true states and the thermodynamics with the oracle's
+    import ctypes
+    rng = np.random.default_rng(12)
+    n = 4000
+    T = rng.uniform(0.05, 4.0, n)
+    mu = rng.uniform(-0.6, 0.6, (n, 3)) * (rng.uniform(size=(n, 1)) < 0.8)
+    X = np.column_stack([T, mu])
+    rc = ics.RunConfig(eos_kind=eos_kind, thermo_mode=thermo_mode)
+    cfg = O.make_config(rc)
+    tgt = np.zeros((n, 4))
+    for i in range(n):
+        o = np.zeros(17)
+        O.lib().orc_eos_full_thermo(ctypes.byref(cfg), None, 0, O._dp(X[i].copy()), O._dp(o))
+        tgt[i] = [o[1], o[2], o[3], o[4]]
+    seeds = np.tile([580 / 197.3269804, 0, 0, 0], (n, 1))
+    xo, tho, sto, _ = O.eos_invert_batch(rc, 1, tgt, seeds=seeds)
+    gpu = api.GpuHydro(rc)
+    xg, thg, stg, itg = gpu.eos_invert(1, tgt, seeds, seed_mode=1)
+    assert np.array_equal(stg, sto)
+    assert np.mean(itg == 0) > 0.99
+    assert relerr(xg[:, 0], X[:, 0]) < 1e-13
+    assert np.max(np.abs(xg[:, 1:] - X[:, 1:])) < 1e-13
+    for c in (4, 5, 9, 10, 12, 13):
+        assert relerr(thg[:, c], tho[:, c]) < 1e-11, c
+
+
 def test_gubser_flow_matches_analytic_on_gpu():
     p, rc = ics.gubser_2d(n_side=200)
     gpu = api.GpuHydro(rc)
