@@ -26,7 +26,7 @@ class CcakeConfig(ctypes.Structure):
         [(n, _f64) for n in (
             "hT", "hEta", "t0", "dt", "eos_c", "eos_T0", "eos_muB0", "eos_muQ0", "eos_muS0", "eta_over_s",
             "zeta_over_s", "zeta_cs2_A", "zeta_cs2_p", "zeta_peak_T", "zeta_peak_width", "xmin", "ymin",
-            "etamin", "freeze_out_T")]
+            "etamin", "freeze_out_T", "skin_frac")]
 
 
 class ParticlesSoA(ctypes.Structure):

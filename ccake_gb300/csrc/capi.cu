@@ -32,6 +32,12 @@ struct ccake_ctx {
   int32_t* ibuf = nullptr;
   double* d_table = nullptr;
   int records_form = 0;   // which smoothing record matches the state: 0 FP64, 1 mixed
+  // candidate list: skin (fm), validity and rebuild schedule
+  double skin = 0.0;
+  bool lists_valid = false;
+  int steps_since_build = 0;
+  cudaGraph_t build_graph = nullptr;
+  cudaGraphExec_t build_exec = nullptr;
 };
 
 namespace {
@@ -50,8 +56,12 @@ ccake_status_t fail(ccake_ctx* c, ccake_status_t s, const std::string& msg) {
 void drop_graph(ccake_ctx* ctx) {
   if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
   if (ctx->graph) cudaGraphDestroy(ctx->graph);
+  if (ctx->build_exec) cudaGraphExecDestroy(ctx->build_exec);
+  if (ctx->build_graph) cudaGraphDestroy(ctx->build_graph);
   ctx->graph_exec = nullptr;
   ctx->graph = nullptr;
+  ctx->build_exec = nullptr;
+  ctx->build_graph = nullptr;
 }
 
 void free_lists(ccake_ctx* ctx) {
@@ -62,9 +72,17 @@ void free_lists(ccake_ctx* ctx) {
   ctx->p.K = 0;
 }
 
+void free_candidates(ccake_ctx* ctx) {
+  if (ctx->p.cand_idx) cudaFree(ctx->p.cand_idx);
+  ctx->p.cand_idx = nullptr;
+  ctx->p.Kc = 0;
+  ctx->lists_valid = false;
+}
+
 void free_buffers(ccake_ctx* ctx) {
   drop_graph(ctx);
   free_lists(ctx);
+  free_candidates(ctx);
   if (ctx->dbuf) cudaFree(ctx->dbuf);
   if (ctx->ibuf) cudaFree(ctx->ibuf);
   ctx->dbuf = nullptr;
@@ -73,10 +91,10 @@ void free_buffers(ccake_ctx* ctx) {
 
 // Neighbour-cell grid: the reference's box (twice the IC lower corner,
 // mirrored; src/system_state.cpp:656-692), widened to hold every particle,
-// cell edge >= 2h.
-Grid make_grid(const ccake_config& cfg, const ccake_particles_soa* h) {
+// cell edge >= 2h + skin (the candidate-list radius).
+Grid make_grid(const ccake_config& cfg, const ccake_particles_soa* h, double skin) {
   Grid g{};
-  const double cut = 2.0 * cfg.hT;
+  const double cut = 2.0 * cfg.hT + skin;
   const double corner[3] = {cfg.xmin, cfg.ymin, cfg.etamin};
   const double* xs[3] = {h->x, h->y, h->eta};
   for (int k = 0; k < 3; k++) {
@@ -143,9 +161,42 @@ void enqueue_passB(ccake_ctx* ctx, int mode, double dt_sub) {
   else launch_passB(ctx->rc, ctx->p, mode, dt_sub, ctx->stream);
 }
 
+// Cell list and candidate list at the current positions.
+void enqueue_build(ccake_ctx* ctx) {
+  launch_build_cells(ctx->rc, ctx->p, ctx->stream);
+  launch_candidates(ctx->rc, ctx->p, ctx->stream);
+}
+
+// Steps a candidate list stays valid from time tau: a particle moves at most
+// dt * vmax per RK2 step in (x, y, eta_s) coordinates (|v| < 1 by
+// construction, v^eta < 1/tau), so no pair can close from beyond 2h + skin to
+// within 2h while R dt vmax <= skin / 2.
+int build_every(const ccake_ctx* ctx, double tau) {
+  const double vmax = ctx->cfg.dim == 3 ? std::max(1.0, 1.0 / tau) : 1.0;
+  return std::max(1, (int)std::floor(ctx->skin / (2.0 * ctx->cfg.dt * vmax)));
+}
+
+// Rebuilds the lists when the schedule asks for it (before a step).
+ccake_status_t maybe_rebuild(ccake_ctx* ctx, bool graph) {
+  if (ctx->lists_valid && ctx->steps_since_build < build_every(ctx, ctx->t)) return CCAKE_OK;
+  if (graph) {
+    if (!ctx->build_exec) {
+      CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+      enqueue_build(ctx);
+      CK(cudaStreamEndCapture(ctx->stream, &ctx->build_graph));
+      CK(cudaGraphInstantiate(&ctx->build_exec, ctx->build_graph, 0));
+    }
+    CK(cudaGraphLaunch(ctx->build_exec, ctx->stream));
+  } else {
+    enqueue_build(ctx);
+  }
+  ctx->lists_valid = true;
+  ctx->steps_since_build = 0;
+  return CCAKE_OK;
+}
+
 void enqueue_substep(ccake_ctx* ctx, int sub) {
   const double dt = ctx->cfg.dt;
-  launch_build_cells(ctx->rc, ctx->p, ctx->stream);
   enqueue_passA(ctx);
   int mode = B_EOM | B_UPDATE | (sub == 2 ? B_WRITE_Y0 : 0);
   enqueue_passB(ctx, mode, sub == 1 ? 0.5 * dt : dt);
@@ -235,6 +286,7 @@ ccake_status_t ccake_ctx_create(const ccake_config* cfg, ccake_ctx** out) {
   if (cfg->coord != 0) return CCAKE_ERR_INVALID;
   if (cfg->eos_kind != 0 && cfg->eos_kind != 1) return CCAKE_ERR_INVALID;
   if (cfg->precision != 0 && cfg->precision != 1) return CCAKE_ERR_INVALID;
+  if (!(cfg->skin_frac >= 0.0)) return CCAKE_ERR_INVALID;
   if (!(cfg->hT > 0) || !(cfg->t0 > 0) || !(cfg->dt > 0)) return CCAKE_ERR_INVALID;
   if (cfg->dim == 3 && cfg->factorized_kernel) return CCAKE_ERR_INVALID;
   ccake_ctx* ctx = new ccake_ctx;
@@ -248,6 +300,11 @@ ccake_status_t ccake_ctx_create(const ccake_config* cfg, ccake_ctx** out) {
   const int D = cfg->dim;
   const double h = cfg->hT;
   rc.cut2 = (2.0 * h) * (2.0 * h);
+  // skin: at least one RK2 step of travel at the largest coordinate speed
+  // (tau only grows from t0), so that a list lasts a step or more
+  const double vmax0 = D == 3 ? std::max(1.0, 1.0 / cfg->t0) : 1.0;
+  ctx->skin = std::max((cfg->skin_frac > 0.0 ? cfg->skin_frac : 0.1) * 2.0 * h, 2.0 * cfg->dt * vmax0 * (1.0 + 1e-6));
+  rc.cutc2 = (2.0 * h + ctx->skin) * (2.0 * h + ctx->skin);
   rc.inv_h = 1.0 / h;
   rc.wn = knorm(D) / std::pow(h, D);
   rc.wn2 = knorm2(D) / std::pow(h, D);
@@ -282,7 +339,7 @@ ccake_status_t ccake_load_particles(ccake_ctx* ctx, const ccake_particles_soa* h
   free_buffers(ctx);
   const int64_t n = h->n;
   ctx->n = n;
-  ctx->rc.grid = make_grid(ctx->cfg, h);
+  ctx->rc.grid = make_grid(ctx->cfg, h, ctx->skin);
   const Grid& g = ctx->rc.grid;
   // storage order: by neighbour cell, then by input index
   std::vector<int64_t> key(n);
@@ -296,7 +353,7 @@ ccake_status_t ccake_load_particles(ccake_ctx* ctx, const ccake_particles_soa* h
   std::stable_sort(ctx->perm.begin(), ctx->perm.end(), [&](int32_t a, int32_t b) { return key[a] < key[b]; });
   // device memory: one double slab, one int slab
   const size_t nd = (size_t)n * kDoublesPerParticle + (size_t)kTotBlocks * 6 + 8;
-  const size_t ni = (size_t)n * 7 + (size_t)g.ncell * 2 + 1 + NERR + 2 * (size_t)scan_tiles(g.ncell) + 1 + 8;
+  const size_t ni = (size_t)n * 8 + (size_t)g.ncell * 2 + 1 + NERR + 2 * (size_t)scan_tiles(g.ncell) + 1 + 8;
   if (cudaMalloc(&ctx->dbuf, nd * sizeof(double)) != cudaSuccess) return fail(ctx, CCAKE_ERR_NOMEM, "device allocation");
   if (cudaMalloc(&ctx->ibuf, ni * sizeof(int32_t)) != cudaSuccess) return fail(ctx, CCAKE_ERR_NOMEM, "device allocation");
   CK(cudaMemsetAsync(ctx->dbuf, 0, nd * sizeof(double), ctx->stream));
@@ -320,7 +377,7 @@ ccake_status_t ccake_load_particles(ccake_ctx* ctx, const ccake_particles_soa* h
   int32_t* ip = ctx->ibuf;
   auto itake = [&](size_t k) { int32_t* r = ip; ip += k; return r; };
   p.eos_id = itake(n); p.eos_iters = itake(n); p.btrack = itake(n); p.freeze = itake(n);
-  p.cell_of = itake(n); p.cell_rank = itake(n); p.cell_idx = itake(n);
+  p.cell_of = itake(n); p.cell_rank = itake(n); p.cell_idx = itake(n); p.cand_cnt = itake(n);
   p.cell_count = itake(g.ncell); p.cell_start = itake(g.ncell + 1); p.err = itake(NERR);
   p.scan_aux = itake(2 * (size_t)scan_tiles(g.ncell) + 1);
   // upload permuted inputs
@@ -371,7 +428,30 @@ ccake_status_t ccake_initialize(ccake_ctx* ctx) {
   }
   launch_init_state(ctx->rc, ctx->p, ctx->stream);
   launch_init_invert(ctx->rc, ctx->eos, ctx->p, ctx->stream);
-  launch_build_cells(ctx->rc, ctx->p, ctx->stream);
+  // candidate-list capacity: 1.5x the largest count + 16 (a build flags an
+  // overflow, reported as CCAKE_ERR_CAPACITY)
+  {
+    launch_build_cells(ctx->rc, ctx->p, ctx->stream);
+    const int keep = ctx->p.Kc;
+    ctx->p.Kc = 0;   // count only
+    launch_candidates(ctx->rc, ctx->p, ctx->stream);
+    ctx->p.Kc = keep;
+    std::vector<int32_t> cnt((size_t)ctx->n);
+    CK(cudaMemcpyAsync(cnt.data(), ctx->p.cand_cnt, ctx->n * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    const int mx = *std::max_element(cnt.begin(), cnt.end());
+    const int Kc = ((mx * 3 / 2 + 16) + 15) / 16 * 16;
+    if (Kc > ctx->p.Kc) {
+      drop_graph(ctx);
+      free_candidates(ctx);
+      if (cudaMalloc(&ctx->p.cand_idx, (size_t)Kc * ctx->n * sizeof(int32_t)) != cudaSuccess)
+        return fail(ctx, CCAKE_ERR_NOMEM, "candidate list allocation");
+      ctx->p.Kc = Kc;
+    }
+  }
+  ctx->lists_valid = false;
+  s = maybe_rebuild(ctx, false);
+  if (s) return s;
   launch_passA(ctx->rc, ctx->eos, ctx->p, A_SMOOTH_ONLY, ctx->stream);   // initial sigma
   launch_init_ext(ctx->rc, ctx->p, ctx->stream);
   launch_passA(ctx->rc, ctx->eos, ctx->p, A_WITH_THERMO, ctx->stream);   // initial smoothing
@@ -398,7 +478,11 @@ ccake_status_t ccake_step(ccake_ctx* ctx, int32_t n_steps) {
     CK(cudaStreamEndCapture(ctx->stream, &ctx->graph));
     CK(cudaGraphInstantiate(&ctx->graph_exec, ctx->graph, 0));
   }
-  for (int k = 0; k < n_steps; k++) CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
+  for (int k = 0; k < n_steps; k++) {
+    if ((s = maybe_rebuild(ctx, true))) return s;
+    CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
+    ctx->steps_since_build++;
+  }
   s = check_errors(ctx);
   Clock c;
   CK(cudaMemcpy(&c, ctx->p.clock, sizeof(Clock), cudaMemcpyDeviceToHost));
@@ -415,7 +499,11 @@ ccake_status_t ccake_step_timed(ccake_ctx* ctx, int32_t n_steps, float* device_m
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
   CK(cudaEventRecord(e0, ctx->stream));
-  for (int k = 0; k < n_steps; k++) CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
+  for (int k = 0; k < n_steps; k++) {
+    if ((s = maybe_rebuild(ctx, true))) return s;
+    CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
+    ctx->steps_since_build++;
+  }
   CK(cudaEventRecord(e1, ctx->stream));
   CK(cudaEventSynchronize(e1));
   CK(cudaEventElapsedTime(device_ms, e0, e1));
@@ -441,13 +529,14 @@ ccake_status_t ccake_profile_phases(ccake_ctx* ctx, int32_t n_steps, double* ms3
   for (int k = 0; k < n_steps; k++) {
     for (int sub = 1; sub <= 2; sub++) {
       CK(cudaEventRecord(ev[0], ctx->stream));
-      launch_build_cells(ctx->rc, ctx->p, ctx->stream);
+      if (sub == 1 && (s = maybe_rebuild(ctx, false))) return s;
       CK(cudaEventRecord(ev[1], ctx->stream));
       enqueue_passA(ctx);
       CK(cudaEventRecord(ev[2], ctx->stream));
       enqueue_passB(ctx, B_EOM | B_UPDATE | (sub == 2 ? B_WRITE_Y0 : 0), sub == 1 ? 0.5 * dt : dt);
       CK(cudaEventRecord(ev[3], ctx->stream));
       launch_clock(ctx->p, sub, dt, ctx->stream);
+      if (sub == 2) ctx->steps_since_build++;
       CK(cudaEventSynchronize(ev[3]));
       float m;
       for (int q = 0; q < 3; q++) {
@@ -469,8 +558,8 @@ ccake_status_t ccake_device_bytes(const ccake_ctx* ctx, int64_t* bytes) {
   if (!ctx || !bytes) return CCAKE_ERR_INVALID;
   const int64_t n = ctx->n;
   const int64_t nd = n * kDoublesPerParticle;
-  const int64_t ni = n * 7 + (int64_t)ctx->rc.grid.ncell * 2 + 2 * (int64_t)scan_tiles(ctx->rc.grid.ncell);
-  *bytes = nd * 8 + ni * 4 + (int64_t)ctx->p.K * n * 12;
+  const int64_t ni = n * 8 + (int64_t)ctx->rc.grid.ncell * 2 + 2 * (int64_t)scan_tiles(ctx->rc.grid.ncell);
+  *bytes = nd * 8 + ni * 4 + (int64_t)ctx->p.K * n * 12 + (int64_t)ctx->p.Kc * n * 4;
   return CCAKE_OK;
 }
 
@@ -478,6 +567,11 @@ ccake_status_t ccake_build_neighbours(ccake_ctx* ctx) {
   if (!ctx) return CCAKE_ERR_INVALID;
   if (!ctx->loaded) return fail(ctx, CCAKE_ERR_STATE, "load particles first");
   launch_build_cells(ctx->rc, ctx->p, ctx->stream);
+  if (ctx->p.cand_idx) {
+    launch_candidates(ctx->rc, ctx->p, ctx->stream);
+    ctx->lists_valid = true;
+    ctx->steps_since_build = 0;
+  }
   return check_errors(ctx);
 }
 
@@ -485,7 +579,8 @@ ccake_status_t ccake_smooth_fields(ccake_ctx* ctx) {
   if (!ctx) return CCAKE_ERR_INVALID;
   if (!ctx->initialized) return fail(ctx, CCAKE_ERR_STATE, "initialize first");
   ensure_records(ctx, 0);   // the phase entry points run the FP64 form
-  launch_build_cells(ctx->rc, ctx->p, ctx->stream);
+  ccake_status_t s = maybe_rebuild(ctx, false);   // lists valid by the schedule are kept
+  if (s) return s;
   launch_passA(ctx->rc, ctx->eos, ctx->p, A_SMOOTH_ONLY, ctx->stream);
   return check_errors(ctx);
 }

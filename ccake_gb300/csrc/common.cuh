@@ -65,6 +65,7 @@ struct RunConst {
   ccake_config cfg;
   Grid grid;
   double cut2;           // (2h)^2
+  double cutc2;          // (2h + skin)^2, radius of the candidate list
   double inv_h;
   double wn, wn2;        // W normalisations knorm/h^D, knorm2/h^D
   double gn, gn2;        // grad W normalisations kgrad/h^(D+1), kgrad2/h^(D+1)

@@ -193,6 +193,35 @@ __global__ void k_sort_cells(Ptrs p, int ncell) {
   }
 }
 
+// Candidate (Verlet) list of particle i: every b != i in the 3^D cells around
+// it whose FP32 squared distance is not above (2h + skin)^2 by more than its
+// error bound (so no pair within 2h + skin in FP64 is dropped), in cell order.
+// With Kc = 0 it only counts.
+template <int D>
+__global__ void __launch_bounds__(kBlock) k_candidates(RunConst rc, Ptrs p) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.n) return;
+  const int n = p.n;
+  const double xa[3] = {p.y[Y_X0 * n + i], p.y[Y_X1 * n + i], D == 3 ? p.y[Y_X2 * n + i] : 0.0};
+  const float4 pa = p.posf[i];
+  const float cut2f = (float)rc.cutc2 * 1.000001f;
+  int rlo[D == 3 ? 9 : 3], rhi[D == 3 ? 9 : 3];
+  const int nr = neighbour_ranges<D>(rc.grid, p.cell_start, xa, rlo, rhi);
+  const int Kc = p.Kc;
+  int c = 0;
+  for (int r = 0; r < nr; r++)
+    for (int j = rlo[r]; j < rhi[r]; j++) {
+      const int b = p.cell_idx[j];
+      if (b == i) continue;
+      float d2f, bound;
+      if (!maybe_neighbour<D>(pa, __ldg(&p.posf[b]), cut2f, d2f, bound)) continue;
+      if (c < Kc) p.cand_idx[(size_t)c * n + i] = b;
+      c++;
+    }
+  if (c > Kc && Kc > 0) atomicAdd(&p.err[E_NBR_OVERFLOW], 1);
+  p.cand_cnt[i] = c;
+}
+
 // Iterates the 3^D neighbour cells of a position; calls f(b) for every
 // particle b != a in them.
 template <int D, class F>
@@ -238,18 +267,17 @@ __global__ void __launch_bounds__(kBlock) k_passA(RunConst rc, EosDev eos, Ptrs 
   // FP64 predicate, W and the grad-W factor on the survivors.
   __shared__ int32_t surv[kSurv][kBlock];
   const int tid = threadIdx.x;
-  const Grid& gr = rc.grid;
   const float4 pa = p.posf[i];
   const float cut2f = (float)rc.cut2 * 1.000001f;
-  int rlo[D == 3 ? 9 : 3], rhi[D == 3 ? 9 : 3];
-  const int nr = neighbour_ranges<D>(gr, p.cell_start, xa, rlo, rhi);
-  int r = 0, j = nr > 0 ? rlo[0] : 0;
-  while (r < nr) {
+  // the candidate list of the last build holds every b that can be within
+  // 2h now
+  const int nc = min(p.cand_cnt[i], p.Kc);
+  int kk = 0;
+  while (kk < nc) {
     int ns = 0;
-    while (r < nr && ns < kSurv) {            // phase 1 (FP32)
-      if (j >= rhi[r]) { if (++r < nr) j = rlo[r]; continue; }
-      const int b = p.cell_idx[j++];
-      if (b == i) continue;
+    while (kk < nc && ns < kSurv) {           // phase 1 (FP32)
+      const int b = p.cand_idx[(size_t)kk * n + i];
+      kk++;
       const float4 pb = __ldg(&p.posf[b]);
       // the screen never drops a pair the exact predicate below accepts, so
       // the neighbour set is the FP64 one
@@ -617,6 +645,12 @@ void launch_build_cells(const RunConst& rc, const Ptrs& p, cudaStream_t s) {
   k_scan_add<<<(ncell + 255) / 256, 256, 0, s>>>(p.cell_start, p.scan_aux, ncell, ntiles);
   k_scatter<<<nb, kBlock, 0, s>>>(p);
   k_sort_cells<<<(int)(((int64_t)ncell * 32 + 255) / 256), 256, 0, s>>>(p, ncell);
+}
+
+void launch_candidates(const RunConst& rc, const Ptrs& p, cudaStream_t s) {
+  const int nb = (p.n + kBlock - 1) / kBlock;
+  if (rc.cfg.dim == 3) k_candidates<3><<<nb, kBlock, 0, s>>>(rc, p);
+  else k_candidates<2><<<nb, kBlock, 0, s>>>(rc, p);
 }
 
 void launch_passA(const RunConst& rc, const EosDev& eos, const Ptrs& p, int mode, cudaStream_t s) {

@@ -44,6 +44,11 @@ struct Ptrs {
   int32_t* nbr_idx;      // K * n
   double* nbr_f;         // K * n
   int K;                 // list capacity per particle
+  // candidate (Verlet) list: every b within 2h + skin of a at the last
+  // build, k-major like the neighbour list; rebuilt every few steps
+  int32_t* cand_idx;     // Kc * n
+  int32_t* cand_cnt;     // n
+  int Kc;
   // mixed-precision form (precision = 1): FP32 neighbour records
   float* recAf;          // RAF * n
   float* recBf;          // RBF * n
@@ -65,6 +70,7 @@ enum : int { A_SMOOTH_ONLY = 0, A_WITH_THERMO = 1 };
 enum : int { B_GRADS = 1, B_EOM = 2, B_DERIVS = 4, B_UPDATE = 8, B_WRITE_Y0 = 16 };
 
 void launch_build_cells(const RunConst& rc, const Ptrs& p, cudaStream_t s);
+void launch_candidates(const RunConst& rc, const Ptrs& p, cudaStream_t s);
 void launch_passA(const RunConst& rc, const EosDev& eos, const Ptrs& p, int mode, cudaStream_t s);
 void launch_thermo(const RunConst& rc, const EosDev& eos, const Ptrs& p, cudaStream_t s);
 void launch_passB(const RunConst& rc, const Ptrs& p, int mode, double dt_sub, cudaStream_t s);

@@ -58,61 +58,40 @@ __global__ void __launch_bounds__(kBlock) k_passA_mixed(RunConst rc, Ptrs p) {
   const float wn = (float)rc.wn, wn2 = (float)rc.wn2, gn = (float)rc.gn, gn2 = (float)rc.gn2;
   const int K = p.K;
   float* nf = reinterpret_cast<float*>(p.nbr_f);
-  const double xa[3] = {p.y[Y_X0 * n + i], p.y[Y_X1 * n + i], D == 3 ? p.y[Y_X2 * n + i] : 0.0};
-  int rlo[D == 3 ? 9 : 3], rhi[D == 3 ? 9 : 3];
-  const int nr = neighbour_ranges<D>(rc.grid, p.cell_start, xa, rlo, rhi);
+  // the candidate list of the last build holds every b that can be within
+  // 2h now (most are); its entries are streamed two iterations ahead of use
+  const int nc = min(p.cand_cnt[i], p.Kc);
   int nn = 0;
-  // candidates in groups of four: the cell-list entries, then the records,
-  // then the energy records of the accepted ones are each loaded together so
-  // that their latencies overlap; accepted pairs are visited in candidate
-  // order, as a one-at-a-time loop would
-  constexpr int U = 4;
-  for (int r = 0; r < nr; r++) {
-    const int je = rhi[r];
-    for (int j0 = rlo[r]; j0 < je; j0 += U) {
-      int bb[U];
-      float4 bh[U], bl[U], be[U];
-      float d2[U];
-      bool ok[U];
-#pragma unroll
-      for (int u = 0; u < U; u++) bb[u] = (j0 + u < je) ? p.cell_idx[j0 + u] : i;
-#pragma unroll
-      for (int u = 0; u < U; u++) {
-        bh[u] = __ldg(&ra[(size_t)bb[u] * SA]);
-        bl[u] = __ldg(&ra[(size_t)bb[u] * SA + 1]);
-      }
-#pragma unroll
-      for (int u = 0; u < U; u++) {
-        const float dx = (ah.x - bh[u].x) + (al.x - bl[u].x);
-        const float dy = (ah.y - bh[u].y) + (al.y - bl[u].y);
-        const float dz = (D == 3) ? (ah.z - bh[u].z) + (al.z - bl[u].z) : 0.0f;
-        d2[u] = dx * dx + dy * dy + dz * dz;
-        ok[u] = (d2[u] <= cut2) && bb[u] != i;
-      }
-#pragma unroll
-      for (int u = 0; u < U; u++)
-        if (ok[u]) be[u] = __ldg(&ra[(size_t)bb[u] * SA + 2]);
-#pragma unroll
-      for (int u = 0; u < U; u++) {
-        if (!ok[u]) continue;
-        // W (src/kernel.cpp:34-48) and grad_a W = fg (r_a - r_b) (:95-118)
-        const float rs = d2[u] > 0.0f ? rsqrtf(d2[u]) : 0.0f;
-        const float q = d2[u] * rs * ih;
-        const float z = fmaxf(2.0f - q, 0.0f), qq = q * q;
-        const float W = q < 1.0f ? wn * (1.0f - 1.5f * qq + 0.75f * q * qq) : wn2 * z * z * z;
-        const float fg = q < 1.0f ? gn2 * (1.5f * q - 2.0f) * ih : gn * rs * z * z;
-        if (nn < K) {
-          p.nbr_idx[(size_t)nn * n + i] = bb[u];
-          nf[(size_t)nn * n + i] = fg;
-        }
-        nn++;
-        sl.add(bh[u].w * W);
-        s0.add(be[u].x * W);
-        s1.add(be[u].y * W);
-        s2.add(be[u].z * W);
-        s3.add(be[u].w * W);
-      }
+  int bq0 = 0, bq1 = 0;
+  if (nc > 0) bq0 = p.cand_idx[i];
+  if (nc > 1) bq1 = p.cand_idx[(size_t)n + i];
+  for (int kk = 0; kk < nc; kk++) {
+    const int b = bq0;
+    bq0 = bq1;
+    if (kk + 2 < nc) bq1 = p.cand_idx[(size_t)(kk + 2) * n + i];
+    const float4 bh = __ldg(&ra[(size_t)b * SA]), bl = __ldg(&ra[(size_t)b * SA + 1]);
+    const float dx = (ah.x - bh.x) + (al.x - bl.x);
+    const float dy = (ah.y - bh.y) + (al.y - bl.y);
+    const float dz = (D == 3) ? (ah.z - bh.z) + (al.z - bl.z) : 0.0f;
+    const float d2 = dx * dx + dy * dy + dz * dz;
+    if (!(d2 <= cut2)) continue;
+    const float4 be = __ldg(&ra[(size_t)b * SA + 2]);
+    // W (src/kernel.cpp:34-48) and grad_a W = fg (r_a - r_b) (:95-118)
+    const float rs = d2 > 0.0f ? rsqrtf(d2) : 0.0f;
+    const float q = d2 * rs * ih;
+    const float z = fmaxf(2.0f - q, 0.0f), qq = q * q;
+    const float W = q < 1.0f ? wn * (1.0f - 1.5f * qq + 0.75f * q * qq) : wn2 * z * z * z;
+    const float fg = q < 1.0f ? gn2 * (1.5f * q - 2.0f) * ih : gn * rs * z * z;
+    if (nn < K) {
+      p.nbr_idx[(size_t)nn * n + i] = b;
+      nf[(size_t)nn * n + i] = fg;
     }
+    nn++;
+    sl.add(bh.w * W);
+    s0.add(be.x * W);
+    s1.add(be.y * W);
+    s2.add(be.z * W);
+    s3.add(be.w * W);
   }
   if (nn > K) atomicAdd(&p.err[E_NBR_OVERFLOW], 1);
   const double u3[3] = {p.y[Y_U0 * n + i], p.y[Y_U1 * n + i], D == 3 ? p.y[Y_U2 * n + i] : 0.0};

@@ -87,6 +87,7 @@ __device__ __forceinline__ void write_recAf(const Ptrs& p, int i, const double* 
   ra[0] = make_float4(hi[0], hi[1], hi[2], (float)m);
   ra[1] = make_float4(lo[0], lo[1], lo[2], 0.0f);
   ra[2] = make_float4((float)(m * ext[0]), (float)(m * ext[1]), (float)(m * ext[2]), (float)(m * ext[3]));
+  p.posf[i] = make_float4(hi[0], hi[1], hi[2], 0.0f);
 }
 
 // EoS inversion of the smoothed densities of particle i, pi^{mu nu} and Pi

@@ -60,6 +60,7 @@ class RunConfig:
     ymin: float = -5.0
     etamin: float = -0.1
     freeze_out_T: float = 150.0 / HBARC_MEVFM
+    skin_frac: float = 0.0         # candidate-list skin / 2h (0: 0.1), GPU only
 
 
 @dataclasses.dataclass

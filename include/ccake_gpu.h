@@ -55,6 +55,9 @@ typedef struct ccake_config {
   double zeta_peak_T, zeta_peak_width;
   double xmin, ymin, etamin;  /* lower corner of the IC grid (IC header, src/BSQHydro.cpp:241-249) */
   double freeze_out_T;        /* fm^-1 */
+  double skin_frac;           /* candidate-list skin as a fraction of 2h (0: 0.1); the
+                                 list is rebuilt every R steps, R = floor(skin / (2 dt vmax)),
+                                 vmax = max(1, 1/tau) in Milne (x, y, eta_s) coordinates */
 } ccake_config;
 
 /* Host struct-of-arrays particle input, the columns of the reference's

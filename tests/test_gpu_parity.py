@@ -135,6 +135,24 @@ def test_neighbours_after_motion_bit_exact():
     assert csr_rows(go, gi) == csr_rows(oo, oi)
 
 
+def test_candidate_list_schedule_does_not_change_results():
+    # the candidate list is rebuilt every floor(skin / (2 dt vmax)) steps; a
+    # skin of one step's travel rebuilds it every step. Both find the same
+    # neighbours, so the runs agree to rounding (summation order differs)
+    p, rc = cases()["hotspots"]
+    out = {}
+    for frac in (0.0, 1e-6):
+        g = api.GpuHydro(dataclasses.replace(rc, skin_frac=frac))
+        g.load(p)
+        g.initialize()
+        g.step(25)
+        out[frac] = {f: g.get(f) for f in ("x", "u0", "ext_s", "T", "ext_shv0")}
+        out[frac]["btrack"] = g.get_int("btrack")
+    for f in ("x", "u0", "ext_s", "T", "ext_shv0"):
+        assert relerr(out[1e-6][f], out[0.0][f]) < 1e-12, f
+    assert np.array_equal(out[1e-6]["btrack"], out[0.0]["btrack"])
+
+
 def test_runs_are_bitwise_reproducible():
     p, rc = cases()["hotspots"]
     outs = []
