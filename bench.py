@@ -345,6 +345,100 @@ def run_e2e(p, rc, steps):
             "what": "ccake_load_particles + ccake_initialize + ccake_step(K) + ccake_copy_out of 11 fields"}
 
 
+def run_eos_table(args):
+    """EoS-inversion stress test: the synthetic 4-D table (151 x 41^3 nodes,
+    FP64), 2M states uniform in its (T, mu) box mapped forward to
+    (e, rhoB, rhoS, rhoQ) through the table and inverted on the GPU (energy
+    mode, the reference's seed chain and cs2 guards). Reports inversions/s,
+    Newton iterations, the rate of rows solved by a fallback model or not at
+    all, and the error of table-solved rows against the drawn states."""
+    import torch
+    from ccake_gb300 import api, build, eos_table, ics
+    build.build()
+    n_rows = args.eos_rows
+    n, lo, d, fields = eos_table.synthetic_table()
+    conf5, cdiag5 = eos_table.fallback_scales()
+    rc = ics.RunConfig(eos_kind=2, thermo_mode=1)
+    g = api.GpuHydro(rc)
+    g.set_eos_table(n, lo, d, fields, conf5, cdiag5)
+    x_true = eos_table.sample_states(n_rows)
+    fw = g.eos_thermo(0, x_true)
+    tgt = np.ascontiguousarray(np.column_stack([fw[:, 5], fw[:, 2], fw[:, 3], fw[:, 4]]))
+    dev = torch.device("cuda")
+    d_in = torch.from_numpy(tgt).to(dev)
+    seed0 = torch.tensor([580 / 197.3269804, 0, 0, 0], dtype=torch.float64, device=dev).repeat(n_rows, 1)
+    d_x = seed0.clone()
+    d_th = torch.empty((n_rows, 16), dtype=torch.float64, device=dev)
+    d_st = torch.empty(n_rows, dtype=torch.int32, device=dev)
+    d_it = torch.empty(n_rows, dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def run_once():
+        d_x.copy_(seed0)
+        g.eos_invert_device(0, 0, n_rows, d_in.data_ptr(), d_x.data_ptr(), d_th.data_ptr(), d_st.data_ptr(),
+                            d_it.data_ptr(), stream.cuda_stream)
+
+    for _ in range(max(1, args.warmup)):
+        run_once()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        run_once()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    x = d_x.cpu().numpy()
+    st = d_st.cpu().numpy()
+    it = d_it.cpu().numpy()
+    tab = st == 0
+    hb = eos_table.HBARC
+    # states where the EoS is thermodynamically stable (positive-definite
+    # Hessian of p, 0 <= cs2 <= 1): the table root is unique there
+    Hm = np.zeros((n_rows, 4, 4))
+    Hm[:, 0, 0] = fw[:, 16]
+    for a_, c_ in ((1, 13), (2, 14), (3, 15)):
+        Hm[:, 0, a_] = Hm[:, a_, 0] = fw[:, c_]
+    Hm[:, 1, 1], Hm[:, 2, 2], Hm[:, 3, 3] = fw[:, 7], fw[:, 8], fw[:, 9]
+    stable = (np.linalg.eigvalsh(Hm)[:, 0] > 0) & (fw[:, 6] >= 0) & (fw[:, 6] <= 1)
+    del Hm
+    err_T = np.abs(x[tab, 0] / x_true[tab, 0] - 1.0)
+    err_mu = np.abs(x[tab, 1:] - x_true[tab, 1:]) * hb
+    ts = tab & stable
+    err_Ts = np.abs(x[ts, 0] / x_true[ts, 0] - 1.0)
+    err_mus = np.abs(x[ts, 1:] - x_true[ts, 1:]) * hb
+    # residual of the table rows against their targets
+    fr = g.eos_thermo(0, x[tab])
+    res = np.max(np.abs(np.column_stack([fr[:, 5], fr[:, 2], fr[:, 3], fr[:, 4]]) - tgt[tab]), axis=1)
+    line = {"metric": "EoS inversions/s (2M states, synthetic 4-D table 151x41^3, energy mode)",
+            "workload": "eos-table", "value": n_rows / (ms * 1e-3), "unit": "inversions/s",
+            "ms_per_batch": ms, "rows": n_rows, "steps": args.steps, "warmup": args.warmup, "dtype": "f64",
+            "seed": "reference chain (580 MeV forced seed, conformal-diagonal analytic seed), no learned seed",
+            "iterations": {"mean": float(it.mean()), "p99": float(np.percentile(it, 99)), "max": int(it.max())},
+            "table_rate": float(tab.mean()), "fallback_rate": float(np.mean(st > 0)),
+            "fail_rate": float(np.mean(st < 0)),
+            "stable_rate": float(stable.mean()),
+            "max_err_table_rows": {"T_rel": float(err_T.max()), "mu_GeV": float(err_mu.max()),
+                                   "p99_T_rel": float(np.percentile(err_T, 99)),
+                                   "residual_fm": float(res.max())},
+            "max_err_stable_table_rows": {"T_rel": float(err_Ts.max()), "mu_GeV": float(err_mus.max()),
+                                          "p99_T_rel": float(np.percentile(err_Ts, 99))},
+            "note": "rows in the band where this EoS is thermodynamically unstable (T ~ 0.10-0.19 GeV) "
+                    "fail the reference's cs2 guard and fall back down the chain"}
+    if not args.no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle_py as O
+        O.build()
+        ot = O.OracleTable(n, lo, d, fields, conf5, cdiag5)
+        m = min(n_rows, args.eos_cpu_rows)
+        t0 = time.perf_counter()
+        O.eos_invert_batch(rc, 0, tgt[:m], seeds=np.tile([580 / 197.3269804, 0, 0, 0], (m, 1)), table=ot)
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": m / dt, "unit": "inversions/s", "cores": os.cpu_count(), "kind": "port",
+                                "sample": f"the first {m} rows, oracle/ OpenMP on {os.cpu_count()} threads"}
+    print(json.dumps(line))
+
+
 def run_form_only(args, form):
     """Only the timed step loop of one precision form (for profiler launch
     lists); prints a partial line."""
@@ -372,6 +466,10 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--ref-steps", type=int, default=4, help="RK2 steps timed on the CPU")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", choices=["hotspots", "eos-table"], default="hotspots",
+                    help="hotspots: the 160k hot-spot event (default); eos-table: the EoS-inversion stress test")
+    ap.add_argument("--eos-rows", type=int, default=2_000_000)
+    ap.add_argument("--eos-cpu-rows", type=int, default=20_000)
     ap.add_argument("--form", choices=["fp64", "mixed"], default=None,
                     help="time only this form's step loop (profiler launch lists); partial output")
     args = ap.parse_args()
@@ -379,6 +477,8 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":
         run_reference(args, world, rank)
+    elif args.workload == "eos-table":
+        run_eos_table(args)
     elif args.form:
         run_form_only(args, args.form)
     else:

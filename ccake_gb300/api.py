@@ -86,6 +86,10 @@ def lib():
         L.ccake_get_neighbours.argtypes = [P, _ip, _ip, _i64, ctypes.POINTER(_i64)]
         L.ccake_eos_invert_batch.argtypes = [P, _i32, _i64, _dp, _dp, _dp, _ip, _ip]
         L.ccake_eos_invert_batch_ex.argtypes = [P, _i32, _i32, _i64, _dp, _dp, _dp, _ip, _ip]
+        L.ccake_eos_invert_device.argtypes = [P, _i32, _i32, _i64, ctypes.c_void_p, ctypes.c_void_p,
+                                              ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        L.ccake_set_eos_table.argtypes = [P, _ip, _dp, _dp, _dp, _dp, _dp]
+        L.ccake_eos_thermo_batch.argtypes = [P, _i32, _i64, _dp, _dp]
         _lib = L
     return _lib
 
@@ -200,6 +204,31 @@ class GpuHydro:
         self._check(lib().ccake_get_neighbours(self.h, _i(off), _i(idx), cnt.value, ctypes.byref(cnt)),
                     "neighbours")
         return off, idx[:cnt.value]
+
+    def set_eos_table(self, n, lo, d, fields, conf5, cdiag5):
+        """Uploads a tabulated EoS (eos_kind 2); see ccake_set_eos_table."""
+        n = np.ascontiguousarray(n, dtype=np.int32)
+        lo = np.ascontiguousarray(lo, dtype=np.float64)
+        d = np.ascontiguousarray(d, dtype=np.float64)
+        f = np.ascontiguousarray(fields, dtype=np.float64)
+        c5 = np.ascontiguousarray(conf5, dtype=np.float64)
+        d5 = np.ascontiguousarray(cdiag5, dtype=np.float64)
+        self._check(lib().ccake_set_eos_table(self.h, _i(n), _d(lo), _d(d), _d(f), _d(c5), _d(d5)), "set_eos_table")
+
+    def eos_thermo(self, chain_index, tbqs):
+        """17 model fields at rows (T, muB, muQ, muS) for EoS chain index chain_index."""
+        x = np.ascontiguousarray(tbqs, dtype=np.float64)
+        out = np.zeros((x.shape[0], 17))
+        self._check(lib().ccake_eos_thermo_batch(self.h, int(chain_index), x.shape[0], _d(x), _d(out)),
+                    "eos_thermo_batch")
+        return out
+
+    def eos_invert_device(self, entropy, seed_mode, n, in4_ptr, tbqs_ptr, th16_ptr, status_ptr, iters_ptr,
+                          stream_ptr=None):
+        """ccake_eos_invert_device on device pointers (ints); asynchronous on the stream."""
+        self._check(lib().ccake_eos_invert_device(self.h, int(entropy), int(seed_mode), int(n), in4_ptr, tbqs_ptr,
+                                                  th16_ptr, status_ptr, iters_ptr, stream_ptr),
+                    "eos_invert_device")
 
     def eos_invert(self, entropy, targets, seeds, seed_mode=0):
         """Batch inversion; seed_mode 0 reference seed chain, 1 analytic exact inverse first."""

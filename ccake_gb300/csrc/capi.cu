@@ -284,7 +284,7 @@ ccake_status_t ccake_ctx_create(const ccake_config* cfg, ccake_ctx** out) {
   *out = nullptr;
   if (cfg->dim != 2 && cfg->dim != 3) return CCAKE_ERR_INVALID;
   if (cfg->coord != 0) return CCAKE_ERR_INVALID;
-  if (cfg->eos_kind != 0 && cfg->eos_kind != 1) return CCAKE_ERR_INVALID;
+  if (cfg->eos_kind < 0 || cfg->eos_kind > 2) return CCAKE_ERR_INVALID;
   if (cfg->precision != 0 && cfg->precision != 1) return CCAKE_ERR_INVALID;
   if (!(cfg->skin_frac >= 0.0)) return CCAKE_ERR_INVALID;
   if (!(cfg->hT > 0) || !(cfg->t0 > 0) || !(cfg->dt > 0)) return CCAKE_ERR_INVALID;
@@ -316,9 +316,11 @@ ccake_status_t ccake_ctx_create(const ccake_config* cfg, ccake_ctx** out) {
   e.thermo_mode = cfg->thermo_mode;
   e.own = make_scales(cfg->eos_c, cfg->eos_T0, cfg->eos_muB0, cfg->eos_muQ0, cfg->eos_muS0);
   e.conf = e.cdiag = e.own;
-  double x4[4] = {cfg->freeze_out_T, 0, 0, 0}, o[17];
-  model_thermo(e, chain_model(e.kind, 0), x4, o);
-  rc.efreeze = o[5];
+  if (e.kind != 2) {   // a table kind sets it with the table
+    double x4[4] = {cfg->freeze_out_T, 0, 0, 0}, o[17];
+    model_thermo(e, chain_model(e.kind, 0), x4, o);
+    rc.efreeze = o[5];
+  }
   *out = ctx;
   return CCAKE_OK;
 }
@@ -403,6 +405,7 @@ ccake_status_t ccake_load_particles(ccake_ctx* ctx, const ccake_particles_soa* h
 ccake_status_t ccake_initialize(ccake_ctx* ctx) {
   if (!ctx) return CCAKE_ERR_INVALID;
   if (!ctx->loaded) return fail(ctx, CCAKE_ERR_STATE, "load particles first");
+  if (ctx->eos.kind == 2 && !ctx->d_table) return fail(ctx, CCAKE_ERR_STATE, "set the EoS table first");
   Clock c{ctx->cfg.t0, ctx->cfg.t0};
   CK(cudaMemcpyAsync(ctx->p.clock, &c, sizeof(Clock), cudaMemcpyHostToDevice, ctx->stream));
   ccake_status_t s = reset_errors(ctx);
@@ -708,6 +711,75 @@ ccake_status_t ccake_get_neighbours(ccake_ctx* ctx, int32_t* offsets, int32_t* i
   return check_errors(ctx);
 }
 
+ccake_status_t ccake_set_eos_table(ccake_ctx* ctx, const int32_t* n, const double* lo, const double* d,
+                                   const double* fields, const double* conf5, const double* cdiag5) {
+  if (!ctx || !n || !lo || !d || !fields || !conf5 || !cdiag5) return CCAKE_ERR_INVALID;
+  if (ctx->eos.kind != 2) return fail(ctx, CCAKE_ERR_INVALID, "eos_kind is not 2 (table)");
+  size_t nodes = 1;
+  for (int k = 0; k < 4; k++) {
+    if (n[k] < 1 || !(d[k] >= 0.0) || !std::isfinite(lo[k])) return fail(ctx, CCAKE_ERR_INVALID, "bad table axis");
+    nodes *= (size_t)n[k];
+  }
+  if (nodes > ((size_t)1 << 31)) return fail(ctx, CCAKE_ERR_INVALID, "table too large");
+  for (int q = 0; q < 5; q++)
+    if (!(conf5[q] > 0.0) || !(cdiag5[q] > 0.0)) return fail(ctx, CCAKE_ERR_INVALID, "bad fallback scales");
+  drop_graph(ctx);
+  if (ctx->d_table) cudaFree(ctx->d_table);
+  ctx->d_table = nullptr;
+  if (cudaMalloc(&ctx->d_table, nodes * 17 * sizeof(double)) != cudaSuccess)
+    return fail(ctx, CCAKE_ERR_NOMEM, "table allocation");
+  CK(cudaMemcpyAsync(ctx->d_table, fields, nodes * 17 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  EosDev& e = ctx->eos;
+  for (int k = 0; k < 4; k++) { e.tab.n[k] = n[k]; e.tab.lo[k] = lo[k]; e.tab.d[k] = d[k]; }
+  e.conf = make_scales(conf5[0], conf5[1], conf5[2], conf5[3], conf5[4]);
+  e.cdiag = make_scales(cdiag5[0], cdiag5[1], cdiag5[2], cdiag5[3], cdiag5[4]);
+  // e(T_FO, 0, 0, 0) from the table, evaluated on the host copy
+  EosDev host = e;
+  host.tab.f = fields;
+  double x4[4] = {ctx->cfg.freeze_out_T, 0, 0, 0}, o[17];
+  model_thermo(host, M_TABLE, x4, o);
+  ctx->rc.efreeze = o[5];
+  e.tab.f = ctx->d_table;
+  return CCAKE_OK;
+}
+
+ccake_status_t ccake_eos_thermo_batch(ccake_ctx* ctx, int32_t chain_index, int64_t n, const double* tbqs,
+                                      double* out17) {
+  if (!ctx || n < 0 || !tbqs || !out17) return CCAKE_ERR_INVALID;
+  if (chain_index < 0 || chain_index >= chain_len(ctx->eos.kind)) return CCAKE_ERR_INVALID;
+  if (ctx->eos.kind == 2 && !ctx->d_table) return fail(ctx, CCAKE_ERR_STATE, "set the EoS table first");
+  if (n == 0) return CCAKE_OK;
+  double *d_x = nullptr, *d_o = nullptr;
+  if (cudaMalloc(&d_x, n * 4 * sizeof(double)) != cudaSuccess) return fail(ctx, CCAKE_ERR_NOMEM, "allocation");
+  if (cudaMalloc(&d_o, n * 17 * sizeof(double)) != cudaSuccess) {
+    cudaFree(d_x);
+    return fail(ctx, CCAKE_ERR_NOMEM, "allocation");
+  }
+  cudaMemcpyAsync(d_x, tbqs, n * 4 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
+  launch_eos_thermo(ctx->eos, chain_index, n, d_x, d_o, ctx->stream);
+  cudaMemcpyAsync(out17, d_o, n * 17 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+  const cudaError_t err = cudaStreamSynchronize(ctx->stream);
+  cudaFree(d_x);
+  cudaFree(d_o);
+  if (err != cudaSuccess) return fail(ctx, CCAKE_ERR_CUDA, cudaGetErrorString(err));
+  CK(cudaGetLastError());
+  return CCAKE_OK;
+}
+
+ccake_status_t ccake_eos_invert_device(ccake_ctx* ctx, int32_t entropy_mode, int32_t seed_mode, int64_t n,
+                                       const double* d_in4, double* d_tbqs, double* d_th16, int32_t* d_status,
+                                       int32_t* d_iters, void* stream) {
+  if (!ctx || n < 0 || (n > 0 && (!d_in4 || !d_tbqs || !d_status))) return CCAKE_ERR_INVALID;
+  if (seed_mode != CCAKE_SEED_REFERENCE && seed_mode != CCAKE_SEED_ANALYTIC) return CCAKE_ERR_INVALID;
+  if (ctx->eos.kind == 2 && !ctx->d_table) return fail(ctx, CCAKE_ERR_STATE, "set the EoS table first");
+  if (n == 0) return CCAKE_OK;
+  launch_eos_batch(ctx->eos, entropy_mode, seed_mode, n, d_in4, d_tbqs, d_th16, d_status, d_iters,
+                   static_cast<cudaStream_t>(stream));
+  CK(cudaGetLastError());
+  return CCAKE_OK;
+}
+
 ccake_status_t ccake_eos_invert_batch(ccake_ctx* ctx, int32_t entropy_mode, int64_t n, const double* in4,
                                       double* tbqs, double* th16, int32_t* status, int32_t* iters) {
   return ccake_eos_invert_batch_ex(ctx, entropy_mode, CCAKE_SEED_REFERENCE, n, in4, tbqs, th16, status, iters);
@@ -718,6 +790,7 @@ ccake_status_t ccake_eos_invert_batch_ex(ccake_ctx* ctx, int32_t entropy_mode, i
                                          int32_t* iters) {
   if (!ctx || n < 0 || !in4 || !tbqs || !status) return CCAKE_ERR_INVALID;
   if (seed_mode != CCAKE_SEED_REFERENCE && seed_mode != CCAKE_SEED_ANALYTIC) return CCAKE_ERR_INVALID;
+  if (ctx->eos.kind == 2 && !ctx->d_table) return fail(ctx, CCAKE_ERR_STATE, "set the EoS table first");
   if (n == 0) return CCAKE_OK;
   double *d_in = nullptr, *d_x = nullptr, *d_th = nullptr;
   int32_t *d_st = nullptr, *d_it = nullptr;

@@ -213,7 +213,7 @@ __host__ __device__ inline bool newton_attempt(const EosDev& e, int model, int e
   // the previous iteration (the same values a fresh evaluation would give),
   // so an undamped iteration costs one density/Jacobian evaluation.
   int extra = -1;
-  double f[4], J[4][4];
+  double f[4], J[4][4], xgood[4] = {0.0, 0.0, 0.0, 0.0};
   bool have = false;
   const bool diag = (model == M_CDIAG);
   for (int it = 0; it < 100; it++) {
@@ -233,15 +233,34 @@ __host__ __device__ inline bool newton_attempt(const EosDev& e, int model, int e
       solve4(J, rhs, dx);
     }
     if (extra >= 0) {
+      // x met the residual test. Full steps continue (at most 8) until the
+      // relative step is below 1e-12; each is verified at the next iteration
+      // and, if its residual left the tolerance, the last verified point is
+      // returned (the point the reference's solver stops at).
+      if (extra > 0 && !(fres < 1e-10)) {
+        for (int i = 0; i < 4; i++) x[i] = xgood[i];
+        *iters += it;
+        return true;
+      }
       double y[4], rel = 0.0;
+      bool inbox = true;
       for (int i = 0; i < 4; i++) {
+        xgood[i] = x[i];
         y[i] = x[i] + dx[i];
         const double r = fabs(dx[i]) / fmax(fabs(x[i]), 1e-300);
         rel = rel > r ? rel : r;
+        // every iterate stays in the model's box (src/rootfinder.cpp:277-330)
+        inbox = inbox && (y[i] >= lo[i] && y[i] <= hi[i]);
       }
-      if (y[0] > 0 && isfinite(y[0])) for (int i = 0; i < 4; i++) x[i] = y[i];
+      const bool usable = y[0] > 0 && isfinite(y[0]) && inbox;
+      if (rel < 1e-12) {
+        if (usable) for (int i = 0; i < 4; i++) x[i] = y[i];
+        *iters += it + 1;
+        return true;
+      }
+      if (extra >= 8 || !usable) { *iters += it + 1; return true; }
+      for (int i = 0; i < 4; i++) x[i] = y[i];
       extra++;
-      if (rel < 1e-12 || extra >= 8) { *iters += it + 1; return true; }
       continue;
     }
     double lam = 1.0, y[4];
@@ -387,7 +406,7 @@ __host__ __device__ inline int eos_invert(const EosDev& e, int entropy, const do
       model_thermo(e, model, y, o);
       const double fres = fmax(fmax(fabs(o[1] - tgt[0]), fabs(o[2] - tgt[1])),
                                fmax(fabs(o[4] - tgt[2]), fabs(o[3] - tgt[3])));
-      if (fres < 1e-10 && !(o[6] < 0.0 || o[6] > 1.0)) {
+      if (fres < 1e-10 && o[6] >= 0.0 && o[6] <= 1.0) {
         for (int i = 0; i < 4; i++) x[i] = y[i];
         if (o_out)
           for (int i = 0; i < 17; i++) o_out[i] = o[i];
@@ -416,7 +435,7 @@ __host__ __device__ inline int eos_invert(const EosDev& e, int entropy, const do
     if (ok) {
       double o[17];
       model_thermo(e, model, y, o);
-      if (o[6] < 0.0 || o[6] > 1.0) continue;   // prohibit unstable / acausal cs2
+      if (!(o[6] >= 0.0 && o[6] <= 1.0)) continue;   // prohibit unstable / acausal cs2
       for (int i = 0; i < 4; i++) x[i] = y[i];
       if (o_out)
         for (int i = 0; i < 17; i++) o_out[i] = o[i];

@@ -613,6 +613,12 @@ __global__ void k_nbr_fill(RunConst rc, Ptrs p, const int32_t* off, int32_t* idx
   });
 }
 
+__global__ void k_eos_thermo(EosDev eos, int model, int64_t n, const double* tbqs, double* out17) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  model_thermo(eos, model, tbqs + 4 * i, out17 + 17 * i);
+}
+
 __global__ void k_eos_batch(EosDev eos, int entropy, int seed_mode, int64_t n, const double* in4, double* tbqs,
                             double* th16, int32_t* status, int32_t* iters) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -713,6 +719,12 @@ void launch_neighbour_fill(const RunConst& rc, const Ptrs& p, const int32_t* off
   const int nb = (p.n + kBlock - 1) / kBlock;
   if (rc.cfg.dim == 3) k_nbr_fill<3><<<nb, kBlock, 0, s>>>(rc, p, offsets, idx);
   else k_nbr_fill<2><<<nb, kBlock, 0, s>>>(rc, p, offsets, idx);
+}
+
+void launch_eos_thermo(const EosDev& eos, int chain_index, int64_t n, const double* tbqs, double* out17,
+                       cudaStream_t s) {
+  const int nb = (int)((n + kBlock - 1) / kBlock);
+  k_eos_thermo<<<nb, kBlock, 0, s>>>(eos, chain_model(eos.kind, chain_index), n, tbqs, out17);
 }
 
 void launch_eos_batch(const EosDev& eos, int entropy, int seed_mode, int64_t n, const double* in4, double* tbqs,

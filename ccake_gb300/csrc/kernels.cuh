@@ -87,6 +87,8 @@ void launch_pack_fp64(const RunConst& rc, const Ptrs& p, cudaStream_t s);
 void launch_pack_mixed(const RunConst& rc, const Ptrs& p, cudaStream_t s);
 void launch_passA_mixed(const RunConst& rc, const EosDev& eos, const Ptrs& p, cudaStream_t s);
 void launch_passB_mixed(const RunConst& rc, const Ptrs& p, int mode, double dt_sub, cudaStream_t s);
+void launch_eos_thermo(const EosDev& eos, int chain_index, int64_t n, const double* tbqs, double* out17,
+                       cudaStream_t s);
 void launch_eos_batch(const EosDev& eos, int entropy, int seed_mode, int64_t n, const double* in4, double* tbqs,
                       double* th16, int32_t* status, int32_t* iters, cudaStream_t s);
 

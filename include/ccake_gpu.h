@@ -170,6 +170,25 @@ ccake_status_t ccake_get_neighbours(ccake_ctx* ctx, int32_t* offsets, int32_t* i
 ccake_status_t ccake_eos_invert_batch(ccake_ctx* ctx, int32_t entropy_mode, int64_t n, const double* in4,
                                       double* tbqs, double* th16, int32_t* status, int32_t* iters);
 
+/* Tabulated EoS (eos_kind 2): uniform grid in (T, muB, muQ, muS) (fm^-1),
+ * n[k] points from lo[k] with spacing d[k], nodes row-major with muS fastest,
+ * 17 FP64 fields per node in the order p s rhoB rhoS rhoQ e cs2 chiBB chiQQ
+ * chiSS chiBQ chiBS chiQS chiTB chiTQ chiTS chiTT (fm units). conf5 / cdiag5:
+ * (c, T0, muB0, muQ0, muS0) of the conformal and conformal-diagonal models
+ * behind the table in the EoS chain. Copied to device memory; call after
+ * ccake_ctx_create and before ccake_initialize. Replaces the table loader of
+ * EquationOfState::init (src/eos_table.cpp:12-100,
+ * src/eos_initialization.cpp:216-501). */
+ccake_status_t ccake_set_eos_table(ccake_ctx* ctx, const int32_t* n, const double* lo, const double* d,
+                                   const double* fields, const double* conf5, const double* cdiag5);
+
+/* Model thermodynamics at n host rows tbqs (T, muB, muQ, muS) for EoS chain
+ * index chain_index (0 = first model of the chain), 17 values per row in the
+ * table's field order (NaN outside a table). Replaces
+ * EquationOfState::tbqs + get_full_thermo (include/eos.h:121-175). */
+ccake_status_t ccake_eos_thermo_batch(ccake_ctx* ctx, int32_t chain_index, int64_t n, const double* tbqs,
+                                      double* out17);
+
 /* Seed rules of the batch inversion (seed_mode of ccake_eos_invert_batch_ex). */
 enum {
   CCAKE_SEED_REFERENCE = 0, /* the reference's seed chain from the tbqs rows */
@@ -183,6 +202,14 @@ enum {
 ccake_status_t ccake_eos_invert_batch_ex(ccake_ctx* ctx, int32_t entropy_mode, int32_t seed_mode, int64_t n,
                                          const double* in4, double* tbqs, double* th16, int32_t* status,
                                          int32_t* iters);
+
+/* The same inversion on DEVICE arrays (same row layouts; th16 and iters may
+ * be NULL), launched on `stream` (a cudaStream_t, NULL for the default
+ * stream) without synchronising. No reference counterpart (batch form of
+ * EquationOfState::update_s for callers whose states live on the GPU). */
+ccake_status_t ccake_eos_invert_device(ccake_ctx* ctx, int32_t entropy_mode, int32_t seed_mode, int64_t n,
+                                       const double* d_in4, double* d_tbqs, double* d_th16, int32_t* d_status,
+                                       int32_t* d_iters, void* stream);
 
 /* Neighbour counts (the number of b != a with |r_a - r_b|^2 <= (2h)^2, the
  * same exact predicate as every other entry point) of n particles whose

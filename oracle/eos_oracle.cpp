@@ -150,6 +150,8 @@ void solve4(double A[4][4], double* b, double* xout) {
   }
 }
 
+inline double nan_max(double a, double b) { return a > b ? a : b; }
+
 // One solver attempt from a seed (replaces GSL hybrids in src/rootfinder.cpp:206-416).
 // Stopping rule: the reference's max |F_i| < 1e-10 (gsl_multiroot_test_residual,
 // include/rootfinder.h:36-37); once it holds, full Newton steps continue (at
@@ -160,25 +162,47 @@ bool newton_attempt(const Config& c, const Table* tab, int model, int entropy,
                     const double* tgt, const double* lo, const double* hi, double* x, int* iters) {
   const double tol = 1e-10;
   int extra = -1;
+  double xgood[4] = {0, 0, 0, 0};
   for (int it = 0; it < 100; it++) {
     double f[4], J[4][4];
     densities_and_jacobian(c, tab, model, entropy, x, f, J);
     double F[4] = {f[0] - tgt[0], f[1] - tgt[1], f[2] - tgt[2], f[3] - tgt[3]};
+    // maxima propagate NaN (std::max(a, NaN) would return a): a NaN residual
+    // fails the iterate, as GSL_EBADFUNC fails the reference's solver
     double fmax = 0;
-    for (int i = 0; i < 4; i++) fmax = std::max(fmax, std::fabs(F[i]));
+    for (int i = 0; i < 4; i++) fmax = nan_max(fmax, std::fabs(F[i]));
     if (!(fmax == fmax)) return false;  // NaN
     if (extra < 0 && fmax < tol) extra = 0;
     double rhs[4] = {-F[0], -F[1], -F[2], -F[3]}, dx[4];
     solve4(J, rhs, dx);
     if (extra >= 0) {
+      // x met the residual test. Full steps continue (at most 8) until the
+      // relative step is below 1e-12; each is verified at the next iteration
+      // and, if its residual left the tolerance, the last verified point is
+      // returned (the point the reference's solver stops at).
+      if (extra > 0 && !(fmax < tol)) {
+        for (int i = 0; i < 4; i++) x[i] = xgood[i];
+        *iters += it;
+        return true;
+      }
       double y[4], rel = 0;
+      bool inbox = true;
       for (int i = 0; i < 4; i++) {
+        xgood[i] = x[i];
         y[i] = x[i] + dx[i];
         rel = std::max(rel, std::fabs(dx[i]) / std::max(std::fabs(x[i]), 1e-300));
+        // every iterate stays in the model's box (src/rootfinder.cpp:277-330)
+        inbox = inbox && (y[i] >= lo[i] && y[i] <= hi[i]);
       }
-      if (y[0] > 0 && std::isfinite(y[0])) for (int i = 0; i < 4; i++) x[i] = y[i];
+      const bool usable = y[0] > 0 && std::isfinite(y[0]) && inbox;
+      if (rel < 1e-12) {
+        if (usable) for (int i = 0; i < 4; i++) x[i] = y[i];
+        *iters += it + 1;
+        return true;
+      }
+      if (extra >= 8 || !usable) { *iters += it + 1; return true; }
+      for (int i = 0; i < 4; i++) x[i] = y[i];
       extra++;
-      if (rel < 1e-12 || extra >= 8) { *iters += it + 1; return true; }
       continue;
     }
     // damped step: halve while the residual grows (at most 6 halvings)
@@ -190,7 +214,7 @@ bool newton_attempt(const Config& c, const Table* tab, int model, int entropy,
         double fy[4], Jy[4][4];
         densities_and_jacobian(c, tab, model, entropy, y, fy, Jy);
         double gmax = 0;
-        for (int i = 0; i < 4; i++) gmax = std::max(gmax, std::fabs(fy[i] - tgt[i]));
+        for (int i = 0; i < 4; i++) gmax = nan_max(gmax, std::fabs(fy[i] - tgt[i]));
         if (gmax <= fmax || h == 6) break;
       }
       lam *= 0.5;
@@ -321,7 +345,7 @@ int eos_invert(const Config& c, const Table* tab, int entropy, const double targ
       double o[17];
       model_thermo(c, tab, model, y, o);
       // prohibit_unstable_cs2 / prohibit_acausal_cs2 default true (include/settings.h:145-147)
-      if (o[6] < 0.0 || o[6] > 1.0) continue;
+      if (!(o[6] >= 0.0 && o[6] <= 1.0)) continue;
       for (int i = 0; i < 4; i++) x[i] = y[i];
       if (iterations) *iterations = it;
       return k;
