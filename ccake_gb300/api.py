@@ -90,6 +90,12 @@ def lib():
                                               ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         L.ccake_set_eos_table.argtypes = [P, _ip, _dp, _dp, _dp, _dp, _dp]
         L.ccake_eos_thermo_batch.argtypes = [P, _i32, _i64, _dp, _dp]
+        _fp = ctypes.POINTER(ctypes.c_float)
+        L.ccake_mlp_train.argtypes = [P, _i64, _i32, _i32, ctypes.c_double, ctypes.c_uint64, _dp]
+        L.ccake_mlp_get_params.argtypes = [P, _fp, _fp]
+        L.ccake_mlp_set_params.argtypes = [P, _fp, _fp]
+        L.ccake_mlp_forward.argtypes = [P, _i64, _fp, _fp]
+        L.ccake_mlp_gradient.argtypes = [P, _i64, _fp, _fp, _fp, _dp]
         _lib = L
     return _lib
 
@@ -100,6 +106,10 @@ def make_config(rc) -> CcakeConfig:
         if hasattr(rc, name):
             setattr(c, name, getattr(rc, name))
     return c
+
+
+def _f(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
 
 
 def _d(a):
@@ -229,6 +239,40 @@ class GpuHydro:
         self._check(lib().ccake_eos_invert_device(self.h, int(entropy), int(seed_mode), int(n), in4_ptr, tbqs_ptr,
                                                   th16_ptr, status_ptr, iters_ptr, stream_ptr),
                     "eos_invert_device")
+
+    # -- learned Newton seed -------------------------------------------------------
+    def mlp_train(self, n_samples=5_000_000, epochs=20, batch=32768, lr=3e-3, seed=1):
+        """Trains the seed network on table samples; returns the last epoch's MSE (standardised)."""
+        mse = ctypes.c_double()
+        self._check(lib().ccake_mlp_train(self.h, int(n_samples), int(epochs), int(batch), float(lr), int(seed),
+                                          ctypes.byref(mse)), "mlp_train")
+        return float(mse.value)
+
+    def mlp_params(self):
+        prm = np.zeros(8900, dtype=np.float32)
+        norm = np.zeros(16, dtype=np.float32)
+        self._check(lib().ccake_mlp_get_params(self.h, _f(prm), _f(norm)), "mlp_get_params")
+        return prm, norm
+
+    def mlp_set_params(self, prm, norm):
+        prm = np.ascontiguousarray(prm, dtype=np.float32)
+        norm = np.ascontiguousarray(norm, dtype=np.float32)
+        self._check(lib().ccake_mlp_set_params(self.h, _f(prm), _f(norm)), "mlp_set_params")
+
+    def mlp_forward(self, feat):
+        f = np.ascontiguousarray(feat, dtype=np.float32)
+        out = np.zeros_like(f)
+        self._check(lib().ccake_mlp_forward(self.h, f.shape[0], _f(f), _f(out)), "mlp_forward")
+        return out
+
+    def mlp_gradient(self, feat, tgt):
+        f = np.ascontiguousarray(feat, dtype=np.float32)
+        t = np.ascontiguousarray(tgt, dtype=np.float32)
+        g = np.zeros(8900, dtype=np.float32)
+        sse = ctypes.c_double()
+        self._check(lib().ccake_mlp_gradient(self.h, f.shape[0], _f(f), _f(t), _f(g), ctypes.byref(sse)),
+                    "mlp_gradient")
+        return g, float(sse.value)
 
     def eos_invert(self, entropy, targets, seeds, seed_mode=0):
         """Batch inversion; seed_mode 0 reference seed chain, 1 analytic exact inverse first."""

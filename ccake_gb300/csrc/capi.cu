@@ -12,6 +12,7 @@
 
 #include "ccake_gpu.h"
 #include "kernels.cuh"
+#include "mlp.cuh"
 
 using namespace ccake;
 
@@ -38,6 +39,15 @@ struct ccake_ctx {
   int steps_since_build = 0;
   cudaGraph_t build_graph = nullptr;
   cudaGraphExec_t build_exec = nullptr;
+  // learned Newton seed: parameters, gradients, Adam moments (4 x mlp::kParams FP32)
+  float* mlp_buf = nullptr;
+  double* mlp_sse = nullptr;
+  int32_t* mlp_err = nullptr;
+  MlpNorm mlp_norm{};
+  bool mlp_ready = false;
+  // scratch of the two-pass batch inversion (capacity + 1 int32)
+  int32_t* eos_scratch = nullptr;
+  int64_t eos_scratch_cap = 0;
 };
 
 namespace {
@@ -260,6 +270,66 @@ FieldRef field_ref(ccake_ctx* ctx, const std::string& k) {
 
 }  // namespace
 
+// learned Newton seed: helpers
+namespace {
+
+ccake_status_t ensure_mlp(ccake_ctx* ctx) {
+  if (ctx->mlp_buf) return CCAKE_OK;
+  if (cudaMalloc(&ctx->mlp_buf, 4 * mlp::kParams * sizeof(float)) != cudaSuccess ||
+      cudaMalloc(&ctx->mlp_sse, sizeof(double)) != cudaSuccess || cudaMalloc(&ctx->mlp_err, sizeof(int32_t)) != cudaSuccess)
+    return fail(ctx, CCAKE_ERR_NOMEM, "network allocation");
+  CK(cudaMemsetAsync(ctx->mlp_buf, 0, 4 * mlp::kParams * sizeof(float), ctx->stream));
+  CK(cudaMemsetAsync(ctx->mlp_err, 0, sizeof(int32_t), ctx->stream));
+  return CCAKE_OK;
+}
+
+ccake_status_t mlp_check(ccake_ctx* ctx) {
+  int32_t e = 0;
+  CK(cudaMemcpyAsync(&e, ctx->mlp_err, sizeof(e), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaGetLastError());
+  if (e) {
+    cudaMemsetAsync(ctx->mlp_err, 0, sizeof(int32_t), ctx->stream);
+    return fail(ctx, CCAKE_ERR_CUDA, "tensor-core wait expired in the seed network");
+  }
+  return CCAKE_OK;
+}
+
+// Device scratch freed on scope exit.
+struct Scratch {
+  std::vector<void*> p;
+  template <class T>
+  T* get(size_t count) {
+    void* q = nullptr;
+    if (cudaMalloc(&q, count * sizeof(T)) != cudaSuccess) return nullptr;
+    p.push_back(q);
+    return static_cast<T*>(q);
+  }
+  ~Scratch() {
+    for (void* q : p) cudaFree(q);
+  }
+};
+
+}  // namespace
+
+
+// Scratch of the two-pass batch inversion, grown on demand (NULL when the
+// allocation fails: the single-pass kernel is used).
+static int32_t* eos_scratch(ccake_ctx* ctx, int64_t n) {
+  if (n > ctx->eos_scratch_cap) {
+    if (ctx->eos_scratch) cudaFree(ctx->eos_scratch);
+    ctx->eos_scratch = nullptr;
+    ctx->eos_scratch_cap = 0;
+    if (cudaMalloc(&ctx->eos_scratch, (size_t)(n + 1) * sizeof(int32_t)) != cudaSuccess) {
+      cudaGetLastError();
+      ctx->eos_scratch = nullptr;
+      return nullptr;
+    }
+    ctx->eos_scratch_cap = n;
+  }
+  return ctx->eos_scratch;
+}
+
 extern "C" {
 
 const char* ccake_status_string(ccake_status_t s) {
@@ -328,6 +398,10 @@ ccake_status_t ccake_ctx_create(const ccake_config* cfg, ccake_ctx** out) {
 ccake_status_t ccake_ctx_destroy(ccake_ctx* ctx) {
   if (!ctx) return CCAKE_ERR_INVALID;
   free_buffers(ctx);
+  if (ctx->mlp_buf) cudaFree(ctx->mlp_buf);
+  if (ctx->mlp_sse) cudaFree(ctx->mlp_sse);
+  if (ctx->mlp_err) cudaFree(ctx->mlp_err);
+  if (ctx->eos_scratch) cudaFree(ctx->eos_scratch);
   if (ctx->d_table) cudaFree(ctx->d_table);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
@@ -771,13 +845,170 @@ ccake_status_t ccake_eos_invert_device(ccake_ctx* ctx, int32_t entropy_mode, int
                                        const double* d_in4, double* d_tbqs, double* d_th16, int32_t* d_status,
                                        int32_t* d_iters, void* stream) {
   if (!ctx || n < 0 || (n > 0 && (!d_in4 || !d_tbqs || !d_status))) return CCAKE_ERR_INVALID;
-  if (seed_mode != CCAKE_SEED_REFERENCE && seed_mode != CCAKE_SEED_ANALYTIC) return CCAKE_ERR_INVALID;
+  if (seed_mode < CCAKE_SEED_REFERENCE || seed_mode > CCAKE_SEED_LEARNED) return CCAKE_ERR_INVALID;
   if (ctx->eos.kind == 2 && !ctx->d_table) return fail(ctx, CCAKE_ERR_STATE, "set the EoS table first");
+  if (seed_mode == CCAKE_SEED_LEARNED && !ctx->mlp_ready) return fail(ctx, CCAKE_ERR_STATE, "train the seed network first");
   if (n == 0) return CCAKE_OK;
+  const cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  if (seed_mode == CCAKE_SEED_LEARNED)
+    launch_mlp_seed(MlpDev{ctx->mlp_buf, ctx->mlp_norm}, n, d_in4, d_tbqs, ctx->mlp_err, cs);
   launch_eos_batch(ctx->eos, entropy_mode, seed_mode, n, d_in4, d_tbqs, d_th16, d_status, d_iters,
-                   static_cast<cudaStream_t>(stream));
+                   eos_scratch(ctx, n), cs);
   CK(cudaGetLastError());
   return CCAKE_OK;
+}
+
+// ---------------------------------------------------------------------------
+// learned Newton seed
+// ---------------------------------------------------------------------------
+ccake_status_t ccake_mlp_train(ccake_ctx* ctx, int64_t n_samples, int32_t epochs, int32_t batch, double lr,
+                               uint64_t seed, double* final_mse) {
+  if (!ctx || n_samples < 128 || epochs < 1 || batch < 128 || batch > n_samples || !(lr > 0.0))
+    return CCAKE_ERR_INVALID;
+  if (ctx->eos.kind != 2 || !ctx->d_table) return fail(ctx, CCAKE_ERR_STATE, "the seed network needs the EoS table");
+  ccake_status_t st = ensure_mlp(ctx);
+  if (st) return st;
+  Scratch sc;
+  float* feat = sc.get<float>(4 * (size_t)n_samples);
+  float* tgt = sc.get<float>(4 * (size_t)n_samples);
+  int32_t* okf = sc.get<int32_t>((size_t)n_samples);
+  if (!feat || !tgt || !okf) return fail(ctx, CCAKE_ERR_NOMEM, "training-set allocation");
+  launch_mlp_samples(ctx->eos, n_samples, seed, feat, tgt, okf, ctx->stream);
+  // standardisation from the first rows (up to 262,144)
+  const int64_t m = std::min<int64_t>(n_samples, 262144);
+  std::vector<float> hf(4 * m), ht(4 * m);
+  std::vector<int32_t> hok(m);
+  CK(cudaMemcpyAsync(hf.data(), feat, 4 * m * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(ht.data(), tgt, 4 * m * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(hok.data(), okf, m * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  MlpNorm nm{};
+  {
+    double s1[8] = {0}, s2[8] = {0};
+    int64_t c = 0;
+    for (int64_t i = 0; i < m; i++) {
+      if (!hok[i]) continue;
+      c++;
+      for (int k = 0; k < 4; k++) {
+        s1[k] += hf[4 * i + k]; s2[k] += (double)hf[4 * i + k] * hf[4 * i + k];
+        s1[4 + k] += ht[4 * i + k]; s2[4 + k] += (double)ht[4 * i + k] * ht[4 * i + k];
+      }
+    }
+    if (c < 16) return fail(ctx, CCAKE_ERR_EOS, "too few valid training states in the table");
+    for (int k = 0; k < 8; k++) {
+      const double mu = s1[k] / c, sd = std::sqrt(std::max(s2[k] / c - mu * mu, 1e-12));
+      if (k < 4) { nm.in_mean[k] = (float)mu; nm.in_std[k] = (float)sd; }
+      else { nm.out_mean[k - 4] = (float)mu; nm.out_std[k - 4] = (float)sd; }
+    }
+  }
+  launch_mlp_standardise(nm, n_samples, feat, tgt, ctx->stream);
+  // Glorot-uniform weights, zero biases (64-bit LCG of the seed)
+  std::vector<float> prm(mlp::kParams, 0.0f);
+  {
+    uint64_t r = seed * 6364136223846793005ull + 1442695040888963407ull;
+    auto uni = [&]() {
+      r = r * 6364136223846793005ull + 1442695040888963407ull;
+      return (double)(r >> 11) * (1.0 / 9007199254740992.0);
+    };
+    auto fill = [&](int off, int nout, int nin) {
+      const double a = std::sqrt(6.0 / (nin + nout));
+      for (int i = 0; i < nout * nin; i++) prm[off + i] = (float)((2.0 * uni() - 1.0) * a);
+    };
+    fill(mlp::kW1, 64, 4);
+    fill(mlp::kW2, 64, 64);
+    fill(mlp::kW3, 64, 64);
+    fill(mlp::kW4, 4, 64);
+  }
+  float* P = ctx->mlp_buf;
+  float* G = P + mlp::kParams;
+  float* M1 = G + mlp::kParams;
+  float* V = M1 + mlp::kParams;
+  CK(cudaMemcpyAsync(P, prm.data(), mlp::kParams * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemsetAsync(M1, 0, 2 * mlp::kParams * sizeof(float), ctx->stream));
+  ctx->mlp_ready = false;
+  const int64_t steps = n_samples / batch;
+  const int64_t total = (int64_t)epochs * steps;
+  int64_t t = 0;
+  double sse = 0.0;
+  for (int ep = 0; ep < epochs; ep++) {
+    CK(cudaMemsetAsync(ctx->mlp_sse, 0, sizeof(double), ctx->stream));
+    for (int64_t s = 0; s < steps; s++) {
+      CK(cudaMemsetAsync(G, 0, mlp::kParams * sizeof(float), ctx->stream));
+      launch_mlp_grad(P, batch, feat + 4 * s * (int64_t)batch, tgt + 4 * s * (int64_t)batch, G, ctx->mlp_sse,
+                      ctx->mlp_err, ctx->stream);
+      t++;
+      const double c = 0.5 * (1.0 + std::cos(M_PI * (double)t / (double)total));
+      launch_mlp_adam(P, G, M1, V, (float)(lr * (0.05 + 0.95 * c)), (int)t, ctx->stream);
+    }
+    if (ep == epochs - 1 || ep % 8 == 0) {
+      if ((st = mlp_check(ctx))) return st;
+    }
+  }
+  CK(cudaMemcpyAsync(&sse, ctx->mlp_sse, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if ((st = mlp_check(ctx))) return st;
+  if (final_mse) *final_mse = sse / (4.0 * (double)batch * (double)steps);
+  ctx->mlp_norm = nm;
+  ctx->mlp_ready = true;
+  return CCAKE_OK;
+}
+
+ccake_status_t ccake_mlp_get_params(ccake_ctx* ctx, float* params, float* norm16) {
+  if (!ctx || !params || !norm16) return CCAKE_ERR_INVALID;
+  if (!ctx->mlp_ready) return fail(ctx, CCAKE_ERR_STATE, "no seed network");
+  CK(cudaMemcpyAsync(params, ctx->mlp_buf, mlp::kParams * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  std::memcpy(norm16, &ctx->mlp_norm, sizeof(MlpNorm));
+  return CCAKE_OK;
+}
+
+ccake_status_t ccake_mlp_set_params(ccake_ctx* ctx, const float* params, const float* norm16) {
+  if (!ctx || !params || !norm16) return CCAKE_ERR_INVALID;
+  for (int k = 4; k < 8; k++)
+    if (!(norm16[k] > 0.0f) || !(norm16[8 + k] > 0.0f)) return fail(ctx, CCAKE_ERR_INVALID, "non-positive std");
+  ccake_status_t st = ensure_mlp(ctx);
+  if (st) return st;
+  CK(cudaMemcpyAsync(ctx->mlp_buf, params, mlp::kParams * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  std::memcpy(&ctx->mlp_norm, norm16, sizeof(MlpNorm));
+  ctx->mlp_ready = true;
+  return CCAKE_OK;
+}
+
+ccake_status_t ccake_mlp_forward(ccake_ctx* ctx, int64_t n, const float* feat, float* out) {
+  if (!ctx || n < 0 || (n > 0 && (!feat || !out))) return CCAKE_ERR_INVALID;
+  if (!ctx->mlp_ready) return fail(ctx, CCAKE_ERR_STATE, "no seed network");
+  if (n == 0) return CCAKE_OK;
+  Scratch sc;
+  float* df = sc.get<float>(4 * (size_t)n);
+  float* dout = sc.get<float>(4 * (size_t)n);
+  if (!df || !dout) return fail(ctx, CCAKE_ERR_NOMEM, "allocation");
+  CK(cudaMemcpyAsync(df, feat, 4 * n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+  launch_mlp_forward(ctx->mlp_buf, n, df, dout, ctx->mlp_err, ctx->stream);
+  CK(cudaMemcpyAsync(out, dout, 4 * n * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+  return mlp_check(ctx);
+}
+
+ccake_status_t ccake_mlp_gradient(ccake_ctx* ctx, int64_t n, const float* feat, const float* tgt, float* grad,
+                                  double* sse) {
+  if (!ctx || n <= 0 || !feat || !tgt || !grad) return CCAKE_ERR_INVALID;
+  if (!ctx->mlp_ready) return fail(ctx, CCAKE_ERR_STATE, "no seed network");
+  Scratch sc;
+  float* df = sc.get<float>(4 * (size_t)n);
+  float* dt = sc.get<float>(4 * (size_t)n);
+  if (!df || !dt) return fail(ctx, CCAKE_ERR_NOMEM, "allocation");
+  float* G = ctx->mlp_buf + mlp::kParams;
+  CK(cudaMemcpyAsync(df, feat, 4 * n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(dt, tgt, 4 * n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemsetAsync(G, 0, mlp::kParams * sizeof(float), ctx->stream));
+  CK(cudaMemsetAsync(ctx->mlp_sse, 0, sizeof(double), ctx->stream));
+  launch_mlp_grad(ctx->mlp_buf, n, df, dt, G, ctx->mlp_sse, ctx->mlp_err, ctx->stream);
+  CK(cudaMemcpyAsync(grad, G, mlp::kParams * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+  double s = 0.0;
+  CK(cudaMemcpyAsync(&s, ctx->mlp_sse, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  ccake_status_t st = mlp_check(ctx);
+  if (sse) *sse = s;
+  return st;
 }
 
 ccake_status_t ccake_eos_invert_batch(ccake_ctx* ctx, int32_t entropy_mode, int64_t n, const double* in4,
@@ -789,8 +1020,9 @@ ccake_status_t ccake_eos_invert_batch_ex(ccake_ctx* ctx, int32_t entropy_mode, i
                                          const double* in4, double* tbqs, double* th16, int32_t* status,
                                          int32_t* iters) {
   if (!ctx || n < 0 || !in4 || !tbqs || !status) return CCAKE_ERR_INVALID;
-  if (seed_mode != CCAKE_SEED_REFERENCE && seed_mode != CCAKE_SEED_ANALYTIC) return CCAKE_ERR_INVALID;
+  if (seed_mode < CCAKE_SEED_REFERENCE || seed_mode > CCAKE_SEED_LEARNED) return CCAKE_ERR_INVALID;
   if (ctx->eos.kind == 2 && !ctx->d_table) return fail(ctx, CCAKE_ERR_STATE, "set the EoS table first");
+  if (seed_mode == CCAKE_SEED_LEARNED && !ctx->mlp_ready) return fail(ctx, CCAKE_ERR_STATE, "train the seed network first");
   if (n == 0) return CCAKE_OK;
   double *d_in = nullptr, *d_x = nullptr, *d_th = nullptr;
   int32_t *d_st = nullptr, *d_it = nullptr;
@@ -801,7 +1033,10 @@ ccake_status_t ccake_eos_invert_batch_ex(ccake_ctx* ctx, int32_t entropy_mode, i
   if (iters) CK(cudaMalloc(&d_it, n * sizeof(int32_t)));
   CK(cudaMemcpyAsync(d_in, in4, n * 4 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(d_x, tbqs, n * 4 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-  launch_eos_batch(ctx->eos, entropy_mode, seed_mode, n, d_in, d_x, d_th, d_st, d_it, ctx->stream);
+  if (seed_mode == CCAKE_SEED_LEARNED)
+    launch_mlp_seed(MlpDev{ctx->mlp_buf, ctx->mlp_norm}, n, d_in, d_x, ctx->mlp_err, ctx->stream);
+  launch_eos_batch(ctx->eos, entropy_mode, seed_mode, n, d_in, d_x, d_th, d_st, d_it, eos_scratch(ctx, n),
+                   ctx->stream);
   CK(cudaMemcpyAsync(tbqs, d_x, n * 4 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   if (th16) CK(cudaMemcpyAsync(th16, d_th, n * 16 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaMemcpyAsync(status, d_st, n * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));

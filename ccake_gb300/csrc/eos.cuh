@@ -102,30 +102,45 @@ __host__ __device__ inline void confdiag_thermo(const Scales& k, const double* x
 // Multilinear lookup with the reference's index rule (src/interpolatorND.cpp:250-317):
 // integer part by truncation toward zero, last cell reused at the upper edge,
 // NaN outside.
-__host__ __device__ inline void table_thermo(const TableView& t, const double* x, double* o) {
+// jac (optional): derivatives of the interpolated s, rhoB, rhoS, rhoQ, e
+// (fields 1..5) with respect to (T, muB, muQ, muS), the exact Jacobian of the
+// multilinear interpolant inside the cell.
+__host__ __device__ inline void table_thermo(const TableView& t, const double* x, double* o,
+                                             double (*jac)[4] = nullptr) {
   int ind[4];
-  double fr[4];
+  double fr[4], dfr[4];
   for (int k = 0; k < 4; k++) {
     if (isnan(x[k])) { for (int i = 0; i < 17; i++) o[i] = NAN; return; }
-    if (t.n[k] <= 1 || fabs(t.d[k]) < 1e-30) { ind[k] = 0; fr[k] = 1.0; continue; }
+    if (t.n[k] <= 1 || fabs(t.d[k]) < 1e-30) { ind[k] = 0; fr[k] = 1.0; dfr[k] = 0.0; continue; }
     const double q = (x[k] - t.lo[k]) / t.d[k];
     const double ip = trunc(q);
     fr[k] = 1.0 - (q - ip);
+    dfr[k] = -1.0 / t.d[k];
     ind[k] = (int)ip;
-    if (ind[k] + 1 == t.n[k]) { fr[k] = 1.0 - fr[k]; ind[k]--; }
+    if (ind[k] + 1 == t.n[k]) { fr[k] = 1.0 - fr[k]; dfr[k] = -dfr[k]; ind[k]--; }
     if (ind[k] < 0 || ind[k] >= t.n[k] || !(fabs(q) < 2e9)) { for (int i = 0; i < 17; i++) o[i] = NAN; return; }
   }
   for (int i = 0; i < 17; i++) o[i] = 0.0;
+  if (jac)
+    for (int f = 0; f < 5; f++) for (int j = 0; j < 4; j++) jac[f][j] = 0.0;
   for (int h = 0; h < 16; h++) {
     const int b[4] = {(h >> 3) & 1, (h >> 2) & 1, (h >> 1) & 1, h & 1};
-    double w = 1.0;
+    double wk[4], w = 1.0;
     long idx = 0;
     for (int k = 0; k < 4; k++) {
-      w *= (fr[k] + b[k] - 2.0 * b[k] * fr[k]);
+      wk[k] = fr[k] + b[k] - 2.0 * b[k] * fr[k];
+      w *= wk[k];
       const int c = (t.n[k] <= 1) ? 0 : ind[k] + b[k];
       idx = idx * t.n[k] + c;
     }
     const double* node = t.f + (size_t)idx * 17;
+    if (jac)
+      for (int j = 0; j < 4; j++) {
+        double dw = (1.0 - 2.0 * b[j]) * dfr[j];
+        for (int k = 0; k < 4; k++)
+          if (k != j) dw *= wk[k];
+        for (int f = 0; f < 5; f++) jac[f][j] += dw * node[1 + f];
+      }
     for (int i = 0; i < 17; i++) o[i] += w * node[i];
   }
 }
@@ -147,9 +162,28 @@ __host__ __device__ inline void model_box(const EosDev& e, int model, double* lo
 
 // Densities (e|s, B, Q, S) at x = (T, muB, muQ, muS) and their Jacobian: the
 // Hessian of p (exactly diagonal for the conformal-diagonal model).
+// For the table the Jacobian is that of the interpolated densities (the
+// function the solver zeroes; the reference's GSL hybrids solver
+// differentiates it by finite differences), not the interpolated
+// susceptibilities.
 __host__ __device__ inline void dens_jac(const EosDev& e, int model, int entropy, const double* x, double* f,
                                          double J[4][4]) {
   double o[17];
+  if (model == M_TABLE) {
+    double jac[5][4];
+    table_thermo(e.tab, x, o, jac);
+    f[0] = entropy ? o[1] : o[5];
+    f[1] = o[2];
+    f[2] = o[4];
+    f[3] = o[3];
+    for (int j = 0; j < 4; j++) {
+      J[0][j] = entropy ? jac[0][j] : jac[4][j];
+      J[1][j] = jac[1][j];
+      J[2][j] = jac[3][j];
+      J[3][j] = jac[2][j];
+    }
+    return;
+  }
   model_thermo(e, model, x, o);
   double H[4][4];
   if (model == M_CDIAG) {
@@ -208,20 +242,21 @@ __host__ __device__ inline void solve4(double A[4][4], double* b, double* x) {
 // relative step is below 1e-12. 100 iterations at most; damped by residual
 // halving; leaving the model box fails.
 __host__ __device__ inline bool newton_attempt(const EosDev& e, int model, int entropy, const double* tgt,
-                                               const double* lo, const double* hi, double* x, int* iters) {
+                                               const double* lo, const double* hi, double* x, int* iters,
+                                               int max_it = 100) {
   // f, J at the current x are carried over from the accepted trial point of
   // the previous iteration (the same values a fresh evaluation would give),
   // so an undamped iteration costs one density/Jacobian evaluation.
-  int extra = -1;
+  int extra = -1, nslow1 = 0, nslow2 = 0;
   double f[4], J[4][4], xgood[4] = {0.0, 0.0, 0.0, 0.0};
   bool have = false;
   const bool diag = (model == M_CDIAG);
-  for (int it = 0; it < 100; it++) {
+  for (int it = 0; it < max_it; it++) {
     if (!have) dens_jac(e, model, entropy, x, f, J);
     have = false;
     double F[4], fres = 0.0;
     for (int i = 0; i < 4; i++) { F[i] = f[i] - tgt[i]; fres = fres > fabs(F[i]) ? fres : fabs(F[i]); }
-    if (!(fres == fres)) return false;
+    if (!(fres == fres)) { *iters += it + 1; return false; }
     if (extra < 0 && fres < 1e-10) extra = 0;
     double dx[4];
     if (diag) {
@@ -275,10 +310,29 @@ __host__ __device__ inline bool newton_attempt(const EosDev& e, int model, int e
       lam *= 0.5;
     }
     if (!(y[0] > 0)) { y[0] = 0.5 * x[0]; have = false; }
+    // progress test of the reference's solver (GSL hybrids, called from
+    // src/rootfinder.cpp:206-416): the actual relative reduction of |F|^2;
+    // five iterations below 0.1 or ten below 0.001 fail the attempt
+    if (have) {
+      double n0 = 0.0, n1 = 0.0;
+      for (int i = 0; i < 4; i++) {
+        n0 += F[i] * F[i];
+        const double r = f[i] - tgt[i];
+        n1 += r * r;
+      }
+      const double actred = n0 > 0.0 ? 1.0 - n1 / n0 : 0.0;
+      nslow1 = actred >= 0.001 ? 0 : nslow1 + 1;
+      nslow2 = actred >= 0.1 ? 0 : nslow2 + 1;
+    } else {
+      nslow1++;
+      nslow2++;
+    }
     for (int i = 0; i < 4; i++) x[i] = y[i];
     for (int i = 0; i < 4; i++)
-      if (!(x[i] >= lo[i] && x[i] <= hi[i])) return false;
+      if (!(x[i] >= lo[i] && x[i] <= hi[i])) { *iters += it + 1; return false; }
+    if (nslow2 >= 5 || nslow1 >= 10) { *iters += it + 1; return false; }
   }
+  *iters += max_it;
   return false;
 }
 
@@ -385,7 +439,8 @@ __host__ __device__ inline bool analytic_seed(const EosDev& e, int model, const 
 // (e|s, B, S, Q) -> (T, muB, muQ, muS) through the EoS chain with the
 // reference's seeds (src/eos.cpp:629-804 entropy mode, :813-975 energy mode).
 // seed_mode 1 (entropy mode) first tries Newton from the analytic model's
-// exact inverse, then the reference's seeds. o_out, if given, receives the
+// exact inverse, seed_mode 2 from the given x (a learned seed) on the first
+// model tried; then the reference's seeds. o_out, if given, receives the
 // model thermodynamics at the solution (17 values). Returns the chain index
 // used, or -1.
 __host__ __device__ inline int eos_invert(const EosDev& e, int entropy, const double* target, int start, double* x,
@@ -399,7 +454,20 @@ __host__ __device__ inline int eos_invert(const EosDev& e, int entropy, const do
     const int model = chain_model(e.kind, k);
     double y[4];
     bool ok = false;
-    if (entropy && seed_mode == 1 && analytic_seed(e, model, tgt, y)) {
+    if (seed_mode == 2 && k == (entropy ? (start > 0 ? start : 0) : 0)) {
+      // learned seed (the given x) for the first model tried
+      double lo[4], hi[4];
+      model_box(e, model, lo, hi);
+      for (int i = 0; i < 4; i++) y[i] = fmin(fmax(prev[i], lo[i]), hi[i]);
+      ok = y[0] > 0.0 && newton_attempt(e, model, entropy, tgt, lo, hi, y, &it);
+      if (ok) {   // a root the c_s^2 guard rejects leaves this model to the reference seeds
+        double o[17];
+        model_thermo(e, model, y, o);
+        ok = o[6] >= 0.0 && o[6] <= 1.0;
+        if (!ok)
+          for (int i = 0; i < 4; i++) y[i] = prev[i];
+      }
+    } else if (entropy && seed_mode == 1 && analytic_seed(e, model, tgt, y)) {
       // the exact inverse is accepted when it meets the reference's residual
       // test (max |F| < 1e-10); otherwise Newton starts from it
       double o[17];
@@ -445,6 +513,46 @@ __host__ __device__ inline int eos_invert(const EosDev& e, int entropy, const do
   }
   *iters = it;
   return -1;
+}
+
+// The first attempt of eos_invert (first model of the chain, its first seed)
+// with Newton capped at max_it iterations. Returns the chain index, with the
+// same x, iterations and o_out as eos_invert gives whenever that attempt
+// succeeds, or -2 when it does not settle the row (the caller then runs
+// eos_invert from the same seed). Not for seed_mode 1.
+__host__ __device__ inline int eos_invert_first(const EosDev& e, int entropy, const double* target, int start,
+                                                double* x, int* iters, int seed_mode, int max_it, double* o_out) {
+  const double tgt[4] = {target[0], target[1], target[3], target[2]};  // (e|s, B, Q, S)
+  const int k = entropy ? (start > 0 ? start : 0) : 0;
+  if (k >= chain_len(e.kind) || seed_mode == 1) return -2;
+  const int model = chain_model(e.kind, k);
+  double lo[4], hi[4];
+  model_box(e, model, lo, hi);
+  double y[4];
+  if (seed_mode == 2) {
+    for (int i = 0; i < 4; i++) y[i] = fmin(fmax(x[i], lo[i]), hi[i]);
+    if (!(y[0] > 0.0)) return -2;
+  } else {
+    if (entropy) {
+      for (int i = 0; i < 4; i++) y[i] = x[i];
+    } else {
+      y[0] = 580.0 / kHbarcMeVfm; y[1] = sgnd(tgt[1]); y[2] = sgnd(tgt[2]); y[3] = sgnd(tgt[3]);
+    }
+    // find_root's seed sanitising
+    const double sg[4] = {1.0, sgnd(tgt[1]), sgnd(tgt[2]), sgnd(tgt[3])};
+    for (int i = 0; i < 4; i++)
+      if (y[i] * y[i] < 1e-10) y[i] = fmin(0.5 * hi[i], 1.0) * sg[i];
+  }
+  int it = 0;
+  if (!newton_attempt(e, model, entropy, tgt, lo, hi, y, &it, max_it)) return -2;
+  double o[17];
+  model_thermo(e, model, y, o);
+  if (!(o[6] >= 0.0 && o[6] <= 1.0)) return -2;
+  for (int i = 0; i < 4; i++) x[i] = y[i];
+  if (o_out)
+    for (int i = 0; i < 17; i++) o_out[i] = o[i];
+  *iters = it;
+  return k;
 }
 
 // a^T m^-1 b with the reference's guard on m11, m22 (src/eos_derivatives.cpp:457-560).

@@ -619,6 +619,46 @@ __global__ void k_eos_thermo(EosDev eos, int model, int64_t n, const double* tbq
   model_thermo(eos, model, tbqs + 4 * i, out17 + 17 * i);
 }
 
+// Pass 1 of the two-pass batch inversion: the first attempt of each row
+// with a Newton budget; rows it does not settle are appended to `list` (an
+// atomic append: rows are independent, so the order does not matter).
+__global__ void k_eos_first(EosDev eos, int entropy, int seed_mode, int max_it, int64_t n, const double* in4,
+                            double* tbqs, double* th16, int32_t* status, int32_t* iters, int32_t* list,
+                            int32_t* count) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double x[4] = {tbqs[4 * i], tbqs[4 * i + 1], tbqs[4 * i + 2], tbqs[4 * i + 3]};
+  int it = 0;
+  double o[17];
+  const int k = eos_invert_first(eos, entropy, in4 + 4 * i, 0, x, &it, seed_mode, max_it, o);
+  if (k == -2) {
+    list[atomicAdd(count, 1)] = (int32_t)i;
+    return;
+  }
+  status[i] = k;
+  if (iters) iters[i] = it;
+  for (int q = 0; q < 4; q++) tbqs[4 * i + q] = x[q];
+  if (th16) set_thermo_o(eos, k, x, o, th16 + 16 * i);
+}
+
+// Pass 2: the full inversion of the listed rows.
+__global__ void k_eos_rest(EosDev eos, int entropy, int seed_mode, const int32_t* list, const int32_t* count,
+                           const double* in4, double* tbqs, double* th16, int32_t* status, int32_t* iters) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= *count) return;
+  const int64_t i = list[j];
+  double x[4] = {tbqs[4 * i], tbqs[4 * i + 1], tbqs[4 * i + 2], tbqs[4 * i + 3]};
+  int it = 0;
+  double o[17];
+  const int k = eos_invert(eos, entropy, in4 + 4 * i, 0, x, &it, seed_mode, o);
+  status[i] = k;
+  if (iters) iters[i] = it;
+  if (k >= 0) {
+    for (int q = 0; q < 4; q++) tbqs[4 * i + q] = x[q];
+    if (th16) set_thermo_o(eos, k, x, o, th16 + 16 * i);
+  }
+}
+
 __global__ void k_eos_batch(EosDev eos, int entropy, int seed_mode, int64_t n, const double* in4, double* tbqs,
                             double* th16, int32_t* status, int32_t* iters) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -728,9 +768,21 @@ void launch_eos_thermo(const EosDev& eos, int chain_index, int64_t n, const doub
 }
 
 void launch_eos_batch(const EosDev& eos, int entropy, int seed_mode, int64_t n, const double* in4, double* tbqs,
-                      double* th16, int32_t* status, int32_t* iters, cudaStream_t s) {
+                      double* th16, int32_t* status, int32_t* iters, int32_t* scratch, cudaStream_t s) {
   const int nb = (int)((n + kBlock - 1) / kBlock);
-  k_eos_batch<<<nb, kBlock, 0, s>>>(eos, entropy, seed_mode, n, in4, tbqs, th16, status, iters);
+  if (seed_mode == 1 || !scratch) {
+    k_eos_batch<<<nb, kBlock, 0, s>>>(eos, entropy, seed_mode, n, in4, tbqs, th16, status, iters);
+    return;
+  }
+  // two passes: a warp of the single-pass kernel runs as long as its slowest
+  // row; the capped first pass settles most rows in a few Newton steps and
+  // the compacted second pass gives the hard rows warps of their own
+  int32_t* count = scratch;
+  int32_t* list = scratch + 1;
+  cudaMemsetAsync(count, 0, sizeof(int32_t), s);
+  k_eos_first<<<nb, kBlock, 0, s>>>(eos, entropy, seed_mode, kEosFirstIters, n, in4, tbqs, th16, status, iters, list,
+                                    count);
+  k_eos_rest<<<nb, kBlock, 0, s>>>(eos, entropy, seed_mode, list, count, in4, tbqs, th16, status, iters);
 }
 
 }  // namespace ccake

@@ -89,8 +89,13 @@ void launch_passA_mixed(const RunConst& rc, const EosDev& eos, const Ptrs& p, cu
 void launch_passB_mixed(const RunConst& rc, const Ptrs& p, int mode, double dt_sub, cudaStream_t s);
 void launch_eos_thermo(const EosDev& eos, int chain_index, int64_t n, const double* tbqs, double* out17,
                        cudaStream_t s);
+// Batch inversion. With scratch (n + 1 int32, device) and seed_mode 0 or 2,
+// two passes: the first attempt of every row with a Newton budget of
+// kEosFirstIters, then the full inversion of the rows it left (same results
+// as one pass).
+constexpr int kEosFirstIters = 8;
 void launch_eos_batch(const EosDev& eos, int entropy, int seed_mode, int64_t n, const double* in4, double* tbqs,
-                      double* th16, int32_t* status, int32_t* iters, cudaStream_t s);
+                      double* th16, int32_t* status, int32_t* iters, int32_t* scratch, cudaStream_t s);
 
 constexpr int kTotBlocks = 608;   // 4 x 152 SMs; fixed so the sums are reproducible
 

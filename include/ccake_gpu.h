@@ -192,9 +192,11 @@ ccake_status_t ccake_eos_thermo_batch(ccake_ctx* ctx, int32_t chain_index, int64
 /* Seed rules of the batch inversion (seed_mode of ccake_eos_invert_batch_ex). */
 enum {
   CCAKE_SEED_REFERENCE = 0, /* the reference's seed chain from the tbqs rows */
-  CCAKE_SEED_ANALYTIC = 1   /* entropy mode, conformal models: the exact inverse,
+  CCAKE_SEED_ANALYTIC = 1,  /* entropy mode, conformal models: the exact inverse,
                                accepted when max|F| < 1e-10, else Newton from it,
                                then the reference's seed chain */
+  CCAKE_SEED_LEARNED = 2    /* the learned seed (ccake_mlp_train) for the first
+                               model of the chain, then the reference's seed chain */
 };
 
 /* ccake_eos_invert_batch with a seed rule. No reference counterpart: the
@@ -210,6 +212,31 @@ ccake_status_t ccake_eos_invert_batch_ex(ccake_ctx* ctx, int32_t entropy_mode, i
 ccake_status_t ccake_eos_invert_device(ccake_ctx* ctx, int32_t entropy_mode, int32_t seed_mode, int64_t n,
                                        const double* d_in4, double* d_tbqs, double* d_th16, int32_t* d_status,
                                        int32_t* d_iters, void* stream);
+
+/* Learned Newton seed for the tabulated EoS: a 4-64-64-64-4 tanh MLP from
+ * (log e, rho_i / e^(3/4)) to (log T, mu_i / T), both standardised, trained
+ * and evaluated with BF16 tensor-core kernels. No reference counterpart (the
+ * reference seeds from fixed values and the previous solution).
+ *
+ * ccake_mlp_train: n_samples states uniform in the table's box (seeded),
+ * mapped forward through the table, epochs of Adam (learning rate lr, cosine
+ * decay to lr/20) on minibatches of `batch` rows; *final_mse = mean squared
+ * error of the last epoch (standardised units). Needs the table. */
+ccake_status_t ccake_mlp_train(ccake_ctx* ctx, int64_t n_samples, int32_t epochs, int32_t batch, double lr,
+                               uint64_t seed, double* final_mse);
+/* Parameters (8900 FP32: W1 [64][4], b1, W2 [64][64], b2, W3, b3, W4 [4][64],
+ * b4) and standardisation (16 FP32: input mean[4], std[4], output mean[4],
+ * std[4]) of the context's network. */
+ccake_status_t ccake_mlp_get_params(ccake_ctx* ctx, float* params, float* norm16);
+ccake_status_t ccake_mlp_set_params(ccake_ctx* ctx, const float* params, const float* norm16);
+/* Network on n host rows of standardised features (4 floats each) ->
+ * standardised outputs (4 floats each). */
+ccake_status_t ccake_mlp_forward(ccake_ctx* ctx, int64_t n, const float* feat, float* out);
+/* Gradient of the mean squared error over n host rows (standardised features
+ * and targets) with respect to the 8900 parameters; *sse = sum of squared
+ * errors. */
+ccake_status_t ccake_mlp_gradient(ccake_ctx* ctx, int64_t n, const float* feat, const float* tgt, float* grad,
+                                  double* sse);
 
 /* Neighbour counts (the number of b != a with |r_a - r_b|^2 <= (2h)^2, the
  * same exact predicate as every other entry point) of n particles whose

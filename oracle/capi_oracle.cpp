@@ -207,6 +207,15 @@ void* orc_table_create(const int32_t* n, const double* lo, const double* d, cons
 }
 void orc_table_destroy(void* t) { delete (Table*)t; }
 
+// Interpolated fields (17) and the Jacobian (5 x 4) of s, rhoB, rhoS, rhoQ, e
+// with respect to (T, muB, muQ, muS) at one point.
+void orc_table_jacobian(void* t, const double* x, double* out17, double* jac20) {
+  double jac[5][4];
+  table_full_thermo(*(Table*)t, x, out17, jac);
+  for (int f = 0; f < 5; f++)
+    for (int j = 0; j < 4; j++) jac20[4 * f + j] = jac[f][j];
+}
+
 void orc_eos_full_thermo(const Config* c, void* tab, int chain_index, const double* tbqs, double* out17) {
   eos_full_thermo(*c, (Table*)tab, chain_index, tbqs, out17);
 }

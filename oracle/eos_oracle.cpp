@@ -92,9 +92,28 @@ void model_thermo(const Config& c, const Table* tab, int model, const double* x4
 // numerically; here the exact derivative of the same function is used. For the
 // conformal-diagonal model that Jacobian is diagonal (its tabulated TINY cross
 // terms are placeholders, not derivatives).
+// For the table the Jacobian is that of the interpolated densities (the
+// function the solver zeroes; the reference's GSL hybrids solver
+// differentiates it by finite differences), not the interpolated
+// susceptibilities.
 void densities_and_jacobian(const Config& c, const Table* tab, int model, int entropy,
                             const double* x, double* f, double J[4][4]) {
   double o[17];
+  if (model == mTable) {
+    double jac[5][4];
+    table_full_thermo(*tab, x, o, jac);
+    f[0] = entropy ? o[1] : o[5];
+    f[1] = o[2];
+    f[2] = o[4];
+    f[3] = o[3];
+    for (int j = 0; j < 4; j++) {
+      J[0][j] = entropy ? jac[0][j] : jac[4][j];
+      J[1][j] = jac[1][j];
+      J[2][j] = jac[3][j];
+      J[3][j] = jac[2][j];
+    }
+    return;
+  }
   model_thermo(c, tab, model, x, o);
   // Hessian of p in (T, muB, muQ, muS) order
   double H[4][4];
@@ -161,7 +180,7 @@ inline double nan_max(double a, double b) { return a > b ? a : b; }
 bool newton_attempt(const Config& c, const Table* tab, int model, int entropy,
                     const double* tgt, const double* lo, const double* hi, double* x, int* iters) {
   const double tol = 1e-10;
-  int extra = -1;
+  int extra = -1, nslow1 = 0, nslow2 = 0;
   double xgood[4] = {0, 0, 0, 0};
   for (int it = 0; it < 100; it++) {
     double f[4], J[4][4];
@@ -171,7 +190,7 @@ bool newton_attempt(const Config& c, const Table* tab, int model, int entropy,
     // fails the iterate, as GSL_EBADFUNC fails the reference's solver
     double fmax = 0;
     for (int i = 0; i < 4; i++) fmax = nan_max(fmax, std::fabs(F[i]));
-    if (!(fmax == fmax)) return false;  // NaN
+    if (!(fmax == fmax)) { *iters += it + 1; return false; }  // NaN
     if (extra < 0 && fmax < tol) extra = 0;
     double rhs[4] = {-F[0], -F[1], -F[2], -F[3]}, dx[4];
     solve4(J, rhs, dx);
@@ -219,11 +238,33 @@ bool newton_attempt(const Config& c, const Table* tab, int model, int entropy,
       }
       lam *= 0.5;
     }
+    bool have = y[0] > 0;
     if (!(y[0] > 0)) y[0] = 0.5 * x[0];
+    // progress test of the reference's solver (GSL hybrids, called from
+    // src/rootfinder.cpp:206-416): the actual relative reduction of |F|^2;
+    // five iterations below 0.1 or ten below 0.001 fail the attempt
+    if (have) {
+      double fy[4], Jy[4][4];
+      densities_and_jacobian(c, tab, model, entropy, y, fy, Jy);
+      double n0 = 0.0, n1 = 0.0;
+      for (int i = 0; i < 4; i++) {
+        n0 += F[i] * F[i];
+        const double r = fy[i] - tgt[i];
+        n1 += r * r;
+      }
+      const double actred = n0 > 0.0 ? 1.0 - n1 / n0 : 0.0;
+      nslow1 = actred >= 0.001 ? 0 : nslow1 + 1;
+      nslow2 = actred >= 0.1 ? 0 : nslow2 + 1;
+    } else {
+      nslow1++;
+      nslow2++;
+    }
     for (int i = 0; i < 4; i++) x[i] = y[i];
     for (int i = 0; i < 4; i++)
-      if (!(x[i] >= lo[i] && x[i] <= hi[i])) return false;
+      if (!(x[i] >= lo[i] && x[i] <= hi[i])) { *iters += it + 1; return false; }
+    if (nslow2 >= 5 || nslow1 >= 10) { *iters += it + 1; return false; }
   }
+  *iters += 100;
   return false;
 }
 

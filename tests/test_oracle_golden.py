@@ -169,3 +169,34 @@ def test_gubser_against_analytic():
     tot = r.totals()
     assert abs(tot["S"] / tot0["S"] - 1) < 1e-12          # ideal: entropy conserved
     assert abs((tot["E"] + tot["Ez"]) / tot0["E"] - 1) < 2e-3
+
+
+def test_table_jacobian_is_the_interpolant_derivative():
+    # the Newton Jacobian of the table model: derivatives of the multilinear
+    # interpolant of s, rho and e, against central differences inside a cell
+    import ctypes
+    from ccake_gb300 import eos_table
+    n, lo, d, f = eos_table.synthetic_table(nT=9, nmu=5)
+    c5, d5 = eos_table.fallback_scales()
+    t = O.OracleTable(n, lo, d, f, c5, d5)
+    L = O.lib()
+    dp = ctypes.POINTER(ctypes.c_double)
+    L.orc_table_jacobian.argtypes = [ctypes.c_void_p, dp, dp, dp]
+    rng = np.random.default_rng(5)
+    for _ in range(20):
+        cell = rng.integers(0, n - 1)
+        frac = rng.uniform(0.2, 0.8, 4)
+        x = lo + d * (cell + frac)
+        o, jac = np.zeros(17), np.zeros(20)
+        L.orc_table_jacobian(t.h, O._dp(x), O._dp(o), O._dp(jac))
+        jac = jac.reshape(5, 4)
+        for j in range(4):
+            h = 1e-4 * d[j]
+            xp, xm = x.copy(), x.copy()
+            xp[j] += h
+            xm[j] -= h
+            op, om = np.zeros(17), np.zeros(17)
+            L.orc_table_jacobian(t.h, O._dp(xp), O._dp(op), O._dp(np.zeros(20)))
+            L.orc_table_jacobian(t.h, O._dp(xm), O._dp(om), O._dp(np.zeros(20)))
+            fd = (op[1:6] - om[1:6]) / (2 * h)
+            assert np.allclose(jac[:, j], fd, rtol=1e-6, atol=1e-9 * np.abs(fd).max()), j
