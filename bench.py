@@ -458,6 +458,152 @@ def run_eos_table(args):
     print(json.dumps(line))
 
 
+def run_hotspots3d(args):
+    """3+1-D Milne viscous BSQ event: 120 x 120 x 100 (x, y, eta_s) lattice
+    (1.44M particles), dx = 0.1 fm, deta = 0.06, h = 0.2 fm, 30 hot spots,
+    shear eta/s = 0.08, bulk zeta/s peaked at T = 0.16 GeV, the synthetic
+    tabulated EoS; RK2 steps in the mixed form (FP32 sums, FP64 state and
+    EoS) and in the FP64 form, and the mixed form's error against the FP64
+    form after the same steps."""
+    import dataclasses
+    import torch
+    from ccake_gb300 import api, build, eos_table, ics
+    build.build()
+    p, rc = ics.hotspots_3d(eos_kind=2, zeta_over_s=0.1)
+    n, lo, d, fields = eos_table.synthetic_table()
+    conf5, cdiag5 = eos_table.fallback_scales()
+    steps = args.steps
+    out = {}
+    for form, prec in (("mixed", 1), ("fp64", 0)):
+        g = api.GpuHydro(dataclasses.replace(rc, precision=prec))
+        g.set_eos_table(n, lo, d, fields, conf5, cdiag5)
+        g.load(p)
+        g.initialize()
+        for _ in range(args.warmup):
+            g.step(1)
+        torch.cuda.synchronize()
+        ms = g.step_timed(steps)
+        out[form] = {"ms": ms, "state": {f: g.get(f) for f in ("e", "rhoB", "rhoQ", "T", "u0", "u2")},
+                     "bytes": g.device_bytes(), "phase_ms": [float(v) for v in g.profile_phases(2)]}
+        g.close()
+    err = {}
+    for f in ("e", "rhoB", "rhoQ", "T"):
+        a, b = out["mixed"]["state"][f], out["fp64"]["state"][f]
+        err[f] = float(np.max(np.abs(a - b) / (np.abs(b) + 1e-300)))
+    for f in ("u0", "u2"):
+        a, b = out["mixed"]["state"][f], out["fp64"]["state"][f]
+        err[f + "_of_range"] = float(np.max(np.abs(a - b)) / (np.max(np.abs(b)) + 1e-300))
+    npart = p.n
+    line = {"metric": "particle-steps/s (3+1-D Milne viscous BSQ, tabulated EoS)", "workload": "hotspots3d",
+            "value": npart * steps / (out["mixed"]["ms"] * 1e-3), "unit": "particle-steps/s",
+            "form": "mixed (FP32 Kahan sums and EoM, FP64 EoS Newton, state and RK2)",
+            "ms_per_step": out["mixed"]["ms"] / steps, "steps": steps, "warmup": args.warmup, "particles": npart,
+            "fp64": {"value": npart * steps / (out["fp64"]["ms"] * 1e-3), "ms_per_step": out["fp64"]["ms"] / steps,
+                     "phase_ms": out["fp64"]["phase_ms"]},
+            "mixed_phase_ms": out["mixed"]["phase_ms"],
+            "max_rel_err_mixed_vs_fp64": err, "device_bytes": out["mixed"]["bytes"],
+            "config": {"lattice": "120x120x100", "dx_fm": 0.1, "deta": 0.06, "h_fm": 0.2, "eta_over_s": 0.08,
+                       "zeta_over_s_peak": 0.1, "zeta_peak_T_GeV": 0.16, "eos": "synthetic table 151x41^3",
+                       "dt": rc.dt, "tau0": rc.t0}}
+    print(json.dumps(line))
+
+
+def serve_events(n_events, seed=3, steps=100):
+    """Events as the serving stream specifies (hot-spot count ~ U{10..60},
+    particle count log-uniform in [10k, 400k] on a dx = 0.05 fm lattice,
+    otherwise the 160k event's physics), each run for `steps` RK2 steps or
+    until every particle is below the freeze-out temperature."""
+    from ccake_gb300 import ics
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for j in range(n_events):
+        npart = float(np.exp(rng.uniform(np.log(1e4), np.log(4e5))))
+        side = max(20, int(round(np.sqrt(npart))))
+        n_hot = int(rng.integers(10, 61))
+        p, rc = ics.hotspots_2d(n_side=side, n_hot=n_hot, seed=int(rng.integers(1 << 31)))
+        out.append((p, rc, rc.t0 + steps * rc.dt))
+    return out
+
+
+def run_serve(args):
+    """Serving stream on one GPU through ccake_server_*: capacity with the
+    queue saturated, then Poisson arrivals at 80 % of that capacity (p50/p99
+    latency, events/h), and a subset of the same events run one at a time in
+    the plain FP64 form."""
+    import dataclasses
+    from ccake_gb300 import api, build
+    build.build()
+    n_ev = args.serve_events
+    evs = serve_events(n_ev, steps=args.steps)
+    mixed = [(p, dataclasses.replace(rc, precision=1), tm) for p, rc, tm in evs]
+    psteps = sum(p.n * args.steps for p, _, _ in evs)
+    # warm-up: one small event through a server (build, first graph capture)
+    srv = api.Server(steps_per_launch=args.serve_quantum)
+    t = srv.submit(mixed[0][0], mixed[0][1], mixed[0][2])
+    srv.wait_all()
+    srv.release(t)
+    # 1. capacity: every event submitted at once
+    t0 = time.perf_counter()
+    tickets = [srv.submit(p, rc, tm) for p, rc, tm in mixed]
+    srv.wait_all()
+    makespan = time.perf_counter() - t0
+    res = [srv.poll(t) for t in tickets]
+    for t in tickets:
+        srv.release(t)
+    failed = sum(r["state"] != "done" for r in res)
+    frozen = sum(r["frozen"] for r in res)
+    psteps = sum(r["particles"] * r["steps"] for r in res)
+    capacity = n_ev / makespan
+    # 2. Poisson arrivals at 80 % of capacity
+    rng = np.random.Generator(np.random.PCG64(3))
+    gaps = rng.exponential(1.0 / (0.8 * capacity), n_ev)
+    t_start = time.perf_counter()
+    tickets = []
+    next_t = t_start
+    for (p, rc, tm), gap in zip(mixed, gaps):
+        next_t += gap
+        while time.perf_counter() < next_t:
+            time.sleep(min(1e-3, max(0.0, next_t - time.perf_counter())))
+        tickets.append(srv.submit(p, rc, tm))
+    srv.wait_all()
+    wall = time.perf_counter() - t_start
+    res2 = [srv.poll(t) for t in tickets]
+    for t in tickets:
+        srv.release(t)
+    srv.close()
+    lat = np.array([r["latency_s"] for r in res2])
+    que = np.array([r["queue_s"] for r in res2])
+    # 3. the same events one at a time, plain FP64 form, on a subset
+    sub = evs[:args.serve_fp64_events]
+    t0 = time.perf_counter()
+    for p, rc, tm in sub:
+        g = api.GpuHydro(rc)
+        g.load(p)
+        g.initialize()
+        g.step(args.steps)
+        g.close()
+    fp64_each = (time.perf_counter() - t0) / len(sub)
+    line = {"metric": "events/h (serving stream, continuous batching, mixed form)", "workload": "serve",
+            "value": 3600.0 * n_ev / makespan, "unit": "events/h",
+            "events": n_ev, "steps_per_event": args.steps, "failed": failed, "stopped_by_freeze_out": frozen,
+            "particle_steps_per_s": psteps / makespan, "makespan_s": makespan,
+            "poisson": {"rate_events_per_s": 0.8 * capacity, "wall_s": wall,
+                        "events_per_h": 3600.0 * n_ev / wall,
+                        "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                                      "max": float(lat.max())},
+                        "queue_s": {"p50": float(np.percentile(que, 50)), "p99": float(np.percentile(que, 99))},
+                        "failed": sum(r["state"] != "done" for r in res2)},
+            "one_at_a_time_fp64": {"events": len(sub), "seconds_per_event": fp64_each,
+                                   "events_per_h": 3600.0 / fp64_each},
+            "config": {"events": "hot spots ~ U{10..60}, particles log-uniform in [10k, 400k] (dx = 0.05 fm "
+                                 "lattice), conformal-diagonal EoS, eta/s = 0.08, dt = 0.001 fm/c",
+                       "stop": f"{args.steps} RK2 steps or all particles below T = 150 MeV",
+                       "scaled": "runs are capped at the given steps (to freeze-out or 10 fm/c an event takes "
+                                 "~9000 steps at this dt)",
+                       "server": {"steps_per_launch": args.serve_quantum, "hbm_budget": "80% of free memory"}}}
+    print(json.dumps(line))
+
+
 def run_form_only(args, form):
     """Only the timed step loop of one precision form (for profiler launch
     lists); prints a partial line."""
@@ -485,8 +631,12 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--ref-steps", type=int, default=4, help="RK2 steps timed on the CPU")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", choices=["hotspots", "eos-table"], default="hotspots",
-                    help="hotspots: the 160k hot-spot event (default); eos-table: the EoS-inversion stress test")
+    ap.add_argument("--workload", choices=["hotspots", "eos-table", "hotspots3d", "serve"], default="hotspots",
+                    help="hotspots: the 160k hot-spot event (default); eos-table: the EoS-inversion stress test; "
+                         "hotspots3d: the 1.44M-particle 3+1-D event; serve: the serving stream")
+    ap.add_argument("--serve-events", type=int, default=64)
+    ap.add_argument("--serve-quantum", type=int, default=20)
+    ap.add_argument("--serve-fp64-events", type=int, default=8)
     ap.add_argument("--eos-rows", type=int, default=2_000_000)
     ap.add_argument("--eos-cpu-rows", type=int, default=20_000)
     ap.add_argument("--form", choices=["fp64", "mixed"], default=None,
@@ -498,6 +648,10 @@ def main():
         run_reference(args, world, rank)
     elif args.workload == "eos-table":
         run_eos_table(args)
+    elif args.workload == "hotspots3d":
+        run_hotspots3d(args)
+    elif args.workload == "serve":
+        run_serve(args)
     elif args.form:
         run_form_only(args, args.form)
     else:

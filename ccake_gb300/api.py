@@ -287,6 +287,88 @@ class GpuHydro:
         return x, th, st, it
 
 
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", _i64), ("max_active", _i32), ("steps_per_launch", _i32)]
+
+
+class EventResult(ctypes.Structure):
+    _fields_ = [("ticket", _i64), ("particles", _i64), ("state", _i32), ("status", _i32), ("steps", _i32),
+                ("frozen", _i32), ("tau", _f64), ("queue_s", _f64), ("latency_s", _f64), ("device_bytes", _i64)]
+
+
+class Server:
+    """ccake_server_*: continuous batching of independent events on one GPU."""
+
+    STATES = {0: "queued", 1: "running", 2: "done", 3: "failed"}
+
+    def __init__(self, hbm_budget_bytes=0, max_active=0, steps_per_launch=0):
+        L = lib()
+        P = ctypes.c_void_p
+        L.ccake_server_create.argtypes = [ctypes.POINTER(ServerConfig), ctypes.POINTER(P)]
+        L.ccake_server_destroy.argtypes = [P]
+        L.ccake_server_submit.argtypes = [P, ctypes.POINTER(CcakeConfig), ctypes.POINTER(ParticlesSoA), _f64,
+                                          ctypes.POINTER(_i64)]
+        L.ccake_server_poll.argtypes = [P, _i64, ctypes.POINTER(EventResult)]
+        L.ccake_server_wait_all.argtypes = [P]
+        L.ccake_server_copy_out.argtypes = [P, _i64, ctypes.c_char_p, _dp]
+        L.ccake_server_release.argtypes = [P, _i64]
+        cfg = ServerConfig(int(hbm_budget_bytes), int(max_active), int(steps_per_launch))
+        self.h = P()
+        code = L.ccake_server_create(ctypes.byref(cfg), ctypes.byref(self.h))
+        if code:
+            raise CcakeError(code, "server_create")
+        self._n = {}
+
+    def submit(self, particles, rc, tau_max):
+        cfg = make_config(rc)
+        arrs = {k: np.ascontiguousarray(getattr(particles, k), dtype=np.float64)
+                for k in ("x", "y", "eta", "e", "rhoB", "rhoS", "rhoQ", "ux", "uy", "ueta")}
+        soa = ParticlesSoA(particles.n, _d(arrs["x"]), _d(arrs["y"]), _d(arrs["eta"]), _d(arrs["e"]),
+                           _d(arrs["rhoB"]), _d(arrs["rhoS"]), _d(arrs["rhoQ"]), _d(arrs["ux"]),
+                           _d(arrs["uy"]), _d(arrs["ueta"]))
+        t = _i64()
+        code = lib().ccake_server_submit(self.h, ctypes.byref(cfg), ctypes.byref(soa), float(tau_max),
+                                         ctypes.byref(t))
+        if code:
+            raise CcakeError(code, "server_submit")
+        self._n[t.value] = particles.n
+        return t.value
+
+    def poll(self, ticket):
+        r = EventResult()
+        code = lib().ccake_server_poll(self.h, int(ticket), ctypes.byref(r))
+        if code:
+            raise CcakeError(code, "server_poll")
+        d = {k: getattr(r, k) for k, _ in EventResult._fields_}
+        d["state"] = self.STATES[d["state"]]
+        return d
+
+    def wait_all(self):
+        lib().ccake_server_wait_all(self.h)
+
+    def get(self, ticket, field):
+        out = np.empty(self._n[ticket], dtype=np.float64)
+        code = lib().ccake_server_copy_out(self.h, int(ticket), field.encode(), _d(out))
+        if code:
+            raise CcakeError(code, f"server_copy_out {field}")
+        return out
+
+    def release(self, ticket):
+        lib().ccake_server_release(self.h, int(ticket))
+        self._n.pop(ticket, None)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().ccake_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def exported_symbols():
     """Names declared in include/ccake_gpu.h."""
     import re

@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "ccake_gpu.h"
+#include "internal.hpp"
 #include "kernels.cuh"
 #include "mlp.cuh"
 
@@ -329,6 +330,50 @@ static int32_t* eos_scratch(ccake_ctx* ctx, int64_t n) {
   }
   return ctx->eos_scratch;
 }
+
+// ---------------------------------------------------------------------------
+// hooks for the event server
+// ---------------------------------------------------------------------------
+namespace ccake_internal {
+
+ccake_status_t step_enqueue(ccake_ctx* ctx, int n) {
+  if (!ctx || !ctx->initialized || n < 0) return CCAKE_ERR_STATE;
+  ensure_records(ctx, ctx->cfg.precision);
+  if (!ctx->graph_exec) {
+    CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    enqueue_substep(ctx, 1);
+    enqueue_substep(ctx, 2);
+    CK(cudaStreamEndCapture(ctx->stream, &ctx->graph));
+    CK(cudaGraphInstantiate(&ctx->graph_exec, ctx->graph, 0));
+  }
+  ccake_status_t s;
+  for (int k = 0; k < n; k++) {
+    if ((s = maybe_rebuild(ctx, true))) return s;
+    CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
+    ctx->steps_since_build++;
+  }
+  return CCAKE_OK;
+}
+
+ccake_status_t probe_enqueue(ccake_ctx* ctx, Probe* dev, Probe* host) {
+  launch_probe(ctx->p, dev, ctx->stream);
+  CK(cudaMemcpyAsync(host, dev, sizeof(Probe), cudaMemcpyDeviceToHost, ctx->stream));
+  return CCAKE_OK;
+}
+
+ccake_status_t clear_errors(ccake_ctx* ctx) { return reset_errors(ctx); }
+
+cudaStream_t ctx_stream(ccake_ctx* ctx) { return ctx->stream; }
+void ctx_set_time(ccake_ctx* ctx, double t) { ctx->t = t; }
+
+int64_t estimate_bytes(const ccake_config& cfg, int64_t n) {
+  // state and records, plus neighbour and candidate lists at the lattice
+  // densities of the bundled workloads (48 / 447 neighbours in 2-D / 3-D)
+  const int64_t K = cfg.dim == 3 ? 688 : 96, Kc = cfg.dim == 3 ? 912 : 112;
+  return n * (kDoublesPerParticle * 8 + 8 * 4 + K * 12 + Kc * 4) + (int64_t)(1 << 20);
+}
+
+}  // namespace ccake_internal
 
 extern "C" {
 

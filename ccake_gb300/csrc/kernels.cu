@@ -675,6 +675,28 @@ __global__ void k_eos_batch(EosDev eos, int entropy, int seed_mode, int64_t n, c
   }
 }
 
+// One block: the largest T over the particles, tau and the error counters.
+__global__ void __launch_bounds__(1024) k_probe(Ptrs p, Probe* out) {
+  __shared__ double red[32];
+  double m = 0.0;
+  const double* T = p.th + T_T * p.n;
+  for (int i = threadIdx.x; i < p.n; i += blockDim.x) m = fmax(m, T[i]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    m = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (threadIdx.x == 0) {
+      out->maxT = m;
+      out->tau = p.clock->t;
+      for (int q = 0; q < NERR; q++) out->err[q] = p.err[q];
+    }
+  }
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -744,6 +766,8 @@ void launch_pack_fp64(const RunConst& rc, const Ptrs& p, cudaStream_t s) {
   if (rc.cfg.dim == 3) k_pack_fp64<3><<<nb, kBlock, 0, s>>>(p);
   else k_pack_fp64<2><<<nb, kBlock, 0, s>>>(p);
 }
+
+void launch_probe(const Ptrs& p, Probe* out, cudaStream_t s) { k_probe<<<1, 1024, 0, s>>>(p, out); }
 
 void launch_totals(const RunConst& rc, const Ptrs& p, int nblocks, cudaStream_t s) {
   k_totals<<<nblocks, 256, 0, s>>>(rc, p);

@@ -97,6 +97,15 @@ constexpr int kEosFirstIters = 8;
 void launch_eos_batch(const EosDev& eos, int entropy, int seed_mode, int64_t n, const double* in4, double* tbqs,
                       double* th16, int32_t* status, int32_t* iters, int32_t* scratch, cudaStream_t s);
 
+// Stop-rule probe of an event: the largest temperature, the current tau and
+// the error counters (filled by launch_probe).
+struct Probe {
+  double maxT;
+  double tau;
+  int32_t err[NERR];
+};
+void launch_probe(const Ptrs& p, Probe* out, cudaStream_t s);
+
 constexpr int kTotBlocks = 608;   // 4 x 152 SMs; fixed so the sums are reproducible
 
 // CTAs of the cell-count scan (1024 cells each)

@@ -169,7 +169,7 @@ def hotspots_2d(n_side=400, dx=0.05, h=0.1, n_hot=30, sigma=0.4, seed=20251203, 
 
 def hotspots_3d(n_xy=120, n_eta=100, dx=0.1, deta=0.06, h=0.2, n_hot=30, sigma_perp=0.4, sigma_eta=0.5,
                 plateau=1.5, tail=1.0, seed=20251204, tau0=1.0, dt=0.001, eta_over_s=0.08, floor_GeV=0.01,
-                peak_range=(5.0, 50.0), eos_kind=1):
+                peak_range=(5.0, 50.0), eos_kind=1, zeta_over_s=0.0):
     """Config 4 lattice: (x, y, eta_s) grid, 30 hot spots with sigma_perp = 0.4 fm
     and sigma_eta = 0.5 (centres ~ N(0, 3 fm) in x, y and ~ U[-plateau, plateau]
     in eta), multiplied by a longitudinal plateau of half-width 1.5 with
@@ -177,6 +177,8 @@ def hotspots_3d(n_xy=120, n_eta=100, dx=0.1, deta=0.06, h=0.2, n_hot=30, sigma_p
     Milne coordinates, non-factorised 3-D kernel on (x, y, eta) as in the
     reference's default (src/kernel.cpp:34-84). ``eos_kind`` 1 is the
     conformal-diagonal EoS; the tabulated EoS of the 3+1-D benchmark is 2.
+    ``zeta_over_s`` > 0 adds bulk viscosity zeta/s peaked at T = 0.16 GeV
+    (Gaussian of width 0.02 GeV, zeta_mode 3) with that peak value.
     """
     rng = np.random.Generator(np.random.PCG64(seed))
     cx = rng.normal(0.0, 3.0, n_hot)
@@ -200,6 +202,7 @@ def hotspots_3d(n_xy=120, n_eta=100, dx=0.1, deta=0.06, h=0.2, n_hot=30, sigma_p
     z = np.zeros_like(x)
     p = Particles(x, y, eta, eG / HBARC_GEVFM, rhoB, z.copy(), rhoQ, z.copy(), z.copy(), z.copy())
     cfg = RunConfig(dim=3, eos_kind=eos_kind, using_shear=1 if eta_over_s > 1e-10 else 0,
-                    shear_relax_mode=1, thermo_mode=1, zeta_mode=1, zeta_over_s=0.0, eta_over_s=eta_over_s,
+                    shear_relax_mode=1, thermo_mode=1, zeta_mode=3 if zeta_over_s > 0 else 1,
+                    zeta_over_s=zeta_over_s, eta_over_s=eta_over_s,
                     hT=h, hEta=h, t0=tau0, dt=dt, xmin=xmin, ymin=xmin, etamin=emin)
     return p, cfg

@@ -213,6 +213,53 @@ ccake_status_t ccake_eos_invert_device(ccake_ctx* ctx, int32_t entropy_mode, int
                                        const double* d_in4, double* d_tbqs, double* d_th16, int32_t* d_status,
                                        int32_t* d_iters, void* stream);
 
+/* ------------------------------------------------------------------------
+ * Event server: continuous batching of independent hydro events on one GPU.
+ * No reference counterpart (the reference runs one event per process).
+ *
+ * Submitted events wait in a FIFO queue; an internal thread admits them while
+ * the device bytes of the resident events stay within hbm_budget_bytes (and
+ * at most max_active run at once), keeps their state resident, and advances
+ * each on its own stream in quanta of steps_per_launch RK2 steps (CUDA-graph
+ * launches) until every particle has T < freeze_out_T of its config or tau
+ * reaches its tau_max. Events admitted while others run share the GPU.
+ * ------------------------------------------------------------------------ */
+typedef struct ccake_server ccake_server;
+
+typedef struct ccake_server_config {
+  int64_t hbm_budget_bytes; /* device bytes for resident events (0: 80 % of the free memory) */
+  int32_t max_active;       /* events advanced concurrently (0: 32) */
+  int32_t steps_per_launch; /* RK2 steps per quantum (0: 20) */
+} ccake_server_config;
+
+typedef struct ccake_event_result {
+  int64_t ticket;
+  int64_t particles;
+  int32_t state;     /* 0 queued, 1 running, 2 done, 3 failed */
+  int32_t status;    /* ccake_status_t of a failed event, else 0 */
+  int32_t steps;     /* RK2 steps taken */
+  int32_t frozen;    /* 1 if it stopped because every particle had T < freeze_out_T */
+  double tau;        /* final tau (fm/c) */
+  double queue_s;    /* submit -> admission */
+  double latency_s;  /* submit -> done */
+  int64_t device_bytes;
+} ccake_event_result;
+
+ccake_status_t ccake_server_create(const ccake_server_config* cfg, ccake_server** out);
+/* Stops the internal thread (events still running are abandoned) and frees everything. */
+ccake_status_t ccake_server_destroy(ccake_server* srv);
+/* Copies the event (config and host arrays) into the queue; *ticket identifies it. */
+ccake_status_t ccake_server_submit(ccake_server* srv, const ccake_config* cfg, const ccake_particles_soa* p,
+                                   double tau_max, int64_t* ticket);
+/* Current state of an event (CCAKE_ERR_INVALID for an unknown or released ticket). */
+ccake_status_t ccake_server_poll(ccake_server* srv, int64_t ticket, ccake_event_result* out);
+/* Blocks until no event is queued or running. */
+ccake_status_t ccake_server_wait_all(ccake_server* srv);
+/* A field of a finished event, caller's particle order (as ccake_copy_out). */
+ccake_status_t ccake_server_copy_out(ccake_server* srv, int64_t ticket, const char* field, double* host_out);
+/* Frees a finished event's device memory and forgets it. */
+ccake_status_t ccake_server_release(ccake_server* srv, int64_t ticket);
+
 /* Learned Newton seed for the tabulated EoS: a 4-64-64-64-4 tanh MLP from
  * (log e, rho_i / e^(3/4)) to (log T, mu_i / T), both standardised, trained
  * and evaluated with BF16 tensor-core kernels. No reference counterpart (the

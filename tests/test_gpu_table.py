@@ -159,3 +159,22 @@ def test_table_eos_hydro_parity(table, precision):
     for f in ("u0", "shv11"):
         assert relerr(g.get(f), orc.get(f), floor=1e-2) < tol, f
     assert np.array_equal(g.get_int("eos_id"), orc.get_int("eos_id"))
+
+
+def test_three_d_table_eos_with_bulk_parity(table):
+    # 3+1-D Milne lattice with the table EoS, shear and peaked bulk
+    # viscosity, FP64 form against the oracle
+    p, rc = ics.hotspots_3d(n_xy=14, n_eta=10, n_hot=3, seed=5, eos_kind=2, zeta_over_s=0.1, floor_GeV=4.0,
+                            peak_range=(5.0, 20.0))
+    g = gpu_with_table(rc, table)
+    g.load(p)
+    g.initialize()
+    ot = O.OracleTable(*table)
+    orc = O.OracleRun(p, rc, table=ot)
+    assert orc.initialize() == 0
+    g.step(3)
+    assert orc.step(3) == 0
+    for f in ("T", "muB", "e", "ext_s", "ext_bulk", "sigma_lab"):
+        assert relerr(g.get(f), orc.get(f), floor=1e-3) < 1e-10, f
+    for f in ("u0", "u2", "shv33", "bulk"):
+        assert relerr(g.get(f), orc.get(f), floor=1e-2) < 1e-10, f
