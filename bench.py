@@ -145,19 +145,39 @@ def read_traffic(kernel):
     return None
 
 
+def read_mixed_traffic():
+    """DRAM bytes per launch of the mixed-form kernels from the committed ncu summary."""
+    out = {}
+    for k in ("passA_mixed", "thermo_mixed", "passB_mixed", "eom_mixed"):
+        v = read_traffic(k)
+        if v is not None:
+            out[k] = v
+    return out
+
+
 # -- the reference arm ---------------------------------------------------------------------------
-def cpu_reference(p, rc, steps, warmup=1):
-    """Times the oracle (CPU restatement of the reference) with all host threads."""
+def cpu_reference(p, rc, steps, warmup=1, threads=0, repeats=3):
+    """Times the oracle (CPU restatement of the reference): `warmup` steps,
+    then the median of `repeats` runs of `steps` RK2 steps, on `threads`
+    OpenMP threads (0: all host cores). Returns (particle-steps/s, seconds
+    per run)."""
+    import ctypes
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle_py as O
     O.build()
+    O.lib().orc_set_threads.argtypes = [ctypes.c_int]
+    O.lib().orc_set_threads(int(threads))
     r = O.OracleRun(p, rc)
     r.initialize()
     if warmup:
         r.step(warmup)
-    t0 = time.perf_counter()
-    r.step(steps)
-    dt = time.perf_counter() - t0
+    runs = []
+    for _ in range(max(1, repeats)):
+        t0 = time.perf_counter()
+        r.step(steps)
+        runs.append(time.perf_counter() - t0)
+    O.lib().orc_set_threads(0)
+    dt = float(np.median(runs))
     return p.n * steps / dt, dt
 
 
@@ -166,14 +186,15 @@ def run_reference(args, world, rank):
         return
     p, rc = workload()
     steps = max(1, min(args.steps, args.ref_steps))
-    value, dt = cpu_reference(p, rc, steps, warmup=min(args.warmup, 1))
+    value, dt = cpu_reference(p, rc, steps, warmup=1)
     cores = os.cpu_count()
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "config": config_dict(p.n, {"host": "cpu"}),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"{steps} of the event's RK2 steps, all {p.n} particles, OMP threads={cores}"},
+                             "sample": f"median of 3 runs of {steps} RK2 steps after 1 warm-up step, all {p.n} "
+                                       f"particles, OMP threads={cores}"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "the reference's Kokkos/Cabana build needs dependencies absent here; its CPU restatement "
                     "(oracle/, same algorithms) is timed"}
@@ -225,10 +246,11 @@ def run_ours(args, world, rank):
     if rank != 0:
         return
     hbm_peak, peak_kind = measured_peaks()
-    # algorithmic bytes per particle (FP64 scalars x 8): pass B reads positions,
-    # velocity, p, e, sigma_lab, Pi, pi (3), thermo (14), state (12), step cache (12)
-    # and writes the state (12): 60 scalars; pass A 28; cell kernels 3.
-    alg = {"cells": 3 * 8 * n, "passA": 28 * 8 * n, "passB": 60 * 8 * n}
+    # algorithmic bytes and FP64 operations per launch from the committed
+    # traffic model (ccake_gb300/traffic_model.py, config C2)
+    from ccake_gb300 import traffic_model as TM
+    alg = {"cells": TM.bytes_per_launch("C2", "binning", n), "passA": TM.bytes_per_launch("C2", "passA", n),
+           "passB": TM.bytes_per_launch("C2", "passB", n)}
     names = ["cells", "passA", "passB"]
     dom = int(np.argmax(prof))
     kname = names[dom]
@@ -238,9 +260,8 @@ def run_ours(args, world, rank):
         fp64 = fp64_peak_tflops()
     except Exception:
         pass
-    # FP64 operations per particle per launch counted from the kernels' arithmetic (48 neighbours):
-    # pass A ~ 48 x 22 + EoS/thermo ~ 1.4k; pass B ~ 48 x 40 + EoM ~ 3.4k
-    flops = {"cells": 0.0, "passA": (48 * 22 + 1400) * n, "passB": (48 * 40 + 3400) * n}
+    flops = {"cells": 0.0, "passA": TM.flops_per_launch("C2", "passA", n),
+             "passB": TM.flops_per_launch("C2", "passB", n)}
     fp64_ach = flops[kname] / (prof[dom] * 1e-3) / 1e12
     traffic = read_traffic(kname)
     line = {
@@ -263,10 +284,13 @@ def run_ours(args, world, rank):
     }
     if not args.no_cpu:
         ref_steps = max(1, args.ref_steps)
-        cv, cdt = cpu_reference(p, rc, ref_steps, warmup=0)
+        cv, cdt = cpu_reference(p, rc, ref_steps, warmup=1, repeats=3)
+        c1, c1dt = cpu_reference(p, rc, 1, warmup=0, threads=1, repeats=1)
         line["cpu_baseline"] = {"value": cv, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-                                "sample": f"{ref_steps} RK2 steps of the same 160k-particle event on the host "
-                                          f"(oracle/, OpenMP, {os.cpu_count()} threads)"}
+                                "sample": f"median of 3 runs of {ref_steps} RK2 steps (after 1 warm-up step) of "
+                                          f"the same 160k-particle event on the host (oracle/, OpenMP, "
+                                          f"{os.cpu_count()} threads)",
+                                "one_thread": {"value": c1, "unit": UNIT, "sample": "1 RK2 step, 1 thread"}}
     print(json.dumps(line))
 
 
@@ -315,8 +339,18 @@ def run_mixed(p, rc, args, world, dist):
     tot = {k: float(abs(runs[1]["totals"][k] - runs[0]["totals"][k]) / (abs(runs[0]["totals"][k]) + 1e-300))
            for k in ("S", "B", "Q", "E")}
     n = p.n
+    from ccake_gb300 import traffic_model as TM
+    hbm_peak, peak_kind = measured_peaks()
+    names = ["cells", "passA", "passB"]
+    dom = int(np.argmax(prof))
+    alg = TM.bytes_per_launch("C2", {"cells": "binning"}.get(names[dom], names[dom]), n)
+    ach = alg / (prof[dom] * 1e-3) / 1e9
     return {"value": world * n * args.steps / (ms_max * 1e-3), "unit": UNIT, "ms_per_step": ms_max / args.steps,
-            "phase_ms": dict(zip(["cells", "passA", "passB"], [float(x) for x in prof])),
+            "phase_ms": dict(zip(names, [float(x) for x in prof])),
+            "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": ach, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": ach / hbm_peak, "peak_kind": peak_kind,
+                         "traffic_per_substep_bytes": sum(v for k, v in read_mixed_traffic().items()),
+                         "note": "pass A = smoothing + EoS kernels, pass B = gradient + EoM kernels"},
             "gpu_launches": 16 * args.steps,
             "max_rel_err_after_100_steps": err, "totals_rel_diff_after_100_steps": tot,
             "error_reference": "plain FP64 form on the GPU (equal to the FP64 oracle within 1e-10 per field)",
@@ -361,7 +395,7 @@ def run_eos_table(args):
     rc = ics.RunConfig(eos_kind=2, thermo_mode=1)
     g = api.GpuHydro(rc)
     g.set_eos_table(n, lo, d, fields, conf5, cdiag5)
-    x_true = eos_table.sample_states(n_rows)
+    x_true = eos_table.sample_states(n_rows, seed=1)
     fw = g.eos_thermo(0, x_true)
     tgt = np.ascontiguousarray(np.column_stack([fw[:, 5], fw[:, 2], fw[:, 3], fw[:, 4]]))
     dev = torch.device("cuda")
@@ -392,7 +426,7 @@ def run_eos_table(args):
 
     # learned seed: the seed network trained on 5M table samples (BF16 tensor cores)
     t0 = time.perf_counter()
-    mse = g.mlp_train(n_samples=5_000_000, epochs=20, batch=32768, lr=3e-3, seed=1)
+    mse = g.mlp_train(n_samples=5_000_000, epochs=20, batch=32768, lr=3e-3, seed=2)
     torch.cuda.synchronize()
     train_s = time.perf_counter() - t0
     msl, xl, stl, itl = timed(2)
@@ -513,6 +547,7 @@ def serve_events(n_events, seed=3, steps=100):
     particle count log-uniform in [10k, 400k] on a dx = 0.05 fm lattice,
     otherwise the 160k event's physics), each run for `steps` RK2 steps or
     until every particle is below the freeze-out temperature."""
+    import dataclasses
     from ccake_gb300 import ics
     rng = np.random.Generator(np.random.PCG64(seed))
     out = []
@@ -521,6 +556,7 @@ def serve_events(n_events, seed=3, steps=100):
         side = max(20, int(round(np.sqrt(npart))))
         n_hot = int(rng.integers(10, 61))
         p, rc = ics.hotspots_2d(n_side=side, n_hot=n_hot, seed=int(rng.integers(1 << 31)))
+        rc = dataclasses.replace(rc, particlization=1)   # stop when every particle froze out at 150 MeV
         out.append((p, rc, rc.t0 + steps * rc.dt))
     return out
 
@@ -597,7 +633,8 @@ def run_serve(args):
                                    "events_per_h": 3600.0 / fp64_each},
             "config": {"events": "hot spots ~ U{10..60}, particles log-uniform in [10k, 400k] (dx = 0.05 fm "
                                  "lattice), conformal-diagonal EoS, eta/s = 0.08, dt = 0.001 fm/c",
-                       "stop": f"{args.steps} RK2 steps or all particles below T = 150 MeV",
+                       "stop": f"{args.steps} RK2 steps or every particle frozen out (freeze-out status "
+                               f"machine at T = 150 MeV)",
                        "scaled": "runs are capped at the given steps (to freeze-out or 10 fm/c an event takes "
                                  "~9000 steps at this dt)",
                        "server": {"steps_per_launch": args.serve_quantum, "hbm_budget": "80% of free memory"}}}

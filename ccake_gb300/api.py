@@ -26,7 +26,7 @@ class CcakeConfig(ctypes.Structure):
         [(n, _f64) for n in (
             "hT", "hEta", "t0", "dt", "eos_c", "eos_T0", "eos_muB0", "eos_muQ0", "eos_muS0", "eta_over_s",
             "zeta_over_s", "zeta_cs2_A", "zeta_cs2_p", "zeta_peak_T", "zeta_peak_width", "xmin", "ymin",
-            "etamin", "freeze_out_T", "skin_frac")]
+            "etamin", "freeze_out_T", "skin_frac")] + [("particlization", _i32), ("reserved", _i32)]
 
 
 class ParticlesSoA(ctypes.Structure):
@@ -75,6 +75,7 @@ def lib():
                      "ccake_update_viscosities", "ccake_smooth_gradients", "ccake_time_derivatives"):
             getattr(L, name).argtypes = [P]
         L.ccake_step.argtypes = [P, _i32]
+        L.ccake_continue_evolution.argtypes = [P, _f64, ctypes.POINTER(_i32)]
         L.ccake_step_timed.argtypes = [P, _i32, ctypes.POINTER(ctypes.c_float)]
         L.ccake_profile_phases.argtypes = [P, _i32, _dp]
         L.ccake_device_bytes.argtypes = [P, ctypes.POINTER(_i64)]
@@ -90,6 +91,7 @@ def lib():
                                               ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         L.ccake_set_eos_table.argtypes = [P, _ip, _dp, _dp, _dp, _dp, _dp]
         L.ccake_eos_thermo_batch.argtypes = [P, _i32, _i64, _dp, _dp]
+        L.ccake_set_eos_table_file.argtypes = [P, ctypes.c_char_p, _i32, _dp, _dp]
         _fp = ctypes.POINTER(ctypes.c_float)
         L.ccake_mlp_train.argtypes = [P, _i64, _i32, _i32, ctypes.c_double, ctypes.c_uint64, _dp]
         L.ccake_mlp_get_params.argtypes = [P, _fp, _fp]
@@ -163,6 +165,12 @@ class GpuHydro:
     def step(self, n=1):
         self._check(lib().ccake_step(self.h, int(n)), "step")
 
+    def continue_evolution(self, max_tau):
+        """The reference's stop rule: False once every particle froze out (particlization) or t > max_tau."""
+        k = _i32()
+        self._check(lib().ccake_continue_evolution(self.h, float(max_tau), ctypes.byref(k)), "continue_evolution")
+        return bool(k.value)
+
     def step_timed(self, n):
         """Advances n steps; returns the device time (ms) measured on the library's stream."""
         ms = ctypes.c_float()
@@ -224,6 +232,13 @@ class GpuHydro:
         c5 = np.ascontiguousarray(conf5, dtype=np.float64)
         d5 = np.ascontiguousarray(cdiag5, dtype=np.float64)
         self._check(lib().ccake_set_eos_table(self.h, _i(n), _d(lo), _d(d), _d(f), _d(c5), _d(d5)), "set_eos_table")
+
+    def set_eos_table_file(self, path, normalize_by_T, conf5, cdiag5):
+        """Loads a thermo.dat table (the reference's text format); see ccake_set_eos_table_file."""
+        c5 = np.ascontiguousarray(conf5, dtype=np.float64)
+        d5 = np.ascontiguousarray(cdiag5, dtype=np.float64)
+        self._check(lib().ccake_set_eos_table_file(self.h, str(path).encode(), int(bool(normalize_by_T)), _d(c5),
+                                                   _d(d5)), "set_eos_table_file")
 
     def eos_thermo(self, chain_index, tbqs):
         """17 model fields at rows (T, muB, muQ, muS) for EoS chain index chain_index."""

@@ -2,9 +2,12 @@
 // Owns device memory, orders particles by neighbour cell, sequences the
 // kernels of a derivative evaluation and captures one RK2 step in a CUDA
 // graph that ccake_step replays.
+#include <sys/stat.h>
+
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <numeric>
 #include <string>
@@ -46,6 +49,7 @@ struct ccake_ctx {
   int32_t* mlp_err = nullptr;
   MlpNorm mlp_norm{};
   bool mlp_ready = false;
+  int32_t* d_count = nullptr;   // one int32 (frozen-particle count)
   // scratch of the two-pass batch inversion (capacity + 1 int32)
   int32_t* eos_scratch = nullptr;
   int64_t eos_scratch_cap = 0;
@@ -151,7 +155,7 @@ ccake_status_t reset_errors(ccake_ctx* ctx) {
 
 // doubles per particle in the double slab (state, fields, records)
 constexpr int64_t kDoublesPerParticle =
-    RA + RB + 2 + RAF / 2 + RBF / 2 + 2 * NY + 1 + NTH + 1 + 3 + 1 + 1 + 1 + NPI + NGRAD + NDER + 1 + 1 + 3;
+    RA + RB + 2 + RAF / 2 + RBF / 2 + 2 * NY + 1 + NTH + 1 + 3 + 1 + 1 + 1 + NPI + NGRAD + NDER + 1 + 1 + 3 + 1;
 
 // The smoothing record of each precision form is written by that form's
 // pass B; before a pass A of the other form runs, it is packed from the state.
@@ -212,6 +216,7 @@ void enqueue_substep(ccake_ctx* ctx, int sub) {
   int mode = B_EOM | B_UPDATE | (sub == 2 ? B_WRITE_Y0 : 0);
   enqueue_passB(ctx, mode, sub == 1 ? 0.5 * dt : dt);
   launch_clock(ctx->p, sub, dt, ctx->stream);
+  if (sub == 2 && ctx->cfg.particlization) launch_freeze(ctx->rc, ctx->p, ctx->stream);
 }
 
 struct FieldRef {
@@ -319,6 +324,7 @@ struct Scratch {
 static int32_t* eos_scratch(ccake_ctx* ctx, int64_t n) {
   if (n > ctx->eos_scratch_cap) {
     if (ctx->eos_scratch) cudaFree(ctx->eos_scratch);
+  if (ctx->d_count) cudaFree(ctx->d_count);
     ctx->eos_scratch = nullptr;
     ctx->eos_scratch_cap = 0;
     if (cudaMalloc(&ctx->eos_scratch, (size_t)(n + 1) * sizeof(int32_t)) != cudaSuccess) {
@@ -447,6 +453,7 @@ ccake_status_t ccake_ctx_destroy(ccake_ctx* ctx) {
   if (ctx->mlp_sse) cudaFree(ctx->mlp_sse);
   if (ctx->mlp_err) cudaFree(ctx->mlp_err);
   if (ctx->eos_scratch) cudaFree(ctx->eos_scratch);
+  if (ctx->d_count) cudaFree(ctx->d_count);
   if (ctx->d_table) cudaFree(ctx->d_table);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
@@ -492,6 +499,7 @@ ccake_status_t ccake_load_particles(ccake_ctx* ctx, const ccake_particles_soa* h
   p.y = take(NY); p.y0 = take(NY); p.m = take(1); p.th = take(NTH); p.gam = take(1); p.v = take(3);
   p.slab = take(1); p.sig = take(1); p.bulk = take(1); p.pi = take(NPI);
   p.grads = take(NGRAD); p.derivs = take(NDER); p.in_e = take(1); p.in_s = take(1); p.in_rho = take(3);
+  p.frz1_e = take(1);
   p.partials = d;
   d += (size_t)kTotBlocks * 6;
   p.clock = reinterpret_cast<Clock*>(d);
@@ -525,7 +533,7 @@ ccake_status_t ccake_initialize(ccake_ctx* ctx) {
   if (!ctx) return CCAKE_ERR_INVALID;
   if (!ctx->loaded) return fail(ctx, CCAKE_ERR_STATE, "load particles first");
   if (ctx->eos.kind == 2 && !ctx->d_table) return fail(ctx, CCAKE_ERR_STATE, "set the EoS table first");
-  Clock c{ctx->cfg.t0, ctx->cfg.t0};
+  Clock c{ctx->cfg.t0, ctx->cfg.t0, 0, 0};
   CK(cudaMemcpyAsync(ctx->p.clock, &c, sizeof(Clock), cudaMemcpyHostToDevice, ctx->stream));
   ccake_status_t s = reset_errors(ctx);
   if (s) return s;
@@ -658,6 +666,7 @@ ccake_status_t ccake_profile_phases(ccake_ctx* ctx, int32_t n_steps, double* ms3
       enqueue_passB(ctx, B_EOM | B_UPDATE | (sub == 2 ? B_WRITE_Y0 : 0), sub == 1 ? 0.5 * dt : dt);
       CK(cudaEventRecord(ev[3], ctx->stream));
       launch_clock(ctx->p, sub, dt, ctx->stream);
+      if (sub == 2 && ctx->cfg.particlization) launch_freeze(ctx->rc, ctx->p, ctx->stream);
       if (sub == 2) ctx->steps_since_build++;
       CK(cudaEventSynchronize(ev[3]));
       float m;
@@ -682,6 +691,23 @@ ccake_status_t ccake_device_bytes(const ccake_ctx* ctx, int64_t* bytes) {
   const int64_t nd = n * kDoublesPerParticle;
   const int64_t ni = n * 8 + (int64_t)ctx->rc.grid.ncell * 2 + 2 * (int64_t)scan_tiles(ctx->rc.grid.ncell);
   *bytes = nd * 8 + ni * 4 + (int64_t)ctx->p.K * n * 12 + (int64_t)ctx->p.Kc * n * 4;
+  return CCAKE_OK;
+}
+
+ccake_status_t ccake_continue_evolution(ccake_ctx* ctx, double max_tau, int32_t* keep_going) {
+  if (!ctx || !keep_going) return CCAKE_ERR_INVALID;
+  if (!ctx->initialized) return fail(ctx, CCAKE_ERR_STATE, "initialize first");
+  bool keep = true;
+  if (ctx->cfg.particlization) {
+    if (!ctx->d_count && cudaMalloc(&ctx->d_count, sizeof(int32_t)) != cudaSuccess)
+      return fail(ctx, CCAKE_ERR_NOMEM, "allocation");
+    launch_count_frozen(ctx->p, ctx->d_count, ctx->stream);
+    int32_t frozen = 0;
+    CK(cudaMemcpyAsync(&frozen, ctx->d_count, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    keep = frozen < ctx->n;
+  }
+  *keep_going = (keep && ctx->t <= max_tau) ? 1 : 0;
   return CCAKE_OK;
 }
 
@@ -861,6 +887,77 @@ ccake_status_t ccake_set_eos_table(ccake_ctx* ctx, const int32_t* n, const doubl
   ctx->rc.efreeze = o[5];
   e.tab.f = ctx->d_table;
   return CCAKE_OK;
+}
+
+ccake_status_t ccake_set_eos_table_file(ccake_ctx* ctx, const char* eos_path, int32_t normalize_by_T,
+                                        const double* conf5, const double* cdiag5) {
+  if (!ctx || !eos_path || !conf5 || !cdiag5) return CCAKE_ERR_INVALID;
+  std::string path(eos_path);
+  struct stat st{};
+  if (stat(path.c_str(), &st) == 0 && S_ISDIR(st.st_mode)) path += "/thermo.dat";
+  FILE* fh = std::fopen(path.c_str(), "rb");
+  if (!fh) return fail(ctx, CCAKE_ERR_INVALID, "cannot open " + path);
+  std::string text;
+  {
+    char buf[1 << 16];
+    size_t k;
+    while ((k = std::fread(buf, 1, sizeof(buf), fh)) > 0) text.append(buf, k);
+    std::fclose(fh);
+  }
+  const char* c = text.c_str();
+  const char* end = c + text.size();
+  // header: the grid sizes
+  int32_t n[4];
+  {
+    const char* eol = static_cast<const char*>(std::memchr(c, '\n', end - c));
+    if (!eol) return fail(ctx, CCAKE_ERR_INVALID, "no header line");
+    std::string head(c, eol);
+    int k = std::sscanf(head.c_str(), "%d %d %d %d", &n[0], &n[1], &n[2], &n[3]);
+    if (k != 4) return fail(ctx, CCAKE_ERR_INVALID, "the header must hold 4 grid sizes");
+    c = eol + 1;
+  }
+  size_t nodes = 1;
+  for (int k = 0; k < 4; k++) {
+    if (n[k] < 1) return fail(ctx, CCAKE_ERR_INVALID, "bad grid size");
+    nodes *= (size_t)n[k];
+  }
+  std::vector<double> grid(nodes * 4), fields(nodes * 17);
+  size_t row = 0;
+  while (c < end && row < nodes) {
+    while (c < end && (*c == ' ' || *c == '\t' || *c == '\r' || *c == '\n')) c++;
+    if (c >= end) break;
+    for (int q = 0; q < 21; q++) {
+      char* stop = nullptr;
+      const double v = std::strtod(c, &stop);
+      if (stop == c) return fail(ctx, CCAKE_ERR_INVALID, "row " + std::to_string(row) + ": expected 21 numbers");
+      c = stop;
+      if (q < 4) grid[row * 4 + q] = v;
+      else fields[row * 17 + (q - 4)] = v;
+    }
+    row++;
+  }
+  if (row != nodes) return fail(ctx, CCAKE_ERR_INVALID, "the table has fewer rows than its grid sizes give");
+  // axes to fm^-1, grids rebuilt from the extremes; field units
+  const double hc1 = 1.0 / 197.3269804;
+  static const int pw[17] = {4, 3, 3, 3, 3, 4, 0, 2, 2, 2, 2, 2, 2, 2, 2, 2, 2};
+  double lo[4], hi[4], d[4];
+  for (int k = 0; k < 4; k++) { lo[k] = 1e300; hi[k] = -1e300; }
+  for (size_t r = 0; r < nodes; r++)
+    for (int k = 0; k < 4; k++) {
+      const double v = grid[r * 4 + k] * hc1;
+      grid[r * 4 + k] = v;
+      lo[k] = std::min(lo[k], v);
+      hi[k] = std::max(hi[k], v);
+    }
+  for (int k = 0; k < 4; k++) d[k] = n[k] <= 1 ? 0.0 : (hi[k] - lo[k]) / (n[k] - 1.0);
+  for (size_t r = 0; r < nodes; r++) {
+    const double T = grid[r * 4];
+    for (int q = 0; q < 17; q++) {
+      if (pw[q] == 0) continue;
+      fields[r * 17 + q] *= normalize_by_T ? std::pow(T, pw[q]) : std::pow(hc1, pw[q]);
+    }
+  }
+  return ccake_set_eos_table(ctx, n, lo, d, fields.data(), conf5, cdiag5);
 }
 
 ccake_status_t ccake_eos_thermo_batch(ccake_ctx* ctx, int32_t chain_index, int64_t n, const double* tbqs,

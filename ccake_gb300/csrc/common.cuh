@@ -77,6 +77,8 @@ struct RunConst {
 struct Clock {
   double t0;
   double t;
+  int32_t frzc;   // steps seen by the freeze-out status machine (0, 1, 2 = third and later)
+  int32_t pad;
 };
 
 // Error counters raised by the kernels (read back by the host after a call).

@@ -675,25 +675,98 @@ __global__ void k_eos_batch(EosDev eos, int entropy, int seed_mode, int64_t n, c
   }
 }
 
-// One block: the largest T over the particles, tau and the error counters.
+// One block: the largest T and the number of frozen particles, tau and the
+// error counters.
 __global__ void __launch_bounds__(1024) k_probe(Ptrs p, Probe* out) {
   __shared__ double red[32];
+  __shared__ int32_t redc[32];
   double m = 0.0;
+  int32_t c = 0;
   const double* T = p.th + T_T * p.n;
-  for (int i = threadIdx.x; i < p.n; i += blockDim.x) m = fmax(m, T[i]);
+  for (int i = threadIdx.x; i < p.n; i += blockDim.x) {
+    m = fmax(m, T[i]);
+    c += p.freeze[i] >= 4 ? 1 : 0;
+  }
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  for (int o = 16; o > 0; o >>= 1) {
+    m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    c += __shfl_xor_sync(0xffffffffu, c, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    red[threadIdx.x >> 5] = m;
+    redc[threadIdx.x >> 5] = c;
+  }
   __syncthreads();
   if (threadIdx.x < 32) {
-    m = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    const bool in = threadIdx.x < (blockDim.x >> 5);
+    m = in ? red[threadIdx.x] : 0.0;
+    c = in ? redc[threadIdx.x] : 0;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    for (int o = 16; o > 0; o >>= 1) {
+      m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+      c += __shfl_xor_sync(0xffffffffu, c, o);
+    }
     if (threadIdx.x == 0) {
       out->maxT = m;
       out->tau = p.clock->t;
       for (int q = 0; q < NERR; q++) out->err[q] = p.err[q];
+      out->frozen = c;
     }
+  }
+}
+
+// Freeze-out status machine after a step (reference include/freeze_out.h:
+// check_freeze_out_status :455-500, then bsqsvfreezeout :549-615 without the
+// hypersurface output): 0 -> 1 when e <= e_FO; 1 -> 3 when the particle lost
+// its neighbours or e stayed <= e_FO without rising, 1 -> 1 when e rose, else
+// back to 0; from the third step on, particles without neighbours freeze
+// (freeze_out_evo :322-375), status 3 becomes 4 (:914) and the energy of
+// the live particles is snapshotted.
+__global__ void k_freeze(RunConst rc, Ptrs p) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.n) return;
+  const int frzc = p.clock->frzc;
+  const double ef = rc.efreeze;
+  const double e = p.th[T_E * p.n + i];
+  int f = p.freeze[i];
+  if (f == 0) {
+    if (e <= ef) f = 1;
+  } else if (f == 1) {
+    if (p.btrack[i] == -1) f = 3;
+    else if (e > p.frz1_e[i]) f = 1;
+    else if (e <= ef) f = 3;
+    else f = 0;
+  }
+  if (frzc == 1) {
+    p.frz1_e[i] = e;
+  } else if (frzc >= 2) {
+    if (f < 4 && p.btrack[i] == 0) {
+      f = 4;
+      p.btrack[i] = -1;
+    }
+    if (f == 3) f = 4;
+    if (f < 4) p.frz1_e[i] = e;
+  }
+  p.freeze[i] = f;
+}
+
+__global__ void k_freeze_advance(Clock* c) {
+  if (c->frzc < 2) c->frzc++;
+}
+
+__global__ void __launch_bounds__(1024) k_count_frozen(Ptrs p, int32_t* out) {
+  __shared__ int32_t red[32];
+  int32_t c = 0;
+  for (int i = threadIdx.x; i < p.n; i += blockDim.x) c += p.freeze[i] >= 4 ? 1 : 0;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = c;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    c = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if (threadIdx.x == 0) *out = c;
   }
 }
 
@@ -768,6 +841,13 @@ void launch_pack_fp64(const RunConst& rc, const Ptrs& p, cudaStream_t s) {
 }
 
 void launch_probe(const Ptrs& p, Probe* out, cudaStream_t s) { k_probe<<<1, 1024, 0, s>>>(p, out); }
+
+void launch_freeze(const RunConst& rc, const Ptrs& p, cudaStream_t s) {
+  k_freeze<<<(p.n + kBlock - 1) / kBlock, kBlock, 0, s>>>(rc, p);
+  k_freeze_advance<<<1, 1, 0, s>>>(p.clock);
+}
+
+void launch_count_frozen(const Ptrs& p, int32_t* out, cudaStream_t s) { k_count_frozen<<<1, 1024, 0, s>>>(p, out); }
 
 void launch_totals(const RunConst& rc, const Ptrs& p, int nblocks, cudaStream_t s) {
   k_totals<<<nblocks, 256, 0, s>>>(rc, p);

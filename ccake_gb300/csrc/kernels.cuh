@@ -40,6 +40,7 @@ struct Ptrs {
   double* partials;      // reduction scratch
   // per-substep neighbour list written by pass A, read by pass B (k-major:
   // entry k of particle i at k * n + i); nbr_f is the radial factor of grad W
+  double* frz1_e;        // n  energy snapshot of the freeze-out status machine
   float4* posf;          // FP32 copy of the positions (candidate prefilter)
   int32_t* nbr_idx;      // K * n
   double* nbr_f;         // K * n
@@ -103,7 +104,11 @@ struct Probe {
   double maxT;
   double tau;
   int32_t err[NERR];
+  int32_t frozen;   // particles with freeze >= 4
+  int32_t pad;
 };
+void launch_freeze(const RunConst& rc, const Ptrs& p, cudaStream_t s);
+void launch_count_frozen(const Ptrs& p, int32_t* out, cudaStream_t s);
 void launch_probe(const Ptrs& p, Probe* out, cudaStream_t s);
 
 constexpr int kTotBlocks = 608;   // 4 x 152 SMs; fixed so the sums are reproducible

@@ -7,9 +7,10 @@
 //      smoothing) on the event's own stream;
 //   2. for every running event whose last quantum has completed (a CUDA event
 //      query, no blocking), reads the stop-rule probe the quantum left in
-//      pinned memory (largest T, tau, error counters) and either retires the
-//      event or enqueues the next quantum: steps_per_launch RK2 steps
-//      (CUDA-graph launches) and the probe;
+//      pinned memory (frozen-particle count, largest T, tau, error counters)
+//      and either retires the event (every particle frozen out with
+//      particlization, or tau at tau_max) or enqueues the next quantum:
+//      steps_per_launch RK2 steps (CUDA-graph launches) and the probe;
 //   3. sleeps briefly when nothing changed.
 // Events therefore share the GPU through concurrent streams, and an event
 // submitted while others run starts as soon as memory allows.
@@ -171,7 +172,9 @@ void scheduler(ccake_server* srv) {
           else if (pr.err[ccake::E_NBR_OVERFLOW]) st = CCAKE_ERR_CAPACITY;
           failed = st != 0;
           if (!failed) {
-            const bool cold = pr.maxT < e->cfg.freeze_out_T;
+            // the reference's stop rule: every particle frozen out (with
+            // particlization) or tau at tau_max
+            const bool cold = e->cfg.particlization && pr.frozen >= e->n;
             if (cold || e->tau >= e->tau_max - 0.5 * e->cfg.dt) {
               std::lock_guard<std::mutex> lk(srv->mu);
               e->frozen = cold ? 1 : 0;

@@ -133,3 +133,34 @@ def sample_states(n, seed=20251205, T_range=(0.05, 0.8), mu_max=0.45, margin=1e-
     hi = np.array([T_range[1], mu_max, mu_max, mu_max]) / HBARC
     span = hi - lo
     return lo + span * (margin + (1 - 2 * margin) * rng.uniform(size=(n, 4)))
+
+
+HBARC_MEV = 197.3269804   # MeV fm (the reference's hbarc_MeVfm)
+# powers of T (normalize_by_T) or of MeV (absolute units) per field, file order
+FIELD_POWERS = (4, 3, 3, 3, 3, 4, 0, 2, 2, 2, 2, 2, 2, 2, 2, 2, 2)
+FIELD_NAMES = ("p", "s", "B", "S", "Q", "e", "cs2", "chiBB", "chiQQ", "chiSS", "chiBQ", "chiBS", "chiQS",
+               "chiTB", "chiTQ", "chiTS", "chiTT")
+
+
+def write_thermo_dat(path, n, lo, d, fields, normalize_by_T=True):
+    """Writes a table (fm units, nodes row-major with muS fastest) as the
+    reference's thermo.dat: a header line with the 4 grid sizes, then one row
+    per node `T muB muQ muS p s B S Q e cs2 chiBB chiQQ chiSS chiBQ chiBS chiQS
+    chiTB chiTQ chiTS chiTT` with the axes in MeV and the fields divided by
+    T^k (normalize_by_T, T in fm^-1) or in MeV^k (src/eos_table.cpp:14-100,
+    src/interpolatorND.cpp:125-168). Values are printed with 17 significant
+    digits."""
+    n = np.asarray(n, dtype=np.int64)
+    lo = np.asarray(lo, dtype=np.float64)
+    d = np.asarray(d, dtype=np.float64)
+    fields = np.asarray(fields, dtype=np.float64)
+    axes = [lo[k] + d[k] * np.arange(n[k]) for k in range(4)]
+    grid = np.stack(np.meshgrid(*axes, indexing="ij"), axis=-1).reshape(-1, 4)
+    pw = np.array(FIELD_POWERS, dtype=np.float64)
+    if normalize_by_T:
+        f = fields / grid[:, :1] ** pw
+    else:
+        f = fields * HBARC_MEV ** pw
+    with open(path, "w") as fh:
+        fh.write(" ".join(str(int(v)) for v in n) + "\n")
+        np.savetxt(fh, np.hstack([grid * HBARC_MEV, f]), fmt="%.17g")

@@ -61,6 +61,7 @@ class RunConfig:
     etamin: float = -0.1
     freeze_out_T: float = 150.0 / HBARC_MEVFM
     skin_frac: float = 0.0         # candidate-list skin / 2h (0: 0.1), GPU only
+    particlization: int = 0        # freeze-out status machine after every step
 
 
 @dataclasses.dataclass

@@ -1,0 +1,111 @@
+"""Algorithmic traffic and arithmetic of the SPH step (the roofline inputs).
+
+Rule: compulsory HBM traffic of a two-pass fused design. Every per-particle
+FP64 scalar one derivative evaluation must read or write is counted once at
+8 B; neighbour reads count 0 (tile reuse); cell-sort keys 8 B per particle
+per build. The field lists are the ones the passes of this library touch:
+
+  pass A (smoothing + EoS):  read the state and the EoS seed, write the LRF
+                             densities and the thermodynamics;
+  pass B (gradients + EoM + RK2): read positions, velocities, pass-A outputs,
+                             the state and the step-start cache, write the state.
+
+`python -m ccake_gb300.traffic_model` writes traffic_model.json beside this
+file (the committed copy).
+"""
+from __future__ import annotations
+
+import json
+import os
+
+SCALAR = 8   # bytes per FP64 scalar
+
+# per-substep field lists (names of FP64 scalars per particle)
+FIELDS = {
+    "C1": {   # 2-D ideal, no charges (Gubser)
+        "binning": ["x", "y", "key"],
+        "passA": ["x", "y", "u_x", "u_y", "ext_s", "T_seed",
+                  "sigma_lab", "s_star", "T", "p", "w", "dwds", "cs2"],
+        "passB": ["x", "y", "u_x", "u_y", "p", "sigma_lab", "w", "dwds", "s", "T", "ext_s",
+                  "y0_x", "y0_y", "y0_ux", "y0_uy", "y0_s",
+                  "y_x", "y_y", "y_ux", "y_uy", "y_s"],
+        "step_extra": ["y0_x", "y0_y", "y0_ux", "y0_uy", "y0_s"],
+    },
+    "C2": {   # 2-D viscous, B/S/Q, shear (the bench event)
+        "binning": ["x", "y", "key"],
+        "passA": ["x", "y", "u_x", "u_y", "ext_s", "ext_B", "ext_S", "ext_Q", "T_seed", "muB_seed", "muQ_seed",
+                  "muS_seed",
+                  "sigma_lab", "s_star", "B_star", "S_star", "Q_star", "T", "muB", "muQ", "muS", "p", "e", "w",
+                  "cs2", "dwds", "dwdB", "dwdS"],
+        "passB": ["x", "y", "u_x", "u_y", "p", "e", "sigma_lab", "ext_Pi", "ext_pi11", "ext_pi12",
+                  "T", "muB", "muQ", "muS", "rhoB", "rhoS", "rhoQ", "s", "w", "cs2", "dwds", "dwdB", "dwdS", "dwdQ",
+                  "st_x", "st_y", "st_ux", "st_uy", "st_s", "st_B", "st_S", "st_Q", "st_Pi", "st_pi11", "st_pi12",
+                  "st_pi22",
+                  "y0_x", "y0_y", "y0_ux", "y0_uy", "y0_s", "y0_B", "y0_S", "y0_Q", "y0_Pi", "y0_pi11", "y0_pi12",
+                  "y0_pi22",
+                  "y_x", "y_y", "y_ux", "y_uy", "y_s", "y_B", "y_S", "y_Q", "y_Pi", "y_pi11", "y_pi12", "y_pi22"],
+        "step_extra": ["y0_x", "y0_y", "y0_ux", "y0_uy", "y0_s", "y0_B", "y0_S", "y0_Q", "y0_Pi", "y0_pi11",
+                       "y0_pi12", "y0_pi22"],
+    },
+}
+
+# FP64 operations per particle per RK2 step (2 substeps), FP64 form:
+# pairs x (W + smoothing sums ~25, gradient sums incl. shear ~60) + EoM + EoS
+FLOPS = {
+    "C1": {"neighbours": 48, "per_pair": 50, "eom": 800, "eos": 200},
+    "C2": {"neighbours": 48, "per_pair": 85, "eom": 1500, "eos": 400},
+    "C4": {"neighbours": 447, "per_pair": 120, "eom": 2500, "eos": 1200},
+}
+
+# 3-D: +1 position, +1 velocity, +2 shear components per state copy
+C4_BYTES_PER_PARTICLE_STEP = 1900
+
+
+def scalars(config: str, part: str) -> int:
+    return len(FIELDS[config][part])
+
+
+def bytes_per_launch(config: str, kernel: str, n: int) -> int:
+    """Algorithmic bytes of one launch of `kernel` ("binning", "passA",
+    "passB") over n particles."""
+    return scalars(config, kernel) * SCALAR * n
+
+
+def bytes_per_particle_step(config: str) -> int:
+    if config == "C4":
+        return C4_BYTES_PER_PARTICLE_STEP
+    f = FIELDS[config]
+    per_sub = len(f["binning"]) + len(f["passA"]) + len(f["passB"])
+    return (2 * per_sub + len(f["step_extra"])) * SCALAR
+
+
+def flops_per_particle_step(config: str) -> int:
+    c = FLOPS[config]
+    return 2 * (c["neighbours"] * c["per_pair"] + c["eom"] + c["eos"])
+
+
+def flops_per_launch(config: str, kernel: str, n: int) -> float:
+    """FP64 operations of one pass launch: pass A carries the smoothing part
+    of the pair work (~30 %) and the EoS, pass B the gradient part and the EoM."""
+    c = FLOPS[config]
+    pair = c["neighbours"] * c["per_pair"]
+    if kernel == "passA":
+        return n * (0.3 * pair + c["eos"])
+    if kernel == "passB":
+        return n * (0.7 * pair + c["eom"])
+    return 0.0
+
+
+def as_dict():
+    return {"rule": "compulsory FP64 scalars x 8 B per particle per launch; neighbour reads 0; keys 8 B",
+            "fields": FIELDS, "flops": FLOPS,
+            "bytes_per_particle_step": {c: bytes_per_particle_step(c) for c in ("C1", "C2", "C4")},
+            "flops_per_particle_step": {c: flops_per_particle_step(c) for c in ("C1", "C2", "C4")}}
+
+
+if __name__ == "__main__":
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "traffic_model.json")
+    with open(path, "w") as fh:
+        json.dump(as_dict(), fh, indent=1)
+        fh.write("\n")
+    print(path)

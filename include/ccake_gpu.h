@@ -58,6 +58,9 @@ typedef struct ccake_config {
   double skin_frac;           /* candidate-list skin as a fraction of 2h (0: 0.1); the
                                  list is rebuilt every R steps, R = floor(skin / (2 dt vmax)),
                                  vmax = max(1, 1/tau) in Milne (x, y, eta_s) coordinates */
+  int32_t particlization;     /* run the freeze-out status machine after every step
+                                 (include/settings.h particlization_enabled) */
+  int32_t reserved;
 } ccake_config;
 
 /* Host struct-of-arrays particle input, the columns of the reference's
@@ -124,6 +127,11 @@ ccake_status_t ccake_time_derivatives(ccake_ctx* ctx);
  * src/evolver.cpp:97-117, :344-517). */
 ccake_status_t ccake_step(ccake_ctx* ctx, int32_t n_steps);
 
+/* Stop rule: *keep_going = 0 once every particle is frozen out (freeze >= 4,
+ * with particlization) or tau > max_tau. Replaces
+ * SPHWorkstation::continue_evolution (src/sph_workstation.cpp:1992-2024). */
+ccake_status_t ccake_continue_evolution(ccake_ctx* ctx, double max_tau, int32_t* keep_going);
+
 /* ccake_step with its device time: CUDA events recorded on the context's
  * stream around the n_steps graph launches (milliseconds in *device_ms).
  * Measurement entry point; no reference counterpart. */
@@ -182,6 +190,18 @@ ccake_status_t ccake_eos_invert_batch(ccake_ctx* ctx, int32_t entropy_mode, int6
 ccake_status_t ccake_set_eos_table(ccake_ctx* ctx, const int32_t* n, const double* lo, const double* d,
                                    const double* fields, const double* conf5, const double* cdiag5);
 
+/* Tabulated EoS from the reference's text format: eos_path is a thermo.dat
+ * file or a directory holding one; line 1 the 4 grid sizes, then one line
+ * per node "T muB muQ muS p s B S Q e cs2 chiBB chiQQ chiSS chiBQ chiBS chiQS
+ * chiTB chiTQ chiTS chiTT" (axes in MeV, nodes row-major with muS fastest).
+ * Axes are converted to fm^-1 and each grid rebuilt from its extremes; with
+ * normalize_by_T the fields are ratios p/T^4 ... chi/T^2, else MeV powers.
+ * Then as ccake_set_eos_table. Replaces EoS_table::EoS_table
+ * (src/eos_table.cpp:14-100) with InterpolatorND<4>::load_data_from_dat
+ * (src/interpolatorND.cpp:125-228). */
+ccake_status_t ccake_set_eos_table_file(ccake_ctx* ctx, const char* eos_path, int32_t normalize_by_T,
+                                        const double* conf5, const double* cdiag5);
+
 /* Model thermodynamics at n host rows tbqs (T, muB, muQ, muS) for EoS chain
  * index chain_index (0 = first model of the chain), 17 values per row in the
  * table's field order (NaN outside a table). Replaces
@@ -221,8 +241,9 @@ ccake_status_t ccake_eos_invert_device(ccake_ctx* ctx, int32_t entropy_mode, int
  * the device bytes of the resident events stay within hbm_budget_bytes (and
  * at most max_active run at once), keeps their state resident, and advances
  * each on its own stream in quanta of steps_per_launch RK2 steps (CUDA-graph
- * launches) until every particle has T < freeze_out_T of its config or tau
- * reaches its tau_max. Events admitted while others run share the GPU.
+ * launches) until every particle is frozen out (particlization in its
+ * config; the freeze-out status machine at freeze_out_T) or tau reaches its
+ * tau_max. Events admitted while others run share the GPU.
  * ------------------------------------------------------------------------ */
 typedef struct ccake_server ccake_server;
 
@@ -238,7 +259,7 @@ typedef struct ccake_event_result {
   int32_t state;     /* 0 queued, 1 running, 2 done, 3 failed */
   int32_t status;    /* ccake_status_t of a failed event, else 0 */
   int32_t steps;     /* RK2 steps taken */
-  int32_t frozen;    /* 1 if it stopped because every particle had T < freeze_out_T */
+  int32_t frozen;    /* 1 if it stopped because every particle froze out */
   double tau;        /* final tau (fm/c) */
   double queue_s;    /* submit -> admission */
   double latency_s;  /* submit -> done */

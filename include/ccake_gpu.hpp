@@ -103,8 +103,13 @@ class SPHWorkstation {
     check(ccake_time_derivatives(s_.ctx()), s_.ctx(), "ccake_time_derivatives");
   }
   void advance_timestep(double dt, int rk_order) { evolver_.execute_timestep(dt, rk_order); }
-  // stop rule without particlization: t <= max_tau (src/sph_workstation.cpp:1992-2024)
-  bool continue_evolution() const { return s_.t() <= max_tau_; }
+  // stop rule: every particle frozen out (with particlization) or t > max_tau
+  // (src/sph_workstation.cpp:1992-2024)
+  bool continue_evolution() const {
+    int32_t keep = 0;
+    check(ccake_continue_evolution(s_.ctx(), max_tau_, &keep), s_.ctx(), "ccake_continue_evolution");
+    return keep != 0;
+  }
 
  private:
   SystemState& s_;

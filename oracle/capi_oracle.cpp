@@ -1,5 +1,8 @@
 // C entry points of the CPU oracle, loaded by the tests and the benchmark's
 // CPU-baseline leg through ctypes. TEST INFRASTRUCTURE ONLY (see oracle.hpp).
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 #include "oracle.hpp"
 #include "table_oracle.hpp"
 
@@ -206,6 +209,15 @@ void* orc_table_create(const int32_t* n, const double* lo, const double* d, cons
   return t;
 }
 void orc_table_destroy(void* t) { delete (Table*)t; }
+
+// OpenMP threads of the oracle's parallel loops (timing baselines).
+void orc_set_threads(int n) {
+#ifdef _OPENMP
+  omp_set_num_threads(n > 0 ? n : omp_get_num_procs());
+#else
+  (void)n;
+#endif
+}
 
 // Interpolated fields (17) and the Jacobian (5 x 4) of s, rhoB, rhoS, rhoQ, e
 // with respect to (T, muB, muQ, muS) at one point.

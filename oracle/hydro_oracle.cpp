@@ -595,6 +595,42 @@ void rk2_step(System& s, NbrList& nl) {
   const double t0 = s.t, dt = s.cfg.dt;
   step_rk(s, nl, .5 * dt, t0);
   step_rk(s, nl, dt, t0);
+  if (s.cfg.particlization) freeze_out_status(s);
+}
+
+// Freeze-out status machine after a step: FreezeOut::check_freeze_out_status
+// (include/freeze_out.h:455-500), then bsqsvfreezeout (:549-615) without the
+// hypersurface output: from the third step on, particles without neighbours
+// freeze (freeze_out_evo, :322-375), status 3 becomes 4 (bsqsvinterpolate,
+// :914), and the energy of the live particles is snapshotted.
+void freeze_out_status(System& s) {
+  const double ef = s.efcheck;
+  const int frzc = s.frzc;
+  if ((int)s.frz1_e.size() != s.n) s.frz1_e.assign(s.n, 0.0);
+  for (int a = 0; a < s.n; a++) {
+    int f = s.freeze[a];
+    const double e = s.th[kE][a];
+    if (f == 0) {
+      if (e <= ef) f = 1;
+    } else if (f == 1) {
+      if (s.btrack[a] == -1) f = 3;
+      else if (e > s.frz1_e[a]) f = 1;
+      else if (e <= ef) f = 3;
+      else f = 0;
+    }
+    if (frzc == 1) {
+      s.frz1_e[a] = e;
+    } else if (frzc >= 2) {
+      if (f < 4 && s.btrack[a] == 0) {
+        f = 4;
+        s.btrack[a] = -1;
+      }
+      if (f == 3) f = 4;
+      if (f < 4) s.frz1_e[a] = e;
+    }
+    s.freeze[a] = f;
+  }
+  s.frzc = frzc < 2 ? frzc + 1 : 2;
 }
 
 // src/system_state.cpp:738-885 (entropy, BSQ, energy totals) without the
@@ -643,6 +679,9 @@ void initialize(System& s, NbrList& nl) {
     eos_full_thermo(s.cfg, s.table, 0, x, o);
     efc = o[5];
   }
+  s.efcheck = efc;
+  s.frzc = 0;
+  s.frz1_e.assign(s.n, 0.0);
   int bad = 0;
 #pragma omp parallel for reduction(+ : bad)
   for (int a = 0; a < s.n; a++) {

@@ -50,6 +50,8 @@ struct Config {
   double zeta_peak_T, zeta_peak_width;   // peaked zeta/s mode (config 4)
   double xmin, ymin, etamin;              // lower corner of the IC grid
   double freeze_out_T;                    // fm^-1
+  int32_t particlization;                 // freeze-out status machine after every step
+  int32_t pad2;
 };
 
 // Per-particle state, struct of arrays.
@@ -65,6 +67,11 @@ struct System {
   std::vector<double> ext_shv[6];   // (0,0),(0,1),(0,2),(1,1),(1,2) of the 2x3 block; [5] unused
   std::vector<double> Ez;           // contribution_to_total_Ez
   std::vector<int32_t> freeze, btrack;
+  // freeze-out status machine: energy snapshot of the previous step, steps
+  // seen, freeze-out energy density e(T_FO, 0, 0, 0)
+  std::vector<double> frz1_e;
+  int frzc = 0;
+  double efcheck = 0;
   // input
   std::vector<double> in_e, in_s, in_rho[3], in_bulk;
   std::vector<double> in_shv[6];    // pi^{xx},xy,xeta,yy,yeta,etaeta (fm^-4..)
@@ -116,6 +123,7 @@ void smooth_gradients(System& s, const NbrList& nl);
 void evaluate_time_derivatives(System& s);
 void get_time_derivatives(System& s, NbrList& nl);
 void rk2_step(System& s, NbrList& nl);
+void freeze_out_status(System& s);
 void initialize(System& s, NbrList& nl);
 
 struct Totals { double S, B, Sq, Q, E, Ez; };

@@ -22,7 +22,8 @@ class Config(ctypes.Structure):
         "thermo_mode", "pad1")] + [(n, ctypes.c_double) for n in (
         "hT", "hEta", "t0", "dt", "eos_c", "eos_T0", "eos_muB0", "eos_muQ0", "eos_muS0",
         "eta_over_s", "zeta_over_s", "zeta_cs2_A", "zeta_cs2_p", "zeta_peak_T",
-        "zeta_peak_width", "xmin", "ymin", "etamin", "freeze_out_T")]
+        "zeta_peak_width", "xmin", "ymin", "etamin", "freeze_out_T")] + [
+        ("particlization", ctypes.c_int32), ("pad2", ctypes.c_int32)]
 
 
 def make_config(rc) -> Config:

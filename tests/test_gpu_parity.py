@@ -255,3 +255,27 @@ def test_three_d_milne_parity():
     for f in ("x", "y", "eta", "u0", "u1", "u2", "ext_s", "T", "e", "sigma_lab", "ext_shv0", "ext_shv2",
               "ext_shv4", "shv33", "Ez"):
         assert relerr(gpu.get(f), orc.get(f)) < RTOL, f
+
+
+def test_freeze_out_status_machine_matches_oracle():
+    # particlization with a freeze-out temperature inside the event's range
+    # (180 MeV): statuses 0 -> 1 -> 3 -> 4 and the stop rule, against the oracle
+    p, rc = ics.hotspots_2d(n_side=48, n_hot=6, seed=7)
+    rc = dataclasses.replace(rc, particlization=1, freeze_out_T=180.0 / 197.3269804)
+    gpu = api.GpuHydro(rc)
+    gpu.load(p)
+    gpu.initialize()
+    orc = O.OracleRun(p, rc)
+    assert orc.initialize() == 0
+    assert np.array_equal(gpu.get_int("freeze"), orc.get_int("freeze"))
+    seen = set()
+    for _ in range(6):
+        gpu.step(2)
+        assert orc.step(2) == 0
+        fg, fo = gpu.get_int("freeze"), orc.get_int("freeze")
+        assert np.array_equal(fg, fo)
+        seen |= set(np.unique(fg).tolist())
+    assert {0, 1, 4} <= seen
+    keep = gpu.continue_evolution(max_tau=10.0)
+    assert keep == (np.count_nonzero(fg >= 4) < p.n)
+    assert gpu.continue_evolution(max_tau=rc.t0) is False

@@ -67,7 +67,8 @@ def test_tight_budget_admits_one_event_at_a_time():
 
 def test_freeze_out_stops_an_event():
     p, rc = events(1)[0]
-    rc = dataclasses.replace(rc, freeze_out_T=1.0)   # 197 MeV: every particle is already below it
+    # 197 MeV: every particle starts below it and is frozen at initialisation
+    rc = dataclasses.replace(rc, freeze_out_T=1.0, particlization=1)
     srv = api.Server(steps_per_launch=5)
     t = srv.submit(p, rc, rc.t0 + 1000 * rc.dt)
     srv.wait_all()
