@@ -561,6 +561,60 @@ def serve_events(n_events, seed=3, steps=100):
     return out
 
 
+def run_serve_replicated(args, world, rank):
+    """The serving stream over N GPUs: every rank builds the same events, runs
+    its share (by device bytes, ccake_gb300.replicas) on its own event
+    server with the queue saturated, and rank 0 reports the aggregate
+    events/h over the slowest rank's makespan."""
+    import dataclasses
+    import torch
+    import torch.distributed as dist
+    from ccake_gb300 import api, build, replicas
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    build.build()
+    dist.init_process_group("nccl")
+    evs = serve_events(args.serve_events, steps=args.steps)
+    mixed = [(p, dataclasses.replace(rc, precision=1), tm) for p, rc, tm in evs]
+    sizes = [p.n for p, _, _ in evs]
+
+    def run_share(share):
+        srv = api.Server(steps_per_launch=args.serve_quantum)
+        if share:   # warm-up
+            t = srv.submit(*share[0][1])
+            srv.wait_all()
+            srv.release(t)
+        dist.barrier()
+        t0 = time.perf_counter()
+        tick = [(i, srv.submit(*ev)) for i, ev in share]
+        srv.wait_all()
+        span = time.perf_counter() - t0
+        out = []
+        for i, t in tick:
+            r = srv.poll(t)
+            r["makespan"] = span
+            out.append((i, r))
+            srv.release(t)
+        srv.close()
+        return out
+
+    if not mixed:
+        return
+    # ranks with no event still join the barrier and the gather
+    res = replicas.run_replicated(mixed, sizes, rank, world, run_share, dist)
+    dist.destroy_process_group()
+    if rank != 0:
+        return
+    span = max(r["makespan"] for r in res)
+    psteps = sum(r["particles"] * r["steps"] for r in res)
+    print(json.dumps({"metric": "events/h (serving stream, continuous batching, mixed form)", "workload": "serve",
+                      "value": 3600.0 * len(res) / span, "unit": "events/h", "n_gpus": world,
+                      "events": len(res), "steps_per_event": args.steps, "scaling": "strong",
+                      "failed": sum(r["state"] != "done" for r in res),
+                      "particle_steps_per_s": psteps / span, "makespan_s": span,
+                      "parallelism": f"replicas{world}: events split by device bytes, one event server per GPU"}))
+
+
 def run_serve(args):
     """Serving stream on one GPU through ccake_server_*: capacity with the
     queue saturated, then Poisson arrivals at 80 % of that capacity (p50/p99
@@ -568,6 +622,10 @@ def run_serve(args):
     the plain FP64 form."""
     import dataclasses
     from ccake_gb300 import api, build
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world > 1:
+        run_serve_replicated(args, world, int(os.environ.get("RANK", "0")))
+        return
     build.build()
     n_ev = args.serve_events
     evs = serve_events(n_ev, steps=args.steps)
