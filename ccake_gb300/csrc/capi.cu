@@ -36,6 +36,7 @@ struct ccake_ctx {
   double* dbuf = nullptr;
   int32_t* ibuf = nullptr;
   double* d_table = nullptr;
+  float* d_table_f = nullptr;   // FP32 densities of the nodes (mixed-form Newton Jacobians)
   int records_form = 0;   // which smoothing record matches the state: 0 FP64, 1 mixed
   // candidate list: skin (fm), validity and rebuild schedule
   double skin = 0.0;
@@ -455,6 +456,7 @@ ccake_status_t ccake_ctx_destroy(ccake_ctx* ctx) {
   if (ctx->eos_scratch) cudaFree(ctx->eos_scratch);
   if (ctx->d_count) cudaFree(ctx->d_count);
   if (ctx->d_table) cudaFree(ctx->d_table);
+  if (ctx->d_table_f) cudaFree(ctx->d_table_f);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return CCAKE_OK;
@@ -490,12 +492,13 @@ ccake_status_t ccake_load_particles(ccake_ctx* ctx, const ccake_particles_soa* h
   p.n = (int)n;
   double* d = ctx->dbuf;
   auto take = [&](size_t k) { double* r = d; d += k * n; return r; };
-  // the records come first: their slabs are multiples of 64 bytes, so the
-  // 16-byte vector loads stay aligned for any n
+  // the records come first: their slabs are multiples of 32 bytes a
+  // particle, so the 16- and 32-byte vector loads stay aligned for any n
+  static_assert(RA % 4 == 0 && RB % 4 == 0 && RAF % 8 == 0 && RBF % 8 == 0, "record alignment");
   p.recA = take(RA); p.recB = take(RB);
-  p.posf = reinterpret_cast<float4*>(take(2));
   p.recAf = reinterpret_cast<float*>(take(RAF / 2));
   p.recBf = reinterpret_cast<float*>(take(RBF / 2));
+  p.posf = reinterpret_cast<float4*>(take(2));
   p.y = take(NY); p.y0 = take(NY); p.m = take(1); p.th = take(NTH); p.gam = take(1); p.v = take(3);
   p.slab = take(1); p.sig = take(1); p.bulk = take(1); p.pi = take(NPI);
   p.grads = take(NGRAD); p.derivs = take(NDER); p.in_e = take(1); p.in_s = take(1); p.in_rho = take(3);
@@ -870,10 +873,14 @@ ccake_status_t ccake_set_eos_table(ccake_ctx* ctx, const int32_t* n, const doubl
     if (!(conf5[q] > 0.0) || !(cdiag5[q] > 0.0)) return fail(ctx, CCAKE_ERR_INVALID, "bad fallback scales");
   drop_graph(ctx);
   if (ctx->d_table) cudaFree(ctx->d_table);
+  if (ctx->d_table_f) cudaFree(ctx->d_table_f);
   ctx->d_table = nullptr;
-  if (cudaMalloc(&ctx->d_table, nodes * 17 * sizeof(double)) != cudaSuccess)
+  ctx->d_table_f = nullptr;
+  if (cudaMalloc(&ctx->d_table, nodes * 17 * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&ctx->d_table_f, nodes * 8 * sizeof(float)) != cudaSuccess)
     return fail(ctx, CCAKE_ERR_NOMEM, "table allocation");
   CK(cudaMemcpyAsync(ctx->d_table, fields, nodes * 17 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  launch_table_f32(ctx->d_table, ctx->d_table_f, (int64_t)nodes, ctx->stream);
   CK(cudaStreamSynchronize(ctx->stream));
   EosDev& e = ctx->eos;
   for (int k = 0; k < 4; k++) { e.tab.n[k] = n[k]; e.tab.lo[k] = lo[k]; e.tab.d[k] = d[k]; }
@@ -882,10 +889,12 @@ ccake_status_t ccake_set_eos_table(ccake_ctx* ctx, const int32_t* n, const doubl
   // e(T_FO, 0, 0, 0) from the table, evaluated on the host copy
   EosDev host = e;
   host.tab.f = fields;
+  host.tab.fd = nullptr;
   double x4[4] = {ctx->cfg.freeze_out_T, 0, 0, 0}, o[17];
   model_thermo(host, M_TABLE, x4, o);
   ctx->rc.efreeze = o[5];
   e.tab.f = ctx->d_table;
+  e.tab.fd = ctx->d_table_f;
   return CCAKE_OK;
 }
 

@@ -22,6 +22,9 @@ __host__ __device__ inline Scales make_scales(double c, double T0, double muB0, 
 // chiQS chiTB chiTQ chiTS chiTT), layout of reference src/eos_table.cpp:31-35.
 struct TableView {
   const double* f = nullptr;
+  // FP32 copy of the densities s, rhoB, rhoS, rhoQ, e of every node (8 floats
+  // a node, the last 3 zero), for the FP32 Newton Jacobian of the mixed form
+  const float* fd = nullptr;
   int n[4] = {1, 1, 1, 1};
   double lo[4] = {0, 0, 0, 0};
   double d[4] = {0, 0, 0, 0};
@@ -33,6 +36,8 @@ struct EosDev {
   Scales own;               // scales of the analytic default model
   Scales conf, cdiag;       // fallback scales behind a table
   TableView tab;
+  // 1: Newton Jacobians of the table in FP32 (residuals stay FP64)
+  int jac32 = 0;
 };
 
 enum Model : int { M_CONF = 0, M_CDIAG = 1, M_TABLE = 2 };
@@ -104,9 +109,10 @@ __host__ __device__ inline void confdiag_thermo(const Scales& k, const double* x
 // NaN outside.
 // jac (optional): derivatives of the interpolated s, rhoB, rhoS, rhoQ, e
 // (fields 1..5) with respect to (T, muB, muQ, muS), the exact Jacobian of the
-// multilinear interpolant inside the cell.
+// multilinear interpolant inside the cell; with jf32 (and the FP32 node copy)
+// formed in FP32 from the FP32 densities, the values in o staying FP64.
 __host__ __device__ inline void table_thermo(const TableView& t, const double* x, double* o,
-                                             double (*jac)[4] = nullptr) {
+                                             double (*jac)[4] = nullptr, bool jf32 = false) {
   int ind[4];
   double fr[4], dfr[4];
   for (int k = 0; k < 4; k++) {
@@ -120,7 +126,40 @@ __host__ __device__ inline void table_thermo(const TableView& t, const double* x
     if (ind[k] + 1 == t.n[k]) { fr[k] = 1.0 - fr[k]; dfr[k] = -dfr[k]; ind[k]--; }
     if (ind[k] < 0 || ind[k] >= t.n[k] || !(fabs(q) < 2e9)) { for (int i = 0; i < 17; i++) o[i] = NAN; return; }
   }
-  for (int i = 0; i < 17; i++) o[i] = 0.0;
+  if (jac && jf32 && t.fd) {
+    // Newton iterations of the mixed form: FP64 densities, FP32 Jacobian
+    float frf[4], dfrf[4], jf[5][4];
+    for (int k = 0; k < 4; k++) { frf[k] = (float)fr[k]; dfrf[k] = (float)dfr[k]; }
+    for (int f = 0; f < 5; f++) for (int j = 0; j < 4; j++) jf[f][j] = 0.0f;
+    for (int i = 1; i < 6; i++) o[i] = 0.0;
+    for (int h = 0; h < 16; h++) {
+      const int b[4] = {(h >> 3) & 1, (h >> 2) & 1, (h >> 1) & 1, h & 1};
+      double w = 1.0;
+      float wkf[4];
+      long idx = 0;
+      for (int k = 0; k < 4; k++) {
+        w *= fr[k] + b[k] - 2.0 * b[k] * fr[k];   // the FP64 path's weight, bit for bit
+        wkf[k] = b[k] ? 1.0f - frf[k] : frf[k];
+        const int c = (t.n[k] <= 1) ? 0 : ind[k] + b[k];
+        idx = idx * t.n[k] + c;
+      }
+      const double* node = t.f + (size_t)idx * 17;
+      for (int i = 1; i < 6; i++) o[i] += w * node[i];
+      const float* nd = t.fd + (size_t)idx * 8;
+      for (int j = 0; j < 4; j++) {
+        float dw = b[j] ? -dfrf[j] : dfrf[j];
+        for (int k = 0; k < 4; k++)
+          if (k != j) dw *= wkf[k];
+        for (int f = 0; f < 5; f++) jf[f][j] += dw * nd[f];
+      }
+    }
+    for (int f = 0; f < 5; f++) for (int j = 0; j < 4; j++) jac[f][j] = jf[f][j];
+    return;
+  }
+  // with a Jacobian (the Newton iterations) only the densities o[1..5] are
+  // formed: the other fields are not read there
+  if (jac) for (int i = 1; i < 6; i++) o[i] = 0.0;
+  else for (int i = 0; i < 17; i++) o[i] = 0.0;
   if (jac)
     for (int f = 0; f < 5; f++) for (int j = 0; j < 4; j++) jac[f][j] = 0.0;
   for (int h = 0; h < 16; h++) {
@@ -134,14 +173,17 @@ __host__ __device__ inline void table_thermo(const TableView& t, const double* x
       idx = idx * t.n[k] + c;
     }
     const double* node = t.f + (size_t)idx * 17;
-    if (jac)
+    if (jac) {
       for (int j = 0; j < 4; j++) {
         double dw = (1.0 - 2.0 * b[j]) * dfr[j];
         for (int k = 0; k < 4; k++)
           if (k != j) dw *= wk[k];
         for (int f = 0; f < 5; f++) jac[f][j] += dw * node[1 + f];
       }
-    for (int i = 0; i < 17; i++) o[i] += w * node[i];
+      for (int i = 1; i < 6; i++) o[i] += w * node[i];
+    } else {
+      for (int i = 0; i < 17; i++) o[i] += w * node[i];
+    }
   }
 }
 
@@ -171,7 +213,7 @@ __host__ __device__ inline void dens_jac(const EosDev& e, int model, int entropy
   double o[17];
   if (model == M_TABLE) {
     double jac[5][4];
-    table_thermo(e.tab, x, o, jac);
+    table_thermo(e.tab, x, o, jac, e.jac32 != 0);
     f[0] = entropy ? o[1] : o[5];
     f[1] = o[2];
     f[2] = o[4];

@@ -754,6 +754,16 @@ __global__ void k_freeze_advance(Clock* c) {
   if (c->frzc < 2) c->frzc++;
 }
 
+// FP32 copy of the table densities (fields 1..5 of 17) at 8 floats a node.
+__global__ void k_table_f32(const double* f, float* fd, int64_t nodes) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nodes) return;
+  const double* node = f + q * 17;
+  float4* o = reinterpret_cast<float4*>(fd + q * 8);
+  o[0] = make_float4((float)node[1], (float)node[2], (float)node[3], (float)node[4]);
+  o[1] = make_float4((float)node[5], 0.0f, 0.0f, 0.0f);
+}
+
 __global__ void __launch_bounds__(1024) k_count_frozen(Ptrs p, int32_t* out) {
   __shared__ int32_t red[32];
   int32_t c = 0;
@@ -848,6 +858,11 @@ void launch_freeze(const RunConst& rc, const Ptrs& p, cudaStream_t s) {
 }
 
 void launch_count_frozen(const Ptrs& p, int32_t* out, cudaStream_t s) { k_count_frozen<<<1, 1024, 0, s>>>(p, out); }
+
+void launch_table_f32(const double* f, float* fd, int64_t nodes, cudaStream_t s) {
+  if (nodes <= 0) return;
+  k_table_f32<<<(unsigned)((nodes + 255) / 256), 256, 0, s>>>(f, fd, nodes);
+}
 
 void launch_totals(const RunConst& rc, const Ptrs& p, int nblocks, cudaStream_t s) {
   k_totals<<<nblocks, 256, 0, s>>>(rc, p);

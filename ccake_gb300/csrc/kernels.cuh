@@ -55,14 +55,19 @@ struct Ptrs {
   float* recBf;          // RBF * n
 };
 
-// Mixed-precision neighbour records, float4-aligned per particle. A position
-// x is carried as the float pair (hi, lo), hi = fl(x), lo = fl(x - hi), so a
-// difference of nearby positions keeps full FP32 precision.
-//   A: xhi0 xhi1 xhi2 m | xlo0 xlo1 xlo2 0 | m*ext_s m*ext_B m*ext_S m*ext_Q
+// Mixed-precision neighbour records. A position x is carried as the float
+// pair (hi, lo), hi = fl(x), lo = fl(x - hi), so a difference of nearby
+// positions keeps full FP32 precision. Record B (96 bytes) and the 3-D record
+// A (64 bytes, padded) are 32-byte aligned, so that each pair of float4 is
+// one 32-byte gather; the 2-D record A keeps 48 bytes (three 16-byte
+// gathers), which holds more neighbours in L1 than the padded form.
+//   A: xhi0 xhi1 xhi2 m | xlo0 xlo1 xlo2 0 | m*ext_s m*ext_B m*ext_S m*ext_Q [| 0 0 0 0 in 3-D]
 //   B: xhi0 xhi1 xhi2 m | xlo0 xlo1 xlo2 p/sl^2 | e Pi/sl^2 v0 v1 |
 //      v2 pi01/sl^2 pi02/sl^2 pi03/sl^2 | pi11 pi12 pi13 pi22 | pi23 pi33 0 0
 //      (the pi^{ij} entries divided by sl^2 as well)
-constexpr int RAF = 12;
+constexpr int RAF = 16;   // slab floats a particle (the 3-D stride)
+template <int D>
+constexpr int raf_stride() { return D == 3 ? 16 : 12; }
 constexpr int RBF = 24;
 
 // Pass A modes
@@ -95,6 +100,7 @@ void launch_eos_thermo(const EosDev& eos, int chain_index, int64_t n, const doub
 // kEosFirstIters, then the full inversion of the rows it left (same results
 // as one pass).
 constexpr int kEosFirstIters = 8;
+void launch_table_f32(const double* f, float* fd, int64_t nodes, cudaStream_t s);
 void launch_eos_batch(const EosDev& eos, int entropy, int seed_mode, int64_t n, const double* in4, double* tbqs,
                       double* th16, int32_t* status, int32_t* iters, int32_t* scratch, cudaStream_t s);
 

@@ -36,16 +36,33 @@ __global__ void k_pack_mixed(Ptrs p) {
 }
 
 // Pass A, mixed form: smoothing sums (sigma_lab and the four extensive
-// densities, src/sph_workstation.cpp:495-578 of the reference), the
-// per-substep neighbour list with FP32 grad-W factors.
+// densities, src/sph_workstation.cpp:495-578 of the reference) over the
+// candidate list, and the per-substep neighbour list with FP32 grad-W
+// factors for pass B.
+//
+// The list is k-major (entry k of particle i at k * n + i) so that pass B
+// reads it coalesced. The lanes of a warp reach entry k at different
+// candidates; in 3-D (~450 entries a particle) the entries are staged in a
+// per-warp ring of kRing rows in shared memory and each row is stored as one
+// coalesced row once every lane still walking candidates has passed it
+// (checked every kCheck candidates). A lane that would run more than kRing
+// rows ahead of the slowest forces out the oldest rows; entries of a lane
+// that is behind an already written row go straight to memory. In 2-D (~48
+// entries) the entries are stored directly.
+constexpr int kRing = 16, kCheck = 4;
+
 template <int D>
 __global__ void __launch_bounds__(kBlock) k_passA_mixed(RunConst rc, Ptrs p) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= p.n) return;
+  constexpr bool kStage = (D == 3);
+  // every lane of a warp takes part in the warp-wide staging below: lanes
+  // past the end stay in with no candidates and write nothing
   const int n = p.n;
+  const int i_ = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool live = i_ < n;
+  const int i = live ? i_ : n - 1;
   const double t = p.clock->t;
   const float4* ra = reinterpret_cast<const float4*>(p.recAf);
-  constexpr int SA = RAF / 4;
+  constexpr int SA = raf_stride<D>() / 4;
   const float4 ah = ra[(size_t)i * SA], al = ra[(size_t)i * SA + 1], ae = ra[(size_t)i * SA + 2];
   const float k0 = (float)rc.k0;
   KSum sl, s0, s1, s2, s3;
@@ -58,41 +75,104 @@ __global__ void __launch_bounds__(kBlock) k_passA_mixed(RunConst rc, Ptrs p) {
   const float wn = (float)rc.wn, wn2 = (float)rc.wn2, gn = (float)rc.gn, gn2 = (float)rc.gn2;
   const int K = p.K;
   float* nf = reinterpret_cast<float*>(p.nbr_f);
+  // a lane reads and writes only its own column of the ring (dynamically
+  // indexed per-lane storage); the warp agrees on base by reductions
+  __shared__ int ring_b[kBlock / 32][kRing][32];
+  __shared__ float ring_f[kBlock / 32][kRing][32];
+  const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
+  // stores row r of the ring for every lane that has an entry there
+  int nn = 0, base = 0;
+  auto flush_row = [&](int r) {
+    if (nn > r && r < K) {
+      p.nbr_idx[(size_t)r * n + i] = ring_b[wq][r % kRing][lane];
+      nf[(size_t)r * n + i] = ring_f[wq][r % kRing][lane];
+    }
+  };
   // the candidate list of the last build holds every b that can be within
   // 2h now (most are); its entries are streamed two iterations ahead of use
-  const int nc = min(p.cand_cnt[i], p.Kc);
-  int nn = 0;
+  const int nc = live ? min(p.cand_cnt[i], p.Kc) : 0;
+  const int wnc = kStage ? __reduce_max_sync(0xffffffffu, nc) : nc;
   int bq0 = 0, bq1 = 0;
   if (nc > 0) bq0 = p.cand_idx[i];
   if (nc > 1) bq1 = p.cand_idx[(size_t)n + i];
-  for (int kk = 0; kk < nc; kk++) {
+  for (int kk = 0; kk < wnc; kk++) {
+    const bool act = kk < nc;
+    if (kStage && (kk % kCheck) == 0) {
+      // rows every lane still walking has passed are complete
+      const int lo = __reduce_min_sync(0xffffffffu, act ? nn : 0x7fffffff);
+      while (base < lo && lo != 0x7fffffff) {
+        flush_row(base);
+        base++;
+      }
+      // room for kCheck more rows a lane: the ring holds base .. base + kRing - 1
+      const int hi = __reduce_max_sync(0xffffffffu, nn);
+      while (hi + kCheck > base + kRing) {
+        flush_row(base);
+        base++;
+      }
+    }
     const int b = bq0;
     bq0 = bq1;
     if (kk + 2 < nc) bq1 = p.cand_idx[(size_t)(kk + 2) * n + i];
-    const float4 bh = __ldg(&ra[(size_t)b * SA]), bl = __ldg(&ra[(size_t)b * SA + 1]);
-    const float dx = (ah.x - bh.x) + (al.x - bl.x);
-    const float dy = (ah.y - bh.y) + (al.y - bl.y);
-    const float dz = (D == 3) ? (ah.z - bh.z) + (al.z - bl.z) : 0.0f;
-    const float d2 = dx * dx + dy * dy + dz * dz;
-    if (!(d2 <= cut2)) continue;
-    const float4 be = __ldg(&ra[(size_t)b * SA + 2]);
-    // W (src/kernel.cpp:34-48) and grad_a W = fg (r_a - r_b) (:95-118)
-    const float rs = d2 > 0.0f ? rsqrtf(d2) : 0.0f;
-    const float q = d2 * rs * ih;
-    const float z = fmaxf(2.0f - q, 0.0f), qq = q * q;
-    const float W = q < 1.0f ? wn * (1.0f - 1.5f * qq + 0.75f * q * qq) : wn2 * z * z * z;
-    const float fg = q < 1.0f ? gn2 * (1.5f * q - 2.0f) * ih : gn * rs * z * z;
-    if (nn < K) {
-      p.nbr_idx[(size_t)nn * n + i] = b;
-      nf[(size_t)nn * n + i] = fg;
+    bool in = false;
+    float fg = 0.0f;
+    if (act) {
+      float4 bh, bl;
+      if (D == 3) {
+        ldg256(&ra[(size_t)b * SA], bh, bl);
+      } else {
+        bh = __ldg(&ra[(size_t)b * SA]);
+        bl = __ldg(&ra[(size_t)b * SA + 1]);
+      }
+      const float dx = (ah.x - bh.x) + (al.x - bl.x);
+      const float dy = (ah.y - bh.y) + (al.y - bl.y);
+      const float dz = (D == 3) ? (ah.z - bh.z) + (al.z - bl.z) : 0.0f;
+      const float d2 = pair_d2f(dx, dy, dz);
+      if (d2 <= cut2) {
+        in = true;
+        const float4 be = __ldg(&ra[(size_t)b * SA + 2]);
+        // W (src/kernel.cpp:34-48) and grad_a W = fg (r_a - r_b) (:95-118)
+        const float rs = d2 > 0.0f ? rsqrtf(d2) : 0.0f;
+        const float q = d2 * rs * ih;
+        const float z = fmaxf(2.0f - q, 0.0f), qq = q * q;
+        const float W = q < 1.0f ? wn * (1.0f - 1.5f * qq + 0.75f * q * qq) : wn2 * z * z * z;
+        fg = pair_fgf(d2, rs, ih, gn, gn2);
+        sl.add(bh.w * W);
+        s0.add(be.x * W);
+        s1.add(be.y * W);
+        s2.add(be.z * W);
+        s3.add(be.w * W);
+      }
     }
-    nn++;
-    sl.add(bh.w * W);
-    s0.add(be.x * W);
-    s1.add(be.y * W);
-    s2.add(be.z * W);
-    s3.add(be.w * W);
+    if constexpr (kStage) {
+      if (in) {
+        if (nn < base) {
+          if (nn < K) {
+            p.nbr_idx[(size_t)nn * n + i] = b;
+            nf[(size_t)nn * n + i] = fg;
+          }
+        } else {
+          ring_b[wq][nn % kRing][lane] = b;
+          ring_f[wq][nn % kRing][lane] = fg;
+        }
+        nn++;
+      }
+    } else if (in) {
+      if (nn < K) {
+        p.nbr_idx[(size_t)nn * n + i] = b;
+        nf[(size_t)nn * n + i] = fg;
+      }
+      nn++;
+    }
   }
+  if constexpr (kStage) {
+    const int hi = __reduce_max_sync(0xffffffffu, nn);
+    while (base < hi) {
+      flush_row(base);
+      base++;
+    }
+  }
+  if (!live) return;
   if (nn > K) atomicAdd(&p.err[E_NBR_OVERFLOW], 1);
   const double u3[3] = {p.y[Y_U0 * n + i], p.y[Y_U1 * n + i], D == 3 ? p.y[Y_U2 * n + i] : 0.0};
   const double g = gamma_milne<D>(u3, t * t);
@@ -156,11 +236,25 @@ __global__ void __launch_bounds__(kBlock) k_passB_mixed(RunConst rc, Ptrs p) {
   // the list entries are streamed from memory two iterations ahead of use
   int bq0 = 0, bq1 = 0;
   float fq0 = 0.0f, fq1 = 0.0f;
-  if (cnt > 0) { bq0 = p.nbr_idx[i]; fq0 = nf[i]; }
+  // and, in 2-D, the first 32 bytes of the next neighbour's record one
+  // ahead (in 3-D the extra registers would cost a block an SM)
+  constexpr bool kAhead = (D == 2);
+  float4 N0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), N1 = N0;
+  if (cnt > 0) {
+    bq0 = p.nbr_idx[i];
+    fq0 = nf[i];
+    if (kAhead) ldg256(rbf + (size_t)bq0 * SB, N0, N1);
+  }
   if (cnt > 1) { bq1 = p.nbr_idx[(size_t)n + i]; fq1 = nf[(size_t)n + i]; }
   for (int kk = 0; kk < cnt; kk++) {
     const int b = bq0;
     const float fg = fq0;
+    float4 B0 = N0, B1 = N1;
+    if (kAhead) {
+      if (kk + 1 < cnt) ldg256(rbf + (size_t)bq1 * SB, N0, N1);
+    } else {
+      ldg256(rbf + (size_t)b * SB, B0, B1);
+    }
     bq0 = bq1;
     fq0 = fq1;
     if (kk + 2 < cnt) {
@@ -168,7 +262,9 @@ __global__ void __launch_bounds__(kBlock) k_passB_mixed(RunConst rc, Ptrs p) {
       fq1 = nf[(size_t)(kk + 2) * n + i];
     }
     const float4* rb = rbf + (size_t)b * SB;
-    const float4 B0 = __ldg(rb), B1 = __ldg(rb + 1), B2 = __ldg(rb + 2);
+    float4 B2, B3 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (D == 3 || shear) ldg256(rb + 2, B2, B3);
+    else B2 = __ldg(rb + 2);
     const float d[3] = {(A0.x - B0.x) + (A1.x - B1.x), (A0.y - B0.y) + (A1.y - B1.y),
                         (D == 3) ? (A0.z - B0.z) + (A1.z - B1.z) : 0.0f};
     const float mf = B0.w * fg;
@@ -176,8 +272,6 @@ __global__ void __launch_bounds__(kBlock) k_passB_mixed(RunConst rc, Ptrs p) {
 #pragma unroll
     for (int k = 0; k < D; k++) gm[k] = mf * d[k];
     float vb[3] = {B2.z, B2.w, 0.0f};
-    float4 B3 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    if (D == 3 || shear) B3 = __ldg(rb + 3);
     if (D == 3) vb[2] = B3.x;
 #pragma unroll
     for (int k = 0; k < D; k++) {
@@ -189,8 +283,9 @@ __global__ void __launch_bounds__(kBlock) k_passB_mixed(RunConst rc, Ptrs p) {
       for (int l = 0; l < D; l++) SV[k][l].add(vb[l] * gm[k]);
     }
     if (shear) {
-      const float4 B4 = __ldg(rb + 4);
-      const float4 B5 = (D == 3) ? __ldg(rb + 5) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      float4 B4, B5 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      if (D == 3) ldg256(rb + 4, B4, B5);
+      else B4 = __ldg(rb + 4);
       const float p0[3] = {B3.y, B3.z, B3.w};
       // pi^{ij}/sl^2 packed (11 12 13 22 23 33)
       const float pij[6] = {B4.x, B4.y, B4.z, B4.w, B5.x, B5.y};
@@ -292,12 +387,15 @@ void launch_pack_mixed(const RunConst& rc, const Ptrs& p, cudaStream_t s) {
 
 void launch_passA_mixed(const RunConst& rc, const EosDev& eos, const Ptrs& p, cudaStream_t s) {
   const int nb = (p.n + kBlock - 1) / kBlock;
+  // table Newton Jacobians in FP32 (the residual and its tolerance stay FP64)
+  EosDev em = eos;
+  em.jac32 = 1;
   if (rc.cfg.dim == 3) {
     k_passA_mixed<3><<<nb, kBlock, 0, s>>>(rc, p);
-    k_thermo_mixed<3><<<nb, kBlock, 0, s>>>(rc, eos, p);
+    k_thermo_mixed<3><<<nb, kBlock, 0, s>>>(rc, em, p);
   } else {
     k_passA_mixed<2><<<nb, kBlock, 0, s>>>(rc, p);
-    k_thermo_mixed<2><<<nb, kBlock, 0, s>>>(rc, eos, p);
+    k_thermo_mixed<2><<<nb, kBlock, 0, s>>>(rc, em, p);
   }
 }
 

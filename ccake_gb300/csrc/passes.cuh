@@ -60,6 +60,30 @@ struct KSum {
   __device__ __forceinline__ double value64() const { return (double)s - (double)c; }
 };
 
+// Squared FP32 pair distance and the radial factor fg of grad_a W =
+// fg (r_a - r_b) (src/kernel.cpp:95-118 of the reference), every rounding
+// explicit (no contraction), so that the mixed pass A's predicate and pass
+// B's recomputation from the same float positions agree bit for bit.
+__device__ __forceinline__ float pair_d2f(float dx, float dy, float dz) {
+  return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+}
+
+__device__ __forceinline__ float pair_fgf(float d2, float rs, float ih, float gn, float gn2) {
+  const float q = __fmul_rn(__fmul_rn(d2, rs), ih);
+  const float z = fmaxf(__fsub_rn(2.0f, q), 0.0f);
+  return q < 1.0f ? __fmul_rn(__fmul_rn(gn2, __fmaf_rn(1.5f, q, -2.0f)), ih)
+                  : __fmul_rn(__fmul_rn(__fmul_rn(gn, rs), z), z);
+}
+
+// 32-byte load through the non-coherent path (ld.global.nc.v8.f32, sm_100
+// and later): one gather instruction for two float4 of a neighbour record.
+// p must be 32-byte aligned.
+__device__ __forceinline__ void ldg256(const float4* p, float4& a, float4& b) {
+  asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+      : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+      : "l"(p));
+}
+
 // x = hi + lo with hi = fl32(x): the pair carries x to ~2^-48 relative.
 __device__ __forceinline__ void split2(double x, float& hi, float& lo) {
   hi = (float)x;
@@ -83,10 +107,11 @@ __device__ __forceinline__ void write_recAf(const Ptrs& p, int i, const double* 
   float hi[3], lo[3];
 #pragma unroll
   for (int k = 0; k < 3; k++) split2(k < D ? x[k] : 0.0, hi[k], lo[k]);
-  float4* ra = reinterpret_cast<float4*>(p.recAf) + (size_t)i * (RAF / 4);
+  float4* ra = reinterpret_cast<float4*>(p.recAf) + (size_t)i * (raf_stride<D>() / 4);
   ra[0] = make_float4(hi[0], hi[1], hi[2], (float)m);
   ra[1] = make_float4(lo[0], lo[1], lo[2], 0.0f);
   ra[2] = make_float4((float)(m * ext[0]), (float)(m * ext[1]), (float)(m * ext[2]), (float)(m * ext[3]));
+  if (D == 3) ra[3] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   p.posf[i] = make_float4(hi[0], hi[1], hi[2], 0.0f);
 }
 
