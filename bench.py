@@ -519,12 +519,14 @@ def run_hotspots3d(args):
         torch.cuda.synchronize()
         ms = g.step_timed(steps)
         out[form] = {"ms": ms, "state": {f: g.get(f) for f in ("e", "rhoB", "rhoQ", "T", "u0", "u2")},
-                     "bytes": g.device_bytes(), "phase_ms": [float(v) for v in g.profile_phases(2)]}
+                     "bytes": g.device_bytes(), "phase_ms": [float(v) for v in g.profile_phases(2)],
+                     "eos_iters_mean": float(np.mean(g.get_int("eos_iters")))}
         g.close()
     if len(out) < 2:
         f0 = next(iter(out))
         print(json.dumps({"partial": True, "workload": "hotspots3d", "form": f0, "particles": p.n,
-                          "ms_per_step": out[f0]["ms"] / steps, "phase_ms": out[f0]["phase_ms"]}))
+                          "ms_per_step": out[f0]["ms"] / steps, "phase_ms": out[f0]["phase_ms"],
+                          "eos_iters_mean": out[f0]["eos_iters_mean"]}))
         return
     err = {}
     for f in ("e", "rhoB", "rhoQ", "T"):
@@ -539,8 +541,8 @@ def run_hotspots3d(args):
             "form": "mixed (FP32 Kahan sums and EoM, FP64 EoS Newton, state and RK2)",
             "ms_per_step": out["mixed"]["ms"] / steps, "steps": steps, "warmup": args.warmup, "particles": npart,
             "fp64": {"value": npart * steps / (out["fp64"]["ms"] * 1e-3), "ms_per_step": out["fp64"]["ms"] / steps,
-                     "phase_ms": out["fp64"]["phase_ms"]},
-            "mixed_phase_ms": out["mixed"]["phase_ms"],
+                     "phase_ms": out["fp64"]["phase_ms"], "eos_iters_mean": out["fp64"]["eos_iters_mean"]},
+            "mixed_phase_ms": out["mixed"]["phase_ms"], "mixed_eos_iters_mean": out["mixed"]["eos_iters_mean"],
             "max_rel_err_mixed_vs_fp64": err, "device_bytes": out["mixed"]["bytes"],
             "config": {"lattice": f"{args.h3d_nxy}x{args.h3d_nxy}x{args.h3d_neta}", "dx_fm": 0.1, "deta": 0.06, "h_fm": 0.2, "eta_over_s": 0.08,
                        "zeta_over_s_peak": 0.1, "zeta_peak_T_GeV": 0.16, "eos": "synthetic table 151x41^3",

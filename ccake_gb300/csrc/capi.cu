@@ -433,6 +433,14 @@ ccake_status_t ccake_ctx_create(const ccake_config* cfg, ccake_ctx** out) {
   rc.gn = kgrad(D) / std::pow(h, D + 1);
   rc.gn2 = kgrad2(D) / std::pow(h, D + 1);
   rc.k0 = rc.wn;   // W(0)
+  rc.fcut2 = (float)rc.cut2;
+  rc.fcutc2 = (float)rc.cutc2;
+  rc.finv_h = (float)rc.inv_h;
+  rc.fwn = (float)rc.wn;
+  rc.fwn2 = (float)rc.wn2;
+  rc.fgn = (float)rc.gn;
+  rc.fgn2 = (float)rc.gn2;
+  rc.fk0 = (float)rc.k0;
   EosDev& e = ctx->eos;
   e.kind = cfg->eos_kind;
   e.thermo_mode = cfg->thermo_mode;

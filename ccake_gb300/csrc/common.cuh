@@ -71,6 +71,10 @@ struct RunConst {
   double gn, gn2;        // grad W normalisations kgrad/h^(D+1), kgrad2/h^(D+1)
   double k0;             // W(0)
   double efreeze;        // e(T_FO, 0, 0, 0)
+  // FP32 copies for the FP32 pair loops, rounded once on the host (a
+  // conversion in a kernel is an FP64-pipe instruction, and the compiler may
+  // repeat it inside a loop rather than hold its result in a register)
+  float fcut2, fcutc2, finv_h, fwn, fwn2, fgn, fgn2, fk0;
 };
 
 // Device-side clock: tau at the start of the RK2 step and the current tau.

@@ -679,6 +679,32 @@ __host__ __device__ inline double schur_term(const Chi& x, int which) {
 // o: the model thermodynamics at x (model_thermo of the chain's model k).
 // fp32_derivs: the conformal-diagonal enthalpy derivatives dw/ds, dw/drho in
 // FP32 arithmetic (they feed only FP32 equations of motion in the mixed form).
+// G = H^-1 over the rows keep[0..m) (Gauss-Jordan, partial pivoting) in the
+// arithmetic R; zero elsewhere.
+template <class R>
+__host__ __device__ inline void hessian_inverse(const double H[4][4], const int* keep, int m, double G[4][4]) {
+  R A[4][8];
+  for (int i = 0; i < 4; i++) for (int j = 0; j < 8; j++) A[i][j] = R(0);
+  for (int i = 0; i < m; i++) {
+    for (int j = 0; j < m; j++) A[i][j] = R(H[keep[i]][keep[j]]);
+    A[i][m + i] = R(1);
+  }
+  for (int col = 0; col < m; col++) {
+    int p = col;
+    for (int r = col + 1; r < m; r++) if (fabs(A[r][col]) > fabs(A[p][col])) p = r;
+    if (p != col) for (int j = 0; j < 2 * m; j++) { R t = A[col][j]; A[col][j] = A[p][j]; A[p][j] = t; }
+    const R ipiv = R(1) / A[col][col];
+    for (int j = 0; j < 2 * m; j++) A[col][j] *= ipiv;
+    for (int r = 0; r < m; r++) {
+      if (r == col || A[r][col] == R(0)) continue;
+      const R f = A[r][col];
+      for (int j = 0; j < 2 * m; j++) A[r][j] -= f * A[col][j];
+    }
+  }
+  for (int i = 0; i < 4; i++) for (int j = 0; j < 4; j++) G[i][j] = 0.0;
+  for (int i = 0; i < m; i++) for (int j = 0; j < m; j++) G[keep[i]][keep[j]] = double(A[i][m + j]);
+}
+
 __host__ __device__ inline void set_thermo_o(const EosDev& e, int k, const double* x, const double* o, double* th,
                                              bool fp32_derivs = false) {
   const int model = chain_model(e.kind, k);
@@ -717,27 +743,9 @@ __host__ __device__ inline void set_thermo_o(const EosDev& e, int k, const doubl
       for (int j = 0; j < 4; j++) zero = zero && (H[i][j] == 0.0);
       if (!zero) keep[m++] = i;
     }
-    double A[4][8];
-    for (int i = 0; i < 4; i++) for (int j = 0; j < 8; j++) A[i][j] = 0.0;
-    for (int i = 0; i < m; i++) {
-      for (int j = 0; j < m; j++) A[i][j] = H[keep[i]][keep[j]];
-      A[i][m + i] = 1.0;
-    }
-    for (int col = 0; col < m; col++) {
-      int p = col;
-      for (int r = col + 1; r < m; r++) if (fabs(A[r][col]) > fabs(A[p][col])) p = r;
-      if (p != col) for (int j = 0; j < 2 * m; j++) { double t = A[col][j]; A[col][j] = A[p][j]; A[p][j] = t; }
-      const double ipiv = 1.0 / A[col][col];
-      for (int j = 0; j < 2 * m; j++) A[col][j] *= ipiv;
-      for (int r = 0; r < m; r++) {
-        if (r == col || A[r][col] == 0.0) continue;
-        const double f = A[r][col];
-        for (int j = 0; j < 2 * m; j++) A[r][j] -= f * A[col][j];
-      }
-    }
     double G[4][4];
-    for (int i = 0; i < 4; i++) for (int j = 0; j < 4; j++) G[i][j] = 0.0;
-    for (int i = 0; i < m; i++) for (int j = 0; j < m; j++) G[keep[i]][keep[j]] = A[i][m + j];
+    if (fp32_derivs) hessian_inverse<float>(H, keep, m, G);
+    else hessian_inverse<double>(H, keep, m, G);
     for (int a = 0; a < 4; a++) {
       double acc = mu[a];
       if (a == 0 || act[a]) {

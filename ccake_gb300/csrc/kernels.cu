@@ -204,7 +204,7 @@ __global__ void __launch_bounds__(kBlock) k_candidates(RunConst rc, Ptrs p) {
   const int n = p.n;
   const double xa[3] = {p.y[Y_X0 * n + i], p.y[Y_X1 * n + i], D == 3 ? p.y[Y_X2 * n + i] : 0.0};
   const float4 pa = p.posf[i];
-  const float cut2f = (float)rc.cutc2 * 1.000001f;
+  const float cut2f = rc.fcutc2 * 1.000001f;
   int rlo[D == 3 ? 9 : 3], rhi[D == 3 ? 9 : 3];
   const int nr = neighbour_ranges<D>(rc.grid, p.cell_start, xa, rlo, rhi);
   const int Kc = p.Kc;
@@ -268,7 +268,7 @@ __global__ void __launch_bounds__(kBlock) k_passA(RunConst rc, EosDev eos, Ptrs 
   __shared__ int32_t surv[kSurv][kBlock];
   const int tid = threadIdx.x;
   const float4 pa = p.posf[i];
-  const float cut2f = (float)rc.cut2 * 1.000001f;
+  const float cut2f = rc.fcut2 * 1.000001f;
   // the candidate list of the last build holds every b that can be within
   // 2h now
   const int nc = min(p.cand_cnt[i], p.Kc);

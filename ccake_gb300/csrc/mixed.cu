@@ -64,15 +64,15 @@ __global__ void __launch_bounds__(kBlock) k_passA_mixed(RunConst rc, Ptrs p) {
   const float4* ra = reinterpret_cast<const float4*>(p.recAf);
   constexpr int SA = raf_stride<D>() / 4;
   const float4 ah = ra[(size_t)i * SA], al = ra[(size_t)i * SA + 1], ae = ra[(size_t)i * SA + 2];
-  const float k0 = (float)rc.k0;
+  const float k0 = rc.fk0;
   KSum sl, s0, s1, s2, s3;
   sl.init(ah.w * k0);
   s0.init(ae.x * k0);
   s1.init(ae.y * k0);
   s2.init(ae.z * k0);
   s3.init(ae.w * k0);
-  const float cut2 = (float)rc.cut2, ih = (float)rc.inv_h;
-  const float wn = (float)rc.wn, wn2 = (float)rc.wn2, gn = (float)rc.gn, gn2 = (float)rc.gn2;
+  const float cut2 = rc.fcut2, ih = rc.finv_h;
+  const float wn = rc.fwn, wn2 = rc.fwn2, gn = rc.fgn, gn2 = rc.fgn2;
   const int K = p.K;
   float* nf = reinterpret_cast<float*>(p.nbr_f);
   // a lane reads and writes only its own column of the ring (dynamically
@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(kBlock) k_passA_mixed(RunConst rc, Ptrs p) {
         in = true;
         const float4 be = __ldg(&ra[(size_t)b * SA + 2]);
         // W (src/kernel.cpp:34-48) and grad_a W = fg (r_a - r_b) (:95-118)
-        const float rs = d2 > 0.0f ? rsqrtf(d2) : 0.0f;
+        const float rs = d2 > 0.0f ? rsqrt_hw(d2) : 0.0f;
         const float q = d2 * rs * ih;
         const float z = fmaxf(2.0f - q, 0.0f), qq = q * q;
         const float W = q < 1.0f ? wn * (1.0f - 1.5f * qq + 0.75f * q * qq) : wn2 * z * z * z;

@@ -60,6 +60,16 @@ struct KSum {
   __device__ __forceinline__ double value64() const { return (double)s - (double)c; }
 };
 
+// 1/sqrt(x) for normal x > 0 by the hardware approximation
+// (rsqrt.approx.ftz.f32, about 2^-22.9 relative error): one special-function
+// instruction. Pair distances squared are never subnormal (and zero is
+// excluded by the callers).
+__device__ __forceinline__ float rsqrt_hw(float x) {
+  float r;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
 // Squared FP32 pair distance and the radial factor fg of grad_a W =
 // fg (r_a - r_b) (src/kernel.cpp:95-118 of the reference), every rounding
 // explicit (no contraction), so that the mixed pass A's predicate and pass
