@@ -891,7 +891,12 @@ ccake_status_t ccake_set_eos_table(ccake_ctx* ctx, const int32_t* n, const doubl
   launch_table_f32(ctx->d_table, ctx->d_table_f, (int64_t)nodes, ctx->stream);
   CK(cudaStreamSynchronize(ctx->stream));
   EosDev& e = ctx->eos;
-  for (int k = 0; k < 4; k++) { e.tab.n[k] = n[k]; e.tab.lo[k] = lo[k]; e.tab.d[k] = d[k]; }
+  for (int k = 0; k < 4; k++) {
+    e.tab.n[k] = n[k];
+    e.tab.lo[k] = lo[k];
+    e.tab.d[k] = d[k];
+    e.tab.id[k] = d[k] > 0.0 ? 1.0 / d[k] : 0.0;
+  }
   e.conf = make_scales(conf5[0], conf5[1], conf5[2], conf5[3], conf5[4]);
   e.cdiag = make_scales(cdiag5[0], cdiag5[1], cdiag5[2], cdiag5[3], cdiag5[4]);
   // e(T_FO, 0, 0, 0) from the table, evaluated on the host copy

@@ -28,6 +28,7 @@ struct TableView {
   int n[4] = {1, 1, 1, 1};
   double lo[4] = {0, 0, 0, 0};
   double d[4] = {0, 0, 0, 0};
+  double id[4] = {0, 0, 0, 0};   // 1 / d, rounded on the host (mixed-form lookup)
 };
 
 struct EosDev {
@@ -109,10 +110,9 @@ __host__ __device__ inline void confdiag_thermo(const Scales& k, const double* x
 // NaN outside.
 // jac (optional): derivatives of the interpolated s, rhoB, rhoS, rhoQ, e
 // (fields 1..5) with respect to (T, muB, muQ, muS), the exact Jacobian of the
-// multilinear interpolant inside the cell; with jf32 (and the FP32 node copy)
-// formed in FP32 from the FP32 densities, the values in o staying FP64.
+// multilinear interpolant inside the cell.
 __host__ __device__ inline void table_thermo(const TableView& t, const double* x, double* o,
-                                             double (*jac)[4] = nullptr, bool jf32 = false) {
+                                             double (*jac)[4] = nullptr) {
   int ind[4];
   double fr[4], dfr[4];
   for (int k = 0; k < 4; k++) {
@@ -125,36 +125,6 @@ __host__ __device__ inline void table_thermo(const TableView& t, const double* x
     ind[k] = (int)ip;
     if (ind[k] + 1 == t.n[k]) { fr[k] = 1.0 - fr[k]; dfr[k] = -dfr[k]; ind[k]--; }
     if (ind[k] < 0 || ind[k] >= t.n[k] || !(fabs(q) < 2e9)) { for (int i = 0; i < 17; i++) o[i] = NAN; return; }
-  }
-  if (jac && jf32 && t.fd) {
-    // Newton iterations of the mixed form: FP64 densities, FP32 Jacobian
-    float frf[4], dfrf[4], jf[5][4];
-    for (int k = 0; k < 4; k++) { frf[k] = (float)fr[k]; dfrf[k] = (float)dfr[k]; }
-    for (int f = 0; f < 5; f++) for (int j = 0; j < 4; j++) jf[f][j] = 0.0f;
-    for (int i = 1; i < 6; i++) o[i] = 0.0;
-    for (int h = 0; h < 16; h++) {
-      const int b[4] = {(h >> 3) & 1, (h >> 2) & 1, (h >> 1) & 1, h & 1};
-      double w = 1.0;
-      float wkf[4];
-      long idx = 0;
-      for (int k = 0; k < 4; k++) {
-        w *= fr[k] + b[k] - 2.0 * b[k] * fr[k];   // the FP64 path's weight, bit for bit
-        wkf[k] = b[k] ? 1.0f - frf[k] : frf[k];
-        const int c = (t.n[k] <= 1) ? 0 : ind[k] + b[k];
-        idx = idx * t.n[k] + c;
-      }
-      const double* node = t.f + (size_t)idx * 17;
-      for (int i = 1; i < 6; i++) o[i] += w * node[i];
-      const float* nd = t.fd + (size_t)idx * 8;
-      for (int j = 0; j < 4; j++) {
-        float dw = b[j] ? -dfrf[j] : dfrf[j];
-        for (int k = 0; k < 4; k++)
-          if (k != j) dw *= wkf[k];
-        for (int f = 0; f < 5; f++) jf[f][j] += dw * nd[f];
-      }
-    }
-    for (int f = 0; f < 5; f++) for (int j = 0; j < 4; j++) jac[f][j] = jf[f][j];
-    return;
   }
   // with a Jacobian (the Newton iterations) only the densities o[1..5] are
   // formed: the other fields are not read there
@@ -187,8 +157,78 @@ __host__ __device__ inline void table_thermo(const TableView& t, const double* x
   }
 }
 
+// The same multilinear lookup for the mixed form (EosDev::jac32): cell
+// fractions from the host-rounded inverse spacings (a multiplication instead
+// of a division), the 16 corner weights as products of two pair products,
+// and, with jac, the Jacobian of the densities in FP32 from the FP32 node
+// copy; the interpolated values stay FP64. It differs from table_thermo by
+// roundings of the weights only (relative 1e-16).
+__host__ __device__ inline void table_thermo_fast(const TableView& t, const double* x, double* o,
+                                                  float (*jac)[4] = nullptr) {
+  int ind[4];
+  double fr[4];
+  float dfrf[4];
+  for (int k = 0; k < 4; k++) {
+    if (isnan(x[k])) { for (int i = 0; i < 17; i++) o[i] = NAN; return; }
+    if (t.n[k] <= 1 || fabs(t.d[k]) < 1e-30) { ind[k] = 0; fr[k] = 1.0; dfrf[k] = 0.0f; continue; }
+    const double q = (x[k] - t.lo[k]) * t.id[k];
+    const double ip = trunc(q);
+    fr[k] = 1.0 - (q - ip);
+    dfrf[k] = -(float)t.id[k];
+    ind[k] = (int)ip;
+    if (ind[k] + 1 == t.n[k]) { fr[k] = 1.0 - fr[k]; dfrf[k] = -dfrf[k]; ind[k]--; }
+    if (ind[k] < 0 || ind[k] >= t.n[k] || !(fabs(q) < 2e9)) { for (int i = 0; i < 17; i++) o[i] = NAN; return; }
+  }
+  // corner h = (b0 b1 b2 b3): weight p01[b0 b1] * p23[b2 b3]; node offset
+  // from the lower corner by the row-major strides (0 on a single-node axis)
+  double w1[4];
+  for (int k = 0; k < 4; k++) w1[k] = 1.0 - fr[k];
+  const double p01[4] = {fr[0] * fr[1], fr[0] * w1[1], w1[0] * fr[1], w1[0] * w1[1]};
+  const double p23[4] = {fr[2] * fr[3], fr[2] * w1[3], w1[2] * fr[3], w1[2] * w1[3]};
+  long st[4], base = 0;
+  {
+    long s = 1;
+    for (int k = 3; k >= 0; k--) {
+      st[k] = (t.n[k] <= 1) ? 0 : s;
+      base += (long)ind[k] * s;
+      s *= t.n[k];
+    }
+  }
+  const int i0 = jac ? 1 : 0, i1 = jac ? 6 : 17;
+  for (int i = i0; i < i1; i++) o[i] = 0.0;
+  float frf[4], w1f[4];
+  if (jac) {
+    for (int k = 0; k < 4; k++) { frf[k] = (float)fr[k]; w1f[k] = 1.0f - frf[k]; }
+    for (int f = 0; f < 5; f++) for (int j = 0; j < 4; j++) jac[f][j] = 0.0f;
+  }
+  for (int h = 0; h < 16; h++) {
+    const int b[4] = {(h >> 3) & 1, (h >> 2) & 1, (h >> 1) & 1, h & 1};
+    const double w = p01[h >> 2] * p23[h & 3];
+    const long idx = base + b[0] * st[0] + b[1] * st[1] + b[2] * st[2] + b[3] * st[3];
+    const double* node = t.f + (size_t)idx * 17;
+    if (jac) {
+      for (int i = 1; i < 6; i++) o[i] += w * node[i];
+      const float* nd = t.fd + (size_t)idx * 8;
+      float wk[4];
+      for (int k = 0; k < 4; k++) wk[k] = b[k] ? w1f[k] : frf[k];
+      for (int j = 0; j < 4; j++) {
+        float dw = b[j] ? -dfrf[j] : dfrf[j];
+        for (int k = 0; k < 4; k++)
+          if (k != j) dw *= wk[k];
+        for (int f = 0; f < 5; f++) jac[f][j] += dw * nd[f];
+      }
+    } else {
+      for (int i = 0; i < 17; i++) o[i] += w * node[i];
+    }
+  }
+}
+
 __host__ __device__ inline void model_thermo(const EosDev& e, int model, const double* x4, double* o) {
-  if (model == M_TABLE) { table_thermo(e.tab, x4, o); return; }
+  if (model == M_TABLE) {
+    if (e.jac32 && e.tab.fd) table_thermo_fast(e.tab, x4, o);
+    else table_thermo(e.tab, x4, o);
+    return;
+  }
   const Scales k = model_scales(e, model);
   if (model == M_CONF) conformal_thermo(k, x4, o); else confdiag_thermo(k, x4, o);
 }
@@ -208,12 +248,28 @@ __host__ __device__ inline void model_box(const EosDev& e, int model, double* lo
 // function the solver zeroes; the reference's GSL hybrids solver
 // differentiates it by finite differences), not the interpolated
 // susceptibilities.
+// Jf (mixed form, table model): the Jacobian in FP32 instead of J.
 __host__ __device__ inline void dens_jac(const EosDev& e, int model, int entropy, const double* x, double* f,
-                                         double J[4][4]) {
+                                         double J[4][4], float (*Jf)[4] = nullptr) {
   double o[17];
+  if (model == M_TABLE && Jf) {
+    float jac[5][4];
+    table_thermo_fast(e.tab, x, o, jac);
+    f[0] = entropy ? o[1] : o[5];
+    f[1] = o[2];
+    f[2] = o[4];
+    f[3] = o[3];
+    for (int j = 0; j < 4; j++) {
+      Jf[0][j] = entropy ? jac[0][j] : jac[4][j];
+      Jf[1][j] = jac[1][j];
+      Jf[2][j] = jac[3][j];
+      Jf[3][j] = jac[2][j];
+    }
+    return;
+  }
   if (model == M_TABLE) {
     double jac[5][4];
-    table_thermo(e.tab, x, o, jac, e.jac32 != 0);
+    table_thermo(e.tab, x, o, jac);
     f[0] = entropy ? o[1] : o[5];
     f[1] = o[2];
     f[2] = o[4];
@@ -250,30 +306,31 @@ __host__ __device__ inline void dens_jac(const EosDev& e, int model, int entropy
 }
 
 // 4x4 solve, partial pivoting; a zero pivot leaves its unknown unchanged.
-__host__ __device__ inline void solve4(double A[4][4], double* b, double* x) {
+template <class R>
+__host__ __device__ inline void solve4(R A[4][4], R* b, R* x) {
   bool dead[4] = {false, false, false, false};
 #pragma unroll
   for (int k = 0; k < 4; k++) {
     int p = k;
-    double best = fabs(A[k][k]);
+    R best = fabs(A[k][k]);
     for (int i = k + 1; i < 4; i++)
       if (fabs(A[i][k]) > best) { best = fabs(A[i][k]); p = i; }
     if (p != k) {
-      for (int j = 0; j < 4; j++) { double tmp = A[k][j]; A[k][j] = A[p][j]; A[p][j] = tmp; }
-      double tb = b[k]; b[k] = b[p]; b[p] = tb;
+      for (int j = 0; j < 4; j++) { R tmp = A[k][j]; A[k][j] = A[p][j]; A[p][j] = tmp; }
+      R tb = b[k]; b[k] = b[p]; b[p] = tb;
     }
-    if (A[k][k] == 0.0) { dead[k] = true; continue; }
+    if (A[k][k] == R(0)) { dead[k] = true; continue; }
     for (int i = k + 1; i < 4; i++) {
-      if (A[i][k] == 0.0) continue;
-      const double m = A[i][k] / A[k][k];
+      if (A[i][k] == R(0)) continue;
+      const R m = A[i][k] / A[k][k];
       for (int j = k; j < 4; j++) A[i][j] -= m * A[k][j];
       b[i] -= m * b[k];
     }
   }
 #pragma unroll
   for (int k = 3; k >= 0; k--) {
-    if (dead[k]) { x[k] = 0.0; continue; }
-    double acc = b[k];
+    if (dead[k]) { x[k] = R(0); continue; }
+    R acc = b[k];
     for (int j = k + 1; j < 4; j++) acc -= A[k][j] * x[j];
     x[k] = acc / A[k][k];
   }
@@ -291,10 +348,14 @@ __host__ __device__ inline bool newton_attempt(const EosDev& e, int model, int e
   // so an undamped iteration costs one density/Jacobian evaluation.
   int extra = -1, nslow1 = 0, nslow2 = 0;
   double f[4], J[4][4], xgood[4] = {0.0, 0.0, 0.0, 0.0};
+  // mixed form, table model: FP32 Jacobian and Newton step (the residual,
+  // its tests and the iterate stay FP64)
+  const bool f32 = e.jac32 && model == M_TABLE && e.tab.fd;
+  float Jf[4][4];
   bool have = false;
   const bool diag = (model == M_CDIAG);
   for (int it = 0; it < max_it; it++) {
-    if (!have) dens_jac(e, model, entropy, x, f, J);
+    if (!have) dens_jac(e, model, entropy, x, f, J, f32 ? Jf : nullptr);
     have = false;
     double F[4], fres = 0.0;
     for (int i = 0; i < 4; i++) { F[i] = f[i] - tgt[i]; fres = fres > fabs(F[i]) ? fres : fabs(F[i]); }
@@ -305,6 +366,10 @@ __host__ __device__ inline bool newton_attempt(const EosDev& e, int model, int e
       // the conformal-diagonal Jacobian is diagonal: the 4x4 elimination
       // reduces to these divisions (a zero pivot leaves its unknown unchanged)
       for (int i = 0; i < 4; i++) dx[i] = (J[i][i] == 0.0) ? 0.0 : (-F[i]) / J[i][i];
+    } else if (f32) {
+      float rhs[4] = {(float)-F[0], (float)-F[1], (float)-F[2], (float)-F[3]}, dxf[4];
+      solve4(Jf, rhs, dxf);
+      for (int i = 0; i < 4; i++) dx[i] = dxf[i];
     } else {
       double rhs[4] = {-F[0], -F[1], -F[2], -F[3]};
       solve4(J, rhs, dx);
@@ -344,7 +409,7 @@ __host__ __device__ inline bool newton_attempt(const EosDev& e, int model, int e
     for (int h = 0; h < 7; h++) {
       for (int i = 0; i < 4; i++) y[i] = x[i] + lam * dx[i];
       if (y[0] > 0) {
-        dens_jac(e, model, entropy, y, f, J);
+        dens_jac(e, model, entropy, y, f, J, f32 ? Jf : nullptr);
         double gmax = 0.0;
         for (int i = 0; i < 4; i++) { const double r = fabs(f[i] - tgt[i]); gmax = gmax > r ? gmax : r; }
         if (gmax <= fres || h == 6) { have = true; break; }
