@@ -34,6 +34,16 @@ class ParticlesSoA(ctypes.Structure):
                                                     "uy", "ueta")]
 
 
+class IcOptions(ctypes.Structure):
+    _fields_ = [("input_as_entropy", _i32), ("input_initial_diffusion", _i32), ("baryon", _i32),
+                ("strange", _i32), ("electric", _i32), ("reserved", _i32), ("e_cutoff", _f64)]
+
+
+IC_COLUMNS = ("x", "y", "eta", "e", "rhoB", "rhoS", "rhoQ", "ux", "uy", "ueta", "bulk", "pixx", "pixy", "pixeta",
+              "piyy", "piyeta", "pietaeta", "qB0", "qB1", "qB2", "qB3", "qS0", "qS1", "qS2", "qS3", "qQ0", "qQ1",
+              "qQ2", "qQ3")
+
+
 class Totals(ctypes.Structure):
     _fields_ = [(k, _f64) for k in ("S", "B", "Sq", "Q", "E", "Ez")]
 
@@ -71,6 +81,14 @@ def lib():
         L.ccake_ctx_create.argtypes = [ctypes.POINTER(CcakeConfig), ctypes.POINTER(P)]
         L.ccake_ctx_destroy.argtypes = [P]
         L.ccake_load_particles.argtypes = [P, ctypes.POINTER(ParticlesSoA)]
+        L.ccake_hydro_numbers.argtypes = [P]
+        L.ccake_write_system_state.argtypes = [P, ctypes.c_char_p]
+        L.ccake_ic_read_ccake.argtypes = [ctypes.c_char_p, ctypes.POINTER(IcOptions), ctypes.POINTER(P)]
+        L.ccake_ic_info.argtypes = [P, ctypes.POINTER(_i64), _dp]
+        L.ccake_ic_column.argtypes = [P, ctypes.c_char_p, _dp]
+        L.ccake_ic_particles.argtypes = [P, ctypes.POINTER(ParticlesSoA)]
+        L.ccake_ic_free.argtypes = [P]
+        L.ccake_ic_free.restype = None
         for name in ("ccake_initialize", "ccake_build_neighbours", "ccake_smooth_fields", "ccake_update_thermo",
                      "ccake_update_viscosities", "ccake_smooth_gradients", "ccake_time_derivatives"):
             getattr(L, name).argtypes = [P]
@@ -164,6 +182,16 @@ class GpuHydro:
 
     def step(self, n=1):
         self._check(lib().ccake_step(self.h, int(n)), "step")
+
+    def hydro_numbers(self):
+        """theta, sigma^{ij}, Knudsen and inverse Reynolds numbers and the
+        transport coefficients of the last derivative evaluation, into the
+        fields of get() (ccake_hydro_numbers)."""
+        self._check(lib().ccake_hydro_numbers(self.h), "hydro_numbers")
+
+    def write_system_state(self, path):
+        """The reference's system_state_<n>.dat text output at path."""
+        self._check(lib().ccake_write_system_state(self.h, os.fsencode(path)), "write_system_state")
 
     def continue_evolution(self, max_tau):
         """The reference's stop rule: False once every particle froze out (particlization) or t > max_tau."""
@@ -390,3 +418,36 @@ def exported_symbols():
     hdr = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "ccake_gpu.h")
     src = open(hdr).read()
     return sorted(set(re.findall(r"\b(ccake_[a-z_0-9]+)\s*\(", src)))
+
+
+def read_ccake_ic(path, input_as_entropy=0, input_initial_diffusion=0, charges=(1, 1, 1), e_cutoff=0.0):
+    """Reads a "ccake" initial-condition file through the library
+    (ccake_ic_read_ccake, the rules of src/BSQHydro.cpp:206-425).
+
+    Returns (particles, columns, grid): an ics.Particles for GpuHydro.load,
+    every column by name (internal units: e, bulk and pi^{ij} divided by
+    hbar c), and (dx, dy, deta, xmin, ymin, etamin) from the header."""
+    from . import ics
+    L = lib()
+    opt = IcOptions(int(input_as_entropy), int(input_initial_diffusion), int(charges[0]), int(charges[1]),
+                    int(charges[2]), 0, float(e_cutoff))
+    h = ctypes.c_void_p()
+    code = L.ccake_ic_read_ccake(os.fsencode(path), ctypes.byref(opt), ctypes.byref(h))
+    if code != 0:
+        raise CcakeError(code, f"read_ccake_ic {path}: {L.ccake_status_string(code).decode()}")
+    try:
+        n = _i64()
+        grid = np.zeros(6)
+        L.ccake_ic_info(h, ctypes.byref(n), _d(grid))
+        cols = {}
+        for name in IC_COLUMNS:
+            a = np.zeros(n.value)
+            code = L.ccake_ic_column(h, name.encode(), _d(a))
+            if code != 0:
+                raise CcakeError(code, f"ccake_ic_column {name}")
+            cols[name] = a
+    finally:
+        L.ccake_ic_free(h)
+    p = ics.Particles(x=cols["x"], y=cols["y"], eta=cols["eta"], e=cols["e"], rhoB=cols["rhoB"],
+                      rhoS=cols["rhoS"], rhoQ=cols["rhoQ"], ux=cols["ux"], uy=cols["uy"], ueta=cols["ueta"])
+    return p, cols, tuple(float(v) for v in grid)

@@ -6,6 +6,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <fstream>
+#include <iomanip>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -38,6 +40,7 @@ struct ccake_ctx {
   double* d_table = nullptr;
   float* d_table_f = nullptr;   // FP32 densities of the nodes (mixed-form Newton Jacobians)
   int records_form = 0;   // which smoothing record matches the state: 0 FP64, 1 mixed
+  bool evaluated = false; // derivatives were evaluated since the initialisation
   // candidate list: skin (fm), validity and rebuild schedule
   double skin = 0.0;
   bool lists_valid = false;
@@ -272,6 +275,13 @@ FieldRef field_ref(ccake_ctx* ctx, const std::string& k) {
   if (k == "zeta_Pi") return FieldRef{p.derivs + D_ZETA * n, true};
   if (k == "tau_Pi") return FieldRef{p.derivs + D_TAUBULK * n, true};
   if (k == "in_s") return FieldRef{p.in_s, true};
+  if (k == "theta") return FieldRef{p.derivs + D_THETA * n, true};
+  for (int q = 0; q < 5; q++)
+    if (k == "sigma_tensor" + std::to_string(q)) return FieldRef{p.derivs + (D_SIG0 + q) * n, true};
+  if (k == "shear_knudsen") return FieldRef{p.derivs + D_KNS * n, true};
+  if (k == "bulk_knudsen") return FieldRef{p.derivs + D_KNB * n, true};
+  if (k == "inverse_reynolds_shear") return FieldRef{p.derivs + D_IRS * n, true};
+  if (k == "inverse_reynolds_bulk") return FieldRef{p.derivs + D_IRB * n, true};
   return FieldRef{nullptr, false};
 }
 
@@ -544,7 +554,7 @@ ccake_status_t ccake_initialize(ccake_ctx* ctx) {
   if (!ctx) return CCAKE_ERR_INVALID;
   if (!ctx->loaded) return fail(ctx, CCAKE_ERR_STATE, "load particles first");
   if (ctx->eos.kind == 2 && !ctx->d_table) return fail(ctx, CCAKE_ERR_STATE, "set the EoS table first");
-  Clock c{ctx->cfg.t0, ctx->cfg.t0, 0, 0};
+  Clock c{ctx->cfg.t0, ctx->cfg.t0, ctx->cfg.t0, 0, 0};
   CK(cudaMemcpyAsync(ctx->p.clock, &c, sizeof(Clock), cudaMemcpyHostToDevice, ctx->stream));
   ccake_status_t s = reset_errors(ctx);
   if (s) return s;
@@ -623,6 +633,7 @@ ccake_status_t ccake_step(ccake_ctx* ctx, int32_t n_steps) {
     if ((s = maybe_rebuild(ctx, true))) return s;
     CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
     ctx->steps_since_build++;
+    ctx->evaluated = true;
   }
   s = check_errors(ctx);
   Clock c;
@@ -644,6 +655,7 @@ ccake_status_t ccake_step_timed(ccake_ctx* ctx, int32_t n_steps, float* device_m
     if ((s = maybe_rebuild(ctx, true))) return s;
     CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
     ctx->steps_since_build++;
+    ctx->evaluated = true;
   }
   CK(cudaEventRecord(e1, ctx->stream));
   CK(cudaEventSynchronize(e1));
@@ -1212,6 +1224,74 @@ ccake_status_t ccake_eos_invert_batch_ex(ccake_ctx* ctx, int32_t entropy_mode, i
   cudaFree(d_st);
   if (d_it) cudaFree(d_it);
   CK(cudaGetLastError());
+  return CCAKE_OK;
+}
+
+ccake_status_t ccake_hydro_numbers(ccake_ctx* ctx) {
+  if (!ctx) return CCAKE_ERR_INVALID;
+  if (!ctx->initialized) return fail(ctx, CCAKE_ERR_STATE, "initialize first");
+  const int64_t n = ctx->n;
+  if (!ctx->evaluated) {
+    // before the first step no derivative evaluation happened: the
+    // reference's stored numbers are still zero
+    CK(cudaMemsetAsync(ctx->p.derivs + (size_t)D_THETA * n, 0, (size_t)(NDER - D_THETA) * n * sizeof(double),
+                       ctx->stream));
+    return check_errors(ctx);
+  }
+  // the step keeps its gradients in registers: the gradient sums of the last
+  // evaluation run again from its records and neighbour list (unchanged since),
+  // then the equations of motion from the stored inputs
+  const int mixed = ctx->records_form == 1 ? 1 : 0;
+  if (mixed) launch_gradients_mixed(ctx->rc, ctx->p, ctx->stream);
+  else launch_passB(ctx->rc, ctx->p, B_GRADS, 0.0, ctx->stream);
+  launch_diagnostics(ctx->rc, ctx->p, mixed, ctx->stream);
+  return check_errors(ctx);
+}
+
+ccake_status_t ccake_write_system_state(ccake_ctx* ctx, const char* path) {
+  if (!ctx || !path) return CCAKE_ERR_INVALID;
+  ccake_status_t st = ccake_hydro_numbers(ctx);
+  if (st) return st;
+  const int64_t n = ctx->n;
+  const int D = ctx->cfg.dim;
+  static const char* names[] = {"x", "y", "eta", "p", "T", "muB", "muS", "muQ", "e", "rhoB", "rhoS", "rhoQ", "s",
+                                "eta_pi", "zeta_Pi", "tau_Pi", "tau_pi", "theta", "inverse_reynolds_shear",
+                                "inverse_reynolds_bulk", "shear_knudsen", "bulk_knudsen", "shv00", "shv11", "shv22",
+                                "shv01", "shv02", "shv12", "shv13", "shv23", "shv33", "u0", "u1", "u2", "gamma"};
+  constexpr int NF = sizeof(names) / sizeof(names[0]);
+  std::vector<std::vector<double>> f(NF, std::vector<double>((size_t)n));
+  for (int q = 0; q < NF; q++)
+    if ((st = ccake_copy_out(ctx, names[q], f[q].data()))) return st;
+  std::vector<int32_t> frz((size_t)n), eid((size_t)n);
+  if ((st = ccake_copy_out_int(ctx, "freeze", frz.data()))) return st;
+  if ((st = ccake_copy_out_int(ctx, "eos_id", eid.data()))) return st;
+  std::ofstream out(path);
+  if (!out.is_open()) return fail(ctx, CCAKE_ERR_INVALID, std::string("cannot write ") + path);
+  // src/output.cpp:102-181 (print_system_state_to_txt), the same stream
+  // manipulators in the same places: the header time and the first row's
+  // time come out in the default format, every later number in scientific
+  // notation with 6 digits; positions and velocities padded to 3 components;
+  // energies and chemical potentials in GeV; no diffusion sector (its six
+  // numbers are 0) and no causality check (0).
+  const double t = ctx->t;
+  const double hc = kHbarcGeVfm;
+  out << t << "\n";
+  for (int64_t i = 0; i < n; i++) {
+    auto F = [&](int q) { return f[q][(size_t)i]; };
+    out << i << " " << t << " " << std::setprecision(6) << std::scientific;
+    for (int k = 0; k < 3; k++) out << (k < D ? F(k) : 0.0) << " ";
+    out << F(3) * hc << " " << F(4) * hc << " " << F(5) * hc << " " << F(6) * hc << " " << F(7) * hc << " "
+        << F(8) * hc << " ";
+    for (int q = 9; q <= 30; q++) out << F(q) << " ";
+    for (int k = 0; k < 3; k++) out << (k < D ? F(31 + k) : 0.0) << " ";
+    const int model = chain_model(ctx->eos.kind, eid[(size_t)i]);
+    const char* eos_name = model == M_TABLE ? "table" : model == M_CDIAG ? "conformal_diagonal" : "conformal";
+    out << F(34) << " " << frz[(size_t)i] << " " << eos_name << " " << 0 << " ";
+    for (int k = 0; k < 6; k++) out << 0.0 << " ";
+    out << "\n";
+  }
+  out << std::flush;
+  if (!out.good()) return fail(ctx, CCAKE_ERR_INVALID, std::string("write failed: ") + path);
   return CCAKE_OK;
 }
 

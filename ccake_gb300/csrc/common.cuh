@@ -41,7 +41,11 @@ enum GradSlot : int { G_P = 0, G_E = 3, G_B = 6, G_SH = 9, G_DS = 12, G_V = 15, 
 
 // Derivative slots written only when a caller asks for them.
 enum DerivSlot : int { D_DU0 = 0, D_DU1, D_DU2, D_DS, D_DBULK, D_DSHV0, D_DSHV1, D_DSHV2, D_DSHV3,
-                       D_DSHV4, D_DEZ, D_ETA, D_TAUPI, D_ZETA, D_TAUBULK, NDER };
+                       D_DSHV4, D_DEZ, D_ETA, D_TAUPI, D_ZETA, D_TAUBULK,
+                       // diagnostics of the last derivative evaluation (ccake_hydro_numbers):
+                       // theta, sigma^{11,12,13,22,23}, shear / bulk Knudsen and inverse
+                       // Reynolds numbers
+                       D_THETA, D_SIG0, D_SIG1, D_SIG2, D_SIG3, D_SIG4, D_KNS, D_KNB, D_IRS, D_IRB, NDER };
 
 // Neighbour-record strides (doubles). Record A feeds the smoothing pass,
 // record B the gradient pass; both are rewritten once per substep.
@@ -81,6 +85,7 @@ struct RunConst {
 struct Clock {
   double t0;
   double t;
+  double teval;   // time of the last substep-2 derivative evaluation (t0 + dt/2)
   int32_t frzc;   // steps seen by the freeze-out status machine (0, 1, 2 = third and later)
   int32_t pad;
 };

@@ -459,7 +459,7 @@ __global__ void k_visc(RunConst rc, Ptrs p) {
 }
 
 __global__ void k_clock(Clock* c, int substep, double dt) {
-  if (substep == 1) c->t = c->t0 + 0.5 * dt;
+  if (substep == 1) c->t = c->teval = c->t0 + 0.5 * dt;
   else { c->t = c->t0 + dt; c->t0 = c->t; }
 }
 
@@ -754,6 +754,100 @@ __global__ void k_freeze_advance(Clock* c) {
   if (c->frzc < 2) c->frzc++;
 }
 
+// Diagnostics of the last derivative evaluation (the substep-2 evaluation of
+// the last RK2 step, at t = t0 + dt/2), for the system-state output: the
+// equations of motion again from the stored inputs of that evaluation
+// (thermodynamics, gradients, pi^{mu nu}, Pi, gamma, v; u = gamma v), with
+// theta and sigma^{ij} taken out (src/eom_default.cpp:774-807), the transport
+// coefficients, and, with shear, src/eom_default.cpp:1831-1985
+// (compute_hydro_numbers): sigma^{mu nu} completed by symmetry,
+// orthogonality to u and tracelessness, Knudsen numbers tau_pi
+// sqrt|sigma:sigma| and tau_Pi |theta|, inverse Reynolds numbers
+// sqrt|pi:pi| / p and |Pi| / p. grads_f32: the gradients are the mixed
+// form's FP32 view.
+template <int D>
+__global__ void k_diag(RunConst rc, Ptrs p, int grads_f32) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.n) return;
+  const int n = p.n;
+  const double t = p.clock->teval, t2 = t * t;
+  double th[NTH];
+#pragma unroll
+  for (int q = 0; q < NTH; q++) th[q] = p.th[q * n + i];
+  const float* gf = reinterpret_cast<const float*>(p.grads);
+  auto G = [&](int slot) { return grads_f32 ? double(gf[(size_t)slot * n + i]) : p.grads[(size_t)slot * n + i]; };
+  EomIn<D, double> in;
+  in.th = th;
+  in.g = p.gam[i];
+#pragma unroll
+  for (int q = 0; q < 3; q++) {
+    in.v[q] = p.v[q * n + i];
+    in.u[q] = (q < D) ? in.v[q] * in.g : 0.0;
+    in.gradP[q] = (q < D) ? G(G_P + q) : 0.0;
+    in.gradBulk[q] = (q < D) ? G(G_B + q) : 0.0;
+    in.gradshear[q] = (q < D) ? G(G_SH + q) : 0.0;
+    in.divshear[q] = (q < D) ? G(G_DS + q) : 0.0;
+  }
+#pragma unroll
+  for (int q = 0; q < 9; q++) in.gradV[q] = (q < D * D) ? G(G_V + q) : 0.0;
+  in.sigma = p.sig[i];
+  in.sigma_lab = p.slab[i];
+  in.m = p.m[i];
+  in.Pi = p.bulk[i];
+#pragma unroll
+  for (int q = 0; q < NPI; q++) in.pi[q] = p.pi[q * n + i];
+  const TransportT<double> k = transport<double>(rc.cfg, th);
+  EomOut<double> o;
+  double dg[6];
+  eom<D, double>(rc.cfg, k, in, t, o, dg);
+  double* dv = p.derivs;
+  dv[D_ETA * n + i] = k.eta;
+  dv[D_TAUPI * n + i] = k.tau_pi;
+  dv[D_ZETA * n + i] = k.zeta;
+  dv[D_TAUBULK * n + i] = k.tau_Pi;
+  dv[D_THETA * n + i] = dg[0];
+  double kns = 0.0, knb = 0.0, irs = 0.0, irb = 0.0;
+  if (rc.cfg.using_shear) {
+    for (int q = 0; q < 5; q++) dv[(D_SIG0 + q) * n + i] = dg[1 + q];
+    const double g = in.g;
+    const double uc[3] = {-in.u[0], -in.u[1], D == 3 ? -t2 * in.u[2] : 0.0};
+    double st[4][4];
+    for (int a = 0; a < 4; a++) for (int b = 0; b < 4; b++) st[a][b] = 0.0;
+    st[1][1] = dg[1]; st[1][2] = dg[2]; st[1][3] = dg[3]; st[2][2] = dg[4]; st[2][3] = dg[5];
+    for (int a = 1; a < 4; a++) for (int b = a + 1; b < 4; b++) st[b][a] = st[a][b];
+    for (int a = 1; a < D + 1; a++) {
+      double c = 0.0;
+      for (int b = 1; b < D + 1; b++) c += uc[b - 1] * st[a][b];
+      st[0][a] = -1. * c / g;
+    }
+    for (int a = 1; a < 4; a++) st[a][0] = st[0][a];
+    st[0][0] = (uc[0] * uc[0] * st[1][1] + uc[1] * uc[1] * st[2][2] + 2. * uc[1] * uc[0] * st[2][1] +
+                2. * uc[2] * uc[0] * st[3][1] + 2. * uc[2] * uc[1] * st[3][2] -
+                uc[2] * uc[2] * (st[1][1] + st[2][2]) / t2) /
+               (g * g - uc[2] * uc[2] / t2);
+    st[3][3] = (st[0][0] - st[1][1] - st[2][2]) / t2;
+    const double gm[4] = {1.0, -1.0, -1.0, -t2};
+    double sn = 0.0, pn = 0.0;
+    for (int a = 0; a < 4; a++)
+      for (int b = 0; b < 4; b++) {
+        sn += st[a][b] * (st[a][b] * gm[b] * gm[a]);
+        const double pab = in.pi[pi_slot(a, b)];
+        pn += pab * (pab * gm[b] * gm[a]);
+      }
+    const double pr = th[T_P];
+    kns = k.tau_pi * sqrt(fabs(sn));
+    knb = k.tau_Pi * fabs(dg[0]);
+    irs = sqrt(fabs(pn)) / pr;
+    irb = fabs(in.Pi) / pr;
+  } else {
+    for (int q = 0; q < 5; q++) dv[(D_SIG0 + q) * n + i] = 0.0;
+  }
+  dv[D_KNS * n + i] = kns;
+  dv[D_KNB * n + i] = knb;
+  dv[D_IRS * n + i] = irs;
+  dv[D_IRB * n + i] = irb;
+}
+
 // FP32 copy of the table densities (fields 1..5 of 17) at 8 floats a node.
 __global__ void k_table_f32(const double* f, float* fd, int64_t nodes) {
   const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -858,6 +952,12 @@ void launch_freeze(const RunConst& rc, const Ptrs& p, cudaStream_t s) {
 }
 
 void launch_count_frozen(const Ptrs& p, int32_t* out, cudaStream_t s) { k_count_frozen<<<1, 1024, 0, s>>>(p, out); }
+
+void launch_diagnostics(const RunConst& rc, const Ptrs& p, int grads_f32, cudaStream_t s) {
+  const int nb = (p.n + kBlock - 1) / kBlock;
+  if (rc.cfg.dim == 3) k_diag<3><<<nb, kBlock, 0, s>>>(rc, p, grads_f32);
+  else k_diag<2><<<nb, kBlock, 0, s>>>(rc, p, grads_f32);
+}
 
 void launch_table_f32(const double* f, float* fd, int64_t nodes, cudaStream_t s) {
   if (nodes <= 0) return;

@@ -101,6 +101,9 @@ void launch_eos_thermo(const EosDev& eos, int chain_index, int64_t n, const doub
 // as one pass).
 constexpr int kEosFirstIters = 8;
 void launch_table_f32(const double* f, float* fd, int64_t nodes, cudaStream_t s);
+void launch_diagnostics(const RunConst& rc, const Ptrs& p, int grads_f32, cudaStream_t s);
+// the gradient sums of the mixed pass B alone (no equations of motion)
+void launch_gradients_mixed(const RunConst& rc, const Ptrs& p, cudaStream_t s);
 void launch_eos_batch(const EosDev& eos, int entropy, int seed_mode, int64_t n, const double* in4, double* tbqs,
                       double* th16, int32_t* status, int32_t* iters, int32_t* scratch, cudaStream_t s);
 

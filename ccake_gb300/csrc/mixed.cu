@@ -410,4 +410,10 @@ void launch_passB_mixed(const RunConst& rc, const Ptrs& p, int mode, double dt_s
   }
 }
 
+void launch_gradients_mixed(const RunConst& rc, const Ptrs& p, cudaStream_t s) {
+  const int nb = (p.n + kBlock - 1) / kBlock;
+  if (rc.cfg.dim == 3) k_passB_mixed<3><<<nb, kBlock, 0, s>>>(rc, p);
+  else k_passB_mixed<2><<<nb, kBlock, 0, s>>>(rc, p);
+}
+
 }  // namespace ccake

@@ -120,9 +120,12 @@ struct EomOut {
 // sector, for one particle at time t.
 // R = double is the plain FP64 form; R = float is the mixed form's EoM (the
 // state update it feeds stays FP64).
+// diag (optional, 6 values): theta and sigma^{11,12,13,22,23}
+// (src/eom_default.cpp:774-807); the hot kernels pass none.
 template <int D, typename R = double>
 __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, const EomIn<D, R>& in, double td,
-                           EomOut<R>& o) {
+                           EomOut<R>& o, R* diag = nullptr) {
+  R sigF[5] = {0, 0, 0, 0, 0}, sigM[5][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
   const R t = R(td);
   const R t2 = t * t;
   const R g = in.g, sig = in.sigma;
@@ -321,6 +324,7 @@ __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, cons
           Fds2 += -cmd[i + 1] * sgu_s * k13 - cmd[i + 1] * hy[0][0] * geo * k13 -
                   cmd[i + 1] * (hy[3][0] * f2 * t + g * hy[3][3] * it + f2 * hy[0][3] * it) * k13;
         }
+        if (diag) sigF[slot] = Fsg;
         R F = (-pi[i + 1][j + 1] - tdelta * Fdl - tpi * FD2 + R(2.) * tpi * Fdo2 * uv - tpp * Fds2 +
                     (R(2.) * eta + lpP * Pi) * Fsg + phi6 * Pi * pi[i + 1][j + 1] + phi7 * (sml + fu[i] * fu[j] * ss * k13)) *
                    istg;
@@ -351,6 +355,7 @@ __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, cons
             Msg += cmd[i + 1] * fuc[kk] * (ig * k13);
             Mds2 += -cmd[i + 1] * (hy[0][kk + 1] - hy[0][0] * fuc[kk] * ig) * k13;
           }
+          if (diag) sigM[slot][kk] = Msg;
           Mext[slot][kk] = (-tpi * MD2 - tdelta * Mdl + R(2.) * tpi * Mdo2 * uv - tpp * Mds2 + (R(2.) * eta + lpP * Pi) * Msg) *
                            istg;
         }
@@ -435,6 +440,19 @@ __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, cons
 #pragma unroll
     for (int kk = 0; kk < D; kk++) acc += Mext[sl][kk] * du[kk];
     o.dShv[sl] = cfg.using_shear ? acc + Fext[sl] : R(0.0);
+  }
+  if (diag) {
+    R c1 = R(0.0);
+#pragma unroll
+    for (int i = 0; i < D; i++) c1 += uc[i] * du[i];
+    diag[0] = -R(1.) * c1 / g + g * divV + g / t + geo;
+#pragma unroll
+    for (int sl = 0; sl < 5; sl++) {
+      R acc = R(0.0);
+#pragma unroll
+      for (int kk = 0; kk < D; kk++) acc += sigM[sl][kk] * du[kk];
+      diag[1 + sl] = acc + sigF[sl];
+    }
   }
   // ---- dEz (reference :827-862) ---------------------------------------------
   const R u3 = (D == 3) ? u[2] : R(0.0);

@@ -74,6 +74,37 @@ typedef struct ccake_particles_soa {
   const double *ux, *uy, *ueta;
 } ccake_particles_soa;
 
+/* ---- on-disk formats --------------------------------------------------
+ * The "ccake" initial-condition text format, src/BSQHydro.cpp:206-425
+ * (BSQHydro::read_ccake; the IC_file setting): a header line
+ * "#<n> dx dy deta <n> xmin ymin etamin", then one cell a line,
+ *   x y eta e|s rhoB rhoS rhoQ ux uy ueta bulk pixx pixy pixeta piyy piyeta pietaeta
+ * plus qB^0..3 qS^0..3 qQ^0..3 with initial diffusion. Blank and '#' lines
+ * after the header are skipped. */
+typedef struct ccake_ic ccake_ic;
+typedef struct ccake_ic_options {
+  int32_t input_as_entropy;         /* column 4 is s (1/fm^3), else e (GeV/fm^3) */
+  int32_t input_initial_diffusion;  /* 29 columns instead of 17 */
+  int32_t baryon, strange, electric;/* charges enabled (settings *_charge_enabled);
+                                       disabled ones read as zero */
+  int32_t reserved;
+  double e_cutoff;                  /* GeV/fm^3: a cell is kept when e (with entropy
+                                       input, the ideal pion gas e(s)) is above it */
+} ccake_ic_options;
+
+/* Reads and converts the file (e, bulk and pi^{ij} divided by hbar c);
+ * CCAKE_ERR_INVALID for a missing file, a header without '#' and eight
+ * numbers, or a data line with fewer numbers than the format has. */
+ccake_status_t ccake_ic_read_ccake(const char* path, const ccake_ic_options* opt, ccake_ic** out);
+/* Number of cells kept; grid6 (may be NULL) = dx, dy, deta, xmin, ymin, etamin. */
+ccake_status_t ccake_ic_info(const ccake_ic* ic, int64_t* n, double* grid6);
+/* One column by name (x y eta e s rhoB rhoS rhoQ ux uy ueta bulk pixx pixy
+ * pixeta piyy piyeta pietaeta qB0..qB3 qS0..qS3 qQ0..qQ3) into dst[n]. */
+ccake_status_t ccake_ic_column(const ccake_ic* ic, const char* name, double* dst);
+/* Points soa at the cells (valid until ccake_ic_free), for ccake_load_particles. */
+ccake_status_t ccake_ic_particles(const ccake_ic* ic, ccake_particles_soa* soa);
+void ccake_ic_free(ccake_ic* ic);
+
 /* Conserved totals, src/system_state.cpp:738-885. */
 typedef struct ccake_totals {
   double S, B, Sq, Q, E, Ez;
@@ -163,6 +194,25 @@ ccake_status_t ccake_conservation(ccake_ctx* ctx, ccake_totals* out);
 ccake_status_t ccake_copy_out(ccake_ctx* ctx, const char* field, double* host_out);
 /* Integer fields: btrack eos_id eos_iters freeze. */
 ccake_status_t ccake_copy_out_int(ccake_ctx* ctx, const char* field, int32_t* host_out);
+
+/* Diagnostics of the last derivative evaluation (the second substep of the
+ * last RK2 step) into the copy-out fields theta, sigma_tensor0..4
+ * (sigma^{11,12,13,22,23}), shear_knudsen, bulk_knudsen,
+ * inverse_reynolds_shear, inverse_reynolds_bulk and the transport
+ * coefficients eta_pi, zeta_Pi, tau_Pi, tau_pi: theta and sigma^{ij} of
+ * src/eom_default.cpp:774-807, the numbers of compute_hydro_numbers
+ * (:1831-1985, computed with shear only). All zero before the first step. */
+ccake_status_t ccake_hydro_numbers(ccake_ctx* ctx);
+
+/* The reference's text output system_state_<n>.dat (src/output.cpp:102-181,
+ * Output::print_system_state_to_txt) at path: the time, then one row a
+ * particle in input order: index, t, position (3), p, T, muB, muS, muQ, e
+ * (GeV units), rhoB, rhoS, rhoQ, s, eta_pi, zeta_Pi, tau_Pi, tau_pi, theta,
+ * inverse Reynolds and Knudsen numbers (shear, bulk), pi^{00,11,22,01,02,12,
+ * 13,23,33}, u (3), gamma, freeze status, EoS name, causality (0: not
+ * checked), six diffusion numbers (0: no diffusion sector). */
+ccake_status_t ccake_write_system_state(ccake_ctx* ctx, const char* path);
+
 
 /* Neighbour list of the current positions in CSR form, input order, each row
  * sorted by index (parity checks only). offsets has n+1 entries; returns

@@ -29,6 +29,8 @@ void alloc(System& s, int n) {
   A(s.bulk); A(s.eta_pi); A(s.tau_pi); A(s.zeta_Pi); A(s.tau_Pi); A(s.delta_PiPi); A(s.delta_pipi);
   A(s.lambda_piPi); A(s.lambda_Pipi); A(s.phi1); A(s.phi3); A(s.phi6); A(s.phi7); A(s.tau_pipi);
   A(s.d_ext_bulk); A(s.dEz); A(s.theta); A(s.shv_nabla_u); A(s.ext_bulk0); A(s.Ez0);
+  for (int i = 0; i < 5; i++) A(s.sigma_t[i]);
+  A(s.kn_shear); A(s.kn_bulk); A(s.ire_shear); A(s.ire_bulk);
   s.freeze.assign(n, 0); s.btrack.assign(n, 0); s.eos_id.assign(n, 0); s.eos_status.assign(n, 0);
   s.n = n;
 }
@@ -82,6 +84,11 @@ std::vector<double>* field(System& s, const std::string& k) {
   if (k == "d_ext_bulk") return &s.d_ext_bulk;
   if (k == "theta") return &s.theta;
   if (k == "shv_nabla_u") return &s.shv_nabla_u;
+  for (int i = 0; i < 5; i++) if (k == "sigma_tensor" + std::to_string(i)) return &s.sigma_t[i];
+  if (k == "shear_knudsen") return &s.kn_shear;
+  if (k == "bulk_knudsen") return &s.kn_bulk;
+  if (k == "inverse_reynolds_shear") return &s.ire_shear;
+  if (k == "inverse_reynolds_bulk") return &s.ire_bulk;
   return nullptr;
 }
 }  // namespace

@@ -128,6 +128,7 @@ void inverse(int D, const double* A, double* Ai) {
 struct ShearMRF {
   double M0i[9], F0i[3], Mnab[3], Fnab;
   double Mext[2][3][3], Fext[2][3];
+  double Msig[2][3][3], Fsig[2][3];   // M_sigma, F_sigma of the shear tensor sigma^{ij}
 };
 
 // src/eom_default.cpp:882-1412 (calculate_MRF_shear) for one particle.
@@ -352,6 +353,57 @@ void shear_mrf(const System& s, int a, double t, bool use_vort, ShearMRF& o) {
     }
     o.Fext[i][i] += phi7 * (-cmd[i + 1] * ss) / (3. * tpi * g * sigma);
   }
+  for (int i = 0; i < 2; i++)
+    for (int j = 0; j < 3; j++) {
+      o.Fsig[i][j] = Fsg[i][j];
+      for (int k = 0; k < 3; k++) o.Msig[i][j][k] = Msg[i][j][k];
+    }
+}
+
+// src/eom_default.cpp:1831-1985 (compute_hydro_numbers), without the
+// diffusion sector: the full sigma^{mu nu} from its five stored spatial
+// entries (symmetry, orthogonality to u, tracelessness), the shear and bulk
+// Knudsen numbers tau_pi sqrt|sigma:sigma| and tau_Pi |theta|, and the inverse
+// Reynolds numbers sqrt|pi:pi| / p and |Pi| / p.
+void hydro_numbers(System& s, int a, const double* sig5) {
+  const int D = s.cfg.dim;
+  const double t = s.t, t2 = t * t;
+  const double g = s.gamma[a];
+  double uc[3] = {0, 0, 0};
+  for (int i = 0; i < D; i++) uc[i] = s.u[i][a];
+  uc[0] = -uc[0];
+  uc[1] = -uc[1];
+  uc[2] *= -t2;
+  double st[4][4] = {{0}};
+  const int map[2][3] = {{0, 1, 2}, {-1, 3, 4}};
+  for (int i = 0; i < 2; i++)
+    for (int j = i; j < 3; j++) st[i + 1][j + 1] = sig5[map[i][j]];
+  for (int i = 1; i < 4; i++)
+    for (int j = i + 1; j < 4; j++) st[j][i] = st[i][j];
+  for (int i = 1; i < D + 1; i++) {
+    double c = 0.0;
+    for (int j = 1; j < D + 1; j++) c += uc[j - 1] * st[i][j];
+    st[0][i] = -1. * c / g;
+  }
+  for (int i = 1; i < 4; i++) st[i][0] = st[0][i];
+  st[0][0] = (uc[0] * uc[0] * st[1][1] + uc[1] * uc[1] * st[2][2] + 2. * uc[1] * uc[0] * st[2][1] +
+              2. * uc[2] * uc[0] * st[3][1] + 2. * uc[2] * uc[1] * st[3][2] -
+              uc[2] * uc[2] * (st[1][1] + st[2][2]) / t2) /
+             (g * g - uc[2] * uc[2] / t2);
+  st[3][3] = (st[0][0] - st[1][1] - st[2][2]) / t2;
+  const double gm[4] = {1.0, -1.0, -1.0, -t2};
+  double sn = 0.0, pn = 0.0;
+  for (int i = 0; i < 4; i++)
+    for (int j = 0; j < 4; j++) {
+      sn += st[i][j] * (st[i][j] * gm[j] * gm[i]);
+      pn += s.shv[i * 4 + j][a] * (s.shv[i * 4 + j][a] * gm[j] * gm[i]);
+    }
+  const double p = s.th[kP][a];
+  for (int k = 0; k < 5; k++) s.sigma_t[k][a] = sig5[k];
+  s.kn_shear[a] = s.tau_pi[a] * std::sqrt(std::fabs(sn));
+  s.kn_bulk[a] = s.tau_Pi[a] * std::fabs(s.theta[a]);
+  s.ire_shear[a] = std::sqrt(std::fabs(pn)) / p;
+  s.ire_bulk[a] = std::fabs(s.bulk[a]) / p;
 }
 
 }  // namespace
@@ -533,12 +585,17 @@ void evaluate_time_derivatives(System& s) {
     s.shv_nabla_u[a] = snu;
     if (shear) {
       const int map[2][3] = {{0, 1, 2}, {-1, 3, 4}};
+      double sig5[5];
       for (int i = 0; i < 2; i++)
         for (int j = i; j < 3; j++) {
           double acc = 0.;
           for (int k = 0; k < D; k++) acc += sm.Mext[i][j][k] * du[k];
           s.d_ext_shv[map[i][j]][a] = acc + sm.Fext[i][j];
+          double as = 0.;
+          for (int k = 0; k < D; k++) as += sm.Msig[i][j][k] * du[k];
+          sig5[map[i][j]] = as + sm.Fsig[i][j];
         }
+      hydro_numbers(s, a, sig5);
     } else {
       for (int k = 0; k < 6; k++) s.d_ext_shv[k][a] = 0.0;
     }

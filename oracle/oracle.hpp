@@ -90,6 +90,9 @@ struct System {
   std::vector<double> gradP[3], gradE[3], gradBulk[3], gradshear[3], divshear[3], gradV[9];
   // time derivatives
   std::vector<double> du_dt[3], d_ext[4], d_ext_bulk, d_ext_shv[6], dEz, theta, shv_nabla_u;
+  // src/eom_default.cpp:1831-1985 (with shear): sigma^{11,12,13,22,23},
+  // shear / bulk Knudsen and inverse Reynolds numbers
+  std::vector<double> sigma_t[5], kn_shear, kn_bulk, ire_shear, ire_bulk;
   // evolver cache
   std::vector<double> r0[3], u0[3], ext0[4], ext_bulk0, ext_shv0[6], Ez0;
   // table EoS (optional)

@@ -279,3 +279,67 @@ def test_freeze_out_status_machine_matches_oracle():
     keep = gpu.continue_evolution(max_tau=10.0)
     assert keep == (np.count_nonzero(fg >= 4) < p.n)
     assert gpu.continue_evolution(max_tau=rc.t0) is False
+
+
+def test_ic_file_run_matches_oracle(tmp_path):
+    # an IC file in the reference's "ccake" format (e in GeV/fm^3), read by the
+    # library's reader, run on the GPU and in the oracle from the same cells
+    p0, rc = ics.gubser_2d(n_side=40)
+    path = tmp_path / "ic_gubser.dat"
+    with open(path, "w") as fh:
+        fh.write(f"#0 0.05 0.05 0.1 0 {rc.xmin} {rc.ymin} -0.1\n")
+        for i in range(p0.n):
+            row = [p0.x[i], p0.y[i], 0.0, p0.e[i] * 0.1973269804, 0, 0, 0, p0.ux[i], p0.uy[i], 0] + [0.0] * 7
+            fh.write(" ".join(f"{v:.17g}" for v in row) + "\n")
+    p, cols, grid = api.read_ccake_ic(path)
+    assert p.n == p0.n and grid[0] == 0.05
+    assert np.max(np.abs(p.e - p0.e) / p0.e) < 1e-15
+    gpu = api.GpuHydro(rc)
+    gpu.load(p)
+    orc = O.OracleRun(p, rc)
+    gpu.initialize()
+    orc.initialize()
+    gpu.step(5)
+    assert orc.step(5) == 0
+    for f in ("x", "u0", "ext_s", "T", "e", "sigma_lab"):
+        assert relerr(gpu.get(f), orc.get(f)) < RTOL, f
+
+
+def test_hydro_numbers_and_system_state_file(tmp_path):
+    # theta, sigma^{ij}, Knudsen / inverse Reynolds numbers of the last
+    # derivative evaluation against the oracle's compute_hydro_numbers
+    # (src/eom_default.cpp:1831-1985), then the system_state text output
+    p, rc, gpu, orc = pair("hotspots")
+    gpu.initialize()
+    orc.initialize()
+    gpu.hydro_numbers()
+    assert not np.any(gpu.get("theta")) and not np.any(gpu.get("shear_knudsen"))
+    gpu.step(5)
+    assert orc.step(5) == 0
+    gpu.hydro_numbers()
+    for f in ("theta", "eta_pi", "tau_pi", "zeta_Pi", "tau_Pi", "inverse_reynolds_shear", "inverse_reynolds_bulk"):
+        assert relerr(gpu.get(f), orc.get(f)) < 1e-9, f
+    for f in ("sigma_tensor0", "sigma_tensor1", "sigma_tensor3", "shear_knudsen", "bulk_knudsen"):
+        assert relerr(gpu.get(f), orc.get(f), GRAD_FLOOR) < 1e-9, f
+    assert np.max(gpu.get("shear_knudsen")) > 0
+    path = tmp_path / "system_state_5.dat"
+    gpu.write_system_state(path)
+    lines = path.read_text().splitlines()
+    assert abs(float(lines[0]) - gpu.t) < 1e-5
+    rows = [ln.split() for ln in lines[1:]]
+    # 46 numbers and names a row (the reference's column comments skip the
+    # causality flag, 39, and end at 44)
+    assert len(rows) == p.n and all(len(r) == 46 for r in rows)
+    # the first row's time in the default format, the later ones scientific
+    assert "e" not in rows[0][1] and "e+00" in rows[1][1]
+    assert [r[0] for r in rows[:3]] == ["0", "1", "2"]
+    col = lambda k: np.array([float(r[k]) for r in rows])
+    hc = 0.1973269804
+    for k, f, scale in ((2, "x", 1.0), (5, "p", hc), (6, "T", hc), (10, "e", hc), (11, "rhoB", 1.0), (14, "s", 1.0),
+                        (19, "theta", 1.0), (22, "shear_knudsen", 1.0), (25, "shv11", 1.0), (33, "u0", 1.0),
+                        (36, "gamma", 1.0)):
+        ref = gpu.get(f) * scale
+        assert np.all(np.abs(col(k) - ref) <= 6e-7 * np.abs(ref) + 1e-300), f
+    assert {r[38] for r in rows} == {"conformal_diagonal"}
+    assert [int(r[37]) for r in rows] == list(gpu.get_int("freeze")) and {r[39] for r in rows} == {"0"}
+    assert not np.any(col(4)) and not np.any(col(35)) and not np.any(col(45))
