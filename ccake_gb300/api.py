@@ -34,6 +34,10 @@ class ParticlesSoA(ctypes.Structure):
                                                     "uy", "ueta")]
 
 
+class PreinvConfig(ctypes.Structure):
+    _fields_ = [("exp_lo", _i32 * 4), ("exp_hi", _i32 * 4), ("nodes", _i32), ("reserved", _i32)]
+
+
 class IcOptions(ctypes.Structure):
     _fields_ = [("input_as_entropy", _i32), ("input_initial_diffusion", _i32), ("baryon", _i32),
                 ("strange", _i32), ("electric", _i32), ("reserved", _i32), ("e_cutoff", _f64)]
@@ -81,6 +85,10 @@ def lib():
         L.ccake_ctx_create.argtypes = [ctypes.POINTER(CcakeConfig), ctypes.POINTER(P)]
         L.ccake_ctx_destroy.argtypes = [P]
         L.ccake_load_particles.argtypes = [P, ctypes.POINTER(ParticlesSoA)]
+        L.ccake_preinverted_build.argtypes = [P, ctypes.POINTER(PreinvConfig)]
+        L.ccake_preinverted_use.argtypes = [P, _i32]
+        L.ccake_preinverted_lookup.argtypes = [P, _i64, _dp, _dp]
+        L.ccake_preinverted_copy.argtypes = [P, ctypes.POINTER(_i64), _dp]
         L.ccake_hydro_numbers.argtypes = [P]
         L.ccake_write_system_state.argtypes = [P, ctypes.c_char_p]
         L.ccake_ic_read_ccake.argtypes = [ctypes.c_char_p, ctypes.POINTER(IcOptions), ctypes.POINTER(P)]
@@ -182,6 +190,29 @@ class GpuHydro:
 
     def step(self, n=1):
         self._check(lib().ccake_step(self.h, int(n)), "step")
+
+    def preinverted_build(self, exp_lo=(-3, -3, -3, -3), exp_hi=(1, 0, 0, 0), nodes=20):
+        """Pre-inverted (s, rho) -> thermodynamics tables from this context's
+        EoS (ccake_preinverted_build; defaults: the reference generator's)."""
+        c = PreinvConfig((_i32 * 4)(*exp_lo), (_i32 * 4)(*exp_hi), int(nodes), 0)
+        self._check(lib().ccake_preinverted_build(self.h, ctypes.byref(c)), "preinverted_build")
+
+    def preinverted_use(self, on=True):
+        self._check(lib().ccake_preinverted_use(self.h, 1 if on else 0), "preinverted_use")
+
+    def preinverted_lookup(self, sBSQ):
+        """(n, 4) densities -> (n, 11): T, muB, muQ, muS, e, p, cs2, dwds, dwdB, dwdQ, dwdS."""
+        a = np.ascontiguousarray(sBSQ, dtype=np.float64).reshape(-1, 4)
+        out = np.zeros((a.shape[0], 11))
+        self._check(lib().ccake_preinverted_lookup(self.h, a.shape[0], _d(a), _d(out)), "preinverted_lookup")
+        return out
+
+    def preinverted_values(self):
+        n = _i64()
+        self._check(lib().ccake_preinverted_copy(self.h, ctypes.byref(n), None), "preinverted_copy")
+        out = np.zeros((n.value, 11))
+        self._check(lib().ccake_preinverted_copy(self.h, ctypes.byref(n), _d(out)), "preinverted_copy")
+        return out
 
     def hydro_numbers(self):
         """theta, sigma^{ij}, Knudsen and inverse Reynolds numbers and the

@@ -39,6 +39,11 @@ struct ccake_ctx {
   int32_t* ibuf = nullptr;
   double* d_table = nullptr;
   float* d_table_f = nullptr;   // FP32 densities of the nodes (mixed-form Newton Jacobians)
+  // pre-inverted tables: values, description (host and device copies)
+  double* pre_v = nullptr;
+  int64_t pre_count = 0;
+  PreinvView pre_host{};
+  PreinvView* pre_dev = nullptr;
   int records_form = 0;   // which smoothing record matches the state: 0 FP64, 1 mixed
   bool evaluated = false; // derivatives were evaluated since the initialisation
   // candidate list: skin (fm), validity and rebuild schedule
@@ -335,7 +340,6 @@ struct Scratch {
 static int32_t* eos_scratch(ccake_ctx* ctx, int64_t n) {
   if (n > ctx->eos_scratch_cap) {
     if (ctx->eos_scratch) cudaFree(ctx->eos_scratch);
-  if (ctx->d_count) cudaFree(ctx->d_count);
     ctx->eos_scratch = nullptr;
     ctx->eos_scratch_cap = 0;
     if (cudaMalloc(&ctx->eos_scratch, (size_t)(n + 1) * sizeof(int32_t)) != cudaSuccess) {
@@ -475,6 +479,8 @@ ccake_status_t ccake_ctx_destroy(ccake_ctx* ctx) {
   if (ctx->d_count) cudaFree(ctx->d_count);
   if (ctx->d_table) cudaFree(ctx->d_table);
   if (ctx->d_table_f) cudaFree(ctx->d_table_f);
+  if (ctx->pre_v) cudaFree(ctx->pre_v);
+  if (ctx->pre_dev) cudaFree(ctx->pre_dev);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return CCAKE_OK;
@@ -915,6 +921,7 @@ ccake_status_t ccake_set_eos_table(ccake_ctx* ctx, const int32_t* n, const doubl
   EosDev host = e;
   host.tab.f = fields;
   host.tab.fd = nullptr;
+  host.pre = nullptr;
   double x4[4] = {ctx->cfg.freeze_out_T, 0, 0, 0}, o[17];
   model_thermo(host, M_TABLE, x4, o);
   ctx->rc.efreeze = o[5];
@@ -1292,6 +1299,117 @@ ccake_status_t ccake_write_system_state(ccake_ctx* ctx, const char* path) {
   }
   out << std::flush;
   if (!out.good()) return fail(ctx, CCAKE_ERR_INVALID, std::string("write failed: ") + path);
+  return CCAKE_OK;
+}
+
+ccake_status_t ccake_preinverted_build(ccake_ctx* ctx, const ccake_preinv_config* cfg) {
+  if (!ctx || !cfg) return CCAKE_ERR_INVALID;
+  if (ctx->eos.kind == 2 && !ctx->d_table) return fail(ctx, CCAKE_ERR_STATE, "set the EoS table first");
+  PreinvView P{};
+  int64_t tiles = 1;
+  for (int k = 0; k < 4; k++) {
+    P.nt[k] = cfg->exp_hi[k] - cfg->exp_lo[k] + 1;
+    if (P.nt[k] < 1 || P.nt[k] > kPreMaxTiles) return fail(ctx, CCAKE_ERR_INVALID, "1 to 8 decades an axis");
+    P.e_lo[k] = cfg->exp_lo[k];
+    tiles *= P.nt[k];
+  }
+  if (cfg->nodes < 2 || cfg->nodes > 64) return fail(ctx, CCAKE_ERR_INVALID, "2 to 64 nodes a tile axis");
+  P.N = cfg->nodes;
+  for (int k = 0; k < 4; k++)
+    for (int j = 0; j < P.nt[k]; j++) {
+      const int e = cfg->exp_lo[k] + j;
+      P.mn[k][j] = std::pow(10., (double)e);
+      P.st[k][j] = std::pow(10., (double)(e + 1)) / P.N;
+    }
+  const int64_t tn = (int64_t)P.N * P.N * P.N * P.N, total = tiles * tn;
+  if (ctx->pre_v) cudaFree(ctx->pre_v);
+  ctx->pre_v = nullptr;
+  ctx->pre_count = 0;
+  if (ctx->eos.pre) {
+    ctx->eos.pre = nullptr;
+    drop_graph(ctx);
+  }
+  if (cudaMalloc(&ctx->pre_v, (size_t)total * kPreVars * sizeof(double)) != cudaSuccess)
+    return fail(ctx, CCAKE_ERR_NOMEM, "pre-inverted table allocation");
+  P.v = ctx->pre_v;
+  // chunks of whole tiles, about 4M nodes at a time
+  const int64_t per = std::max<int64_t>(1, ((int64_t)1 << 22) / tn), chunk = per * tn;
+  double *in4 = nullptr, *tbqs = nullptr, *th16 = nullptr;
+  int32_t* st = nullptr;
+  if (cudaMalloc(&in4, chunk * 4 * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&tbqs, chunk * 4 * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&th16, chunk * 16 * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&st, chunk * sizeof(int32_t)) != cudaSuccess) {
+    cudaFree(in4); cudaFree(tbqs); cudaFree(th16); cudaFree(st);
+    return fail(ctx, CCAKE_ERR_NOMEM, "pre-inverted table scratch");
+  }
+  if (!ctx->d_count && cudaMalloc(&ctx->d_count, sizeof(int32_t)) != cudaSuccess) return fail(ctx, CCAKE_ERR_NOMEM, "allocation");
+  CK(cudaMemsetAsync(ctx->d_count, 0, sizeof(int32_t), ctx->stream));
+  int32_t* scratch = eos_scratch(ctx, chunk);
+  for (int64_t t0 = 0; t0 < tiles; t0 += per) {
+    const int64_t cnt = std::min(per, tiles - t0) * tn;
+    launch_preinv_grid(P, t0, cnt, in4, tbqs, ctx->stream);
+    launch_eos_batch(ctx->eos, 1, 0, cnt, in4, tbqs, th16, st, nullptr, scratch, ctx->stream);
+    launch_preinv_pack(cnt, th16, st, ctx->pre_v + (size_t)t0 * tn * kPreVars, ctx->d_count, ctx->stream);
+  }
+  int32_t nfail = 0;
+  CK(cudaMemcpyAsync(&nfail, ctx->d_count, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  cudaFree(in4); cudaFree(tbqs); cudaFree(th16); cudaFree(st);
+  if (!ctx->pre_dev && cudaMalloc(&ctx->pre_dev, sizeof(PreinvView)) != cudaSuccess)
+    return fail(ctx, CCAKE_ERR_NOMEM, "allocation");
+  CK(cudaMemcpy(ctx->pre_dev, &P, sizeof(PreinvView), cudaMemcpyHostToDevice));
+  ctx->pre_host = P;
+  ctx->pre_count = total;
+  // the reference's generator aborts at a node without a solution
+  if (nfail > 0) return fail(ctx, CCAKE_ERR_EOS, std::to_string(nfail) + " table nodes without an EoS solution");
+  CK(cudaGetLastError());
+  return CCAKE_OK;
+}
+
+ccake_status_t ccake_preinverted_use(ccake_ctx* ctx, int32_t on) {
+  if (!ctx) return CCAKE_ERR_INVALID;
+  if (on && !ctx->pre_count) return fail(ctx, CCAKE_ERR_STATE, "build the pre-inverted tables first");
+  const PreinvView* want = on ? ctx->pre_dev : nullptr;
+  if (ctx->eos.pre != want) {
+    ctx->eos.pre = want;
+    drop_graph(ctx);   // the step graph holds the EoS description by value
+  }
+  return CCAKE_OK;
+}
+
+ccake_status_t ccake_preinverted_lookup(ccake_ctx* ctx, int64_t n, const double* sBSQ, double* out11) {
+  if (!ctx || n < 0 || (n > 0 && (!sBSQ || !out11))) return CCAKE_ERR_INVALID;
+  if (!ctx->pre_count) return fail(ctx, CCAKE_ERR_STATE, "build the pre-inverted tables first");
+  if (n == 0) return CCAKE_OK;
+  double *d_in = nullptr, *d_out = nullptr;
+  CK(cudaMalloc(&d_in, n * 4 * sizeof(double)));
+  CK(cudaMalloc(&d_out, n * kPreVars * sizeof(double)));
+  CK(cudaMemcpyAsync(d_in, sBSQ, n * 4 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  launch_preinv_lookup(ctx->pre_dev, n, d_in, d_out, ctx->stream);
+  CK(cudaMemcpyAsync(out11, d_out, n * kPreVars * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  cudaFree(d_in);
+  cudaFree(d_out);
+  CK(cudaGetLastError());
+  return CCAKE_OK;
+}
+
+ccake_status_t ccake_preinverted_lookup_device(ccake_ctx* ctx, int64_t n, const double* d_sBSQ, double* d_out11,
+                                               void* stream) {
+  if (!ctx || n < 0) return CCAKE_ERR_INVALID;
+  if (!ctx->pre_count) return fail(ctx, CCAKE_ERR_STATE, "build the pre-inverted tables first");
+  launch_preinv_lookup(ctx->pre_dev, n, d_sBSQ, d_out11, stream ? (cudaStream_t)stream : ctx->stream);
+  CK(cudaGetLastError());
+  return CCAKE_OK;
+}
+
+ccake_status_t ccake_preinverted_copy(ccake_ctx* ctx, int64_t* count, double* host) {
+  if (!ctx || !count) return CCAKE_ERR_INVALID;
+  *count = ctx->pre_count;
+  if (host && ctx->pre_count) {
+    CK(cudaMemcpy(host, ctx->pre_v, (size_t)ctx->pre_count * kPreVars * sizeof(double), cudaMemcpyDeviceToHost));
+  }
   return CCAKE_OK;
 }
 

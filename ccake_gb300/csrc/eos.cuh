@@ -31,6 +31,23 @@ struct TableView {
   double id[4] = {0, 0, 0, 0};   // 1 / d, rounded on the host (mixed-form lookup)
 };
 
+// Pre-inverted (s, rhoB, rhoS, rhoQ) -> thermodynamics tables, the
+// reference's EoS_Interpolator (include/eos_interpolator.h:33-165,
+// src/eos_interpolator.cpp:531-739): one tile a decade of each density,
+// tiles of N^4 nodes at x = min + i * step (min = 10^e, step = 10^(e+1) / N,
+// utilities/generate_eos_table.cpp:196-203), 11 values a node in the order of
+// kPreVars, nodes row-major with rhoQ fastest.
+constexpr int kPreMaxTiles = 8;
+enum PreVar : int { PV_T = 0, PV_MUB, PV_MUQ, PV_MUS, PV_E, PV_P, PV_CS2, PV_DWDS, PV_DWDB, PV_DWDQ, PV_DWDS_S, kPreVars };
+struct PreinvView {
+  const double* v = nullptr;             // [tile][node][kPreVars]
+  int nt[4] = {0, 0, 0, 0};              // tiles on each axis (s, rhoB, rhoS, rhoQ)
+  int N = 0;                             // nodes on each axis of a tile
+  int e_lo[4] = {0, 0, 0, 0};            // decade exponent of tile 0
+  double mn[4][kPreMaxTiles];            // tile minimum, 10^e (host pow)
+  double st[4][kPreMaxTiles];            // tile step, 10^(e+1) / N
+};
+
 struct EosDev {
   int kind;                 // ccake_config::eos_kind
   int thermo_mode;          // 0 reference chain, 1 exact Hessian inverse
@@ -39,6 +56,9 @@ struct EosDev {
   TableView tab;
   // 1: Newton Jacobians of the table in FP32 (residuals stay FP64)
   int jac32 = 0;
+  // device copy of the pre-inverted tables' description; non-null: the step's
+  // thermodynamics come from the tables instead of the inversion
+  const PreinvView* pre = nullptr;
 };
 
 enum Model : int { M_CONF = 0, M_CDIAG = 1, M_TABLE = 2 };
@@ -848,6 +868,53 @@ __host__ __device__ inline void set_thermo_o(const EosDev& e, int k, const doubl
   }
   th[T_DWDQ] = mQ + ct;
 }
+
+#ifdef __CUDACC__
+// EoS_Interpolator::fill_thermodynamics and interpolate4D
+// (src/eos_interpolator.cpp:531-739) for one point: densities clamped to
+// max(0.001, |x|) (the tables hold positive densities only, and the
+// chemical potentials are returned as tabulated), the tile of each axis by
+// its decade (the count of tile edges 10^(e_lo + j) at or below x, clamped to
+// the tiles present), the cell by floor((x - min) / step) clamped to the tile,
+// and the 16-corner multilinear sum in the reference's corner order (bit i of
+// the corner number is axis i) with every rounding explicit. out[11] in
+// kPreVars order.
+__device__ inline void preinv_lookup(const PreinvView& P, const double* sBSQ, double* out) {
+  double pos[4];
+  pos[0] = fmax(0.001, sBSQ[0]);
+  for (int k = 1; k < 4; k++) pos[k] = fmax(0.001, fabs(sBSQ[k]));
+  int t[4], idx[4];
+  double x[4];
+  for (int k = 0; k < 4; k++) {
+    int tk = 0;
+    for (int j = 1; j < P.nt[k]; j++) tk += (pos[k] >= P.mn[k][j]) ? 1 : 0;
+    t[k] = tk;
+    const double mn = P.mn[k][tk], st = P.st[k][tk];
+    int ik = (int)floor(__ddiv_rn(__dsub_rn(pos[k], mn), st));
+    ik = ik < 0 ? 0 : ik;
+    // the +1 corner stays inside the tile (the reference clamps to N - 1)
+    ik = ik > P.N - 2 ? P.N - 2 : ik;
+    idx[k] = ik;
+    x[k] = __ddiv_rn(__dsub_rn(__dsub_rn(pos[k], mn), __dmul_rn((double)ik, st)), st);
+  }
+  const long tile = (((long)t[0] * P.nt[1] + t[1]) * P.nt[2] + t[2]) * P.nt[3] + t[3];
+  const long N = P.N, tn = N * N * N * N;
+  const double* base = P.v + (size_t)tile * tn * kPreVars;
+  double phi[16];
+  for (int c = 0; c < 16; c++) {
+    double ph = 1.0;
+    for (int i = 0; i < 4; i++) ph = __dmul_rn(ph, ((c >> i) & 1) ? x[i] : __dsub_rn(1.0, x[i]));
+    phi[c] = ph;
+  }
+  for (int v = 0; v < kPreVars; v++) out[v] = 0.0;
+  for (int c = 0; c < 16; c++) {
+    const long node = (((long)(idx[0] + (c & 1)) * N + idx[1] + ((c >> 1) & 1)) * N + idx[2] + ((c >> 2) & 1)) * N +
+                      idx[3] + ((c >> 3) & 1);
+    const double* nv = base + (size_t)node * kPreVars;
+    for (int v = 0; v < kPreVars; v++) out[v] = __dadd_rn(out[v], __dmul_rn(phi[c], nv[v]));
+  }
+}
+#endif
 
 __host__ __device__ inline void set_thermo(const EosDev& e, int k, const double* x, double* th) {
   double o[17];

@@ -101,6 +101,10 @@ void launch_eos_thermo(const EosDev& eos, int chain_index, int64_t n, const doub
 // as one pass).
 constexpr int kEosFirstIters = 8;
 void launch_table_f32(const double* f, float* fd, int64_t nodes, cudaStream_t s);
+void launch_preinv_grid(const PreinvView& P, int64_t tile0, int64_t count, double* in4, double* tbqs, cudaStream_t s);
+void launch_preinv_pack(int64_t count, const double* th16, const int32_t* status, double* out, int32_t* nfail,
+                        cudaStream_t s);
+void launch_preinv_lookup(const PreinvView* P, int64_t n, const double* sBSQ, double* out, cudaStream_t s);
 void launch_diagnostics(const RunConst& rc, const Ptrs& p, int grads_f32, cudaStream_t s);
 // the gradient sums of the mixed pass B alone (no equations of motion)
 void launch_gradients_mixed(const RunConst& rc, const Ptrs& p, cudaStream_t s);

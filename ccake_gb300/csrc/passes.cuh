@@ -134,14 +134,37 @@ __device__ __forceinline__ void thermo_tail(const RunConst& rc, const EosDev& eo
   double th[NTH];
   double x[4] = {p.th[T_T * n + i], p.th[T_MUB * n + i], p.th[T_MUQ * n + i], p.th[T_MUS * n + i]};
   const double tgt[4] = {p.th[T_S * n + i], p.th[T_RB * n + i], p.th[T_RS * n + i], p.th[T_RQ * n + i]};
-  int iters = 0;
-  double o[17];
-  const int k = eos_invert(eos, 1, tgt, p.eos_id[i], x, &iters, MIX ? 1 : 0, o);
-  if (k < 0) {
-    atomicAdd(&p.err[E_EOS], 1);
-    return;
+  int iters = 0, k = 0;
+  if (eos.pre) {
+    // pre-inverted tables (EoS_Interpolator::fill_thermodynamics): the
+    // densities stay, everything else is interpolated
+    double v[kPreVars];
+    preinv_lookup(*eos.pre, tgt, v);
+    th[T_T] = v[PV_T];
+    th[T_MUB] = v[PV_MUB];
+    th[T_MUS] = v[PV_MUS];
+    th[T_MUQ] = v[PV_MUQ];
+    th[T_P] = v[PV_P];
+    th[T_S] = tgt[0];
+    th[T_RB] = tgt[1];
+    th[T_RS] = tgt[2];
+    th[T_RQ] = tgt[3];
+    th[T_E] = v[PV_E];
+    th[T_W] = v[PV_E] + v[PV_P];
+    th[T_CS2] = v[PV_CS2];
+    th[T_DWDS] = v[PV_DWDS];
+    th[T_DWDB] = v[PV_DWDB];
+    th[T_DWDSS] = v[PV_DWDS_S];
+    th[T_DWDQ] = v[PV_DWDQ];
+  } else {
+    double o[17];
+    k = eos_invert(eos, 1, tgt, p.eos_id[i], x, &iters, MIX ? 1 : 0, o);
+    if (k < 0) {
+      atomicAdd(&p.err[E_EOS], 1);
+      return;
+    }
+    set_thermo_o(eos, k, x, o, th, MIX);
   }
-  set_thermo_o(eos, k, x, o, th, MIX);
 #pragma unroll
   for (int q = 0; q < NTH; q++) p.th[q * n + i] = th[q];
   p.eos_id[i] = k;

@@ -213,6 +213,36 @@ ccake_status_t ccake_hydro_numbers(ccake_ctx* ctx);
  * checked), six diffusion numbers (0: no diffusion sector). */
 ccake_status_t ccake_write_system_state(ccake_ctx* ctx, const char* path);
 
+/* ---- pre-inverted (s, rhoB, rhoS, rhoQ) -> thermodynamics tables ---------
+ * The reference's EoS_Interpolator (include/eos_interpolator.h:33-165,
+ * src/eos_interpolator.cpp:531-739) and its generator
+ * (utilities/generate_eos_table.cpp): one tile a decade [10^e, 10^(e+1)) of
+ * each density, N^4 nodes a tile at min + i * 10^(e+1)/N, 11 values a node:
+ * T, muB, muQ, muS, e, p, cs2, dw/ds, dw/drhoB, dw/drhoQ, dw/drhoS. */
+typedef struct ccake_preinv_config {
+  int32_t exp_lo[4];   /* first decade exponent of s, rhoB, rhoS, rhoQ (generator: -3 -3 -3 -3) */
+  int32_t exp_hi[4];   /* last decade exponent (generator: 1 0 0 0); at most 8 decades an axis */
+  int32_t nodes;       /* nodes a tile axis, 2..64 (generator: 20) */
+  int32_t reserved;
+} ccake_preinv_config;
+
+/* Generates the tables on the device from the context's EoS (every node by
+ * the entropy-mode inversion from T = 750/197 fm^-1, mu = 0);
+ * CCAKE_ERR_EOS if a node has no solution (the generator aborts there). */
+ccake_status_t ccake_preinverted_build(ccake_ctx* ctx, const ccake_preinv_config* cfg);
+/* on != 0: the step takes its thermodynamics from the tables
+ * (fill_thermodynamics) instead of the inversion. */
+ccake_status_t ccake_preinverted_use(ccake_ctx* ctx, int32_t on);
+/* Lookups of n rows (s, rhoB, rhoS, rhoQ) into out11[n][11], host arrays. */
+ccake_status_t ccake_preinverted_lookup(ccake_ctx* ctx, int64_t n, const double* sBSQ, double* out11);
+/* The same on device arrays, enqueued on stream (NULL: the context's). */
+ccake_status_t ccake_preinverted_lookup_device(ccake_ctx* ctx, int64_t n, const double* d_sBSQ, double* d_out11,
+                                               void* stream);
+/* count = number of nodes; host (may be NULL) receives count x 11 values,
+ * tiles in order (rhoQ decade fastest), nodes row-major (rhoQ fastest). */
+ccake_status_t ccake_preinverted_copy(ccake_ctx* ctx, int64_t* count, double* host);
+
+
 
 /* Neighbour list of the current positions in CSR form, input order, each row
  * sorted by index (parity checks only). offsets has n+1 entries; returns
