@@ -462,11 +462,67 @@ def run_eos_table(args):
                             "seconds": train_s},
                "what": "4-64-64-64-4 tanh MLP seed (BF16 tcgen05 kernels) for the table model, "
                        "then the reference seed chain"}
+    # pre-inverted (s, rho) -> thermodynamics tables in the reference
+    # generator's layout (decades 1e-3..1e2 in s, 1e-3..1e1 in rho, 20^4 nodes
+    # a tile, 51.2M nodes). Generated here from the conformal-diagonal EoS,
+    # which has a solution at every node (the generator aborts at a node
+    # without one, and most nodes lie outside the synthetic table's domain).
+    # Lookup throughput on the 2M states' (s, rho) against the entropy-mode
+    # inversion of the same EoS from the generator's seed; accuracy on the rows
+    # inside the tables.
+    gc = api.GpuHydro(ics.RunConfig(eos_kind=1, thermo_mode=1))
+    t0 = time.perf_counter()
+    gc.preinverted_build()
+    torch.cuda.synchronize()
+    gen_s = time.perf_counter() - t0
+    sBSQ = np.ascontiguousarray(fw[:, [1, 2, 3, 4]])
+    a_ = np.abs(sBSQ)
+    cover = (a_[:, 0] >= 1e-3) & (a_[:, 0] < 1e2) & np.all((a_[:, 1:] >= 1e-3) & (a_[:, 1:] < 1e1), axis=1)
+    q = torch.from_numpy(sBSQ).to(dev)
+    look = torch.empty((n_rows, 11), dtype=torch.float64, device=dev)
+    seedS = torch.tensor([750.0 / 197.0, 0, 0, 0], dtype=torch.float64, device=dev).repeat(n_rows, 1)
+    xs = seedS.clone()
+    ths = torch.empty((n_rows, 16), dtype=torch.float64, device=dev)
+    sts = torch.empty(n_rows, dtype=torch.int32, device=dev)
+
+    def timed_fn(fn):
+        for _ in range(max(1, args.warmup)):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / args.steps
+
+    ms_look = timed_fn(lambda: gc.preinverted_lookup_device(n_rows, q.data_ptr(), look.data_ptr(), stream.cuda_stream))
+
+    def newton_s():
+        xs.copy_(seedS)
+        gc.eos_invert_device(1, 0, n_rows, q.data_ptr(), xs.data_ptr(), ths.data_ptr(), sts.data_ptr(), 0,
+                             stream.cuda_stream)
+
+    ms_newt = timed_fn(newton_s)
+    lk, xn, okn = look.cpu().numpy(), xs.cpu().numpy(), sts.cpu().numpy() >= 0
+    sel = cover & okn
+    errT = np.abs(lk[sel, 0] / xn[sel, 0] - 1.0)
+    preinv = {"value": n_rows / (ms_look * 1e-3), "unit": "lookups/s", "rows": n_rows, "ms_per_batch": ms_look,
+              "newton_entropy_mode_same_eos": {"value": n_rows / (ms_newt * 1e-3), "unit": "inversions/s",
+                                               "ms_per_batch": ms_newt, "solved_rate": float(okn.mean())},
+              "generation": {"nodes": 5 * 4 * 4 * 4 * 20 ** 4, "seconds": gen_s, "eos": "conformal-diagonal",
+                             "layout": "decades s 1e-3..1e2, rho 1e-3..1e1, 20^4 nodes a tile"},
+              "rows_inside_tables": int(cover.sum()),
+              "T_rel_err_inside": {"p50": float(np.median(errT)), "p99": float(np.percentile(errT, 99)),
+                                   "max": float(errT.max())},
+              "what": "multilinear lookup (reference EoS_Interpolator) vs Newton from T = 750/197 fm^-1, mu = 0"}
+    gc.close()
     line = {"metric": "EoS inversions/s (2M states, synthetic 4-D table 151x41^3, energy mode)",
             "workload": "eos-table", "value": n_rows / (ms * 1e-3), "unit": "inversions/s",
             "ms_per_batch": ms, "rows": n_rows, "steps": args.steps, "warmup": args.warmup, "dtype": "f64",
             "seed": "reference chain (580 MeV forced seed, conformal-diagonal analytic seed)",
-            "learned_seed": learned,
+            "learned_seed": learned, "preinverted_tables": preinv,
             "iterations": {"mean": float(it.mean()), "p99": float(np.percentile(it, 99)), "max": int(it.max())},
             "table_rate": float(tab.mean()), "fallback_rate": float(np.mean(st > 0)),
             "fail_rate": float(np.mean(st < 0)),

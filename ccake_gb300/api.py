@@ -89,6 +89,7 @@ def lib():
         L.ccake_preinverted_use.argtypes = [P, _i32]
         L.ccake_preinverted_lookup.argtypes = [P, _i64, _dp, _dp]
         L.ccake_preinverted_copy.argtypes = [P, ctypes.POINTER(_i64), _dp]
+        L.ccake_preinverted_lookup_device.argtypes = [P, _i64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         L.ccake_hydro_numbers.argtypes = [P]
         L.ccake_write_system_state.argtypes = [P, ctypes.c_char_p]
         L.ccake_ic_read_ccake.argtypes = [ctypes.c_char_p, ctypes.POINTER(IcOptions), ctypes.POINTER(P)]
@@ -206,6 +207,11 @@ class GpuHydro:
         out = np.zeros((a.shape[0], 11))
         self._check(lib().ccake_preinverted_lookup(self.h, a.shape[0], _d(a), _d(out)), "preinverted_lookup")
         return out
+
+    def preinverted_lookup_device(self, n, in4_ptr, out11_ptr, stream_ptr=None):
+        """ccake_preinverted_lookup_device on device pointers (ints), asynchronous."""
+        self._check(lib().ccake_preinverted_lookup_device(self.h, int(n), in4_ptr, out11_ptr, stream_ptr),
+                    "preinverted_lookup_device")
 
     def preinverted_values(self):
         n = _i64()

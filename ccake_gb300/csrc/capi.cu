@@ -1399,7 +1399,7 @@ ccake_status_t ccake_preinverted_lookup_device(ccake_ctx* ctx, int64_t n, const 
                                                void* stream) {
   if (!ctx || n < 0) return CCAKE_ERR_INVALID;
   if (!ctx->pre_count) return fail(ctx, CCAKE_ERR_STATE, "build the pre-inverted tables first");
-  launch_preinv_lookup(ctx->pre_dev, n, d_sBSQ, d_out11, stream ? (cudaStream_t)stream : ctx->stream);
+  launch_preinv_lookup(ctx->pre_dev, n, d_sBSQ, d_out11, static_cast<cudaStream_t>(stream));
   CK(cudaGetLastError());
   return CCAKE_OK;
 }

@@ -235,7 +235,8 @@ ccake_status_t ccake_preinverted_build(ccake_ctx* ctx, const ccake_preinv_config
 ccake_status_t ccake_preinverted_use(ccake_ctx* ctx, int32_t on);
 /* Lookups of n rows (s, rhoB, rhoS, rhoQ) into out11[n][11], host arrays. */
 ccake_status_t ccake_preinverted_lookup(ccake_ctx* ctx, int64_t n, const double* sBSQ, double* out11);
-/* The same on device arrays, enqueued on stream (NULL: the context's). */
+/* The same on device arrays, enqueued on stream (a cudaStream_t; NULL is
+ * the default stream), as ccake_eos_invert_device. */
 ccake_status_t ccake_preinverted_lookup_device(ccake_ctx* ctx, int64_t n, const double* d_sBSQ, double* d_out11,
                                                void* stream);
 /* count = number of nodes; host (may be NULL) receives count x 11 values,
