@@ -26,7 +26,7 @@ class CcakeConfig(ctypes.Structure):
         [(n, _f64) for n in (
             "hT", "hEta", "t0", "dt", "eos_c", "eos_T0", "eos_muB0", "eos_muQ0", "eos_muS0", "eta_over_s",
             "zeta_over_s", "zeta_cs2_A", "zeta_cs2_p", "zeta_peak_T", "zeta_peak_width", "xmin", "ymin",
-            "etamin", "freeze_out_T", "skin_frac")] + [("particlization", _i32), ("reserved", _i32)]
+            "etamin", "freeze_out_T", "skin_frac")] + [("particlization", _i32), ("surface", _i32)]
 
 
 class ParticlesSoA(ctypes.Structure):
@@ -90,6 +90,8 @@ def lib():
         L.ccake_preinverted_lookup.argtypes = [P, _i64, _dp, _dp]
         L.ccake_preinverted_copy.argtypes = [P, ctypes.POINTER(_i64), _dp]
         L.ccake_preinverted_lookup_device.argtypes = [P, _i64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        L.ccake_freeze_out_rows.argtypes = [P, ctypes.POINTER(_i64), ctypes.POINTER(_i32), _dp]
+        L.ccake_write_freeze_out.argtypes = [P, ctypes.c_char_p, _f64, _f64, _f64]
         L.ccake_hydro_numbers.argtypes = [P]
         L.ccake_write_system_state.argtypes = [P, ctypes.c_char_p]
         L.ccake_ic_read_ccake.argtypes = [ctypes.c_char_p, ctypes.POINTER(IcOptions), ctypes.POINTER(P)]
@@ -219,6 +221,22 @@ class GpuHydro:
         out = np.zeros((n.value, 11))
         self._check(lib().ccake_preinverted_copy(self.h, ctypes.byref(n), _d(out)), "preinverted_copy")
         return out
+
+    def freeze_out_rows(self):
+        """Hypersurface rows so far (cfg.surface): (count, 2 + fields), each
+        step, particle, then the freeze_out.dat fields."""
+        k, w = _i64(), _i32()
+        self._check(lib().ccake_freeze_out_rows(self.h, ctypes.byref(k), ctypes.byref(w), None), "freeze_out_rows")
+        out = np.zeros((k.value, w.value))
+        if k.value:
+            self._check(lib().ccake_freeze_out_rows(self.h, ctypes.byref(k), ctypes.byref(w), _d(out)),
+                        "freeze_out_rows")
+        return out
+
+    def write_freeze_out(self, path, B=0.0, S=0.0, Q=0.0):
+        """freeze_out.dat with the header "# B S Q"."""
+        self._check(lib().ccake_write_freeze_out(self.h, os.fsencode(path), float(B), float(S), float(Q)),
+                    "write_freeze_out")
 
     def hydro_numbers(self):
         """theta, sigma^{ij}, Knudsen and inverse Reynolds numbers and the

@@ -109,8 +109,13 @@ void free_buffers(ccake_ctx* ctx) {
   free_candidates(ctx);
   if (ctx->dbuf) cudaFree(ctx->dbuf);
   if (ctx->ibuf) cudaFree(ctx->ibuf);
+  if (ctx->p.fz) cudaFree(ctx->p.fz);
+  if (ctx->p.fo_rows) cudaFree(ctx->p.fo_rows);
+  if (ctx->p.fo_count) cudaFree(ctx->p.fo_count);
   ctx->dbuf = nullptr;
   ctx->ibuf = nullptr;
+  ctx->p.fz = ctx->p.fo_rows = nullptr;
+  ctx->p.fo_count = nullptr;
 }
 
 // Neighbour-cell grid: the reference's box (twice the IC lower corner,
@@ -219,13 +224,28 @@ ccake_status_t maybe_rebuild(ccake_ctx* ctx, bool graph) {
   return CCAKE_OK;
 }
 
+// The freeze-out stage after a step (SPHWorkstation::freeze_out_particles).
+void enqueue_freeze(ccake_ctx* ctx) {
+  if (ctx->cfg.surface && ctx->p.fz) {
+    // gradients, theta and shv_nabla_u of the evaluation just done, then the
+    // status machine with snapshots and hypersurface rows
+    const int mixed = ctx->cfg.precision == 1 ? 1 : 0;
+    if (mixed) launch_gradients_mixed(ctx->rc, ctx->p, ctx->stream);
+    else launch_passB(ctx->rc, ctx->p, B_GRADS, 0.0, ctx->stream);
+    launch_diagnostics(ctx->rc, ctx->p, mixed, ctx->stream);
+    launch_freeze_surface(ctx->rc, ctx->p, mixed, ctx->cfg.dt, ctx->stream);
+  } else {
+    launch_freeze(ctx->rc, ctx->p, ctx->stream);
+  }
+}
+
 void enqueue_substep(ccake_ctx* ctx, int sub) {
   const double dt = ctx->cfg.dt;
   enqueue_passA(ctx);
   int mode = B_EOM | B_UPDATE | (sub == 2 ? B_WRITE_Y0 : 0);
   enqueue_passB(ctx, mode, sub == 1 ? 0.5 * dt : dt);
   launch_clock(ctx->p, sub, dt, ctx->stream);
-  if (sub == 2 && ctx->cfg.particlization) launch_freeze(ctx->rc, ctx->p, ctx->stream);
+  if (sub == 2 && ctx->cfg.particlization) enqueue_freeze(ctx);
 }
 
 struct FieldRef {
@@ -560,10 +580,22 @@ ccake_status_t ccake_initialize(ccake_ctx* ctx) {
   if (!ctx) return CCAKE_ERR_INVALID;
   if (!ctx->loaded) return fail(ctx, CCAKE_ERR_STATE, "load particles first");
   if (ctx->eos.kind == 2 && !ctx->d_table) return fail(ctx, CCAKE_ERR_STATE, "set the EoS table first");
-  Clock c{ctx->cfg.t0, ctx->cfg.t0, ctx->cfg.t0, 0, 0};
+  Clock c{ctx->cfg.t0, ctx->cfg.t0, ctx->cfg.t0, 0, 0, 0.0, 0.0};
   CK(cudaMemcpyAsync(ctx->p.clock, &c, sizeof(Clock), cudaMemcpyHostToDevice, ctx->stream));
   ccake_status_t s = reset_errors(ctx);
   if (s) return s;
+  if (ctx->cfg.particlization && ctx->cfg.surface) {
+    // freeze-out snapshots (zero, as the reference's freeze_array) and the
+    // hypersurface rows, one a particle at most
+    const size_t n = (size_t)ctx->n;
+    if (!ctx->p.fz && (cudaMalloc(&ctx->p.fz, 6 * NSF * n * sizeof(double)) != cudaSuccess ||
+                       cudaMalloc(&ctx->p.fo_rows, n * kFoRow * sizeof(double)) != cudaSuccess ||
+                       cudaMalloc(&ctx->p.fo_count, sizeof(int32_t)) != cudaSuccess))
+      return fail(ctx, CCAKE_ERR_NOMEM, "freeze-out snapshot allocation");
+    CK(cudaMemsetAsync(ctx->p.fz, 0, 6 * NSF * n * sizeof(double), ctx->stream));
+    CK(cudaMemsetAsync(ctx->p.fo_count, 0, sizeof(int32_t), ctx->stream));
+    drop_graph(ctx);
+  }
   // neighbour-list capacity: 1.5x the largest initial neighbour count + 16
   // (pass A flags an overflow, reported as CCAKE_ERR_CAPACITY)
   {
@@ -695,7 +727,7 @@ ccake_status_t ccake_profile_phases(ccake_ctx* ctx, int32_t n_steps, double* ms3
       enqueue_passB(ctx, B_EOM | B_UPDATE | (sub == 2 ? B_WRITE_Y0 : 0), sub == 1 ? 0.5 * dt : dt);
       CK(cudaEventRecord(ev[3], ctx->stream));
       launch_clock(ctx->p, sub, dt, ctx->stream);
-      if (sub == 2 && ctx->cfg.particlization) launch_freeze(ctx->rc, ctx->p, ctx->stream);
+      if (sub == 2 && ctx->cfg.particlization) enqueue_freeze(ctx);
       if (sub == 2) ctx->steps_since_build++;
       CK(cudaEventSynchronize(ev[3]));
       float m;
@@ -1410,6 +1442,62 @@ ccake_status_t ccake_preinverted_copy(ccake_ctx* ctx, int64_t* count, double* ho
   if (host && ctx->pre_count) {
     CK(cudaMemcpy(host, ctx->pre_v, (size_t)ctx->pre_count * kPreVars * sizeof(double), cudaMemcpyDeviceToHost));
   }
+  return CCAKE_OK;
+}
+
+ccake_status_t ccake_freeze_out_rows(ccake_ctx* ctx, int64_t* count, int32_t* width, double* rows) {
+  if (!ctx || !count || !width) return CCAKE_ERR_INVALID;
+  const int D = ctx->cfg.dim;
+  const int W = D == 2 ? 40 : 45;
+  *width = W + 2;
+  *count = 0;
+  if (!ctx->p.fo_count) return CCAKE_OK;
+  int32_t k = 0;
+  CK(cudaMemcpyAsync(&k, ctx->p.fo_count, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  k = std::min<int32_t>(k, (int32_t)ctx->n);
+  *count = k;
+  if (!rows || k == 0) return CCAKE_OK;
+  std::vector<double> raw((size_t)k * kFoRow);
+  CK(cudaMemcpy(raw.data(), ctx->p.fo_rows, raw.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  // the reference writes a step's rows in particle order (input order here)
+  std::vector<int> ord((size_t)k);
+  std::iota(ord.begin(), ord.end(), 0);
+  auto key = [&](int r) {
+    const double* q = raw.data() + (size_t)r * kFoRow;
+    return std::make_pair((int64_t)q[0], (int64_t)ctx->perm[(size_t)q[1]]);
+  };
+  std::sort(ord.begin(), ord.end(), [&](int a, int b) { return key(a) < key(b); });
+  for (int r = 0; r < k; r++) {
+    const double* q = raw.data() + (size_t)ord[(size_t)r] * kFoRow;
+    double* o = rows + (size_t)r * (W + 2);
+    o[0] = q[0];
+    o[1] = (double)ctx->perm[(size_t)q[1]];
+    for (int c = 0; c < W; c++) o[2 + c] = q[2 + c];
+  }
+  return CCAKE_OK;
+}
+
+ccake_status_t ccake_write_freeze_out(ccake_ctx* ctx, const char* path, double B, double S, double Q) {
+  if (!ctx || !path) return CCAKE_ERR_INVALID;
+  int64_t k = 0;
+  int32_t w = 0;
+  ccake_status_t st = ccake_freeze_out_rows(ctx, &k, &w, nullptr);
+  if (st) return st;
+  std::vector<double> rows((size_t)k * w);
+  if (k && (st = ccake_freeze_out_rows(ctx, &k, &w, rows.data()))) return st;
+  std::ofstream out(path);
+  if (!out.is_open()) return fail(ctx, CCAKE_ERR_INVALID, std::string("cannot write ") + path);
+  // Output::print_freeze_out / flush_freeze_out (src/output.cpp:417-497):
+  // the header "# B S Q", then the rows in the stream's default format
+  out << "# " << B << " " << S << " " << Q << "\n";
+  for (int64_t r = 0; r < k; r++) {
+    const double* q = rows.data() + (size_t)r * w;
+    for (int c = 2; c < w - 1; c++) out << q[c] << " ";
+    out << q[w - 1] << "\n";
+  }
+  out << std::flush;
+  if (!out.good()) return fail(ctx, CCAKE_ERR_INVALID, std::string("write failed: ") + path);
   return CCAKE_OK;
 }
 

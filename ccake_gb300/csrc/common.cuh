@@ -45,7 +45,9 @@ enum DerivSlot : int { D_DU0 = 0, D_DU1, D_DU2, D_DS, D_DBULK, D_DSHV0, D_DSHV1,
                        // diagnostics of the last derivative evaluation (ccake_hydro_numbers):
                        // theta, sigma^{11,12,13,22,23}, shear / bulk Knudsen and inverse
                        // Reynolds numbers
-                       D_THETA, D_SIG0, D_SIG1, D_SIG2, D_SIG3, D_SIG4, D_KNS, D_KNB, D_IRS, D_IRB, NDER };
+                       D_THETA, D_SIG0, D_SIG1, D_SIG2, D_SIG3, D_SIG4, D_KNS, D_KNB, D_IRS, D_IRB,
+                       D_SNU,   // shv_nabla_u = pi^{ij} nabla_i u_j of the last evaluation
+                       NDER };
 
 // Neighbour-record strides (doubles). Record A feeds the smoothing pass,
 // record B the gradient pass; both are rewritten once per substep.
@@ -87,8 +89,21 @@ struct Clock {
   double t;
   double teval;   // time of the last substep-2 derivative evaluation (t0 + dt/2)
   int32_t frzc;   // steps seen by the freeze-out status machine (0, 1, 2 = third and later)
-  int32_t pad;
+  int32_t nstep;  // steps seen by the freeze-out stage (the step of a hypersurface row)
+  double taup, taupp;   // times of the last two freeze-out snapshots (FreezeOut::taup, taupp)
 };
+
+// Freeze-out snapshot fields (FreezeOut::freeze_array, include/freeze_out.h):
+// r[3] u[3] gradP[3] gradE[3] s e rhoB rhoS rhoQ T muB muS muQ theta bulk
+// sigma_lab pi^{mu nu}[10 slots] pi^{33} shv_nabla_u w cs2; six snapshots
+// (frz1 frz2 fback fback2 fback3 fback4), field q of particle i of snapshot k
+// at (k * NSF + q) * n + i.
+enum SnapField : int { SF_R = 0, SF_U = 3, SF_GP = 6, SF_GE = 9, SF_S = 12, SF_E, SF_RB, SF_RS, SF_RQ, SF_T, SF_MUB,
+                       SF_MUS, SF_MUQ, SF_THETA, SF_BULK, SF_SLAB, SF_SHV, SF_SHV33 = SF_SHV + 10, SF_SNU, SF_W, SF_CS2,
+                       NSF };
+// a freeze_out.dat row on the device: step, particle, then the fields
+// (src/output.cpp:433-475), 40 in 2-D, 45 in 3-D
+constexpr int kFoRow = 2 + 45;
 
 // Error counters raised by the kernels (read back by the host after a call).
 enum ErrSlot : int { E_EOS = 0, E_NEGS = 1, E_NONFINITE = 2, E_NBR_OVERFLOW = 3, NERR = 4 };

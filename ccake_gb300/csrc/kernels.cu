@@ -739,6 +739,7 @@ __global__ void k_freeze(RunConst rc, Ptrs p) {
   }
   if (frzc == 1) {
     p.frz1_e[i] = e;
+    if (f == 3) f = 4;   // bsqsvinterpolate in the second step (:559-566)
   } else if (frzc >= 2) {
     if (f < 4 && p.btrack[i] == 0) {
       f = 4;
@@ -748,6 +749,207 @@ __global__ void k_freeze(RunConst rc, Ptrs p) {
     if (f < 4) p.frz1_e[i] = e;
   }
   p.freeze[i] = f;
+}
+
+// The freeze-out stage with the hypersurface (cfg.surface), after a step:
+// check_freeze_out_status (include/freeze_out.h:455-500) and bsqsvfreezeout
+// (:549-615) per particle. Snapshots of every field (first step: frz2;
+// second: frz1; later: the few-neighbour backups and restores of
+// freeze_out_evo, :322-375, the no-neighbour freeze, the interpolation, then
+// frz2 <- frz1 for the live particles and frz1 <- now for all). A particle at
+// status 3 is interpolated (bsqsvinterpolate, :617-936) from the snapshot
+// whose energy is closer to e_FO, its freeze_out.dat row appended
+// (src/output.cpp:433-475; the order of the appends is fixed on the host),
+// and it becomes 4. The current gradients, theta and shv_nabla_u are those
+// of the last derivative evaluation (recomputed before this kernel).
+template <int D>
+__global__ void k_freeze_surface(RunConst rc, Ptrs p, int grads_f32, double dt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.n) return;
+  const int n = p.n;
+  const Clock c = *p.clock;
+  const int frzc = c.frzc;
+  const double ef = rc.efreeze, t = c.t;
+  const double taup = frzc == 1 ? t : c.taup, taupp = c.taupp;
+  auto SN = [&](int k, int q) -> double& { return p.fz[((size_t)k * NSF + q) * n + i]; };
+  auto copy_snap = [&](int dst, int src) {
+    for (int q = 0; q < NSF; q++) SN(dst, q) = SN(src, q);
+  };
+  const float* gf = reinterpret_cast<const float*>(p.grads);
+  auto G = [&](int slot) { return grads_f32 ? double(gf[(size_t)slot * n + i]) : p.grads[(size_t)slot * n + i]; };
+  // the current values
+  double cur[NSF];
+  for (int k = 0; k < 3; k++) {
+    cur[SF_R + k] = k < D ? p.y[(Y_X0 + k) * n + i] : 0.0;
+    cur[SF_U + k] = k < D ? p.y[(Y_U0 + k) * n + i] : 0.0;
+    cur[SF_GP + k] = k < D ? G(G_P + k) : 0.0;
+    cur[SF_GE + k] = k < D ? G(G_E + k) : 0.0;
+  }
+  cur[SF_S] = p.th[T_S * n + i];
+  cur[SF_E] = p.th[T_E * n + i];
+  cur[SF_RB] = p.th[T_RB * n + i];
+  cur[SF_RS] = p.th[T_RS * n + i];
+  cur[SF_RQ] = p.th[T_RQ * n + i];
+  cur[SF_T] = p.th[T_T * n + i];
+  cur[SF_MUB] = p.th[T_MUB * n + i];
+  cur[SF_MUS] = p.th[T_MUS * n + i];
+  cur[SF_MUQ] = p.th[T_MUQ * n + i];
+  cur[SF_THETA] = p.derivs[D_THETA * n + i];
+  cur[SF_BULK] = p.bulk[i];
+  cur[SF_SLAB] = p.slab[i];
+  const int sl[10][2] = {{0, 0}, {0, 1}, {0, 2}, {0, 3}, {1, 1}, {1, 2}, {1, 3}, {2, 2}, {2, 3}, {3, 3}};
+  for (int q = 0; q < 10; q++) cur[SF_SHV + q] = p.pi[pi_slot(sl[q][0], sl[q][1]) * n + i];
+  cur[SF_SHV33] = p.pi[pi_slot(3, 3) * n + i];
+  cur[SF_SNU] = p.derivs[D_SNU * n + i];
+  cur[SF_W] = p.th[T_W * n + i];
+  cur[SF_CS2] = p.th[T_CS2 * n + i];
+  // check_freeze_out_status
+  int f = p.freeze[i];
+  const double e = cur[SF_E];
+  if (f == 0) {
+    if (e <= ef) f = 1;
+  } else if (f == 1) {
+    if (p.btrack[i] == -1) f = 3;
+    else if (e > p.frz1_e[i]) f = 1;
+    else if (e <= ef) f = 3;
+    else f = 0;
+  }
+  // bsqsvinterpolate from snapshot k taken at tp
+  auto interpolate = [&](int k, double tp) {
+    const double tlist = p.btrack[i] != -1 ? tp : tp - dt;
+    const double t2 = tlist * tlist;
+    double uout[3], ucov[3], gP[3], gE[3], gPc[3], gEc[3];
+    for (int a = 0; a < D; a++) {
+      uout[a] = SN(k, SF_U + a);
+      gP[a] = SN(k, SF_GP + a);
+      gE[a] = SN(k, SF_GE + a);
+      ucov[a] = -uout[a];
+      gPc[a] = -gP[a];
+      gEc[a] = -gE[a];
+    }
+    if (rc.cfg.coord == 0 && D == 3) {
+      ucov[2] = uout[2] * -t2;
+      gPc[2] = gP[2] * (-1. / t2);
+      gEc[2] = gE[2] * (-1. / t2);
+    }
+    const double bulk = SN(k, SF_BULK), theta = SN(k, SF_THETA), snu = SN(k, SF_SNU);
+    double sigsub = SN(k, SF_SLAB);
+    double Tfluc = SN(k, SF_T), sFO = SN(k, SF_S);
+    double norm2 = 0.0;
+    for (int a = 0; a < D; a++) norm2 += uout[a] * ucov[a];
+    const double gsub = sqrt(-norm2 + 1);
+    if (rc.cfg.coord == 1) sigsub /= gsub;
+    else sigsub /= gsub * tlist;
+    const double swsub = p.m[i] / sigsub;
+    double divT[3], divE[3], divTc[3];
+    for (int a = 0; a < D; a++) {
+      divT[a] = (1.0 / sFO) * gP[a];
+      divE[a] = gE[a];
+      divTc[a] = (1.0 / sFO) * gPc[a];
+    }
+    const double cs2 = SN(k, SF_CS2), w = SN(k, SF_W);
+    double inner = 0;
+    for (int a = 0; a < D; a++) inner += uout[a] * gP[a];
+    const double divPpress = -(1.0 / gsub) * (cs2 * (w + bulk) * theta - cs2 * snu + inner);
+    double divTtemp = divPpress / sFO;
+    inner = 0;
+    for (int a = 0; a < D; a++) inner += uout[a] * gE[a];
+    double divEener = -(1.0 / gsub) * ((w + bulk) * theta - snu + inner);
+    norm2 = 0;
+    for (int a = 0; a < D; a++) norm2 += divT[a] * divTc[a];
+    double nrm = -sqrt(fabs(divTtemp * divTtemp + norm2));
+    nrm = fabs(nrm) > 1.E-14 ? nrm : 1.E-14;
+    divTtemp /= nrm;
+    for (int a = 0; a < D; a++) divT[a] /= nrm;
+    norm2 = 0;
+    for (int a = 0; a < D; a++) norm2 += divE[a] * gEc[a];
+    double nrmE = -sqrt(fabs(divEener * divEener + norm2));
+    nrmE = fabs(nrmE) > 1.E-14 ? nrmE : 1.E-14;
+    divEener /= nrmE;
+    for (int a = 0; a < D; a++) divE[a] /= nrmE;
+    sFO *= pow(Tfluc * kHbarcGeVfm, 3);
+    Tfluc *= kHbarcGeVfm;
+    const int row = atomicAdd(p.fo_count, 1);
+    if (row >= n) return;   // never: a particle is interpolated once
+    double* r = p.fo_rows + (size_t)row * kFoRow;
+    int w_ = 0;
+    r[w_++] = (double)c.nstep;
+    r[w_++] = (double)i;
+    r[w_++] = divEener;
+    for (int a = 0; a < D; a++) r[w_++] = divE[a];
+    r[w_++] = gsub;
+    for (int a = 0; a < D; a++) r[w_++] = uout[a];
+    r[w_++] = swsub;
+    r[w_++] = bulk;
+    r[w_++] = SN(k, SF_SHV + 0);
+    r[w_++] = SN(k, SF_SHV + 4);
+    r[w_++] = SN(k, SF_SHV + 7);
+    r[w_++] = SN(k, SF_SHV33);
+    r[w_++] = SN(k, SF_SHV + 5);
+    if (D != 2) {
+      r[w_++] = SN(k, SF_SHV + 6);
+      r[w_++] = SN(k, SF_SHV + 8);
+    }
+    r[w_++] = tlist;
+    for (int a = 0; a < D; a++) r[w_++] = SN(k, SF_R + a);
+    const double tail[11] = {sFO, SN(k, SF_E), Tfluc, SN(k, SF_MUB), SN(k, SF_MUS), SN(k, SF_MUQ), w, cs2,
+                             SN(k, SF_RB), SN(k, SF_RS), SN(k, SF_RQ)};
+    for (int a = 0; a < 11; a++) r[w_++] = tail[a];
+    for (int a = 0; a < 12; a++) r[w_++] = 0.0;   // diffusion sector off
+    r[w_++] = (rc.cfg.eos_kind == 2 && p.eos_id[i] == 0) ? 1.0 : 0.0;
+  };
+  auto closer = [&]() { return fabs(SN(0, SF_E) - ef) < fabs(SN(1, SF_E) - ef) ? 0 : 1; };
+  if (frzc == 0) {
+    for (int q = 0; q < NSF; q++) SN(1, q) = cur[q];
+  } else if (frzc == 1) {
+    p.frz1_e[i] = e;
+    for (int q = 0; q < NSF; q++) SN(0, q) = cur[q];
+    if (f == 3) {
+      const int k = closer();
+      interpolate(k, k == 0 ? taup : taupp);
+      f = 4;
+    }
+  } else {
+    const int bt = p.btrack[i];
+    if (f < 4 && bt <= 3 && bt > 0) {
+      copy_snap(5, 3);
+      copy_snap(4, 2);
+      copy_snap(3, 1);
+      copy_snap(2, 0);
+    }
+    if (f < 4 && bt == 0 && SN(2, SF_GP) != 0) {
+      copy_snap(1, 3);
+      copy_snap(0, 2);
+    }
+    if (f < 4 && bt == 0 && SN(2, SF_GP) == 0) {
+      copy_snap(1, 5);
+      copy_snap(0, 4);
+    }
+    if (f < 4 && bt == 0) {
+      f = 4;
+      p.btrack[i] = -1;
+    }
+    if (f == 3) {
+      const int k = closer();
+      interpolate(k, k == 0 ? taup : taupp);
+      f = 4;
+    }
+    if (f < 4) copy_snap(1, 0);
+    for (int q = 0; q < NSF; q++) SN(0, q) = cur[q];
+    if (f < 4) p.frz1_e[i] = e;
+  }
+  p.freeze[i] = f;
+}
+
+__global__ void k_freeze_surface_advance(Clock* c) {
+  if (c->frzc == 0) c->taupp = c->t;
+  else if (c->frzc == 1) c->taup = c->t;
+  else {
+    c->taupp = c->taup;
+    c->taup = c->t;
+  }
+  if (c->frzc < 2) c->frzc++;
+  c->nstep++;
 }
 
 __global__ void k_freeze_advance(Clock* c) {
@@ -798,7 +1000,7 @@ __global__ void k_diag(RunConst rc, Ptrs p, int grads_f32) {
   for (int q = 0; q < NPI; q++) in.pi[q] = p.pi[q * n + i];
   const TransportT<double> k = transport<double>(rc.cfg, th);
   EomOut<double> o;
-  double dg[6];
+  double dg[7];
   eom<D, double>(rc.cfg, k, in, t, o, dg);
   double* dv = p.derivs;
   dv[D_ETA * n + i] = k.eta;
@@ -806,6 +1008,7 @@ __global__ void k_diag(RunConst rc, Ptrs p, int grads_f32) {
   dv[D_ZETA * n + i] = k.zeta;
   dv[D_TAUBULK * n + i] = k.tau_Pi;
   dv[D_THETA * n + i] = dg[0];
+  dv[D_SNU * n + i] = dg[6];
   double kns = 0.0, knb = 0.0, irs = 0.0, irb = 0.0;
   if (rc.cfg.using_shear) {
     for (int q = 0; q < 5; q++) dv[(D_SIG0 + q) * n + i] = dg[1 + q];
@@ -952,6 +1155,13 @@ void launch_freeze(const RunConst& rc, const Ptrs& p, cudaStream_t s) {
 }
 
 void launch_count_frozen(const Ptrs& p, int32_t* out, cudaStream_t s) { k_count_frozen<<<1, 1024, 0, s>>>(p, out); }
+
+void launch_freeze_surface(const RunConst& rc, const Ptrs& p, int grads_f32, double dt, cudaStream_t s) {
+  const int nb = (p.n + kBlock - 1) / kBlock;
+  if (rc.cfg.dim == 3) k_freeze_surface<3><<<nb, kBlock, 0, s>>>(rc, p, grads_f32, dt);
+  else k_freeze_surface<2><<<nb, kBlock, 0, s>>>(rc, p, grads_f32, dt);
+  k_freeze_surface_advance<<<1, 1, 0, s>>>(p.clock);
+}
 
 void launch_diagnostics(const RunConst& rc, const Ptrs& p, int grads_f32, cudaStream_t s) {
   const int nb = (p.n + kBlock - 1) / kBlock;

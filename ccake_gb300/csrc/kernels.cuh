@@ -41,6 +41,9 @@ struct Ptrs {
   // per-substep neighbour list written by pass A, read by pass B (k-major:
   // entry k of particle i at k * n + i); nbr_f is the radial factor of grad W
   double* frz1_e;        // n  energy snapshot of the freeze-out status machine
+  double* fz;            // 6 * NSF * n  freeze-out snapshots (with surface), else null
+  double* fo_rows;       // n * kFoRow   hypersurface rows appended on the device
+  int32_t* fo_count;     // 1            rows written
   float4* posf;          // FP32 copy of the positions (candidate prefilter)
   int32_t* nbr_idx;      // K * n
   double* nbr_f;         // K * n
@@ -106,6 +109,8 @@ void launch_preinv_pack(int64_t count, const double* th16, const int32_t* status
                         cudaStream_t s);
 void launch_preinv_lookup(const PreinvView* P, int64_t n, const double* sBSQ, double* out, cudaStream_t s);
 void launch_diagnostics(const RunConst& rc, const Ptrs& p, int grads_f32, cudaStream_t s);
+// status machine, snapshots and hypersurface rows after a step (cfg.surface)
+void launch_freeze_surface(const RunConst& rc, const Ptrs& p, int grads_f32, double dt, cudaStream_t s);
 // the gradient sums of the mixed pass B alone (no equations of motion)
 void launch_gradients_mixed(const RunConst& rc, const Ptrs& p, cudaStream_t s);
 void launch_eos_batch(const EosDev& eos, int entropy, int seed_mode, int64_t n, const double* in4, double* tbqs,

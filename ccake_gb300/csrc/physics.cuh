@@ -120,8 +120,8 @@ struct EomOut {
 // sector, for one particle at time t.
 // R = double is the plain FP64 form; R = float is the mixed form's EoM (the
 // state update it feeds stays FP64).
-// diag (optional, 6 values): theta and sigma^{11,12,13,22,23}
-// (src/eom_default.cpp:774-807); the hot kernels pass none.
+// diag (optional, 7 values): theta, sigma^{11,12,13,22,23} and
+// shv_nabla_u (src/eom_default.cpp:764-807); the hot kernels pass none.
 template <int D, typename R = double>
 __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, const EomIn<D, R>& in, double td,
                            EomOut<R>& o, R* diag = nullptr) {
@@ -453,6 +453,10 @@ __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, cons
       for (int kk = 0; kk < D; kk++) acc += sigM[sl][kk] * du[kk];
       diag[1 + sl] = acc + sigF[sl];
     }
+    R m3 = R(0.0);
+#pragma unroll
+    for (int i = 0; i < D; i++) m3 += Mnab[i] * du[i];
+    diag[6] = m3 + Fnab;
   }
   // ---- dEz (reference :827-862) ---------------------------------------------
   const R u3 = (D == 3) ? u[2] : R(0.0);

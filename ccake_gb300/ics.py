@@ -62,6 +62,7 @@ class RunConfig:
     freeze_out_T: float = 150.0 / HBARC_MEVFM
     skin_frac: float = 0.0         # candidate-list skin / 2h (0: 0.1), GPU only
     particlization: int = 0        # freeze-out status machine after every step
+    surface: int = 0               # with particlization: the freeze-out hypersurface rows
 
 
 @dataclasses.dataclass

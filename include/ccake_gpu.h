@@ -60,7 +60,9 @@ typedef struct ccake_config {
                                  vmax = max(1, 1/tau) in Milne (x, y, eta_s) coordinates */
   int32_t particlization;     /* run the freeze-out status machine after every step
                                  (include/settings.h particlization_enabled) */
-  int32_t reserved;
+  int32_t surface;            /* with particlization: interpolate the freeze-out
+                                 hypersurface (FreezeOut::bsqsvinterpolate), rows
+                                 of freeze_out.dat, ccake_freeze_out_rows */
 } ccake_config;
 
 /* Host struct-of-arrays particle input, the columns of the reference's
@@ -212,6 +214,16 @@ ccake_status_t ccake_hydro_numbers(ccake_ctx* ctx);
  * 13,23,33}, u (3), gamma, freeze status, EoS name, causality (0: not
  * checked), six diffusion numbers (0: no diffusion sector). */
 ccake_status_t ccake_write_system_state(ccake_ctx* ctx, const char* path);
+
+/* Freeze-out hypersurface rows (cfg.particlization and cfg.surface), one
+ * for each particle interpolated so far (FreezeOut::bsqsvinterpolate,
+ * include/freeze_out.h:617-936): step, particle (input index), then the
+ * fields of a freeze_out.dat row (src/output.cpp:433-475; 40 in 2-D, 45 in
+ * 3-D), ordered by step, then particle. width = fields + 2; rows may be NULL
+ * (count and width only). */
+ccake_status_t ccake_freeze_out_rows(ccake_ctx* ctx, int64_t* count, int32_t* width, double* rows);
+/* freeze_out.dat (Output::flush_freeze_out): "# B S Q", then the rows. */
+ccake_status_t ccake_write_freeze_out(ccake_ctx* ctx, const char* path, double B, double S, double Q);
 
 /* ---- pre-inverted (s, rhoB, rhoS, rhoQ) -> thermodynamics tables ---------
  * The reference's EoS_Interpolator (include/eos_interpolator.h:33-165,

@@ -258,4 +258,16 @@ void orc_eos_set_thermo(const Config* c, void* tab, int chain_index, const doubl
   eos_set_thermo(*c, (Table*)tab, chain_index, tbqs, th16);
 }
 
+
+int orc_fo_count(void* hp) { return (int)((Handle*)hp)->s.fo_rows.size(); }
+int orc_fo_width(void* hp) {
+  const auto& r = ((Handle*)hp)->s.fo_rows;
+  return r.empty() ? 0 : (int)r[0].size();
+}
+void orc_fo_rows(void* hp, double* out) {
+  size_t k = 0;
+  for (const auto& row : ((Handle*)hp)->s.fo_rows)
+    for (double v : row) out[k++] = v;
+}
+
 }  // extern "C"

@@ -655,16 +655,153 @@ void rk2_step(System& s, NbrList& nl) {
   if (s.cfg.particlization) freeze_out_status(s);
 }
 
-// Freeze-out status machine after a step: FreezeOut::check_freeze_out_status
-// (include/freeze_out.h:455-500), then bsqsvfreezeout (:549-615) without the
-// hypersurface output: from the third step on, particles without neighbours
-// freeze (freeze_out_evo, :322-375), status 3 becomes 4 (bsqsvinterpolate,
-// :914), and the energy of the live particles is snapshotted.
+// Freeze-out after a step (include/freeze_out.h; src/sph_workstation.cpp:1475-1486,
+// freeze_out_particles): FreezeOut::check_freeze_out_status (:455-500), then
+// bsqsvfreezeout (:549-615). Without cfg.surface only the energy of the
+// snapshots is kept (what the status machine reads); with it every snapshot
+// field, the backups of few-neighbour particles (freeze_out_evo, :322-375),
+// and the hypersurface element of each particle that freezes
+// (bsqsvinterpolate, :617-936), written as a freeze_out.dat row
+// (src/output.cpp:417-482).
+namespace {
+
+void take_snapshot(const System& s, int a, double* out, int n) {
+  const int D = s.cfg.dim;
+  auto O = [&](int q) -> double& { return out[(size_t)q * n + a]; };
+  for (int k = 0; k < 3; k++) {
+    O(SF_R + k) = k < D ? s.r[k][a] : 0.0;
+    O(SF_U + k) = k < D ? s.u[k][a] : 0.0;
+    O(SF_GP + k) = k < D ? s.gradP[k][a] : 0.0;
+    O(SF_GE + k) = k < D ? s.gradE[k][a] : 0.0;
+  }
+  O(SF_S) = s.th[kS][a];
+  O(SF_E) = s.th[kE][a];
+  O(SF_RB) = s.th[kRhoB][a];
+  O(SF_RS) = s.th[kRhoS][a];
+  O(SF_RQ) = s.th[kRhoQ][a];
+  O(SF_T) = s.th[kT][a];
+  O(SF_MUB) = s.th[kMuB][a];
+  O(SF_MUS) = s.th[kMuS][a];
+  O(SF_MUQ) = s.th[kMuQ][a];
+  O(SF_THETA) = s.theta[a];
+  O(SF_BULK) = s.bulk[a];
+  O(SF_SLAB) = s.sigma_lab[a];
+  const int sl[10][2] = {{0, 0}, {0, 1}, {0, 2}, {0, 3}, {1, 1}, {1, 2}, {1, 3}, {2, 2}, {2, 3}, {3, 3}};
+  for (int q = 0; q < 10; q++) O(SF_SHV + q) = s.shv[sl[q][0] * 4 + sl[q][1]][a];
+  O(SF_SHV33) = s.shv[15][a];
+  O(SF_SNU) = s.shv_nabla_u[a];
+  O(SF_W) = s.th[kW][a];
+  O(SF_CS2) = s.th[kCs2][a];
+}
+
+void copy_snapshot(std::vector<double>& dst, const std::vector<double>& src, int a, int n) {
+  for (int q = 0; q < NSF; q++) dst[(size_t)q * n + a] = src[(size_t)q * n + a];
+}
+
+// bsqsvinterpolate for particle a (status 3), from snapshot S taken at tp
+void interpolate(System& s, int a, const std::vector<double>& Sv, double tp) {
+  const int D = s.cfg.dim, n = s.n;
+  auto S = [&](int q) { return Sv[(size_t)q * n + a]; };
+  const double tlist = s.btrack[a] != -1 ? tp : tp - s.cfg.dt;
+  const double t2 = tlist * tlist;
+  double uout[3], ucov[3], gP[3], gE[3], gPc[3], gEc[3];
+  for (int k = 0; k < D; k++) {
+    uout[k] = S(SF_U + k);
+    gP[k] = S(SF_GP + k);
+    gE[k] = S(SF_GE + k);
+    ucov[k] = -uout[k];
+    gPc[k] = -gP[k];
+    gEc[k] = -gE[k];
+  }
+  if (s.cfg.coord == 0 && D == 3) {   // milne::Vector make_covariant / make_contravariant
+    ucov[2] = uout[2] * -t2;
+    gPc[2] = gP[2] * (-1. / t2);
+    gEc[2] = gE[2] * (-1. / t2);
+  }
+  const double bulk = S(SF_BULK), theta = S(SF_THETA), snu = S(SF_SNU);
+  double sigsub = S(SF_SLAB);
+  const double Efluc = S(SF_E);
+  double Tfluc = S(SF_T), sFO = S(SF_S);
+  double norm2 = 0.0;
+  for (int k = 0; k < D; k++) norm2 += uout[k] * ucov[k];
+  const double gsub = std::sqrt(-norm2 + 1);
+  if (s.cfg.coord == 1) sigsub /= gsub;
+  else sigsub /= gsub * tlist;
+  const double swsub = s.mass[0][a] / sigsub;
+  double divT[3], divE[3], divTc[3];
+  for (int k = 0; k < D; k++) {
+    divT[k] = (1.0 / sFO) * gP[k];
+    divE[k] = gE[k];
+    divTc[k] = (1.0 / sFO) * gPc[k];
+  }
+  const double cs2 = S(SF_CS2), w = S(SF_W);
+  double inner = 0;
+  for (int k = 0; k < D; k++) inner += uout[k] * gP[k];
+  const double divPpress = -(1.0 / gsub) * (cs2 * (w + bulk) * theta - cs2 * snu + inner);
+  double divTtemp = divPpress / sFO;
+  inner = 0;
+  for (int k = 0; k < D; k++) inner += uout[k] * gE[k];
+  double divEener = -(1.0 / gsub) * ((w + bulk) * theta - snu + inner);
+  norm2 = 0;
+  for (int k = 0; k < D; k++) norm2 += divT[k] * divTc[k];
+  const double insub = divTtemp * divTtemp + norm2;
+  double nrm = -std::sqrt(std::fabs(insub));
+  nrm = std::fabs(nrm) > 1.E-14 ? nrm : 1.E-14;
+  divTtemp /= nrm;
+  for (int k = 0; k < D; k++) divT[k] /= nrm;
+  norm2 = 0;
+  for (int k = 0; k < D; k++) norm2 += divE[k] * gEc[k];
+  const double insubE = divEener * divEener + norm2;
+  double nrmE = -std::sqrt(std::fabs(insubE));
+  nrmE = std::fabs(nrmE) > 1.E-14 ? nrmE : 1.E-14;
+  divEener /= nrmE;
+  for (int k = 0; k < D; k++) divE[k] /= nrmE;
+  sFO *= std::pow(Tfluc * 0.1973269804, 3);
+  Tfluc *= 0.1973269804;
+  // the row of freeze_out.dat (src/output.cpp:433-475)
+  std::vector<double> row = {(double)s.nstep, (double)a, divEener};
+  for (int k = 0; k < D; k++) row.push_back(divE[k]);
+  row.push_back(gsub);
+  for (int k = 0; k < D; k++) row.push_back(uout[k]);
+  row.push_back(swsub);
+  row.push_back(bulk);
+  row.push_back(S(SF_SHV + 0));   // (0,0)
+  row.push_back(S(SF_SHV + 4));   // (1,1)
+  row.push_back(S(SF_SHV + 7));   // (2,2)
+  row.push_back(S(SF_SHV33));
+  row.push_back(S(SF_SHV + 5));   // (1,2)
+  if (D != 2) {
+    row.push_back(S(SF_SHV + 6));  // (1,3)
+    row.push_back(S(SF_SHV + 8));  // (2,3)
+  }
+  row.push_back(tlist);
+  for (int k = 0; k < D; k++) row.push_back(S(SF_R + k));
+  for (double v : {sFO, Efluc, Tfluc, S(SF_MUB), S(SF_MUS), S(SF_MUQ), S(SF_W), cs2, S(SF_RB), S(SF_RS), S(SF_RQ)})
+    row.push_back(v);
+  for (int k = 0; k < 12; k++) row.push_back(0.0);   // diffusion sector off
+  row.push_back(s.eos_id[a] >= 0 && s.cfg.eos_kind == 2 && s.eos_id[a] == 0 ? 1.0 : 0.0);
+  s.fo_rows.push_back(row);
+}
+
+}  // namespace
+
 void freeze_out_status(System& s) {
   const double ef = s.efcheck;
-  const int frzc = s.frzc;
-  if ((int)s.frz1_e.size() != s.n) s.frz1_e.assign(s.n, 0.0);
-  for (int a = 0; a < s.n; a++) {
+  const int frzc = s.frzc, n = s.n;
+  const bool surf = s.cfg.surface != 0;
+  if ((int)s.frz1_e.size() != n) s.frz1_e.assign(n, 0.0);
+  if (surf && (int)s.snap[0].size() != NSF * n)
+    for (int k = 0; k < 6; k++) s.snap[k].assign((size_t)NSF * n, 0.0);
+  std::vector<double>&frz1 = s.snap[0], &frz2 = s.snap[1], &fb1 = s.snap[2], &fb2 = s.snap[3], &fb3 = s.snap[4],
+      &fb4 = s.snap[5];
+  const double t = s.t;
+  // times of the snapshots as the interpolation sees them (the second step
+  // sets taup before interpolating)
+  const double taup = frzc == 1 ? t : s.taup, taupp = s.taupp;
+  std::vector<double> cur;
+  if (surf) cur.assign((size_t)NSF * n, 0.0);
+  for (int a = 0; a < n; a++) {
+    // check_freeze_out_status
     int f = s.freeze[a];
     const double e = s.th[kE][a];
     if (f == 0) {
@@ -675,19 +812,65 @@ void freeze_out_status(System& s) {
       else if (e <= ef) f = 3;
       else f = 0;
     }
-    if (frzc == 1) {
+    if (surf) take_snapshot(s, a, cur.data(), n);
+    // bsqsvfreezeout
+    if (frzc == 0) {
+      if (surf) copy_snapshot(frz2, cur, a, n);
+    } else if (frzc == 1) {
       s.frz1_e[a] = e;
-    } else if (frzc >= 2) {
-      if (f < 4 && s.btrack[a] == 0) {
+      if (surf) copy_snapshot(frz1, cur, a, n);
+      if (f == 3) {
+        if (surf) {
+          const double d1 = std::fabs(frz1[(size_t)SF_E * n + a] - ef), d2 = std::fabs(frz2[(size_t)SF_E * n + a] - ef);
+          interpolate(s, a, d1 < d2 ? frz1 : frz2, d1 < d2 ? taup : taupp);
+        }
+        f = 4;
+      }
+    } else {
+      const int bt = s.btrack[a];
+      if (surf) {
+        if (f < 4 && bt <= 3 && bt > 0) {
+          copy_snapshot(fb4, fb2, a, n);
+          copy_snapshot(fb3, fb1, a, n);
+          copy_snapshot(fb2, frz2, a, n);
+          copy_snapshot(fb1, frz1, a, n);
+        }
+        if (f < 4 && bt == 0 && fb1[(size_t)SF_GP * n + a] != 0) {
+          copy_snapshot(frz2, fb2, a, n);
+          copy_snapshot(frz1, fb1, a, n);
+        }
+        if (f < 4 && bt == 0 && fb1[(size_t)SF_GP * n + a] == 0) {
+          copy_snapshot(frz2, fb4, a, n);
+          copy_snapshot(frz1, fb3, a, n);
+        }
+      }
+      if (f < 4 && bt == 0) {
         f = 4;
         s.btrack[a] = -1;
       }
-      if (f == 3) f = 4;
+      if (f == 3) {
+        if (surf) {
+          const double d1 = std::fabs(frz1[(size_t)SF_E * n + a] - ef), d2 = std::fabs(frz2[(size_t)SF_E * n + a] - ef);
+          interpolate(s, a, d1 < d2 ? frz1 : frz2, d1 < d2 ? taup : taupp);
+        }
+        f = 4;
+      }
+      if (surf) {
+        if (f < 4) copy_snapshot(frz2, frz1, a, n);
+        copy_snapshot(frz1, cur, a, n);
+      }
       if (f < 4) s.frz1_e[a] = e;
     }
     s.freeze[a] = f;
   }
+  if (frzc == 0) s.taupp = t;
+  else if (frzc == 1) s.taup = t;
+  else {
+    s.taupp = s.taup;
+    s.taup = t;
+  }
   s.frzc = frzc < 2 ? frzc + 1 : 2;
+  s.nstep++;
 }
 
 // src/system_state.cpp:738-885 (entropy, BSQ, energy totals) without the

@@ -51,8 +51,16 @@ struct Config {
   double xmin, ymin, etamin;              // lower corner of the IC grid
   double freeze_out_T;                    // fm^-1
   int32_t particlization;                 // freeze-out status machine after every step
-  int32_t pad2;
+  int32_t surface;                        // with particlization: the freeze-out hypersurface
 };
+
+// Freeze-out snapshot of one step (FreezeOut::freeze_array,
+// include/freeze_out.h:20-80): per particle r[3] u[3] gradP[3] gradE[3]
+// s e rhoB rhoS rhoQ T muB muS muQ theta bulk sigma_lab pi^{mu nu}[10]
+// pi^{33} shv_nabla_u w cs2.
+enum SnapField : int { SF_R = 0, SF_U = 3, SF_GP = 6, SF_GE = 9, SF_S = 12, SF_E, SF_RB, SF_RS, SF_RQ, SF_T, SF_MUB,
+                       SF_MUS, SF_MUQ, SF_THETA, SF_BULK, SF_SLAB, SF_SHV, SF_SHV33 = SF_SHV + 10, SF_SNU, SF_W, SF_CS2,
+                       NSF };
 
 // Per-particle state, struct of arrays.
 struct System {
@@ -72,6 +80,14 @@ struct System {
   std::vector<double> frz1_e;
   int frzc = 0;
   double efcheck = 0;
+  // hypersurface (cfg.surface): snapshots frz1, frz2, fback, fback2, fback3,
+  // fback4 (NSF x n each), the times of the last two steps, the step count,
+  // and the rows of freeze_out.dat in the order they are written (each with
+  // its step and particle index in front)
+  std::vector<double> snap[6];
+  double taup = 0, taupp = 0;
+  int nstep = 0;
+  std::vector<std::vector<double>> fo_rows;
   // input
   std::vector<double> in_e, in_s, in_rho[3], in_bulk;
   std::vector<double> in_shv[6];    // pi^{xx},xy,xeta,yy,yeta,etaeta (fm^-4..)

@@ -23,7 +23,7 @@ class Config(ctypes.Structure):
         "hT", "hEta", "t0", "dt", "eos_c", "eos_T0", "eos_muB0", "eos_muQ0", "eos_muS0",
         "eta_over_s", "zeta_over_s", "zeta_cs2_A", "zeta_cs2_p", "zeta_peak_T",
         "zeta_peak_width", "xmin", "ymin", "etamin", "freeze_out_T")] + [
-        ("particlization", ctypes.c_int32), ("pad2", ctypes.c_int32)]
+        ("particlization", ctypes.c_int32), ("surface", ctypes.c_int32)]
 
 
 def make_config(rc) -> Config:
@@ -57,6 +57,10 @@ def lib():
         L.orc_destroy.argtypes = [P]
         L.orc_initialize.argtypes = [P]
         L.orc_step.argtypes = [P, I]
+        L.orc_fo_count.argtypes = [P]
+        L.orc_fo_width.argtypes = [P]
+        L.orc_fo_rows.argtypes = [P, dp]
+        L.orc_fo_rows.restype = None
         L.orc_phase.argtypes = [P, ctypes.c_char_p]
         L.orc_time.restype = D
         L.orc_time.argtypes = [P]
@@ -116,6 +120,15 @@ class OracleRun:
 
     def phase(self, name):
         return lib().orc_phase(self.h, name.encode())
+
+    def freeze_out_rows(self):
+        """Rows of freeze_out.dat written so far, each (step, particle, fields...)."""
+        L = lib()
+        k, w = L.orc_fo_count(self.h), L.orc_fo_width(self.h)
+        out = np.zeros((k, w))
+        if k:
+            L.orc_fo_rows(self.h, _dp(out))
+        return out
 
     @property
     def t(self):

@@ -343,3 +343,39 @@ def test_hydro_numbers_and_system_state_file(tmp_path):
     assert {r[38] for r in rows} == {"conformal_diagonal"}
     assert [int(r[37]) for r in rows] == list(gpu.get_int("freeze")) and {r[39] for r in rows} == {"0"}
     assert not np.any(col(4)) and not np.any(col(35)) and not np.any(col(45))
+
+
+@pytest.mark.parametrize("case,precision", [("gubser", 0), ("hotspots", 0), ("gubser", 1)])
+def test_freeze_out_hypersurface_matches_oracle(tmp_path, case, precision):
+    # FreezeOut::bsqsvinterpolate (include/freeze_out.h:617-936): the rows of
+    # freeze_out.dat of the particles that freeze, against the oracle's
+    # restatement (ideal Gubser flow with T_FO = 1 fm^-1: 36 rows; the viscous
+    # hot spots with T_FO = 0.3 GeV: 7); the mixed form at its tolerance
+    if case == "gubser":
+        p, rc = ics.gubser_2d(n_side=40)
+        rc = dataclasses.replace(rc, freeze_out_T=1.0)
+        nmin = 30
+    else:
+        p, rc = ics.hotspots_2d(n_side=40, n_hot=4, seed=11)
+        rc = dataclasses.replace(rc, freeze_out_T=0.3 / 0.1973269804)
+        nmin = 5
+    rc = dataclasses.replace(rc, particlization=1, surface=1, precision=precision)
+    gpu = api.GpuHydro(rc)
+    gpu.load(p)
+    orc = O.OracleRun(p, rc)
+    gpu.initialize()
+    orc.initialize()
+    for _ in range(3):
+        gpu.step(4)
+        assert orc.step(4) == 0
+    rg, ro = gpu.freeze_out_rows(), orc.freeze_out_rows()
+    assert ro.shape[0] >= nmin and rg.shape == ro.shape
+    assert np.array_equal(rg[:, :2], ro[:, :2])
+    tol = 1e-9 if precision == 0 else 2e-4
+    scale = np.abs(ro) + 1e-6 * np.max(np.abs(ro), axis=0) + 1e-300
+    assert np.max(np.abs(rg - ro) / scale) < tol
+    path = tmp_path / "freeze_out.dat"
+    gpu.write_freeze_out(path, 1.0, 2.0, 3.0)
+    lines = path.read_text().splitlines()
+    assert lines[0] == "# 1 2 3" and len(lines) == 1 + rg.shape[0]
+    assert all(len(ln.split()) == 40 for ln in lines[1:])
