@@ -201,7 +201,7 @@ void enqueue_build(ccake_ctx* ctx) {
 // construction, v^eta < 1/tau), so no pair can close from beyond 2h + skin to
 // within 2h while R dt vmax <= skin / 2.
 int build_every(const ccake_ctx* ctx, double tau) {
-  const double vmax = ctx->cfg.dim == 3 ? std::max(1.0, 1.0 / tau) : 1.0;
+  const double vmax = (ctx->cfg.dim == 3 && ctx->cfg.coord == 0) ? std::max(1.0, 1.0 / tau) : 1.0;
   return std::max(1, (int)std::floor(ctx->skin / (2.0 * ctx->cfg.dt * vmax)));
 }
 
@@ -439,7 +439,7 @@ ccake_status_t ccake_ctx_create(const ccake_config* cfg, ccake_ctx** out) {
   if (!cfg || !out) return CCAKE_ERR_INVALID;
   *out = nullptr;
   if (cfg->dim != 2 && cfg->dim != 3) return CCAKE_ERR_INVALID;
-  if (cfg->coord != 0) return CCAKE_ERR_INVALID;
+  if (cfg->coord != 0 && cfg->coord != 1) return CCAKE_ERR_INVALID;
   if (cfg->eos_kind < 0 || cfg->eos_kind > 2) return CCAKE_ERR_INVALID;
   if (cfg->precision != 0 && cfg->precision != 1) return CCAKE_ERR_INVALID;
   if (!(cfg->skin_frac >= 0.0)) return CCAKE_ERR_INVALID;
@@ -458,7 +458,7 @@ ccake_status_t ccake_ctx_create(const ccake_config* cfg, ccake_ctx** out) {
   rc.cut2 = (2.0 * h) * (2.0 * h);
   // skin: at least one RK2 step of travel at the largest coordinate speed
   // (tau only grows from t0), so that a list lasts a step or more
-  const double vmax0 = D == 3 ? std::max(1.0, 1.0 / cfg->t0) : 1.0;
+  const double vmax0 = (D == 3 && cfg->coord == 0) ? std::max(1.0, 1.0 / cfg->t0) : 1.0;
   ctx->skin = std::max((cfg->skin_frac > 0.0 ? cfg->skin_frac : 0.1) * 2.0 * h, 2.0 * cfg->dt * vmax0 * (1.0 + 1e-6));
   rc.cutc2 = (2.0 * h + ctx->skin) * (2.0 * h + ctx->skin);
   rc.inv_h = 1.0 / h;

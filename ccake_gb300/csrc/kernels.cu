@@ -318,18 +318,28 @@ __global__ void __launch_bounds__(kBlock) k_passA(RunConst rc, EosDev eos, Ptrs 
     }
   }
   if (nn > K) atomicAdd(&p.err[E_NBR_OVERFLOW], 1);
-  // gamma and v from u (update_velocity), LRF densities (get_LRF = lab/(gamma t))
+  // gamma and v from u (update_velocity), LRF densities (get_LRF: lab/(gamma t)
+  // in Milne coordinates, lab/gamma in Cartesian ones)
+  const double tm = rc.cfg.coord == 1 ? 1.0 : t;
   const double u3[3] = {p.y[Y_U0 * n + i], p.y[Y_U1 * n + i], D == 3 ? p.y[Y_U2 * n + i] : 0.0};
-  const double g = gamma_milne<D>(u3, t * t);
+  const double g = gamma_milne<D>(u3, tm * tm);
   p.gam[i] = g;
 #pragma unroll
   for (int q = 0; q < 3; q++) p.v[q * n + i] = (q < D) ? u3[q] / g : 0.0;
   p.slab[i] = sl;
-  p.sig[i] = sl / g / t;
-  p.th[T_S * n + i] = s0 / g / t;
-  p.th[T_RB * n + i] = s1 / g / t;
-  p.th[T_RS * n + i] = s2 / g / t;
-  p.th[T_RQ * n + i] = s3 / g / t;
+  if (rc.cfg.coord == 1) {
+    p.sig[i] = sl / g;
+    p.th[T_S * n + i] = s0 / g;
+    p.th[T_RB * n + i] = s1 / g;
+    p.th[T_RS * n + i] = s2 / g;
+    p.th[T_RQ * n + i] = s3 / g;
+  } else {
+    p.sig[i] = sl / g / t;
+    p.th[T_S * n + i] = s0 / g / t;
+    p.th[T_RB * n + i] = s1 / g / t;
+    p.th[T_RS * n + i] = s2 / g / t;
+    p.th[T_RQ * n + i] = s3 / g / t;
+  }
   p.btrack[i] = nn;
   if (mode == A_WITH_THERMO) thermo_tail<D, false>(rc, eos, p, i, t);
 }
@@ -471,7 +481,7 @@ __global__ void k_init_state(RunConst rc, Ptrs p) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= p.n) return;
   const int n = p.n;
-  const double t = p.clock->t;
+  const double t = rc.cfg.coord == 1 ? 1.0 : p.clock->t;   // the metric's tau (1 in Cartesian coordinates)
   const double u3[3] = {p.y[Y_U0 * n + i], p.y[Y_U1 * n + i], D == 3 ? p.y[Y_U2 * n + i] : 0.0};
   const double g = gamma_milne<D>(u3, t * t);
   p.gam[i] = g;
@@ -972,7 +982,8 @@ __global__ void k_diag(RunConst rc, Ptrs p, int grads_f32) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= p.n) return;
   const int n = p.n;
-  const double t = p.clock->teval, t2 = t * t;
+  const double t = p.clock->teval;
+  const double t2 = rc.cfg.coord == 1 ? 1.0 : t * t;
   double th[NTH];
 #pragma unroll
   for (int q = 0; q < NTH; q++) th[q] = p.th[q * n + i];

@@ -175,12 +175,13 @@ __global__ void __launch_bounds__(kBlock) k_passA_mixed(RunConst rc, Ptrs p) {
   if (!live) return;
   if (nn > K) atomicAdd(&p.err[E_NBR_OVERFLOW], 1);
   const double u3[3] = {p.y[Y_U0 * n + i], p.y[Y_U1 * n + i], D == 3 ? p.y[Y_U2 * n + i] : 0.0};
-  const double g = gamma_milne<D>(u3, t * t);
+  const double tm = rc.cfg.coord == 1 ? 1.0 : t;   // the metric's tau (1 in Cartesian coordinates)
+  const double g = gamma_milne<D>(u3, tm * tm);
   p.gam[i] = g;
 #pragma unroll
   for (int q = 0; q < 3; q++) p.v[q * n + i] = (q < D) ? u3[q] / g : 0.0;
   const double slab = sl.value64();
-  const double igt = 1.0 / (g * t);
+  const double igt = 1.0 / (g * tm);
   p.slab[i] = slab;
   p.sig[i] = slab * igt;
   p.th[T_S * n + i] = s0.value64() * igt;

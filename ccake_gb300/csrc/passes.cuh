@@ -130,7 +130,7 @@ __device__ __forceinline__ void write_recAf(const Ptrs& p, int i, const double* 
 template <int D, bool MIX>
 __device__ __forceinline__ void thermo_tail(const RunConst& rc, const EosDev& eos, const Ptrs& p, int i, double t) {
   const int n = p.n;
-  const double t2 = t * t;
+  const double t2 = rc.cfg.coord == 1 ? 1.0 : t * t;   // the metric's tau^2 (1 in Cartesian coordinates)
   double th[NTH];
   double x[4] = {p.th[T_T * n + i], p.th[T_MUB * n + i], p.th[T_MUQ * n + i], p.th[T_MUS * n + i]};
   const double tgt[4] = {p.th[T_S * n + i], p.th[T_RB * n + i], p.th[T_RS * n + i], p.th[T_RQ * n + i]};

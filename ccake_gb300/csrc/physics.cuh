@@ -127,11 +127,17 @@ __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, cons
                            EomOut<R>& o, R* diag = nullptr) {
   R sigF[5] = {0, 0, 0, 0, 0}, sigM[5][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
   const R t = R(td);
-  const R t2 = t * t;
+  // Cartesian coordinates (coord = 1, src/eom_cartesian.cpp:210-1400): the
+  // metric without tau (tm = 1) and none of the Milne connection terms (1/tau
+  // sources, the geometric factor, the eta deltas; ch = 0, itc = 0)
+  const bool cart = cfg.coord == 1;
+  const R tm = cart ? R(1.0) : t, ch = cart ? R(0.0) : R(1.0);
+  const R t2 = tm * tm;
   const R g = in.g, sig = in.sigma;
   // reciprocals: FP64 division is a long instruction sequence on the scarce
   // FP64 pipe, so each divisor is inverted once
   const R ig = R(1.0) / g, it = R(1.0) / t, it2 = R(1.0) / t2;
+  const R itc = cart ? R(0.0) : it, itm = cart ? R(1.0) : it;
   const R k13 = R(1.0) / R(3.0), k16 = R(1.0) / R(6.0);
   const double* th = in.th;
   const R T = R(th[T_T]), w = R(th[T_W]), sden = R(th[T_S]), dwds = R(th[T_DWDS]);
@@ -146,16 +152,16 @@ __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, cons
 #pragma unroll
   for (int i = 0; i < D; i++) divV += in.gradV[i * D + i];
   const R uD = u[D - 1];
-  const R geo = (D == 3) ? uD * uD * t * ig : R(0.0);
-  const R expn = g * divV + g * it + geo;
-  auto dEta = [](int i) { return (D == 3 && i == 2) ? R(1.0) : R(0.0); };
+  const R geo = (D == 3 && !cart) ? uD * uD * t * ig : R(0.0);
+  const R expn = g * divV + g * itc + geo;
+  auto dEta = [cart](int i) { return (!cart && D == 3 && i == 2) ? R(1.0) : R(0.0); };
 
   // ---- shear MRFs --------------------------------------------------------
   R M0i[9] = {0}, F0i[3] = {0}, Mnab[3] = {0}, Fnab = R(0.0);
   R Mext[5][3] = {{0}}, Fext[5] = {0};
   R ss = R(0.0);   // pi^{mu nu} pi_{mu nu}
   if (cfg.using_shear) {
-    const R cmd[4] = {R(1.0), -R(1.0), -R(1.0), -R(1.0) * it * it};
+    const R cmd[4] = {R(1.0), -R(1.0), -R(1.0), -R(1.0) * itm * itm};
     const R eta = k.eta, phi6 = k.phi6, phi7 = k.phi7, lpP = k.lambda_piPi;
     const R tpp = k.tau_pipi, dpp = k.delta_pipi, tpi = k.tau_pi;
     const R tdelta = dpp - tpi;
@@ -234,15 +240,15 @@ __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, cons
       R Fds = -(vgs[i] - ggs[i] - R(4.) * g * u[i] * sgu_s * k13 - sgu[i] + vsg[i]) / R(4.) +
                    (hy[i + 1][0] - g * g * hy[i + 1][0] - g * u[i] * hy[0][0] + pi[0][i + 1] +
                     R(4.) * u[i] * g * hy[0][0] * k13) * geo / R(4.) +
-                   (g * cmd[i + 1] * hy[0][3] * di * it + g * pi[3][0] * di * it + R(4.) * g * u[i] * (g * hy[3][3] * it) * k13) / R(4.) -
-                   pi[0][i + 1] * (g * it + geo + g * divV) * k13;
+                   ch * ((g * cmd[i + 1] * hy[0][3] * di * it + g * pi[3][0] * di * it + R(4.) * g * u[i] * (g * hy[3][3] * it) * k13) / R(4.)) -
+                   pi[0][i + 1] * (g * itc + geo + g * divV) * k13;
       R Fdo = -(vgs[i] - ggs[i] + sgu[i] - vsg[i]) / R(4.) +
                    (hy[i + 1][0] - g * g * hy[i + 1][0] - g * u[i] * hy[0][0] - pi[0][i + 1]) * geo / R(4.) +
                    (g * cmd[i + 1] * hy[0][3] * di * it - g * pi[3][0] * di * it) / R(4.);
       const R Fdd = pi[i + 1][0] * expn;
       Fs += di * (-(-uD * t - uD * it + g * uD * uD * t + R(2.) * g * g * uD * it) / R(2.));
       FD += di * (uD * pi[0][0] * it + g * pi[3][0] * it);
-      if (D == 3) {
+      if (D == 3 && !cart) {
         Fds += (t * uD * di * cmd[i + 1] * hy[0][0] + uD * hy[i + 1][3] * g * it / R(4.) + hy[i + 1][3] * t * uD +
                 pi[0][0] * di * uD * it + t * uD * uD * (g * hy[i + 1][0] + u[i] * hy[0][0]) +
                 R(2.) * g * uD * (g * hy[i + 1][3] + u[i] * pi[0][3]) * it) / R(4.) +
@@ -280,7 +286,7 @@ __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, cons
       for (int j = 0; j < D; j++) Fnab += (hy[i + 1][j + 1] - v[i] * hy[0][j + 1]) * gu[i][j];
       Fnab += (hy[i + 1][0] - v[i] * hy[0][0]) * gu0[i];
     }
-    Fnab += +hy[3][3] * g * it + hy[0][0] * geo + (t * hy[3][0] + hy[0][3] * it) * uD * dEta(D - 1);
+    Fnab += +ch * (hy[3][3] * g * it) + hy[0][0] * geo + (t * hy[3][0] + hy[0][3] * it) * uD * dEta(D - 1);
     // shear-tensor evolution MRFs on the (i <= j) entries of the 2x3 block
     const R f2 = fu[2];
 #pragma unroll
@@ -304,25 +310,25 @@ __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, cons
         const R cg_ij = (i < D && j < D) ? cgu[i][j] : R(0.0), cg_ji = (i < D && j < D) ? cgu[j][i] : R(0.0);
         R Fsg = cg_ij / R(2.) + cg_ji / R(2.) + fu[i] * fu[j] * expn * k13;
         const R Fdl = pi[i + 1][j + 1] * expn;
-        const R common = t * f2 * (cmd[i + 1] * hy[j + 1][0] * di + cmd[j + 1] * hy[i + 1][0] * dj) +
+        const R common = ch * (t * f2 * (cmd[i + 1] * hy[j + 1][0] * di + cmd[j + 1] * hy[i + 1][0] * dj) +
                               g * (cmd[i + 1] * hy[j + 1][3] * di + cmd[j + 1] * hy[i + 1][3] * dj) * it +
                               f2 * f2 * t * (fu[i] * hy[j + 1][0] + fu[j] * hy[i + 1][0]) +
-                              R(2.) * g * f2 * (fu[i] * hy[j + 1][3] + fu[j] * hy[i + 1][3]) * it;
-        const R cross = g * (pi[3][i + 1] * dj + pi[3][j + 1] * di) * it + f2 * (pi[0][i + 1] * dj + pi[0][j + 1] * di) * it;
+                              R(2.) * g * f2 * (fu[i] * hy[j + 1][3] + fu[j] * hy[i + 1][3]) * it);
+        const R cross = ch * (g * (pi[3][i + 1] * dj + pi[3][j + 1] * di) * it + f2 * (pi[0][i + 1] * dj + pi[0][j + 1] * di) * it);
         const R Fdo2 = -(-gugjs + sigu - vsig) / R(4.) + (-fu[i] * g * hy[j + 1][0] - fu[j] * g * hy[i + 1][0]) * geo / R(4.) +
                             (common - cross) / R(4.);
         R Fds2 = -(-gugjs - sigu + vsig - R(4.) * (fu[i] * fu[j]) * sgu_s * k13) / R(4.) +
                       (-fu[i] * g * hy[j + 1][0] - fu[j] * g * hy[i + 1][0] + R(4.) * fu[i] * fu[j] * hy[0][0] * k13) * geo / R(4.) +
-                      (common + cross + R(4.) * fu[i] * fu[j] * (hy[3][0] * f2 * t + g * hy[3][3] * it + f2 * hy[0][3] * it) * k13) / R(4.) -
-                      pi[i + 1][j + 1] * (g * it + geo + g * divV) * k13;
-        if (j == 2) {
+                      (common + cross + ch * (R(4.) * fu[i] * fu[j] * (hy[3][0] * f2 * t + g * hy[3][3] * it + f2 * hy[0][3] * it) * k13)) / R(4.) -
+                      pi[i + 1][j + 1] * (g * itc + geo + g * divV) * k13;
+        if (j == 2 && !cart) {
           FD2 += g * pi[3][i + 1] * it + f2 * pi[0][i + 1] * it;
           Fsg += -fu[i] * f2 * f2 * t / R(2.) - fu[i] * f2 * g * it;
         }
         if (i == j) {
           Fsg += -cmd[i + 1] * expn * k13;
           Fds2 += -cmd[i + 1] * sgu_s * k13 - cmd[i + 1] * hy[0][0] * geo * k13 -
-                  cmd[i + 1] * (hy[3][0] * f2 * t + g * hy[3][3] * it + f2 * hy[0][3] * it) * k13;
+                  ch * (cmd[i + 1] * (hy[3][0] * f2 * t + g * hy[3][3] * it + f2 * hy[0][3] * it) * k13);
         }
         if (diag) sigF[slot] = Fsg;
         R F = (-pi[i + 1][j + 1] - tdelta * Fdl - tpi * FD2 + R(2.) * tpi * Fdo2 * uv - tpp * Fds2 +
@@ -395,8 +401,8 @@ __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, cons
   R Mw[3];
 #pragma unroll
   for (int i = 0; i < D; i++) Mw[i] = X * uc[i] * ig + sig * dwds * Ms[i];
-  const R Fw = -X * (geo + g * it + g * divV) + sig * dwds * Fs;
-  const R Fbulk = sig * Fb - Pi * (g * divV + g * it + geo) * ig;
+  const R Fw = -X * (geo + g * itc + g * divV) + sig * dwds * Fs;
+  const R Fbulk = sig * Fb - Pi * (g * divV + g * itc + geo) * ig;
   R Mu[9], Fu[3];
 #pragma unroll
   for (int i = 0; i < D; i++) {
@@ -405,7 +411,7 @@ __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, cons
     Mu[i * D + i] += g * (w + Pi);
     Fu[i] = (gP[i] + gB[i]) - g * (Fw + Fbulk) * u[i] - (w + Pi) * expn * u[i] - R(2.) * (w + Pi) * g * uD * dEta(i) * it;
     if (cfg.using_shear)
-      Fu[i] += -P(i + 1, 0) * it - R(2.) * dEta(i) * P(0, 3) * it - in.divshear[i] + in.gradshear[i] - F0i[i];
+      Fu[i] += -P(i + 1, 0) * itc - R(2.) * dEta(i) * P(0, 3) * it - in.divshear[i] + in.gradshear[i] - F0i[i];
   }
   // du/dt = M^-1 F by cofactors (include/milne.hpp:788-834)
   R du[3];
@@ -445,7 +451,7 @@ __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, cons
     R c1 = R(0.0);
 #pragma unroll
     for (int i = 0; i < D; i++) c1 += uc[i] * du[i];
-    diag[0] = -R(1.) * c1 / g + g * divV + g / t + geo;
+    diag[0] = -R(1.) * c1 / g + g * divV + (cart ? R(0.0) : g / t) + geo;
 #pragma unroll
     for (int sl = 0; sl < 5; sl++) {
       R acc = R(0.0);

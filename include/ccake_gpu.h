@@ -38,7 +38,7 @@ typedef enum ccake_status {
  * (include/settings.h:23-287) that the hot path reads. */
 typedef struct ccake_config {
   int32_t dim;               /* spatial dimensions: 2 or 3 */
-  int32_t coord;             /* 0 Milne ("hyperbolic", EoM_default); Cartesian not supported */
+  int32_t coord;             /* 0 Milne ("hyperbolic", EoM_default), 1 Cartesian (EoM_cartesian) */
   int32_t eos_kind;          /* 0 conformal, 1 conformal_diagonal, 2 table */
   int32_t using_shear;       /* include/settings.h:263-270 */
   int32_t using_vorticity;

@@ -134,8 +134,13 @@ struct ShearMRF {
 // src/eom_default.cpp:882-1412 (calculate_MRF_shear) for one particle.
 void shear_mrf(const System& s, int a, double t, bool use_vort, ShearMRF& o) {
   const int D = s.cfg.dim;
-  const double t2 = t * t;
-  const double cmd[4] = {1.0, -1.0, -1.0, -1.0 / t / t};
+  // Cartesian (src/eom_cartesian.cpp:840-1400): the metric without tau and
+  // none of the Milne connection terms (1/tau, the geometric factor, eta deltas)
+  const bool cart = s.cfg.coord == 1;
+  const double tm = cart ? 1.0 : t, ch = cart ? 0.0 : 1.0;
+  auto dE = [&](int i) { return cart ? 0.0 : dEta(D, i); };
+  const double t2 = tm * tm;
+  const double cmd[4] = {1.0, -1.0, -1.0, -1.0 / tm / tm};
   const double sigma = s.sigma[a], g = s.gamma[a];
   const double eta = s.eta_pi[a], phi6 = s.phi6[a], phi7 = s.phi7[a], lpP = s.lambda_piPi[a];
   const double tpp = s.tau_pipi[a], dpp = s.delta_pipi[a], tpi = s.tau_pi[a];
@@ -157,7 +162,8 @@ void shear_mrf(const System& s, int a, double t, bool use_vort, ShearMRF& o) {
       double f = (i == 1 || i == 2) ? -1.0 : (i == 3 ? -t2 : 1.0);
       pc[i][j] = hy[i][j] * f;
     }
-  const double geo = dEta(D, D - 1) * u[D - 1] * u[D - 1] * t / g;
+  const double geo = dE(D - 1) * u[D - 1] * u[D - 1] * t / g;
+  const double gt = cart ? 0.0 : g / t;
   double gV[3][3] = {{0}}, divV = 0;
   for (int i = 0; i < D; i++) {
     divV += s.gradV[i * D + i][a];
@@ -216,21 +222,21 @@ void shear_mrf(const System& s, int a, double t, bool use_vort, ShearMRF& o) {
     for (int j = 0; j < 4; j++) sl0[i] += (pi[0][j] * hy[i + 1][j] + pi[i + 1][j] * hy[0][j]) / 2.;
   }
   const double uD = u[D - 1];
-  const double expn = geo + g / t + g * divV;
+  const double expn = geo + gt + g * divV;
   double Fs[3], FD[3], Fds[3], Fdo[3], Fdd[3], Ms[3][3], MD[3][3], Mds[3][3], Mdo[3][3], Mdd[3][3];
   for (int i = 0; i < D; i++) {
-    const double di = dEta(D, i);
-    Fs[i] = -(guv[i] - gu0c[i]) / 2. + u[i] * g * (geo + g / t + g * divV) / 3. - g * geo * u[i] / 2.;
+    const double di = dE(i);
+    Fs[i] = -(guv[i] - gu0c[i]) / 2. + u[i] * g * (geo + gt + g * divV) / 3. - g * geo * u[i] / 2.;
     FD[i] = g * (u[i] * hy[0][0] + g * hy[i + 1][0]) * geo + t * uD * pi[3][i + 1] * di;
     Fds[i] = -(v_gradu_shv[i] - gugs[i] - 4. * g * u[i] * sgu_s / 3. - sgu[i] + vsgu[i]) / 4. +
              (hy[i + 1][0] - g * g * hy[i + 1][0] - g * u[i] * hy[0][0] + pi[0][i + 1] +
               4. * u[i] * g * hy[0][0] / 3.) * geo / 4. +
-             (g * cmd[i + 1] * hy[0][3] * di / t + g * pi[3][0] * di / t +
-              4. * g * u[i] * (g * hy[3][3] / t) / 3.) / 4. -
-             pi[0][i + 1] * (g / t + geo + g * divV) / 3.;
+             ch * (g * cmd[i + 1] * hy[0][3] * di / t + g * pi[3][0] * di / t +
+                   4. * g * u[i] * (g * hy[3][3] / t) / 3.) / 4. -
+             pi[0][i + 1] * (gt + geo + g * divV) / 3.;
     Fdo[i] = -(v_gradu_shv[i] - gugs[i] + sgu[i] - vsgu[i]) / 4. +
              (hy[i + 1][0] - g * g * hy[i + 1][0] - g * u[i] * hy[0][0] - pi[0][i + 1]) * geo / 4. +
-             (g * cmd[i + 1] * hy[0][3] * di / t - g * pi[3][0] * di / t) / 4.;
+             ch * (g * cmd[i + 1] * hy[0][3] * di / t - g * pi[3][0] * di / t) / 4.;
     Fdd[i] = pi[i + 1][0] * expn;
     for (int j = 0; j < D; j++) {
       Ms[i][j] = u[i] * uc[j] / (2. * 3.);
@@ -248,7 +254,7 @@ void shear_mrf(const System& s, int a, double t, bool use_vort, ShearMRF& o) {
     Mds[i][i] += +pi[0][0] / 4.;
     Fs[i] += di * (-(-uD * t - uD / t + g * uD * uD * t + 2. * g * g * uD / t) / 2.);
     FD[i] += di * (uD * pi[0][0] / t + g * pi[3][0] / t);
-    if (D != 2) {
+    if (D != 2 && !cart) {
       Fds[i] += (t * uD * di * cmd[i + 1] * hy[0][0] + uD * hy[i + 1][3] * g / t / 4. + hy[i + 1][3] * t * uD +
                  pi[0][0] * di * uD / t + t * uD * uD * (g * hy[i + 1][0] + u[i] * hy[0][0]) +
                  2. * g * uD * (g * hy[i + 1][3] + u[i] * pi[0][3]) / t) / 4. +
@@ -264,7 +270,7 @@ void shear_mrf(const System& s, int a, double t, bool use_vort, ShearMRF& o) {
     for (int j = 0; j < D; j++) Fnab += (hy[i + 1][j + 1] - v[i] * hy[0][j + 1]) * gu[i][j];
     Fnab += (hy[i + 1][0] - v[i] * hy[0][0]) * gu0[i];
   }
-  Fnab += +hy[3][3] * g / t + hy[0][0] * geo + (t * hy[3][0] + hy[0][3] / t) * uD * dEta(D, D - 1);
+  Fnab += +ch * (hy[3][3] * g / t) + hy[0][0] * geo + (t * hy[3][0] + hy[0][3] / t) * uD * dE(D - 1);
   o.Fnab = Fnab;
   const double uv = use_vort ? 1.0 : 0.0;
   for (int i = 0; i < D; i++) {
@@ -293,24 +299,24 @@ void shear_mrf(const System& s, int a, double t, bool use_vort, ShearMRF& o) {
   const double f2 = fu[2];
   for (int i = 0; i < 2; i++) {
     for (int j = i; j < 3; j++) {
-      const double di = dEta(D, i), dj = dEta(D, j);
+      const double di = dE(i), dj = dE(j);
       FD2[i][j] = g * geo * (fu[i] * hy[j + 1][0] + fu[j] * hy[i + 1][0]);
       Fsg[i][j] = cgu[i][j] / 2. + cgu[j][i] / 2. + fu[i] * fu[j] * expn / 3.;
       Fdl[i][j] = pi[i + 1][j + 1] * expn;
-      const double common =
-          t * f2 * (cmd[i + 1] * hy[j + 1][0] * di + cmd[j + 1] * hy[i + 1][0] * dj) +
+      const double common = ch *
+          (t * f2 * (cmd[i + 1] * hy[j + 1][0] * di + cmd[j + 1] * hy[i + 1][0] * dj) +
           g * (cmd[i + 1] * hy[j + 1][3] * di + cmd[j + 1] * hy[i + 1][3] * dj) / t +
           f2 * f2 * t * (fu[i] * hy[j + 1][0] + fu[j] * hy[i + 1][0]) +
-          2. * g * f2 * (fu[i] * hy[j + 1][3] + fu[j] * hy[i + 1][3]) / t;
-      const double cross = g * (pi[3][i + 1] * dj + pi[3][j + 1] * di) / t +
-                           f2 * (pi[0][i + 1] * dj + pi[0][j + 1] * di) / t;
+          2. * g * f2 * (fu[i] * hy[j + 1][3] + fu[j] * hy[i + 1][3]) / t);
+      const double cross = ch * (g * (pi[3][i + 1] * dj + pi[3][j + 1] * di) / t +
+                                 f2 * (pi[0][i + 1] * dj + pi[0][j + 1] * di) / t);
       Fdo2[i][j] = -(-gugjs[i][j] + sigu[i][j] - vsig[i][j]) / 4. +
                    (-fu[i] * g * hy[j + 1][0] - fu[j] * g * hy[i + 1][0]) * geo / 4. + (common - cross) / 4.;
       Fds2[i][j] = -(-gugjs[i][j] - sigu[i][j] + vsig[i][j] - 4. * (fu[i] * fu[j]) * sgu_s / 3.) / 4. +
                    (-fu[i] * g * hy[j + 1][0] - fu[j] * g * hy[i + 1][0] + 4. * fu[i] * fu[j] * hy[0][0] / 3.) * geo / 4. +
                    (common + cross +
-                    4. * fu[i] * fu[j] * (hy[3][0] * f2 * t + g * hy[3][3] / t + f2 * hy[0][3] / t) / 3.) / 4. -
-                   pi[i + 1][j + 1] * (g / t + geo + g * divV) / 3.;
+                    ch * (4. * fu[i] * fu[j] * (hy[3][0] * f2 * t + g * hy[3][3] / t + f2 * hy[0][3] / t) / 3.)) / 4. -
+                   pi[i + 1][j + 1] * (gt + geo + g * divV) / 3.;
       for (int k = 0; k < D; k++) {
         MD2[i][j][k] = g * (fu[i] * hy[j + 1][k + 1] - fu[i] * hy[j + 1][0] * fuc[k] / g + fu[j] * hy[i + 1][k + 1] -
                             fu[j] * hy[i + 1][0] * fuc[k] / g);
@@ -336,11 +342,11 @@ void shear_mrf(const System& s, int a, double t, bool use_vort, ShearMRF& o) {
       Msg[i][i][k] += cmd[i + 1] * fuc[k] / (g * 3.);
       Mds2[i][i][k] += -cmd[i + 1] * (hy[0][k + 1] - hy[0][0] * fuc[k] / g) / 3.;
     }
-    FD2[i][2] += g * pi[3][i + 1] / t + f2 * pi[0][i + 1] / t;
+    if (!cart) FD2[i][2] += g * pi[3][i + 1] / t + f2 * pi[0][i + 1] / t;
     Fsg[i][i] += -cmd[i + 1] * expn / 3.;
-    Fsg[i][2] += -fu[i] * f2 * f2 * t / 2. - fu[i] * f2 * g / t;
+    if (!cart) Fsg[i][2] += -fu[i] * f2 * f2 * t / 2. - fu[i] * f2 * g / t;
     Fds2[i][i] += -cmd[i + 1] * sgu_s / 3. - cmd[i + 1] * hy[0][0] * geo / 3. -
-                  cmd[i + 1] * (hy[3][0] * f2 * t + g * hy[3][3] / t + f2 * hy[0][3] / t) / 3.;
+                  ch * (cmd[i + 1] * (hy[3][0] * f2 * t + g * hy[3][3] / t + f2 * hy[0][3] / t) / 3.);
   }
   for (int i = 0; i < 2; i++) {
     for (int j = i; j < 3; j++) {
@@ -367,7 +373,7 @@ void shear_mrf(const System& s, int a, double t, bool use_vort, ShearMRF& o) {
 // Reynolds numbers sqrt|pi:pi| / p and |Pi| / p.
 void hydro_numbers(System& s, int a, const double* sig5) {
   const int D = s.cfg.dim;
-  const double t = s.t, t2 = t * t;
+  const double t = s.cfg.coord == 1 ? 1.0 : s.t, t2 = t * t;
   const double g = s.gamma[a];
   double uc[3] = {0, 0, 0};
   for (int i = 0; i < D; i++) uc[i] = s.u[i][a];
@@ -411,7 +417,7 @@ void hydro_numbers(System& s, int a, const double* sig5) {
 // src/eom_default.cpp:17-38 (update_velocity)
 void update_velocity(System& s) {
   const int D = s.cfg.dim;
-  const double t2 = s.t * s.t;
+  const double tm = s.cfg.coord == 1 ? 1.0 : s.t, t2 = tm * tm;
 #pragma omp parallel for
   for (int a = 0; a < s.n; a++) {
     double u[3] = {s.u[0][a], s.u[1][a], s.u[2][a]};
@@ -424,7 +430,7 @@ void update_velocity(System& s) {
 // src/eom_default.cpp:56-172 (reset_pi_tensor), diffusion part omitted.
 void reset_pi_tensor(System& s) {
   const int D = s.cfg.dim;
-  const double t2 = s.t * s.t;
+  const double tm = s.cfg.coord == 1 ? 1.0 : s.t, t2 = tm * tm;
 #pragma omp parallel for
   for (int a = 0; a < s.n; a++) {
     const double g = s.gamma[a], sig = s.sigma[a];
@@ -486,10 +492,14 @@ int update_thermodynamics(System& s) {
 }
 
 // src/eom_default.cpp:211-869 (evaluate_time_derivatives) without sources and
-// without the diffusion sector (dN/dt is then zero).
+// without the diffusion sector (dN/dt is then zero); with coord = 1 its
+// Cartesian twin src/eom_cartesian.cpp:210-840 (no tau in the metric, no
+// connection terms).
 void evaluate_time_derivatives(System& s) {
   const int D = s.cfg.dim;
-  const double t = s.t, t2 = t * t;
+  const bool cart = s.cfg.coord == 1;
+  const double t = s.t, tm = cart ? 1.0 : t, t2 = tm * tm;
+  auto dE = [&](int i) { return cart ? 0.0 : dEta(D, i); };
   const bool shear = s.cfg.using_shear;
 #pragma omp parallel for
   for (int a = 0; a < s.n; a++) {
@@ -516,8 +526,9 @@ void evaluate_time_derivatives(System& s) {
       }
     double divV = 0;
     for (int i = 0; i < D; i++) divV += s.gradV[i * D + i][a];
-    const double geo = dEta(D, D - 1) * u[D - 1] * u[D - 1] * t / g;
-    const double expn = g * divV + g / t + geo;
+    const double geo = dE(D - 1) * u[D - 1] * u[D - 1] * t / g;
+    const double gt = cart ? 0.0 : g / t;
+    const double expn = g * divV + gt + geo;
     // fill_auxiliary_variables (:229-362)
     double Mb[3], Ms[3];
     for (int i = 0; i < D; i++) {
@@ -527,8 +538,8 @@ void evaluate_time_derivatives(System& s) {
     // R_extensive_entropy = -mu/T multiplies dN/dt, which is zero without the
     // diffusion sector and sources
     (void)mu;
-    double Fb = -(ztil * (g * divV + g / t + geo) + Pi - phi1 * Pi * Pi) / (sig * g * tPi);
-    double Fs = (-Pi * (g * divV + g / t + geo)) / (sig * g * T);
+    double Fb = -(ztil * (g * divV + gt + geo) + Pi - phi1 * Pi * Pi) / (sig * g * tPi);
+    double Fs = (-Pi * (g * divV + gt + geo)) / (sig * g * T);
     double Fnab = 0, Mnab[3] = {0, 0, 0};
     if (shear) {
       Fnab = sm.Fnab;
@@ -550,18 +561,19 @@ void evaluate_time_derivatives(System& s) {
     const double X = sden * dwds / g + (rho[0] * dwdr[0] + rho[1] * dwdr[1] + rho[2] * dwdr[2]) / g;
     double Mw[3];
     for (int i = 0; i < D; i++) Mw[i] = X * uc[i] / g + sig * dwds * Ms[i];
-    const double Fw = -X * (geo + g / t + g * divV) + sig * dwds * Fs;
-    const double Fbulk = sig * Fb - Pi * (g * divV + g / t + geo) / g;
+    const double Fw = -X * (geo + gt + g * divV) + sig * dwds * Fs;
+    const double Fbulk = sig * Fb - Pi * (g * divV + gt + geo) / g;
     double Mu[9], Fu[3];
     for (int i = 0; i < D; i++) {
       for (int j = 0; j < D; j++) Mu[i * D + j] = u[i] * g * (Mb[j] + Mw[j]) - u[i] * uc[j] * (w + Pi) / g;
       Mu[i * D + i] += g * (w + Pi);
-      Fu[i] = (gP[i] + gB[i]) - g * (Fw + Fbulk) * u[i] - (w + Pi) * expn * u[i] -
-              2. * (w + Pi) * g * u[D - 1] * dEta(D, i) / t;
+      Fu[i] = (gP[i] + gB[i]) - g * (Fw + Fbulk) * u[i] - (w + Pi) * expn * u[i];
+      if (!cart) Fu[i] -= 2. * (w + Pi) * g * u[D - 1] * dEta(D, i) / t;
     }
     if (shear) {
       for (int i = 0; i < D; i++) {
-        Fu[i] += -pi[i + 1][0] / t - 2. * dEta(D, i) * pi[0][3] / t - s.divshear[i][a] + s.gradshear[i][a] - sm.F0i[i];
+        if (cart) Fu[i] += -s.divshear[i][a] + s.gradshear[i][a] - sm.F0i[i];
+        else Fu[i] += -pi[i + 1][0] / t - 2. * dEta(D, i) * pi[0][3] / t - s.divshear[i][a] + s.gradshear[i][a] - sm.F0i[i];
         for (int j = 0; j < D; j++) Mu[i * D + j] += sm.M0i[i * D + j];
       }
     }
@@ -576,7 +588,7 @@ void evaluate_time_derivatives(System& s) {
     double m1 = 0, m2 = 0, m3 = 0, c1 = 0;
     for (int i = 0; i < D; i++) { m1 += Ms[i] * du[i]; m2 += Mb[i] * du[i]; m3 += Mnab[i] * du[i]; c1 += uc[i] * du[i]; }
     const double dS = m1 + Fs, dB = m2 + Fb, snu = m3 + Fnab;
-    const double th = -1. * c1 / g + g * divV + g / t + geo;
+    const double th = -1. * c1 / g + g * divV + gt + geo;
     for (int i = 0; i < D; i++) s.du_dt[i][a] = du[i];
     s.d_ext[0][a] = dS;
     s.d_ext[1][a] = s.d_ext[2][a] = s.d_ext[3][a] = 0.0;
@@ -898,7 +910,7 @@ Totals conservation(const System& s) {
 void initialize(System& s, NbrList& nl) {
   const int D = s.cfg.dim;
   s.t = s.cfg.t0;
-  const double t2 = s.t * s.t;
+  const double tm = s.cfg.coord == 1 ? 1.0 : s.t, t2 = tm * tm;
   const double T_seed = 580.0 / kHbarcMeVfm;
   for (int a = 0; a < s.n; a++) {
     double u[3] = {s.u[0][a], s.u[1][a], s.u[2][a]};

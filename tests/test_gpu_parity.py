@@ -379,3 +379,46 @@ def test_freeze_out_hypersurface_matches_oracle(tmp_path, case, precision):
     lines = path.read_text().splitlines()
     assert lines[0] == "# 1 2 3" and len(lines) == 1 + rg.shape[0]
     assert all(len(ln.split()) == 40 for ln in lines[1:])
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_cartesian_parity(dim):
+    # EoM_cartesian (src/eom_cartesian.cpp): the same events in Cartesian
+    # coordinates (coord = 1) against the oracle, and the mixed form against
+    # the FP64 form there
+    if dim == 2:
+        p, rc = ics.hotspots_2d(n_side=40, n_hot=4, seed=9)
+        fields = ["x", "y", "u0", "u1", "ext_s", "ext_B", "T", "e", "p", "sigma_lab", "ext_shv0", "ext_shv1",
+                  "shv00", "shv11", "shv33", "Ez"]
+        steps = 10
+    else:
+        p, rc = ics.hotspots_3d(n_xy=16, n_eta=12, n_hot=4, seed=3)
+        fields = ["x", "y", "eta", "u0", "u1", "u2", "ext_s", "T", "e", "sigma_lab", "ext_shv0", "ext_shv2",
+                  "ext_shv4", "shv33", "Ez"]
+        steps = 3
+    rc = dataclasses.replace(rc, coord=1)
+    gpu = api.GpuHydro(rc)
+    gpu.load(p)
+    orc = O.OracleRun(p, rc)
+    gpu.initialize()
+    assert orc.initialize() == 0
+    gpu.step(steps)
+    assert orc.step(steps) == 0
+    for f in fields:
+        # velocities cross zero: judged against 1e-5 of their range
+        floor = 1e-5 if f in ("u0", "u1", "u2") else 1e-6
+        assert relerr(gpu.get(f), orc.get(f), floor) < RTOL, f
+    tg, to = gpu.totals(), orc.totals()
+    for k in ("S", "B", "E"):
+        assert abs(tg[k] - to[k]) <= 1e-10 * (abs(to[k]) + 1e-30), k
+    # Milne and Cartesian differ (the tau terms are gone)
+    m = api.GpuHydro(dataclasses.replace(rc, coord=0))
+    m.load(p)
+    m.initialize()
+    m.step(steps)
+    assert relerr(m.get("e"), gpu.get("e")) > 1e-6
+    mixed = api.GpuHydro(dataclasses.replace(rc, precision=1))
+    mixed.load(p)
+    mixed.initialize()
+    mixed.step(steps)
+    assert relerr(mixed.get("e"), gpu.get("e")) < 1e-5
