@@ -26,7 +26,11 @@ class CcakeConfig(ctypes.Structure):
         [(n, _f64) for n in (
             "hT", "hEta", "t0", "dt", "eos_c", "eos_T0", "eos_muB0", "eos_muQ0", "eos_muS0", "eta_over_s",
             "zeta_over_s", "zeta_cs2_A", "zeta_cs2_p", "zeta_peak_T", "zeta_peak_width", "xmin", "ymin",
-            "etamin", "freeze_out_T", "skin_frac")] + [("particlization", _i32), ("surface", _i32)]
+            "etamin", "freeze_out_T", "skin_frac")] + [("particlization", _i32), ("surface", _i32)] + \
+        [(n, _i32) for n in ("using_diffusion", "diffusion_mode", "diffusion_relax_mode", "diffusion_regulator",
+                             "critical_scaling_diffusion", "pad2")] + [("kappa_over_T2", _f64 * 9)] + \
+        [(n, _f64) for n in ("C_B", "reg_chi0", "reg_e0", "reg_xi0", "reg_rq_max", "crit_T", "crit_muB", "crit_wT",
+                             "crit_wmuB")]
 
 
 class ParticlesSoA(ctypes.Structure):
@@ -93,6 +97,7 @@ def lib():
         L.ccake_freeze_out_rows.argtypes = [P, ctypes.POINTER(_i64), ctypes.POINTER(_i32), _dp]
         L.ccake_write_freeze_out.argtypes = [P, ctypes.c_char_p, _f64, _f64, _f64]
         L.ccake_hydro_numbers.argtypes = [P]
+        L.ccake_set_initial_diffusion.argtypes = [P, _dp]
         L.ccake_write_system_state.argtypes = [P, ctypes.c_char_p]
         L.ccake_ic_read_ccake.argtypes = [ctypes.c_char_p, ctypes.POINTER(IcOptions), ctypes.POINTER(P)]
         L.ccake_ic_info.argtypes = [P, ctypes.POINTER(_i64), _dp]
@@ -135,7 +140,10 @@ def make_config(rc) -> CcakeConfig:
     c = CcakeConfig()
     for name, _ in CcakeConfig._fields_:
         if hasattr(rc, name):
-            setattr(c, name, getattr(rc, name))
+            v = getattr(rc, name)
+            if name == "kappa_over_T2":
+                v = (_f64 * 9)(*[float(x) for x in v])
+            setattr(c, name, v)
     return c
 
 
@@ -187,6 +195,14 @@ class GpuHydro:
                            _d(arrs["uy"]), _d(arrs["ueta"]))
         self._check(lib().ccake_load_particles(self.h, ctypes.byref(soa)), "load")
         self.n = particles.n
+
+    def set_initial_diffusion(self, q):
+        """Initial diffusion currents, q[4 c + mu, i] = q^mu of charge c (B, S,
+        Q) of particle i (the spatial q^i are used); between load and initialize."""
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        if q.shape != (12, self.n):
+            raise ValueError("q must have shape (12, n)")
+        self._check(lib().ccake_set_initial_diffusion(self.h, q.ctypes.data_as(_dp)), "set_initial_diffusion")
 
     def initialize(self):
         self._check(lib().ccake_initialize(self.h), "initialize")

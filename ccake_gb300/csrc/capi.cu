@@ -112,6 +112,9 @@ void free_buffers(ccake_ctx* ctx) {
   if (ctx->p.fz) cudaFree(ctx->p.fz);
   if (ctx->p.fo_rows) cudaFree(ctx->p.fo_rows);
   if (ctx->p.fo_count) cudaFree(ctx->p.fo_count);
+  if (ctx->p.dif) cudaFree(ctx->p.dif);
+  if (ctx->p.recQ) cudaFree(ctx->p.recQ);
+  ctx->p.dif = ctx->p.recQ = nullptr;
   ctx->dbuf = nullptr;
   ctx->ibuf = nullptr;
   ctx->p.fz = ctx->p.fo_rows = nullptr;
@@ -307,6 +310,28 @@ FieldRef field_ref(ccake_ctx* ctx, const std::string& k) {
   if (k == "bulk_knudsen") return FieldRef{p.derivs + D_KNB * n, true};
   if (k == "inverse_reynolds_shear") return FieldRef{p.derivs + D_IRS * n, true};
   if (k == "inverse_reynolds_bulk") return FieldRef{p.derivs + D_IRB * n, true};
+  if (p.dif) {
+    // diffusion sector, charge letters B, S, Q
+    auto F = [&](int slot) { return FieldRef{p.dif + (size_t)slot * n, true}; };
+    const char ch[3] = {'B', 'S', 'Q'};
+    for (int c = 0; c < 3; c++) {
+      const std::string C(1, ch[c]);
+      if (k == "d_ext_" + C) return F(F_DN + c);
+      for (int m = 0; m < 4; m++)
+        if (k == "q" + C + std::to_string(m)) return F(F_Q + 4 * c + m);
+      for (int i = 0; i < 3; i++) {
+        if (k == "ext_q" + C + std::to_string(i)) return F(F_YQ + 3 * c + i);
+        if (k == "d_ext_q" + C + std::to_string(i)) return F(F_DYQ + 3 * c + i);
+        if (k == "grad_alpha" + std::to_string(i) + C) return F(F_GA + 3 * i + c);
+      }
+      if (k == "div_qa" + C) return F(F_DQ + c);
+      if (k == "grad_qa" + C) return F(F_GQ + c);
+      if (k == "kn_diff" + C) return F(F_KN + c);
+      if (k == "ire_diff" + C) return F(F_IR + c);
+    }
+    for (int j = 0; j < 12; j++)
+      if (k == "dalpha" + std::to_string(j)) return F(F_DA + j);
+  }
   return FieldRef{nullptr, false};
 }
 
@@ -445,6 +470,13 @@ ccake_status_t ccake_ctx_create(const ccake_config* cfg, ccake_ctx** out) {
   if (!(cfg->skin_frac >= 0.0)) return CCAKE_ERR_INVALID;
   if (!(cfg->hT > 0) || !(cfg->t0 > 0) || !(cfg->dt > 0)) return CCAKE_ERR_INVALID;
   if (cfg->dim == 3 && cfg->factorized_kernel) return CCAKE_ERR_INVALID;
+  // the diffusion sector runs in the FP64 form, Milne coordinates, with the
+  // constant_over_T2 or kappaB_coth coefficients, without the hypersurface
+  // rows (whose diffusion columns it does not fill)
+  if (cfg->using_diffusion &&
+      (cfg->precision != 0 || cfg->coord != 0 || (cfg->diffusion_mode != 0 && cfg->diffusion_mode != 2) ||
+       (cfg->particlization && cfg->surface)))
+    return CCAKE_ERR_INVALID;
   ccake_ctx* ctx = new ccake_ctx;
   ctx->cfg = *cfg;
   if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
@@ -564,6 +596,14 @@ ccake_status_t ccake_load_particles(ccake_ctx* ctx, const ccake_particles_soa* h
     CK(cudaStreamSynchronize(ctx->stream));
     return CCAKE_OK;
   };
+  if (ctx->cfg.using_diffusion) {
+    // diffusion slabs (zero: no initial current unless one is set)
+    if (cudaMalloc(&p.dif, (size_t)NDIF * n * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&p.recQ, (size_t)RQ * n * sizeof(double)) != cudaSuccess)
+      return fail(ctx, CCAKE_ERR_NOMEM, "diffusion allocation");
+    CK(cudaMemsetAsync(p.dif, 0, (size_t)NDIF * n * sizeof(double), ctx->stream));
+    CK(cudaMemsetAsync(p.recQ, 0, (size_t)RQ * n * sizeof(double), ctx->stream));
+  }
   ccake_status_t s;
   if ((s = up(h->x, p.y + Y_X0 * n)) || (s = up(h->y, p.y + Y_X1 * n)) ||
       (s = up(ctx->cfg.dim == 3 ? h->eta : nullptr, p.y + Y_X2 * n)) || (s = up(h->ux, p.y + Y_U0 * n)) ||
@@ -573,6 +613,24 @@ ccake_status_t ccake_load_particles(ccake_ctx* ctx, const ccake_particles_soa* h
     return s;
   ctx->loaded = true;
   ctx->initialized = false;
+  return CCAKE_OK;
+}
+
+ccake_status_t ccake_set_initial_diffusion(ccake_ctx* ctx, const double* q) {
+  if (!ctx || !q) return CCAKE_ERR_INVALID;
+  if (!ctx->loaded) return fail(ctx, CCAKE_ERR_STATE, "load particles first");
+  if (!ctx->p.dif) return fail(ctx, CCAKE_ERR_STATE, "the diffusion sector is off");
+  if (ctx->initialized) return fail(ctx, CCAKE_ERR_STATE, "set the initial current before initialize");
+  const int64_t n = ctx->n;
+  std::vector<double> tmp((size_t)n);
+  for (int c = 0; c < 3; c++)
+    for (int i = 0; i < 3; i++) {
+      const double* src = q + (size_t)(4 * c + i + 1) * n;
+      for (int64_t k = 0; k < n; k++) tmp[k] = src[ctx->perm[k]];
+      CK(cudaMemcpyAsync(ctx->p.dif + (size_t)(F_YQ0 + 3 * c + i) * n, tmp.data(), n * sizeof(double),
+                         cudaMemcpyHostToDevice, ctx->stream));
+      CK(cudaStreamSynchronize(ctx->stream));
+    }
   return CCAKE_OK;
 }
 
@@ -643,8 +701,19 @@ ccake_status_t ccake_initialize(ccake_ctx* ctx) {
   if (s) return s;
   launch_passA(ctx->rc, ctx->eos, ctx->p, A_SMOOTH_ONLY, ctx->stream);   // initial sigma
   launch_init_ext(ctx->rc, ctx->p, ctx->stream);
-  launch_passA(ctx->rc, ctx->eos, ctx->p, A_WITH_THERMO, ctx->stream);   // initial smoothing
   const int64_t n = ctx->n;
+  if (ctx->p.dif) {
+    // initial smoothing, then set_diffusion (ext q = q^i / sigma of that
+    // smoothing, src/sph_workstation.cpp:394-457, :1441-1458), then the
+    // thermodynamics and q^mu
+    launch_passA(ctx->rc, ctx->eos, ctx->p, A_SMOOTH_ONLY, ctx->stream);
+    launch_init_diffusion(ctx->rc, ctx->p, ctx->stream);
+    launch_thermo(ctx->rc, ctx->eos, ctx->p, ctx->stream);
+    CK(cudaMemcpyAsync(ctx->p.dif + (size_t)F_YQ0 * n, ctx->p.dif + (size_t)F_YQ * n, 9 * n * sizeof(double),
+                       cudaMemcpyDeviceToDevice, ctx->stream));
+  } else {
+    launch_passA(ctx->rc, ctx->eos, ctx->p, A_WITH_THERMO, ctx->stream);   // initial smoothing
+  }
   CK(cudaMemcpyAsync(ctx->p.y0, ctx->p.y, NY * n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
   s = check_errors(ctx);
   if (s) return s;
@@ -1275,6 +1344,8 @@ ccake_status_t ccake_hydro_numbers(ccake_ctx* ctx) {
     // reference's stored numbers are still zero
     CK(cudaMemsetAsync(ctx->p.derivs + (size_t)D_THETA * n, 0, (size_t)(NDER - D_THETA) * n * sizeof(double),
                        ctx->stream));
+    if (ctx->p.dif)
+      CK(cudaMemsetAsync(ctx->p.dif + (size_t)F_KN * n, 0, 6 * (size_t)n * sizeof(double), ctx->stream));
     return check_errors(ctx);
   }
   // the step keeps its gradients in registers: the gradient sums of the last
@@ -1304,14 +1375,21 @@ ccake_status_t ccake_write_system_state(ccake_ctx* ctx, const char* path) {
   std::vector<int32_t> frz((size_t)n), eid((size_t)n);
   if ((st = ccake_copy_out_int(ctx, "freeze", frz.data()))) return st;
   if ((st = ccake_copy_out_int(ctx, "eos_id", eid.data()))) return st;
+  // diffusion Knudsen and inverse Reynolds numbers (B, S, Q), zero without
+  // the sector
+  static const char* dnames[6] = {"kn_diffB", "kn_diffS", "kn_diffQ", "ire_diffB", "ire_diffS", "ire_diffQ"};
+  std::vector<std::vector<double>> dn(6, std::vector<double>((size_t)n, 0.0));
+  if (ctx->p.dif)
+    for (int q = 0; q < 6; q++)
+      if ((st = ccake_copy_out(ctx, dnames[q], dn[q].data()))) return st;
   std::ofstream out(path);
   if (!out.is_open()) return fail(ctx, CCAKE_ERR_INVALID, std::string("cannot write ") + path);
   // src/output.cpp:102-181 (print_system_state_to_txt), the same stream
   // manipulators in the same places: the header time and the first row's
   // time come out in the default format, every later number in scientific
   // notation with 6 digits; positions and velocities padded to 3 components;
-  // energies and chemical potentials in GeV; no diffusion sector (its six
-  // numbers are 0) and no causality check (0).
+  // energies and chemical potentials in GeV; the six diffusion numbers
+  // (zero without the sector) and no causality check (0).
   const double t = ctx->t;
   const double hc = kHbarcGeVfm;
   out << t << "\n";
@@ -1326,7 +1404,7 @@ ccake_status_t ccake_write_system_state(ccake_ctx* ctx, const char* path) {
     const int model = chain_model(ctx->eos.kind, eid[(size_t)i]);
     const char* eos_name = model == M_TABLE ? "table" : model == M_CDIAG ? "conformal_diagonal" : "conformal";
     out << F(34) << " " << frz[(size_t)i] << " " << eos_name << " " << 0 << " ";
-    for (int k = 0; k < 6; k++) out << 0.0 << " ";
+    for (int k = 0; k < 6; k++) out << dn[k][(size_t)i] << " ";
     out << "\n";
   }
   out << std::flush;
@@ -1402,6 +1480,8 @@ ccake_status_t ccake_preinverted_build(ccake_ctx* ctx, const ccake_preinv_config
 ccake_status_t ccake_preinverted_use(ccake_ctx* ctx, int32_t on) {
   if (!ctx) return CCAKE_ERR_INVALID;
   if (on && !ctx->pre_count) return fail(ctx, CCAKE_ERR_STATE, "build the pre-inverted tables first");
+  if (on && ctx->cfg.using_diffusion)
+    return fail(ctx, CCAKE_ERR_INVALID, "the diffusion sector needs the Newton EoS (alpha derivatives)");
   const PreinvView* want = on ? ctx->pre_dev : nullptr;
   if (ctx->eos.pre != want) {
     ctx->eos.pre = want;

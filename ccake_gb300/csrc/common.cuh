@@ -49,6 +49,26 @@ enum DerivSlot : int { D_DU0 = 0, D_DU1, D_DU2, D_DS, D_DBULK, D_DSHV0, D_DSHV1,
                        D_SNU,   // shv_nabla_u = pi^{ij} nabla_i u_j of the last evaluation
                        NDER };
 
+// Diffusion-sector slots (one n-long slab each; allocated only when the
+// sector is on). Charges c = B, S, Q; spatial directions i = 0..2.
+enum DifSlot : int {
+  F_YQ = 0,     // 9: extensive q (3c + i), current state
+  F_YQ0 = 9,    // 9: extensive q at the start of the RK2 step
+  F_Q = 18,     // 12: q^mu (4c + mu) of the last evaluation (after the regulator)
+  F_DA = 30,    // 12: dalpha_c/ds (c), dalpha_c/drho_d (3 + 3c + d)
+  F_GQ = 42,    // 3: v . grad q^0 sums (grad_qa)
+  F_DQ = 45,    // 3: div q (div_qa)
+  F_GA = 48,    // 9: grad alpha (3i + c)
+  F_DYQ = 57,   // 9: d(ext q)/dt (3c + i), written with the derivatives
+  F_DN = 66,    // 3: d(ext rho)/dt, written with the derivatives
+  F_KN = 69,    // 3: diffusion Knudsen numbers
+  F_IR = 72,    // 3: diffusion inverse Reynolds numbers
+  NDIF = 75
+};
+// Diffusion neighbour record (doubles): q^0_c / sl^2 (3), alpha_c (3),
+// q^i_c / sl^2 at 6 + 3i + c (9), one pad.
+constexpr int RQ = 16;
+
 // Neighbour-record strides (doubles). Record A feeds the smoothing pass,
 // record B the gradient pass; both are rewritten once per substep.
 //   A: x0 x1 x2 m | m*ext_s m*ext_B m*ext_S m*ext_Q

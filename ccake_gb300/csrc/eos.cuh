@@ -869,6 +869,77 @@ __host__ __device__ inline void set_thermo_o(const EosDev& e, int k, const doubl
   th[T_DWDQ] = mQ + ct;
 }
 
+// The twelve derivatives of alpha_a = mu_a / T at fixed (s, rho) read by the
+// diffusion sector (src/eos.cpp:337-493, dalpha_Bds .. dalpha_QdQ), at a
+// solution x with model thermodynamics o. out[a] = dalpha_a/ds,
+// out[3 + 3a + b] = dalpha_a/drho_b, a, b over (B, S, Q). The reference
+// chain (thermo_mode 0): dalpha_a/ds = -mu_a/T^2 / term1 + [rho_a] (1/T) /
+// term2(a); dalpha_a/drho_b = [rho_b] (-mu_a/T^2 / term3(b) + [rho_a] (1/T) /
+// term4(b, a)), [rho] meaning |rho| > TINY, dalpha_BdB with its 1/T term
+// first. thermo_mode 1: the same with the entries of H^-1 for 1/term.
+__host__ __device__ inline void alpha_derivs_o(const EosDev& e, int k, const double* x, const double* o,
+                                               double* out) {
+  const double T = x[0];
+  const double mu[3] = {x[1], x[3], x[2]};
+  const double rho[3] = {o[2], o[3], o[4]};
+  const Chi X{o[16], o[13], o[14], o[15], o[7], o[8], o[9], o[10], o[11], o[12]};
+  bool h[3];
+  for (int a = 0; a < 3; a++) h[a] = fabs(rho[a]) > kTiny;
+  const double iT = 1 / T;
+  if (e.thermo_mode == 1) {
+    const int model = chain_model(e.kind, k);
+    double H[4][4] = {{X.t2, X.tb, X.ts, X.tq}, {X.tb, X.b2, X.bs, X.bq}, {X.ts, X.bs, X.s2, X.sq},
+                      {X.tq, X.bq, X.sq, X.q2}};
+    if (model == M_CDIAG)
+      for (int i = 0; i < 4; i++) for (int j = 0; j < 4; j++) if (i != j) H[i][j] = 0.0;
+    int keep[4], m = 0;
+    for (int i = 0; i < 4; i++) {
+      bool zero = true;
+      for (int j = 0; j < 4; j++) zero = zero && (H[i][j] == 0.0);
+      if (!zero) keep[m++] = i;
+    }
+    double G[4][4];
+    hessian_inverse<double>(H, keep, m, G);
+    for (int a = 0; a < 3; a++) {
+      double ct = 0.0;
+      if (h[a]) ct += iT * G[a + 1][0];
+      out[a] = -mu[a] / T / T * G[0][0] + ct;
+      for (int b = 0; b < 3; b++) {
+        double v = 0.0;
+        if (h[b]) {
+          v += -mu[a] / T / T * G[0][b + 1];
+          if (h[a]) v += iT * G[a + 1][b + 1];
+        }
+        out[3 + 3 * a + b] = v;
+      }
+    }
+    return;
+  }
+  const double t1 = schur_term(X, 0);
+  for (int a = 0; a < 3; a++) {
+    double ct = 0.0;
+    if (h[a]) ct += iT / schur_term(X, 1 + a);
+    out[a] = -mu[a] / T / T / t1 + ct;
+  }
+  for (int b = 0; b < 3; b++) {
+    if (!h[b]) {
+      for (int a = 0; a < 3; a++) out[3 + 3 * a + b] = 0.0;
+      continue;
+    }
+    const double t3 = schur_term(X, 4 + b);
+    for (int a = 0; a < 3; a++) {
+      double v = 0.0;
+      if (a == 0 && b == 0) {
+        v += iT / schur_term(X, 7) - mu[0] / T / T / t3;
+      } else {
+        v += -mu[a] / T / T / t3;
+        if (h[a]) v += iT / schur_term(X, 7 + 3 * b + a);
+      }
+      out[3 + 3 * a + b] = v;
+    }
+  }
+}
+
 #ifdef __CUDACC__
 // EoS_Interpolator::fill_thermodynamics and interpolate4D
 // (src/eos_interpolator.cpp:531-739) for one point: densities clamped to

@@ -246,7 +246,7 @@ __device__ __forceinline__ void for_candidates(const RunConst& rc, const Ptrs& p
 // ---------------------------------------------------------------------------
 // pass A
 // ---------------------------------------------------------------------------
-template <int D>
+template <int D, bool DIFF>
 __global__ void __launch_bounds__(kBlock) k_passA(RunConst rc, EosDev eos, Ptrs p, int mode) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= p.n) return;
@@ -341,20 +341,88 @@ __global__ void __launch_bounds__(kBlock) k_passA(RunConst rc, EosDev eos, Ptrs 
     p.th[T_RQ * n + i] = s3 / g / t;
   }
   p.btrack[i] = nn;
-  if (mode == A_WITH_THERMO) thermo_tail<D, false>(rc, eos, p, i, t);
+  if (mode == A_WITH_THERMO) thermo_tail<D, false, DIFF>(rc, eos, p, i, t);
 }
 
-template <int D>
+template <int D, bool DIFF>
 __global__ void __launch_bounds__(kBlock) k_thermo(RunConst rc, EosDev eos, Ptrs p) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= p.n) return;
-  thermo_tail<D, false>(rc, eos, p, i, p.clock->t);
+  thermo_tail<D, false, DIFF>(rc, eos, p, i, p.clock->t);
+}
+
+// Diffusion sums of src/sph_workstation.cpp:909-967 over the list pass A
+// wrote, for particle a: v.grad q^0_c = sl_a sum_b m_b (v_a . grad W)
+// (q^0_b / sl_b^2 + q^0_a / sl_a^2), div q_c = sl_a sum_b m_b grad_k W
+// (q^k_b / sl_b^2 + q^k_a / sl_a^2) and grad_k alpha_c = sum_b (m_b / sl_a)
+// (alpha_b - alpha_a) grad_k W, in the separable form of pass B.
+template <int D>
+__global__ void __launch_bounds__(kBlock) k_diffgrad(Ptrs p) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.n) return;
+  const int n = p.n;
+  const double* rbA = p.recB + (size_t)i * RB;
+  const double xa[3] = {rbA[B_X0], rbA[B_X1], rbA[B_X2]};
+  double S1[D], SQ0[3][D], SA[3][D], SQI[3] = {0, 0, 0};
+#pragma unroll
+  for (int k = 0; k < D; k++) {
+    S1[k] = 0.0;
+#pragma unroll
+    for (int c = 0; c < 3; c++) SQ0[c][k] = SA[c][k] = 0.0;
+  }
+  const int cnt = min(p.btrack[i], p.K);
+  for (int kk = 0; kk < cnt; kk++) {
+    const int b = p.nbr_idx[(size_t)kk * n + i];
+    const double fg = p.nbr_f[(size_t)kk * n + i];
+    const double* rb = p.recB + (size_t)b * RB;
+    const double* rq = p.recQ + (size_t)b * RQ;
+    const double d[3] = {xa[0] - __ldg(rb + B_X0), xa[1] - __ldg(rb + B_X1), xa[2] - __ldg(rb + B_X2)};
+    const double mf = __ldg(rb + B_M) * fg;
+    double gm[D];
+#pragma unroll
+    for (int k = 0; k < D; k++) gm[k] = mf * d[k];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      const double q0 = __ldg(rq + c), al = __ldg(rq + 3 + c);
+      double acc = 0.0;
+#pragma unroll
+      for (int k = 0; k < D; k++) {
+        SQ0[c][k] += q0 * gm[k];
+        SA[c][k] += al * gm[k];
+        acc += __ldg(rq + 6 + 3 * k + c) * gm[k];
+      }
+      SQI[c] += acc;
+    }
+#pragma unroll
+    for (int k = 0; k < D; k++) S1[k] += gm[k];
+  }
+  const double sla = p.slab[i];
+  const double* rqA = p.recQ + (size_t)i * RQ;
+  const double va[3] = {rbA[B_V0], rbA[B_V0 + 1], rbA[B_V0 + 2]};
+  double vS1 = 0.0;
+#pragma unroll
+  for (int k = 0; k < D; k++) vS1 += va[k] * S1[k];
+  double* df = p.dif;
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    double vq = 0.0, qs = 0.0;
+#pragma unroll
+    for (int k = 0; k < D; k++) {
+      vq += va[k] * SQ0[c][k];
+      qs += rqA[6 + 3 * k + c] * S1[k];
+    }
+    df[(size_t)(F_GQ + c) * n + i] = sla * (vq + rqA[c] * vS1);
+    df[(size_t)(F_DQ + c) * n + i] = sla * (SQI[c] + qs);
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+      df[(size_t)(F_GA + 3 * k + c) * n + i] = (k < D) ? (SA[c][k] - rqA[3 + c] * S1[k]) / sla : 0.0;
+  }
 }
 
 // ---------------------------------------------------------------------------
 // pass B
 // ---------------------------------------------------------------------------
-template <int D>
+template <int D, bool DIFF>
 __global__ void __launch_bounds__(kBlock) k_passB(RunConst rc, Ptrs p, int mode, double dt_sub) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= p.n) return;
@@ -452,7 +520,7 @@ __global__ void __launch_bounds__(kBlock) k_passB(RunConst rc, Ptrs p, int mode,
       dS[k] = sla * acc2;
     }
   }
-  finish_particle<D, double, false>(rc, p, i, mode, t, dt_sub, va, gP, gE, gB, gS, dS, gV);
+  finish_particle<D, double, false, DIFF>(rc, p, i, mode, t, dt_sub, va, gP, gE, gB, gS, dS, gV);
 }
 
 __global__ void k_visc(RunConst rc, Ptrs p) {
@@ -550,6 +618,17 @@ __global__ void k_init_ext(RunConst rc, Ptrs p) {
   ra[3] = make_double2(m * p.y[Y_ESS * n + i], m * p.y[Y_EQ * n + i]);
 }
 
+// set_diffusion (src/sph_workstation.cpp:1441-1458): ext q = q^i / sigma;
+// the initial spatial currents q^i wait in the step-start slots until here
+__global__ void k_init_diffusion(Ptrs p) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.n) return;
+  const int n = p.n;
+  const double sg = p.sig[i];
+#pragma unroll
+  for (int q = 0; q < 9; q++) p.dif[(size_t)(F_YQ + q) * n + i] = p.dif[(size_t)(F_YQ0 + q) * n + i] / sg;
+}
+
 // FP64 smoothing record from the state (after mixed substeps moved the particles)
 template <int D>
 __global__ void k_pack_fp64(Ptrs p) {
@@ -573,11 +652,23 @@ __global__ void __launch_bounds__(256) k_totals(RunConst rc, Ptrs p) {
   double acc[6] = {0, 0, 0, 0, 0, 0};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const double m = p.m[i];
-    acc[0] += p.y[Y_ES * n + i] * m;
-    acc[1] += p.y[Y_EB * n + i] * m;
-    acc[2] += p.y[Y_ESS * n + i] * m;
-    acc[3] += p.y[Y_EQ * n + i] * m;
     const double g = p.gam[i];
+    acc[0] += p.y[Y_ES * n + i] * m;
+    if (p.dif) {
+      // the q^0 terms of src/system_state.cpp:755-828, with the reference's
+      // mass factors
+      const double sg = p.sig[i];
+      const double eqb = p.dif[(size_t)F_Q * n + i] * m / sg / g;
+      const double eqs = p.dif[(size_t)(F_Q + 4) * n + i] * m / sg / g;
+      const double eqq = p.dif[(size_t)(F_Q + 8) * n + i] * m / sg / g;
+      acc[1] += p.y[Y_EB * n + i] * m + eqb * m / g;
+      acc[2] += p.y[Y_ESS * n + i] * m + (eqs);
+      acc[3] += p.y[Y_EQ * n + i] * m + (eqq);
+    } else {
+      acc[1] += p.y[Y_EB * n + i] * m;
+      acc[2] += p.y[Y_ESS * n + i] * m;
+      acc[3] += p.y[Y_EQ * n + i] * m;
+    }
     const double C = p.th[T_W * n + i] + p.bulk[i];
     acc[4] += (C * g * g - p.th[T_P * n + i] - p.bulk[i] + p.pi[P00 * n + i]) * m * sqrtg / p.slab[i];
     acc[5] += p.y[Y_EZ * n + i];
@@ -977,7 +1068,7 @@ __global__ void k_freeze_advance(Clock* c) {
 // sqrt|sigma:sigma| and tau_Pi |theta|, inverse Reynolds numbers
 // sqrt|pi:pi| / p and |Pi| / p. grads_f32: the gradients are the mixed
 // form's FP32 view.
-template <int D>
+template <int D, bool DIFF>
 __global__ void k_diag(RunConst rc, Ptrs p, int grads_f32) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= p.n) return;
@@ -1012,7 +1103,30 @@ __global__ void k_diag(RunConst rc, Ptrs p, int grads_f32) {
   const TransportT<double> k = transport<double>(rc.cfg, th);
   EomOut<double> o;
   double dg[7];
-  eom<D, double>(rc.cfg, k, in, t, o, dg);
+  if constexpr (DIFF) {
+    // with the diffusion sector: its coupling into du/dt, and its Knudsen
+    // and inverse Reynolds numbers (src/eom_default.cpp:1944-1982)
+    DiffIn din;
+    DiffOut dout;
+    load_diff_in(rc, p, i, th, din);
+    eom<D, double>(rc.cfg, k, in, t, o, dg, &din, &dout);
+    const double rho[3] = {th[T_RB], th[T_RS], th[T_RQ]};
+    for (int c = 0; c < 3; c++) {
+      double gsq = 0.0;
+      for (int a = 0; a < D; a++) {
+        const double gg = din.ga[3 * a + c];
+        gsq += gg * gg;
+      }
+      p.dif[(size_t)(F_KN + c) * n + i] = din.tq[4 * c] * sqrt(gsq);
+      const double* q = din.q + 4 * c;
+      const double q_sq = q[1] * q[1] + q[2] * q[2] + t2 * q[3] * q[3] - q[0] * q[0];
+      const double q_mag = q_sq > 0.0 ? sqrt(q_sq) : 0.0;
+      const double n_abs = fabs(rho[c]);
+      p.dif[(size_t)(F_IR + c) * n + i] = (n_abs > 1e-15) ? q_mag / n_abs : 0.0;
+    }
+  } else {
+    eom<D, double>(rc.cfg, k, in, t, o, dg);
+  }
   double* dv = p.derivs;
   dv[D_ETA * n + i] = k.eta;
   dv[D_TAUPI * n + i] = k.tau_pi;
@@ -1021,7 +1135,9 @@ __global__ void k_diag(RunConst rc, Ptrs p, int grads_f32) {
   dv[D_THETA * n + i] = dg[0];
   dv[D_SNU * n + i] = dg[6];
   double kns = 0.0, knb = 0.0, irs = 0.0, irb = 0.0;
-  if (rc.cfg.using_shear) {
+  // computed with shear or diffusion (src/eom_default.cpp:865-867); without
+  // shear the sigma tensor and pi are zero
+  if (rc.cfg.using_shear || DIFF) {
     for (int q = 0; q < 5; q++) dv[(D_SIG0 + q) * n + i] = dg[1 + q];
     const double g = in.g;
     const double uc[3] = {-in.u[0], -in.u[1], D == 3 ? -t2 * in.u[2] : 0.0};
@@ -1114,20 +1230,48 @@ void launch_candidates(const RunConst& rc, const Ptrs& p, cudaStream_t s) {
 
 void launch_passA(const RunConst& rc, const EosDev& eos, const Ptrs& p, int mode, cudaStream_t s) {
   const int nb = (p.n + kBlock - 1) / kBlock;
-  if (rc.cfg.dim == 3) k_passA<3><<<nb, kBlock, 0, s>>>(rc, eos, p, mode);
-  else k_passA<2><<<nb, kBlock, 0, s>>>(rc, eos, p, mode);
+  const bool dif = rc.cfg.using_diffusion && p.dif;
+  if (rc.cfg.dim == 3) {
+    if (dif) k_passA<3, true><<<nb, kBlock, 0, s>>>(rc, eos, p, mode);
+    else k_passA<3, false><<<nb, kBlock, 0, s>>>(rc, eos, p, mode);
+  } else {
+    if (dif) k_passA<2, true><<<nb, kBlock, 0, s>>>(rc, eos, p, mode);
+    else k_passA<2, false><<<nb, kBlock, 0, s>>>(rc, eos, p, mode);
+  }
 }
 
 void launch_thermo(const RunConst& rc, const EosDev& eos, const Ptrs& p, cudaStream_t s) {
   const int nb = (p.n + kBlock - 1) / kBlock;
-  if (rc.cfg.dim == 3) k_thermo<3><<<nb, kBlock, 0, s>>>(rc, eos, p);
-  else k_thermo<2><<<nb, kBlock, 0, s>>>(rc, eos, p);
+  const bool dif = rc.cfg.using_diffusion && p.dif;
+  if (rc.cfg.dim == 3) {
+    if (dif) k_thermo<3, true><<<nb, kBlock, 0, s>>>(rc, eos, p);
+    else k_thermo<3, false><<<nb, kBlock, 0, s>>>(rc, eos, p);
+  } else {
+    if (dif) k_thermo<2, true><<<nb, kBlock, 0, s>>>(rc, eos, p);
+    else k_thermo<2, false><<<nb, kBlock, 0, s>>>(rc, eos, p);
+  }
 }
 
+// With the diffusion sector, its gradient sums run first (they read the
+// diffusion records of the neighbours, complete after the thermo pass).
 void launch_passB(const RunConst& rc, const Ptrs& p, int mode, double dt_sub, cudaStream_t s) {
   const int nb = (p.n + kBlock - 1) / kBlock;
-  if (rc.cfg.dim == 3) k_passB<3><<<nb, kBlock, 0, s>>>(rc, p, mode, dt_sub);
-  else k_passB<2><<<nb, kBlock, 0, s>>>(rc, p, mode, dt_sub);
+  const bool dif = rc.cfg.using_diffusion && p.dif;
+  if (rc.cfg.dim == 3) {
+    if (dif) {
+      k_diffgrad<3><<<nb, kBlock, 0, s>>>(p);
+      k_passB<3, true><<<nb, kBlock, 0, s>>>(rc, p, mode, dt_sub);
+    } else {
+      k_passB<3, false><<<nb, kBlock, 0, s>>>(rc, p, mode, dt_sub);
+    }
+  } else {
+    if (dif) {
+      k_diffgrad<2><<<nb, kBlock, 0, s>>>(p);
+      k_passB<2, true><<<nb, kBlock, 0, s>>>(rc, p, mode, dt_sub);
+    } else {
+      k_passB<2, false><<<nb, kBlock, 0, s>>>(rc, p, mode, dt_sub);
+    }
+  }
 }
 
 void launch_visc(const RunConst& rc, const Ptrs& p, cudaStream_t s) {
@@ -1150,6 +1294,11 @@ void launch_init_ext(const RunConst& rc, const Ptrs& p, cudaStream_t s) {
   const int nb = (p.n + kBlock - 1) / kBlock;
   if (rc.cfg.dim == 3) k_init_ext<3><<<nb, kBlock, 0, s>>>(rc, p);
   else k_init_ext<2><<<nb, kBlock, 0, s>>>(rc, p);
+}
+
+void launch_init_diffusion(const RunConst& rc, const Ptrs& p, cudaStream_t s) {
+  (void)rc;
+  if (p.dif) k_init_diffusion<<<(p.n + kBlock - 1) / kBlock, kBlock, 0, s>>>(p);
 }
 
 void launch_pack_fp64(const RunConst& rc, const Ptrs& p, cudaStream_t s) {
@@ -1176,8 +1325,14 @@ void launch_freeze_surface(const RunConst& rc, const Ptrs& p, int grads_f32, dou
 
 void launch_diagnostics(const RunConst& rc, const Ptrs& p, int grads_f32, cudaStream_t s) {
   const int nb = (p.n + kBlock - 1) / kBlock;
-  if (rc.cfg.dim == 3) k_diag<3><<<nb, kBlock, 0, s>>>(rc, p, grads_f32);
-  else k_diag<2><<<nb, kBlock, 0, s>>>(rc, p, grads_f32);
+  const bool dif = rc.cfg.using_diffusion && p.dif;
+  if (rc.cfg.dim == 3) {
+    if (dif) k_diag<3, true><<<nb, kBlock, 0, s>>>(rc, p, grads_f32);
+    else k_diag<3, false><<<nb, kBlock, 0, s>>>(rc, p, grads_f32);
+  } else {
+    if (dif) k_diag<2, true><<<nb, kBlock, 0, s>>>(rc, p, grads_f32);
+    else k_diag<2, false><<<nb, kBlock, 0, s>>>(rc, p, grads_f32);
+  }
 }
 
 void launch_table_f32(const double* f, float* fd, int64_t nodes, cudaStream_t s) {

@@ -56,6 +56,9 @@ struct Ptrs {
   // mixed-precision form (precision = 1): FP32 neighbour records
   float* recAf;          // RAF * n
   float* recBf;          // RBF * n
+  // diffusion sector (null when off)
+  double* dif;           // NDIF * n
+  double* recQ;          // RQ * n   neighbour record of the diffusion sums
 };
 
 // Mixed-precision neighbour records. A position x is carried as the float
@@ -88,6 +91,7 @@ void launch_clock(const Ptrs& p, int substep, double dt, cudaStream_t s);
 void launch_init_state(const RunConst& rc, const Ptrs& p, cudaStream_t s);
 void launch_init_invert(const RunConst& rc, const EosDev& eos, const Ptrs& p, cudaStream_t s);
 void launch_init_ext(const RunConst& rc, const Ptrs& p, cudaStream_t s);
+void launch_init_diffusion(const RunConst& rc, const Ptrs& p, cudaStream_t s);
 void launch_totals(const RunConst& rc, const Ptrs& p, int nblocks, cudaStream_t s);
 void launch_neighbour_counts(const RunConst& rc, const Ptrs& p, int32_t* counts, cudaStream_t s);
 void launch_neighbour_fill(const RunConst& rc, const Ptrs& p, const int32_t* offsets, int32_t* idx,

@@ -127,7 +127,10 @@ __device__ __forceinline__ void write_recAf(const Ptrs& p, int i, const double* 
 
 // EoS inversion of the smoothed densities of particle i, pi^{mu nu} and Pi
 // from the extensive forms, and its gradient record (FP64 or mixed form).
-template <int D, bool MIX>
+// DIFF: the diffusion sector (FP64 form): the alpha derivatives at the
+// solution, q^mu from the extensive current (src/eom_default.cpp:140-165),
+// the regulator (src/sph_workstation.cpp:132-218) and the diffusion record.
+template <int D, bool MIX, bool DIFF = false>
 __device__ __forceinline__ void thermo_tail(const RunConst& rc, const EosDev& eos, const Ptrs& p, int i, double t) {
   const int n = p.n;
   const double t2 = rc.cfg.coord == 1 ? 1.0 : t * t;   // the metric's tau^2 (1 in Cartesian coordinates)
@@ -164,6 +167,12 @@ __device__ __forceinline__ void thermo_tail(const RunConst& rc, const EosDev& eo
       return;
     }
     set_thermo_o(eos, k, x, o, th, MIX);
+    if constexpr (DIFF) {
+      double da[12];
+      alpha_derivs_o(eos, k, x, o, da);
+#pragma unroll
+      for (int q = 0; q < 12; q++) p.dif[(size_t)(F_DA + q) * n + i] = da[q];
+    }
   }
 #pragma unroll
   for (int q = 0; q < NTH; q++) p.th[q * n + i] = th[q];
@@ -183,6 +192,53 @@ __device__ __forceinline__ void thermo_tail(const RunConst& rc, const EosDev& eo
   for (int q = 0; q < NPI; q++) p.pi[q * n + i] = pi[q];
   // neighbour record B
   const double isl2 = 1.0 / (slab * slab);
+  if constexpr (DIFF) {
+    // q^i = ext q sigma, q^0 = -q^i u_i / gamma (u_i of the three-vector u
+    // padded with zeros); then the regulator caps |q| at rq_max |n| f(e)
+    const double fc[3] = {-u3[0], -u3[1], -t2 * u3[2]};
+    double q[12];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      double q0 = 0.;
+#pragma unroll
+      for (int k2 = 0; k2 < 3; k2++) q[4 * c + k2 + 1] = p.dif[(size_t)(F_YQ + 3 * c + k2) * n + i] * sig;
+#pragma unroll
+      for (int k2 = 0; k2 < 3; k2++) q0 += -q[4 * c + k2 + 1] * fc[k2] / g;
+      q[4 * c] = q0;
+    }
+    if (rc.cfg.diffusion_regulator) {
+      const double e0 = rc.cfg.reg_e0 / kHbarcGeVfm, xi0 = rc.cfg.reg_xi0 / kHbarcGeVfm;
+      const double fermi_offset = 1.0 / (exp(e0 / xi0) + 1.0);
+      const double ferm = 1.0 / (exp(-(th[T_E] - e0) / xi0) + 1.0);
+      const double f_str = rc.cfg.reg_chi0 * (ferm - fermi_offset);
+      const double rho[3] = {th[T_RB], th[T_RS], th[T_RQ]};
+      for (int c = 0; c < 3; c++) {
+        const double n_abs = fabs(rho[c]);
+        if (n_abs < 1.0e-15) continue;
+        const double q3_sq = rc.cfg.coord == 0 ? t2 * q[4 * c + 3] * q[4 * c + 3] : q[4 * c + 3] * q[4 * c + 3];
+        const double q_sq = q[4 * c + 1] * q[4 * c + 1] + q[4 * c + 2] * q[4 * c + 2] + q3_sq - q[4 * c] * q[4 * c];
+        if (q_sq <= 0.0) continue;
+        const double q_mag = sqrt(q_sq);
+        const double threshold = rc.cfg.reg_rq_max * n_abs * f_str;
+        if (q_mag <= threshold) continue;
+        const double scale = threshold / q_mag;
+        for (int m = 0; m < 4; m++) q[4 * c + m] = q[4 * c + m] * scale;
+      }
+    }
+    double* rq = p.recQ + (size_t)i * RQ;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+#pragma unroll
+      for (int m = 0; m < 4; m++) p.dif[(size_t)(F_Q + 4 * c + m) * n + i] = q[4 * c + m];
+      rq[c] = q[4 * c] * isl2;
+#pragma unroll
+      for (int k2 = 0; k2 < 3; k2++) rq[6 + 3 * k2 + c] = q[4 * c + k2 + 1] * isl2;
+    }
+    rq[3] = th[T_MUB] / th[T_T];
+    rq[4] = th[T_MUS] / th[T_T];
+    rq[5] = th[T_MUQ] / th[T_T];
+    rq[15] = 0.0;
+  }
   if constexpr (MIX) {
     float hi[3], lo[3];
 #pragma unroll
@@ -219,12 +275,34 @@ __device__ __forceinline__ void thermo_tail(const RunConst& rc, const EosDev& eo
   }
 }
 
+// Diffusion inputs of the equations of motion of particle i: q^mu, the
+// alpha derivatives and the diffusion sums of the last evaluation, tau_q and
+// kappa_q from its thermodynamics th.
+__device__ __forceinline__ void load_diff_in(const RunConst& rc, const Ptrs& p, int i, const double* th,
+                                             DiffIn& din) {
+  const int n = p.n;
+  const double* df = p.dif;
+#pragma unroll
+  for (int q = 0; q < 12; q++) {
+    din.q[q] = df[(size_t)(F_Q + q) * n + i];
+    din.da[q] = df[(size_t)(F_DA + q) * n + i];
+  }
+#pragma unroll
+  for (int q = 0; q < 9; q++) din.ga[q] = df[(size_t)(F_GA + q) * n + i];
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    din.gq[c] = df[(size_t)(F_GQ + c) * n + i];
+    din.dq[c] = df[(size_t)(F_DQ + c) * n + i];
+  }
+  diffusion_coefs(rc.cfg, th, rc.cfg.eos_kind == 2 && p.eos_id[i] == 0, din.tq, din.kq);
+}
+
 // Everything of pass B after the gradients, for particle i: optional export
 // of the gradients, the equations of motion (in type R), optional export of
 // the derivatives, the midpoint RK2 update of the FP64 state from the
 // step-start cache (reference src/evolver.cpp:344-486) and the smoothing
 // record for the next substep (FP64 or mixed form).
-template <int D, typename R, bool MIX>
+template <int D, typename R, bool MIX, bool DIFF = false>
 __device__ __forceinline__ void finish_particle(const RunConst& rc, const Ptrs& p, int i, int mode, double t,
                                                 double dt_sub, const R* va, const R* gP, const R* gE, const R* gB,
                                                 const R* gS, const R* dS, const R* gV) {
@@ -267,7 +345,14 @@ __device__ __forceinline__ void finish_particle(const RunConst& rc, const Ptrs& 
   for (int q = 0; q < NPI; q++) in.pi[q] = R(p.pi[q * n + i]);
   const TransportT<R> k = transport<R>(rc.cfg, th);
   EomOut<R> o;
-  eom<D, R>(rc.cfg, k, in, t, o);
+  DiffOut dout;
+  if constexpr (DIFF) {
+    DiffIn din;
+    load_diff_in(rc, p, i, th, din);
+    eom<D, R>(rc.cfg, k, in, t, o, nullptr, &din, &dout);
+  } else {
+    eom<D, R>(rc.cfg, k, in, t, o);
+  }
   if (mode & B_DERIVS) {
 #pragma unroll
     for (int q = 0; q < 3; q++) p.derivs[(D_DU0 + q) * n + i] = (q < D) ? double(o.du[q]) : 0.0;
@@ -280,6 +365,12 @@ __device__ __forceinline__ void finish_particle(const RunConst& rc, const Ptrs& 
     p.derivs[D_TAUPI * n + i] = k.tau_pi;
     p.derivs[D_ZETA * n + i] = k.zeta;
     p.derivs[D_TAUBULK * n + i] = k.tau_Pi;
+    if constexpr (DIFF) {
+#pragma unroll
+      for (int c = 0; c < 3; c++) p.dif[(size_t)(F_DN + c) * n + i] = dout.dN[c];
+#pragma unroll
+      for (int q = 0; q < 9; q++) p.dif[(size_t)(F_DYQ + q) * n + i] = dout.dQ[q];
+    }
   }
   if (!(mode & B_UPDATE)) return;
   const double* y0 = p.y0;
@@ -296,6 +387,13 @@ __device__ __forceinline__ void finish_particle(const RunConst& rc, const Ptrs& 
 #pragma unroll
   for (int q = 0; q < 5; q++) ynew[Y_SHV0 + q] += dt_sub * double(o.dShv[q]);
   ynew[Y_EZ] += dt_sub * double(o.dEz);
+  double yq[9];
+  if constexpr (DIFF) {
+#pragma unroll
+    for (int c = 0; c < 3; c++) ynew[Y_EB + c] += dt_sub * dout.dN[c];
+#pragma unroll
+    for (int q = 0; q < 9; q++) yq[q] = p.dif[(size_t)(F_YQ0 + q) * n + i] + dt_sub * dout.dQ[q];
+  }
   if (es < 0.0) {
     if (p.freeze[i] > 3) es = 1.e-3;
     else atomicAdd(&p.err[E_NEGS], 1);
@@ -304,12 +402,24 @@ __device__ __forceinline__ void finish_particle(const RunConst& rc, const Ptrs& 
   bool finite = true;
 #pragma unroll
   for (int q = 0; q < NY; q++) finite = finite && isfinite(ynew[q]);
+  if constexpr (DIFF) {
+#pragma unroll
+    for (int q = 0; q < 9; q++) finite = finite && isfinite(yq[q]);
+  }
   if (!finite) atomicAdd(&p.err[E_NONFINITE], 1);
 #pragma unroll
   for (int q = 0; q < NY; q++) p.y[q * n + i] = ynew[q];
+  if constexpr (DIFF) {
+#pragma unroll
+    for (int q = 0; q < 9; q++) p.dif[(size_t)(F_YQ + q) * n + i] = yq[q];
+  }
   if (mode & B_WRITE_Y0) {
 #pragma unroll
     for (int q = 0; q < NY; q++) p.y0[q * n + i] = ynew[q];
+    if constexpr (DIFF) {
+#pragma unroll
+      for (int q = 0; q < 9; q++) p.dif[(size_t)(F_YQ0 + q) * n + i] = yq[q];
+    }
   }
   const double x[3] = {ynew[Y_X0], ynew[Y_X1], D == 3 ? ynew[Y_X2] : 0.0};
   const double ext[4] = {ynew[Y_ES], ynew[Y_EB], ynew[Y_ESS], ynew[Y_EQ]};

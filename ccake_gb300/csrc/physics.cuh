@@ -2,6 +2,8 @@
 // pi^{mu nu} constraints, and the MRF equations of motion (ideal + shear +
 // bulk, Milne coordinates) for one particle. FP64, templated on dimension.
 #pragma once
+#include <type_traits>
+
 #include "common.cuh"
 
 namespace ccake {
@@ -72,6 +74,71 @@ __device__ inline TransportT<R> transport(const ccake_config& c, const double* t
   return k;
 }
 
+// Diffusion coefficients, src/transport_coefficients.cpp:571-617 (kappa,
+// tauq), :918-973 (default_kappa = kappa/T^2 T^2, default_tauq = 0.2/T on
+// the diagonal), :981-1040 (kappaB_coth, tauqB_only) and :1048-1057 (the
+// Gaussian suppression near the critical point, table EoS only). tq, kq
+// row-major 3x3 over (B, S, Q).
+__device__ inline void diffusion_coefs(const ccake_config& c, const double* th, bool table_eos, double* tq,
+                                       double* kq) {
+  const double T = th[T_T];
+  for (int k = 0; k < 9; k++) tq[k] = kq[k] = 0.0;
+  if (c.diffusion_mode == 2) {
+    const double muB = th[T_MUB], nB = th[T_RB], w = th[T_W];
+    const double x = (T > kTiny) ? muB / T : 0.0;
+    if (T > kTiny && fabs(w) > kTiny && fabs(x) > 1.0e-2) {
+      const double kB = (c.C_B / T) * nB * ((1.0 / 3.0) / tanh(x) - nB * T / w);
+      if (isfinite(kB) && kB > 0.0) kq[0] = kB;
+    }
+    if (c.diffusion_relax_mode == 1) {
+      if (T > kTiny)
+        for (int i = 0; i < 3; i++) tq[4 * i] = c.C_B / T;
+    } else {
+      for (int i = 0; i < 3; i++) tq[4 * i] += 0.2 / T;
+    }
+    return;
+  }
+  double sup = 1.0;
+  if (c.critical_scaling_diffusion && table_eos) {
+    const double dT = T - c.crit_T / kHbarcMeVfm, dm = th[T_MUB] - c.crit_muB / kHbarcMeVfm;
+    const double sT = c.crit_wT / kHbarcMeVfm, sm = c.crit_wmuB / kHbarcMeVfm;
+    const double ex = 0.5 * (dT * dT / (sT * sT) + dm * dm / (sm * sm));
+    sup = 1.0 - exp(-ex);
+  }
+  for (int k = 0; k < 9; k++) kq[k] = sup * c.kappa_over_T2[k] * (T * T);
+  for (int i = 0; i < 3; i++) tq[4 * i] += 0.2 / T;
+}
+
+// 3x3 inverse by cofactors over the determinant (include/milne.hpp:788-834).
+__device__ inline void inverse3(const double* A, double* Ai) {
+#define M3(i, j) A[(i) * 3 + (j)]
+  const double det = M3(0, 0) * M3(1, 1) * M3(2, 2) + M3(0, 1) * M3(1, 2) * M3(2, 0) + M3(0, 2) * M3(1, 0) * M3(2, 1) -
+                     M3(0, 2) * M3(1, 1) * M3(2, 0) - M3(0, 1) * M3(1, 0) * M3(2, 2) - M3(0, 0) * M3(1, 2) * M3(2, 1);
+  Ai[0] = (M3(1, 1) * M3(2, 2) - M3(1, 2) * M3(2, 1)) / det;
+  Ai[1] = (M3(0, 2) * M3(2, 1) - M3(0, 1) * M3(2, 2)) / det;
+  Ai[2] = (M3(0, 1) * M3(1, 2) - M3(0, 2) * M3(1, 1)) / det;
+  Ai[3] = (M3(1, 2) * M3(2, 0) - M3(1, 0) * M3(2, 2)) / det;
+  Ai[4] = (M3(0, 0) * M3(2, 2) - M3(0, 2) * M3(2, 0)) / det;
+  Ai[5] = (M3(0, 2) * M3(1, 0) - M3(0, 0) * M3(1, 2)) / det;
+  Ai[6] = (M3(1, 0) * M3(2, 1) - M3(1, 1) * M3(2, 0)) / det;
+  Ai[7] = (M3(0, 1) * M3(2, 0) - M3(0, 0) * M3(2, 1)) / det;
+  Ai[8] = (M3(0, 0) * M3(1, 1) - M3(0, 1) * M3(1, 0)) / det;
+#undef M3
+}
+
+// Diffusion inputs of the equations of motion for one particle (FP64 form).
+struct DiffIn {
+  double q[12];          // q^mu of charge c at 4c + mu
+  double da[12];         // dalpha_c/ds (c), dalpha_c/drho_d (3 + 3c + d)
+  double ga[9];          // grad alpha, direction i, charge c at 3i + c (i < D)
+  double gq[3], dq[3];   // v . grad q^0 and div q sums
+  double tq[9], kq[9];   // tau_q, kappa_q
+};
+struct DiffOut {
+  double dN[3];          // d(ext rho_c)/dt
+  double dQ[9];          // d(ext q)/dt, charge c, direction i at 3c + i
+};
+
 // gamma = sqrt(1 - u_i u^i) in Milne coordinates (reference src/eom_default.cpp:17-38,
 // include/milne.hpp:92-96 and :354).
 template <int D>
@@ -122,9 +189,13 @@ struct EomOut {
 // state update it feeds stays FP64).
 // diag (optional, 7 values): theta, sigma^{11,12,13,22,23} and
 // shv_nabla_u (src/eom_default.cpp:764-807); the hot kernels pass none.
+// dif / dout (FP64 form only): the diffusion sector, src/eom_default.cpp:
+// 1415-1817 (calculate_MRF_diffusion; the stray semicolon of :1744 ends
+// F_D_ib after its second term), :368-451 (charge MRFs), :579-617 (coupling
+// into du/dt), :690-736 (dN/dt, d(ext q)/dt) and the R_S dN/dt entropy term.
 template <int D, typename R = double>
 __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, const EomIn<D, R>& in, double td,
-                           EomOut<R>& o, R* diag = nullptr) {
+                           EomOut<R>& o, R* diag = nullptr, const DiffIn* dif = nullptr, DiffOut* dout = nullptr) {
   R sigF[5] = {0, 0, 0, 0, 0}, sigM[5][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
   const R t = R(td);
   // Cartesian coordinates (coord = 1, src/eom_cartesian.cpp:210-1400): the
@@ -413,6 +484,104 @@ __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, cons
     if (cfg.using_shear)
       Fu[i] += -P(i + 1, 0) * itc - R(2.) * dEta(i) * P(0, 3) * it - in.divshear[i] + in.gradshear[i] - F0i[i];
   }
+  // ---- diffusion sector: time components of the q MRFs and the charge
+  // MRFs, coupled into the four-acceleration -----------------------------------
+  double RI[9], MN[3][3], FN[3];
+  if constexpr (std::is_same<R, double>::value) {
+    if (dif) {
+      const double sig_ = sig, g_ = g;
+      const double mu[3] = {th[T_MUB], th[T_MUS], th[T_MUQ]};
+      double RS[3], MS[3] = {0, 0, 0};
+      for (int c = 0; c < 3; c++) RS[c] = -mu[c] / T;
+      for (int i = 0; i < D; i++) MS[i] = Ms[i];
+      double itq[9], itt[9], itk[9];
+      inverse3(dif->tq, itq);
+      for (int c = 0; c < 3; c++)
+        for (int d = 0; d < 3; d++) {
+          double a1 = 0.0, a2 = 0.0;
+          for (int kk = 0; kk < 3; kk++) {
+            a1 += itq[3 * c + kk] * dif->tq[3 * kk + d];
+            a2 += itq[3 * c + kk] * dif->kq[3 * kk + d];
+          }
+          itt[3 * c + d] = a1;
+          itk[3 * c + d] = a2;
+        }
+      const double X_ = g_ * divV + geo + g_ / t;
+      const double omg = 1. - g_ * g_;
+      double qc[3][4];
+      for (int c = 0; c < 3; c++) {
+        qc[c][0] = dif->q[4 * c];
+        qc[c][1] = -dif->q[4 * c + 1];
+        qc[c][2] = -dif->q[4 * c + 2];
+        qc[c][3] = -t2 * dif->q[4 * c + 3];
+      }
+      double F0D[3], F0a[3], A0a[3], R0a[3][3], M0a[3][3], M0D[3][3];
+      for (int c = 0; c < 3; c++) {
+        const double q0 = dif->q[4 * c];
+        F0D[c] = g_ * g_ * geo * q0 + 2. * g_ * g_ * qc[c][3] * u[2] / t + t * g_ * qc[c][0] * u[2] * u[2] +
+                 t * u[2] * dif->q[4 * c + 3];
+        F0a[c] = omg * sig_ * dif->da[c] * Fs;
+        A0a[c] = -omg * dif->da[c] * double(sden) / g_;
+        for (int i = 0; i < D; i++) {
+          M0D[c][i] = g_ * g_ * (qc[c][i + 1] - qc[c][0] * uc[i] / g_);
+          M0a[c][i] = omg * sig_ * dif->da[c] * MS[i];
+          F0a[c] += -dif->ga[3 * i + c] * u[i] / g_;
+        }
+        for (int d = 0; d < 3; d++) {
+          R0a[c][d] = omg * sig_ * (dif->da[c] * RS[d] + dif->da[3 + 3 * c + d]);
+          A0a[c] += -omg * dif->da[3 + 3 * c + d] * rho[d] / g_;
+        }
+      }
+      // charge MRFs: R_N = gamma sigma 1 - R_0q, M_N = -M_0q, F_N = -F_0q +
+      // grad q - div q - q^0 / t (no external sources)
+      double RN[9];
+      for (int c = 0; c < 9; c++) RN[c] = 0.0;
+      for (int c = 0; c < 3; c++) RN[4 * c] += g_ * sig_;
+      for (int c = 0; c < 3; c++) {
+        double F0q = 0.0;
+        for (int d = 0; d < 3; d++)
+          F0q += (-itt[3 * c + d] * F0D[d] - itq[3 * c + d] * dif->q[4 * d] + itk[3 * c + d] * F0a[d] +
+                  itk[3 * c + d] * A0a[d] * X_) / (g_) -
+                 itt[3 * c + d] * dif->q[4 * d] * X_ / g_;
+        for (int i = 0; i < 3; i++) MN[i][c] = 0.0;
+        for (int i = 0; i < D; i++) {
+          double acc = 0.0;
+          for (int d = 0; d < 3; d++)
+            acc += (-itt[3 * c + d] * M0D[d][i] + itk[3 * c + d] * M0a[d][i] - itk[3 * c + d] * A0a[d] * uc[i] / g_) /
+                       (g_) +
+                   itt[3 * c + d] * dif->q[4 * d] * uc[i] / g_ / g_;
+          MN[i][c] = 0.0 + -acc;
+        }
+        for (int d = 0; d < 3; d++) {
+          double acc = 0.0;
+          for (int kk = 0; kk < 3; kk++) acc += itk[3 * c + kk] * R0a[kk][d] / (g_);
+          RN[3 * c + d] += -acc;
+        }
+        FN[c] = 0.0;
+        FN[c] += -F0q + dif->gq[c] - dif->dq[c] - dif->q[4 * c] / t;
+      }
+      inverse3(RN, RI);
+      // R_u = -u gamma (R_w + R_bulk sigma), R_w = sigma dw/drho + sigma dw/ds R_S
+      double Ru[3][3];
+      for (int i = 0; i < D; i++)
+        for (int c = 0; c < 3; c++) {
+          const double Rw = sig_ * dwdr[c] + sig_ * dwds * RS[c];
+          Ru[i][c] = -u[i] * g_ * (Rw + 0.0 * sig_);
+        }
+      for (int i = 0; i < D; i++) {
+        double FR = 0.0;
+        for (int j = 0; j < D; j++) {
+          double MR = 0.0;
+          for (int c = 0; c < 3; c++)
+            for (int d = 0; d < 3; d++) MR += Ru[i][c] * RI[3 * c + d] * MN[j][d];
+          Mu[i * D + j] = Mu[i * D + j] - MR;
+        }
+        for (int c = 0; c < 3; c++)
+          for (int d = 0; d < 3; d++) FR += Ru[i][c] * RI[3 * c + d] * FN[d];
+        Fu[i] = Fu[i] + FR;
+      }
+    }
+  }
   // du/dt = M^-1 F by cofactors (include/milne.hpp:788-834)
   R du[3];
   if (D == 2) {
@@ -440,6 +609,90 @@ __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, cons
   for (int i = 0; i < D; i++) { m1 += Ms[i] * du[i]; m2 += Mb[i] * du[i]; o.du[i] = du[i]; }
   o.dS = m1 + Fs;
   o.dBulk = m2 + Fb;
+  if constexpr (std::is_same<R, double>::value) {
+    if (dif) {
+      // dN/dt = R_N^-1 (F_N + M_N du/dt); the entropy picks up R_S dN/dt;
+      // d(ext q)/dt = F_q + M_q du/dt + R_q dN/dt over all three directions
+      double MU[3], dN[3];
+      for (int c = 0; c < 3; c++) {
+        MU[c] = 0.;
+        for (int i = 0; i < D; i++) MU[c] += MN[i][c] * du[i];
+      }
+      for (int c = 0; c < 3; c++) {
+        dN[c] = 0.;
+        for (int d = 0; d < 3; d++) dN[c] += RI[3 * c + d] * (FN[d] + MU[d]);
+        dout->dN[c] = dN[c];
+      }
+      const double mu[3] = {th[T_MUB], th[T_MUS], th[T_MUQ]};
+      double RS[3], MS[3] = {0, 0, 0};
+      for (int c = 0; c < 3; c++) RS[c] = -mu[c] / T;
+      for (int i = 0; i < D; i++) MS[i] = Ms[i];
+      double rdn = 0.0;
+      for (int c = 0; c < 3; c++) rdn += RS[c] * dN[c];
+      o.dS = m1 + Fs + rdn;
+      double itq[9], itt[9], itk[9];
+      inverse3(dif->tq, itq);
+      for (int c = 0; c < 3; c++)
+        for (int d = 0; d < 3; d++) {
+          double a1 = 0.0, a2 = 0.0;
+          for (int kk = 0; kk < 3; kk++) {
+            a1 += itq[3 * c + kk] * dif->tq[3 * kk + d];
+            a2 += itq[3 * c + kk] * dif->kq[3 * kk + d];
+          }
+          itt[3 * c + d] = a1;
+          itk[3 * c + d] = a2;
+        }
+      const double X_ = g * divV + geo + g / t;
+      const double gs = g * sig;
+      const double cmd[4] = {1., -1., -1., -1. / t / t};
+      const double fuc[3] = {-u[0], -u[1], -t2 * u[2]};
+      double qc[3][4];
+      for (int c = 0; c < 3; c++) {
+        qc[c][0] = dif->q[4 * c];
+        qc[c][1] = -dif->q[4 * c + 1];
+        qc[c][2] = -dif->q[4 * c + 2];
+        qc[c][3] = -t2 * dif->q[4 * c + 3];
+      }
+      for (int i = 0; i < 3; i++) {
+        const double fui = u[i];
+        const double gai[3] = {i < D ? dif->ga[3 * i] : 0.0, i < D ? dif->ga[3 * i + 1] : 0.0,
+                               i < D ? dif->ga[3 * i + 2] : 0.0};
+        double FD[3], Fa[3], Aa[3], MD[3][3], Ma[3][3], Ra[3][3];
+        for (int c = 0; c < 3; c++) {
+          FD[c] = fui * g * dif->q[4 * c] * geo + 2. * fui * qc[c][3] * u[2] * g / t;
+          Fa[c] = -fui * g * sig * dif->da[c] * Fs + cmd[i + 1] * gai[c];
+          Aa[c] = fui * dif->da[c] * double(sden);
+          for (int j = 0; j < 3; j++) {
+            MD[c][j] = fui * g * (qc[c][j + 1] - qc[c][0] * fuc[j] / g);
+            Ma[c][j] = -fui * g * sig * dif->da[c] * MS[j];
+          }
+          for (int d = 0; d < 3; d++) {
+            Ra[c][d] = -fui * g * sig * (dif->da[c] * RS[d] + dif->da[3 + 3 * c + d]);
+            Aa[c] += fui * dif->da[3 + 3 * c + d] * rho[d];
+          }
+        }
+        for (int c = 0; c < 3; c++) {
+          double F = 0.0, Rq[3];
+          for (int d = 0; d < 3; d++) {
+            F += (-itt[3 * c + d] * FD[d] - itq[3 * c + d] * dif->q[4 * d + i + 1] + itk[3 * c + d] * Fa[d] +
+                  itk[3 * c + d] * Aa[d] * X_) / (gs);
+            double R_ = 0.0;
+            for (int kk = 0; kk < 3; kk++) R_ += itk[3 * c + kk] * Ra[kk][d] / (gs);
+            Rq[d] = R_;
+          }
+          double v = F;
+          for (int j = 0; j < D; j++) {
+            double M = 0.0;
+            for (int d = 0; d < 3; d++)
+              M += (-itt[3 * c + d] * MD[d][j] + itk[3 * c + d] * Ma[d][j] - itk[3 * c + d] * Aa[d] * fuc[j] / g) / (gs);
+            v += M * du[j];
+          }
+          for (int d = 0; d < 3; d++) v += Rq[d] * dN[d];
+          dout->dQ[3 * c + i] = v;
+        }
+      }
+    }
+  }
 #pragma unroll
   for (int sl = 0; sl < 5; sl++) {
     R acc = R(0.0);

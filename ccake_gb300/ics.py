@@ -63,6 +63,22 @@ class RunConfig:
     skin_frac: float = 0.0         # candidate-list skin / 2h (0: 0.1), GPU only
     particlization: int = 0        # freeze-out status machine after every step
     surface: int = 0               # with particlization: the freeze-out hypersurface rows
+    # diffusion sector (FP64 form, Milne coordinates)
+    using_diffusion: int = 0
+    diffusion_mode: int = 0        # 0 constant_over_T2, 2 kappaB_coth
+    diffusion_relax_mode: int = 0  # 0 tau_q = 0.2/T, 1 tau_q = C_B/T (kappaB_coth)
+    diffusion_regulator: int = 0   # regulate_diffusion (PhysRevC.98.034916 Eqs. C6-C8)
+    critical_scaling_diffusion: int = 0
+    kappa_over_T2: tuple = (0.0,) * 9   # row-major 3x3 over (B, S, Q)
+    C_B: float = 0.0
+    reg_chi0: float = 10.0
+    reg_e0: float = 0.1            # GeV/fm^3
+    reg_xi0: float = 0.01          # GeV/fm^3
+    reg_rq_max: float = 1.0
+    crit_T: float = 150.0          # MeV
+    crit_muB: float = 350.0        # MeV
+    crit_wT: float = 30.0          # MeV
+    crit_wmuB: float = 50.0        # MeV
 
 
 @dataclasses.dataclass

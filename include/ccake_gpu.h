@@ -63,6 +63,19 @@ typedef struct ccake_config {
   int32_t surface;            /* with particlization: interpolate the freeze-out
                                  hypersurface (FreezeOut::bsqsvinterpolate), rows
                                  of freeze_out.dat, ccake_freeze_out_rows */
+  /* diffusion sector (include/settings.h diffusionMode != "disabled";
+   * src/eom_default.cpp:1415-1817): FP64 form (precision 0), Milne
+   * coordinates (coord 0), Newton EoS (no pre-inverted tables) */
+  int32_t using_diffusion;
+  int32_t diffusion_mode;       /* 0 constant_over_T2 (kappa = kappa_over_T2 T^2), 2 kappaB_coth */
+  int32_t diffusion_relax_mode; /* 0 tau_q = 0.2/T; 1 tau_q = C_B/T (kappaB_coth) */
+  int32_t diffusion_regulator;  /* regulate_diffusion (src/sph_workstation.cpp:132-218) */
+  int32_t critical_scaling_diffusion;  /* Gaussian suppression of kappa near the critical point */
+  int32_t pad2;
+  double kappa_over_T2[9];      /* constant_kappa_over_T2, row-major over (B, S, Q) */
+  double C_B;
+  double reg_chi0, reg_e0, reg_xi0, reg_rq_max;   /* regulator; e0, xi0 in GeV/fm^3 */
+  double crit_T, crit_muB, crit_wT, crit_wmuB;    /* critical point and widths, MeV */
 } ccake_config;
 
 /* Host struct-of-arrays particle input, the columns of the reference's
@@ -131,6 +144,16 @@ ccake_status_t ccake_ctx_destroy(ccake_ctx* ctx);
  * SystemState::allocate_cabana_particles (src/sph_workstation.cpp:1228-1340,
  * src/system_state.cpp:57-326). */
 ccake_status_t ccake_load_particles(ccake_ctx* ctx, const ccake_particles_soa* host);
+
+/* Initial diffusion currents of the loaded particles (the reference's
+ * input_initial_diffusion columns, src/BSQHydro.cpp:345-375): q has 12 rows
+ * of n doubles in the caller's particle order, row 4c + mu = q^mu of charge
+ * c (B, S, Q). Only the spatial q^i are used: ccake_initialize sets the
+ * extensive current q^i / sigma (SPHWorkstation::set_diffusion,
+ * src/sph_workstation.cpp:1441-1458) and q^0 follows from orthogonality to u.
+ * Needs using_diffusion; call between ccake_load_particles and
+ * ccake_initialize (without it the currents start at zero). */
+ccake_status_t ccake_set_initial_diffusion(ccake_ctx* ctx, const double* q);
 
 /* e -> s inversion, initial sigma, extensive densities and initial smoothing.
  * Replaces BSQHydro::initialize_hydrodynamics (src/BSQHydro.cpp:568-646). */

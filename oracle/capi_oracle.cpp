@@ -31,6 +31,10 @@ void alloc(System& s, int n) {
   A(s.d_ext_bulk); A(s.dEz); A(s.theta); A(s.shv_nabla_u); A(s.ext_bulk0); A(s.Ez0);
   for (int i = 0; i < 5; i++) A(s.sigma_t[i]);
   A(s.kn_shear); A(s.kn_bulk); A(s.ire_shear); A(s.ire_bulk);
+  for (int i = 0; i < 9; i++) { A(s.ext_q[i]); A(s.ext_q0[i]); A(s.tau_q[i]); A(s.kappa_q[i]); A(s.grad_alpha[i]);
+    A(s.d_ext_q[i]); }
+  for (int i = 0; i < 12; i++) { A(s.q[i]); A(s.in_q[i]); A(s.dalpha[i]); }
+  for (int i = 0; i < 3; i++) { A(s.div_qa[i]); A(s.grad_qa[i]); A(s.kn_diff[i]); A(s.ire_diff[i]); }
   s.freeze.assign(n, 0); s.btrack.assign(n, 0); s.eos_id.assign(n, 0); s.eos_status.assign(n, 0);
   s.n = n;
 }
@@ -89,6 +93,29 @@ std::vector<double>* field(System& s, const std::string& k) {
   if (k == "bulk_knudsen") return &s.kn_bulk;
   if (k == "inverse_reynolds_shear") return &s.ire_shear;
   if (k == "inverse_reynolds_bulk") return &s.ire_bulk;
+  // diffusion sector: charge letters B, S, Q; q{c}{mu}, ext_q{c}{i},
+  // d_ext_q{c}{i}, in_q{c}{mu}, tau_q{c}{d}, kappa_q{c}{d}, grad_alpha{i}{c},
+  // dalpha{k} (0..11), div_qa{c}, grad_qa{c}, kn_diff{c}, ire_diff{c}
+  const char ch[3] = {'B', 'S', 'Q'};
+  for (int c = 0; c < 3; c++) {
+    const std::string C(1, ch[c]);
+    for (int m = 0; m < 4; m++) {
+      if (k == "q" + C + std::to_string(m)) return &s.q[4 * c + m];
+      if (k == "in_q" + C + std::to_string(m)) return &s.in_q[4 * c + m];
+    }
+    for (int i = 0; i < 3; i++) {
+      if (k == "ext_q" + C + std::to_string(i)) return &s.ext_q[3 * c + i];
+      if (k == "d_ext_q" + C + std::to_string(i)) return &s.d_ext_q[3 * c + i];
+      if (k == "grad_alpha" + std::to_string(i) + C) return &s.grad_alpha[3 * i + c];
+      if (k == "tau_q" + C + std::string(1, ch[i])) return &s.tau_q[3 * c + i];
+      if (k == "kappa_q" + C + std::string(1, ch[i])) return &s.kappa_q[3 * c + i];
+    }
+    if (k == "div_qa" + C) return &s.div_qa[c];
+    if (k == "grad_qa" + C) return &s.grad_qa[c];
+    if (k == "kn_diff" + C) return &s.kn_diff[c];
+    if (k == "ire_diff" + C) return &s.ire_diff[c];
+  }
+  for (int j = 0; j < 12; j++) if (k == "dalpha" + std::to_string(j)) return &s.dalpha[j];
   return nullptr;
 }
 }  // namespace
@@ -145,6 +172,7 @@ int orc_phase(void* p, const char* name) {
   else if (k == "smooth_fields") smooth_fields(h->s, h->nl);
   else if (k == "thermo") return update_thermodynamics(h->s);
   else if (k == "reset_pi") reset_pi_tensor(h->s);
+  else if (k == "regulate_diffusion") regulate_diffusion(h->s);
   else if (k == "viscosities") update_viscosities(h->s);
   else if (k == "gradients") smooth_gradients(h->s, h->nl);
   else if (k == "eom") evaluate_time_derivatives(h->s);
@@ -252,6 +280,11 @@ void orc_eos_invert_batch(const Config* c, void* tab, int entropy, long n, const
     if (iters) iters[i] = it;
     if (k >= 0 && th16) eos_set_thermo(*c, (Table*)tab, k, tbqs4 + 4 * i, th16 + 16 * i);
   }
+}
+
+void orc_eos_alpha_derivs(const Config* c, void* tab, int chain_index, long n, const double* tbqs, double* out12) {
+#pragma omp parallel for
+  for (long i = 0; i < n; i++) eos_alpha_derivs(*c, (const Table*)tab, chain_index, tbqs + 4 * i, out12 + 12 * i);
 }
 
 void orc_eos_set_thermo(const Config* c, void* tab, int chain_index, const double* tbqs, double* th16) {

@@ -496,6 +496,40 @@ double term4(const Chi& x, int j, int i) {
   }
   return base - aTmb(a, m, b);
 }
+// G = H^-1 of the (T, muB, muS, muQ) Hessian of p over the directions that
+// are not decoupled-and-frozen (an all-zero row), Gauss-Jordan with partial
+// pivoting; the conformal-diagonal model's cross terms are its exact zeros.
+void exact_hessian_inverse(const Chi& X, bool diag, double G[4][4]) {
+  double H[4][4] = {{X.t2, X.tb, X.ts, X.tq}, {X.tb, X.b2, X.bs, X.bq},
+                    {X.ts, X.bs, X.s2, X.sq}, {X.tq, X.bq, X.sq, X.q2}};
+  if (diag)
+    for (int i = 0; i < 4; i++) for (int j = 0; j < 4; j++) if (i != j) H[i][j] = 0.0;
+  int keep[4], m = 0;
+  for (int i = 0; i < 4; i++) {
+    bool zero = true;
+    for (int j = 0; j < 4; j++) zero = zero && (H[i][j] == 0.0);
+    if (!zero) keep[m++] = i;
+  }
+  double A[4][8] = {{0}};
+  for (int i = 0; i < m; i++) {
+    for (int j = 0; j < m; j++) A[i][j] = H[keep[i]][keep[j]];
+    A[i][m + i] = 1.0;
+  }
+  for (int col = 0; col < m; col++) {
+    int p = col;
+    for (int r = col + 1; r < m; r++) if (std::fabs(A[r][col]) > std::fabs(A[p][col])) p = r;
+    if (p != col) for (int j = 0; j < 2 * m; j++) std::swap(A[col][j], A[p][j]);
+    const double piv = A[col][col];
+    for (int j = 0; j < 2 * m; j++) A[col][j] /= piv;
+    for (int r = 0; r < m; r++) {
+      if (r == col || A[r][col] == 0.0) continue;
+      const double f = A[r][col];
+      for (int j = 0; j < 2 * m; j++) A[r][j] -= f * A[col][j];
+    }
+  }
+  for (int i = 0; i < 4; i++) for (int j = 0; j < 4; j++) G[i][j] = 0.0;
+  for (int i = 0; i < m; i++) for (int j = 0; j < m; j++) G[keep[i]][keep[j]] = A[i][m + j];
+}
 }  // namespace
 
 // include/eos.h:121-175 (set_thermo) restricted to the fields the hot path
@@ -516,36 +550,8 @@ void eos_set_thermo(const Config& c, const Table* tab, int k, const double x[4],
     // the conformal-diagonal model taken as the exact zeros its p(T, mu) has.
     // dw/ds|rho = T + s G_TT + sum_a rho_a G_aT, dw/drho_a = mu_a + s G_Ta +
     // sum_b rho_b G_ba, charge terms gated by |rho| > TINY as in the reference.
-    const bool diag = chain_model(c, k) == mConfDiag;
-    double H[4][4] = {{X.t2, X.tb, X.ts, X.tq}, {X.tb, X.b2, X.bs, X.bq},
-                      {X.ts, X.bs, X.s2, X.sq}, {X.tq, X.bq, X.sq, X.q2}};
-    if (diag)
-      for (int i = 0; i < 4; i++) for (int j = 0; j < 4; j++) if (i != j) H[i][j] = 0.0;
-    int keep[4], m = 0;
-    for (int i = 0; i < 4; i++) {
-      bool zero = true;
-      for (int j = 0; j < 4; j++) zero = zero && (H[i][j] == 0.0);
-      if (!zero) keep[m++] = i;
-    }
-    double A[4][8] = {{0}};
-    for (int i = 0; i < m; i++) {
-      for (int j = 0; j < m; j++) A[i][j] = H[keep[i]][keep[j]];
-      A[i][m + i] = 1.0;
-    }
-    for (int col = 0; col < m; col++) {  // Gauss-Jordan, partial pivoting
-      int p = col;
-      for (int r = col + 1; r < m; r++) if (std::fabs(A[r][col]) > std::fabs(A[p][col])) p = r;
-      if (p != col) for (int j = 0; j < 2 * m; j++) std::swap(A[col][j], A[p][j]);
-      const double piv = A[col][col];
-      for (int j = 0; j < 2 * m; j++) A[col][j] /= piv;
-      for (int r = 0; r < m; r++) {
-        if (r == col || A[r][col] == 0.0) continue;
-        const double f = A[r][col];
-        for (int j = 0; j < 2 * m; j++) A[r][j] -= f * A[col][j];
-      }
-    }
-    double G[4][4] = {{0}};
-    for (int i = 0; i < m; i++) for (int j = 0; j < m; j++) G[keep[i]][keep[j]] = A[i][m + j];
+    double G[4][4];
+    exact_hessian_inverse(X, chain_model(c, k) == mConfDiag, G);
     const double rho[4] = {0.0, B, S, Q};
     const bool act[4] = {true, hB, hS, hQ};
     const double mu[4] = {T, mB, mS, mQ};
@@ -585,6 +591,62 @@ void eos_set_thermo(const Config& c, const Table* tab, int k, const double x[4],
     if (hS) ct += S / term4(X, 2, 1);
   }
   th[kDwdQ] = mQ + ct;
+}
+
+// The twelve derivatives of alpha_a = mu_a / T at fixed (s, rho) that the
+// diffusion sector reads (src/eos.cpp:337-493, dalpha_Bds .. dalpha_QdQ).
+// out[a] = dalpha_a/ds, out[3 + 3a + b] = dalpha_a/drho_b, charges a, b in
+// the order B, S, Q. The reference chain (thermo_mode 0) uses
+// dalpha_a/ds = -mu_a/T^2 / (ds/dT) + [rho_a] 1/T / (ds/dmu_a) and
+// dalpha_a/drho_b = [rho_b] (-mu_a/T^2 / (drho_b/dT) + [rho_a] 1/T / (drho_b/dmu_a)),
+// [rho] meaning |rho| > TINY, with its operation order (dalpha_BdB adds the
+// 1/T term first). The exact form (thermo_mode 1) replaces 1/(dx/dy) by the
+// entries of H^-1 under the same gates.
+void eos_alpha_derivs(const Config& c, const Table* tab, int k, const double x[4], double out[12]) {
+  double o[17];
+  model_thermo(c, tab, chain_model(c, k), x, o);
+  const double T = x[0];
+  const double mu[3] = {x[1], x[3], x[2]};            // muB, muS, muQ
+  const double rho[3] = {o[2], o[3], o[4]};           // B, S, Q
+  const Chi X{o[16], o[13], o[14], o[15], o[7], o[8], o[9], o[10], o[11], o[12]};
+  bool h[3];
+  for (int a = 0; a < 3; a++) h[a] = std::fabs(rho[a]) > kTiny;
+  if (c.thermo_mode == 1) {
+    double G[4][4];
+    exact_hessian_inverse(X, chain_model(c, k) == mConfDiag, G);
+    // H index: 0 T, 1 B, 2 S, 3 Q
+    for (int a = 0; a < 3; a++) {
+      double ct = 0.0;
+      if (h[a]) ct += 1 / T * G[a + 1][0];
+      out[a] = -mu[a] / T / T * G[0][0] + ct;
+      for (int b = 0; b < 3; b++) {
+        double v = 0.0;
+        if (h[b]) {
+          v += -mu[a] / T / T * G[0][b + 1];
+          if (h[a]) v += 1 / T * G[a + 1][b + 1];
+        }
+        out[3 + 3 * a + b] = v;
+      }
+    }
+    return;
+  }
+  for (int a = 0; a < 3; a++) {
+    double ct = 0.0;
+    if (h[a]) ct += 1 / T / term2(X, a);
+    out[a] = -mu[a] / T / T / term1(X) + ct;
+    for (int b = 0; b < 3; b++) {
+      double v = 0.0;
+      if (h[b]) {
+        if (a == b && a == 0) {
+          v += 1 / T / term4(X, b, a) - mu[a] / T / T / term3(X, b);
+        } else {
+          v += -mu[a] / T / T / term3(X, b);
+          if (h[a]) v += 1 / T / term4(X, b, a);
+        }
+      }
+      out[3 + 3 * a + b] = v;
+    }
+  }
 }
 
 }  // namespace orc

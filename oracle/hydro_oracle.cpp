@@ -124,6 +124,168 @@ void inverse(int D, const double* A, double* Ai) {
 #undef M
 }
 
+// Diffusion coefficients, src/transport_coefficients.cpp:571-617 (kappa,
+// tauq), :918-973 (default_kappa = kappa/T^2 T^2, default_tauq = 0.2/T on
+// the diagonal), :981-1040 (kappaB_coth, tauqB_only) and :1048-1057 (the
+// Gaussian suppression near the critical point, table EoS only). tq, kq are
+// row-major 3x3 over (B, S, Q).
+void diffusion_coefs(const Config& c, const double* th, bool table_eos, double* tq, double* kq) {
+  const double T = th[kT];
+  for (int k = 0; k < 9; k++) tq[k] = kq[k] = 0.0;
+  if (c.diffusion_mode == 2) {
+    const double muB = th[kMuB], nB = th[kRhoB], w = th[kW];
+    const double x = (T > kTiny) ? muB / T : 0.0;
+    if (T > kTiny && std::fabs(w) > kTiny && std::fabs(x) > 1.0e-2) {
+      const double kB = (c.C_B / T) * nB * ((1.0 / 3.0) / std::tanh(x) - nB * T / w);
+      if (std::isfinite(kB) && kB > 0.0) kq[0] = kB;
+    }
+    if (c.diffusion_relax_mode == 1) {
+      if (T > kTiny)
+        for (int i = 0; i < 3; i++) tq[4 * i] = c.C_B / T;
+    } else {
+      for (int i = 0; i < 3; i++) tq[4 * i] += 0.2 / T;
+    }
+    return;
+  }
+  double sup = 1.0;
+  if (c.critical_scaling_diffusion && table_eos) {
+    const double dT = T - c.crit_T / kHbarcMeVfm, dm = th[kMuB] - c.crit_muB / kHbarcMeVfm;
+    const double sT = c.crit_wT / kHbarcMeVfm, sm = c.crit_wmuB / kHbarcMeVfm;
+    const double ex = 0.5 * (dT * dT / (sT * sT) + dm * dm / (sm * sm));
+    sup = 1.0 - std::exp(-ex);
+  }
+  for (int k = 0; k < 9; k++) kq[k] = sup * c.kappa_over_T2[k] * (T * T);
+  for (int i = 0; i < 3; i++) tq[4 * i] += 0.2 / T;
+}
+
+// Per-particle output of the diffusion MRF assembly.
+struct DiffMRF {
+  double F0q[3], R0q[9], M0q[9];   // F_0_q_b (b), R_0_q_bc (3b + c), M_0_q_bj (3b + j)
+  double Fq[9], Rq[27], Mq[27];    // F_q_ib (3i + b), R_q_ibc (9i + 3b + c), M_q_ibj (9i + 3b + j)
+};
+
+// src/eom_default.cpp:1415-1817 (calculate_MRF_diffusion) for one particle
+// (D = 2, 3; Milne coordinates). Ms, Fs: M and F of the extensive entropy.
+// The stray semicolon of :1744 ends F_D_ib after its second term; the two
+// lines after it have no effect and are not restated.
+void diffusion_mrf(const System& s, int a, double t, const double* Ms, double Fs, DiffMRF& o) {
+  const int D = s.cfg.dim;
+  const double t2 = t * t;
+  const double sig = s.sigma[a], g = s.gamma[a], sden = s.th[kS][a], T = s.th[kT][a];
+  const double rho[3] = {s.th[kRhoB][a], s.th[kRhoS][a], s.th[kRhoQ][a]};
+  const double mu[3] = {s.th[kMuB][a], s.th[kMuS][a], s.th[kMuQ][a]};
+  double das[3], dar[3][3], RS[3], MS[3] = {0, 0, 0}, ga[3][3] = {{0}}, q[3][4], qc[3][4];
+  for (int c = 0; c < 3; c++) {
+    das[c] = s.dalpha[c][a];
+    for (int d = 0; d < 3; d++) dar[c][d] = s.dalpha[3 + 3 * c + d][a];
+    RS[c] = -mu[c] / T;
+    for (int m = 0; m < 4; m++) q[c][m] = s.q[4 * c + m][a];
+    qc[c][0] = q[c][0];
+    qc[c][1] = -q[c][1];
+    qc[c][2] = -q[c][2];
+    qc[c][3] = -t2 * q[c][3];
+  }
+  double u[3] = {0, 0, 0}, uc[3], fu[3] = {0, 0, 0}, divV = 0;
+  for (int i = 0; i < D; i++) {
+    u[i] = s.u[i][a];
+    fu[i] = u[i];
+    MS[i] = Ms[i];
+    divV += s.gradV[i * D + i][a];
+    for (int c = 0; c < 3; c++) ga[i][c] = s.grad_alpha[3 * i + c][a];
+  }
+  for (int i = 0; i < 3; i++) uc[i] = u[i];
+  cov_D(D, uc, t2);
+  const double fuc[3] = {-fu[0], -fu[1], -t2 * fu[2]};
+  const double geo = dEta(D, D - 1) * u[D - 1] * u[D - 1] * t / g;
+  const double cmd[4] = {1., -1., -1., -1. / t / t};
+  double tq[9], kq[9], itq[9], itt[9], itk[9];
+  for (int k = 0; k < 9; k++) { tq[k] = s.tau_q[k][a]; kq[k] = s.kappa_q[k][a]; }
+  inverse(3, tq, itq);
+  for (int c = 0; c < 3; c++)
+    for (int d = 0; d < 3; d++) {
+      itt[3 * c + d] = 0.0;
+      itk[3 * c + d] = 0.0;
+      for (int k = 0; k < 3; k++) {
+        itt[3 * c + d] += itq[3 * c + k] * tq[3 * k + d];
+        itk[3 * c + d] += itq[3 * c + k] * kq[3 * k + d];
+      }
+    }
+  const double X = g * divV + geo + g / t;
+  const double omg = 1. - g * g;
+  // the 0 (time) components
+  double F0D[3], F0a[3], A0a[3], R0a[3][3], M0a[3][3] = {{0}}, M0D[3][3] = {{0}};
+  for (int c = 0; c < 3; c++) {
+    F0D[c] = g * g * geo * q[c][0] + 2. * g * g * qc[c][3] * fu[2] / t + t * g * qc[c][0] * fu[2] * fu[2] +
+             t * fu[2] * q[c][3];
+    F0a[c] = omg * sig * das[c] * Fs;
+    A0a[c] = -omg * das[c] * sden / g;
+    for (int i = 0; i < D; i++) {
+      M0D[c][i] = g * g * (qc[c][i + 1] - qc[c][0] * uc[i] / g);
+      M0a[c][i] = omg * sig * das[c] * MS[i];
+      F0a[c] += -ga[i][c] * u[i] / g;
+    }
+    for (int d = 0; d < 3; d++) {
+      R0a[c][d] = omg * sig * (das[c] * RS[d] + dar[c][d]);
+      A0a[c] += -omg * dar[c][d] * rho[d] / g;
+    }
+  }
+  for (int c = 0; c < 3; c++) {
+    o.F0q[c] = 0.0;
+    for (int i = 0; i < 3; i++) o.M0q[3 * c + i] = 0.0;
+    for (int i = 0; i < D; i++) {
+      double acc = 0;
+      for (int d = 0; d < 3; d++)
+        acc += (-itt[3 * c + d] * M0D[d][i] + itk[3 * c + d] * M0a[d][i] - itk[3 * c + d] * A0a[d] * uc[i] / g) / (g) +
+               itt[3 * c + d] * q[d][0] * uc[i] / g / g;
+      o.M0q[3 * c + i] = acc;
+    }
+    for (int d = 0; d < 3; d++)
+      o.F0q[c] += (-itt[3 * c + d] * F0D[d] - itq[3 * c + d] * q[d][0] + itk[3 * c + d] * F0a[d] +
+                   itk[3 * c + d] * A0a[d] * X) / (g) -
+                  itt[3 * c + d] * q[d][0] * X / g;
+    for (int d = 0; d < 3; d++) {
+      double acc = 0.0;
+      for (int k = 0; k < 3; k++) acc += itk[3 * c + k] * R0a[k][d] / (g);
+      o.R0q[3 * c + d] = acc;
+    }
+  }
+  // the spatial components, all three directions
+  double FD[3][3], Fa[3][3], Aa[3][3], MD[3][3][3], Ma[3][3][3], Ra[3][3][3];
+  for (int i = 0; i < 3; i++)
+    for (int c = 0; c < 3; c++) {
+      FD[i][c] = fu[i] * g * q[c][0] * geo + 2. * fu[i] * qc[c][3] * fu[2] * g / t;
+      Fa[i][c] = -fu[i] * g * sig * das[c] * Fs + cmd[i + 1] * ga[i][c];
+      Aa[i][c] = fu[i] * das[c] * sden;
+      for (int j = 0; j < 3; j++) {
+        MD[i][c][j] = fu[i] * g * (qc[c][j + 1] - qc[c][0] * fuc[j] / g);
+        Ma[i][c][j] = -fu[i] * g * sig * das[c] * MS[j];
+      }
+      for (int d = 0; d < 3; d++) {
+        Ra[i][c][d] = -fu[i] * g * sig * (das[c] * RS[d] + dar[c][d]);
+        Aa[i][c] += fu[i] * dar[c][d] * rho[d];
+      }
+    }
+  for (int i = 0; i < 3; i++)
+    for (int c = 0; c < 3; c++) {
+      double F = 0.0;
+      for (int d = 0; d < 3; d++) {
+        F += (-itt[3 * c + d] * FD[i][d] - itq[3 * c + d] * q[d][i + 1] + itk[3 * c + d] * Fa[i][d] +
+              itk[3 * c + d] * Aa[i][d] * X) / (g * sig);
+        double R = 0.0;
+        for (int k = 0; k < 3; k++) R += itk[3 * c + k] * Ra[i][k][d] / (g * sig);
+        o.Rq[9 * i + 3 * c + d] = R;
+      }
+      o.Fq[3 * i + c] = F;
+      for (int j = 0; j < 3; j++) {
+        double M = 0.0;
+        for (int d = 0; d < 3; d++)
+          M += (-itt[3 * c + d] * MD[i][d][j] + itk[3 * c + d] * Ma[i][d][j] - itk[3 * c + d] * Aa[i][d] * fuc[j] / g) /
+               (g * sig);
+        o.Mq[9 * i + 3 * c + j] = M;
+      }
+    }
+}
+
 // Per-particle output of the shear MRF assembly.
 struct ShearMRF {
   double M0i[9], F0i[3], Mnab[3], Fnab;
@@ -412,6 +574,27 @@ void hydro_numbers(System& s, int a, const double* sig5) {
   s.ire_bulk[a] = std::fabs(s.bulk[a]) / p;
 }
 
+// src/eom_default.cpp:1944-1982: per charge, Kn = tau_q^{aa} |grad alpha_a|
+// and the inverse Reynolds number |q_a| / |n_a| (zero for |n_a| <= 1e-15).
+void diffusion_numbers(System& s, int a) {
+  const int D = s.cfg.dim;
+  const double t2 = s.t * s.t;
+  const double rho[3] = {s.th[kRhoB][a], s.th[kRhoS][a], s.th[kRhoQ][a]};
+  for (int c = 0; c < 3; c++) {
+    double gsq = 0.0;
+    for (int i = 0; i < D; i++) {
+      const double gg = s.grad_alpha[3 * i + c][a];
+      gsq += gg * gg;
+    }
+    s.kn_diff[c][a] = s.tau_q[4 * c][a] * std::sqrt(gsq);
+    const double q0 = s.q[4 * c][a], q1 = s.q[4 * c + 1][a], q2 = s.q[4 * c + 2][a], q3 = s.q[4 * c + 3][a];
+    const double q_sq = q1 * q1 + q2 * q2 + t2 * q3 * q3 - q0 * q0;
+    const double q_mag = q_sq > 0.0 ? std::sqrt(q_sq) : 0.0;
+    const double n_abs = std::fabs(rho[c]);
+    s.ire_diff[c][a] = (n_abs > 1e-15) ? q_mag / n_abs : 0.0;
+  }
+}
+
 }  // namespace
 
 // src/eom_default.cpp:17-38 (update_velocity)
@@ -427,7 +610,7 @@ void update_velocity(System& s) {
   }
 }
 
-// src/eom_default.cpp:56-172 (reset_pi_tensor), diffusion part omitted.
+// src/eom_default.cpp:56-172 (reset_pi_tensor).
 void reset_pi_tensor(System& s) {
   const int D = s.cfg.dim;
   const double tm = s.cfg.coord == 1 ? 1.0 : s.t, t2 = tm * tm;
@@ -454,6 +637,54 @@ void reset_pi_tensor(System& s) {
     }
     for (int i = 1; i < 4; i++) p[i][0] = p[0][i];
     for (int i = 0; i < 4; i++) for (int j = 0; j < 4; j++) s.shv[i * 4 + j][a] = p[i][j];
+    // diffusion (:140-165): q^i = ext_q sigma, q^0 = -q^i u_i / gamma
+    for (int c = 0; c < 3; c++) {
+      double q0 = 0.;
+      for (int i = 0; i < 3; i++) {
+        const double qi = s.ext_q[3 * c + i][a] * sig;
+        s.q[4 * c + i + 1][a] = qi;
+      }
+      for (int i = 0; i < 3; i++) q0 += -s.q[4 * c + i + 1][a] * fc[i] / g;
+      s.q[4 * c][a] = q0;
+    }
+  }
+}
+
+// src/sph_workstation.cpp:132-218 (regulate_diffusion, PhysRevC.98.034916
+// Eqs. C6-C8): |q_a| is capped at rq_max |n_a| f(e), f(e) = chi0 (Fermi(e) -
+// Fermi(0)), Fermi(e) = 1 / (exp(-(e - e0) / xi0) + 1); the capped q^mu
+// rescales all four components and the extensive current follows.
+void regulate_diffusion(System& s) {
+  if (!s.cfg.using_diffusion || !s.cfg.diffusion_regulator) return;
+  const double chi0 = s.cfg.reg_chi0, e0 = s.cfg.reg_e0 / kHbarcGeVfm, xi0 = s.cfg.reg_xi0 / kHbarcGeVfm;
+  const double rq_max = s.cfg.reg_rq_max;
+  const double fermi_offset = 1.0 / (std::exp(e0 / xi0) + 1.0);
+  const bool milne = s.cfg.coord == 0;
+  const double t2 = s.t * s.t;
+#pragma omp parallel for
+  for (int a = 0; a < s.n; a++) {
+    const double e = s.th[kE][a];
+    const double ferm = 1.0 / (std::exp(-(e - e0) / xi0) + 1.0);
+    const double f_str = chi0 * (ferm - fermi_offset);
+    const double sigma = s.sigma[a];
+    const double rho[3] = {s.th[kRhoB][a], s.th[kRhoS][a], s.th[kRhoQ][a]};
+    for (int c = 0; c < 3; c++) {
+      const double n_abs = std::fabs(rho[c]);
+      if (n_abs < 1.0e-15) continue;
+      const double q0 = s.q[4 * c][a], q1 = s.q[4 * c + 1][a], q2 = s.q[4 * c + 2][a], q3 = s.q[4 * c + 3][a];
+      const double q3_sq = milne ? t2 * q3 * q3 : q3 * q3;
+      const double q_sq = q1 * q1 + q2 * q2 + q3_sq - q0 * q0;
+      if (q_sq <= 0.0) continue;
+      const double q_mag = std::sqrt(q_sq);
+      const double threshold = rq_max * n_abs * f_str;
+      if (q_mag <= threshold) continue;
+      const double scale = threshold / q_mag;
+      s.q[4 * c][a] = q0 * scale;
+      s.q[4 * c + 1][a] = q1 * scale;
+      s.q[4 * c + 2][a] = q2 * scale;
+      s.q[4 * c + 3][a] = q3 * scale;
+      for (int i = 0; i < 3; i++) s.ext_q[3 * c + i][a] = s.q[4 * c + i + 1][a] / sigma;
+    }
   }
 }
 
@@ -468,6 +699,11 @@ void update_viscosities(System& s) {
     s.delta_PiPi[a] = k.delta_PiPi; s.delta_pipi[a] = k.delta_pipi; s.lambda_piPi[a] = k.lambda_piPi;
     s.lambda_Pipi[a] = k.lambda_Pipi; s.phi1[a] = k.phi1; s.phi3[a] = k.phi3; s.phi6[a] = k.phi6;
     s.phi7[a] = k.phi7; s.tau_pipi[a] = k.tau_pipi;
+    if (s.cfg.using_diffusion) {
+      double tq[9], kq[9];
+      diffusion_coefs(s.cfg, th, s.cfg.eos_kind == kTable && s.eos_id[a] == 0, tq, kq);
+      for (int j = 0; j < 9; j++) { s.tau_q[j][a] = tq[j]; s.kappa_q[j][a] = kq[j]; }
+    }
   }
 }
 
@@ -487,6 +723,11 @@ int update_thermodynamics(System& s) {
     for (int j = 0; j < 16; j++) s.th[j][a] = th[j];
     s.eos_id[a] = k;
     s.eos_status[a] = it;
+    if (s.cfg.using_diffusion) {
+      double da[12];
+      eos_alpha_derivs(s.cfg, s.table, k, x, da);
+      for (int j = 0; j < 12; j++) s.dalpha[j][a] = da[j];
+    }
   }
   return failures;
 }
@@ -535,9 +776,10 @@ void evaluate_time_derivatives(System& s) {
       Mb[i] = (ztil * uc[i] / g) / (sig * g * tPi);
       Ms[i] = (Pi * uc[i] / g) / (sig * g * T);
     }
-    // R_extensive_entropy = -mu/T multiplies dN/dt, which is zero without the
-    // diffusion sector and sources
-    (void)mu;
+    // R_extensive_entropy = -mu/T multiplies dN/dt (zero without the
+    // diffusion sector and sources)
+    double RS[3];
+    for (int c = 0; c < 3; c++) RS[c] = -mu[c] / T;
     double Fb = -(ztil * (g * divV + gt + geo) + Pi - phi1 * Pi * Pi) / (sig * g * tPi);
     double Fs = (-Pi * (g * divV + gt + geo)) / (sig * g * T);
     double Fnab = 0, Mnab[3] = {0, 0, 0};
@@ -577,21 +819,86 @@ void evaluate_time_derivatives(System& s) {
         for (int j = 0; j < D; j++) Mu[i * D + j] += sm.M0i[i * D + j];
       }
     }
+    // diffusion sector: the charge MRFs (compute_charge_derivative,
+    // :368-451) and their coupling into du/dt (:579-617)
+    const bool diff = s.cfg.using_diffusion;
+    DiffMRF dm{};
+    double RI[9], MN[3][3] = {{0}}, FN[3] = {0, 0, 0};
+    if (diff) {
+      diffusion_mrf(s, a, t, Ms, Fs, dm);
+      double RN[9];
+      for (int c = 0; c < 9; c++) RN[c] = 0.0;
+      for (int c = 0; c < 3; c++) {
+        RN[4 * c] += g * sig;
+        FN[c] = 0.0;   // external charge sources
+      }
+      for (int i = 0; i < D; i++)
+        for (int c = 0; c < 3; c++) MN[i][c] += -dm.M0q[3 * c + i];
+      for (int c = 0; c < 3; c++) {
+        for (int d = 0; d < 3; d++) RN[3 * c + d] += -dm.R0q[3 * c + d];
+        FN[c] += -dm.F0q[c] + s.grad_qa[c][a] - s.div_qa[c][a] - s.q[4 * c][a] / t;
+      }
+      inverse(3, RN, RI);
+      // R_u = -u gamma (R_w + R_bulk sigma), R_w = sigma dw/drho + sigma dw/ds R_S;
+      // R_bulk and the shear R_0i are zero
+      double Ru[3][3];
+      for (int i = 0; i < D; i++)
+        for (int c = 0; c < 3; c++) {
+          const double Rw = sig * dwdr[c] + sig * dwds * RS[c];
+          Ru[i][c] = -u[i] * g * (Rw + 0.0 * sig);
+        }
+      double MR[9], FR[3];
+      for (int i = 0; i < D; i++) {
+        FR[i] = 0.0;
+        for (int j = 0; j < D; j++) {
+          MR[i * D + j] = 0.0;
+          for (int c = 0; c < 3; c++)
+            for (int d = 0; d < 3; d++) MR[i * D + j] += Ru[i][c] * RI[3 * c + d] * MN[j][d];
+        }
+        for (int c = 0; c < 3; c++)
+          for (int d = 0; d < 3; d++) FR[i] += Ru[i][c] * RI[3 * c + d] * FN[d];
+      }
+      for (int i = 0; i < D; i++) {
+        for (int j = 0; j < D; j++) Mu[i * D + j] = Mu[i * D + j] - MR[i * D + j];
+        Fu[i] = Fu[i] + FR[i];
+      }
+    }
     double MI[9], du[3];
     inverse(D, Mu, MI);
     for (int i = 0; i < D; i++) {
       du[i] = 0;
       for (int j = 0; j < D; j++) du[i] += MI[i * D + j] * Fu[j];
     }
+    double dN[3] = {0, 0, 0};
+    if (diff) {
+      double MU[3];
+      for (int c = 0; c < 3; c++) {
+        MU[c] = 0.;
+        for (int i = 0; i < D; i++) MU[c] += MN[i][c] * du[i];
+      }
+      for (int c = 0; c < 3; c++) {
+        dN[c] = 0.;
+        for (int d = 0; d < 3; d++) dN[c] += RI[3 * c + d] * (FN[d] + MU[d]);
+      }
+      for (int i = 0; i < 3; i++)
+        for (int c = 0; c < 3; c++) {
+          double v = dm.Fq[3 * i + c];
+          for (int j = 0; j < D; j++) v += dm.Mq[9 * i + 3 * c + j] * du[j];
+          for (int d = 0; d < 3; d++) v += dm.Rq[9 * i + 3 * c + d] * dN[d];
+          s.d_ext_q[3 * c + i][a] = v;
+        }
+    }
     // compute_derivatives (:622-826)
     // contractions with du/dt first, then the F terms, as in the reference
     double m1 = 0, m2 = 0, m3 = 0, c1 = 0;
     for (int i = 0; i < D; i++) { m1 += Ms[i] * du[i]; m2 += Mb[i] * du[i]; m3 += Mnab[i] * du[i]; c1 += uc[i] * du[i]; }
-    const double dS = m1 + Fs, dB = m2 + Fb, snu = m3 + Fnab;
+    double rdn = 0.0;
+    for (int c = 0; c < 3; c++) rdn += RS[c] * dN[c];
+    const double dS = diff ? m1 + Fs + rdn : m1 + Fs, dB = m2 + Fb, snu = m3 + Fnab;
     const double th = -1. * c1 / g + g * divV + gt + geo;
     for (int i = 0; i < D; i++) s.du_dt[i][a] = du[i];
     s.d_ext[0][a] = dS;
-    s.d_ext[1][a] = s.d_ext[2][a] = s.d_ext[3][a] = 0.0;
+    for (int c = 0; c < 3; c++) s.d_ext[1 + c][a] = dN[c];
     s.d_ext_bulk[a] = dB;
     s.theta[a] = th;
     s.shv_nabla_u[a] = snu;
@@ -610,7 +917,14 @@ void evaluate_time_derivatives(System& s) {
       hydro_numbers(s, a, sig5);
     } else {
       for (int k = 0; k < 6; k++) s.d_ext_shv[k][a] = 0.0;
+      if (diff) {
+        // the numbers are computed with shear or diffusion (:865-867); without
+        // shear the stored sigma tensor stays zero
+        const double zero5[5] = {0, 0, 0, 0, 0};
+        hydro_numbers(s, a, zero5);
+      }
     }
+    if (diff) diffusion_numbers(s, a);
     // compute_Ez_derivative (:827-862)
     const double u3 = (D == 3) ? u[2] : 0.0;
     const double e = s.th[kE][a], p = s.th[kP][a];
@@ -625,6 +939,7 @@ void get_time_derivatives(System& s, NbrList& nl) {
   smooth_fields(s, nl);           // 03_smooth_fields
   update_thermodynamics(s);       // 04_thermodynamics
   reset_pi_tensor(s);             // 05_reset_pi_tensor
+  regulate_diffusion(s);          // 06_regulate_diffusion
   update_viscosities(s);          // 08_viscosities
   smooth_gradients(s, nl);        // 09_smooth_gradients
   evaluate_time_derivatives(s);   // 10_time_derivatives
@@ -645,6 +960,8 @@ static void step_rk(System& s, NbrList& nl, double dt, double t0) {
       s.u[i][a] = s.u0[i][a] + dt * s.du_dt[i][a];
     }
     for (int k = 0; k < 5; k++) s.ext_shv[k][a] = s.ext_shv0[k][a] + dt * s.d_ext_shv[k][a];
+    if (s.cfg.using_diffusion)
+      for (int k = 0; k < 9; k++) s.ext_q[k][a] = s.ext_q0[k][a] + dt * s.d_ext_q[k][a];
     if (es < 0.0 && s.freeze[a] > 3) es = 1.e-3;
     else if (es < 0.0) s.eos_status[a] = -2;  // negative entropy: fatal in the reference
     s.ext[0][a] = es;
@@ -659,6 +976,7 @@ void rk2_step(System& s, NbrList& nl) {
     for (int k = 0; k < 4; k++) s.ext0[k][a] = s.ext[k][a];
     s.ext_bulk0[a] = s.ext_bulk[a];
     for (int k = 0; k < 6; k++) s.ext_shv0[k][a] = s.ext_shv[k][a];
+    for (int k = 0; k < 9; k++) s.ext_q0[k][a] = s.ext_q[k][a];
     s.Ez0[a] = s.Ez[a];
   }
   const double t0 = s.t, dt = s.cfg.dt;
@@ -885,17 +1203,28 @@ void freeze_out_status(System& s) {
   s.nstep++;
 }
 
-// src/system_state.cpp:738-885 (entropy, BSQ, energy totals) without the
-// diffusion q^0 terms (zero here).
+// src/system_state.cpp:738-885 (entropy, BSQ, energy totals), with the
+// diffusion q^0 terms when the diffusion sector is on.
 Totals conservation(const System& s) {
   Totals T{0, 0, 0, 0, 0, 0};
   const double sqrtg = s.cfg.coord == 0 ? s.t : 1.0;
   for (int a = 0; a < s.n; a++) {
-    T.S += s.ext[0][a] * s.mass[0][a];
-    T.B += s.ext[1][a] * s.mass[1][a];
-    T.Sq += s.ext[2][a] * s.mass[2][a];
-    T.Q += s.ext[3][a] * s.mass[3][a];
     const double g = s.gamma[a];
+    T.S += s.ext[0][a] * s.mass[0][a];
+    if (s.cfg.using_diffusion) {
+      // the q^0 terms of :755-828, each with the reference's mass factors
+      const double sg = s.sigma[a];
+      const double eqb = s.q[0][a] * s.mass[1][a] / sg / g;
+      const double eqs = s.q[4][a] * s.mass[0][a] / sg / g;
+      const double eqq = s.q[8][a] * s.mass[0][a] / sg / g;
+      T.B += s.ext[1][a] * s.mass[1][a] + eqb * s.mass[1][a] / g;
+      T.Sq += s.ext[2][a] * s.mass[2][a] + (eqs);
+      T.Q += s.ext[3][a] * s.mass[3][a] + (eqq);
+    } else {
+      T.B += s.ext[1][a] * s.mass[1][a];
+      T.Sq += s.ext[2][a] * s.mass[2][a];
+      T.Q += s.ext[3][a] * s.mass[3][a];
+    }
     const double C = s.th[kW][a] + s.bulk[a];
     T.E += (C * g * g - s.th[kP][a] - s.bulk[a] + s.shv[0][a]) * s.mass[0][a] * sqrtg / s.sigma_lab[a];
     T.Ez += s.Ez[a];
@@ -978,6 +1307,10 @@ void initialize(System& s, NbrList& nl) {
     for (int k = 0; k < 16; k++) s.shv[k][a] = 0.0;
     s.ext_bulk[a] = 0.0;
     s.bulk[a] = 0.0;
+    // set_diffusion (src/sph_workstation.cpp:1441-1458): ext q = q^i / sigma
+    for (int c = 0; c < 3; c++)
+      for (int i = 0; i < 3; i++)
+        s.ext_q[3 * c + i][a] = s.cfg.using_diffusion ? s.in_q[4 * c + i + 1][a] / s.sigma[a] : 0.0;
   }
   reset_pi_tensor(s);
   update_thermodynamics(s);

@@ -52,6 +52,17 @@ struct Config {
   double freeze_out_T;                    // fm^-1
   int32_t particlization;                 // freeze-out status machine after every step
   int32_t surface;                        // with particlization: the freeze-out hypersurface
+  // diffusion sector (include/settings.h; src/transport_coefficients.cpp:82-115)
+  int32_t using_diffusion;                // diffusionMode != "disabled"
+  int32_t diffusion_mode;                 // 0 constant_over_T2, 2 kappaB_coth
+  int32_t diffusion_relax_mode;           // 0 tau_q = 0.2/T, 1 tau_q = C_B/T (kappaB_coth)
+  int32_t diffusion_regulator;            // regulate_diffusion enabled
+  int32_t critical_scaling_diffusion;     // Gaussian suppression of kappa near (T_c, muB_c)
+  int32_t pad2;
+  double kappa_over_T2[9];                // constant_kappa_over_T2 (row-major B, S, Q)
+  double C_B;
+  double reg_chi0, reg_e0, reg_xi0, reg_rq_max;   // regulator; e0, xi0 in GeV/fm^3
+  double crit_T, crit_muB, crit_wT, crit_wmuB;    // critical point and widths, MeV
 };
 
 // Freeze-out snapshot of one step (FreezeOut::freeze_array,
@@ -109,8 +120,15 @@ struct System {
   // src/eom_default.cpp:1831-1985 (with shear): sigma^{11,12,13,22,23},
   // shear / bulk Knudsen and inverse Reynolds numbers
   std::vector<double> sigma_t[5], kn_shear, kn_bulk, ire_shear, ire_bulk;
+  // diffusion sector: extensive q (charge c = B, S, Q; direction i) at 3c + i,
+  // q^mu of the last reset_pi_tensor at 4c + mu, the initial q^mu, the twelve
+  // alpha derivatives (eos_alpha_derivs order), tau_q and kappa_q (3c + d),
+  // grad alpha (direction i, charge c at 3i + c), div q_a, v.grad q^0_a,
+  // d(ext q)/dt, and the diffusion Knudsen / inverse Reynolds numbers
+  std::vector<double> ext_q[9], q[12], in_q[12], dalpha[12], tau_q[9], kappa_q[9];
+  std::vector<double> grad_alpha[9], div_qa[3], grad_qa[3], d_ext_q[9], kn_diff[3], ire_diff[3];
   // evolver cache
-  std::vector<double> r0[3], u0[3], ext0[4], ext_bulk0, ext_shv0[6], Ez0;
+  std::vector<double> r0[3], u0[3], ext0[4], ext_bulk0, ext_shv0[6], Ez0, ext_q0[9];
   // table EoS (optional)
   struct Table* table = nullptr;
 };
@@ -137,6 +155,7 @@ void smooth_fields(System& s, const NbrList& nl);
 void calculate_initial_sigma(System& s, const NbrList& nl, double t);
 int update_thermodynamics(System& s);
 void reset_pi_tensor(System& s);
+void regulate_diffusion(System& s);
 void update_viscosities(System& s);
 void smooth_gradients(System& s, const NbrList& nl);
 void evaluate_time_derivatives(System& s);
@@ -159,6 +178,9 @@ int eos_invert(const Config& c, const Table* tab, int mode_entropy, const double
                int start_model, double tbqs_inout[4], int* iterations);
 // Derived thermodynamics after a solution (include/eos.h:121-175 set_thermo subset).
 void eos_set_thermo(const Config& c, const Table* tab, int model, const double tbqs[4], double th16[16]);
+// dalpha_a/ds (out[a]) and dalpha_a/drho_b (out[3 + 3a + b]), a, b = B, S, Q
+// (src/eos.cpp:337-493).
+void eos_alpha_derivs(const Config& c, const Table* tab, int model, const double tbqs[4], double out12[12]);
 int eos_chain_length(const Config& c);
 
 }  // namespace orc

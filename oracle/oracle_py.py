@@ -23,14 +23,21 @@ class Config(ctypes.Structure):
         "hT", "hEta", "t0", "dt", "eos_c", "eos_T0", "eos_muB0", "eos_muQ0", "eos_muS0",
         "eta_over_s", "zeta_over_s", "zeta_cs2_A", "zeta_cs2_p", "zeta_peak_T",
         "zeta_peak_width", "xmin", "ymin", "etamin", "freeze_out_T")] + [
-        ("particlization", ctypes.c_int32), ("surface", ctypes.c_int32)]
+        ("particlization", ctypes.c_int32), ("surface", ctypes.c_int32)] + [
+        (n, ctypes.c_int32) for n in ("using_diffusion", "diffusion_mode", "diffusion_relax_mode",
+                                      "diffusion_regulator", "critical_scaling_diffusion", "pad2")] + [
+        ("kappa_over_T2", ctypes.c_double * 9)] + [(n, ctypes.c_double) for n in (
+        "C_B", "reg_chi0", "reg_e0", "reg_xi0", "reg_rq_max", "crit_T", "crit_muB", "crit_wT", "crit_wmuB")]
 
 
 def make_config(rc) -> Config:
     c = Config()
-    for name, _ in Config._fields_:
+    for name, typ in Config._fields_:
         if hasattr(rc, name):
-            setattr(c, name, getattr(rc, name))
+            v = getattr(rc, name)
+            if name == "kappa_over_T2":
+                v = (ctypes.c_double * 9)(*[float(x) for x in v])
+            setattr(c, name, v)
     return c
 
 
@@ -80,6 +87,7 @@ def lib():
         L.orc_eos_full_thermo.argtypes = [ctypes.POINTER(Config), P, I, dp, dp]
         L.orc_eos_invert_batch.argtypes = [ctypes.POINTER(Config), P, I, ctypes.c_long, dp, dp, dp, ip, ip]
         L.orc_eos_set_thermo.argtypes = [ctypes.POINTER(Config), P, I, dp, dp]
+        L.orc_eos_alpha_derivs.argtypes = [ctypes.POINTER(Config), P, I, ctypes.c_long, dp, dp]
         _lib = L
     return _lib
 
@@ -212,3 +220,14 @@ def eos_invert_batch(rc, entropy, targets, seeds=None, table=None):
 
 THERMO_NAMES = ("T", "muB", "muS", "muQ", "p", "s", "rhoB", "rhoS", "rhoQ", "e", "w", "cs2",
                 "dwds", "dwdB", "dwdS", "dwdQ")
+
+
+def eos_alpha_derivs(rc, chain_index, tbqs, table=None):
+    """dalpha_a/ds (columns 0..2) and dalpha_a/drho_b (3 + 3a + b), a, b = B, S, Q,
+    at the (T, muB, muQ, muS) rows of tbqs."""
+    x = np.ascontiguousarray(tbqs, dtype=np.float64).reshape(-1, 4)
+    out = np.zeros((x.shape[0], 12))
+    cfg = make_config(rc)
+    lib().orc_eos_alpha_derivs(ctypes.byref(cfg), table.h if table is not None else None, int(chain_index),
+                               x.shape[0], _dp(x), _dp(out))
+    return out

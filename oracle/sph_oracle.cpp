@@ -191,16 +191,25 @@ void calculate_initial_sigma(System& s, const NbrList& nl, double t) {
 }
 
 // src/sph_workstation.cpp:796-986 (smooth_all_particle_gradients, generic /
-// Milne form, D > 1, without the diffusion sector).
+// Milne form, D > 1, with the diffusion sums of :909-967).
 void smooth_gradients(System& s, const NbrList& nl) {
   const int D = s.cfg.dim;
   const bool shear = s.cfg.using_shear;
+  const bool diff = s.cfg.using_diffusion;
   const double hT = s.cfg.hT, hEta = s.cfg.hEta;
   const bool fact = (D == 3) && s.cfg.factorized_kernel;
 #pragma omp parallel for schedule(static)
   for (int a = 0; a < s.n; a++) {
     double gP[3] = {0, 0, 0}, gE[3] = {0, 0, 0}, gB[3] = {0, 0, 0}, gS[3] = {0, 0, 0},
            dS[3] = {0, 0, 0}, gV[9] = {0};
+    // diffusion sector (:909-967): v.grad q^0_a, div q_a, grad (mu_a / T)
+    double gq[3] = {0, 0, 0}, dq[3] = {0, 0, 0}, ga[9] = {0};
+    double alpha_a[3] = {0, 0, 0};
+    if (diff) {
+      alpha_a[0] = s.th[kMuB][a] / s.th[kT][a];
+      alpha_a[1] = s.th[kMuS][a] / s.th[kT][a];
+      alpha_a[2] = s.th[kMuQ][a] / s.th[kT][a];
+    }
     const double pa = s.th[kP][a], ea = s.th[kE][a], sla = s.sigma_lab[a];
     const double sqa = 1.0 / (sla * sla);
     const double Pia = s.bulk[a];
@@ -245,6 +254,28 @@ void smooth_gradients(System& s, const NbrList& nl) {
           dS[i] += acc;
         }
       }
+      if (diff) {
+        const double alpha_b[3] = {s.th[kMuB][b] / s.th[kT][b], s.th[kMuS][b] / s.th[kT][b],
+                                   s.th[kMuQ][b] / s.th[kT][b]};
+        double ssKv = 0;
+        for (int d = 0; d < D; d++) ssKv += ssK[d] * va[d];
+        for (int c = 0; c < 3; c++) {
+          gq[c] += ssKv * (sqb * s.q[4 * c][b] + sqa * s.q[4 * c][a]);
+          double acc = 0.0;
+          for (int i = 0; i < D; i++) {
+            acc += sqb * ssK[i] * s.q[4 * c + i + 1][b] + sqa * ssK[i] * s.q[4 * c + i + 1][a];
+            ga[3 * i + c] += (mb / sla) * (alpha_b[c] - alpha_a[c]) * gK[i];
+          }
+          dq[c] += acc;
+        }
+      }
+    }
+    if (diff) {
+      for (int c = 0; c < 3; c++) {
+        s.grad_qa[c][a] = gq[c];
+        s.div_qa[c][a] = dq[c];
+      }
+      for (int k = 0; k < 9; k++) s.grad_alpha[k][a] = ga[k];
     }
     for (int d = 0; d < D; d++) {
       s.gradP[d][a] = gP[d];

@@ -1,0 +1,93 @@
+"""The oracle's diffusion sector on the CPU: the alpha derivatives against
+finite differences of the EoS inversion, the reference's derivative chain
+against the exact Hessian inverse where the chain is regular, the regulator
+cap, and an event that moves charge while keeping it."""
+import dataclasses
+
+import numpy as np
+
+from ccake_gb300 import ics
+import oracle_py as O
+
+
+def _alpha(rc, tgt, seed):
+    x, th, st, _ = O.eos_invert_batch(rc, 1, tgt[None, :], seeds=seed)
+    assert st[0] == 0
+    return np.array([th[0, 1], th[0, 2], th[0, 3]]) / th[0, 0], x   # muB, muS, muQ over T
+
+
+def test_alpha_derivatives_match_finite_differences():
+    # conformal-diagonal EoS, all three charges non-zero, exact inverse
+    rc = ics.RunConfig(eos_kind=1, thermo_mode=1)
+    tgt = np.array([20.0, 0.5, 0.1, 0.2])
+    a0, x = _alpha(rc, tgt, np.array([[1.0, 0.1, 0.1, 0.1]]))
+    da = O.eos_alpha_derivs(rc, 0, x)[0]
+    fd = np.zeros(12)
+    for j in range(4):
+        h = 1e-6 * max(abs(tgt[j]), 1.0)
+        tp, tm = tgt.copy(), tgt.copy()
+        tp[j] += h
+        tm[j] -= h
+        d = (_alpha(rc, tp, x)[0] - _alpha(rc, tm, x)[0]) / (2 * h)
+        if j == 0:
+            fd[0:3] = d
+        else:
+            for a in range(3):
+                fd[3 + 3 * a + (j - 1)] = d[a]
+    assert np.allclose(da, fd, rtol=1e-6, atol=1e-10 * np.max(np.abs(fd)))
+
+
+def test_alpha_chain_matches_exact_inverse_where_regular():
+    # conformal EoS: the Schur-complement chain of src/eos.cpp equals H^-1
+    for charges in ((0.5, 0.1, 0.2), (0.5, 0.0, 0.0)):
+        out = []
+        for tm in (0, 1):
+            rc = ics.RunConfig(eos_kind=0, thermo_mode=tm)
+            x, _, st, _ = O.eos_invert_batch(rc, 1, np.array([[20.0, *charges]]),
+                                             seeds=np.array([[1.0, 0.1, 0.1, 0.1]]))
+            assert st[0] == 0
+            out.append(O.eos_alpha_derivs(rc, 0, x)[0])
+        scale = np.max(np.abs(out[1]))
+        assert np.allclose(out[0], out[1], rtol=1e-12, atol=1e-14 * scale), charges
+    # baryon only: the S and Q rows vanish
+    assert np.all(np.abs(out[0][[4, 5, 6, 7, 8, 9, 10, 11]]) < 1e-100)
+
+
+def test_regulator_caps_the_current():
+    p, rc = ics.hotspots_2d(n_side=24, n_hot=3, seed=13)
+    # e above the regulator's e0 = 0.1 GeV/fm^3 everywhere, so that its
+    # strength is near chi0 and part of the current stays below the cap
+    p = dataclasses.replace(p, e=50.0 * p.e, rhoB=10.0 * p.rhoB, rhoQ=np.zeros_like(p.rhoQ))
+    rc = dataclasses.replace(rc, eos_kind=0, thermo_mode=0, using_diffusion=1, diffusion_mode=2,
+                             diffusion_relax_mode=1, C_B=0.4, diffusion_regulator=1)
+    o = O.OracleRun(p, rc)
+    o.set("in_qB1", 15.0 * p.rhoB * np.cos(6.0 * p.x))
+    assert o.initialize() == 0
+    for ph in ("neighbours", "velocity", "smooth_fields", "thermo", "reset_pi"):
+        o.phase(ph)
+    n = np.abs(o.get("rhoB"))
+    before = np.sqrt(np.maximum(o.get("qB1") ** 2 + o.get("qB2") ** 2 - o.get("qB0") ** 2, 0)) / n
+    o.phase("regulate_diffusion")
+    after = np.sqrt(np.maximum(o.get("qB1") ** 2 + o.get("qB2") ** 2 - o.get("qB0") ** 2, 0)) / n
+    # f(e) = chi0 (Fermi(e) - Fermi(0)) ~ 10 for e >> e0 = 0.1 GeV/fm^3
+    assert before.max() > 12.0
+    assert after.max() <= 10.0 * (1 + 1e-12)
+    capped = after < before * (1 - 1e-12)
+    assert capped.any() and (~capped).any()
+    assert np.allclose(after[~capped], before[~capped], rtol=1e-14)
+
+
+def test_diffusion_moves_charge_and_keeps_it():
+    p, rc = ics.hotspots_2d(n_side=24, n_hot=3, seed=11)
+    rc = dataclasses.replace(rc, using_diffusion=1, kappa_over_T2=(0.3, 0, 0, 0, 0, 0, 0, 0, 0.3))
+    o = O.OracleRun(p, rc)
+    assert o.initialize() == 0
+    b0, t0 = o.get("ext_B"), o.totals()
+    assert o.step(10) == 0
+    t1 = o.totals()
+    moved = np.max(np.abs(o.get("ext_B") - b0))
+    assert moved > 1e-6 * np.max(np.abs(b0))
+    # net baryon charge (with the q^0 terms) changes far less than it moves
+    assert abs(t1["B"] - t0["B"]) < 0.1 * moved * p.n
+    assert abs(t1["B"] - t0["B"]) < 1e-4 * abs(t0["B"])
+    assert np.isfinite(o.get("u0")).all() and np.max(np.abs(o.get("qB1"))) > 0
