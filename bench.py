@@ -771,15 +771,27 @@ def run_form_only(args, form):
     from ccake_gb300 import api, build
     build.build()
     p, rc = workload()
-    g = api.GpuHydro(dataclasses.replace(rc, precision=1 if form == "mixed" else 0))
+    rc = dataclasses.replace(rc, precision=1 if form == "mixed" else 0)
+    if args.diffusion:
+        # the diffusion sector on the same event: B and Q diffuse with
+        # kappa/T^2 = 0.3 (the event carries no strangeness)
+        rc = dataclasses.replace(rc, using_diffusion=1, kappa_over_T2=(0.3, 0, 0, 0, 0, 0, 0, 0, 0.3))
+    g = api.GpuHydro(rc)
     g.load(p)
     g.initialize()
     for _ in range(args.warmup):
         g.step(1)
     torch.cuda.synchronize()
     ms = g.step_timed(args.steps)
-    print(json.dumps({"partial": True, "form": form, "metric": METRIC, "unit": UNIT, "steps": args.steps,
-                      "ms_per_step": ms / args.steps, "value": p.n * args.steps / (ms * 1e-3)}))
+    line = {"partial": True, "form": form, "diffusion": bool(args.diffusion), "metric": METRIC, "unit": UNIT,
+            "steps": args.steps, "ms_per_step": ms / args.steps, "value": p.n * args.steps / (ms * 1e-3)}
+    if args.diffusion and not args.no_cpu:
+        steps = max(1, args.ref_steps)
+        value, dt = cpu_reference(p, rc, steps, warmup=1)
+        line["cpu_port"] = {"value": value, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                            "sample": f"median of 3 runs of {steps} RK2 steps after 1 warm-up step, all {p.n} "
+                                      "particles, diffusion on"}
+    print(json.dumps(line))
 
 
 def main():
@@ -802,6 +814,8 @@ def main():
     ap.add_argument("--eos-cpu-rows", type=int, default=20_000)
     ap.add_argument("--form", choices=["fp64", "mixed"], default=None,
                     help="time only this form's step loop (profiler launch lists); partial output")
+    ap.add_argument("--diffusion", action="store_true",
+                    help="with --form fp64: the diffusion sector on (kappa/T^2 = 0.3 for B and Q)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -115,12 +115,12 @@ struct Clock {
 
 // Freeze-out snapshot fields (FreezeOut::freeze_array, include/freeze_out.h):
 // r[3] u[3] gradP[3] gradE[3] s e rhoB rhoS rhoQ T muB muS muQ theta bulk
-// sigma_lab pi^{mu nu}[10 slots] pi^{33} shv_nabla_u w cs2; six snapshots
+// sigma_lab pi^{mu nu}[10 slots] pi^{33} shv_nabla_u w cs2 q^mu[3][4]; six snapshots
 // (frz1 frz2 fback fback2 fback3 fback4), field q of particle i of snapshot k
 // at (k * NSF + q) * n + i.
 enum SnapField : int { SF_R = 0, SF_U = 3, SF_GP = 6, SF_GE = 9, SF_S = 12, SF_E, SF_RB, SF_RS, SF_RQ, SF_T, SF_MUB,
                        SF_MUS, SF_MUQ, SF_THETA, SF_BULK, SF_SLAB, SF_SHV, SF_SHV33 = SF_SHV + 10, SF_SNU, SF_W, SF_CS2,
-                       NSF };
+                       SF_Q, NSF = SF_Q + 12 };
 // a freeze_out.dat row on the device: step, particle, then the fields
 // (src/output.cpp:433-475), 40 in 2-D, 45 in 3-D
 constexpr int kFoRow = 2 + 45;

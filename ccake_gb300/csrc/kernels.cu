@@ -904,6 +904,8 @@ __global__ void k_freeze_surface(RunConst rc, Ptrs p, int grads_f32, double dt) 
   cur[SF_SNU] = p.derivs[D_SNU * n + i];
   cur[SF_W] = p.th[T_W * n + i];
   cur[SF_CS2] = p.th[T_CS2 * n + i];
+  // the diffusion current q^mu of the evaluation (zero without the sector)
+  for (int k = 0; k < 12; k++) cur[SF_Q + k] = p.dif ? p.dif[(size_t)(F_Q + k) * n + i] : 0.0;
   // check_freeze_out_status
   int f = p.freeze[i];
   const double e = cur[SF_E];
@@ -996,7 +998,7 @@ __global__ void k_freeze_surface(RunConst rc, Ptrs p, int grads_f32, double dt) 
     const double tail[11] = {sFO, SN(k, SF_E), Tfluc, SN(k, SF_MUB), SN(k, SF_MUS), SN(k, SF_MUQ), w, cs2,
                              SN(k, SF_RB), SN(k, SF_RS), SN(k, SF_RQ)};
     for (int a = 0; a < 11; a++) r[w_++] = tail[a];
-    for (int a = 0; a < 12; a++) r[w_++] = 0.0;   // diffusion sector off
+    for (int a = 0; a < 12; a++) r[w_++] = SN(k, SF_Q + a);   // q^mu of the snapshot (diffout)
     r[w_++] = (rc.cfg.eos_kind == 2 && p.eos_id[i] == 0) ? 1.0 : 0.0;
   };
   auto closer = [&]() { return fabs(SN(0, SF_E) - ef) < fabs(SN(1, SF_E) - ef) ? 0 : 1; };

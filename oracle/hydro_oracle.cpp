@@ -1022,6 +1022,7 @@ void take_snapshot(const System& s, int a, double* out, int n) {
   O(SF_SNU) = s.shv_nabla_u[a];
   O(SF_W) = s.th[kW][a];
   O(SF_CS2) = s.th[kCs2][a];
+  for (int k = 0; k < 12; k++) O(SF_Q + k) = s.q[k][a];
 }
 
 void copy_snapshot(std::vector<double>& dst, const std::vector<double>& src, int a, int n) {
@@ -1108,7 +1109,7 @@ void interpolate(System& s, int a, const std::vector<double>& Sv, double tp) {
   for (int k = 0; k < D; k++) row.push_back(S(SF_R + k));
   for (double v : {sFO, Efluc, Tfluc, S(SF_MUB), S(SF_MUS), S(SF_MUQ), S(SF_W), cs2, S(SF_RB), S(SF_RS), S(SF_RQ)})
     row.push_back(v);
-  for (int k = 0; k < 12; k++) row.push_back(0.0);   // diffusion sector off
+  for (int k = 0; k < 12; k++) row.push_back(S(SF_Q + k));   // q^mu of the snapshot (diffout)
   row.push_back(s.eos_id[a] >= 0 && s.cfg.eos_kind == 2 && s.eos_id[a] == 0 ? 1.0 : 0.0);
   s.fo_rows.push_back(row);
 }

@@ -68,10 +68,10 @@ struct Config {
 // Freeze-out snapshot of one step (FreezeOut::freeze_array,
 // include/freeze_out.h:20-80): per particle r[3] u[3] gradP[3] gradE[3]
 // s e rhoB rhoS rhoQ T muB muS muQ theta bulk sigma_lab pi^{mu nu}[10]
-// pi^{33} shv_nabla_u w cs2.
+// pi^{33} shv_nabla_u w cs2 q^mu[3][4].
 enum SnapField : int { SF_R = 0, SF_U = 3, SF_GP = 6, SF_GE = 9, SF_S = 12, SF_E, SF_RB, SF_RS, SF_RQ, SF_T, SF_MUB,
                        SF_MUS, SF_MUQ, SF_THETA, SF_BULK, SF_SLAB, SF_SHV, SF_SHV33 = SF_SHV + 10, SF_SNU, SF_W, SF_CS2,
-                       NSF };
+                       SF_Q, NSF = SF_Q + 12 };
 
 // Per-particle state, struct of arrays.
 struct System {

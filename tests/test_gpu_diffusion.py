@@ -175,3 +175,22 @@ def test_diffusion_off_matches_plain_and_rejects_unsupported():
     for bad in (dict(precision=1), dict(coord=1), dict(diffusion_mode=1)):
         with pytest.raises(api.CcakeError):
             api.GpuHydro(dataclasses.replace(rc, using_diffusion=1, **bad))
+
+
+def test_diffusion_freeze_out_rows():
+    # the hypersurface rows carry the snapshot's q^mu in their twelve
+    # diffusion columns (FreezeOut diffout, src/output.cpp:463-474)
+    p, rc = ics.hotspots_2d(n_side=40, n_hot=4, seed=11)
+    rc = dataclasses.replace(rc, using_diffusion=1, kappa_over_T2=KAPPA, freeze_out_T=0.3 / 0.1973269804,
+                             particlization=1, surface=1)
+    gpu, orc = make_pair(p, rc)
+    for _ in range(3):
+        gpu.step(4)
+        assert orc.step(4) == 0
+    rg, ro = gpu.freeze_out_rows(), orc.freeze_out_rows()
+    assert ro.shape[0] >= 3 and rg.shape == ro.shape
+    assert np.array_equal(rg[:, :2], ro[:, :2])
+    scale = np.abs(ro) + 1e-6 * np.max(np.abs(ro), axis=0) + 1e-300
+    assert np.max(np.abs(rg - ro) / scale) < 1e-9
+    q = ro[:, -13:-1]
+    assert np.max(np.abs(q[:, 1:3])) > 0.0      # q_B^x, q_B^y
