@@ -470,10 +470,9 @@ ccake_status_t ccake_ctx_create(const ccake_config* cfg, ccake_ctx** out) {
   if (!(cfg->skin_frac >= 0.0)) return CCAKE_ERR_INVALID;
   if (!(cfg->hT > 0) || !(cfg->t0 > 0) || !(cfg->dt > 0)) return CCAKE_ERR_INVALID;
   if (cfg->dim == 3 && cfg->factorized_kernel) return CCAKE_ERR_INVALID;
-  // the diffusion sector runs in the FP64 form, Milne coordinates, with the
-  // constant_over_T2 or kappaB_coth coefficients
-  if (cfg->using_diffusion &&
-      (cfg->precision != 0 || cfg->coord != 0 || (cfg->diffusion_mode != 0 && cfg->diffusion_mode != 2)))
+  // the diffusion sector runs in the FP64 form with the constant_over_T2 or
+  // kappaB_coth coefficients
+  if (cfg->using_diffusion && (cfg->precision != 0 || (cfg->diffusion_mode != 0 && cfg->diffusion_mode != 2)))
     return CCAKE_ERR_INVALID;
   ccake_ctx* ctx = new ccake_ctx;
   ctx->cfg = *cfg;

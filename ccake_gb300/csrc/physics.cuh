@@ -506,7 +506,9 @@ __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, cons
           itt[3 * c + d] = a1;
           itk[3 * c + d] = a2;
         }
-      const double X_ = g_ * divV + geo + g_ / t;
+      // Cartesian twin (src/eom_cartesian.cpp:1327-1722): no F_D terms, the
+      // expansion rate gamma div v alone, metric without tau
+      const double X_ = cart ? g_ * divV : g_ * divV + geo + g_ / t;
       const double omg = 1. - g_ * g_;
       double qc[3][4];
       for (int c = 0; c < 3; c++) {
@@ -518,8 +520,9 @@ __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, cons
       double F0D[3], F0a[3], A0a[3], R0a[3][3], M0a[3][3], M0D[3][3];
       for (int c = 0; c < 3; c++) {
         const double q0 = dif->q[4 * c];
-        F0D[c] = g_ * g_ * geo * q0 + 2. * g_ * g_ * qc[c][3] * u[2] / t + t * g_ * qc[c][0] * u[2] * u[2] +
-                 t * u[2] * dif->q[4 * c + 3];
+        F0D[c] = cart ? 0.0
+                      : g_ * g_ * geo * q0 + 2. * g_ * g_ * qc[c][3] * u[2] / t + t * g_ * qc[c][0] * u[2] * u[2] +
+                            t * u[2] * dif->q[4 * c + 3];
         F0a[c] = omg * sig_ * dif->da[c] * Fs;
         A0a[c] = -omg * dif->da[c] * double(sden) / g_;
         for (int i = 0; i < D; i++) {
@@ -558,7 +561,8 @@ __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, cons
           RN[3 * c + d] += -acc;
         }
         FN[c] = 0.0;
-        FN[c] += -F0q + dif->gq[c] - dif->dq[c] - dif->q[4 * c] / t;
+        if (cart) FN[c] += -F0q + dif->gq[c] - dif->dq[c];
+        else FN[c] += -F0q + dif->gq[c] - dif->dq[c] - dif->q[4 * c] / t;
       }
       inverse3(RN, RI);
       // R_u = -u gamma (R_w + R_bulk sigma), R_w = sigma dw/drho + sigma dw/ds R_S
@@ -642,9 +646,9 @@ __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, cons
           itt[3 * c + d] = a1;
           itk[3 * c + d] = a2;
         }
-      const double X_ = g * divV + geo + g / t;
+      const double X_ = cart ? g * divV : g * divV + geo + g / t;
       const double gs = g * sig;
-      const double cmd[4] = {1., -1., -1., -1. / t / t};
+      const double cmd[4] = {1., -1., -1., cart ? -1. : -1. / t / t};
       const double fuc[3] = {-u[0], -u[1], -t2 * u[2]};
       double qc[3][4];
       for (int c = 0; c < 3; c++) {
@@ -659,7 +663,7 @@ __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, cons
                                i < D ? dif->ga[3 * i + 2] : 0.0};
         double FD[3], Fa[3], Aa[3], MD[3][3], Ma[3][3], Ra[3][3];
         for (int c = 0; c < 3; c++) {
-          FD[c] = fui * g * dif->q[4 * c] * geo + 2. * fui * qc[c][3] * u[2] * g / t;
+          FD[c] = cart ? 0.0 : fui * g * dif->q[4 * c] * geo + 2. * fui * qc[c][3] * u[2] * g / t;
           Fa[c] = -fui * g * sig * dif->da[c] * Fs + cmd[i + 1] * gai[c];
           Aa[c] = fui * dif->da[c] * double(sden);
           for (int j = 0; j < 3; j++) {

@@ -64,8 +64,8 @@ typedef struct ccake_config {
                                  hypersurface (FreezeOut::bsqsvinterpolate), rows
                                  of freeze_out.dat, ccake_freeze_out_rows */
   /* diffusion sector (include/settings.h diffusionMode != "disabled";
-   * src/eom_default.cpp:1415-1817): FP64 form (precision 0), Milne
-   * coordinates (coord 0), Newton EoS (no pre-inverted tables) */
+   * src/eom_default.cpp:1415-1817, src/eom_cartesian.cpp:1327-1722): FP64
+   * form (precision 0), Newton EoS (no pre-inverted tables) */
   int32_t using_diffusion;
   int32_t diffusion_mode;       /* 0 constant_over_T2 (kappa = kappa_over_T2 T^2), 2 kappaB_coth */
   int32_t diffusion_relax_mode; /* 0 tau_q = 0.2/T; 1 tau_q = C_B/T (kappaB_coth) */

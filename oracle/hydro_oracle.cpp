@@ -170,7 +170,10 @@ struct DiffMRF {
 // lines after it have no effect and are not restated.
 void diffusion_mrf(const System& s, int a, double t, const double* Ms, double Fs, DiffMRF& o) {
   const int D = s.cfg.dim;
-  const double t2 = t * t;
+  // the Cartesian twin (src/eom_cartesian.cpp:1327-1722): metric without
+  // tau, no F_D terms, expansion rate gamma div v
+  const bool cart = s.cfg.coord == 1;
+  const double t2 = cart ? 1.0 : t * t;
   const double sig = s.sigma[a], g = s.gamma[a], sden = s.th[kS][a], T = s.th[kT][a];
   const double rho[3] = {s.th[kRhoB][a], s.th[kRhoS][a], s.th[kRhoQ][a]};
   const double mu[3] = {s.th[kMuB][a], s.th[kMuS][a], s.th[kMuQ][a]};
@@ -196,8 +199,8 @@ void diffusion_mrf(const System& s, int a, double t, const double* Ms, double Fs
   for (int i = 0; i < 3; i++) uc[i] = u[i];
   cov_D(D, uc, t2);
   const double fuc[3] = {-fu[0], -fu[1], -t2 * fu[2]};
-  const double geo = dEta(D, D - 1) * u[D - 1] * u[D - 1] * t / g;
-  const double cmd[4] = {1., -1., -1., -1. / t / t};
+  const double geo = cart ? 0.0 : dEta(D, D - 1) * u[D - 1] * u[D - 1] * t / g;
+  const double cmd[4] = {1., -1., -1., cart ? -1. : -1. / t / t};
   double tq[9], kq[9], itq[9], itt[9], itk[9];
   for (int k = 0; k < 9; k++) { tq[k] = s.tau_q[k][a]; kq[k] = s.kappa_q[k][a]; }
   inverse(3, tq, itq);
@@ -210,13 +213,14 @@ void diffusion_mrf(const System& s, int a, double t, const double* Ms, double Fs
         itk[3 * c + d] += itq[3 * c + k] * kq[3 * k + d];
       }
     }
-  const double X = g * divV + geo + g / t;
+  const double X = cart ? g * divV : g * divV + geo + g / t;
   const double omg = 1. - g * g;
   // the 0 (time) components
   double F0D[3], F0a[3], A0a[3], R0a[3][3], M0a[3][3] = {{0}}, M0D[3][3] = {{0}};
   for (int c = 0; c < 3; c++) {
-    F0D[c] = g * g * geo * q[c][0] + 2. * g * g * qc[c][3] * fu[2] / t + t * g * qc[c][0] * fu[2] * fu[2] +
-             t * fu[2] * q[c][3];
+    F0D[c] = cart ? 0.0
+                  : g * g * geo * q[c][0] + 2. * g * g * qc[c][3] * fu[2] / t + t * g * qc[c][0] * fu[2] * fu[2] +
+                        t * fu[2] * q[c][3];
     F0a[c] = omg * sig * das[c] * Fs;
     A0a[c] = -omg * das[c] * sden / g;
     for (int i = 0; i < D; i++) {
@@ -253,7 +257,7 @@ void diffusion_mrf(const System& s, int a, double t, const double* Ms, double Fs
   double FD[3][3], Fa[3][3], Aa[3][3], MD[3][3][3], Ma[3][3][3], Ra[3][3][3];
   for (int i = 0; i < 3; i++)
     for (int c = 0; c < 3; c++) {
-      FD[i][c] = fu[i] * g * q[c][0] * geo + 2. * fu[i] * qc[c][3] * fu[2] * g / t;
+      FD[i][c] = cart ? 0.0 : fu[i] * g * q[c][0] * geo + 2. * fu[i] * qc[c][3] * fu[2] * g / t;
       Fa[i][c] = -fu[i] * g * sig * das[c] * Fs + cmd[i + 1] * ga[i][c];
       Aa[i][c] = fu[i] * das[c] * sden;
       for (int j = 0; j < 3; j++) {
@@ -578,7 +582,7 @@ void hydro_numbers(System& s, int a, const double* sig5) {
 // and the inverse Reynolds number |q_a| / |n_a| (zero for |n_a| <= 1e-15).
 void diffusion_numbers(System& s, int a) {
   const int D = s.cfg.dim;
-  const double t2 = s.t * s.t;
+  const double t2 = s.cfg.coord == 1 ? 1.0 : s.t * s.t;
   const double rho[3] = {s.th[kRhoB][a], s.th[kRhoS][a], s.th[kRhoQ][a]};
   for (int c = 0; c < 3; c++) {
     double gsq = 0.0;
@@ -836,7 +840,8 @@ void evaluate_time_derivatives(System& s) {
         for (int c = 0; c < 3; c++) MN[i][c] += -dm.M0q[3 * c + i];
       for (int c = 0; c < 3; c++) {
         for (int d = 0; d < 3; d++) RN[3 * c + d] += -dm.R0q[3 * c + d];
-        FN[c] += -dm.F0q[c] + s.grad_qa[c][a] - s.div_qa[c][a] - s.q[4 * c][a] / t;
+        if (cart) FN[c] += -dm.F0q[c] + s.grad_qa[c][a] - s.div_qa[c][a];
+        else FN[c] += -dm.F0q[c] + s.grad_qa[c][a] - s.div_qa[c][a] - s.q[4 * c][a] / t;
       }
       inverse(3, RN, RI);
       // R_u = -u gamma (R_w + R_bulk sigma), R_w = sigma dw/drho + sigma dw/ds R_S;

@@ -110,15 +110,18 @@ def test_diffusion_phase_parity(case):
         assert relerr(gpu.get(f), orc.get(f), GRAD_FLOOR) < RTOL, f
 
 
-@pytest.mark.parametrize("case", ["hotspots2d", "hotspots3d", "coth"])
+@pytest.mark.parametrize("case", ["hotspots2d", "hotspots3d", "coth", "cartesian2d", "cartesian3d"])
 def test_diffusion_evolution_parity(case):
+    # cartesian: the twin of src/eom_cartesian.cpp:1327-1722 (coord = 1)
     q = None
     if case == "coth":
         p, rc, q = baryon_coth()
         steps = 10
     else:
-        p, rc = hotspots_diffusion(2 if case == "hotspots2d" else 3)
-        steps = 10 if case == "hotspots2d" else 3
+        p, rc = hotspots_diffusion(3 if case.endswith("3d") else 2)
+        steps = 3 if case.endswith("3d") else 10
+        if case.startswith("cartesian"):
+            rc = dataclasses.replace(rc, coord=1)
     gpu, orc = make_pair(p, rc, q)
     b0 = gpu.get("ext_B")
     gpu.step(steps)
@@ -126,7 +129,7 @@ def test_diffusion_evolution_parity(case):
     fields = ["x", "y", "u0", "u1", "ext_s", "ext_B", "T", "e", "muB", "ext_qB0", "ext_qB1", "qB0", "qB1"]
     if case != "coth":
         fields += ["ext_Q", "ext_qQ0", "ext_qQ1", "ext_shv0", "shv00"]
-    if case == "hotspots3d":
+    if case.endswith("3d"):
         fields += ["eta", "u2", "ext_qB2"]
     for f in fields:
         floor = 1e-5 if f[0] in "uq" or f.startswith("ext_q") else 1e-6
@@ -160,7 +163,7 @@ def test_diffusion_numbers_and_system_state(tmp_path):
 
 def test_diffusion_off_matches_plain_and_rejects_unsupported():
     # with kappa = 0 and no initial current the sector leaves the evolution as
-    # it is without it; the mixed form and Cartesian coordinates reject it
+    # it is without it; the mixed form and the DNMR mode reject it
     p, rc = ics.hotspots_2d(n_side=32, n_hot=4, seed=5)
     plain = api.GpuHydro(rc)
     plain.load(p)
@@ -172,7 +175,7 @@ def test_diffusion_off_matches_plain_and_rejects_unsupported():
     zero.step(5)
     for f in ("x", "u0", "e", "ext_B"):
         assert relerr(zero.get(f), plain.get(f), 1e-5) < 1e-12, f
-    for bad in (dict(precision=1), dict(coord=1), dict(diffusion_mode=1)):
+    for bad in (dict(precision=1), dict(diffusion_mode=1)):
         with pytest.raises(api.CcakeError):
             api.GpuHydro(dataclasses.replace(rc, using_diffusion=1, **bad))
 
