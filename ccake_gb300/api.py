@@ -98,6 +98,7 @@ def lib():
         L.ccake_write_freeze_out.argtypes = [P, ctypes.c_char_p, _f64, _f64, _f64]
         L.ccake_hydro_numbers.argtypes = [P]
         L.ccake_set_initial_diffusion.argtypes = [P, _dp]
+        L.ccake_set_initial_viscous.argtypes = [P, _dp, _dp]
         L.ccake_write_system_state.argtypes = [P, ctypes.c_char_p]
         L.ccake_ic_read_ccake.argtypes = [ctypes.c_char_p, ctypes.POINTER(IcOptions), ctypes.POINTER(P)]
         L.ccake_ic_info.argtypes = [P, ctypes.POINTER(_i64), _dp]
@@ -195,6 +196,20 @@ class GpuHydro:
                            _d(arrs["uy"]), _d(arrs["ueta"]))
         self._check(lib().ccake_load_particles(self.h, ctypes.byref(soa)), "load")
         self.n = particles.n
+
+    def set_initial_viscous(self, trace=None, pi=None):
+        """Initial bulk (trace input of bulk_from_trace, n) and/or shear (pi[6, n]:
+        xx xy xeta yy yeta etaeta) of the loaded particles; between load and initialize."""
+        tr = None if trace is None else np.ascontiguousarray(trace, dtype=np.float64)
+        pv = None if pi is None else np.ascontiguousarray(pi, dtype=np.float64)
+        if tr is not None and tr.shape != (self.n,):
+            raise ValueError("trace must have shape (n,)")
+        if pv is not None and pv.shape != (6, self.n):
+            raise ValueError("pi must have shape (6, n)")
+        self._keep_visc = (tr, pv)
+        self._check(lib().ccake_set_initial_viscous(self.h, None if tr is None else tr.ctypes.data_as(_dp),
+                                                    None if pv is None else pv.ctypes.data_as(_dp)),
+                    "set_initial_viscous")
 
     def set_initial_diffusion(self, q):
         """Initial diffusion currents, q[4 c + mu, i] = q^mu of charge c (B, S,

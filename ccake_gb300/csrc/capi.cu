@@ -62,6 +62,9 @@ struct ccake_ctx {
   // scratch of the two-pass batch inversion (capacity + 1 int32)
   int32_t* eos_scratch = nullptr;
   int64_t eos_scratch_cap = 0;
+  // initial viscous input (ccake_set_initial_viscous): trace, pi^{xx xy xeta yy yeta}
+  double* init_visc = nullptr;
+  int init_bulk = 0, init_shear = 0;
 };
 
 namespace {
@@ -115,6 +118,9 @@ void free_buffers(ccake_ctx* ctx) {
   if (ctx->p.dif) cudaFree(ctx->p.dif);
   if (ctx->p.recQ) cudaFree(ctx->p.recQ);
   ctx->p.dif = ctx->p.recQ = nullptr;
+  if (ctx->init_visc) cudaFree(ctx->init_visc);
+  ctx->init_visc = nullptr;
+  ctx->init_bulk = ctx->init_shear = 0;
   ctx->dbuf = nullptr;
   ctx->ibuf = nullptr;
   ctx->p.fz = ctx->p.fo_rows = nullptr;
@@ -613,6 +619,34 @@ ccake_status_t ccake_load_particles(ccake_ctx* ctx, const ccake_particles_soa* h
   return CCAKE_OK;
 }
 
+ccake_status_t ccake_set_initial_viscous(ccake_ctx* ctx, const double* trace, const double* pi) {
+  if (!ctx || (!trace && !pi)) return CCAKE_ERR_INVALID;
+  if (!ctx->loaded) return fail(ctx, CCAKE_ERR_STATE, "load particles first");
+  if (ctx->initialized) return fail(ctx, CCAKE_ERR_STATE, "set the initial viscous state before initialize");
+  const int64_t n = ctx->n;
+  if (!ctx->init_visc && cudaMalloc(&ctx->init_visc, 6 * (size_t)n * sizeof(double)) != cudaSuccess)
+    return fail(ctx, CCAKE_ERR_NOMEM, "allocation");
+  std::vector<double> tmp((size_t)n);
+  auto up = [&](const double* src, int row) -> ccake_status_t {
+    for (int64_t k = 0; k < n; k++) tmp[k] = src[ctx->perm[k]];
+    CK(cudaMemcpyAsync(ctx->init_visc + (size_t)row * n, tmp.data(), n * sizeof(double), cudaMemcpyHostToDevice,
+                       ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return CCAKE_OK;
+  };
+  ccake_status_t s;
+  if (trace) {
+    if ((s = up(trace, 0))) return s;
+    ctx->init_bulk = 1;
+  }
+  if (pi) {
+    for (int k = 0; k < 5; k++)
+      if ((s = up(pi + (size_t)k * n, 1 + k))) return s;
+    ctx->init_shear = 1;
+  }
+  return CCAKE_OK;
+}
+
 ccake_status_t ccake_set_initial_diffusion(ccake_ctx* ctx, const double* q) {
   if (!ctx || !q) return CCAKE_ERR_INVALID;
   if (!ctx->loaded) return fail(ctx, CCAKE_ERR_STATE, "load particles first");
@@ -699,15 +733,17 @@ ccake_status_t ccake_initialize(ccake_ctx* ctx) {
   launch_passA(ctx->rc, ctx->eos, ctx->p, A_SMOOTH_ONLY, ctx->stream);   // initial sigma
   launch_init_ext(ctx->rc, ctx->p, ctx->stream);
   const int64_t n = ctx->n;
-  if (ctx->p.dif) {
-    // initial smoothing, then set_diffusion (ext q = q^i / sigma of that
-    // smoothing, src/sph_workstation.cpp:394-457, :1441-1458), then the
-    // thermodynamics and q^mu
+  if (ctx->p.dif || ctx->init_bulk || ctx->init_shear) {
+    // initial smoothing, then calculate_extensive_shv, set_bulk_Pi and
+    // set_diffusion against its sigma (src/sph_workstation.cpp:394-457,
+    // :1350-1458), then the thermodynamics, pi, Pi and q^mu
     launch_passA(ctx->rc, ctx->eos, ctx->p, A_SMOOTH_ONLY, ctx->stream);
+    launch_init_viscous(ctx->p, ctx->init_visc, ctx->init_bulk, ctx->init_shear, ctx->stream);
     launch_init_diffusion(ctx->rc, ctx->p, ctx->stream);
     launch_thermo(ctx->rc, ctx->eos, ctx->p, ctx->stream);
-    CK(cudaMemcpyAsync(ctx->p.dif + (size_t)F_YQ0 * n, ctx->p.dif + (size_t)F_YQ * n, 9 * n * sizeof(double),
-                       cudaMemcpyDeviceToDevice, ctx->stream));
+    if (ctx->p.dif)
+      CK(cudaMemcpyAsync(ctx->p.dif + (size_t)F_YQ0 * n, ctx->p.dif + (size_t)F_YQ * n, 9 * n * sizeof(double),
+                         cudaMemcpyDeviceToDevice, ctx->stream));
   } else {
     launch_passA(ctx->rc, ctx->eos, ctx->p, A_WITH_THERMO, ctx->stream);   // initial smoothing
   }

@@ -618,6 +618,21 @@ __global__ void k_init_ext(RunConst rc, Ptrs p) {
   ra[3] = make_double2(m * p.y[Y_ESS * n + i], m * p.y[Y_EQ * n + i]);
 }
 
+// Initial viscous state (src/sph_workstation.cpp:1350-1430): with
+// bulk_from_trace, ext Pi = (trace - p) / sigma (p of the e -> s inversion);
+// with input_initial_shear, ext pi^{ij} = pi^{ij} / sigma for (1,1) (1,2)
+// (1,3) (2,2) (2,3). iv: the input trace, then pi^{xx xy xeta yy yeta}.
+__global__ void k_init_viscous(Ptrs p, const double* iv, int bulk, int shear) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.n) return;
+  const int n = p.n;
+  const double sg = p.sig[i];
+  if (bulk) p.y[Y_EBULK * n + i] = (iv[i] - p.th[T_P * n + i]) / sg;
+  if (shear)
+#pragma unroll
+    for (int k = 0; k < 5; k++) p.y[(Y_SHV0 + k) * n + i] = iv[(size_t)(1 + k) * n + i] / sg;
+}
+
 // set_diffusion (src/sph_workstation.cpp:1441-1458): ext q = q^i / sigma;
 // the initial spatial currents q^i wait in the step-start slots until here
 __global__ void k_init_diffusion(Ptrs p) {
@@ -1296,6 +1311,10 @@ void launch_init_ext(const RunConst& rc, const Ptrs& p, cudaStream_t s) {
   const int nb = (p.n + kBlock - 1) / kBlock;
   if (rc.cfg.dim == 3) k_init_ext<3><<<nb, kBlock, 0, s>>>(rc, p);
   else k_init_ext<2><<<nb, kBlock, 0, s>>>(rc, p);
+}
+
+void launch_init_viscous(const Ptrs& p, const double* iv, int bulk, int shear, cudaStream_t s) {
+  if (iv && (bulk || shear)) k_init_viscous<<<(p.n + kBlock - 1) / kBlock, kBlock, 0, s>>>(p, iv, bulk, shear);
 }
 
 void launch_init_diffusion(const RunConst& rc, const Ptrs& p, cudaStream_t s) {

@@ -145,6 +145,19 @@ ccake_status_t ccake_ctx_destroy(ccake_ctx* ctx);
  * src/system_state.cpp:57-326). */
 ccake_status_t ccake_load_particles(ccake_ctx* ctx, const ccake_particles_soa* host);
 
+/* Initial viscous state of the loaded particles (src/sph_workstation.cpp:
+ * 1350-1430; the IC file's bulk and pi columns, internal units, the caller's
+ * particle order). trace (n doubles, may be NULL): the bulk column as the
+ * trace input of bulk_from_trace, ext Pi = (trace - p) / sigma
+ * (SPHWorkstation::set_bulk_Pi). pi (6 rows of n, may be NULL): pi^{xx},
+ * pi^{xy}, pi^{x eta}, pi^{yy}, pi^{y eta}, pi^{eta eta} as with
+ * input_initial_shear, ext pi^{ij} = pi^{ij} / sigma for the five stored
+ * entries (calculate_extensive_shv; pi^{eta eta} follows from
+ * tracelessness). sigma is that of the initial smoothing. Without this call
+ * both start at zero. Call between ccake_load_particles and
+ * ccake_initialize. */
+ccake_status_t ccake_set_initial_viscous(ccake_ctx* ctx, const double* trace, const double* pi);
+
 /* Initial diffusion currents of the loaded particles (the reference's
  * input_initial_diffusion columns, src/BSQHydro.cpp:345-375): q has 12 rows
  * of n doubles in the caller's particle order, row 4c + mu = q^mu of charge

@@ -74,6 +74,8 @@ std::vector<double>* field(System& s, const std::string& k) {
   if (k == "in_rhoB") return &s.in_rho[0];
   if (k == "in_rhoS") return &s.in_rho[1];
   if (k == "in_rhoQ") return &s.in_rho[2];
+  if (k == "in_bulk") return &s.in_bulk;
+  for (int i = 0; i < 6; i++) if (k == "in_shv" + std::to_string(i)) return &s.in_shv[i];
   if (k == "ext_bulk") return &s.ext_bulk;
   if (k == "Ez") return &s.Ez;
   if (k == "dEz") return &s.dEz;
@@ -179,6 +181,11 @@ int orc_phase(void* p, const char* name) {
   else if (k == "derivatives") get_time_derivatives(h->s, h->nl);
   else return -1;
   return 0;
+}
+
+void orc_set_initial_viscous(void* p, int bulk, int shear) {
+  ((Handle*)p)->s.use_in_bulk = bulk;
+  ((Handle*)p)->s.use_in_shv = shear;
 }
 
 double orc_time(void* p) { return ((Handle*)p)->s.t; }

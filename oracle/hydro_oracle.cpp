@@ -1308,10 +1308,13 @@ void initialize(System& s, NbrList& nl) {
   // initial_smoothing
   update_velocity(s);
   smooth_fields(s, nl);
-  for (int a = 0; a < s.n; a++) {  // calculate_extensive_shv (no initial shear), set_bulk_Pi
-    for (int k = 0; k < 6; k++) s.ext_shv[k][a] = 0.0;
+  // calculate_extensive_shv and set_bulk_Pi (src/sph_workstation.cpp:
+  // 1350-1430): the input pi^{ij} / sigma with input_initial_shear, (trace -
+  // p) / sigma with bulk_from_trace (p of the e -> s inversion), else zero
+  for (int a = 0; a < s.n; a++) {
+    for (int k = 0; k < 6; k++) s.ext_shv[k][a] = (s.use_in_shv && k < 5) ? s.in_shv[k][a] / s.sigma[a] : 0.0;
     for (int k = 0; k < 16; k++) s.shv[k][a] = 0.0;
-    s.ext_bulk[a] = 0.0;
+    s.ext_bulk[a] = s.use_in_bulk ? (s.in_bulk[a] - s.th[kP][a]) / s.sigma[a] : 0.0;
     s.bulk[a] = 0.0;
     // set_diffusion (src/sph_workstation.cpp:1441-1458): ext q = q^i / sigma
     for (int c = 0; c < 3; c++)

@@ -102,6 +102,9 @@ struct System {
   // input
   std::vector<double> in_e, in_s, in_rho[3], in_bulk;
   std::vector<double> in_shv[6];    // pi^{xx},xy,xeta,yy,yeta,etaeta (fm^-4..)
+  // use the input bulk as the trace of bulk_from_trace / the input pi^{ij}
+  // as with input_initial_shear (set_bulk_Pi, calculate_extensive_shv)
+  int use_in_bulk = 0, use_in_shv = 0;
   // derived
   std::vector<double> gamma, v[3], sigma_lab, sigma, smoothed[4];
   // thermo: T, muB, muS, muQ, p, s, rhoB, rhoS, rhoQ, e, w, cs2, dwds, dwdB, dwdS, dwdQ

@@ -72,6 +72,7 @@ def lib():
         L.orc_time.restype = D
         L.orc_time.argtypes = [P]
         L.orc_set_time.argtypes = [P, D]
+        L.orc_set_initial_viscous.argtypes = [P, I, I]
         L.orc_get.argtypes = [P, ctypes.c_char_p, dp]
         L.orc_set.argtypes = [P, ctypes.c_char_p, dp]
         L.orc_get_int.argtypes = [P, ctypes.c_char_p, ip]
@@ -122,6 +123,15 @@ class OracleRun:
 
     def initialize(self) -> int:
         return lib().orc_initialize(self.h)
+
+    def set_initial_viscous(self, trace=None, pi=None):
+        """As GpuHydro.set_initial_viscous (before initialize)."""
+        if trace is not None:
+            self.set("in_bulk", trace)
+        if pi is not None:
+            for k in range(6):
+                self.set(f"in_shv{k}", pi[k])
+        lib().orc_set_initial_viscous(self.h, int(trace is not None), int(pi is not None))
 
     def step(self, n=1) -> int:
         return lib().orc_step(self.h, n)

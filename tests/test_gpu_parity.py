@@ -422,3 +422,34 @@ def test_cartesian_parity(dim):
     mixed.initialize()
     mixed.step(steps)
     assert relerr(mixed.get("e"), gpu.get("e")) < 1e-5
+
+
+def test_initial_viscous_state_parity():
+    # input_initial_shear and bulk_from_trace (src/sph_workstation.cpp:
+    # 1350-1430): the IC's pi^{ij} and trace set the extensive shear and bulk
+    # against the sigma of the initial smoothing
+    p, rc = ics.hotspots_2d(n_side=40, n_hot=5, seed=11)
+    rc = dataclasses.replace(rc, zeta_over_s=0.02)
+    trace = 0.9 * p.e / 3.0
+    pi = np.zeros((6, p.n))
+    pi[0] = 0.05 * p.e * np.cos(3.0 * p.x)
+    pi[3] = -pi[0]
+    pi[1] = 0.02 * p.e * np.sin(2.0 * p.y)
+    gpu = api.GpuHydro(rc)
+    gpu.load(p)
+    gpu.set_initial_viscous(trace, pi)
+    orc = O.OracleRun(p, rc)
+    orc.set_initial_viscous(trace, pi)
+    gpu.initialize()
+    assert orc.initialize() == 0
+    for f in ("ext_bulk", "ext_shv0", "ext_shv1", "ext_shv3", "bulk", "shv11", "shv12", "shv00", "shv33"):
+        assert relerr(gpu.get(f), orc.get(f), 1e-5) < RTOL, f
+    assert np.allclose(gpu.get("shv11"), pi[0], rtol=1e-12, atol=1e-14)
+    gpu.step(10)
+    assert orc.step(10) == 0
+    for f in ("x", "u0", "u1", "ext_s", "e", "ext_bulk", "ext_shv0", "ext_shv1", "shv00"):
+        floor = 1e-5 if f[0] == "u" else 1e-6
+        assert relerr(gpu.get(f), orc.get(f), floor) < RTOL, f
+    tg, to = gpu.totals(), orc.totals()
+    for k in ("S", "E"):
+        assert abs(tg[k] - to[k]) <= 1e-10 * (abs(to[k]) + 1e-30), k
