@@ -23,6 +23,7 @@
 #ifndef CCAKE_GPU_HPP
 #define CCAKE_GPU_HPP
 
+#include <memory>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -103,6 +104,16 @@ class SPHWorkstation {
     check(ccake_time_derivatives(s_.ctx()), s_.ctx(), "ccake_time_derivatives");
   }
   void advance_timestep(double dt, int rk_order) { evolver_.execute_timestep(dt, rk_order); }
+  // the IC's initial currents (set_diffusion, src/sph_workstation.cpp:
+  // 1441-1458): q holds 12 rows of n, q^mu of charge c at row 4c + mu
+  void set_diffusion(const double* q) {
+    check(ccake_set_initial_diffusion(s_.ctx(), q), s_.ctx(), "ccake_set_initial_diffusion");
+  }
+  // the IC's initial shear and bulk (calculate_extensive_shv, set_bulk_Pi,
+  // src/sph_workstation.cpp:1350-1430); either may be null
+  void set_initial_viscous(const double* trace, const double* pi) {
+    check(ccake_set_initial_viscous(s_.ctx(), trace, pi), s_.ctx(), "ccake_set_initial_viscous");
+  }
   // stop rule: every particle frozen out (with particlization) or t > max_tau
   // (src/sph_workstation.cpp:1992-2024)
   bool continue_evolution() const {
@@ -145,9 +156,41 @@ class EquationOfState {
 
 class BSQHydro {
  public:
-  BSQHydro(const ccake_config& cfg, double max_tau) : sys_(cfg), ws_(sys_, max_tau), dt_(cfg.dt) {}
+  BSQHydro(const ccake_config& cfg, double max_tau)
+      : sys_(cfg), ws_(sys_, max_tau), dt_(cfg.dt), diffusion_(cfg.using_diffusion != 0) {}
   void read_in_initial_conditions(const ccake_particles_soa& soa) {
     check(ccake_load_particles(sys_.ctx(), &soa), sys_.ctx(), "ccake_load_particles");
+  }
+  // BSQHydro::read_ccake (src/BSQHydro.cpp:206-425) with the settings it
+  // consults, then the IC's initial currents (input_initial_diffusion) and,
+  // when asked, its initial shear (input_initial_shear) and bulk
+  // (bulk_from_trace)
+  void read_ccake(const char* path, const ccake_ic_options& opt, bool initial_shear = false,
+                  bool bulk_from_trace = false) {
+    ccake_ic* ic = nullptr;
+    check(ccake_ic_read_ccake(path, &opt, &ic), sys_.ctx(), "ccake_ic_read_ccake");
+    std::unique_ptr<ccake_ic, void (*)(ccake_ic*)> keep(ic, ccake_ic_free);
+    ccake_particles_soa soa{};
+    check(ccake_ic_particles(ic, &soa), sys_.ctx(), "ccake_ic_particles");
+    read_in_initial_conditions(soa);
+    const int64_t n = soa.n;
+    auto column = [&](const char* name, double* dst) {
+      check(ccake_ic_column(ic, name, dst), sys_.ctx(), "ccake_ic_column");
+    };
+    // (without the sector the reference keeps the currents but never evolves them)
+    if (opt.input_initial_diffusion && diffusion_) {
+      static const char* qn[12] = {"qB0", "qB1", "qB2", "qB3", "qS0", "qS1", "qS2", "qS3", "qQ0", "qQ1", "qQ2", "qQ3"};
+      std::vector<double> q((size_t)(12 * n));
+      for (int r = 0; r < 12; r++) column(qn[r], q.data() + (size_t)r * n);
+      ws_.set_diffusion(q.data());
+    }
+    if (initial_shear || bulk_from_trace) {
+      static const char* pn[6] = {"pixx", "pixy", "pixeta", "piyy", "piyeta", "pietaeta"};
+      std::vector<double> trace((size_t)n), pi((size_t)(6 * n));
+      column("bulk", trace.data());
+      for (int r = 0; r < 6; r++) column(pn[r], pi.data() + (size_t)r * n);
+      ws_.set_initial_viscous(bulk_from_trace ? trace.data() : nullptr, initial_shear ? pi.data() : nullptr);
+    }
   }
   void initialize_hydrodynamics() { ws_.initialize(); }
   // time loop of src/BSQHydro.cpp:745-814 (no output writers)
@@ -165,6 +208,7 @@ class BSQHydro {
   SystemState sys_;
   SPHWorkstation ws_;
   double dt_;
+  bool diffusion_;
 };
 
 }  // namespace gpu
