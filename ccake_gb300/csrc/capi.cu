@@ -65,6 +65,8 @@ struct ccake_ctx {
   // initial viscous input (ccake_set_initial_viscous): trace, pi^{xx xy xeta yy yeta}
   double* init_visc = nullptr;
   int init_bulk = 0, init_shear = 0;
+  // initial diffusion currents (ccake_set_initial_diffusion): q^i of charge c at row 3c + i
+  double* init_q = nullptr;
 };
 
 namespace {
@@ -119,7 +121,8 @@ void free_buffers(ccake_ctx* ctx) {
   if (ctx->p.recQ) cudaFree(ctx->p.recQ);
   ctx->p.dif = ctx->p.recQ = nullptr;
   if (ctx->init_visc) cudaFree(ctx->init_visc);
-  ctx->init_visc = nullptr;
+  if (ctx->init_q) cudaFree(ctx->init_q);
+  ctx->init_visc = ctx->init_q = nullptr;
   ctx->init_bulk = ctx->init_shear = 0;
   ctx->dbuf = nullptr;
   ctx->ibuf = nullptr;
@@ -653,12 +656,14 @@ ccake_status_t ccake_set_initial_diffusion(ccake_ctx* ctx, const double* q) {
   if (!ctx->p.dif) return fail(ctx, CCAKE_ERR_STATE, "the diffusion sector is off");
   if (ctx->initialized) return fail(ctx, CCAKE_ERR_STATE, "set the initial current before initialize");
   const int64_t n = ctx->n;
+  if (!ctx->init_q && cudaMalloc(&ctx->init_q, 9 * (size_t)n * sizeof(double)) != cudaSuccess)
+    return fail(ctx, CCAKE_ERR_NOMEM, "allocation");
   std::vector<double> tmp((size_t)n);
   for (int c = 0; c < 3; c++)
     for (int i = 0; i < 3; i++) {
       const double* src = q + (size_t)(4 * c + i + 1) * n;
       for (int64_t k = 0; k < n; k++) tmp[k] = src[ctx->perm[k]];
-      CK(cudaMemcpyAsync(ctx->p.dif + (size_t)(F_YQ0 + 3 * c + i) * n, tmp.data(), n * sizeof(double),
+      CK(cudaMemcpyAsync(ctx->init_q + (size_t)(3 * c + i) * n, tmp.data(), n * sizeof(double),
                          cudaMemcpyHostToDevice, ctx->stream));
       CK(cudaStreamSynchronize(ctx->stream));
     }
@@ -739,7 +744,7 @@ ccake_status_t ccake_initialize(ccake_ctx* ctx) {
     // :1350-1458), then the thermodynamics, pi, Pi and q^mu
     launch_passA(ctx->rc, ctx->eos, ctx->p, A_SMOOTH_ONLY, ctx->stream);
     launch_init_viscous(ctx->p, ctx->init_visc, ctx->init_bulk, ctx->init_shear, ctx->stream);
-    launch_init_diffusion(ctx->rc, ctx->p, ctx->stream);
+    launch_init_diffusion(ctx->p, ctx->init_q, ctx->stream);
     launch_thermo(ctx->rc, ctx->eos, ctx->p, ctx->stream);
     if (ctx->p.dif)
       CK(cudaMemcpyAsync(ctx->p.dif + (size_t)F_YQ0 * n, ctx->p.dif + (size_t)F_YQ * n, 9 * n * sizeof(double),

@@ -634,14 +634,14 @@ __global__ void k_init_viscous(Ptrs p, const double* iv, int bulk, int shear) {
 }
 
 // set_diffusion (src/sph_workstation.cpp:1441-1458): ext q = q^i / sigma;
-// the initial spatial currents q^i wait in the step-start slots until here
-__global__ void k_init_diffusion(Ptrs p) {
+// iq: the initial spatial currents q^i (3c + i), or null for none
+__global__ void k_init_diffusion(Ptrs p, const double* iq) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= p.n) return;
   const int n = p.n;
   const double sg = p.sig[i];
 #pragma unroll
-  for (int q = 0; q < 9; q++) p.dif[(size_t)(F_YQ + q) * n + i] = p.dif[(size_t)(F_YQ0 + q) * n + i] / sg;
+  for (int q = 0; q < 9; q++) p.dif[(size_t)(F_YQ + q) * n + i] = iq ? iq[(size_t)q * n + i] / sg : 0.0;
 }
 
 // FP64 smoothing record from the state (after mixed substeps moved the particles)
@@ -1317,9 +1317,8 @@ void launch_init_viscous(const Ptrs& p, const double* iv, int bulk, int shear, c
   if (iv && (bulk || shear)) k_init_viscous<<<(p.n + kBlock - 1) / kBlock, kBlock, 0, s>>>(p, iv, bulk, shear);
 }
 
-void launch_init_diffusion(const RunConst& rc, const Ptrs& p, cudaStream_t s) {
-  (void)rc;
-  if (p.dif) k_init_diffusion<<<(p.n + kBlock - 1) / kBlock, kBlock, 0, s>>>(p);
+void launch_init_diffusion(const Ptrs& p, const double* iq, cudaStream_t s) {
+  if (p.dif) k_init_diffusion<<<(p.n + kBlock - 1) / kBlock, kBlock, 0, s>>>(p, iq);
 }
 
 void launch_pack_fp64(const RunConst& rc, const Ptrs& p, cudaStream_t s) {

@@ -91,7 +91,7 @@ void launch_clock(const Ptrs& p, int substep, double dt, cudaStream_t s);
 void launch_init_state(const RunConst& rc, const Ptrs& p, cudaStream_t s);
 void launch_init_invert(const RunConst& rc, const EosDev& eos, const Ptrs& p, cudaStream_t s);
 void launch_init_ext(const RunConst& rc, const Ptrs& p, cudaStream_t s);
-void launch_init_diffusion(const RunConst& rc, const Ptrs& p, cudaStream_t s);
+void launch_init_diffusion(const Ptrs& p, const double* iq, cudaStream_t s);
 void launch_init_viscous(const Ptrs& p, const double* iv, int bulk, int shear, cudaStream_t s);
 void launch_totals(const RunConst& rc, const Ptrs& p, int nblocks, cudaStream_t s);
 void launch_neighbour_counts(const RunConst& rc, const Ptrs& p, int32_t* counts, cudaStream_t s);

@@ -1,6 +1,8 @@
 // Device per-particle physics of the hot path: transport coefficients, the
 // pi^{mu nu} constraints, and the MRF equations of motion (ideal + shear +
-// bulk, Milne coordinates) for one particle. FP64, templated on dimension.
+// bulk + diffusion, Milne and Cartesian coordinates) for one particle.
+// Templated on dimension and on the arithmetic type (FP64, or FP32 for the
+// mixed form, which has no diffusion sector).
 #pragma once
 #include <type_traits>
 
@@ -183,8 +185,7 @@ struct EomOut {
 };
 
 // Reference src/eom_default.cpp:211-869 (evaluate_time_derivatives) and
-// :882-1412 (calculate_MRF_shear), without sources and without the diffusion
-// sector, for one particle at time t.
+// :882-1412 (calculate_MRF_shear), without sources, for one particle at time t.
 // R = double is the plain FP64 form; R = float is the mixed form's EoM (the
 // state update it feeds stays FP64).
 // diag (optional, 7 values): theta, sigma^{11,12,13,22,23} and

@@ -248,7 +248,8 @@ ccake_status_t ccake_hydro_numbers(ccake_ctx* ctx);
  * (GeV units), rhoB, rhoS, rhoQ, s, eta_pi, zeta_Pi, tau_Pi, tau_pi, theta,
  * inverse Reynolds and Knudsen numbers (shear, bulk), pi^{00,11,22,01,02,12,
  * 13,23,33}, u (3), gamma, freeze status, EoS name, causality (0: not
- * checked), six diffusion numbers (0: no diffusion sector). */
+ * checked), the diffusion Knudsen numbers (B, S, Q) and inverse Reynolds
+ * numbers (B, S, Q) (0 without the diffusion sector). */
 ccake_status_t ccake_write_system_state(ccake_ctx* ctx, const char* path);
 
 /* Freeze-out hypersurface rows (cfg.particlization and cfg.surface), one

@@ -1,6 +1,7 @@
 // CPU oracle: transport coefficients, shear-tensor constraints, the MRF
-// equations of motion (ideal + shear + bulk, Milne coordinates), the midpoint
-// RK2 evolver, conservation sums and initialisation.
+// equations of motion (ideal + shear + bulk + diffusion, Milne and Cartesian
+// coordinates), the midpoint RK2 evolver, conservation sums, initialisation
+// and the freeze-out stage.
 // TEST INFRASTRUCTURE ONLY (see oracle.hpp).
 #include "oracle.hpp"
 #include "table_oracle.hpp"
@@ -736,10 +737,10 @@ int update_thermodynamics(System& s) {
   return failures;
 }
 
-// src/eom_default.cpp:211-869 (evaluate_time_derivatives) without sources and
-// without the diffusion sector (dN/dt is then zero); with coord = 1 its
-// Cartesian twin src/eom_cartesian.cpp:210-840 (no tau in the metric, no
-// connection terms).
+// src/eom_default.cpp:211-869 (evaluate_time_derivatives) without sources,
+// with the diffusion sector when it is on (dN/dt is zero otherwise); with
+// coord = 1 its Cartesian twin src/eom_cartesian.cpp:210-840 (no tau in the
+// metric, no connection terms).
 void evaluate_time_derivatives(System& s) {
   const int D = s.cfg.dim;
   const bool cart = s.cfg.coord == 1;
