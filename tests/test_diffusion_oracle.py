@@ -91,3 +91,45 @@ def test_diffusion_moves_charge_and_keeps_it():
     assert abs(t1["B"] - t0["B"]) < 0.1 * moved * p.n
     assert abs(t1["B"] - t0["B"]) < 1e-4 * abs(t0["B"])
     assert np.isfinite(o.get("u0")).all() and np.max(np.abs(o.get("qB1"))) > 0
+
+
+def test_diffusion_coefficients_follow_their_modes():
+    # constant_over_T2: kappa = kappa/T^2 T^2, tau_q = 0.2/T on the diagonal;
+    # kappaB_coth: kappa_B = (C_B/T) n_B ((1/3) coth(mu_B/T) - n_B T/w) where
+    # |mu_B/T| > 1e-2 and the value is positive, tau_q = C_B/T
+    # (src/transport_coefficients.cpp:918-1040)
+    p, rc = ics.hotspots_2d(n_side=20, n_hot=2, seed=13)
+    kap = (0.3, 0.01, 0.0, 0.01, 0.2, 0.0, 0.0, 0.0, 0.1)
+    o = O.OracleRun(p, dataclasses.replace(rc, using_diffusion=1, kappa_over_T2=kap))
+    assert o.initialize() == 0 and o.step(1) == 0
+    T = o.get("T")
+    for c, C in enumerate("BSQ"):
+        for d, Dd in enumerate("BSQ"):
+            assert np.allclose(o.get(f"kappa_q{C}{Dd}"), kap[3 * c + d] * T * T, rtol=1e-15, atol=0)
+            assert np.allclose(o.get(f"tau_q{C}{Dd}"), (0.2 / T) if c == d else 0.0, rtol=1e-15, atol=0)
+    # a baryon profile whose mu_B/T straddles the 1e-2 floor
+    p2 = dataclasses.replace(p, e=50.0 * p.e, rhoB=400.0 * p.rhoB * (0.5 + 0.5 * np.cos(6.0 * p.x)),
+                             rhoQ=np.zeros_like(p.rhoQ))
+    rc2 = dataclasses.replace(rc, eos_kind=0, thermo_mode=0, using_diffusion=1, diffusion_mode=2,
+                              diffusion_relax_mode=1, C_B=0.4)
+    o2 = O.OracleRun(p2, rc2)
+    assert o2.initialize() == 0 and o2.step(1) == 0
+    T, muB, nB, w = o2.get("T"), o2.get("muB"), o2.get("rhoB"), o2.get("w")
+    x = muB / T
+    kB = (0.4 / T) * nB * ((1.0 / 3.0) / np.tanh(x) - nB * T / w)
+    want = np.where((np.abs(x) > 1e-2) & (kB > 0), kB, 0.0)
+    assert np.any(want > 0) and np.any(want == 0)
+    assert np.allclose(o2.get("kappa_qBB"), want, rtol=1e-13, atol=0)
+    assert np.all(o2.get("kappa_qSS") == 0) and np.all(o2.get("kappa_qBQ") == 0)
+    assert np.allclose(o2.get("tau_qBB"), 0.4 / T, rtol=1e-15) and np.allclose(o2.get("tau_qQQ"), 0.4 / T, rtol=1e-15)
+
+
+def test_cartesian_diffusion_runs_and_keeps_charge():
+    p, rc = ics.hotspots_2d(n_side=24, n_hot=3, seed=11)
+    rc = dataclasses.replace(rc, coord=1, using_diffusion=1, kappa_over_T2=(0.3, 0, 0, 0, 0, 0, 0, 0, 0.3))
+    o = O.OracleRun(p, rc)
+    assert o.initialize() == 0
+    b0, t0 = o.get("ext_B"), o.totals()
+    assert o.step(10) == 0
+    assert np.max(np.abs(o.get("ext_B") - b0)) > 1e-6 * np.max(np.abs(b0))
+    assert abs(o.totals()["B"] - t0["B"]) < 1e-4 * abs(t0["B"])
