@@ -133,3 +133,27 @@ def test_cartesian_diffusion_runs_and_keeps_charge():
     assert o.step(10) == 0
     assert np.max(np.abs(o.get("ext_B") - b0)) > 1e-6 * np.max(np.abs(b0))
     assert abs(o.totals()["B"] - t0["B"]) < 1e-4 * abs(t0["B"])
+
+
+def test_critical_point_suppression_with_the_table_eos():
+    # default_kappa with critical_scaling: kappa = (1 - exp(-[(T - T_c)^2 /
+    # (2 w_T^2) + (mu_B - mu_Bc)^2 / (2 w_mu^2)])) kappa/T^2 T^2 where the
+    # particle's EoS is the table (src/transport_coefficients.cpp:942-948,
+    # :1048-1057); inputs in MeV, converted to fm^-1
+    from ccake_gb300 import eos_table
+    n, lo, d, f = eos_table.synthetic_table(nT=76, nmu=21)
+    ot = O.OracleTable(n, lo, d, f, *eos_table.fallback_scales())
+    p, rc = ics.hotspots_2d(n_side=16, n_hot=3, seed=11, floor_GeV=4.0, peak_range=(5.0, 30.0))
+    rc = dataclasses.replace(rc, eos_kind=2, using_diffusion=1, kappa_over_T2=(0.3, 0, 0, 0, 0, 0, 0, 0, 0.3),
+                             critical_scaling_diffusion=1, crit_T=300.0, crit_muB=100.0, crit_wT=60.0,
+                             crit_wmuB=200.0)
+    o = O.OracleRun(p, rc, table=ot)
+    assert o.initialize() == 0 and o.step(1) == 0
+    hc = 197.3269804
+    T, muB = o.get("T"), o.get("muB")
+    ex = 0.5 * ((T - 300.0 / hc) ** 2 / (60.0 / hc) ** 2 + (muB - 100.0 / hc) ** 2 / (200.0 / hc) ** 2)
+    table = o.get_int("eos_id") == 0
+    sup = np.where(table, 1.0 - np.exp(-ex), 1.0)
+    assert table.any()
+    assert np.allclose(o.get("kappa_qBB"), sup * 0.3 * T * T, rtol=1e-12, atol=0)
+    assert np.min(sup[table]) < 0.999
