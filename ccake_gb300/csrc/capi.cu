@@ -445,7 +445,8 @@ int64_t estimate_bytes(const ccake_config& cfg, int64_t n) {
   // state and records, plus neighbour and candidate lists at the lattice
   // densities of the bundled workloads (48 / 447 neighbours in 2-D / 3-D)
   const int64_t K = cfg.dim == 3 ? 688 : 96, Kc = cfg.dim == 3 ? 912 : 112;
-  return n * (kDoublesPerParticle * 8 + 8 * 4 + K * 12 + Kc * 4) + (int64_t)(1 << 20);
+  const int64_t dif = cfg.using_diffusion ? (int64_t)(NDIF + RQ) * 8 : 0;   // diffusion slabs and record
+  return n * (kDoublesPerParticle * 8 + 8 * 4 + K * 12 + Kc * 4 + dif) + (int64_t)(1 << 20);
 }
 
 }  // namespace ccake_internal
@@ -859,6 +860,9 @@ ccake_status_t ccake_device_bytes(const ccake_ctx* ctx, int64_t* bytes) {
   const int64_t nd = n * kDoublesPerParticle;
   const int64_t ni = n * 8 + (int64_t)ctx->rc.grid.ncell * 2 + 2 * (int64_t)scan_tiles(ctx->rc.grid.ncell);
   *bytes = nd * 8 + ni * 4 + (int64_t)ctx->p.K * n * 12 + (int64_t)ctx->p.Kc * n * 4;
+  if (ctx->p.dif) *bytes += (int64_t)(NDIF + RQ) * n * 8;
+  if (ctx->init_q) *bytes += 9 * n * 8;
+  if (ctx->init_visc) *bytes += 6 * n * 8;
   return CCAKE_OK;
 }
 
