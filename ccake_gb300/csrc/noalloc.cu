@@ -12,7 +12,11 @@
 // Contract:
 //  * The first call on each device looks up the device address of the scratch
 //    array with cudaGetSymbolAddress (with that device current) and caches it;
-//    make that first call before any stream capture.
+//    make that first call before any stream capture. The cache assumes that
+//    the device's primary context lives as long as the process: after a
+//    cudaDeviceReset the module is loaded again and the cached address is
+//    stale, so a caller that resets a device must not call this entry point
+//    on it afterwards.
 //  * All calls share the one scratch array and it keeps the last call's
 //    contents; every call clears the cell counters it uses before binning.
 //    Calls that overlap on the GPU (different streams, or different host
@@ -145,7 +149,11 @@ extern "C" ccake_status_t ccake_neighbour_counts_noalloc(const double* d_x, cons
   if (dim != 2 && dim != 3) return CCAKE_ERR_INVALID;
   if (dim == 3 && !d_eta) return CCAKE_ERR_INVALID;
   if (n > kMaxParticles) return CCAKE_ERR_CAPACITY;
-  // cell grid over the caller's box, cell edge >= 2h, indices clamped
+  // cell grid over the caller's box, indices clamped. The cell edge is kept
+  // strictly above 2h (by a relative margin of 1e-9): with an edge of exactly
+  // 2h, floor((x - lo) * inv_cs) of two particles exactly 2h apart -- four
+  // such pairs around every lattice particle -- can round into cells two
+  // apart, and the pair would be missed.
   Grid g{};
   const double cut = 2.0 * h;
   int64_t ncell = 1;
@@ -153,7 +161,7 @@ extern "C" ccake_status_t ccake_neighbour_counts_noalloc(const double* d_x, cons
     if (k >= dim) { g.lo[k] = 0.0; g.nc[k] = 1; g.inv_cs[k] = 1.0; continue; }
     if (!(hi3[k] > lo3[k])) return CCAKE_ERR_INVALID;
     const double span = hi3[k] - lo3[k];
-    const double ncd = std::floor(span / cut);
+    const double ncd = std::floor(span / (cut * (1.0 + 1e-9)));
     if (!(ncd <= (double)kMaxCells)) return CCAKE_ERR_CAPACITY;
     const int nc = ncd < 1.0 ? 1 : (int)ncd;
     g.lo[k] = lo3[k];

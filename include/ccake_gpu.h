@@ -449,9 +449,11 @@ ccake_status_t ccake_mlp_gradient(ccake_ctx* ctx, int64_t n, const float* feat, 
  * rejected with CCAKE_ERR_CAPACITY. lo3/hi3 (host, 3 doubles) bound the cell
  * grid (particles outside are clamped to edge cells; the counts do not depend
  * on the box). The first call on a device looks up the scratch address; make
- * it before any stream capture. Calls share the scratch: calls that overlap
- * on the GPU race and must be serialised by the caller. Returns once the
- * kernels are enqueued. */
+ * it before any stream capture. That address is cached for the life of the
+ * process, which assumes the device's primary context lives as long: do not
+ * call this entry point on a device after cudaDeviceReset. Calls share the
+ * scratch: calls that overlap on the GPU race and must be serialised by the
+ * caller. Returns once the kernels are enqueued. */
 ccake_status_t ccake_neighbour_counts_noalloc(const double* d_x, const double* d_y, const double* d_eta, int64_t n,
                                               int32_t dim, double h, const double* lo3, const double* hi3,
                                               int32_t* d_counts, void* stream);

@@ -7,7 +7,7 @@ Reads the reference sources as text (nothing is compiled or executed):
   unit_tests/evolver_test.cpp         RK2 with a no-op derivative functional
   unit_tests/eos_interpolator_test.cpp exact multilinear interpolation
 
-Usage: python tests/golden/make_golden.py [/path/to/reference]
+Usage: python tests/golden/make_golden.py <path to a CCAKE checkout>
 The committed JSON files are what the tests read; the reference is not needed
 at test time.
 """
@@ -17,7 +17,6 @@ import os
 import re
 import sys
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
 OUT = os.path.dirname(os.path.abspath(__file__))
 
 
@@ -84,4 +83,7 @@ def main():
 
 
 if __name__ == "__main__":
+    if len(sys.argv) != 2:
+        sys.exit(__doc__)
+    REF = sys.argv[1]
     main()

@@ -24,14 +24,25 @@ def _bind(L):
     return f
 
 
-def test_noalloc_neighbour_counts_match_allocating_entry_point():
+@pytest.mark.parametrize("dim", [2, 3])
+def test_noalloc_neighbour_counts_match_allocating_entry_point(dim):
     import torch
     from ccake_gb300 import api, build, ics
 
     build.build()
     L = api.lib()
     f = _bind(L)
-    p, rc = ics.hotspots_2d(n_side=120, n_hot=8, seed=3)
+    if dim == 2:
+        # lattice spacing 2h/4: four partners of every interior particle sit
+        # exactly 2h away, the case the cell edge's margin is for
+        p, rc = ics.hotspots_2d(n_side=120, n_hot=8, seed=3)
+        lo = (ctypes.c_double * 3)(2 * rc.xmin, 2 * rc.ymin, -rc.hT)
+        hi = (ctypes.c_double * 3)(-2 * rc.xmin, -2 * rc.ymin, rc.hT)
+    else:
+        # (x, y, eta_s) lattice: cells over all three axes, ~280 neighbours
+        p, rc = ics.hotspots_3d(n_xy=20, n_eta=16, n_hot=4, seed=3)
+        lo = (ctypes.c_double * 3)(rc.xmin, rc.ymin, rc.etamin)
+        hi = (ctypes.c_double * 3)(-rc.xmin, -rc.ymin, -rc.etamin)
     n = p.n
     # the allocating entry point: CSR offsets of the full neighbour list
     g = api.GpuHydro(rc)
@@ -43,13 +54,13 @@ def test_noalloc_neighbour_counts_match_allocating_entry_point():
     dev = torch.device("cuda:0")
     dx = torch.tensor(p.x, dtype=torch.float64, device=dev)
     dy = torch.tensor(p.y, dtype=torch.float64, device=dev)
+    de = torch.tensor(p.eta, dtype=torch.float64, device=dev)
     out = torch.empty(n, dtype=torch.int32, device=dev)
-    lo = (ctypes.c_double * 3)(2 * rc.xmin, 2 * rc.ymin, -rc.hT)
-    hi = (ctypes.c_double * 3)(-2 * rc.xmin, -2 * rc.ymin, rc.hT)
     stream = torch.cuda.current_stream().cuda_stream
     for _ in range(2):
         out.fill_(-1)
-        st = f(dx.data_ptr(), dy.data_ptr(), None, n, 2, rc.hT, lo, hi, out.data_ptr(), stream)
+        st = f(dx.data_ptr(), dy.data_ptr(), de.data_ptr() if dim == 3 else None, n, dim, rc.hT, lo, hi,
+               out.data_ptr(), stream)
         assert st == 0, L.ccake_status_string(st)
         torch.cuda.synchronize()
         assert np.array_equal(out.cpu().numpy(), expect)
