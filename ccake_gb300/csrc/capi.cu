@@ -480,6 +480,12 @@ ccake_status_t ccake_ctx_create(const ccake_config* cfg, ccake_ctx** out) {
   if (!(cfg->skin_frac >= 0.0)) return CCAKE_ERR_INVALID;
   if (!(cfg->hT > 0) || !(cfg->t0 > 0) || !(cfg->dt > 0)) return CCAKE_ERR_INVALID;
   if (cfg->dim == 3 && cfg->factorized_kernel) return CCAKE_ERR_INVALID;
+  // second-order coefficient modes: DEFAULT or DISABLED, and IS for the two deltas
+  for (int32_t m : {cfg->tau_pipi_mode, cfg->lambda_piPi_mode, cfg->phi6_mode, cfg->phi7_mode, cfg->lambda_Pipi_mode,
+                    cfg->phi1_mode, cfg->phi3_mode})
+    if (m != CCAKE_COEF_DEFAULT && m != CCAKE_COEF_DISABLED) return CCAKE_ERR_INVALID;
+  for (int32_t m : {cfg->delta_pipi_mode, cfg->delta_PiPi_mode})
+    if (m < CCAKE_COEF_DEFAULT || m > CCAKE_COEF_DISABLED) return CCAKE_ERR_INVALID;
   // the diffusion sector runs in the FP64 form with the constant_over_T2 or
   // kappaB_coth coefficients
   if (cfg->using_diffusion && (cfg->precision != 0 || (cfg->diffusion_mode != 0 && cfg->diffusion_mode != 2)))

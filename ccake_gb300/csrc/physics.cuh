@@ -64,15 +64,20 @@ __device__ inline TransportT<R> transport(const ccake_config& c, const double* t
   const R cc = cs2 > R(1) ? R(1) : cs2;
   const R pw = powi_or_pow<R>(k13 - cc, zp);
   k.tau_Pi = (pw < R(1e-10)) ? R(1e10) : fmax(R(5) * k.zeta / (pw * w), R(0.1));
-  k.delta_PiPi = R(2) * k.tau_Pi / R(3);
-  k.delta_pipi = R(4) * k.tau_pi / R(3);
-  k.lambda_piPi = R(6) / R(5) * k.tau_pi;
-  k.lambda_Pipi = R(8) * (k13 - cc) * k.tau_Pi / R(5);
+  // second-order coefficients by mode (src/transport_coefficients.cpp:
+  // 380-560 switches, :704-912 the functions): 0 the *_DEFAULT function,
+  // 1 israel-stewart (the two deltas), 2 disabled. phi1, phi3 and phi6 are 0
+  // in every mode.
+  auto pick = [](int32_t mode, R def, R is) { return mode == 2 ? R(0) : (mode == 1 ? is : def); };
+  k.delta_PiPi = pick(c.delta_PiPi_mode, R(2) * k.tau_Pi / R(3), k.tau_Pi);
+  k.delta_pipi = pick(c.delta_pipi_mode, R(4) * k.tau_pi / R(3), k.tau_pi);
+  k.lambda_piPi = pick(c.lambda_piPi_mode, R(6) / R(5) * k.tau_pi, R(0));
+  k.lambda_Pipi = pick(c.lambda_Pipi_mode, R(8) * (k13 - cc) * k.tau_Pi / R(5), R(0));
   k.phi1 = R(0);
   k.phi3 = R(0);
   k.phi6 = R(0);
-  k.phi7 = R(9) / (R(70) * p);
-  k.tau_pipi = R(10) * k.tau_pi / R(7);
+  k.phi7 = pick(c.phi7_mode, R(9) / (R(70) * p), R(0));
+  k.tau_pipi = pick(c.tau_pipi_mode, R(10) * k.tau_pi / R(7), R(0));
   return k;
 }
 

@@ -79,6 +79,17 @@ class RunConfig:
     crit_muB: float = 350.0        # MeV
     crit_wT: float = 30.0          # MeV
     crit_wmuB: float = 50.0        # MeV
+    # second-order transport coefficients: 0 the reference's *_DEFAULT
+    # function, 1 "israel-stewart" (delta_pipi, delta_PiPi only), 2 disabled
+    delta_pipi_mode: int = 0
+    tau_pipi_mode: int = 0
+    lambda_piPi_mode: int = 0
+    phi6_mode: int = 0
+    phi7_mode: int = 0
+    delta_PiPi_mode: int = 0
+    lambda_Pipi_mode: int = 0
+    phi1_mode: int = 0
+    phi3_mode: int = 0
 
 
 @dataclasses.dataclass
@@ -151,14 +162,106 @@ def gubser_2d(n_side=200, dx=0.05, h=0.1, tau0=1.0, dt=0.001, c_e=15.6269, q=1.0
     return p, cfg
 
 
+class GubserIS:
+    """Semi-analytic Gubser flow of Israel-Stewart theory with constant
+    eta/s (Marrochio, Noronha, Denicol, Luzum, Jeon, Gale,
+    PhysRevC.91.014903; the reference tabulates it with
+    misc/Gubser_checks/ac/Gubser_semi-analytical_tabulator.wls).
+
+    In de Sitter time rho = -asinh((1 - tau^2 + r^2) / (2 tau)) the flow
+    reduces to two ODEs for That(rho) and the normalised shear pibar(rho):
+        That'/That + (2/3) tanh rho = (1/3) pibar tanh rho
+        c (eta/s)/That (pibar' + (4/3) pibar^2 tanh rho) + pibar
+            = (4/3) (eta/s)/That tanh rho
+    with That(0) = 1.2, pibar(0) = 0 and tau_pi = c eta/(e + p), c = 5. They
+    are integrated here in both directions from rho = 0 (scipy DOP853, rtol
+    1e-12) and mapped back:
+        T = That(rho)/tau,  u^r = sinh(atanh(2 tau r / (1 + tau^2 + r^2))),
+        pihat = (4/3) alpha That^4 pibar,  alpha = 3 c_ref (e = alpha T^4),
+        pi^{ij} = -(1/2) tau^-4 (delta^{ij} + x^i x^j / r^2 (u^r)^2) pihat,
+        tau^2 pi^{eta eta} = pihat / tau^4.
+    Units are the library's: fm^-1 for T, fm^-4 for pi.
+    """
+
+    def __init__(self, eta_over_s=0.2, c_tau=5.0, That0=1.2, rho_range=(-8.0, 4.0)):
+        from scipy.integrate import solve_ivp
+        self.eta_over_s, self.c_tau = eta_over_s, c_tau
+        self.alpha = 3.0 * C_REFERENCE
+
+        def rhs(r, y):
+            T, pb = y
+            th = math.tanh(r)
+            return [T * (pb * th / 3.0 - 2.0 * th / 3.0),
+                    (4.0 / 3.0 * eta_over_s / T * th - pb) * T / (c_tau * eta_over_s) - 4.0 / 3.0 * pb * pb * th]
+
+        kw = dict(method="DOP853", rtol=1e-12, atol=1e-14, dense_output=True)
+        self._neg = solve_ivp(rhs, (0.0, rho_range[0]), [That0, 0.0], **kw).sol
+        self._pos = solve_ivp(rhs, (0.0, rho_range[1]), [That0, 0.0], **kw).sol
+
+    def hat(self, rho):
+        rho = np.asarray(rho, dtype=np.float64)
+        out = np.empty((2,) + rho.shape)
+        m = rho < 0
+        out[:, m] = self._neg(rho[m])
+        out[:, ~m] = self._pos(rho[~m])
+        return out
+
+    def fields(self, tau, x, y):
+        """T, u^x, u^y, pi^xx, pi^yy, pi^xy, tau^2 pi^{eta eta} at (tau, x, y)."""
+        x = np.asarray(x, dtype=np.float64)
+        y = np.asarray(y, dtype=np.float64)
+        r = np.sqrt(x * x + y * y)
+        rho = -np.arcsinh((1.0 - tau * tau + r * r) / (2.0 * tau))
+        Th, pb = self.hat(rho)
+        ur = np.sinh(np.arctanh(2.0 * tau * r / (1.0 + tau * tau + r * r)))
+        rs = np.where(r > 0, r, 1.0)
+        cx, cy = np.where(r > 0, x / rs, 0.0), np.where(r > 0, y / rs, 0.0)
+        pih = 4.0 / 3.0 * self.alpha * Th ** 4 * pb
+        f = -0.5 / tau ** 4 * pih
+        return dict(T=Th / tau, ux=cx * ur, uy=cy * ur, pixx=f * (1.0 + cx * cx * ur * ur),
+                    piyy=f * (1.0 + cy * cy * ur * ur), pixy=f * cx * cy * ur * ur, t2pietaeta=pih / tau ** 4)
+
+
+def gubser_viscous_2d(n_side=281, dx=0.05, h=0.1, tau0=1.0, dt=0.001, eta_over_s=0.2, solution=None):
+    """Viscous Gubser flow (Israel-Stewart, eta/s = 0.2, tau_pi = 5 eta/w) on
+    an n_side^2 lattice centred on the origin, at tau0 = 1 fm/c: T, u^i and
+    pi^{ij} of the semi-analytic solution (``GubserIS``), conformal EoS
+    e = 3p = 3 c_ref T^4 (the reference's constant). Returns (particles,
+    config, pi[6, n] in the order xx xy xeta yy yeta etaeta for
+    ``set_initial_viscous``)."""
+    sol = solution or GubserIS(eta_over_s=eta_over_s)
+    xmin = -0.5 * (n_side - 1) * dx
+    x, y = lattice_2d(n_side, n_side, dx, xmin, xmin)
+    f = sol.fields(tau0, x, y)
+    e = 3.0 * C_REFERENCE * f["T"] ** 4
+    z = np.zeros_like(x)
+    p = Particles(x, y, z.copy(), e, z.copy(), z.copy(), z.copy(), f["ux"], f["uy"], z.copy())
+    pi = np.zeros((6, x.shape[0]))
+    pi[0], pi[1], pi[3] = f["pixx"], f["pixy"], f["piyy"]
+    pi[5] = f["t2pietaeta"] / tau0 ** 2
+    # the reference's viscous Gubser settings (input/config_visc_gubser.yaml):
+    # delta_pipi "default" (4/3 tau_pi), tau_pipi, lambda_piPi, phi6 and phi7
+    # "disabled" -- the Israel-Stewart equations the solution solves
+    cfg = RunConfig(dim=2, eos_kind=0, using_shear=1, shear_relax_mode=1, eta_over_s=eta_over_s,
+                    zeta_mode=1, zeta_over_s=0.0, hT=h, t0=tau0, dt=dt, eos_c=C_REFERENCE,
+                    xmin=xmin, ymin=xmin, etamin=-0.1, delta_pipi_mode=0, tau_pipi_mode=2,
+                    lambda_piPi_mode=2, phi6_mode=2, phi7_mode=2)
+    return p, cfg, pi
+
+
 def hotspots_2d(n_side=400, dx=0.05, h=0.1, n_hot=30, sigma=0.4, seed=20251203, tau0=1.0,
-                dt=0.001, eta_over_s=0.08, floor_GeV=0.01, peak_range=(5.0, 50.0)):
+                dt=0.001, eta_over_s=0.08, floor_GeV=0.01, peak_range=(5.0, 50.0), rhoS_frac=0.0):
     """Config 2: 30 Gaussian hot spots (sigma 0.4 fm), centres ~ N(0, 3 fm),
     peaks ~ U[5, 50] GeV/fm^3, plus a uniform floor of ``floor_GeV`` GeV/fm^3
     so that every lattice particle carries matter. rhoB = e[GeV/fm^3]/20 fm^-3,
     rhoS = 0, rhoQ = 0.4 rhoB. Conformal-diagonal EoS with the reference
     constants, eta/s = 0.08 with tau_pi = 5 eta/w ("Gubser"), zeta = 0, u = 0.
     Generator: numpy PCG64 with the given seed.
+
+    ``rhoS_frac`` != 0 gives the event strangeness, rhoS = rhoS_frac * rhoB
+    * cos(x / 1 fm): a density that changes sign across the event, so that
+    all four densities (and a strangeness chemical potential of either sign)
+    are exercised.
 
     The enthalpy derivatives use the exact inverse of the susceptibility
     matrix (``thermo_mode=1``): with two non-zero charges the reference's
@@ -177,8 +280,9 @@ def hotspots_2d(n_side=400, dx=0.05, h=0.1, n_hot=30, sigma=0.4, seed=20251203, 
         eG += amp[k] * np.exp(-((x - cx[k]) ** 2 + (y - cy[k]) ** 2) / (2.0 * sigma * sigma))
     rhoB = eG / 20.0
     rhoQ = 0.4 * rhoB
+    rhoS = rhoS_frac * rhoB * np.cos(x)
     z = np.zeros_like(x)
-    p = Particles(x, y, z.copy(), eG / HBARC_GEVFM, rhoB, z.copy(), rhoQ, z.copy(), z.copy(), z.copy())
+    p = Particles(x, y, z.copy(), eG / HBARC_GEVFM, rhoB, rhoS, rhoQ, z.copy(), z.copy(), z.copy())
     cfg = RunConfig(dim=2, eos_kind=1, using_shear=1 if eta_over_s > 1e-10 else 0,
                     shear_relax_mode=1, thermo_mode=1, zeta_mode=1, zeta_over_s=0.0, eta_over_s=eta_over_s,
                     hT=h, t0=tau0, dt=dt, xmin=xmin, ymin=xmin, etamin=-0.1)

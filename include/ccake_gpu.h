@@ -76,7 +76,22 @@ typedef struct ccake_config {
   double C_B;
   double reg_chi0, reg_e0, reg_xi0, reg_rq_max;   /* regulator; e0, xi0 in GeV/fm^3 */
   double crit_T, crit_muB, crit_wT, crit_wmuB;    /* critical point and widths, MeV */
+  /* second-order transport coefficients, the reference's *_mode settings
+   * (include/settings.h:172-190, src/transport_coefficients.cpp:117-278 and
+   * :704-912): CCAKE_COEF_DEFAULT takes the reference's *_DEFAULT function
+   * (delta_pipi 4/3 tau_pi, tau_pipi 10/7 tau_pi, lambda_piPi 6/5 tau_pi,
+   * phi6 0, phi7 9/(70 p), delta_PiPi 2/3 tau_Pi, lambda_Pipi
+   * 8/5 (1/3 - cs2) tau_Pi, phi1 0, phi3 0); CCAKE_COEF_IS ("israel-stewart",
+   * delta_pipi and delta_PiPi only) takes tau_pi / tau_Pi; CCAKE_COEF_DISABLED
+   * takes 0. A zeroed config is all DEFAULT; the reference's own setting
+   * defaults (include/defaults.h:48-52) are IS for delta_pipi and DISABLED for
+   * tau_pipi, lambda_piPi, phi6 and phi7. */
+  int32_t delta_pipi_mode, tau_pipi_mode, lambda_piPi_mode, phi6_mode, phi7_mode;
+  int32_t delta_PiPi_mode, lambda_Pipi_mode, phi1_mode, phi3_mode;
+  int32_t pad3;
 } ccake_config;
+
+enum { CCAKE_COEF_DEFAULT = 0, CCAKE_COEF_IS = 1, CCAKE_COEF_DISABLED = 2 };
 
 /* Host struct-of-arrays particle input, the columns of the reference's
  * "ccake" IC format (src/BSQHydro.cpp:206-330) already in internal units.

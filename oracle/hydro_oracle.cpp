@@ -81,16 +81,19 @@ Coefs coefs(const Config& c, const double* th) {
   k.tau_pi = tau_pi_of(c, k.eta, w);
   k.zeta = zeta_of(c, T, w, cs2);
   k.tau_Pi = tau_Pi_of(c, k.zeta, w, cs2);
-  k.delta_PiPi = 2. * k.tau_Pi / 3.0;
-  k.delta_pipi = 4. * k.tau_pi / 3.0;
-  k.lambda_piPi = 6. / 5. * k.tau_pi;
+  // second-order coefficients by mode (src/transport_coefficients.cpp:
+  // 380-560 switches, :704-912 the functions): 0 DEFAULT, 1 IS, 2 disabled
+  auto pick = [](int32_t mode, double def, double is) { return mode == 2 ? 0.0 : (mode == 1 ? is : def); };
+  k.delta_PiPi = pick(c.delta_PiPi_mode, 2. * k.tau_Pi / 3.0, k.tau_Pi);
+  k.delta_pipi = pick(c.delta_pipi_mode, 4. * k.tau_pi / 3.0, k.tau_pi);
+  k.lambda_piPi = pick(c.lambda_piPi_mode, 6. / 5. * k.tau_pi, 0.0);
   const double cc = cs2 > 1 ? 1 : cs2;
-  k.lambda_Pipi = 8. * (1. / 3. - cc) * k.tau_Pi / 5.;
+  k.lambda_Pipi = pick(c.lambda_Pipi_mode, 8. * (1. / 3. - cc) * k.tau_Pi / 5., 0.0);
   k.phi1 = 0.0;
   k.phi3 = 0.0;
   k.phi6 = 0.0;
-  k.phi7 = 9. / (70. * p);
-  k.tau_pipi = 10. * k.tau_pi / 7.0;
+  k.phi7 = pick(c.phi7_mode, 9. / (70. * p), 0.0);
+  k.tau_pipi = pick(c.tau_pipi_mode, 10. * k.tau_pi / 7.0, 0.0);
   return k;
 }
 

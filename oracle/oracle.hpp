@@ -63,6 +63,11 @@ struct Config {
   double C_B;
   double reg_chi0, reg_e0, reg_xi0, reg_rq_max;   // regulator; e0, xi0 in GeV/fm^3
   double crit_T, crit_muB, crit_wT, crit_wmuB;    // critical point and widths, MeV
+  // second-order coefficients (src/transport_coefficients.cpp:117-278):
+  // 0 the *_DEFAULT function, 1 israel-stewart (the two deltas), 2 disabled
+  int32_t delta_pipi_mode, tau_pipi_mode, lambda_piPi_mode, phi6_mode, phi7_mode;
+  int32_t delta_PiPi_mode, lambda_Pipi_mode, phi1_mode, phi3_mode;
+  int32_t pad3;
 };
 
 // Freeze-out snapshot of one step (FreezeOut::freeze_array,

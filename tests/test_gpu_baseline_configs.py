@@ -1,0 +1,200 @@
+"""FP64 GPU path against the CPU oracle at the full sizes of the benchmark
+workloads, through the C ABI.
+
+* Ideal Gubser flow, 200 x 200 lattice (40,000 particles), the reference's
+  conformal constant, 100 RK2 steps.
+* The viscous BSQ hot-spot event, 400 x 400 lattice (160,000 particles),
+  200 RK2 steps; and the same event with strangeness (rhoS != 0), so that
+  all four densities are judged.
+
+Bars: neighbour sets bit-exact at step 0 and at the last step (the oracle is
+given the GPU's positions there, so the two searches see the same inputs);
+every field within 1e-10 in plain relative error wherever |oracle| is at
+least 1e-3 of the field's largest magnitude, and within 1e-10 of that largest
+magnitude elsewhere (fields that cross zero: velocities, shear components);
+S, B, S, Q and E + Ez totals within 1e-10 relative of the oracle's. The mixed
+form (FP32 Kahan sums) is held to 1e-5 in e and the densities after 100
+steps against the oracle.
+
+The oracle's 160k-particle runs take about 30 s on 16 host cores; they are
+shared between tests through module-scoped fixtures.
+"""
+import dataclasses
+
+import numpy as np
+import pytest
+
+from ccake_gb300 import api, ics
+import oracle_py as O
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-10
+MIXED_TOL = 1e-5
+SMALL = 1e-3   # |oracle| below SMALL * max|oracle| counts as "near zero"
+
+
+def field_errors(a, b):
+    """(max plain relative error over |b| >= SMALL*max|b|,
+        max |a - b| / max|b| over the rest)."""
+    scale = float(np.max(np.abs(b)))
+    if scale == 0.0:
+        return 0.0, float(np.max(np.abs(a)))
+    big = np.abs(b) >= SMALL * scale
+    rel = float(np.max(np.abs(a[big] - b[big]) / np.abs(b[big]))) if big.any() else 0.0
+    absn = float(np.max(np.abs(a[~big] - b[~big])) / scale) if (~big).any() else 0.0
+    return rel, absn
+
+
+def assert_fields(gpu, orc, fields, tol):
+    bad = {}
+    for f in fields:
+        rel, absn = field_errors(gpu.get(f), orc.get(f))
+        if not (rel < tol and absn < tol):
+            bad[f] = (rel, absn)
+    assert not bad, bad
+
+
+def csr_rows(off, idx):
+    return [tuple(sorted(idx[off[i]:off[i + 1]])) for i in range(len(off) - 1)]
+
+
+def assert_same_neighbours(gpu, orc):
+    orc.set("x", gpu.get("x"))
+    orc.set("y", gpu.get("y"))
+    go, gi = gpu.neighbours()
+    oo, oi = orc.neighbours()
+    assert np.array_equal(go, oo)
+    assert csr_rows(go, gi) == csr_rows(oo, oi)
+
+
+def assert_totals(gpu, orc, keys=("S", "B", "Sq", "Q", "E", "Ez")):
+    tg, to = gpu.totals(), orc.totals()
+    for k in keys:
+        assert abs(tg[k] - to[k]) <= RTOL * (abs(to[k]) + 1e-300), (k, tg[k], to[k])
+
+
+VISCOUS_FIELDS = ["x", "y", "u0", "u1", "ext_s", "ext_B", "ext_S", "ext_Q", "ext_shv0", "ext_shv1", "ext_shv3",
+                  "T", "muB", "muS", "muQ", "e", "p", "s", "rhoB", "rhoS", "rhoQ", "sigma_lab", "shv00", "shv11",
+                  "shv12", "shv33", "Ez"]
+
+
+def test_gubser_200x200_100_steps_reference_constant():
+    # BASELINE config 1 with the reference's own conformal constant
+    # (p = c T^4, c = pi^2 (2*8 + 3.5*3*2.5)/90, src/eos_initialization.cpp:226-229)
+    p, rc = ics.gubser_2d(n_side=200, c_e=3.0 * ics.C_REFERENCE)
+    gpu = api.GpuHydro(rc)
+    gpu.load(p)
+    orc = O.OracleRun(p, rc)
+    assert_same_neighbours(gpu, orc)
+    gpu.initialize()
+    assert orc.initialize() == 0
+    gpu.step(100)
+    assert orc.step(100) == 0
+    assert abs(gpu.t - orc.t) < 1e-13 and abs(gpu.t - 1.1) < 1e-12
+    assert_fields(gpu, orc, ["x", "y", "u0", "u1", "ext_s", "T", "e", "p", "s", "sigma_lab", "sigma", "gamma", "Ez"],
+                  RTOL)
+    assert_totals(gpu, orc, ("S", "E", "Ez"))
+    # ideal flow conserves the total entropy exactly in both
+    t0 = api.GpuHydro(rc)
+    t0.load(p)
+    t0.initialize()
+    assert abs(gpu.totals()["S"] / t0.totals()["S"] - 1.0) < 1e-12
+    assert_same_neighbours(gpu, orc)
+
+
+@pytest.fixture(scope="module")
+def c2_runs():
+    """The 160k hot-spot event after 100 and after 200 steps: FP64 GPU,
+    mixed GPU (100 steps) and the oracle."""
+    p, rc = ics.hotspots_2d(n_side=400)
+    orc = O.OracleRun(p, rc)
+    gpu = api.GpuHydro(rc)
+    gpu.load(p)
+    nb0 = (gpu.neighbours(), orc.neighbours())
+    gpu.initialize()
+    assert orc.initialize() == 0
+    mixed = api.GpuHydro(dataclasses.replace(rc, precision=1))
+    mixed.load(p)
+    mixed.initialize()
+    mixed.step(100)
+    gpu.step(100)
+    assert orc.step(100) == 0
+    snap100 = {f: (gpu.get(f), orc.get(f), mixed.get(f)) for f in VISCOUS_FIELDS}
+    tot100 = (gpu.totals(), orc.totals(), mixed.totals())
+    gpu.step(100)
+    assert orc.step(100) == 0
+    return dict(p=p, rc=rc, gpu=gpu, orc=orc, nb0=nb0, snap100=snap100, tot100=tot100)
+
+
+def test_hotspots_160k_neighbours_bit_exact_at_start_and_end(c2_runs):
+    (go, gi), (oo, oi) = c2_runs["nb0"]
+    assert np.array_equal(go, oo)
+    assert csr_rows(go, gi) == csr_rows(oo, oi)
+    # interior lattice particles: 44 within 2h plus the exactly-2h pairs
+    assert 44 <= np.median(np.diff(go)) <= 48
+    assert_same_neighbours(c2_runs["gpu"], c2_runs["orc"])
+
+
+def test_hotspots_160k_fields_after_100_and_200_steps(c2_runs):
+    bad = {}
+    for f, (g, o, _) in c2_runs["snap100"].items():
+        rel, absn = field_errors(g, o)
+        if not (rel < RTOL and absn < RTOL):
+            bad[f] = (rel, absn)
+    assert not bad, bad
+    gpu, orc = c2_runs["gpu"], c2_runs["orc"]
+    assert abs(gpu.t - orc.t) < 1e-13 and abs(gpu.t - 1.2) < 1e-12
+    assert_fields(gpu, orc, VISCOUS_FIELDS, RTOL)
+
+
+def test_hotspots_160k_conservation_matches_oracle(c2_runs):
+    gpu, orc = c2_runs["gpu"], c2_runs["orc"]
+    assert_totals(gpu, orc)
+    # B and Q are conserved exactly (no diffusion); E + Ez and S drift alike
+    tg, to = gpu.totals(), orc.totals()
+    fresh = api.GpuHydro(c2_runs["rc"])
+    fresh.load(c2_runs["p"])
+    fresh.initialize()
+    t0 = fresh.totals()
+    for k in ("B", "Q"):
+        assert abs(tg[k] / t0[k] - 1.0) < 1e-12, k
+    for k in ("S", "E"):
+        dg, do = tg[k] - t0[k], to[k] - t0[k]
+        assert abs(dg - do) <= 1e-9 * abs(t0[k]), (k, dg, do)
+
+
+def test_hotspots_160k_mixed_form_within_1e5_of_oracle_after_100_steps(c2_runs):
+    for f in ("e", "rhoB", "rhoQ", "s", "T"):
+        _, o, m = c2_runs["snap100"][f]
+        err = float(np.max(np.abs(m - o) / np.abs(o)))
+        assert err < MIXED_TOL, (f, err)
+    _, to, tm = c2_runs["tot100"]
+    for k in ("S", "B", "Q", "E"):
+        assert abs(tm[k] - to[k]) <= 1e-7 * abs(to[k]), k
+
+
+def test_hotspots_with_strangeness_all_four_densities():
+    # rhoS = 0.2 rhoB cos(x): all four densities and chemical potentials
+    # nonzero, rhoS of both signs; FP64 against the oracle at 1e-10, the mixed
+    # form at 1e-5 in e and rhoB, rhoS, rhoQ, after 100 steps
+    p, rc = ics.hotspots_2d(n_side=200, n_hot=12, seed=21, rhoS_frac=0.2)
+    assert (p.rhoS > 0).any() and (p.rhoS < 0).any()
+    gpu = api.GpuHydro(rc)
+    gpu.load(p)
+    orc = O.OracleRun(p, rc)
+    mixed = api.GpuHydro(dataclasses.replace(rc, precision=1))
+    mixed.load(p)
+    gpu.initialize()
+    mixed.initialize()
+    assert orc.initialize() == 0
+    gpu.step(100)
+    mixed.step(100)
+    assert orc.step(100) == 0
+    assert_fields(gpu, orc, VISCOUS_FIELDS, RTOL)
+    assert_totals(gpu, orc)
+    for f in ("e", "rhoB", "rhoS", "rhoQ"):
+        m, o = mixed.get(f), orc.get(f)
+        rel, absn = field_errors(m, o)
+        assert rel < MIXED_TOL and absn < MIXED_TOL, (f, rel, absn)
+    assert np.max(np.abs(orc.get("muS"))) > 1e-3
