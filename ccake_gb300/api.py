@@ -427,6 +427,17 @@ class EventResult(ctypes.Structure):
                 ("frozen", _i32), ("tau", _f64), ("queue_s", _f64), ("latency_s", _f64), ("device_bytes", _i64)]
 
 
+def estimate_device_bytes(rc, n):
+    """Device bytes the event server reserves for an event of n particles (ccake_estimate_device_bytes)."""
+    cfg = make_config(rc)
+    v = _i64()
+    lib().ccake_estimate_device_bytes.argtypes = [ctypes.POINTER(CcakeConfig), _i64, ctypes.POINTER(_i64)]
+    code = lib().ccake_estimate_device_bytes(ctypes.byref(cfg), int(n), ctypes.byref(v))
+    if code:
+        raise CcakeError(code, "estimate_device_bytes")
+    return int(v.value)
+
+
 class Server:
     """ccake_server_*: continuous batching of independent events on one GPU."""
 

@@ -165,13 +165,19 @@ ccake_status_t check_errors(ccake_ctx* ctx) {
   CK(cudaMemcpyAsync(e, ctx->p.err, sizeof(e), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   CK(cudaGetLastError());
-  if (e[E_EOS]) return fail(ctx, CCAKE_ERR_EOS, std::to_string(e[E_EOS]) + " particles without an EoS solution");
-  if (e[E_NEGS]) return fail(ctx, CCAKE_ERR_NEG_ENTROPY, std::to_string(e[E_NEGS]) + " particles with negative entropy");
-  if (e[E_NONFINITE]) return fail(ctx, CCAKE_ERR_NONFINITE, std::to_string(e[E_NONFINITE]) + " non-finite particles");
-  if (e[E_NBR_OVERFLOW])
-    return fail(ctx, CCAKE_ERR_CAPACITY, std::to_string(e[E_NBR_OVERFLOW]) + " particles exceed the neighbour-list capacity " +
-                                             std::to_string(ctx->p.K) + " (re-initialise to resize)");
-  return CCAKE_OK;
+  // the failure raised first decides the status; the message counts them all
+  const ccake_status_t kind[4] = {CCAKE_ERR_EOS, CCAKE_ERR_NEG_ENTROPY, CCAKE_ERR_NONFINITE, CCAKE_ERR_CAPACITY};
+  const std::string what[4] = {" particles without an EoS solution", " particles with negative entropy",
+                               " non-finite particles",
+                               " particles exceed the neighbour-list capacity " + std::to_string(ctx->p.K)};
+  int first = e[E_FIRST] - 1;
+  if (first < 0 || first > 3)
+    for (int k = 3; k >= 0; k--) if (e[k]) first = k;
+  if (first < 0) return CCAKE_OK;
+  std::string msg = std::to_string(e[first]) + what[first];
+  for (int k = 0; k < 4; k++)
+    if (k != first && e[k]) msg += "; then " + std::to_string(e[k]) + what[k];
+  return fail(ctx, kind[first], msg);
 }
 
 ccake_status_t reset_errors(ccake_ctx* ctx) {
@@ -555,6 +561,17 @@ ccake_status_t ccake_load_particles(ccake_ctx* ctx, const ccake_particles_soa* h
   if (!ctx || !h || h->n <= 0 || !h->x || !h->y || !h->e_or_s || !h->ux || !h->uy) return CCAKE_ERR_INVALID;
   if (ctx->cfg.dim == 3 && (!h->eta || !h->ueta)) return fail(ctx, CCAKE_ERR_INVALID, "dim 3 needs eta and ueta");
   if (h->n > (int64_t)0x3fffffff) return fail(ctx, CCAKE_ERR_INVALID, "too many particles");
+  // positions and velocities place the particles in cells: non-finite ones
+  // are rejected here (a non-finite density is the EoS's to report)
+  {
+    const double* cols[6] = {h->x, h->y, ctx->cfg.dim == 3 ? h->eta : nullptr, h->ux, h->uy,
+                             ctx->cfg.dim == 3 ? h->ueta : nullptr};
+    for (int c = 0; c < 6; c++)
+      if (cols[c])
+        for (int64_t i = 0; i < h->n; i++)
+          if (!std::isfinite(cols[c][i]))
+            return fail(ctx, CCAKE_ERR_INVALID, "non-finite position or velocity at particle " + std::to_string(i));
+  }
   free_buffers(ctx);
   const int64_t n = h->n;
   ctx->n = n;
@@ -1110,6 +1127,9 @@ ccake_status_t ccake_set_eos_table_file(ccake_ctx* ctx, const char* eos_path, in
   for (int k = 0; k < 4; k++) {
     if (n[k] < 1) return fail(ctx, CCAKE_ERR_INVALID, "bad grid size");
     nodes *= (size_t)n[k];
+    // a row is 21 numbers of at least two characters: grid sizes the file
+    // cannot hold are rejected before anything is allocated
+    if (nodes > (text.size() / 42) + 1) return fail(ctx, CCAKE_ERR_INVALID, "the table has fewer rows than its grid sizes give");
   }
   std::vector<double> grid(nodes * 4), fields(nodes * 17);
   size_t row = 0;
@@ -1139,7 +1159,13 @@ ccake_status_t ccake_set_eos_table_file(ccake_ctx* ctx, const char* eos_path, in
       lo[k] = std::min(lo[k], v);
       hi[k] = std::max(hi[k], v);
     }
-  for (int k = 0; k < 4; k++) d[k] = n[k] <= 1 ? 0.0 : (hi[k] - lo[k]) / (n[k] - 1.0);
+  for (int k = 0; k < 4; k++) {
+    d[k] = n[k] <= 1 ? 0.0 : (hi[k] - lo[k]) / (n[k] - 1.0);
+    if (!std::isfinite(lo[k]) || !std::isfinite(hi[k]) || (n[k] > 1 && !(d[k] > 0.0)))
+      return fail(ctx, CCAKE_ERR_INVALID, "grid axis " + std::to_string(k) + " is not an increasing finite range");
+  }
+  for (double v : fields)
+    if (!std::isfinite(v)) return fail(ctx, CCAKE_ERR_INVALID, "non-finite table value");
   for (size_t r = 0; r < nodes; r++) {
     const double T = grid[r * 4];
     for (int q = 0; q < 17; q++) {

@@ -126,7 +126,18 @@ enum SnapField : int { SF_R = 0, SF_U = 3, SF_GP = 6, SF_GE = 9, SF_S = 12, SF_E
 constexpr int kFoRow = 2 + 45;
 
 // Error counters raised by the kernels (read back by the host after a call).
-enum ErrSlot : int { E_EOS = 0, E_NEGS = 1, E_NONFINITE = 2, E_NBR_OVERFLOW = 3, NERR = 4 };
+// E_FIRST holds 1 + the slot of the first failure raised since the counters
+// were cleared, so that the host reports the failure that happened first:
+// the reference aborts at its first failure, and later ones (an EoS failure
+// at a particle whose entropy went negative a substep earlier) follow from it.
+enum ErrSlot : int { E_EOS = 0, E_NEGS = 1, E_NONFINITE = 2, E_NBR_OVERFLOW = 3, E_FIRST = 4, NERR = 5 };
+
+#ifdef __CUDACC__
+__device__ __forceinline__ void flag_error(int32_t* err, int slot) {
+  atomicAdd(&err[slot], 1);
+  atomicCAS(&err[E_FIRST], 0, slot + 1);
+}
+#endif
 
 // Kernel normalisations of the reference, src/kernel.cpp:11-26.
 __host__ __device__ inline double knorm(int D) { return D == 1 ? 2. / 3. : D == 2 ? 10. / (7 * M_PI) : 1. / M_PI; }

@@ -377,9 +377,15 @@ __host__ __device__ inline bool newton_attempt(const EosDev& e, int model, int e
   for (int it = 0; it < max_it; it++) {
     if (!have) dens_jac(e, model, entropy, x, f, J, f32 ? Jf : nullptr);
     have = false;
+    // the largest |F_i|, NaN if any is NaN: a non-finite residual fails the
+    // attempt, as GSL_EBADFUNC fails the reference's solver
     double F[4], fres = 0.0;
-    for (int i = 0; i < 4; i++) { F[i] = f[i] - tgt[i]; fres = fres > fabs(F[i]) ? fres : fabs(F[i]); }
-    if (!(fres == fres)) { *iters += it + 1; return false; }
+    for (int i = 0; i < 4; i++) {
+      F[i] = f[i] - tgt[i];
+      const double a = fabs(F[i]);
+      fres = (a > fres || a != a) ? a : fres;
+    }
+    if (!(fres <= 1e300)) { *iters += it + 1; return false; }
     if (extra < 0 && fres < 1e-10) extra = 0;
     double dx[4];
     if (diag) {
@@ -431,7 +437,10 @@ __host__ __device__ inline bool newton_attempt(const EosDev& e, int model, int e
       if (y[0] > 0) {
         dens_jac(e, model, entropy, y, f, J, f32 ? Jf : nullptr);
         double gmax = 0.0;
-        for (int i = 0; i < 4; i++) { const double r = fabs(f[i] - tgt[i]); gmax = gmax > r ? gmax : r; }
+        for (int i = 0; i < 4; i++) {
+          const double r = fabs(f[i] - tgt[i]);
+          gmax = (r > gmax || r != r) ? r : gmax;
+        }
         if (gmax <= fres || h == 6) { have = true; break; }
       }
       lam *= 0.5;
@@ -627,6 +636,8 @@ __host__ __device__ inline int eos_invert(const EosDev& e, int entropy, const do
       ok = find_root(e, model, 0, tgt, y, &it);
       if (!ok) { confdiag_seed(cdk, 0, target, y); ok = find_root(e, model, 0, tgt, y, &it); }
     }
+    // a solution is a finite point with T > 0
+    ok = ok && y[0] > 0.0 && y[0] <= 1e300 && fabs(y[1]) <= 1e300 && fabs(y[2]) <= 1e300 && fabs(y[3]) <= 1e300;
     if (ok) {
       double o[17];
       model_thermo(e, model, y, o);
@@ -672,6 +683,8 @@ __host__ __device__ inline int eos_invert_first(const EosDev& e, int entropy, co
   }
   int it = 0;
   if (!newton_attempt(e, model, entropy, tgt, lo, hi, y, &it, max_it)) return -2;
+  if (!(y[0] > 0.0 && y[0] <= 1e300 && fabs(y[1]) <= 1e300 && fabs(y[2]) <= 1e300 && fabs(y[3]) <= 1e300))
+    return -2;
   double o[17];
   model_thermo(e, model, y, o);
   if (!(o[6] >= 0.0 && o[6] <= 1.0)) return -2;

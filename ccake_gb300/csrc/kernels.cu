@@ -218,7 +218,7 @@ __global__ void __launch_bounds__(kBlock) k_candidates(RunConst rc, Ptrs p) {
       if (c < Kc) p.cand_idx[(size_t)c * n + i] = b;
       c++;
     }
-  if (c > Kc && Kc > 0) atomicAdd(&p.err[E_NBR_OVERFLOW], 1);
+  if (c > Kc && Kc > 0) flag_error(p.err, E_NBR_OVERFLOW);
   p.cand_cnt[i] = c;
 }
 
@@ -317,7 +317,7 @@ __global__ void __launch_bounds__(kBlock) k_passA(RunConst rc, EosDev eos, Ptrs 
       s3 += b67.y * W;
     }
   }
-  if (nn > K) atomicAdd(&p.err[E_NBR_OVERFLOW], 1);
+  if (nn > K) flag_error(p.err, E_NBR_OVERFLOW);
   // gamma and v from u (update_velocity), LRF densities (get_LRF: lab/(gamma t)
   // in Milne coordinates, lab/gamma in Cartesian ones)
   const double tm = rc.cfg.coord == 1 ? 1.0 : t;
@@ -588,7 +588,11 @@ __global__ void k_init_invert(RunConst rc, EosDev eos, Ptrs p) {
     const double tz[4] = {tgt[0], 0.0, 0.0, 0.0};
     k = eos_invert(eos, 0, tz, 0, x, &iters);
   }
-  if (k < 0) { atomicAdd(&p.err[E_EOS], 1); return; }
+  if (k < 0) {   // per-particle status: no EoS solution
+    p.eos_id[i] = -1;
+    flag_error(p.err, E_EOS);
+    return;
+  }
   double th[NTH];
   set_thermo(eos, k, x, th);
   for (int q = 0; q < NTH; q++) p.th[q * n + i] = th[q];

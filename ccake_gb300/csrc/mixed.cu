@@ -173,7 +173,7 @@ __global__ void __launch_bounds__(kBlock) k_passA_mixed(RunConst rc, Ptrs p) {
     }
   }
   if (!live) return;
-  if (nn > K) atomicAdd(&p.err[E_NBR_OVERFLOW], 1);
+  if (nn > K) flag_error(p.err, E_NBR_OVERFLOW);
   const double u3[3] = {p.y[Y_U0 * n + i], p.y[Y_U1 * n + i], D == 3 ? p.y[Y_U2 * n + i] : 0.0};
   const double tm = rc.cfg.coord == 1 ? 1.0 : t;   // the metric's tau (1 in Cartesian coordinates)
   const double g = gamma_milne<D>(u3, tm * tm);

@@ -162,8 +162,9 @@ __device__ __forceinline__ void thermo_tail(const RunConst& rc, const EosDev& eo
   } else {
     double o[17];
     k = eos_invert(eos, 1, tgt, p.eos_id[i], x, &iters, MIX ? 1 : 0, o);
-    if (k < 0) {
-      atomicAdd(&p.err[E_EOS], 1);
+    if (k < 0) {   // per-particle status: no EoS solution (the next search starts the chain over)
+      p.eos_id[i] = -1;
+      flag_error(p.err, E_EOS);
       return;
     }
     set_thermo_o(eos, k, x, o, th, MIX);
@@ -396,7 +397,7 @@ __device__ __forceinline__ void finish_particle(const RunConst& rc, const Ptrs& 
   }
   if (es < 0.0) {
     if (p.freeze[i] > 3) es = 1.e-3;
-    else atomicAdd(&p.err[E_NEGS], 1);
+    else flag_error(p.err, E_NEGS);
   }
   ynew[Y_ES] = es;
   bool finite = true;
@@ -406,7 +407,7 @@ __device__ __forceinline__ void finish_particle(const RunConst& rc, const Ptrs& 
 #pragma unroll
     for (int q = 0; q < 9; q++) finite = finite && isfinite(yq[q]);
   }
-  if (!finite) atomicAdd(&p.err[E_NONFINITE], 1);
+  if (!finite) flag_error(p.err, E_NONFINITE);
 #pragma unroll
   for (int q = 0; q < NY; q++) p.y[q * n + i] = ynew[q];
   if constexpr (DIFF) {

@@ -166,7 +166,12 @@ void scheduler(ccake_server* srv) {
         if (!failed) {
           const ccake::Probe& pr = *e->host;
           ccake_internal::ctx_set_time(e->ctx, pr.tau);
-          if (pr.err[ccake::E_EOS]) st = CCAKE_ERR_EOS;
+          // the failure raised first decides the event's status
+          const ccake_status_t kind[4] = {CCAKE_ERR_EOS, CCAKE_ERR_NEG_ENTROPY, CCAKE_ERR_NONFINITE,
+                                          CCAKE_ERR_CAPACITY};
+          const int first = pr.err[ccake::E_FIRST] - 1;
+          if (first >= 0 && first < 4) st = kind[first];
+          else if (pr.err[ccake::E_EOS]) st = CCAKE_ERR_EOS;
           else if (pr.err[ccake::E_NEGS]) st = CCAKE_ERR_NEG_ENTROPY;
           else if (pr.err[ccake::E_NONFINITE]) st = CCAKE_ERR_NONFINITE;
           else if (pr.err[ccake::E_NBR_OVERFLOW]) st = CCAKE_ERR_CAPACITY;
@@ -268,6 +273,12 @@ ccake_status_t ccake_server_submit(ccake_server* srv, const ccake_config* cfg, c
   if (!srv || !cfg || !p || !ticket || p->n <= 0 || !p->x || !p->y || !p->e_or_s || !p->ux || !p->uy)
     return CCAKE_ERR_INVALID;
   if (!(tau_max > cfg->t0) || !(cfg->dt > 0)) return CCAKE_ERR_INVALID;
+  // an event that could never fit the budget is refused at once (it would
+  // otherwise wait at the head of the queue for memory that never frees)
+  if (ccake_internal::estimate_bytes(*cfg, p->n) > srv->cfg.hbm_budget_bytes) {
+    *ticket = 0;
+    return CCAKE_ERR_CAPACITY;
+  }
   Event* e = new Event;
   e->cfg = *cfg;
   e->tau_max = tau_max;
@@ -284,6 +295,12 @@ ccake_status_t ccake_server_submit(ccake_server* srv, const ccake_config* cfg, c
   srv->events[e->ticket] = e;
   srv->queue.push_back(e);
   *ticket = e->ticket;
+  return CCAKE_OK;
+}
+
+ccake_status_t ccake_estimate_device_bytes(const ccake_config* cfg, int64_t n, int64_t* bytes) {
+  if (!cfg || n <= 0 || !bytes) return CCAKE_ERR_INVALID;
+  *bytes = ccake_internal::estimate_bytes(*cfg, n);
   return CCAKE_OK;
 }
 

@@ -414,7 +414,13 @@ typedef struct ccake_event_result {
 ccake_status_t ccake_server_create(const ccake_server_config* cfg, ccake_server** out);
 /* Stops the internal thread (events still running are abandoned) and frees everything. */
 ccake_status_t ccake_server_destroy(ccake_server* srv);
-/* Copies the event (config and host arrays) into the queue; *ticket identifies it. */
+/* Device bytes the server reserves for an event of n particles with this
+ * config when it admits it (the admission rule compares these with
+ * hbm_budget_bytes). No reference counterpart. */
+ccake_status_t ccake_estimate_device_bytes(const ccake_config* cfg, int64_t n, int64_t* bytes);
+/* Copies the event (config and host arrays) into the queue; *ticket identifies it.
+ * CCAKE_ERR_CAPACITY (ticket 0, nothing queued) for an event whose device
+ * bytes alone exceed the server's budget. */
 ccake_status_t ccake_server_submit(ccake_server* srv, const ccake_config* cfg, const ccake_particles_soa* p,
                                    double tau_max, int64_t* ticket);
 /* Current state of an event (CCAKE_ERR_INVALID for an unknown or released ticket). */

@@ -151,7 +151,8 @@ void orc_destroy(void* p) { delete (Handle*)p; }
 
 int orc_initialize(void* p) {
   Handle* h = (Handle*)p;
-  initialize(h->s, h->nl);
+  const int failed = initialize(h->s, h->nl);
+  if (failed) return failed;
   int bad = 0;
   for (int a = 0; a < h->s.n; a++) bad += (h->s.eos_status[a] < 0);
   return bad;

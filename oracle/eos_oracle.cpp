@@ -169,7 +169,8 @@ void solve4(double A[4][4], double* b, double* xout) {
   }
 }
 
-inline double nan_max(double a, double b) { return a > b ? a : b; }
+// max(a, b) that returns NaN when either is NaN
+inline double nan_max(double a, double b) { return (b > a || b != b) ? b : a; }
 
 // One solver attempt from a seed (replaces GSL hybrids in src/rootfinder.cpp:206-416).
 // Stopping rule: the reference's max |F_i| < 1e-10 (gsl_multiroot_test_residual,
@@ -190,7 +191,7 @@ bool newton_attempt(const Config& c, const Table* tab, int model, int entropy,
     // fails the iterate, as GSL_EBADFUNC fails the reference's solver
     double fmax = 0;
     for (int i = 0; i < 4; i++) fmax = nan_max(fmax, std::fabs(F[i]));
-    if (!(fmax == fmax)) { *iters += it + 1; return false; }  // NaN
+    if (!(fmax <= 1e300)) { *iters += it + 1; return false; }  // NaN or infinite
     if (extra < 0 && fmax < tol) extra = 0;
     double rhs[4] = {-F[0], -F[1], -F[2], -F[3]}, dx[4];
     solve4(J, rhs, dx);
@@ -382,6 +383,9 @@ int eos_invert(const Config& c, const Table* tab, int entropy, const double targ
       ok = find_root(c, tab, model, 0, tgt, y, &it);
       if (!ok) { confdiag_seed(cdk, 0, target, y); ok = find_root(c, tab, model, 0, tgt, y, &it); }
     }
+    // a solution is a finite point with T > 0
+    ok = ok && y[0] > 0.0 && y[0] <= 1e300 && std::fabs(y[1]) <= 1e300 && std::fabs(y[2]) <= 1e300 &&
+         std::fabs(y[3]) <= 1e300;
     if (ok) {
       double o[17];
       model_thermo(c, tab, model, y, o);

@@ -1246,7 +1246,7 @@ Totals conservation(const System& s) {
 // src/sph_workstation.cpp:1228-1340 (process_initial_conditions),
 // :252-375 (initialize_entropy_and_charge_densities) and :394-457
 // (initial_smoothing); no freeze-in, sources or jets.
-void initialize(System& s, NbrList& nl) {
+int initialize(System& s, NbrList& nl) {
   const int D = s.cfg.dim;
   s.t = s.cfg.t0;
   const double tm = s.cfg.coord == 1 ? 1.0 : s.t, t2 = tm * tm;
@@ -1291,7 +1291,7 @@ void initialize(System& s, NbrList& nl) {
         k = eos_invert(s.cfg, s.table, 0, tz, 0, x, &it);
       }
     }
-    if (k < 0) { s.eos_status[a] = -1; bad++; continue; }
+    if (k < 0) { s.eos_status[a] = -1; s.eos_id[a] = -1; bad++; continue; }
     double th[16];
     eos_set_thermo(s.cfg, s.table, k, x, th);
     for (int j = 0; j < 16; j++) s.th[j][a] = th[j];
@@ -1300,6 +1300,9 @@ void initialize(System& s, NbrList& nl) {
     if (s.cfg.input_as_entropy) s.in_e[a] = th[kE]; else s.in_s[a] = th[kS];
     if (!(s.in_e[a] > efc && s.freeze[a] != 4)) s.freeze[a] = 4;
   }
+  // no solution even at zero charge: the reference throws here
+  // (src/sph_workstation.cpp:1840-1846); the count is returned instead
+  if (bad) return bad;
   calculate_initial_sigma(s, nl, s.cfg.t0);
   for (int a = 0; a < s.n; a++) {
     const double sg = s.sigma[a];
@@ -1327,7 +1330,7 @@ void initialize(System& s, NbrList& nl) {
   }
   reset_pi_tensor(s);
   update_thermodynamics(s);
-  (void)bad;
+  return 0;
 }
 
 }  // namespace orc

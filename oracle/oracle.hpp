@@ -170,7 +170,8 @@ void evaluate_time_derivatives(System& s);
 void get_time_derivatives(System& s, NbrList& nl);
 void rk2_step(System& s, NbrList& nl);
 void freeze_out_status(System& s);
-void initialize(System& s, NbrList& nl);
+// returns the number of particles without an EoS solution (the reference throws)
+int initialize(System& s, NbrList& nl);
 
 struct Totals { double S, B, Sq, Q, E, Ez; };
 Totals conservation(const System& s);
