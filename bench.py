@@ -40,14 +40,30 @@ def workload(n_side=400):
     return ics.hotspots_2d(n_side=n_side)
 
 
-def config_dict(n, extra=None):
-    d = {"workload": "viscous 2+1-D BSQ, 30 hot spots, 400x400 lattice (160k particles), dx=0.05 fm, h=0.1 fm, "
-                     "conformal-diagonal EoS, eta/s=0.08, RK2 dt=0.001 fm/c",
-         "particles_per_gpu": n, "precision": "fp64",
-         "l2": "resident event state larger than the 129 MB L2 (no flush)"}
-    if extra:
-        d.update(extra)
-    return d
+def config_dict(n):
+    """The workload, identical in both arms."""
+    return {"workload": "viscous 2+1-D BSQ, 30 hot spots, 400x400 lattice (160k particles), dx=0.05 fm, h=0.1 fm, "
+                        "conformal-diagonal EoS, eta/s=0.08, RK2 dt=0.001 fm/c",
+            "particles_per_gpu": n, "precision": "fp64",
+            "l2": "resident event state larger than the 129 MB L2 (no flush)"}
+
+
+def cpu_model():
+    """The host CPU's model name (lscpu), for the CPU-baseline lines."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.split(":")[0].strip() == "Model name":
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu model")):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return "unknown"
 
 
 # -- clocks during the timed region ----------------------------------------------------------
@@ -156,44 +172,45 @@ def read_mixed_traffic():
 
 
 # -- the reference arm ---------------------------------------------------------------------------
-def cpu_reference(p, rc, steps, warmup=1, threads=0, repeats=3):
-    """Times the oracle (CPU restatement of the reference): `warmup` steps,
-    then the median of `repeats` runs of `steps` RK2 steps, on `threads`
-    OpenMP threads (0: all host cores). Returns (particle-steps/s, seconds
-    per run)."""
+def _oracle():
     import ctypes
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle_py as O
     O.build()
     O.lib().orc_set_threads.argtypes = [ctypes.c_int]
+    return O
+
+
+def cpu_reference(p, rc, steps, warmup=1, threads=0, keep=False):
+    """Times the oracle (CPU restatement of the reference): `warmup` untimed
+    RK2 steps, then `steps` timed ones, on `threads` OpenMP threads (0: all
+    host cores). Returns (particle-steps/s, seconds, the run if keep)."""
+    O = _oracle()
     O.lib().orc_set_threads(int(threads))
     r = O.OracleRun(p, rc)
-    r.initialize()
+    if r.initialize() != 0:
+        raise RuntimeError("oracle initialisation failed")
     if warmup:
         r.step(warmup)
-    runs = []
-    for _ in range(max(1, repeats)):
-        t0 = time.perf_counter()
-        r.step(steps)
-        runs.append(time.perf_counter() - t0)
+    t0 = time.perf_counter()
+    r.step(steps)
+    dt = time.perf_counter() - t0
     O.lib().orc_set_threads(0)
-    dt = float(np.median(runs))
-    return p.n * steps / dt, dt
+    return p.n * steps / dt, dt, (r if keep else None)
 
 
 def run_reference(args, world, rank):
     if rank != 0:
         return
     p, rc = workload()
-    steps = max(1, min(args.steps, args.ref_steps))
-    value, dt = cpu_reference(p, rc, steps, warmup=1)
+    value, dt, _ = cpu_reference(p, rc, args.steps, warmup=args.warmup)
     cores = os.cpu_count()
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / steps,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": config_dict(p.n, {"host": "cpu"}),
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"median of 3 runs of {steps} RK2 steps after 1 warm-up step, all {p.n} "
+            "data": "synthetic", "config": config_dict(p.n), "host": "cpu",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "cpu_model": cpu_model(),
+                             "sample": f"{args.warmup} warm-up then {args.steps} timed RK2 steps of all {p.n} "
                                        f"particles, OMP threads={cores}"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "the reference's Kokkos/Cabana build needs dependencies absent here; its CPU restatement "
@@ -227,7 +244,9 @@ def run_ours(args, world, rank):
     if rank == 0:
         clocks.start()
         time.sleep(0.3)
+    launches0 = gpu.kernel_launches()
     ms = gpu.step_timed(args.steps)
+    launches = gpu.kernel_launches() - launches0
     torch.cuda.synchronize()
     clk = clocks.stop(local) if rank == 0 else None
     t = torch.tensor([ms], dtype=torch.float64, device="cuda")
@@ -251,54 +270,115 @@ def run_ours(args, world, rank):
     from ccake_gb300 import traffic_model as TM
     alg = {"cells": TM.bytes_per_launch("C2", "binning", n), "passA": TM.bytes_per_launch("C2", "passA", n),
            "passB": TM.bytes_per_launch("C2", "passB", n)}
+    flops = {"cells": 0.0, "passA": TM.flops_per_launch("C2", "passA", n),
+             "passB": TM.flops_per_launch("C2", "passB", n)}
     names = ["cells", "passA", "passB"]
     dom = int(np.argmax(prof))
     kname = names[dom]
-    achieved = alg[kname] / (prof[dom] * 1e-3) / 1e9
     fp64 = None
     try:
         fp64 = fp64_peak_tflops()
     except Exception:
         pass
-    flops = {"cells": 0.0, "passA": TM.flops_per_launch("C2", "passA", n),
-             "passB": TM.flops_per_launch("C2", "passB", n)}
     fp64_ach = flops[kname] / (prof[dom] * 1e-3) / 1e12
+    hbm_ach = alg[kname] / (prof[dom] * 1e-3) / 1e9
     traffic = read_traffic(kname)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": config_dict(n, {"parallelism": f"replicas{world}", "device_bytes": gpu.device_bytes()}),
+        "config": config_dict(n),
+        "parallelism": f"replicas{world}", "device_bytes": gpu.device_bytes(),
         "clocks": clk,
-        "gpu_launches": 14 * args.steps,
+        "gpu_launches": launches,
         "e2e": e2e,
         "mixed": mixed,
-        "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "peak_kind": peak_kind,
-                     "traffic": traffic,
-                     "algorithmic_bytes_per_launch": alg[kname], "avg_launch_ms": prof[dom],
+        # the dominant FP64 pass is bound by the FP64 pipe (ncu: the FP64 pipe
+        # is the busiest unit, DRAM under 3 %); its roofline is the FP64 peak,
+        # with the HBM fraction of the algorithmic bytes beside it
+        "roofline": {"bound": "fp64", "kernel": kname, "achieved": fp64_ach, "peak": fp64, "unit": "TFLOP/s",
+                     "frac": (fp64_ach / fp64) if fp64 else None,
+                     "peak_kind": "measured on this GPU in the same process: cuBLAS DGEMM 8192^3 (no FP64 entry "
+                                  "in MEASURED_PEAKS.json)",
+                     "traffic": traffic, "avg_launch_ms": prof[dom],
+                     "flops_per_launch": flops[kname],
                      "phase_ms": dict(zip(names, [float(x) for x in prof])),
-                     "fp64": {"achieved_tflops": fp64_ach, "peak_tflops": fp64,
-                              "frac": (fp64_ach / fp64) if fp64 else None,
-                              "peak_kind": "measured DGEMM on this GPU (torch/cuBLAS 8192^3)"}},
+                     "hbm": {"achieved": hbm_ach, "peak": hbm_peak, "unit": "GB/s", "frac": hbm_ach / hbm_peak,
+                             "peak_kind": peak_kind, "algorithmic_bytes_per_launch": alg[kname]}},
     }
     if not args.no_cpu:
-        ref_steps = max(1, args.ref_steps)
-        cv, cdt = cpu_reference(p, rc, ref_steps, warmup=1, repeats=3)
-        c1, c1dt = cpu_reference(p, rc, 1, warmup=0, threads=1, repeats=1)
+        # the CPU baseline leg: the oracle on the host cores, 100 RK2 steps of
+        # the same event; its final state is also the reference of the
+        # accuracy block (FP64 and mixed GPU forms after the same 100 steps)
+        O = _oracle()
+        cv, cdt, orc = cpu_reference(p, rc, ACC_STEPS, warmup=0, keep=True)
+        c1, _, _ = cpu_reference(p, rc, 1, warmup=0, threads=1)
         line["cpu_baseline"] = {"value": cv, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-                                "sample": f"median of 3 runs of {ref_steps} RK2 steps (after 1 warm-up step) of "
-                                          f"the same 160k-particle event on the host (oracle/, OpenMP, "
-                                          f"{os.cpu_count()} threads)",
+                                "cpu_model": cpu_model(),
+                                "sample": f"{ACC_STEPS} RK2 steps of the same 160k-particle event from its initial "
+                                          f"state on the host (oracle/, OpenMP, {os.cpu_count()} threads)",
                                 "one_thread": {"value": c1, "unit": UNIT, "sample": "1 RK2 step, 1 thread"}}
+        mixed["accuracy"] = accuracy_vs_oracle(p, rc, orc, O)
+        mixed["error_reference"] = "oracle"
     print(json.dumps(line))
+
+
+ACC_STEPS = 100
+
+
+def accuracy_vs_oracle(p, rc, orc, O):
+    """Per-particle error of the FP64 and mixed GPU forms after ACC_STEPS
+    RK2 steps against the oracle's state after the same steps (plain
+    relative error of e and the densities; velocities against their range),
+    on the 160k event and on the same event with strangeness (rhoS = 0.2
+    rhoB cos x), so that all four densities are judged."""
+    import dataclasses
+    from ccake_gb300 import api, ics
+    fields = ("e", "rhoB", "rhoS", "rhoQ", "s", "T")
+
+    def gpu_state(pp, rcc, prec):
+        h = api.GpuHydro(dataclasses.replace(rcc, precision=prec))
+        h.load(pp)
+        h.initialize()
+        h.step(ACC_STEPS)
+        out = {f: h.get(f) for f in fields + ("u0", "u1")}
+        out["totals"] = h.totals()
+        h.close()
+        return out
+
+    def errors(g, o_get, o_tot):
+        err = {}
+        for f in fields:
+            b = o_get(f)
+            big = np.abs(b) >= 1e-3 * np.max(np.abs(b)) if np.any(b) else np.zeros(b.shape, bool)
+            if big.any():
+                err[f] = float(np.max(np.abs(g[f][big] - b[big]) / np.abs(b[big])))
+        for f in ("u0", "u1"):
+            b = o_get(f)
+            err[f + "_of_range"] = float(np.max(np.abs(g[f] - b)) / (np.max(np.abs(b)) + 1e-300))
+        tot = {k: float(abs(g["totals"][k] - o_tot[k]) / (abs(o_tot[k]) + 1e-300)) for k in ("S", "B", "Q", "E")}
+        return {"max_rel_err": err, "totals_rel_diff": tot}
+
+    out = {"steps": ACC_STEPS}
+    o_tot = orc.totals()
+    for prec, name in ((0, "fp64"), (1, "mixed")):
+        out[name] = errors(gpu_state(p, rc, prec), orc.get, o_tot)
+    ps, rcs = ics.hotspots_2d(n_side=400, rhoS_frac=0.2)
+    o2 = O.OracleRun(ps, rcs)
+    o2.initialize()
+    o2.step(ACC_STEPS)
+    o2_tot = o2.totals()
+    out["with_strangeness"] = {name: errors(gpu_state(ps, rcs, prec), o2.get, o2_tot)
+                               for prec, name in ((0, "fp64"), (1, "mixed"))}
+    out["note"] = ("max over particles of |gpu - oracle| / |oracle| where |oracle| >= 1e-3 of the field's "
+                   "largest magnitude; the north-star bar is 1e-5 in e and rhoB, rhoS, rhoQ for the mixed form")
+    return out
 
 
 def run_mixed(p, rc, args, world, dist):
     """The mixed-precision form (FP32 compensated pair sums, FP32 EoM, FP64
-    EoS/state) on the same event: throughput, and the per-particle error of
-    e and the charge densities after 100 steps against the FP64 form (which
-    matches the FP64 oracle to 1e-10 per field)."""
+    EoS/state) on the same event: throughput and per-kernel times. Its error
+    against the oracle is added by the CPU-baseline leg."""
     import dataclasses
     import torch
     from ccake_gb300 import api
@@ -311,33 +391,15 @@ def run_mixed(p, rc, args, world, dist):
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
+    l0 = g.kernel_launches()
     ms = g.step_timed(args.steps)
+    launches = g.kernel_launches() - l0
     t = torch.tensor([ms], dtype=torch.float64, device="cuda")
     if dist:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
     ms_max = float(t.item())
     prof = g.profile_phases(max(2, min(10, args.steps)))
     g.close()
-    # accuracy: 100 steps of each form from the same initial state
-    steps_err = 100
-    runs = {}
-    for prec in (0, 1):
-        h = api.GpuHydro(dataclasses.replace(rc, precision=prec))
-        h.load(p)
-        h.initialize()
-        h.step(steps_err)
-        runs[prec] = {f: h.get(f) for f in ("e", "rhoB", "rhoQ", "s", "T", "u0", "u1")}
-        runs[prec]["totals"] = h.totals()
-        h.close()
-    err = {}
-    for f in ("e", "rhoB", "rhoQ", "s", "T"):
-        a, b = runs[1][f], runs[0][f]
-        err[f] = float(np.max(np.abs(a - b) / (np.abs(b) + 1e-300)))
-    for f in ("u0", "u1"):
-        a, b = runs[1][f], runs[0][f]
-        err[f + "_of_range"] = float(np.max(np.abs(a - b)) / (np.max(np.abs(b)) + 1e-300))
-    tot = {k: float(abs(runs[1]["totals"][k] - runs[0]["totals"][k]) / (abs(runs[0]["totals"][k]) + 1e-300))
-           for k in ("S", "B", "Q", "E")}
     n = p.n
     from ccake_gb300 import traffic_model as TM
     hbm_peak, peak_kind = measured_peaks()
@@ -351,9 +413,8 @@ def run_mixed(p, rc, args, world, dist):
                          "frac": ach / hbm_peak, "peak_kind": peak_kind,
                          "traffic_per_substep_bytes": sum(v for k, v in read_mixed_traffic().items()),
                          "note": "pass A = smoothing + EoS kernels, pass B = gradient + EoM kernels"},
-            "gpu_launches": 16 * args.steps,
-            "max_rel_err_after_100_steps": err, "totals_rel_diff_after_100_steps": tot,
-            "error_reference": "plain FP64 form on the GPU (equal to the FP64 oracle within 1e-10 per field)",
+            "gpu_launches": launches,
+            "error_reference": "none (run without the CPU leg)",
             "what": "FP32 pair loops with Kahan sums and (hi, lo) float positions, FP32 EoM; FP64 EoS Newton, "
                     "state, RK2 update and totals"}
 
@@ -787,10 +848,10 @@ def run_form_only(args, form):
             "steps": args.steps, "ms_per_step": ms / args.steps, "value": p.n * args.steps / (ms * 1e-3)}
     if args.diffusion and not args.no_cpu:
         steps = max(1, args.ref_steps)
-        value, dt = cpu_reference(p, rc, steps, warmup=1)
+        value, dt, _ = cpu_reference(p, rc, steps, warmup=1)
         line["cpu_port"] = {"value": value, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-                            "sample": f"median of 3 runs of {steps} RK2 steps after 1 warm-up step, all {p.n} "
-                                      "particles, diffusion on"}
+                            "sample": f"{steps} RK2 steps after 1 warm-up step, all {p.n} particles, "
+                                      "diffusion on"}
     print(json.dumps(line))
 
 
@@ -800,7 +861,7 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--ref-steps", type=int, default=4, help="RK2 steps timed on the CPU")
+    ap.add_argument("--ref-steps", type=int, default=4, help="RK2 steps timed on the CPU (--form --diffusion)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", choices=["hotspots", "eos-table", "hotspots3d", "serve"], default="hotspots",
                     help="hotspots: the 160k hot-spot event (default); eos-table: the EoS-inversion stress test; "

@@ -114,6 +114,7 @@ def lib():
         L.ccake_step.argtypes = [P, _i32]
         L.ccake_continue_evolution.argtypes = [P, _f64, ctypes.POINTER(_i32)]
         L.ccake_step_timed.argtypes = [P, _i32, ctypes.POINTER(ctypes.c_float)]
+        L.ccake_kernel_launches.argtypes = [P, ctypes.POINTER(_i64)]
         L.ccake_profile_phases.argtypes = [P, _i32, _dp]
         L.ccake_device_bytes.argtypes = [P, ctypes.POINTER(_i64)]
         L.ccake_get_time.argtypes = [P, _dp]
@@ -292,6 +293,12 @@ class GpuHydro:
         ms = ctypes.c_float()
         self._check(lib().ccake_step_timed(self.h, int(n), ctypes.byref(ms)), "step_timed")
         return float(ms.value)
+
+    def kernel_launches(self):
+        """Kernels launched by step / step_timed on this context so far (graph kernel nodes x launches)."""
+        v = ctypes.c_int64()
+        self._check(lib().ccake_kernel_launches(self.h, ctypes.byref(v)), "kernel_launches")
+        return int(v.value)
 
     def profile_phases(self, n):
         """Average device ms per launch: (cell-list kernels, pass A, pass B)."""

@@ -52,6 +52,9 @@ struct ccake_ctx {
   int steps_since_build = 0;
   cudaGraph_t build_graph = nullptr;
   cudaGraphExec_t build_exec = nullptr;
+  // kernels launched through the step and list-build graphs (kernel nodes of
+  // a graph times its launches), for ccake_kernel_launches
+  int64_t step_kernels = 0, build_kernels = 0, launches = 0;
   // learned Newton seed: parameters, gradients, Adam moments (4 x mlp::kParams FP32)
   float* mlp_buf = nullptr;
   double* mlp_sse = nullptr;
@@ -81,6 +84,20 @@ ccake_status_t fail(ccake_ctx* c, ccake_status_t s, const std::string& msg) {
     cudaError_t e_ = (call);                                                                       \
     if (e_ != cudaSuccess) return fail(ctx, CCAKE_ERR_CUDA, std::string(#call ": ") + cudaGetErrorString(e_)); \
   } while (0)
+
+// Kernel nodes of a captured graph.
+int64_t kernel_nodes(cudaGraph_t g) {
+  size_t m = 0;
+  if (cudaGraphGetNodes(g, nullptr, &m) != cudaSuccess || m == 0) return 0;
+  std::vector<cudaGraphNode_t> nodes(m);
+  if (cudaGraphGetNodes(g, nodes.data(), &m) != cudaSuccess) return 0;
+  int64_t k = 0;
+  for (size_t i = 0; i < m; i++) {
+    cudaGraphNodeType t;
+    if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) k++;
+  }
+  return k;
+}
 
 void drop_graph(ccake_ctx* ctx) {
   if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
@@ -232,8 +249,10 @@ ccake_status_t maybe_rebuild(ccake_ctx* ctx, bool graph) {
       enqueue_build(ctx);
       CK(cudaStreamEndCapture(ctx->stream, &ctx->build_graph));
       CK(cudaGraphInstantiate(&ctx->build_exec, ctx->build_graph, 0));
+      ctx->build_kernels = kernel_nodes(ctx->build_graph);
     }
     CK(cudaGraphLaunch(ctx->build_exec, ctx->stream));
+    ctx->launches += ctx->build_kernels;
   } else {
     enqueue_build(ctx);
   }
@@ -426,11 +445,13 @@ ccake_status_t step_enqueue(ccake_ctx* ctx, int n) {
     enqueue_substep(ctx, 2);
     CK(cudaStreamEndCapture(ctx->stream, &ctx->graph));
     CK(cudaGraphInstantiate(&ctx->graph_exec, ctx->graph, 0));
+    ctx->step_kernels = kernel_nodes(ctx->graph);
   }
   ccake_status_t s;
   for (int k = 0; k < n; k++) {
     if ((s = maybe_rebuild(ctx, true))) return s;
     CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
+    ctx->launches += ctx->step_kernels;
     ctx->steps_since_build++;
   }
   return CCAKE_OK;
@@ -797,10 +818,12 @@ ccake_status_t ccake_step(ccake_ctx* ctx, int32_t n_steps) {
     enqueue_substep(ctx, 2);
     CK(cudaStreamEndCapture(ctx->stream, &ctx->graph));
     CK(cudaGraphInstantiate(&ctx->graph_exec, ctx->graph, 0));
+    ctx->step_kernels = kernel_nodes(ctx->graph);
   }
   for (int k = 0; k < n_steps; k++) {
     if ((s = maybe_rebuild(ctx, true))) return s;
     CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
+    ctx->launches += ctx->step_kernels;
     ctx->steps_since_build++;
     ctx->evaluated = true;
   }
@@ -823,6 +846,7 @@ ccake_status_t ccake_step_timed(ccake_ctx* ctx, int32_t n_steps, float* device_m
   for (int k = 0; k < n_steps; k++) {
     if ((s = maybe_rebuild(ctx, true))) return s;
     CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
+    ctx->launches += ctx->step_kernels;
     ctx->steps_since_build++;
     ctx->evaluated = true;
   }
@@ -836,6 +860,12 @@ ccake_status_t ccake_step_timed(ccake_ctx* ctx, int32_t n_steps, float* device_m
   CK(cudaMemcpy(&c, ctx->p.clock, sizeof(Clock), cudaMemcpyDeviceToHost));
   ctx->t = c.t;
   return s;
+}
+
+ccake_status_t ccake_kernel_launches(const ccake_ctx* ctx, int64_t* launches) {
+  if (!ctx || !launches) return CCAKE_ERR_INVALID;
+  *launches = ctx->launches;
+  return CCAKE_OK;
 }
 
 ccake_status_t ccake_profile_phases(ccake_ctx* ctx, int32_t n_steps, double* ms3) {

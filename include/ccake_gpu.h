@@ -221,6 +221,11 @@ ccake_status_t ccake_continue_evolution(ccake_ctx* ctx, double max_tau, int32_t*
  * Measurement entry point; no reference counterpart. */
 ccake_status_t ccake_step_timed(ccake_ctx* ctx, int32_t n_steps, float* device_ms);
 
+/* Kernels launched by ccake_step / ccake_step_timed on this context so far:
+ * the kernel nodes of the step graph and of the candidate-list build graph,
+ * times their launches. Measurement entry point; no reference counterpart. */
+ccake_status_t ccake_kernel_launches(const ccake_ctx* ctx, int64_t* launches);
+
 /* Runs n_steps RK2 steps kernel by kernel (no graph) with CUDA events between
  * the launches and returns the average device time per launch, in ms, of:
  * ms[0] the four cell-list kernels together, ms[1] the smoothing+EoS pass,
