@@ -452,8 +452,10 @@ def run_eos_table(args):
     build.build()
     n_rows = args.eos_rows
     n, lo, d, fields = eos_table.synthetic_table()
-    conf5, cdiag5 = eos_table.fallback_scales()
     rc = ics.RunConfig(eos_kind=2, thermo_mode=1)
+    # the analytic fallbacks (tanh-conformal, conformal, conformal-diagonal)
+    # matched to the table as the reference does
+    conf5, cdiag5 = api.table_fallback_scales(n, lo, d, fields, rc.freeze_out_T)
     g = api.GpuHydro(rc)
     g.set_eos_table(n, lo, d, fields, conf5, cdiag5)
     x_true = eos_table.sample_states(n_rows, seed=1)
@@ -622,7 +624,7 @@ def run_hotspots3d(args):
     build.build()
     p, rc = ics.hotspots_3d(n_xy=args.h3d_nxy, n_eta=args.h3d_neta, eos_kind=2, zeta_over_s=0.1)
     n, lo, d, fields = eos_table.synthetic_table()
-    conf5, cdiag5 = eos_table.fallback_scales()
+    conf5, cdiag5 = api.table_fallback_scales(n, lo, d, fields, rc.freeze_out_T)
     steps = args.steps
     out = {}
     forms = (("mixed", 1), ("fp64", 0)) if args.form is None else ((args.form, 1 if args.form == "mixed" else 0),)

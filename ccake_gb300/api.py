@@ -130,6 +130,7 @@ def lib():
         L.ccake_set_eos_table.argtypes = [P, _ip, _dp, _dp, _dp, _dp, _dp]
         L.ccake_eos_thermo_batch.argtypes = [P, _i32, _i64, _dp, _dp]
         L.ccake_set_eos_table_file.argtypes = [P, ctypes.c_char_p, _i32, _dp, _dp]
+        L.ccake_eos_table_fallback_scales.argtypes = [_ip, _dp, _dp, _dp, _f64, _dp, _dp]
         _fp = ctypes.POINTER(ctypes.c_float)
         L.ccake_mlp_train.argtypes = [P, _i64, _i32, _i32, ctypes.c_double, ctypes.c_uint64, _dp]
         L.ccake_mlp_get_params.argtypes = [P, _fp, _fp]
@@ -161,6 +162,20 @@ def _d(a):
 
 def _i(a):
     return a.ctypes.data_as(_ip) if a is not None else None
+
+
+def table_fallback_scales(n, lo, d, fields, freeze_out_T):
+    """(conf5, cdiag5) of the analytic fallbacks matched to a table as the
+    reference does (ccake_eos_table_fallback_scales)."""
+    n = np.ascontiguousarray(n, dtype=np.int32)
+    lo = np.ascontiguousarray(lo, dtype=np.float64)
+    d = np.ascontiguousarray(d, dtype=np.float64)
+    f = np.ascontiguousarray(fields, dtype=np.float64)
+    c5, d5 = np.zeros(5), np.zeros(5)
+    code = lib().ccake_eos_table_fallback_scales(_i(n), _d(lo), _d(d), _d(f), float(freeze_out_T), _d(c5), _d(d5))
+    if code:
+        raise CcakeError(code, "eos_table_fallback_scales")
+    return c5, d5
 
 
 class GpuHydro:
@@ -346,20 +361,21 @@ class GpuHydro:
                     "neighbours")
         return off, idx[:cnt.value]
 
-    def set_eos_table(self, n, lo, d, fields, conf5, cdiag5):
-        """Uploads a tabulated EoS (eos_kind 2); see ccake_set_eos_table."""
+    def set_eos_table(self, n, lo, d, fields, conf5=None, cdiag5=None):
+        """Uploads a tabulated EoS (eos_kind 2); see ccake_set_eos_table. Fallback
+        scales left as None are matched to the table as the reference does."""
         n = np.ascontiguousarray(n, dtype=np.int32)
         lo = np.ascontiguousarray(lo, dtype=np.float64)
         d = np.ascontiguousarray(d, dtype=np.float64)
         f = np.ascontiguousarray(fields, dtype=np.float64)
-        c5 = np.ascontiguousarray(conf5, dtype=np.float64)
-        d5 = np.ascontiguousarray(cdiag5, dtype=np.float64)
+        c5 = None if conf5 is None else np.ascontiguousarray(conf5, dtype=np.float64)
+        d5 = None if cdiag5 is None else np.ascontiguousarray(cdiag5, dtype=np.float64)
         self._check(lib().ccake_set_eos_table(self.h, _i(n), _d(lo), _d(d), _d(f), _d(c5), _d(d5)), "set_eos_table")
 
-    def set_eos_table_file(self, path, normalize_by_T, conf5, cdiag5):
+    def set_eos_table_file(self, path, normalize_by_T, conf5=None, cdiag5=None):
         """Loads a thermo.dat table (the reference's text format); see ccake_set_eos_table_file."""
-        c5 = np.ascontiguousarray(conf5, dtype=np.float64)
-        d5 = np.ascontiguousarray(cdiag5, dtype=np.float64)
+        c5 = None if conf5 is None else np.ascontiguousarray(conf5, dtype=np.float64)
+        d5 = None if cdiag5 is None else np.ascontiguousarray(cdiag5, dtype=np.float64)
         self._check(lib().ccake_set_eos_table_file(self.h, str(path).encode(), int(bool(normalize_by_T)), _d(c5),
                                                    _d(d5)), "set_eos_table_file")
 

@@ -1081,9 +1081,52 @@ ccake_status_t ccake_get_neighbours(ccake_ctx* ctx, int32_t* offsets, int32_t* i
   return check_errors(ctx);
 }
 
+ccake_status_t ccake_eos_table_fallback_scales(const int32_t* n, const double* lo, const double* d,
+                                              const double* fields, double freeze_out_T, double* conf5,
+                                              double* cdiag5) {
+  if (!n || !lo || !d || !fields || !conf5 || !cdiag5 || !(freeze_out_T > 0)) return CCAKE_ERR_INVALID;
+  EosDev host{};
+  host.kind = 2;
+  double mx[4];
+  for (int k = 0; k < 4; k++) {
+    if (n[k] < 1 || !(d[k] >= 0.0) || !std::isfinite(lo[k])) return CCAKE_ERR_INVALID;
+    host.tab.n[k] = n[k];
+    host.tab.lo[k] = lo[k];
+    host.tab.d[k] = d[k];
+    mx[k] = lo[k] + d[k] * (n[k] - 1);   // grid maxima (get_tbqs_maxima_no_ext)
+  }
+  host.tab.f = fields;
+  // the reference's matching (src/eos_initialization.cpp:276-341 for the
+  // tanh-conformal and conformal fallbacks, :343-403 and :404-464 for the
+  // conformal-diagonal one): p/T^4 at Tmax = 1.1 T_FO fixes c (T0 = 1), and
+  // p at (Tmax, mu_max) on each axis fixes that axis' scale
+  const double Tmax = 1.1 * freeze_out_T;
+  auto p_at = [&](double T, double mB, double mQ, double mS) {
+    double x4[4] = {T, mB, mQ, mS}, o[17];
+    table_thermo(host.tab, x4, o);
+    return o[0];
+  };
+  const double pT = p_at(Tmax, 0.0, 0.0, 0.0);
+  const double c = pT / (Tmax * Tmax * Tmax * Tmax);
+  conf5[0] = cdiag5[0] = c;
+  conf5[1] = cdiag5[1] = 1.0;
+  for (int a = 1; a < 4; a++) {   // muB, muQ, muS: the scales' order
+    if (std::fabs(mx[a]) < 1e-30) { conf5[1 + a] = cdiag5[1 + a] = 1.0; continue; }
+    double x[4] = {Tmax, 0.0, 0.0, 0.0};
+    x[a] = mx[a];
+    const double pv = p_at(x[0], x[1], x[2], x[3]);
+    conf5[1 + a] = std::pow(c, 0.25) * mx[a] / std::sqrt(std::sqrt(pv) - std::sqrt(pT));
+    cdiag5[1 + a] = std::pow(c / (pv - pT), 0.25) * mx[a];
+  }
+  for (int q = 0; q < 5; q++)
+    if (!(conf5[q] > 0.0) || !(cdiag5[q] > 0.0) || !std::isfinite(conf5[q]) || !std::isfinite(cdiag5[q]))
+      return CCAKE_ERR_INVALID;
+  return CCAKE_OK;
+}
+
 ccake_status_t ccake_set_eos_table(ccake_ctx* ctx, const int32_t* n, const double* lo, const double* d,
-                                   const double* fields, const double* conf5, const double* cdiag5) {
-  if (!ctx || !n || !lo || !d || !fields || !conf5 || !cdiag5) return CCAKE_ERR_INVALID;
+                                   const double* fields, const double* conf5_in, const double* cdiag5_in) {
+  if (!ctx || !n || !lo || !d || !fields) return CCAKE_ERR_INVALID;
   if (ctx->eos.kind != 2) return fail(ctx, CCAKE_ERR_INVALID, "eos_kind is not 2 (table)");
   size_t nodes = 1;
   for (int k = 0; k < 4; k++) {
@@ -1091,6 +1134,16 @@ ccake_status_t ccake_set_eos_table(ccake_ctx* ctx, const int32_t* n, const doubl
     nodes *= (size_t)n[k];
   }
   if (nodes > ((size_t)1 << 31)) return fail(ctx, CCAKE_ERR_INVALID, "table too large");
+  // fallback scales: given, or matched to the table as the reference does
+  double ref_conf[5], ref_cdiag[5];
+  const double* conf5 = conf5_in;
+  const double* cdiag5 = cdiag5_in;
+  if (!conf5 || !cdiag5) {
+    if (ccake_eos_table_fallback_scales(n, lo, d, fields, ctx->cfg.freeze_out_T, ref_conf, ref_cdiag))
+      return fail(ctx, CCAKE_ERR_INVALID, "the table gives no fallback scales at 1.1 T_FO");
+    if (!conf5) conf5 = ref_conf;
+    if (!cdiag5) cdiag5 = ref_cdiag;
+  }
   for (int q = 0; q < 5; q++)
     if (!(conf5[q] > 0.0) || !(cdiag5[q] > 0.0)) return fail(ctx, CCAKE_ERR_INVALID, "bad fallback scales");
   drop_graph(ctx);
@@ -1128,7 +1181,7 @@ ccake_status_t ccake_set_eos_table(ccake_ctx* ctx, const int32_t* n, const doubl
 
 ccake_status_t ccake_set_eos_table_file(ccake_ctx* ctx, const char* eos_path, int32_t normalize_by_T,
                                         const double* conf5, const double* cdiag5) {
-  if (!ctx || !eos_path || !conf5 || !cdiag5) return CCAKE_ERR_INVALID;
+  if (!ctx || !eos_path) return CCAKE_ERR_INVALID;
   std::string path(eos_path);
   struct stat st{};
   if (stat(path.c_str(), &st) == 0 && S_ISDIR(st.st_mode)) path += "/thermo.dat";
@@ -1506,7 +1559,10 @@ ccake_status_t ccake_write_system_state(ccake_ctx* ctx, const char* path) {
     for (int q = 9; q <= 30; q++) out << F(q) << " ";
     for (int k = 0; k < 3; k++) out << (k < D ? F(31 + k) : 0.0) << " ";
     const int model = chain_model(ctx->eos.kind, eid[(size_t)i]);
-    const char* eos_name = model == M_TABLE ? "table" : model == M_CDIAG ? "conformal_diagonal" : "conformal";
+    const char* eos_name = model == M_TABLE  ? "table"
+                           : model == M_TANH  ? "tanh_conformal"
+                           : model == M_CDIAG ? "conformal_diagonal"
+                                              : "conformal";
     out << F(34) << " " << frz[(size_t)i] << " " << eos_name << " " << 0 << " ";
     for (int k = 0; k < 6; k++) out << dn[k][(size_t)i] << " ";
     out << "\n";

@@ -61,19 +61,23 @@ struct EosDev {
   const PreinvView* pre = nullptr;
 };
 
-enum Model : int { M_CONF = 0, M_CDIAG = 1, M_TABLE = 2 };
+enum Model : int { M_CONF = 0, M_CDIAG = 1, M_TABLE = 2, M_TANH = 3 };
 
 // Chains of the reference (src/eos_initialization.cpp:216-501):
 // conformal -> [conformal, conformal_diagonal]; conformal_diagonal -> [itself];
-// table -> [table, conformal, conformal_diagonal].
-__host__ __device__ inline int chain_len(int kind) { return kind == 0 ? 2 : (kind == 1 ? 1 : 3); }
+// table -> [table, tanh_conformal, conformal, conformal_diagonal] (the tanh
+// stage with use_tanh_conformal = true, include/eos_header.h:7).
+__host__ __device__ inline int chain_len(int kind) { return kind == 0 ? 2 : (kind == 1 ? 1 : 4); }
 __host__ __device__ inline int chain_model(int kind, int k) {
   if (kind == 0) return k == 0 ? M_CONF : M_CDIAG;
   if (kind == 1) return M_CDIAG;
-  return k == 0 ? M_TABLE : (k == 1 ? M_CONF : M_CDIAG);
+  return k == 0 ? M_TABLE : (k == 1 ? M_TANH : (k == 2 ? M_CONF : M_CDIAG));
 }
+// The tanh-conformal fallback shares the conformal fallback's scales: the
+// reference derives both from the table by the same rule
+// (src/eos_initialization.cpp:276-341 and :343-403).
 __host__ __device__ inline Scales model_scales(const EosDev& e, int model) {
-  if (e.kind == 2 && model != M_TABLE) return model == M_CONF ? e.conf : e.cdiag;
+  if (e.kind == 2 && model != M_TABLE) return model == M_CDIAG ? e.cdiag : e.conf;
   return e.own;
 }
 
@@ -123,6 +127,50 @@ __host__ __device__ inline void confdiag_thermo(const Scales& k, const double* x
   o[9] = 12.0 * cp * rS * rS * (k.iS0 * k.iS0);
   for (int i = 10; i < 16; i++) o[i] = kTiny;
   o[16] = 12.0 * cp * rT * rT * (k.iT0 * k.iT0);
+}
+
+// The tanh-modulated conformal model (include/eos_tanh_conformal.h): the
+// conformal pressure p_c of the given scales times
+// t(T) = (1 + tanh((T - Tc)/Ts)) / 2 with Tc = 220 MeV and Ts = 120 MeV
+// (src/eos_initialization.cpp:334-335). Densities and susceptibilities follow
+// from p = t p_c by the product rule (t' = sech^2((T - Tc)/Ts) / (2 Ts),
+// t'' = -2 tanh((T - Tc)/Ts) t' / Ts). Its c_s^2 is the adiabatic speed of
+// sound, dp/de at fixed ratios s : rhoB : rhoS : rhoQ. Along dn = n dlambda
+// (n = (s, rho) = grad p, chi = the Hessian of p in (T, mu)) one has
+// dp = n . chi^-1 n dlambda and de = T ds + mu . drho = w dlambda, so
+// c_s^2 = n . chi^-1 n / w with w = T s + mu . rho.
+constexpr double kTanhTc = 220.0 / kHbarcMeVfm, kTanhTs = 120.0 / kHbarcMeVfm;
+
+template <class R>
+__host__ __device__ inline void solve4(R A[4][4], R* b, R* x);
+
+__host__ __device__ inline void tanh_conformal_thermo(const Scales& k, const double* x4, double* o) {
+  double c[17];
+  conformal_thermo(k, x4, c);
+  const double T = x4[0], mB = x4[1], mQ = x4[2], mS = x4[3];
+  const double y = (T - kTanhTc) / kTanhTs;
+  const double th = tanh(y), sc = 1.0 / cosh(y);
+  const double t = 0.5 * (1.0 + th);
+  const double tp = 0.5 * sc * sc / kTanhTs;
+  const double tpp = -2.0 * th * tp / kTanhTs;
+  const double p = t * c[0], s = t * c[1] + tp * c[0];
+  const double B = t * c[2], S = t * c[3], Q = t * c[4];
+  o[0] = p; o[1] = s; o[2] = B; o[3] = S; o[4] = Q;
+  o[5] = (s * T + mB * B + mQ * Q + mS * S) - p;
+  for (int i = 7; i <= 12; i++) o[i] = t * c[i];
+  o[13] = t * c[13] + tp * c[2];
+  o[14] = t * c[14] + tp * c[4];
+  o[15] = t * c[15] + tp * c[3];
+  o[16] = t * c[16] + 2.0 * tp * c[1] + tpp * c[0];
+  // c_s^2 = n . chi^-1 n / w, n and chi in (T, muB, muQ, muS) order
+  double H[4][4] = {{o[16], o[13], o[14], o[15]},
+                    {o[13], o[7], o[10], o[11]},
+                    {o[14], o[10], o[8], o[12]},
+                    {o[15], o[11], o[12], o[9]}};
+  double n[4] = {s, B, Q, S}, r[4] = {s, B, Q, S}, z[4];
+  solve4<double>(H, r, z);
+  const double w = s * T + mB * B + mQ * Q + mS * S;
+  o[6] = (n[0] * z[0] + n[1] * z[1] + n[2] * z[2] + n[3] * z[3]) / w;
 }
 
 // Multilinear lookup with the reference's index rule (src/interpolatorND.cpp:250-317):
@@ -250,7 +298,9 @@ __host__ __device__ inline void model_thermo(const EosDev& e, int model, const d
     return;
   }
   const Scales k = model_scales(e, model);
-  if (model == M_CONF) conformal_thermo(k, x4, o); else confdiag_thermo(k, x4, o);
+  if (model == M_CONF) conformal_thermo(k, x4, o);
+  else if (model == M_TANH) tanh_conformal_thermo(k, x4, o);
+  else confdiag_thermo(k, x4, o);
 }
 
 __host__ __device__ inline void model_box(const EosDev& e, int model, double* lo, double* hi) {
@@ -549,7 +599,7 @@ __host__ __device__ inline double cbrt_halley(double x) {
 }
 
 __host__ __device__ inline bool analytic_seed(const EosDev& e, int model, const double* tgt, double* y) {
-  if (model == M_TABLE) return false;
+  if (model == M_TABLE || model == M_TANH) return false;
   const Scales k = model_scales(e, model);
   const double X0[4] = {k.T0, k.muB0, k.muQ0, k.muS0};
   const double ic4 = 1.0 / (4.0 * k.c * k.T0 * k.T0 * k.T0 * k.T0);

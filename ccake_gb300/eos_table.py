@@ -118,9 +118,11 @@ def synthetic_table(nT=151, nmu=41, T_range=(0.05, 0.8), mu_max=0.45):
 
 
 def fallback_scales():
-    """(c, T0, muB0, muQ0, muS0) of the conformal and conformal-diagonal
-    models behind the table in the EoS chain: the table's high-T limit
-    p -> a T^4 with unit scales."""
+    """Simple (c, T0, muB0, muQ0, muS0) of the analytic fallbacks behind the
+    table: the table's high-T limit p -> a T^4 with unit scales (a fixed
+    choice for tests that need one). The reference matches them to the table
+    at 1.1 T_FO instead: api.table_fallback_scales, or ``None`` scales in
+    GpuHydro.set_eos_table."""
     conf = np.array([A_QGP, 1.0, 1.0, 1.0, 1.0])
     return conf, conf.copy()
 

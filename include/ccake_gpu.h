@@ -331,14 +331,29 @@ ccake_status_t ccake_eos_invert_batch(ccake_ctx* ctx, int32_t entropy_mode, int6
 /* Tabulated EoS (eos_kind 2): uniform grid in (T, muB, muQ, muS) (fm^-1),
  * n[k] points from lo[k] with spacing d[k], nodes row-major with muS fastest,
  * 17 FP64 fields per node in the order p s rhoB rhoS rhoQ e cs2 chiBB chiQQ
- * chiSS chiBQ chiBS chiQS chiTB chiTQ chiTS chiTT (fm units). conf5 / cdiag5:
- * (c, T0, muB0, muQ0, muS0) of the conformal and conformal-diagonal models
- * behind the table in the EoS chain. Copied to device memory; call after
+ * chiSS chiBQ chiBS chiQS chiTB chiTQ chiTS chiTT (fm units). The EoS chain
+ * is then table -> tanh_conformal -> conformal -> conformal_diagonal (eos_id
+ * 0..3). conf5 / cdiag5: (c, T0, muB0, muQ0, muS0) of the conformal (and
+ * tanh-conformal) and of the conformal-diagonal fallbacks; NULL takes the
+ * reference's matching to the table (ccake_eos_table_fallback_scales at the
+ * config's freeze_out_T). Copied to device memory; call after
  * ccake_ctx_create and before ccake_initialize. Replaces the table loader of
  * EquationOfState::init (src/eos_table.cpp:12-100,
  * src/eos_initialization.cpp:216-501). */
 ccake_status_t ccake_set_eos_table(ccake_ctx* ctx, const int32_t* n, const double* lo, const double* d,
                                    const double* fields, const double* conf5, const double* cdiag5);
+
+/* Fallback scales matched to a table as the reference does
+ * (src/eos_initialization.cpp:276-464): with Tmax = 1.1 freeze_out_T and the
+ * grid maxima mu_max, c = p(Tmax, 0, 0, 0) / Tmax^4 and T0 = 1 for both;
+ * tanh-conformal / conformal mu0 = c^(1/4) mu_max / sqrt(sqrt(p(Tmax, mu_max))
+ * - sqrt(p(Tmax, 0))); conformal-diagonal mu0 = (c / (p(Tmax, mu_max) -
+ * p(Tmax, 0)))^(1/4) mu_max; an axis whose maximum is 0 gets mu0 = 1. Host
+ * computation, no context. CCAKE_ERR_INVALID when a scale is not finite and
+ * positive. */
+ccake_status_t ccake_eos_table_fallback_scales(const int32_t* n, const double* lo, const double* d,
+                                              const double* fields, double freeze_out_T, double* conf5,
+                                              double* cdiag5);
 
 /* Tabulated EoS from the reference's text format: eos_path is a thermo.dat
  * file or a directory holding one; line 1 the 4 grid sizes, then one line
@@ -346,7 +361,8 @@ ccake_status_t ccake_set_eos_table(ccake_ctx* ctx, const int32_t* n, const doubl
  * chiTB chiTQ chiTS chiTT" (axes in MeV, nodes row-major with muS fastest).
  * Axes are converted to fm^-1 and each grid rebuilt from its extremes; with
  * normalize_by_T the fields are ratios p/T^4 ... chi/T^2, else MeV powers.
- * Then as ccake_set_eos_table. Replaces EoS_table::EoS_table
+ * Then as ccake_set_eos_table (NULL scales: matched to the table).
+ * Replaces EoS_table::EoS_table
  * (src/eos_table.cpp:14-100) with InterpolatorND<4>::load_data_from_dat
  * (src/interpolatorND.cpp:125-228). */
 ccake_status_t ccake_set_eos_table_file(ccake_ctx* ctx, const char* eos_path, int32_t normalize_by_T,

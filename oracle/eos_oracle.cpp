@@ -16,19 +16,21 @@ struct Scales { double c, T0, muB0, muQ0, muS0; };
 // Reference EoS chains (src/eos_initialization.cpp:216-501):
 //   conformal           -> [conformal, conformal_diagonal]
 //   conformal_diagonal  -> [conformal_diagonal]
-//   table               -> [table, conformal, conformal_diagonal] (the tanh
-//                          fallback of the reference is not part of this chain)
-enum Model { mConformal = 0, mConfDiag = 1, mTable = 2 };
+//   table               -> [table, tanh_conformal, conformal, conformal_diagonal]
+//                          (use_tanh_conformal = true, include/eos_header.h:7)
+enum Model { mConformal = 0, mConfDiag = 1, mTable = 2, mTanh = 3 };
 
 int chain_model(const Config& c, int k) {
   if (c.eos_kind == kConformal) return k == 0 ? mConformal : mConfDiag;
   if (c.eos_kind == kConformalDiagonal) return mConfDiag;
-  return k == 0 ? mTable : (k == 1 ? mConformal : mConfDiag);
+  return k == 0 ? mTable : (k == 1 ? mTanh : (k == 2 ? mConformal : mConfDiag));
 }
 
+// The tanh-conformal fallback is matched to the table by the same rule as the
+// conformal one (src/eos_initialization.cpp:276-341, :343-403): same scales.
 Scales model_scales(const Config& c, const Table* tab, int model) {
   if (c.eos_kind == kTable && tab && model != mTable) {
-    const auto& k = model == mConformal ? tab->conf : tab->cdiag;
+    const auto& k = model == mConfDiag ? tab->cdiag : tab->conf;
     return {k.c, k.T0, k.muB0, k.muQ0, k.muS0};
   }
   return {c.eos_c, c.eos_T0, c.eos_muB0, c.eos_muQ0, c.eos_muS0};
@@ -81,10 +83,51 @@ void confdiag_thermo(const Scales& k, const double* x4, double* o) {
   o[16] = 12.0 * cp * T * T / (k.T0 * k.T0 * k.T0 * k.T0);
 }
 
+void solve4(double A[4][4], double* b, double* xout);
+
+// include/eos_tanh_conformal.h: p = t(T) p_conformal with
+// t = (1 + tanh((T - Tc)/Ts))/2, Tc = 220 MeV, Ts = 120 MeV
+// (src/eos_initialization.cpp:334-335); derivatives by the product rule.
+// c_s^2: the adiabatic speed of sound (dp/de at fixed s : rho ratios),
+// n . chi^-1 . n / (T s + mu . rho) with n = grad p and chi its Hessian.
+void tanh_conformal_thermo(const Scales& k, const double* x4, double* o) {
+  const double Tc = 220.0 / kHbarcMeVfm, Ts = 120.0 / kHbarcMeVfm;
+  double pc[17];
+  conformal_thermo(k, x4, pc);
+  const double T = x4[0], mB = x4[1], mQ = x4[2], mS = x4[3];
+  const double arg = (T - Tc) / Ts;
+  const double tanh_a = std::tanh(arg), sech_a = 1.0 / std::cosh(arg);
+  const double f = 0.5 * (1.0 + tanh_a);
+  const double f1 = 0.5 * sech_a * sech_a / Ts;
+  const double f2 = -2.0 * tanh_a * f1 / Ts;
+  o[0] = f * pc[0];
+  o[1] = f * pc[1] + f1 * pc[0];
+  o[2] = f * pc[2];
+  o[3] = f * pc[3];
+  o[4] = f * pc[4];
+  o[5] = (o[1] * T + mB * o[2] + mQ * o[4] + mS * o[3]) - o[0];
+  for (int i = 7; i <= 12; i++) o[i] = f * pc[i];
+  o[13] = f * pc[13] + f1 * pc[2];   // chi_TB
+  o[14] = f * pc[14] + f1 * pc[4];   // chi_TQ
+  o[15] = f * pc[15] + f1 * pc[3];   // chi_TS
+  o[16] = f * pc[16] + 2.0 * f1 * pc[1] + f2 * pc[0];
+  double chi[4][4] = {{o[16], o[13], o[14], o[15]},
+                      {o[13], o[7], o[10], o[11]},
+                      {o[14], o[10], o[8], o[12]},
+                      {o[15], o[11], o[12], o[9]}};
+  double grad[4] = {o[1], o[2], o[4], o[3]}, rhs[4] = {o[1], o[2], o[4], o[3]}, sol[4];
+  solve4(chi, rhs, sol);
+  double q = 0.0;
+  for (int i = 0; i < 4; i++) q += grad[i] * sol[i];
+  o[6] = q / (o[1] * T + mB * o[2] + mQ * o[4] + mS * o[3]);
+}
+
 void model_thermo(const Config& c, const Table* tab, int model, const double* x4, double* o) {
   if (model == mTable) { table_full_thermo(*tab, x4, o); return; }
   Scales k = model_scales(c, tab, model);
-  if (model == mConformal) conformal_thermo(k, x4, o); else confdiag_thermo(k, x4, o);
+  if (model == mConformal) conformal_thermo(k, x4, o);
+  else if (model == mTanh) tanh_conformal_thermo(k, x4, o);
+  else confdiag_thermo(k, x4, o);
 }
 
 // Densities (e|s, B, Q, S) and their Jacobian with respect to (T, muB, muQ, muS).
@@ -344,7 +387,7 @@ void confdiag_seed(const Scales& k, int entropy, const double* tgt, double* x) {
 }  // namespace
 
 int eos_chain_length(const Config& c) {
-  return c.eos_kind == kConformal ? 2 : (c.eos_kind == kConformalDiagonal ? 1 : 3);
+  return c.eos_kind == kConformal ? 2 : (c.eos_kind == kConformalDiagonal ? 1 : 4);
 }
 
 void eos_full_thermo(const Config& c, const Table* tab, int k, const double tbqs[4], double out[17]) {

@@ -1,22 +1,27 @@
 """Tabulated EoS (eos_kind 2) on the GPU against the oracle, through the C ABI.
 
 Table: the synthetic stress-test EoS of ccake_gb300.eos_table at reduced
-resolution (76 x 21^3 nodes, 95 MB). Strict parity is checked where that EoS
-is thermodynamically stable (T >= 0.2 GeV: positive-definite Hessian, so the
-inverse is unique); the unstable band T ~ 0.10-0.19 GeV is covered by the
-status comparison only.
+resolution (76 x 21^3 nodes, 95 MB), with the EoS chain of the reference:
+table -> tanh_conformal -> conformal -> conformal_diagonal, the fallbacks
+matched to the table at 1.1 T_FO as the reference does. Strict parity is
+checked where that EoS is thermodynamically stable (T >= 0.2 GeV:
+positive-definite Hessian, so the inverse is unique); in the unstable band
+T ~ 0.10-0.19 GeV the c_s^2 guard sends rows down the chain, and the rows
+that land on the tanh-conformal stage are compared there.
 """
 import ctypes
 
 import numpy as np
 import pytest
 
+import fallback_scales as FS
 from ccake_gb300 import api, eos_table, ics
 import oracle_py as O
 
 pytestmark = pytest.mark.gpu
 
 NT, NMU = 76, 21
+TANH = 1
 
 
 def relerr(a, b, floor=1e-6):
@@ -27,8 +32,36 @@ def relerr(a, b, floor=1e-6):
 @pytest.fixture(scope="module")
 def table():
     n, lo, d, f = eos_table.synthetic_table(nT=NT, nmu=NMU)
-    conf5, cdiag5 = eos_table.fallback_scales()
+    conf5, cdiag5 = FS.reference_fallback_scales(n, lo, d, f, ics.RunConfig().freeze_out_T)
     return n, lo, d, f, conf5, cdiag5
+
+
+def test_fallback_scales_match_the_reference_rule(table):
+    n, lo, d, f, conf5, cdiag5 = table
+    c5, d5 = api.table_fallback_scales(n, lo, d, f, ics.RunConfig().freeze_out_T)
+    assert np.allclose(c5, conf5, rtol=1e-13) and np.allclose(d5, cdiag5, rtol=1e-13)
+    # the context matches them itself when none are given
+    rc = ics.RunConfig(eos_kind=2, thermo_mode=1)
+    g1, g2 = api.GpuHydro(rc), api.GpuHydro(rc)
+    g1.set_eos_table(n, lo, d, f)
+    g2.set_eos_table(*table)
+    x = np.array([[3.0, 0.2, 0.1, -0.1], [5.0, 1.0, 0.3, 0.2]])
+    for k in (1, 2, 3):
+        assert np.array_equal(g1.eos_thermo(k, x), g2.eos_thermo(k, x)), k
+
+
+def test_tanh_conformal_thermo_parity(table):
+    rc = ics.RunConfig(eos_kind=2, thermo_mode=1)
+    g = gpu_with_table(rc, table)
+    ot = O.OracleTable(*table)
+    cfg = O.make_config(rc)
+    rng = np.random.default_rng(17)
+    x = np.column_stack([rng.uniform(0.1, 8.0, 500), rng.uniform(-2, 2, (500, 3))])
+    og = g.eos_thermo(TANH, x)
+    for i in range(x.shape[0]):
+        o = np.zeros(17)
+        O.lib().orc_eos_full_thermo(ctypes.byref(cfg), ot.h, TANH, O._dp(x[i].copy()), O._dp(o))
+        assert np.allclose(og[i], o, rtol=1e-12, atol=1e-13 * np.abs(o).max()), i
 
 
 def gpu_with_table(rc, table):
@@ -125,9 +158,17 @@ def test_table_inversion_statuses_across_the_unstable_band(table):
     fw = g.eos_thermo(0, x)
     tgt = np.column_stack([fw[:, 5], fw[:, 2], fw[:, 3], fw[:, 4]])
     seeds = np.tile([580 / 197.3269804, 0, 0, 0], (x.shape[0], 1))
-    _, _, sto, _ = O.eos_invert_batch(rc, 0, tgt, seeds=seeds, table=ot)
-    _, _, stg, _ = g.eos_invert(0, tgt, seeds)
+    xo, tho, sto, _ = O.eos_invert_batch(rc, 0, tgt, seeds=seeds, table=ot)
+    xg, thg, stg, _ = g.eos_invert(0, tgt, seeds)
     assert np.mean(stg == sto) > 0.995
+    # rows the table rejects land on the tanh-conformal stage in both, with
+    # the same roots and thermodynamics there
+    tanh = (stg == TANH) & (sto == TANH)
+    assert tanh.sum() >= 10 and tanh.sum() >= 0.99 * np.count_nonzero((stg == TANH) | (sto == TANH))
+    assert relerr(xg[tanh, 0], xo[tanh, 0]) < 1e-10
+    assert np.max(np.abs(xg[tanh, 1:] - xo[tanh, 1:])) < 1e-10
+    for c in (4, 5, 9, 10, 11):
+        assert relerr(thg[tanh, c], tho[tanh, c]) < 1e-10, c
 
 
 def hot_table_event():
