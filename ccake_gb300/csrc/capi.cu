@@ -228,7 +228,45 @@ void enqueue_passB(ccake_ctx* ctx, int mode, double dt_sub) {
 // Cell list and candidate list at the current positions.
 void enqueue_build(ccake_ctx* ctx) {
   launch_build_cells(ctx->rc, ctx->p, ctx->stream);
+  cudaMemsetAsync(ctx->p.cand_max, 0, sizeof(int32_t), ctx->stream);
   launch_candidates(ctx->rc, ctx->p, ctx->stream);
+}
+
+// List capacity for a count: 1.25x plus 16, in multiples of 16.
+int capacity_for(int count) { return ((count * 5 / 4 + 16) + 15) / 16 * 16; }
+
+// After a candidate build: when the largest candidate count exceeds the
+// capacity of the candidate list (entries past it were dropped) or of the
+// neighbour list (the neighbours of a particle are among its candidates), the
+// lists are reallocated larger and built again. Particles that crowd together
+// (compressing flows) thus never overflow the lists; the reference's Verlet
+// list has no fixed capacity either. The graphs that hold the old pointers
+// are dropped and captured again at their next use.
+ccake_status_t grow_lists(ccake_ctx* ctx) {
+  for (int attempt = 0; attempt < 4; attempt++) {
+    int32_t mx = 0;
+    CK(cudaMemcpyAsync(&mx, ctx->p.cand_max, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (mx <= ctx->p.Kc && mx <= ctx->p.K) return CCAKE_OK;
+    drop_graph(ctx);
+    if (mx > ctx->p.Kc) {
+      const int Kc = capacity_for(mx);
+      free_candidates(ctx);
+      if (cudaMalloc(&ctx->p.cand_idx, (size_t)Kc * ctx->n * sizeof(int32_t)) != cudaSuccess)
+        return fail(ctx, CCAKE_ERR_NOMEM, "candidate list allocation");
+      ctx->p.Kc = Kc;
+    }
+    if (mx > ctx->p.K) {
+      const int K = capacity_for(mx);
+      free_lists(ctx);
+      if (cudaMalloc(&ctx->p.nbr_idx, (size_t)K * ctx->n * sizeof(int32_t)) != cudaSuccess ||
+          cudaMalloc(&ctx->p.nbr_f, (size_t)K * ctx->n * sizeof(double)) != cudaSuccess)
+        return fail(ctx, CCAKE_ERR_NOMEM, "neighbour list allocation");
+      ctx->p.K = K;
+    }
+    enqueue_build(ctx);
+  }
+  return fail(ctx, CCAKE_ERR_CAPACITY, "candidate list did not settle");
 }
 
 // Steps a candidate list stays valid from time tau: a particle moves at most
@@ -256,6 +294,8 @@ ccake_status_t maybe_rebuild(ccake_ctx* ctx, bool graph) {
   } else {
     enqueue_build(ctx);
   }
+  ccake_status_t s = grow_lists(ctx);
+  if (s) return s;
   ctx->lists_valid = true;
   ctx->steps_since_build = 0;
   return CCAKE_OK;
@@ -283,6 +323,18 @@ void enqueue_substep(ccake_ctx* ctx, int sub) {
   enqueue_passB(ctx, mode, sub == 1 ? 0.5 * dt : dt);
   launch_clock(ctx->p, sub, dt, ctx->stream);
   if (sub == 2 && ctx->cfg.particlization) enqueue_freeze(ctx);
+}
+
+// Captures the RK2 step graph (two substeps) if it is not held.
+ccake_status_t ensure_step_graph(ccake_ctx* ctx) {
+  if (ctx->graph_exec) return CCAKE_OK;
+  CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  enqueue_substep(ctx, 1);
+  enqueue_substep(ctx, 2);
+  CK(cudaStreamEndCapture(ctx->stream, &ctx->graph));
+  CK(cudaGraphInstantiate(&ctx->graph_exec, ctx->graph, 0));
+  ctx->step_kernels = kernel_nodes(ctx->graph);
+  return CCAKE_OK;
 }
 
 struct FieldRef {
@@ -439,17 +491,9 @@ namespace ccake_internal {
 ccake_status_t step_enqueue(ccake_ctx* ctx, int n) {
   if (!ctx || !ctx->initialized || n < 0) return CCAKE_ERR_STATE;
   ensure_records(ctx, ctx->cfg.precision);
-  if (!ctx->graph_exec) {
-    CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-    enqueue_substep(ctx, 1);
-    enqueue_substep(ctx, 2);
-    CK(cudaStreamEndCapture(ctx->stream, &ctx->graph));
-    CK(cudaGraphInstantiate(&ctx->graph_exec, ctx->graph, 0));
-    ctx->step_kernels = kernel_nodes(ctx->graph);
-  }
   ccake_status_t s;
   for (int k = 0; k < n; k++) {
-    if ((s = maybe_rebuild(ctx, true))) return s;
+    if ((s = maybe_rebuild(ctx, true)) || (s = ensure_step_graph(ctx))) return s;
     CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
     ctx->launches += ctx->step_kernels;
     ctx->steps_since_build++;
@@ -610,7 +654,7 @@ ccake_status_t ccake_load_particles(ccake_ctx* ctx, const ccake_particles_soa* h
   std::stable_sort(ctx->perm.begin(), ctx->perm.end(), [&](int32_t a, int32_t b) { return key[a] < key[b]; });
   // device memory: one double slab, one int slab
   const size_t nd = (size_t)n * kDoublesPerParticle + (size_t)kTotBlocks * 6 + 8;
-  const size_t ni = (size_t)n * 8 + (size_t)g.ncell * 2 + 1 + NERR + 2 * (size_t)scan_tiles(g.ncell) + 1 + 8;
+  const size_t ni = (size_t)n * 8 + (size_t)g.ncell * 2 + 1 + NERR + 1 + 2 * (size_t)scan_tiles(g.ncell) + 1 + 8;
   if (cudaMalloc(&ctx->dbuf, nd * sizeof(double)) != cudaSuccess) return fail(ctx, CCAKE_ERR_NOMEM, "device allocation");
   if (cudaMalloc(&ctx->ibuf, ni * sizeof(int32_t)) != cudaSuccess) return fail(ctx, CCAKE_ERR_NOMEM, "device allocation");
   CK(cudaMemsetAsync(ctx->dbuf, 0, nd * sizeof(double), ctx->stream));
@@ -637,7 +681,7 @@ ccake_status_t ccake_load_particles(ccake_ctx* ctx, const ccake_particles_soa* h
   auto itake = [&](size_t k) { int32_t* r = ip; ip += k; return r; };
   p.eos_id = itake(n); p.eos_iters = itake(n); p.btrack = itake(n); p.freeze = itake(n);
   p.cell_of = itake(n); p.cell_rank = itake(n); p.cell_idx = itake(n); p.cand_cnt = itake(n);
-  p.cell_count = itake(g.ncell); p.cell_start = itake(g.ncell + 1); p.err = itake(NERR);
+  p.cell_count = itake(g.ncell); p.cell_start = itake(g.ncell + 1); p.err = itake(NERR); p.cand_max = itake(1);
   p.scan_aux = itake(2 * (size_t)scan_tiles(g.ncell) + 1);
   // upload permuted inputs
   std::vector<double> tmp((size_t)n);
@@ -812,16 +856,9 @@ ccake_status_t ccake_step(ccake_ctx* ctx, int32_t n_steps) {
   ccake_status_t s = reset_errors(ctx);
   if (s) return s;
   ensure_records(ctx, ctx->cfg.precision);
-  if (!ctx->graph_exec) {
-    CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-    enqueue_substep(ctx, 1);
-    enqueue_substep(ctx, 2);
-    CK(cudaStreamEndCapture(ctx->stream, &ctx->graph));
-    CK(cudaGraphInstantiate(&ctx->graph_exec, ctx->graph, 0));
-    ctx->step_kernels = kernel_nodes(ctx->graph);
-  }
+  if ((s = ensure_step_graph(ctx))) return s;
   for (int k = 0; k < n_steps; k++) {
-    if ((s = maybe_rebuild(ctx, true))) return s;
+    if ((s = maybe_rebuild(ctx, true)) || (s = ensure_step_graph(ctx))) return s;
     CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
     ctx->launches += ctx->step_kernels;
     ctx->steps_since_build++;
@@ -844,7 +881,7 @@ ccake_status_t ccake_step_timed(ccake_ctx* ctx, int32_t n_steps, float* device_m
   CK(cudaEventCreate(&e1));
   CK(cudaEventRecord(e0, ctx->stream));
   for (int k = 0; k < n_steps; k++) {
-    if ((s = maybe_rebuild(ctx, true))) return s;
+    if ((s = maybe_rebuild(ctx, true)) || (s = ensure_step_graph(ctx))) return s;
     CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
     ctx->launches += ctx->step_kernels;
     ctx->steps_since_build++;

@@ -196,17 +196,20 @@ __global__ void k_sort_cells(Ptrs p, int ncell) {
 // Candidate (Verlet) list of particle i: every b != i in the 3^D cells around
 // it whose FP32 squared distance is not above (2h + skin)^2 by more than its
 // error bound (so no pair within 2h + skin in FP64 is dropped), in cell order.
-// With Kc = 0 it only counts.
+// With Kc = 0 it only counts. The largest count goes to cand_max (zeroed
+// before the build): the host grows the capacities when it exceeds them and
+// builds again, so no entry past Kc is ever used.
 template <int D>
 __global__ void __launch_bounds__(kBlock) k_candidates(RunConst rc, Ptrs p) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= p.n) return;
+  const int i_ = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool live = i_ < p.n;
+  const int i = live ? i_ : 0;
   const int n = p.n;
   const double xa[3] = {p.y[Y_X0 * n + i], p.y[Y_X1 * n + i], D == 3 ? p.y[Y_X2 * n + i] : 0.0};
   const float4 pa = p.posf[i];
   const float cut2f = rc.fcutc2 * 1.000001f;
   int rlo[D == 3 ? 9 : 3], rhi[D == 3 ? 9 : 3];
-  const int nr = neighbour_ranges<D>(rc.grid, p.cell_start, xa, rlo, rhi);
+  const int nr = live ? neighbour_ranges<D>(rc.grid, p.cell_start, xa, rlo, rhi) : 0;
   const int Kc = p.Kc;
   int c = 0;
   for (int r = 0; r < nr; r++)
@@ -218,8 +221,11 @@ __global__ void __launch_bounds__(kBlock) k_candidates(RunConst rc, Ptrs p) {
       if (c < Kc) p.cand_idx[(size_t)c * n + i] = b;
       c++;
     }
-  if (c > Kc && Kc > 0) flag_error(p.err, E_NBR_OVERFLOW);
-  p.cand_cnt[i] = c;
+  // every lane reaches the warp reduction; lanes past the end count 0
+  if (!live) c = 0;
+  const int wmax = __reduce_max_sync(0xffffffffu, c);
+  if ((threadIdx.x & 31) == 0 && p.cand_max) atomicMax(p.cand_max, wmax);
+  if (live) p.cand_cnt[i] = c;
 }
 
 // Iterates the 3^D neighbour cells of a position; calls f(b) for every

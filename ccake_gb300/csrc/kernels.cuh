@@ -52,6 +52,7 @@ struct Ptrs {
   // build, k-major like the neighbour list; rebuilt every few steps
   int32_t* cand_idx;     // Kc * n
   int32_t* cand_cnt;     // n
+  int32_t* cand_max;     // 1: the largest candidate count of the last build
   int Kc;
   // mixed-precision form (precision = 1): FP32 neighbour records
   float* recAf;          // RAF * n
