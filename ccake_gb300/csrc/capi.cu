@@ -70,6 +70,14 @@ struct ccake_ctx {
   int init_bulk = 0, init_shear = 0;
   // initial diffusion currents (ccake_set_initial_diffusion): q^i of charge c at row 3c + i
   double* init_q = nullptr;
+  // the mixed form's step kernels are grouped launches (EventSlot); alone, the
+  // event is a group of one: its slot and block map on the device, and the
+  // host copy last uploaded
+  EventSlot* d_slot = nullptr;
+  int2* d_map = nullptr;
+  int nblk = 0;
+  EventSlot h_slot{};
+  bool slot_up = false;
 };
 
 namespace {
@@ -140,6 +148,12 @@ void free_buffers(ccake_ctx* ctx) {
   if (ctx->init_visc) cudaFree(ctx->init_visc);
   if (ctx->init_q) cudaFree(ctx->init_q);
   ctx->init_visc = ctx->init_q = nullptr;
+  if (ctx->d_slot) cudaFree(ctx->d_slot);
+  if (ctx->d_map) cudaFree(ctx->d_map);
+  ctx->d_slot = nullptr;
+  ctx->d_map = nullptr;
+  ctx->nblk = 0;
+  ctx->slot_up = false;
   ctx->init_bulk = ctx->init_shear = 0;
   ctx->dbuf = nullptr;
   ctx->ibuf = nullptr;
@@ -215,14 +229,41 @@ void ensure_records(ccake_ctx* ctx, int form) {
   ctx->records_form = form;
 }
 
+// The event's slot for the grouped mixed kernels (a group of one), uploaded
+// when it differs from the copy on the device. Called before the mixed form's
+// kernels are launched or captured.
+ccake_status_t sync_slot(ccake_ctx* ctx) {
+  if (!ctx->d_slot) return fail(ctx, CCAKE_ERR_STATE, "load particles first");
+  EventSlot h;
+  std::memset(&h, 0, sizeof(h));
+  h.rc = ctx->rc;
+  h.eos = ctx->eos;
+  h.eos.jac32 = 1;   // table Newton Jacobians in FP32 (the residual stays FP64)
+  h.p = ctx->p;
+  h.tau_max = 1e300;
+  h.active = 1;
+  if (ctx->slot_up && std::memcmp(&h, &ctx->h_slot, sizeof(h)) == 0) return CCAKE_OK;
+  ctx->h_slot = h;
+  CK(cudaMemcpyAsync(ctx->d_slot, &ctx->h_slot, sizeof(EventSlot), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->slot_up = true;
+  return CCAKE_OK;
+}
+
 void enqueue_passA(ccake_ctx* ctx) {
-  if (ctx->cfg.precision == 1) launch_passA_mixed(ctx->rc, ctx->eos, ctx->p, ctx->stream);
+  if (ctx->cfg.precision == 1) launch_passA_mixed(ctx->d_slot, ctx->d_map, ctx->nblk, ctx->cfg.dim, ctx->stream);
   else launch_passA(ctx->rc, ctx->eos, ctx->p, A_WITH_THERMO, ctx->stream);
 }
 
-void enqueue_passB(ccake_ctx* ctx, int mode, double dt_sub) {
-  if (ctx->cfg.precision == 1) launch_passB_mixed(ctx->rc, ctx->p, mode, dt_sub, ctx->stream);
-  else launch_passB(ctx->rc, ctx->p, mode, dt_sub, ctx->stream);
+void enqueue_passB(ccake_ctx* ctx, int mode, int sub) {
+  if (ctx->cfg.precision == 1)
+    launch_passB_mixed(ctx->d_slot, ctx->d_map, ctx->nblk, ctx->cfg.dim, mode, sub, ctx->stream);
+  else launch_passB(ctx->rc, ctx->p, mode, sub == 1 ? 0.5 * ctx->cfg.dt : ctx->cfg.dt, ctx->stream);
+}
+
+void enqueue_clock(ccake_ctx* ctx, int sub) {
+  if (ctx->cfg.precision == 1) launch_clock_group(ctx->d_slot, 1, sub, ctx->stream);
+  else launch_clock(ctx->p, sub, ctx->cfg.dt, ctx->stream);
 }
 
 // Cell list and candidate list at the current positions.
@@ -307,27 +348,30 @@ void enqueue_freeze(ccake_ctx* ctx) {
     // gradients, theta and shv_nabla_u of the evaluation just done, then the
     // status machine with snapshots and hypersurface rows
     const int mixed = ctx->cfg.precision == 1 ? 1 : 0;
-    if (mixed) launch_gradients_mixed(ctx->rc, ctx->p, ctx->stream);
+    if (mixed) launch_gradients_mixed(ctx->d_slot, ctx->d_map, ctx->nblk, ctx->cfg.dim, ctx->stream);
     else launch_passB(ctx->rc, ctx->p, B_GRADS, 0.0, ctx->stream);
     launch_diagnostics(ctx->rc, ctx->p, mixed, ctx->stream);
     launch_freeze_surface(ctx->rc, ctx->p, mixed, ctx->cfg.dt, ctx->stream);
+  } else if (ctx->cfg.precision == 1) {
+    launch_freeze_group(ctx->d_slot, ctx->d_map, ctx->nblk, 1, ctx->stream);
   } else {
     launch_freeze(ctx->rc, ctx->p, ctx->stream);
   }
 }
 
 void enqueue_substep(ccake_ctx* ctx, int sub) {
-  const double dt = ctx->cfg.dt;
   enqueue_passA(ctx);
-  int mode = B_EOM | B_UPDATE | (sub == 2 ? B_WRITE_Y0 : 0);
-  enqueue_passB(ctx, mode, sub == 1 ? 0.5 * dt : dt);
-  launch_clock(ctx->p, sub, dt, ctx->stream);
+  enqueue_passB(ctx, B_EOM | B_UPDATE | (sub == 2 ? B_WRITE_Y0 : 0), sub);
+  enqueue_clock(ctx, sub);
   if (sub == 2 && ctx->cfg.particlization) enqueue_freeze(ctx);
 }
 
-// Captures the RK2 step graph (two substeps) if it is not held.
+// Captures the RK2 step graph (two substeps) if it is not held; the mixed
+// form's slot is made current first (its kernels read it when they run).
 ccake_status_t ensure_step_graph(ccake_ctx* ctx) {
   if (ctx->graph_exec) return CCAKE_OK;
+  ccake_status_t s;
+  if (ctx->cfg.precision == 1 && (s = sync_slot(ctx))) return s;
   CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
   enqueue_substep(ctx, 1);
   enqueue_substep(ctx, 2);
@@ -490,6 +534,8 @@ namespace ccake_internal {
 
 ccake_status_t step_enqueue(ccake_ctx* ctx, int n) {
   if (!ctx || !ctx->initialized || n < 0) return CCAKE_ERR_STATE;
+  ccake_status_t st;
+  if (ctx->cfg.precision == 1 && (st = sync_slot(ctx))) return st;
   ensure_records(ctx, ctx->cfg.precision);
   ccake_status_t s;
   for (int k = 0; k < n; k++) {
@@ -511,6 +557,50 @@ ccake_status_t clear_errors(ccake_ctx* ctx) { return reset_errors(ctx); }
 
 cudaStream_t ctx_stream(ccake_ctx* ctx) { return ctx->stream; }
 void ctx_set_time(ccake_ctx* ctx, double t) { ctx->t = t; }
+
+void fill_slot(ccake_ctx* ctx, EventSlot* out) {
+  std::memset(out, 0, sizeof(EventSlot));
+  out->rc = ctx->rc;
+  out->eos = ctx->eos;
+  out->eos.jac32 = 1;
+  out->p = ctx->p;
+  out->tau_max = 1e300;
+  out->tau = ctx->t;
+  out->active = 1;
+}
+
+int list_period(ccake_ctx* ctx) { return build_every(ctx, ctx->t); }
+
+ccake_status_t group_join(ccake_ctx* ctx) {
+  ccake_status_t s = reset_errors(ctx);
+  if (s) return s;
+  ensure_records(ctx, 1);
+  CK(cudaStreamSynchronize(ctx->stream));
+  return CCAKE_OK;
+}
+
+void group_build(ccake_ctx* ctx, cudaStream_t s, int32_t* host_cand_max) {
+  launch_build_cells(ctx->rc, ctx->p, s);
+  cudaMemsetAsync(ctx->p.cand_max, 0, sizeof(int32_t), s);
+  launch_candidates(ctx->rc, ctx->p, s);
+  cudaMemcpyAsync(host_cand_max, ctx->p.cand_max, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+}
+
+ccake_status_t group_grow(ccake_ctx* ctx, int32_t cand_max, bool* changed) {
+  *changed = false;
+  if (cand_max <= ctx->p.Kc && cand_max <= ctx->p.K) return CCAKE_OK;
+  *changed = true;
+  // the build just done left cand_max on the device: grow_lists reads it,
+  // reallocates and builds again on the context's stream
+  return grow_lists(ctx);
+}
+
+void group_leave(ccake_ctx* ctx, double tau) {
+  ctx->t = tau;
+  ctx->records_form = 1;
+  ctx->lists_valid = false;   // stepped alone later, it builds its lists first
+  ctx->evaluated = true;
+}
 
 int64_t estimate_bytes(const ccake_config& cfg, int64_t n) {
   // state and records, plus neighbour and candidate lists at the lattice
@@ -706,6 +796,18 @@ ccake_status_t ccake_load_particles(ccake_ctx* ctx, const ccake_particles_soa* h
       (s = up(h->e_or_s, p.in_e)) || (s = up(h->rhoB, p.in_rho)) || (s = up(h->rhoS, p.in_rho + n)) ||
       (s = up(h->rhoQ, p.in_rho + 2 * n)))
     return s;
+  // the event's slot and block map for the grouped mixed kernels
+  ctx->nblk = (int)((n + kBlock - 1) / kBlock);
+  if (cudaMalloc(&ctx->d_slot, sizeof(EventSlot)) != cudaSuccess ||
+      cudaMalloc(&ctx->d_map, (size_t)ctx->nblk * sizeof(int2)) != cudaSuccess)
+    return fail(ctx, CCAKE_ERR_NOMEM, "device allocation");
+  {
+    std::vector<int2> map((size_t)ctx->nblk);
+    for (int b = 0; b < ctx->nblk; b++) map[b] = make_int2(0, b * kBlock);
+    CK(cudaMemcpyAsync(ctx->d_map, map.data(), map.size() * sizeof(int2), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  ctx->slot_up = false;
   ctx->loaded = true;
   ctx->initialized = false;
   return CCAKE_OK;
@@ -855,6 +957,7 @@ ccake_status_t ccake_step(ccake_ctx* ctx, int32_t n_steps) {
   if (!ctx->initialized) return fail(ctx, CCAKE_ERR_STATE, "initialize first");
   ccake_status_t s = reset_errors(ctx);
   if (s) return s;
+  if (ctx->cfg.precision == 1 && (s = sync_slot(ctx))) return s;
   ensure_records(ctx, ctx->cfg.precision);
   if ((s = ensure_step_graph(ctx))) return s;
   for (int k = 0; k < n_steps; k++) {
@@ -914,17 +1017,17 @@ ccake_status_t ccake_profile_phases(ccake_ctx* ctx, int32_t n_steps, double* ms3
   cudaEvent_t ev[4];
   for (int q = 0; q < 4; q++) CK(cudaEventCreate(&ev[q]));
   double acc[3] = {0, 0, 0};
-  const double dt = ctx->cfg.dt;
   for (int k = 0; k < n_steps; k++) {
     for (int sub = 1; sub <= 2; sub++) {
       CK(cudaEventRecord(ev[0], ctx->stream));
       if (sub == 1 && (s = maybe_rebuild(ctx, false))) return s;
+      if (ctx->cfg.precision == 1 && (s = sync_slot(ctx))) return s;   // the lists may have grown
       CK(cudaEventRecord(ev[1], ctx->stream));
       enqueue_passA(ctx);
       CK(cudaEventRecord(ev[2], ctx->stream));
-      enqueue_passB(ctx, B_EOM | B_UPDATE | (sub == 2 ? B_WRITE_Y0 : 0), sub == 1 ? 0.5 * dt : dt);
+      enqueue_passB(ctx, B_EOM | B_UPDATE | (sub == 2 ? B_WRITE_Y0 : 0), sub);
       CK(cudaEventRecord(ev[3], ctx->stream));
-      launch_clock(ctx->p, sub, dt, ctx->stream);
+      enqueue_clock(ctx, sub);
       if (sub == 2 && ctx->cfg.particlization) enqueue_freeze(ctx);
       if (sub == 2) ctx->steps_since_build++;
       CK(cudaEventSynchronize(ev[3]));
@@ -1546,7 +1649,9 @@ ccake_status_t ccake_hydro_numbers(ccake_ctx* ctx) {
   // evaluation run again from its records and neighbour list (unchanged since),
   // then the equations of motion from the stored inputs
   const int mixed = ctx->records_form == 1 ? 1 : 0;
-  if (mixed) launch_gradients_mixed(ctx->rc, ctx->p, ctx->stream);
+  ccake_status_t st;
+  if (mixed && (st = sync_slot(ctx))) return st;
+  if (mixed) launch_gradients_mixed(ctx->d_slot, ctx->d_map, ctx->nblk, ctx->cfg.dim, ctx->stream);
   else launch_passB(ctx->rc, ctx->p, B_GRADS, 0.0, ctx->stream);
   launch_diagnostics(ctx->rc, ctx->p, mixed, ctx->stream);
   return check_errors(ctx);

@@ -542,10 +542,7 @@ __global__ void k_visc(RunConst rc, Ptrs p) {
   p.derivs[D_TAUBULK * n + i] = k.tau_Pi;
 }
 
-__global__ void k_clock(Clock* c, int substep, double dt) {
-  if (substep == 1) c->t = c->teval = c->t0 + 0.5 * dt;
-  else { c->t = c->t0 + dt; c->t0 = c->t; }
-}
+__global__ void k_clock(Clock* c, int substep, double dt) { advance_clock(c, substep, dt); }
 
 // ---------------------------------------------------------------------------
 // initialisation (reference src/sph_workstation.cpp:252-375, :1228-1340)
@@ -848,34 +845,7 @@ __global__ void __launch_bounds__(1024) k_probe(Ptrs p, Probe* out) {
 // back to 0; from the third step on, particles without neighbours freeze
 // (freeze_out_evo :322-375), status 3 becomes 4 (:914) and the energy of
 // the live particles is snapshotted.
-__global__ void k_freeze(RunConst rc, Ptrs p) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= p.n) return;
-  const int frzc = p.clock->frzc;
-  const double ef = rc.efreeze;
-  const double e = p.th[T_E * p.n + i];
-  int f = p.freeze[i];
-  if (f == 0) {
-    if (e <= ef) f = 1;
-  } else if (f == 1) {
-    if (p.btrack[i] == -1) f = 3;
-    else if (e > p.frz1_e[i]) f = 1;
-    else if (e <= ef) f = 3;
-    else f = 0;
-  }
-  if (frzc == 1) {
-    p.frz1_e[i] = e;
-    if (f == 3) f = 4;   // bsqsvinterpolate in the second step (:559-566)
-  } else if (frzc >= 2) {
-    if (f < 4 && p.btrack[i] == 0) {
-      f = 4;
-      p.btrack[i] = -1;
-    }
-    if (f == 3) f = 4;
-    if (f < 4) p.frz1_e[i] = e;
-  }
-  p.freeze[i] = f;
-}
+__global__ void k_freeze(RunConst rc, Ptrs p) { freeze_particle(rc, p, blockIdx.x * blockDim.x + threadIdx.x); }
 
 // The freeze-out stage with the hypersurface (cfg.surface), after a step:
 // check_freeze_out_status (include/freeze_out.h:455-500) and bsqsvfreezeout

@@ -5,6 +5,10 @@
 
 namespace ccake {
 
+// Threads a block of the per-particle kernels (also the block size of the
+// grouped launches' per-event block decomposition).
+constexpr int kBlock = 128;
+
 // Device pointers of one event (struct-of-arrays slabs of length n).
 struct Ptrs {
   int n;
@@ -62,6 +66,26 @@ struct Ptrs {
   double* recQ;          // RQ * n   neighbour record of the diffusion sums
 };
 
+// One event of a grouped launch (the mixed form's step kernels): its
+// constants, EoS and device arrays, copied into shared memory by each block
+// that works on it. A grouped launch covers the blocks of every event of a
+// group: block b works on event map[b].x, particles map[b].y onwards (kBlock
+// of them, the event's own block decomposition), so each event runs the same
+// code on the same particles as when it is launched alone, and gives the same
+// bits. active = 0 (the device-side stop rule fired, or the event failed):
+// its blocks return at once.
+struct alignas(16) EventSlot {
+  RunConst rc;
+  EosDev eos;
+  Ptrs p;
+  double tau_max;        // stop rule: no step starts at tau >= tau_max - dt/2
+  double tau;            // tau at the last stop-rule check
+  int32_t active;
+  int32_t frozen_stop;   // 1: stopped because every particle froze out
+  int32_t steps;         // RK2 steps taken (counted by the substep-2 clock)
+  int32_t status;        // ccake_status_t of a failure seen by the stop rule
+};
+
 // Mixed-precision neighbour records. A position x is carried as the float
 // pair (hi, lo), hi = fl(x), lo = fl(x - hi), so a difference of nearby
 // positions keeps full FP32 precision. Record B (96 bytes) and the 3-D record
@@ -100,8 +124,19 @@ void launch_neighbour_fill(const RunConst& rc, const Ptrs& p, const int32_t* off
                            cudaStream_t s);
 void launch_pack_fp64(const RunConst& rc, const Ptrs& p, cudaStream_t s);
 void launch_pack_mixed(const RunConst& rc, const Ptrs& p, cudaStream_t s);
-void launch_passA_mixed(const RunConst& rc, const EosDev& eos, const Ptrs& p, cudaStream_t s);
-void launch_passB_mixed(const RunConst& rc, const Ptrs& p, int mode, double dt_sub, cudaStream_t s);
+// The mixed form's step kernels as grouped launches over slots[0..nev) with
+// the block map map[0..nblocks) (see EventSlot): pass A (smoothing sums and
+// neighbour list, then the FP64 EoS), pass B (gradient sums, then the
+// equations of motion and the RK2 update of substep `sub`, dt from each
+// event's config), the clock, the freeze-out status machine, and the stop
+// rule (before a step: retire events that are all frozen out with
+// particlization, that reached tau_max, or that raised an error).
+void launch_passA_mixed(const EventSlot* slots, const int2* map, int nblocks, int dim, cudaStream_t s);
+void launch_passB_mixed(const EventSlot* slots, const int2* map, int nblocks, int dim, int mode, int sub,
+                        cudaStream_t s);
+void launch_clock_group(EventSlot* slots, int nev, int sub, cudaStream_t s);
+void launch_freeze_group(EventSlot* slots, const int2* map, int nblocks, int nev, cudaStream_t s);
+void launch_stop_group(EventSlot* slots, int nev, cudaStream_t s);
 void launch_eos_thermo(const EosDev& eos, int chain_index, int64_t n, const double* tbqs, double* out17,
                        cudaStream_t s);
 // Batch inversion. With scratch (n + 1 int32, device) and seed_mode 0 or 2,
@@ -118,7 +153,7 @@ void launch_diagnostics(const RunConst& rc, const Ptrs& p, int grads_f32, cudaSt
 // status machine, snapshots and hypersurface rows after a step (cfg.surface)
 void launch_freeze_surface(const RunConst& rc, const Ptrs& p, int grads_f32, double dt, cudaStream_t s);
 // the gradient sums of the mixed pass B alone (no equations of motion)
-void launch_gradients_mixed(const RunConst& rc, const Ptrs& p, cudaStream_t s);
+void launch_gradients_mixed(const EventSlot* slots, const int2* map, int nblocks, int dim, cudaStream_t s);
 void launch_eos_batch(const EosDev& eos, int entropy, int seed_mode, int64_t n, const double* in4, double* tbqs,
                       double* th16, int32_t* status, int32_t* iters, int32_t* scratch, cudaStream_t s);
 

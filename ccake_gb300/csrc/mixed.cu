@@ -52,12 +52,11 @@ __global__ void k_pack_mixed(Ptrs p) {
 constexpr int kRing = 16, kCheck = 4;
 
 template <int D>
-__global__ void __launch_bounds__(kBlock) k_passA_mixed(RunConst rc, Ptrs p) {
+__device__ __forceinline__ void passA_mixed_body(const RunConst& rc, const Ptrs& p, const int i_) {
   constexpr bool kStage = (D == 3);
   // every lane of a warp takes part in the warp-wide staging below: lanes
   // past the end stay in with no candidates and write nothing
   const int n = p.n;
-  const int i_ = blockIdx.x * blockDim.x + threadIdx.x;
   const bool live = i_ < n;
   const int i = live ? i_ : n - 1;
   const double t = p.clock->t;
@@ -195,8 +194,7 @@ __global__ void __launch_bounds__(kBlock) k_passA_mixed(RunConst rc, Ptrs p) {
 // FP64 Newton solve needs ~255 registers a thread, which would cap the
 // occupancy of the gather loop above at 8 warps an SM.
 template <int D>
-__global__ void __launch_bounds__(kBlock) k_thermo_mixed(RunConst rc, EosDev eos, Ptrs p) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void thermo_mixed_body(const RunConst& rc, const EosDev& eos, const Ptrs& p, const int i) {
   if (i >= p.n) return;
   thermo_tail<D, true>(rc, eos, p, i, p.clock->t);
 }
@@ -209,8 +207,7 @@ __global__ void __launch_bounds__(kBlock) k_thermo_mixed(RunConst rc, EosDev eos
 // registers a thread instead of ~170 and keeps enough warps in flight to
 // cover its gather latency.
 template <int D>
-__global__ void __launch_bounds__(kBlock) k_passB_mixed(RunConst rc, Ptrs p) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void passB_mixed_body(const RunConst& rc, const Ptrs& p, const int i) {
   if (i >= p.n) return;
   const int n = p.n;
   const bool shear = rc.cfg.using_shear;
@@ -356,8 +353,8 @@ __global__ void __launch_bounds__(kBlock) k_passB_mixed(RunConst rc, Ptrs p) {
 // Pass B, mixed form, part 2: FP32 equations of motion from the gradients of
 // part 1, FP64 RK2 update, mixed smoothing record for the next substep.
 template <int D>
-__global__ void __launch_bounds__(kBlock) k_eom_mixed(RunConst rc, Ptrs p, int mode, double dt_sub) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void eom_mixed_body(const RunConst& rc, const Ptrs& p, const int i, const int mode,
+                                               const double dt_sub) {
   if (i >= p.n) return;
   const int n = p.n;
   const float* gf = reinterpret_cast<const float*>(p.grads);
@@ -378,6 +375,114 @@ __global__ void __launch_bounds__(kBlock) k_eom_mixed(RunConst rc, Ptrs p, int m
   finish_particle<D, float, true>(rc, p, i, mode & ~B_GRADS, p.clock->t, dt_sub, va, gP, gE, gB, gS, dS, gV);
 }
 
+// ---------------------------------------------------------------------------
+// grouped launches: one launch covers every event of a group (see EventSlot)
+// ---------------------------------------------------------------------------
+static_assert(sizeof(EventSlot) % 16 == 0, "EventSlot is copied as int4");
+
+// Copies the block's event slot into shared memory and returns it, or null
+// when the event is retired; first = the block's first particle.
+__device__ __forceinline__ const EventSlot* enter_group(const EventSlot* __restrict__ slots,
+                                                        const int2* __restrict__ map, int& first) {
+  __shared__ __align__(16) unsigned char raw[sizeof(EventSlot)];
+  const int2 b = map[blockIdx.x];
+  const int4* src = reinterpret_cast<const int4*>(slots + b.x);
+  int4* dst = reinterpret_cast<int4*>(raw);
+  for (int k = threadIdx.x; k < (int)(sizeof(EventSlot) / 16); k += blockDim.x) dst[k] = src[k];
+  __syncthreads();
+  first = b.y;
+  const EventSlot* e = reinterpret_cast<const EventSlot*>(raw);
+  return e->active ? e : nullptr;
+}
+
+template <int D>
+__global__ void __launch_bounds__(kBlock) k_passA_mixed(const EventSlot* slots, const int2* map) {
+  int first;
+  const EventSlot* e = enter_group(slots, map, first);
+  if (!e) return;
+  passA_mixed_body<D>(e->rc, e->p, first + threadIdx.x);
+}
+
+template <int D>
+__global__ void __launch_bounds__(kBlock) k_thermo_mixed(const EventSlot* slots, const int2* map) {
+  int first;
+  const EventSlot* e = enter_group(slots, map, first);
+  if (!e) return;
+  thermo_mixed_body<D>(e->rc, e->eos, e->p, first + threadIdx.x);
+}
+
+template <int D>
+__global__ void __launch_bounds__(kBlock) k_passB_mixed(const EventSlot* slots, const int2* map) {
+  int first;
+  const EventSlot* e = enter_group(slots, map, first);
+  if (!e) return;
+  passB_mixed_body<D>(e->rc, e->p, first + threadIdx.x);
+}
+
+template <int D>
+__global__ void __launch_bounds__(kBlock) k_eom_mixed(const EventSlot* slots, const int2* map, int mode, int sub) {
+  int first;
+  const EventSlot* e = enter_group(slots, map, first);
+  if (!e) return;
+  const double dt = e->rc.cfg.dt;
+  eom_mixed_body<D>(e->rc, e->p, first + threadIdx.x, mode, sub == 1 ? 0.5 * dt : dt);
+}
+
+__global__ void k_clock_group(EventSlot* slots, int nev, int sub) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nev || !slots[k].active) return;
+  advance_clock(slots[k].p.clock, sub, slots[k].rc.cfg.dt);
+  if (sub == 2) slots[k].steps++;
+}
+
+__global__ void __launch_bounds__(kBlock) k_freeze_group(const EventSlot* slots, const int2* map) {
+  int first;
+  const EventSlot* e = enter_group(slots, map, first);
+  if (!e || !e->rc.cfg.particlization) return;
+  freeze_particle(e->rc, e->p, first + threadIdx.x);
+}
+
+__global__ void k_freeze_advance_group(EventSlot* slots, int nev) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nev || !slots[k].active || !slots[k].rc.cfg.particlization) return;
+  Clock* c = slots[k].p.clock;
+  if (c->frzc < 2) c->frzc++;
+}
+
+// The stop rule before a step, one block an event: SPHWorkstation::
+// continue_evolution (src/sph_workstation.cpp:1992-2024: every particle frozen
+// out with particlization), the event's tau_max, and the failures the kernels
+// flagged (the first one decides the status). Idempotent: it may run again
+// with no step in between.
+__global__ void __launch_bounds__(256) k_stop_group(EventSlot* slots) {
+  EventSlot& E = slots[blockIdx.x];
+  if (!E.active) return;
+  const Ptrs& p = E.p;
+  __shared__ int red[8];
+  int frozen = 0;
+  if (E.rc.cfg.particlization)
+    for (int i = threadIdx.x; i < p.n; i += blockDim.x) frozen += p.freeze[i] >= 4 ? 1 : 0;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) frozen += __shfl_xor_sync(0xffffffffu, frozen, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = frozen;
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  frozen = 0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); w++) frozen += red[w];
+  E.tau = p.clock->t;
+  const int first = p.err[E_FIRST] - 1;
+  const int kind[4] = {CCAKE_ERR_EOS, CCAKE_ERR_NEG_ENTROPY, CCAKE_ERR_NONFINITE, CCAKE_ERR_CAPACITY};
+  if (first >= 0 && first < 4) {
+    E.status = kind[first];
+    E.active = 0;
+  } else if (E.rc.cfg.particlization && frozen >= p.n) {
+    E.frozen_stop = 1;
+    E.active = 0;
+  } else if (p.clock->t >= E.tau_max - 0.5 * E.rc.cfg.dt) {
+    E.active = 0;
+  }
+}
+
 }  // namespace
 
 void launch_pack_mixed(const RunConst& rc, const Ptrs& p, cudaStream_t s) {
@@ -386,35 +491,43 @@ void launch_pack_mixed(const RunConst& rc, const Ptrs& p, cudaStream_t s) {
   else k_pack_mixed<2><<<nb, kBlock, 0, s>>>(p);
 }
 
-void launch_passA_mixed(const RunConst& rc, const EosDev& eos, const Ptrs& p, cudaStream_t s) {
-  const int nb = (p.n + kBlock - 1) / kBlock;
-  // table Newton Jacobians in FP32 (the residual and its tolerance stay FP64)
-  EosDev em = eos;
-  em.jac32 = 1;
-  if (rc.cfg.dim == 3) {
-    k_passA_mixed<3><<<nb, kBlock, 0, s>>>(rc, p);
-    k_thermo_mixed<3><<<nb, kBlock, 0, s>>>(rc, em, p);
+// The slots carry the EoS with FP32 table Newton Jacobians (EosDev::jac32;
+// the residual and its tolerance stay FP64).
+void launch_passA_mixed(const EventSlot* slots, const int2* map, int nblocks, int dim, cudaStream_t s) {
+  if (dim == 3) {
+    k_passA_mixed<3><<<nblocks, kBlock, 0, s>>>(slots, map);
+    k_thermo_mixed<3><<<nblocks, kBlock, 0, s>>>(slots, map);
   } else {
-    k_passA_mixed<2><<<nb, kBlock, 0, s>>>(rc, p);
-    k_thermo_mixed<2><<<nb, kBlock, 0, s>>>(rc, em, p);
+    k_passA_mixed<2><<<nblocks, kBlock, 0, s>>>(slots, map);
+    k_thermo_mixed<2><<<nblocks, kBlock, 0, s>>>(slots, map);
   }
 }
 
-void launch_passB_mixed(const RunConst& rc, const Ptrs& p, int mode, double dt_sub, cudaStream_t s) {
-  const int nb = (p.n + kBlock - 1) / kBlock;
-  if (rc.cfg.dim == 3) {
-    k_passB_mixed<3><<<nb, kBlock, 0, s>>>(rc, p);
-    k_eom_mixed<3><<<nb, kBlock, 0, s>>>(rc, p, mode, dt_sub);
+void launch_passB_mixed(const EventSlot* slots, const int2* map, int nblocks, int dim, int mode, int sub,
+                        cudaStream_t s) {
+  if (dim == 3) {
+    k_passB_mixed<3><<<nblocks, kBlock, 0, s>>>(slots, map);
+    k_eom_mixed<3><<<nblocks, kBlock, 0, s>>>(slots, map, mode, sub);
   } else {
-    k_passB_mixed<2><<<nb, kBlock, 0, s>>>(rc, p);
-    k_eom_mixed<2><<<nb, kBlock, 0, s>>>(rc, p, mode, dt_sub);
+    k_passB_mixed<2><<<nblocks, kBlock, 0, s>>>(slots, map);
+    k_eom_mixed<2><<<nblocks, kBlock, 0, s>>>(slots, map, mode, sub);
   }
 }
 
-void launch_gradients_mixed(const RunConst& rc, const Ptrs& p, cudaStream_t s) {
-  const int nb = (p.n + kBlock - 1) / kBlock;
-  if (rc.cfg.dim == 3) k_passB_mixed<3><<<nb, kBlock, 0, s>>>(rc, p);
-  else k_passB_mixed<2><<<nb, kBlock, 0, s>>>(rc, p);
+void launch_gradients_mixed(const EventSlot* slots, const int2* map, int nblocks, int dim, cudaStream_t s) {
+  if (dim == 3) k_passB_mixed<3><<<nblocks, kBlock, 0, s>>>(slots, map);
+  else k_passB_mixed<2><<<nblocks, kBlock, 0, s>>>(slots, map);
 }
+
+void launch_clock_group(EventSlot* slots, int nev, int sub, cudaStream_t s) {
+  k_clock_group<<<(nev + 127) / 128, 128, 0, s>>>(slots, nev, sub);
+}
+
+void launch_freeze_group(EventSlot* slots, const int2* map, int nblocks, int nev, cudaStream_t s) {
+  k_freeze_group<<<nblocks, kBlock, 0, s>>>(slots, map);
+  k_freeze_advance_group<<<(nev + 127) / 128, 128, 0, s>>>(slots, nev);
+}
+
+void launch_stop_group(EventSlot* slots, int nev, cudaStream_t s) { k_stop_group<<<nev, 256, 0, s>>>(slots); }
 
 }  // namespace ccake

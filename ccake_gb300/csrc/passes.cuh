@@ -6,7 +6,6 @@
 namespace ccake {
 namespace passes {
 
-constexpr int kBlock = 128;
 constexpr int kSurv = 64;   // candidate chunk kept per thread in shared memory (pass A)
 
 // Row ranges [lo, hi) of the sorted cell list covering the 3^D neighbour
@@ -428,6 +427,45 @@ __device__ __forceinline__ void finish_particle(const RunConst& rc, const Ptrs& 
   else write_recA<D>(p, i, x, p.m[i], ext);
 }
 
+
+// The device clock of one substep: substep 1 moves tau to t0 + dt/2 (the
+// midpoint evaluation), substep 2 to t0 + dt, the start of the next step.
+__device__ __forceinline__ void advance_clock(Clock* c, int substep, double dt) {
+  if (substep == 1) c->t = c->teval = c->t0 + 0.5 * dt;
+  else { c->t = c->t0 + dt; c->t0 = c->t; }
+}
+
+// The freeze-out status machine of one particle after a step
+// (FreezeOut::check_freeze_out_status, include/freeze_out.h:455-500, and the
+// no-neighbour freeze of freeze_out_evo, :322-375): 0 fluid, 1 below e_FO,
+// 3 freezing, 4 frozen.
+__device__ __forceinline__ void freeze_particle(const RunConst& rc, const Ptrs& p, const int i) {
+  if (i >= p.n) return;
+  const int frzc = p.clock->frzc;
+  const double ef = rc.efreeze;
+  const double e = p.th[T_E * p.n + i];
+  int f = p.freeze[i];
+  if (f == 0) {
+    if (e <= ef) f = 1;
+  } else if (f == 1) {
+    if (p.btrack[i] == -1) f = 3;
+    else if (e > p.frz1_e[i]) f = 1;
+    else if (e <= ef) f = 3;
+    else f = 0;
+  }
+  if (frzc == 1) {
+    p.frz1_e[i] = e;
+    if (f == 3) f = 4;   // bsqsvinterpolate in the second step (:559-566)
+  } else if (frzc >= 2) {
+    if (f < 4 && p.btrack[i] == 0) {
+      f = 4;
+      p.btrack[i] = -1;
+    }
+    if (f == 3) f = 4;
+    if (f < 4) p.frz1_e[i] = e;
+  }
+  p.freeze[i] = f;
+}
 
 }  // namespace passes
 }  // namespace ccake
