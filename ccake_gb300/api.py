@@ -447,7 +447,8 @@ class ServerConfig(ctypes.Structure):
 
 class EventResult(ctypes.Structure):
     _fields_ = [("ticket", _i64), ("particles", _i64), ("state", _i32), ("status", _i32), ("steps", _i32),
-                ("frozen", _i32), ("tau", _f64), ("queue_s", _f64), ("latency_s", _f64), ("device_bytes", _i64)]
+                ("frozen", _i32), ("tau", _f64), ("queue_s", _f64), ("latency_s", _f64), ("device_bytes", _i64),
+                ("grouped", _i32), ("reserved", _i32)]
 
 
 def estimate_device_bytes(rc, n):

@@ -4,16 +4,29 @@
 // One scheduler thread owns the GPU work. Each pass it
 //   1. admits queued events (FIFO) while the resident device bytes stay within
 //      the budget: context, upload, initialisation (e -> s inversion, first
-//      smoothing) on the event's own stream;
-//   2. for every running event whose last quantum has completed (a CUDA event
-//      query, no blocking), reads the stop-rule probe the quantum left in
-//      pinned memory (frozen-particle count, largest T, tau, error counters)
-//      and either retires the event (every particle frozen out with
-//      particlization, or tau at tau_max) or enqueues the next quantum:
-//      steps_per_launch RK2 steps (CUDA-graph launches) and the probe;
-//   3. sleeps briefly when nothing changed.
-// Events therefore share the GPU through concurrent streams, and an event
-// submitted while others run starts as soon as memory allows.
+//      smoothing);
+//   2. advances the resident events.
+//      Mixed-form events (precision 1, no hypersurface output) of the same
+//      dimension form a group: their particles are advanced together by
+//      grouped launches, one launch of each step kernel for every event of
+//      the group (the launch's blocks carry the event's slot, EventSlot).
+//      One CUDA graph holds a candidate-list period of RK2 steps for the
+//      whole group: before every step the device applies each event's stop
+//      rule (every particle frozen out with particlization, tau_max, or a
+//      failure flagged by the kernels) and retires the event, whose blocks
+//      then return at once. Between periods the host rebuilds each event's
+//      candidate list (growing its capacity if needed), retires the events
+//      the device stopped, lets admitted events join, and re-captures the
+//      graph when the group changed. A group event's particles see exactly
+//      the kernels they see when the event runs alone (ccake_step with
+//      precision 1 is a group of one), so its results are the same bits.
+//      Other events advance each on its own stream in quanta of
+//      steps_per_launch RK2 steps (graph launches) followed by a one-block
+//      probe (frozen count, largest T, tau, error counters) copied to pinned
+//      memory; their stop rule is applied after each quantum;
+//   3. sleeps briefly when nothing changed. Completion is seen by
+//      cudaEventQuery; the thread blocks on the GPU only for the list builds
+//      between a group's periods.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -48,11 +61,32 @@ struct Event {
   Clock::time_point t_submit, t_admit, t_done;
   int64_t bytes = 0;
   bool counted = false;           // bytes included in the server's bytes_in_use
+  bool grouped = false;           // advanced by its dimension's group
   bool inflight = false;
   int quantum = 0;
   cudaEvent_t mark = nullptr;
   ccake::Probe* dev = nullptr;
   ccake::Probe* host = nullptr;   // pinned
+};
+
+// Resident mixed-form events of one dimension, advanced together.
+struct Group {
+  int dim = 2;
+  int period = 0;                  // RK2 steps a graph launch advances (a list period)
+  std::vector<Event*> members;     // order of the slot table
+  std::vector<Event*> joining;     // admitted, join at the next period
+  ccake::EventSlot* d_slots = nullptr;
+  ccake::EventSlot* h_slots = nullptr;   // pinned: the table after a period
+  int slot_cap = 0;
+  int2* d_map = nullptr;
+  int map_cap = 0, nblocks = 0;
+  int32_t* h_cand = nullptr;       // pinned: largest candidate count of each event's build
+  int cand_cap = 0;
+  cudaStream_t stream = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaEvent_t mark = nullptr;
+  bool dirty = true, inflight = false;
 };
 
 }  // namespace
@@ -69,6 +103,7 @@ struct ccake_server {
   int64_t next_ticket = 1;
   int64_t bytes_in_use = 0;
   bool stop = false;
+  Group groups[2];                 // dimension 2 and 3
 };
 
 namespace {
@@ -82,6 +117,25 @@ void free_event_gpu(Event* e) {
   e->mark = nullptr;
   e->dev = nullptr;
   e->host = nullptr;
+}
+
+void free_group(Group& g) {
+  if (g.stream) cudaStreamSynchronize(g.stream);
+  if (g.exec) cudaGraphExecDestroy(g.exec);
+  if (g.graph) cudaGraphDestroy(g.graph);
+  if (g.d_slots) cudaFree(g.d_slots);
+  if (g.h_slots) cudaFreeHost(g.h_slots);
+  if (g.d_map) cudaFree(g.d_map);
+  if (g.h_cand) cudaFreeHost(g.h_cand);
+  if (g.mark) cudaEventDestroy(g.mark);
+  if (g.stream) cudaStreamDestroy(g.stream);
+  g = Group{};
+}
+
+bool alloc_probe(Event* e) {
+  return cudaEventCreateWithFlags(&e->mark, cudaEventDisableTiming) == cudaSuccess &&
+         cudaMalloc(&e->dev, sizeof(ccake::Probe)) == cudaSuccess &&
+         cudaMallocHost(&e->host, sizeof(ccake::Probe)) == cudaSuccess;
 }
 
 // Context, upload and initialisation of a queued event (scheduler thread).
@@ -99,13 +153,170 @@ ccake_status_t admit(Event* e) {
   int64_t b = 0;
   ccake_device_bytes(e->ctx, &b);
   e->bytes = b;
-  if (cudaEventCreateWithFlags(&e->mark, cudaEventDisableTiming) != cudaSuccess ||
-      cudaMalloc(&e->dev, sizeof(ccake::Probe)) != cudaSuccess ||
-      cudaMallocHost(&e->host, sizeof(ccake::Probe)) != cudaSuccess)
-    return CCAKE_ERR_NOMEM;
+  if (!e->grouped && !alloc_probe(e)) return CCAKE_ERR_NOMEM;
+  if (e->grouped && (s = ccake_internal::group_join(e->ctx))) return s;
   for (int k = 0; k < 10; k++) std::vector<double>().swap(e->cols[k]);   // host copy no longer needed
   e->tau = e->cfg.t0;
   return CCAKE_OK;
+}
+
+bool groupable(const ccake_config& c) {
+  return c.precision == 1 && !(c.particlization && c.surface) && !c.using_diffusion;
+}
+
+void finish(ccake_server* srv, Event* e, int32_t state, int32_t status) {
+  std::lock_guard<std::mutex> lk(srv->mu);
+  e->state = state;
+  e->status = status;
+  e->t_done = Clock::now();
+  auto it = std::find(srv->running.begin(), srv->running.end(), e);
+  if (it != srv->running.end()) srv->running.erase(it);
+}
+
+// Capacity for `need` entries, at least doubling (cap is updated only on success).
+int grown(int cap, int need) { return std::max(need, 2 * cap + 8); }
+
+template <class T>
+bool ensure_device(T*& p, int& cap, int need) {
+  if (need <= cap) return true;
+  const int c = grown(cap, need);
+  if (p) cudaFree(p);
+  p = nullptr;
+  cap = 0;
+  if (cudaMalloc(&p, (size_t)c * sizeof(T)) != cudaSuccess) return false;
+  cap = c;
+  return true;
+}
+
+template <class T>
+bool ensure_pinned(T*& p, int& cap, int need) {
+  if (need <= cap) return true;
+  const int c = grown(cap, need);
+  if (p) cudaFreeHost(p);
+  p = nullptr;
+  cap = 0;
+  if (cudaMallocHost(&p, (size_t)c * sizeof(T)) != cudaSuccess) return false;
+  cap = c;
+  return true;
+}
+
+// Slot table, block map and period graph of the group's current members.
+ccake_status_t rebuild_group(Group& g) {
+  const int nev = (int)g.members.size();
+  int pinned_cap = g.slot_cap;   // the pinned copy grows with the device table
+  if (!ensure_pinned(g.h_slots, pinned_cap, nev)) return CCAKE_ERR_NOMEM;
+  if (!ensure_device(g.d_slots, g.slot_cap, nev)) return CCAKE_ERR_NOMEM;
+  std::vector<ccake::EventSlot> slots((size_t)nev);
+  std::vector<int2> map;
+  bool freeze = false;
+  for (int k = 0; k < nev; k++) {
+    Event* e = g.members[(size_t)k];
+    ccake_internal::fill_slot(e->ctx, &slots[(size_t)k]);
+    slots[(size_t)k].tau_max = e->tau_max;
+    slots[(size_t)k].tau = e->tau;
+    slots[(size_t)k].steps = e->steps;
+    freeze = freeze || e->cfg.particlization;
+    const int nb = (int)((e->n + ccake::kBlock - 1) / ccake::kBlock);
+    for (int b = 0; b < nb; b++) map.push_back(make_int2(k, b * ccake::kBlock));
+  }
+  g.nblocks = (int)map.size();
+  if (!ensure_device(g.d_map, g.map_cap, g.nblocks)) return CCAKE_ERR_NOMEM;
+  if (cudaMemcpyAsync(g.d_slots, slots.data(), (size_t)nev * sizeof(ccake::EventSlot), cudaMemcpyHostToDevice,
+                      g.stream) != cudaSuccess ||
+      cudaMemcpyAsync(g.d_map, map.data(), map.size() * sizeof(int2), cudaMemcpyHostToDevice, g.stream) !=
+          cudaSuccess ||
+      cudaStreamSynchronize(g.stream) != cudaSuccess)
+    return CCAKE_ERR_CUDA;
+  if (g.exec) cudaGraphExecDestroy(g.exec);
+  if (g.graph) cudaGraphDestroy(g.graph);
+  g.exec = nullptr;
+  g.graph = nullptr;
+  if (cudaStreamBeginCapture(g.stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return CCAKE_ERR_CUDA;
+  for (int k = 0; k < g.period; k++) {
+    ccake::launch_stop_group(g.d_slots, nev, g.stream);
+    for (int sub = 1; sub <= 2; sub++) {
+      ccake::launch_passA_mixed(g.d_slots, g.d_map, g.nblocks, g.dim, g.stream);
+      ccake::launch_passB_mixed(g.d_slots, g.d_map, g.nblocks, g.dim,
+                                ccake::B_EOM | ccake::B_UPDATE | (sub == 2 ? ccake::B_WRITE_Y0 : 0), sub, g.stream);
+      ccake::launch_clock_group(g.d_slots, nev, sub, g.stream);
+    }
+    if (freeze) ccake::launch_freeze_group(g.d_slots, g.d_map, g.nblocks, nev, g.stream);
+  }
+  ccake::launch_stop_group(g.d_slots, nev, g.stream);
+  cudaMemcpyAsync(g.h_slots, g.d_slots, (size_t)nev * sizeof(ccake::EventSlot), cudaMemcpyDeviceToHost, g.stream);
+  if (cudaStreamEndCapture(g.stream, &g.graph) != cudaSuccess ||
+      cudaGraphInstantiate(&g.exec, g.graph, 0) != cudaSuccess)
+    return CCAKE_ERR_CUDA;
+  g.dirty = false;
+  return CCAKE_OK;
+}
+
+// The group after a completed period: retire the events the device stopped.
+void collect_group(ccake_server* srv, Group& g) {
+  std::vector<Event*> keep;
+  for (size_t k = 0; k < g.members.size(); k++) {
+    Event* e = g.members[k];
+    const ccake::EventSlot& h = g.h_slots[k];
+    {
+      std::lock_guard<std::mutex> lk(srv->mu);
+      e->steps = h.steps;
+      e->tau = h.tau;
+    }
+    if (h.active) {
+      keep.push_back(e);
+      continue;
+    }
+    ccake_internal::group_leave(e->ctx, h.tau);
+    e->frozen = h.frozen_stop;
+    finish(srv, e, h.status ? 3 : 2, h.status);
+    g.dirty = true;
+  }
+  g.members.swap(keep);
+}
+
+// A period of the group: list builds (capacities grown where needed), the
+// graph re-captured if the group changed, then launched.
+void launch_group(ccake_server* srv, Group& g) {
+  if (!g.joining.empty()) {
+    g.members.insert(g.members.end(), g.joining.begin(), g.joining.end());
+    g.joining.clear();
+    g.dirty = true;
+  }
+  if (g.members.empty()) return;
+  const int nev = (int)g.members.size();
+  ccake_status_t s = CCAKE_OK;
+  if (!ensure_pinned(g.h_cand, g.cand_cap, nev)) s = CCAKE_ERR_NOMEM;
+  if (!s) {
+    for (int k = 0; k < nev; k++) ccake_internal::group_build(g.members[(size_t)k]->ctx, g.stream, &g.h_cand[k]);
+    if (cudaStreamSynchronize(g.stream) != cudaSuccess) s = CCAKE_ERR_CUDA;
+  }
+  std::vector<Event*> keep;
+  for (int k = 0; k < nev && !s; k++) {
+    Event* e = g.members[(size_t)k];
+    bool changed = false;
+    const ccake_status_t es = ccake_internal::group_grow(e->ctx, g.h_cand[k], &changed);
+    if (es) {
+      finish(srv, e, 3, es);
+      g.dirty = true;
+      continue;
+    }
+    g.dirty = g.dirty || changed;
+    keep.push_back(e);
+  }
+  if (!s) g.members.swap(keep);
+  if (!s && g.members.empty()) return;
+  if (!s && g.dirty) s = rebuild_group(g);
+  if (!s && (cudaGraphLaunch(g.exec, g.stream) != cudaSuccess || cudaEventRecord(g.mark, g.stream) != cudaSuccess))
+    s = CCAKE_ERR_CUDA;
+  if (s) {
+    // the group cannot run: its events fail
+    cudaGetLastError();
+    for (Event* e : g.members) finish(srv, e, 3, s);
+    g.members.clear();
+    g.dirty = true;
+    return;
+  }
+  g.inflight = true;
 }
 
 void scheduler(ccake_server* srv) {
@@ -128,7 +339,21 @@ void scheduler(ccake_server* srv) {
         e->bytes = need;
       }
       const int64_t est = e->bytes;
-      const ccake_status_t s = admit(e);
+      e->grouped = groupable(e->cfg);
+      ccake_status_t s = admit(e);
+      if (!s && e->grouped) {
+        // the group's period is the event's candidate-list period; an event
+        // whose period differs advances alone
+        Group& g = srv->groups[e->cfg.dim == 3 ? 1 : 0];
+        const int period = ccake_internal::list_period(e->ctx);
+        if (g.members.empty() && g.joining.empty() && !g.inflight) g.period = period;
+        if (period != g.period) {
+          e->grouped = false;
+          if (!alloc_probe(e)) s = CCAKE_ERR_NOMEM;
+        } else {
+          g.joining.push_back(e);
+        }
+      }
       std::lock_guard<std::mutex> lk(srv->mu);
       e->t_admit = Clock::now();
       srv->bytes_in_use += (s ? 0 : e->bytes) - est;
@@ -144,11 +369,44 @@ void scheduler(ccake_server* srv) {
       }
       progressed = true;
     }
-    // 2. running events
+    // 2a. groups
+    for (int gi = 0; gi < 2; gi++) {
+      Group& g = srv->groups[gi];
+      if (g.inflight) {
+        const cudaError_t q = cudaEventQuery(g.mark);
+        if (q == cudaErrorNotReady) continue;
+        g.inflight = false;
+        progressed = true;
+        if (q != cudaSuccess) {
+          cudaGetLastError();
+          for (Event* e : g.members) finish(srv, e, 3, CCAKE_ERR_CUDA);
+          g.members.clear();
+          g.dirty = true;
+        } else {
+          collect_group(srv, g);
+        }
+      }
+      if (!g.inflight && (!g.members.empty() || !g.joining.empty())) {
+        if (!g.stream) {
+          g.dim = gi == 1 ? 3 : 2;
+          if (cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking) != cudaSuccess ||
+              cudaEventCreateWithFlags(&g.mark, cudaEventDisableTiming) != cudaSuccess) {
+            cudaGetLastError();
+            for (Event* e : g.joining) finish(srv, e, 3, CCAKE_ERR_CUDA);
+            g.joining.clear();
+            continue;
+          }
+        }
+        launch_group(srv, g);
+        progressed = true;
+      }
+    }
+    // 2b. events advanced alone
     std::vector<Event*> run;
     {
       std::lock_guard<std::mutex> lk(srv->mu);
-      run = srv->running;
+      for (Event* e : srv->running)
+        if (!e->grouped) run.push_back(e);
     }
     for (Event* e : run) {
       if (e->inflight) {
@@ -177,26 +435,19 @@ void scheduler(ccake_server* srv) {
           else if (pr.err[ccake::E_NBR_OVERFLOW]) st = CCAKE_ERR_CAPACITY;
           failed = st != 0;
           if (!failed) {
-            // the reference's stop rule: every particle frozen out (with
-            // particlization) or tau at tau_max
+            // the reference's stop rule after the quantum: every particle
+            // frozen out (with particlization) or tau at tau_max
             const bool cold = e->cfg.particlization && pr.frozen >= e->n;
             if (cold || e->tau >= e->tau_max - 0.5 * e->cfg.dt) {
-              std::lock_guard<std::mutex> lk(srv->mu);
               e->frozen = cold ? 1 : 0;
-              e->state = 2;
-              e->t_done = Clock::now();
-              srv->running.erase(std::find(srv->running.begin(), srv->running.end(), e));
+              finish(srv, e, 2, 0);
               continue;
             }
           }
         }
         if (failed) {
           cudaGetLastError();
-          std::lock_guard<std::mutex> lk(srv->mu);
-          e->state = 3;
-          e->status = st;
-          e->t_done = Clock::now();
-          srv->running.erase(std::find(srv->running.begin(), srv->running.end(), e));
+          finish(srv, e, 3, st);
           continue;
         }
       }
@@ -207,11 +458,7 @@ void scheduler(ccake_server* srv) {
       if (!s) s = ccake_internal::probe_enqueue(e->ctx, e->dev, e->host);
       if (!s && cudaEventRecord(e->mark, ccake_internal::ctx_stream(e->ctx)) != cudaSuccess) s = CCAKE_ERR_CUDA;
       if (s) {
-        std::lock_guard<std::mutex> lk(srv->mu);
-        e->state = 3;
-        e->status = s;
-        e->t_done = Clock::now();
-        srv->running.erase(std::find(srv->running.begin(), srv->running.end(), e));
+        finish(srv, e, 3, s);
         continue;
       }
       e->quantum = k;
@@ -258,6 +505,7 @@ ccake_status_t ccake_server_destroy(ccake_server* srv) {
     srv->stop = true;
   }
   srv->th.join();
+  for (Group& g : srv->groups) free_group(g);
   for (auto& kv : srv->events) {
     Event* e = kv.second;
     if (e->ctx) cudaStreamSynchronize(ccake_internal::ctx_stream(e->ctx));
@@ -319,6 +567,7 @@ ccake_status_t ccake_server_poll(ccake_server* srv, int64_t ticket, ccake_event_
   out->frozen = e->frozen;
   out->tau = e->tau;
   out->device_bytes = e->bytes;
+  out->grouped = e->grouped ? 1 : 0;
   if (e->state >= 1) out->queue_s = std::chrono::duration<double>(e->t_admit - e->t_submit).count();
   if (e->state >= 2) out->latency_s = std::chrono::duration<double>(e->t_done - e->t_submit).count();
   return CCAKE_OK;

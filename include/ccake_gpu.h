@@ -405,11 +405,20 @@ ccake_status_t ccake_eos_invert_device(ccake_ctx* ctx, int32_t entropy_mode, int
  *
  * Submitted events wait in a FIFO queue; an internal thread admits them while
  * the device bytes of the resident events stay within hbm_budget_bytes (and
- * at most max_active run at once), keeps their state resident, and advances
- * each on its own stream in quanta of steps_per_launch RK2 steps (CUDA-graph
- * launches) until every particle is frozen out (particlization in its
- * config; the freeze-out status machine at freeze_out_T) or tau reaches its
- * tau_max. Events admitted while others run share the GPU.
+ * at most max_active run at once) and keeps their state resident. An event
+ * stops once every particle is frozen out (particlization in its config; the
+ * freeze-out status machine at freeze_out_T) or tau reaches its tau_max.
+ *  - Mixed-form events (precision 1, without the hypersurface output) of one
+ *    dimension are advanced together: one CUDA-graph launch runs a
+ *    candidate-list period of RK2 steps for all of them, each step kernel a
+ *    single grouped launch over every event's particles; the stop rule is
+ *    applied on the device before every step, and events join and leave the
+ *    group between periods. Their results are those of the same event run
+ *    alone (ccake_step), bit for bit.
+ *  - Other events advance each on its own stream in quanta of
+ *    steps_per_launch RK2 steps (CUDA-graph launches); their stop rule is
+ *    applied after each quantum.
+ * Events admitted while others run share the GPU.
  * ------------------------------------------------------------------------ */
 typedef struct ccake_server ccake_server;
 
@@ -430,6 +439,8 @@ typedef struct ccake_event_result {
   double queue_s;    /* submit -> admission */
   double latency_s;  /* submit -> done */
   int64_t device_bytes;
+  int32_t grouped;   /* 1: advanced with the other mixed-form events of its dimension by grouped launches */
+  int32_t reserved;
 } ccake_event_result;
 
 ccake_status_t ccake_server_create(const ccake_server_config* cfg, ccake_server** out);

@@ -31,6 +31,10 @@ def standalone(p, rc, steps):
 
 @pytest.mark.parametrize("precision", [0, 1])
 def test_concurrent_events_match_standalone_runs(precision):
+    # FP64 events advance on streams of their own; mixed-form events are
+    # advanced together by grouped launches (one launch of each step kernel
+    # for every event). Either way each event's state is the same bits as
+    # the event run alone.
     evs = [(p, dataclasses.replace(rc, precision=precision)) for p, rc in events()]
     steps = 30
     srv = api.Server(steps_per_launch=7)
@@ -40,6 +44,7 @@ def test_concurrent_events_match_standalone_runs(precision):
         r = srv.poll(t)
         assert r["state"] == "done", r
         assert r["steps"] == steps
+        assert r["grouped"] == precision
         assert abs(r["tau"] - (rc.t0 + steps * rc.dt)) < 1e-9
         assert r["latency_s"] >= r["queue_s"] >= 0
         ref = standalone(p, rc, steps)
@@ -49,9 +54,35 @@ def test_concurrent_events_match_standalone_runs(precision):
     srv.close()
 
 
+def test_group_members_join_and_leave_between_periods():
+    # mixed-form events with different lengths, some submitted while the
+    # group runs: members leave the group at their own tau_max (the device
+    # stops them before the step that would pass it) and newcomers join
+    # between periods; every event still equals its standalone run bit for bit
+    import time
+    evs = [(p, dataclasses.replace(rc, precision=1)) for p, rc in events()]
+    lengths = [7, 25, 40, 13, 31, 18]
+    srv = api.Server()
+    tickets = [srv.submit(p, rc, rc.t0 + k * rc.dt) for (p, rc), k in zip(evs[:3], lengths[:3])]
+    time.sleep(0.05)
+    tickets += [srv.submit(p, rc, rc.t0 + k * rc.dt) for (p, rc), k in zip(evs[3:], lengths[3:])]
+    srv.wait_all()
+    for t, (p, rc), k in zip(tickets, evs, lengths):
+        r = srv.poll(t)
+        assert r["state"] == "done" and r["grouped"] == 1 and r["steps"] == k, r
+        ref = standalone(p, rc, k)
+        for f, v in ref.items():
+            assert np.array_equal(srv.get(t, f), v), (k, f)
+        srv.release(t)
+    srv.close()
+
+
 def test_tight_budget_admits_one_event_at_a_time():
-    evs = events(4)
-    srv = api.Server(hbm_budget_bytes=1, steps_per_launch=5)   # below any event: one resident at a time
+    # equal events and a budget that holds one of them, not two
+    evs = [(p, dataclasses.replace(rc, freeze_out_T=2.0 / 197.3269804))
+           for p, rc in (ics.hotspots_2d(n_side=30, n_hot=4, seed=300 + j) for j in range(4))]
+    need = api.estimate_device_bytes(evs[0][1], evs[0][0].n)
+    srv = api.Server(hbm_budget_bytes=int(1.5 * need), steps_per_launch=5)
     tickets = [srv.submit(p, rc, rc.t0 + 10 * rc.dt) for p, rc in evs]
     srv.wait_all()
     res = [srv.poll(t) for t in tickets]
@@ -65,13 +96,18 @@ def test_tight_budget_admits_one_event_at_a_time():
     srv.close()
 
 
-def test_freeze_out_stops_an_event():
+@pytest.mark.parametrize("precision", [0, 1])
+def test_freeze_out_stops_an_event(precision):
     p, rc = events(1)[0]
-    # 197 MeV: every particle starts below it and is frozen at initialisation
-    rc = dataclasses.replace(rc, freeze_out_T=1.0, particlization=1)
+    # 197 MeV: every particle starts below it and is frozen at initialisation.
+    # A grouped (mixed-form) event is stopped by the device before its first
+    # step, as the reference's loop tests continue_evolution before each step;
+    # an event advanced alone is stopped after its first quantum.
+    rc = dataclasses.replace(rc, freeze_out_T=1.0, particlization=1, precision=precision)
     srv = api.Server(steps_per_launch=5)
     t = srv.submit(p, rc, rc.t0 + 1000 * rc.dt)
     srv.wait_all()
     r = srv.poll(t)
-    assert r["state"] == "done" and r["frozen"] == 1 and r["steps"] == 5
+    assert r["state"] == "done" and r["frozen"] == 1
+    assert r["steps"] == (0 if precision else 5)
     srv.close()
