@@ -11,7 +11,7 @@ namespace ccake {
 
 namespace {
 
-using passes::kBlock;
+
 
 // densities of the nodes of tiles [tile0, tile0 + ntiles): x = min + i * step
 // (generate_eos_table.cpp:305-308, roundings explicit)
