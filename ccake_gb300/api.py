@@ -32,7 +32,8 @@ class CcakeConfig(ctypes.Structure):
         [(n, _f64) for n in ("C_B", "reg_chi0", "reg_e0", "reg_xi0", "reg_rq_max", "crit_T", "crit_muB", "crit_wT",
                              "crit_wmuB")] + \
         [(n, _i32) for n in ("delta_pipi_mode", "tau_pipi_mode", "lambda_piPi_mode", "phi6_mode", "phi7_mode",
-                             "delta_PiPi_mode", "lambda_Pipi_mode", "phi1_mode", "phi3_mode", "pad3")]
+                             "delta_PiPi_mode", "lambda_Pipi_mode", "phi1_mode", "phi3_mode", "pad3",
+                             "seed_mode", "pad4")]
 
 
 class ParticlesSoA(ctypes.Structure):

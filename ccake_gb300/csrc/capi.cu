@@ -641,6 +641,10 @@ ccake_status_t ccake_ctx_create(const ccake_config* cfg, ccake_ctx** out) {
   if (!(cfg->skin_frac >= 0.0)) return CCAKE_ERR_INVALID;
   if (!(cfg->hT > 0) || !(cfg->t0 > 0) || !(cfg->dt > 0)) return CCAKE_ERR_INVALID;
   if (cfg->dim == 3 && cfg->factorized_kernel) return CCAKE_ERR_INVALID;
+  // initial inversion seed: the reference's, or the learned one (table EoS)
+  if (cfg->seed_mode != CCAKE_SEED_REFERENCE &&
+      !(cfg->seed_mode == CCAKE_SEED_LEARNED && cfg->eos_kind == 2 && !cfg->input_as_entropy))
+    return CCAKE_ERR_INVALID;
   // second-order coefficient modes: DEFAULT or DISABLED, and IS for the two deltas
   for (int32_t m : {cfg->tau_pipi_mode, cfg->lambda_piPi_mode, cfg->phi6_mode, cfg->phi7_mode, cfg->lambda_Pipi_mode,
                     cfg->phi1_mode, cfg->phi3_mode})
@@ -901,7 +905,26 @@ ccake_status_t ccake_initialize(ccake_ctx* ctx) {
     }
   }
   launch_init_state(ctx->rc, ctx->p, ctx->stream);
-  launch_init_invert(ctx->rc, ctx->eos, ctx->p, ctx->stream);
+  if (ctx->cfg.seed_mode == CCAKE_SEED_LEARNED) {
+    // the seed network maps every particle's (e, rho) to a (T, mu) seed
+    if (!ctx->mlp_ready) return fail(ctx, CCAKE_ERR_STATE, "seed_mode learned: train the seed network first");
+    double *in4 = nullptr, *tbqs = nullptr;
+    if (cudaMalloc(&in4, (size_t)4 * ctx->n * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&tbqs, (size_t)4 * ctx->n * sizeof(double)) != cudaSuccess) {
+      if (in4) cudaFree(in4);
+      return fail(ctx, CCAKE_ERR_NOMEM, "seed allocation");
+    }
+    launch_pack_inputs(ctx->p, in4, ctx->stream);
+    launch_mlp_seed(MlpDev{ctx->mlp_buf, ctx->mlp_norm}, ctx->n, in4, tbqs, ctx->mlp_err, ctx->stream);
+    launch_init_invert(ctx->rc, ctx->eos, ctx->p, tbqs, ctx->stream);
+    const cudaError_t e1 = cudaStreamSynchronize(ctx->stream);
+    cudaFree(in4);
+    cudaFree(tbqs);
+    if (e1 != cudaSuccess) return fail(ctx, CCAKE_ERR_CUDA, cudaGetErrorString(e1));
+    if ((s = mlp_check(ctx))) return s;
+  } else {
+    launch_init_invert(ctx->rc, ctx->eos, ctx->p, nullptr, ctx->stream);
+  }
   // candidate-list capacity: 1.5x the largest count + 16 (a build flags an
   // overflow, reported as CCAKE_ERR_CAPACITY)
   {

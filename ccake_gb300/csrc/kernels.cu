@@ -575,15 +575,19 @@ __global__ void k_init_state(RunConst rc, Ptrs p) {
   ra[3] = make_double2(1.0, 1.0);
 }
 
-__global__ void k_init_invert(RunConst rc, EosDev eos, Ptrs p) {
+// seeds (n rows of T, muB, muQ, muS, or null): the learned seed of every
+// particle, tried first on the first model of the chain
+__global__ void k_init_invert(RunConst rc, EosDev eos, Ptrs p, const double* seeds) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= p.n) return;
   const int n = p.n;
   const int entropy = rc.cfg.input_as_entropy;
   double x[4] = {p.th[T_T * n + i], 0.0, 0.0, 0.0};
+  if (seeds)
+    for (int q = 0; q < 4; q++) x[q] = seeds[(size_t)4 * i + q];
   double tgt[4] = {p.in_e[i], p.in_rho[i], p.in_rho[n + i], p.in_rho[2 * n + i]};
   int iters = 0;
-  int k = eos_invert(eos, entropy, tgt, 0, x, &iters);
+  int k = eos_invert(eos, entropy, tgt, 0, x, &iters, seeds ? 2 : 0);
   if (k < 0 && !entropy) {
     // freeze the particle and retry at zero charge (src/sph_workstation.cpp:1825-1848)
     p.freeze[i] = 4;
@@ -1283,8 +1287,21 @@ void launch_init_state(const RunConst& rc, const Ptrs& p, cudaStream_t s) {
   else k_init_state<2><<<nb, kBlock, 0, s>>>(rc, p);
 }
 
-void launch_init_invert(const RunConst& rc, const EosDev& eos, const Ptrs& p, cudaStream_t s) {
-  k_init_invert<<<(p.n + kBlock - 1) / kBlock, kBlock, 0, s>>>(rc, eos, p);
+void launch_init_invert(const RunConst& rc, const EosDev& eos, const Ptrs& p, const double* seeds, cudaStream_t s) {
+  k_init_invert<<<(p.n + kBlock - 1) / kBlock, kBlock, 0, s>>>(rc, eos, p, seeds);
+}
+
+// The input densities as rows (e|s, rhoB, rhoS, rhoQ), for the seed network.
+__global__ void k_pack_inputs(Ptrs p, double* in4) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.n) return;
+  const int n = p.n;
+  in4[(size_t)4 * i] = p.in_e[i];
+  for (int c = 0; c < 3; c++) in4[(size_t)4 * i + 1 + c] = p.in_rho[(size_t)c * n + i];
+}
+
+void launch_pack_inputs(const Ptrs& p, double* in4, cudaStream_t s) {
+  k_pack_inputs<<<(p.n + kBlock - 1) / kBlock, kBlock, 0, s>>>(p, in4);
 }
 
 void launch_init_ext(const RunConst& rc, const Ptrs& p, cudaStream_t s) {

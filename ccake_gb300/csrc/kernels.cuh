@@ -114,7 +114,9 @@ void launch_passB(const RunConst& rc, const Ptrs& p, int mode, double dt_sub, cu
 void launch_visc(const RunConst& rc, const Ptrs& p, cudaStream_t s);
 void launch_clock(const Ptrs& p, int substep, double dt, cudaStream_t s);
 void launch_init_state(const RunConst& rc, const Ptrs& p, cudaStream_t s);
-void launch_init_invert(const RunConst& rc, const EosDev& eos, const Ptrs& p, cudaStream_t s);
+// seeds: n rows (T, muB, muQ, muS) of learned seeds, or null for the reference's
+void launch_init_invert(const RunConst& rc, const EosDev& eos, const Ptrs& p, const double* seeds, cudaStream_t s);
+void launch_pack_inputs(const Ptrs& p, double* in4, cudaStream_t s);
 void launch_init_ext(const RunConst& rc, const Ptrs& p, cudaStream_t s);
 void launch_init_diffusion(const Ptrs& p, const double* iq, cudaStream_t s);
 void launch_init_viscous(const Ptrs& p, const double* iv, int bulk, int shear, cudaStream_t s);

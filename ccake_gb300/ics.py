@@ -90,6 +90,9 @@ class RunConfig:
     lambda_Pipi_mode: int = 0
     phi1_mode: int = 0
     phi3_mode: int = 0
+    # initial e -> (T, mu) inversion: 0 the reference's seeds, 2 the learned
+    # seed (trained network, table EoS) first
+    seed_mode: int = 0
 
 
 @dataclasses.dataclass

@@ -89,6 +89,15 @@ typedef struct ccake_config {
   int32_t delta_pipi_mode, tau_pipi_mode, lambda_piPi_mode, phi6_mode, phi7_mode;
   int32_t delta_PiPi_mode, lambda_Pipi_mode, phi1_mode, phi3_mode;
   int32_t pad3;
+  /* seed of the initial e -> (T, mu) inversion (ccake_initialize; the
+   * reference's s_out, src/sph_workstation.cpp:1791-1851):
+   * CCAKE_SEED_REFERENCE (0) the reference's 580 MeV forced seed,
+   * CCAKE_SEED_LEARNED (2) the trained seed network (ccake_mlp_train /
+   * ccake_mlp_set_params; table EoS only), then the reference's seeds. The
+   * step's entropy-mode inversions always start from each particle's
+   * previous (T, mu), as the reference's do. */
+  int32_t seed_mode;
+  int32_t pad4;
 } ccake_config;
 
 enum { CCAKE_COEF_DEFAULT = 0, CCAKE_COEF_IS = 1, CCAKE_COEF_DISABLED = 2 };

@@ -219,3 +219,27 @@ def test_three_d_table_eos_with_bulk_parity(table):
         assert relerr(g.get(f), orc.get(f), floor=1e-3) < 1e-10, f
     for f in ("u0", "u2", "shv33", "bulk"):
         assert relerr(g.get(f), orc.get(f), floor=1e-2) < 1e-10, f
+
+
+def test_learned_seed_initialisation_finds_the_same_states(table):
+    # seed_mode learned: the trained seed network supplies the first seed of
+    # every particle's e -> (T, mu) inversion at initialisation; where the
+    # root is unique (this event stays above the unstable band) the states
+    # are the reference seeds' states
+    import dataclasses
+    p, rc = hot_table_event()
+    ref = gpu_with_table(rc, table)
+    ref.load(p)
+    ref.initialize()
+    g = gpu_with_table(dataclasses.replace(rc, seed_mode=2), table)
+    g.mlp_train(n_samples=300_000, epochs=8, batch=16384, seed=3)
+    g.load(p)
+    g.initialize()
+    for f in ("T", "muB", "muQ", "s", "e", "sigma_lab"):
+        assert relerr(g.get(f), ref.get(f)) < 1e-10, f
+    assert np.array_equal(g.get_int("eos_id"), ref.get_int("eos_id"))
+    # without a trained network the context refuses to initialise
+    h = gpu_with_table(dataclasses.replace(rc, seed_mode=2), table)
+    h.load(p)
+    with pytest.raises(api.CcakeError):
+        h.initialize()
