@@ -70,14 +70,11 @@ struct ccake_ctx {
   int init_bulk = 0, init_shear = 0;
   // initial diffusion currents (ccake_set_initial_diffusion): q^i of charge c at row 3c + i
   double* init_q = nullptr;
-  // the mixed form's step kernels are grouped launches (EventSlot); alone, the
-  // event is a group of one: its slot and block map on the device, and the
-  // host copy last uploaded
-  EventSlot* d_slot = nullptr;
-  int2* d_map = nullptr;
+  // the mixed form's step kernels are grouped launches (GroupArgs); alone,
+  // the event is a group of one: its arguments and its device-side state
+  GroupArgs grp{};
+  EventState* d_state = nullptr;
   int nblk = 0;
-  EventSlot h_slot{};
-  bool slot_up = false;
 };
 
 namespace {
@@ -148,12 +145,9 @@ void free_buffers(ccake_ctx* ctx) {
   if (ctx->init_visc) cudaFree(ctx->init_visc);
   if (ctx->init_q) cudaFree(ctx->init_q);
   ctx->init_visc = ctx->init_q = nullptr;
-  if (ctx->d_slot) cudaFree(ctx->d_slot);
-  if (ctx->d_map) cudaFree(ctx->d_map);
-  ctx->d_slot = nullptr;
-  ctx->d_map = nullptr;
+  if (ctx->d_state) cudaFree(ctx->d_state);
+  ctx->d_state = nullptr;
   ctx->nblk = 0;
-  ctx->slot_up = false;
   ctx->init_bulk = ctx->init_shear = 0;
   ctx->dbuf = nullptr;
   ctx->ibuf = nullptr;
@@ -229,40 +223,40 @@ void ensure_records(ccake_ctx* ctx, int form) {
   ctx->records_form = form;
 }
 
-// The event's slot for the grouped mixed kernels (a group of one), uploaded
-// when it differs from the copy on the device. Called before the mixed form's
-// kernels are launched or captured.
+// The event's descriptor: constants, EoS with FP32 table Newton Jacobians
+// (the residual stays FP64), arrays.
+void fill_desc(const ccake_ctx* ctx, EventDesc* d) {
+  d->rc = ctx->rc;
+  d->eos = ctx->eos;
+  d->eos.jac32 = 1;
+  d->p = ctx->p;
+}
+
+// The event's arguments of the grouped mixed kernels (a group of one),
+// refreshed from the context before those kernels are launched or captured.
 ccake_status_t sync_slot(ccake_ctx* ctx) {
-  if (!ctx->d_slot) return fail(ctx, CCAKE_ERR_STATE, "load particles first");
-  EventSlot h;
-  std::memset(&h, 0, sizeof(h));
-  h.rc = ctx->rc;
-  h.eos = ctx->eos;
-  h.eos.jac32 = 1;   // table Newton Jacobians in FP32 (the residual stays FP64)
-  h.p = ctx->p;
-  h.tau_max = 1e300;
-  h.active = 1;
-  if (ctx->slot_up && std::memcmp(&h, &ctx->h_slot, sizeof(h)) == 0) return CCAKE_OK;
-  ctx->h_slot = h;
-  CK(cudaMemcpyAsync(ctx->d_slot, &ctx->h_slot, sizeof(EventSlot), cudaMemcpyHostToDevice, ctx->stream));
-  CK(cudaStreamSynchronize(ctx->stream));
-  ctx->slot_up = true;
+  if (!ctx->d_state) return fail(ctx, CCAKE_ERR_STATE, "load particles first");
+  ctx->grp.nev = 1;
+  ctx->grp.first_block[0] = 0;
+  ctx->grp.first_block[1] = ctx->nblk;
+  ctx->grp.state = ctx->d_state;
+  fill_desc(ctx, &ctx->grp.ev[0]);
   return CCAKE_OK;
 }
 
 void enqueue_passA(ccake_ctx* ctx) {
-  if (ctx->cfg.precision == 1) launch_passA_mixed(ctx->d_slot, ctx->d_map, ctx->nblk, ctx->cfg.dim, ctx->stream);
+  if (ctx->cfg.precision == 1) launch_passA_mixed(ctx->grp, ctx->cfg.dim, ctx->stream);
   else launch_passA(ctx->rc, ctx->eos, ctx->p, A_WITH_THERMO, ctx->stream);
 }
 
 void enqueue_passB(ccake_ctx* ctx, int mode, int sub) {
   if (ctx->cfg.precision == 1)
-    launch_passB_mixed(ctx->d_slot, ctx->d_map, ctx->nblk, ctx->cfg.dim, mode, sub, ctx->stream);
+    launch_passB_mixed(ctx->grp, ctx->cfg.dim, mode, sub, ctx->stream);
   else launch_passB(ctx->rc, ctx->p, mode, sub == 1 ? 0.5 * ctx->cfg.dt : ctx->cfg.dt, ctx->stream);
 }
 
 void enqueue_clock(ccake_ctx* ctx, int sub) {
-  if (ctx->cfg.precision == 1) launch_clock_group(ctx->d_slot, 1, sub, ctx->stream);
+  if (ctx->cfg.precision == 1) launch_clock_group(ctx->grp, sub, ctx->stream);
   else launch_clock(ctx->p, sub, ctx->cfg.dt, ctx->stream);
 }
 
@@ -348,12 +342,12 @@ void enqueue_freeze(ccake_ctx* ctx) {
     // gradients, theta and shv_nabla_u of the evaluation just done, then the
     // status machine with snapshots and hypersurface rows
     const int mixed = ctx->cfg.precision == 1 ? 1 : 0;
-    if (mixed) launch_gradients_mixed(ctx->d_slot, ctx->d_map, ctx->nblk, ctx->cfg.dim, ctx->stream);
+    if (mixed) launch_gradients_mixed(ctx->grp, ctx->cfg.dim, ctx->stream);
     else launch_passB(ctx->rc, ctx->p, B_GRADS, 0.0, ctx->stream);
     launch_diagnostics(ctx->rc, ctx->p, mixed, ctx->stream);
     launch_freeze_surface(ctx->rc, ctx->p, mixed, ctx->cfg.dt, ctx->stream);
   } else if (ctx->cfg.precision == 1) {
-    launch_freeze_group(ctx->d_slot, ctx->d_map, ctx->nblk, 1, ctx->stream);
+    launch_freeze_group(ctx->grp, ctx->stream);
   } else {
     launch_freeze(ctx->rc, ctx->p, ctx->stream);
   }
@@ -558,16 +552,7 @@ ccake_status_t clear_errors(ccake_ctx* ctx) { return reset_errors(ctx); }
 cudaStream_t ctx_stream(ccake_ctx* ctx) { return ctx->stream; }
 void ctx_set_time(ccake_ctx* ctx, double t) { ctx->t = t; }
 
-void fill_slot(ccake_ctx* ctx, EventSlot* out) {
-  std::memset(out, 0, sizeof(EventSlot));
-  out->rc = ctx->rc;
-  out->eos = ctx->eos;
-  out->eos.jac32 = 1;
-  out->p = ctx->p;
-  out->tau_max = 1e300;
-  out->tau = ctx->t;
-  out->active = 1;
-}
+void group_desc(ccake_ctx* ctx, EventDesc* out) { fill_desc(ctx, out); }
 
 int list_period(ccake_ctx* ctx) { return build_every(ctx, ctx->t); }
 
@@ -800,18 +785,18 @@ ccake_status_t ccake_load_particles(ccake_ctx* ctx, const ccake_particles_soa* h
       (s = up(h->e_or_s, p.in_e)) || (s = up(h->rhoB, p.in_rho)) || (s = up(h->rhoS, p.in_rho + n)) ||
       (s = up(h->rhoQ, p.in_rho + 2 * n)))
     return s;
-  // the event's slot and block map for the grouped mixed kernels
+  // the event's device-side state for the grouped mixed kernels: active,
+  // no tau limit (the host decides how many steps it takes alone)
   ctx->nblk = (int)((n + kBlock - 1) / kBlock);
-  if (cudaMalloc(&ctx->d_slot, sizeof(EventSlot)) != cudaSuccess ||
-      cudaMalloc(&ctx->d_map, (size_t)ctx->nblk * sizeof(int2)) != cudaSuccess)
+  if (cudaMalloc(&ctx->d_state, sizeof(EventState)) != cudaSuccess)
     return fail(ctx, CCAKE_ERR_NOMEM, "device allocation");
   {
-    std::vector<int2> map((size_t)ctx->nblk);
-    for (int b = 0; b < ctx->nblk; b++) map[b] = make_int2(0, b * kBlock);
-    CK(cudaMemcpyAsync(ctx->d_map, map.data(), map.size() * sizeof(int2), cudaMemcpyHostToDevice, ctx->stream));
+    EventState st{};
+    st.tau_max = 1e300;
+    st.active = 1;
+    CK(cudaMemcpyAsync(ctx->d_state, &st, sizeof(st), cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
   }
-  ctx->slot_up = false;
   ctx->loaded = true;
   ctx->initialized = false;
   return CCAKE_OK;
@@ -1674,7 +1659,7 @@ ccake_status_t ccake_hydro_numbers(ccake_ctx* ctx) {
   const int mixed = ctx->records_form == 1 ? 1 : 0;
   ccake_status_t st;
   if (mixed && (st = sync_slot(ctx))) return st;
-  if (mixed) launch_gradients_mixed(ctx->d_slot, ctx->d_map, ctx->nblk, ctx->cfg.dim, ctx->stream);
+  if (mixed) launch_gradients_mixed(ctx->grp, ctx->cfg.dim, ctx->stream);
   else launch_passB(ctx->rc, ctx->p, B_GRADS, 0.0, ctx->stream);
   launch_diagnostics(ctx->rc, ctx->p, mixed, ctx->stream);
   return check_errors(ctx);

@@ -592,6 +592,7 @@ __host__ __device__ inline void confdiag_seed(const Scales& k, int entropy, cons
 // outside the FP32 normal range go to cbrt.
 __host__ __device__ inline double cbrt_halley(double x) {
   const double ax = fabs(x);
+  if (ax == 0.0) return x;   // a zero density (no strangeness, say) is its own cube root
   if (!(ax > 1e-30 && ax < 1e30)) return cbrt(x);
   const double y = (double)cbrtf((float)x);
   const double y3 = y * y * y;

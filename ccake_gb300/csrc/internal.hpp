@@ -28,10 +28,9 @@ void ctx_set_time(ccake_ctx* ctx, double t);
 // neighbour-list capacities are known).
 int64_t estimate_bytes(const ccake_config& cfg, int64_t n);
 
-// --- groups of mixed-form events advanced by grouped launches (EventSlot) ---
-// The event's slot: its constants, EoS (FP32 table Jacobians) and arrays,
-// active, no tau limit.
-void fill_slot(ccake_ctx* ctx, ccake::EventSlot* out);
+// --- groups of mixed-form events advanced by grouped launches (GroupArgs) ---
+// The event's descriptor: its constants, EoS (FP32 table Jacobians) and arrays.
+void group_desc(ccake_ctx* ctx, ccake::EventDesc* out);
 // RK2 steps a candidate list stays valid (the group's quantum).
 int list_period(ccake_ctx* ctx);
 // Before the event's first grouped step: error counters cleared and the

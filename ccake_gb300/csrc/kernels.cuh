@@ -66,24 +66,38 @@ struct Ptrs {
   double* recQ;          // RQ * n   neighbour record of the diffusion sums
 };
 
-// One event of a grouped launch (the mixed form's step kernels): its
-// constants, EoS and device arrays, copied into shared memory by each block
-// that works on it. A grouped launch covers the blocks of every event of a
-// group: block b works on event map[b].x, particles map[b].y onwards (kBlock
-// of them, the event's own block decomposition), so each event runs the same
-// code on the same particles as when it is launched alone, and gives the same
-// bits. active = 0 (the device-side stop rule fired, or the event failed):
-// its blocks return at once.
-struct alignas(16) EventSlot {
+// Grouped launches (the mixed form's step kernels). One launch covers up to
+// kGroupMax events: event e owns blocks first_block[e] .. first_block[e + 1]
+// - 1, kBlock particles each in the event's own block decomposition, so each
+// event runs the same code on the same particles as when it is launched alone
+// (a group of one) and gives the same bits. The events' constants, EoS and
+// array pointers travel in the launch's parameter space (GroupArgs is passed
+// by value, read as __grid_constant__), as the single-event kernels' did;
+// what the kernels change between steps lives in device memory (EventState).
+constexpr int kGroupMax = 16;
+
+struct EventDesc {
   RunConst rc;
   EosDev eos;
   Ptrs p;
+};
+
+// Mutable per-event state of a group in device memory. active = 0 (the
+// device-side stop rule fired, or the event failed): its blocks return at once.
+struct EventState {
   double tau_max;        // stop rule: no step starts at tau >= tau_max - dt/2
   double tau;            // tau at the last stop-rule check
   int32_t active;
   int32_t frozen_stop;   // 1: stopped because every particle froze out
   int32_t steps;         // RK2 steps taken (counted by the substep-2 clock)
   int32_t status;        // ccake_status_t of a failure seen by the stop rule
+};
+
+struct GroupArgs {
+  int32_t nev;
+  int32_t first_block[kGroupMax + 1];
+  EventState* state;     // device, nev entries
+  EventDesc ev[kGroupMax];
 };
 
 // Mixed-precision neighbour records. A position x is carried as the float
@@ -126,19 +140,18 @@ void launch_neighbour_fill(const RunConst& rc, const Ptrs& p, const int32_t* off
                            cudaStream_t s);
 void launch_pack_fp64(const RunConst& rc, const Ptrs& p, cudaStream_t s);
 void launch_pack_mixed(const RunConst& rc, const Ptrs& p, cudaStream_t s);
-// The mixed form's step kernels as grouped launches over slots[0..nev) with
-// the block map map[0..nblocks) (see EventSlot): pass A (smoothing sums and
-// neighbour list, then the FP64 EoS), pass B (gradient sums, then the
-// equations of motion and the RK2 update of substep `sub`, dt from each
-// event's config), the clock, the freeze-out status machine, and the stop
-// rule (before a step: retire events that are all frozen out with
-// particlization, that reached tau_max, or that raised an error).
-void launch_passA_mixed(const EventSlot* slots, const int2* map, int nblocks, int dim, cudaStream_t s);
-void launch_passB_mixed(const EventSlot* slots, const int2* map, int nblocks, int dim, int mode, int sub,
-                        cudaStream_t s);
-void launch_clock_group(EventSlot* slots, int nev, int sub, cudaStream_t s);
-void launch_freeze_group(EventSlot* slots, const int2* map, int nblocks, int nev, cudaStream_t s);
-void launch_stop_group(EventSlot* slots, int nev, cudaStream_t s);
+// The mixed form's step kernels as grouped launches (see GroupArgs): pass A
+// (smoothing sums and neighbour list, then the FP64 EoS), pass B (gradient
+// sums, then the equations of motion and the RK2 update of substep `sub`, dt
+// from each event's config), the clock, the freeze-out status machine, and
+// the stop rule (before a step: retire events that are all frozen out with
+// particlization, that reached tau_max, or that raised an error). The
+// events' EoS must carry jac32 = 1 (FP32 table Newton Jacobians).
+void launch_passA_mixed(const GroupArgs& g, int dim, cudaStream_t s);
+void launch_passB_mixed(const GroupArgs& g, int dim, int mode, int sub, cudaStream_t s);
+void launch_clock_group(const GroupArgs& g, int sub, cudaStream_t s);
+void launch_freeze_group(const GroupArgs& g, cudaStream_t s);
+void launch_stop_group(const GroupArgs& g, cudaStream_t s);
 void launch_eos_thermo(const EosDev& eos, int chain_index, int64_t n, const double* tbqs, double* out17,
                        cudaStream_t s);
 // Batch inversion. With scratch (n + 1 int32, device) and seed_mode 0 or 2,
@@ -155,7 +168,7 @@ void launch_diagnostics(const RunConst& rc, const Ptrs& p, int grads_f32, cudaSt
 // status machine, snapshots and hypersurface rows after a step (cfg.surface)
 void launch_freeze_surface(const RunConst& rc, const Ptrs& p, int grads_f32, double dt, cudaStream_t s);
 // the gradient sums of the mixed pass B alone (no equations of motion)
-void launch_gradients_mixed(const EventSlot* slots, const int2* map, int nblocks, int dim, cudaStream_t s);
+void launch_gradients_mixed(const GroupArgs& g, int dim, cudaStream_t s);
 void launch_eos_batch(const EosDev& eos, int entropy, int seed_mode, int64_t n, const double* in4, double* tbqs,
                       double* th16, int32_t* status, int32_t* iters, int32_t* scratch, cudaStream_t s);
 

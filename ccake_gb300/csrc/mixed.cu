@@ -376,76 +376,69 @@ __device__ __forceinline__ void eom_mixed_body(const RunConst& rc, const Ptrs& p
 }
 
 // ---------------------------------------------------------------------------
-// grouped launches: one launch covers every event of a group (see EventSlot)
+// grouped launches (GroupArgs): the events' descriptors in parameter space
 // ---------------------------------------------------------------------------
-static_assert(sizeof(EventSlot) % 16 == 0, "EventSlot is copied as int4");
-
-// Copies the block's event slot into shared memory and returns it, or null
-// when the event is retired; first = the block's first particle.
-__device__ __forceinline__ const EventSlot* enter_group(const EventSlot* __restrict__ slots,
-                                                        const int2* __restrict__ map, int& first) {
-  __shared__ __align__(16) unsigned char raw[sizeof(EventSlot)];
-  const int2 b = map[blockIdx.x];
-  const int4* src = reinterpret_cast<const int4*>(slots + b.x);
-  int4* dst = reinterpret_cast<int4*>(raw);
-  for (int k = threadIdx.x; k < (int)(sizeof(EventSlot) / 16); k += blockDim.x) dst[k] = src[k];
-  __syncthreads();
-  first = b.y;
-  const EventSlot* e = reinterpret_cast<const EventSlot*>(raw);
-  return e->active ? e : nullptr;
+// The event of this block (first_block is ascending; at most kGroupMax
+// uniform comparisons), or -1 when that event is retired.
+__device__ __forceinline__ int group_event(const GroupArgs& g, int& first) {
+  int e = 0;
+#pragma unroll 1
+  while (e + 1 < g.nev && (int)blockIdx.x >= g.first_block[e + 1]) e++;
+  first = ((int)blockIdx.x - g.first_block[e]) * kBlock;
+  return g.state[e].active ? e : -1;
 }
 
 template <int D>
-__global__ void __launch_bounds__(kBlock) k_passA_mixed(const EventSlot* slots, const int2* map) {
+__global__ void __launch_bounds__(kBlock) k_passA_mixed(const __grid_constant__ GroupArgs g) {
   int first;
-  const EventSlot* e = enter_group(slots, map, first);
-  if (!e) return;
-  passA_mixed_body<D>(e->rc, e->p, first + threadIdx.x);
+  const int e = group_event(g, first);
+  if (e < 0) return;
+  passA_mixed_body<D>(g.ev[e].rc, g.ev[e].p, first + threadIdx.x);
 }
 
 template <int D>
-__global__ void __launch_bounds__(kBlock) k_thermo_mixed(const EventSlot* slots, const int2* map) {
+__global__ void __launch_bounds__(kBlock) k_thermo_mixed(const __grid_constant__ GroupArgs g) {
   int first;
-  const EventSlot* e = enter_group(slots, map, first);
-  if (!e) return;
-  thermo_mixed_body<D>(e->rc, e->eos, e->p, first + threadIdx.x);
+  const int e = group_event(g, first);
+  if (e < 0) return;
+  thermo_mixed_body<D>(g.ev[e].rc, g.ev[e].eos, g.ev[e].p, first + threadIdx.x);
 }
 
 template <int D>
-__global__ void __launch_bounds__(kBlock) k_passB_mixed(const EventSlot* slots, const int2* map) {
+__global__ void __launch_bounds__(kBlock) k_passB_mixed(const __grid_constant__ GroupArgs g) {
   int first;
-  const EventSlot* e = enter_group(slots, map, first);
-  if (!e) return;
-  passB_mixed_body<D>(e->rc, e->p, first + threadIdx.x);
+  const int e = group_event(g, first);
+  if (e < 0) return;
+  passB_mixed_body<D>(g.ev[e].rc, g.ev[e].p, first + threadIdx.x);
 }
 
 template <int D>
-__global__ void __launch_bounds__(kBlock) k_eom_mixed(const EventSlot* slots, const int2* map, int mode, int sub) {
+__global__ void __launch_bounds__(kBlock) k_eom_mixed(const __grid_constant__ GroupArgs g, int mode, int sub) {
   int first;
-  const EventSlot* e = enter_group(slots, map, first);
-  if (!e) return;
-  const double dt = e->rc.cfg.dt;
-  eom_mixed_body<D>(e->rc, e->p, first + threadIdx.x, mode, sub == 1 ? 0.5 * dt : dt);
+  const int e = group_event(g, first);
+  if (e < 0) return;
+  const double dt = g.ev[e].rc.cfg.dt;
+  eom_mixed_body<D>(g.ev[e].rc, g.ev[e].p, first + threadIdx.x, mode, sub == 1 ? 0.5 * dt : dt);
 }
 
-__global__ void k_clock_group(EventSlot* slots, int nev, int sub) {
+__global__ void k_clock_group(const __grid_constant__ GroupArgs g, int sub) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= nev || !slots[k].active) return;
-  advance_clock(slots[k].p.clock, sub, slots[k].rc.cfg.dt);
-  if (sub == 2) slots[k].steps++;
+  if (k >= g.nev || !g.state[k].active) return;
+  advance_clock(g.ev[k].p.clock, sub, g.ev[k].rc.cfg.dt);
+  if (sub == 2) g.state[k].steps++;
 }
 
-__global__ void __launch_bounds__(kBlock) k_freeze_group(const EventSlot* slots, const int2* map) {
+__global__ void __launch_bounds__(kBlock) k_freeze_group(const __grid_constant__ GroupArgs g) {
   int first;
-  const EventSlot* e = enter_group(slots, map, first);
-  if (!e || !e->rc.cfg.particlization) return;
-  freeze_particle(e->rc, e->p, first + threadIdx.x);
+  const int e = group_event(g, first);
+  if (e < 0 || !g.ev[e].rc.cfg.particlization) return;
+  freeze_particle(g.ev[e].rc, g.ev[e].p, first + threadIdx.x);
 }
 
-__global__ void k_freeze_advance_group(EventSlot* slots, int nev) {
+__global__ void k_freeze_advance_group(const __grid_constant__ GroupArgs g) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= nev || !slots[k].active || !slots[k].rc.cfg.particlization) return;
-  Clock* c = slots[k].p.clock;
+  if (k >= g.nev || !g.state[k].active || !g.ev[k].rc.cfg.particlization) return;
+  Clock* c = g.ev[k].p.clock;
   if (c->frzc < 2) c->frzc++;
 }
 
@@ -454,13 +447,14 @@ __global__ void k_freeze_advance_group(EventSlot* slots, int nev) {
 // out with particlization), the event's tau_max, and the failures the kernels
 // flagged (the first one decides the status). Idempotent: it may run again
 // with no step in between.
-__global__ void __launch_bounds__(256) k_stop_group(EventSlot* slots) {
-  EventSlot& E = slots[blockIdx.x];
+__global__ void __launch_bounds__(256) k_stop_group(const __grid_constant__ GroupArgs g) {
+  EventState& E = g.state[blockIdx.x];
   if (!E.active) return;
-  const Ptrs& p = E.p;
+  const Ptrs& p = g.ev[blockIdx.x].p;
+  const ccake_config& cfg = g.ev[blockIdx.x].rc.cfg;
   __shared__ int red[8];
   int frozen = 0;
-  if (E.rc.cfg.particlization)
+  if (cfg.particlization)
     for (int i = threadIdx.x; i < p.n; i += blockDim.x) frozen += p.freeze[i] >= 4 ? 1 : 0;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) frozen += __shfl_xor_sync(0xffffffffu, frozen, o);
@@ -475,10 +469,10 @@ __global__ void __launch_bounds__(256) k_stop_group(EventSlot* slots) {
   if (first >= 0 && first < 4) {
     E.status = kind[first];
     E.active = 0;
-  } else if (E.rc.cfg.particlization && frozen >= p.n) {
+  } else if (cfg.particlization && frozen >= p.n) {
     E.frozen_stop = 1;
     E.active = 0;
-  } else if (p.clock->t >= E.tau_max - 0.5 * E.rc.cfg.dt) {
+  } else if (p.clock->t >= E.tau_max - 0.5 * cfg.dt) {
     E.active = 0;
   }
 }
@@ -491,43 +485,43 @@ void launch_pack_mixed(const RunConst& rc, const Ptrs& p, cudaStream_t s) {
   else k_pack_mixed<2><<<nb, kBlock, 0, s>>>(p);
 }
 
-// The slots carry the EoS with FP32 table Newton Jacobians (EosDev::jac32;
-// the residual and its tolerance stay FP64).
-void launch_passA_mixed(const EventSlot* slots, const int2* map, int nblocks, int dim, cudaStream_t s) {
+void launch_passA_mixed(const GroupArgs& g, int dim, cudaStream_t s) {
+  const int nb = g.first_block[g.nev];
   if (dim == 3) {
-    k_passA_mixed<3><<<nblocks, kBlock, 0, s>>>(slots, map);
-    k_thermo_mixed<3><<<nblocks, kBlock, 0, s>>>(slots, map);
+    k_passA_mixed<3><<<nb, kBlock, 0, s>>>(g);
+    k_thermo_mixed<3><<<nb, kBlock, 0, s>>>(g);
   } else {
-    k_passA_mixed<2><<<nblocks, kBlock, 0, s>>>(slots, map);
-    k_thermo_mixed<2><<<nblocks, kBlock, 0, s>>>(slots, map);
+    k_passA_mixed<2><<<nb, kBlock, 0, s>>>(g);
+    k_thermo_mixed<2><<<nb, kBlock, 0, s>>>(g);
   }
 }
 
-void launch_passB_mixed(const EventSlot* slots, const int2* map, int nblocks, int dim, int mode, int sub,
-                        cudaStream_t s) {
+void launch_passB_mixed(const GroupArgs& g, int dim, int mode, int sub, cudaStream_t s) {
+  const int nb = g.first_block[g.nev];
   if (dim == 3) {
-    k_passB_mixed<3><<<nblocks, kBlock, 0, s>>>(slots, map);
-    k_eom_mixed<3><<<nblocks, kBlock, 0, s>>>(slots, map, mode, sub);
+    k_passB_mixed<3><<<nb, kBlock, 0, s>>>(g);
+    k_eom_mixed<3><<<nb, kBlock, 0, s>>>(g, mode, sub);
   } else {
-    k_passB_mixed<2><<<nblocks, kBlock, 0, s>>>(slots, map);
-    k_eom_mixed<2><<<nblocks, kBlock, 0, s>>>(slots, map, mode, sub);
+    k_passB_mixed<2><<<nb, kBlock, 0, s>>>(g);
+    k_eom_mixed<2><<<nb, kBlock, 0, s>>>(g, mode, sub);
   }
 }
 
-void launch_gradients_mixed(const EventSlot* slots, const int2* map, int nblocks, int dim, cudaStream_t s) {
-  if (dim == 3) k_passB_mixed<3><<<nblocks, kBlock, 0, s>>>(slots, map);
-  else k_passB_mixed<2><<<nblocks, kBlock, 0, s>>>(slots, map);
+void launch_gradients_mixed(const GroupArgs& g, int dim, cudaStream_t s) {
+  const int nb = g.first_block[g.nev];
+  if (dim == 3) k_passB_mixed<3><<<nb, kBlock, 0, s>>>(g);
+  else k_passB_mixed<2><<<nb, kBlock, 0, s>>>(g);
 }
 
-void launch_clock_group(EventSlot* slots, int nev, int sub, cudaStream_t s) {
-  k_clock_group<<<(nev + 127) / 128, 128, 0, s>>>(slots, nev, sub);
+void launch_clock_group(const GroupArgs& g, int sub, cudaStream_t s) {
+  k_clock_group<<<(g.nev + 127) / 128, 128, 0, s>>>(g, sub);
 }
 
-void launch_freeze_group(EventSlot* slots, const int2* map, int nblocks, int nev, cudaStream_t s) {
-  k_freeze_group<<<nblocks, kBlock, 0, s>>>(slots, map);
-  k_freeze_advance_group<<<(nev + 127) / 128, 128, 0, s>>>(slots, nev);
+void launch_freeze_group(const GroupArgs& g, cudaStream_t s) {
+  k_freeze_group<<<g.first_block[g.nev], kBlock, 0, s>>>(g);
+  k_freeze_advance_group<<<(g.nev + 127) / 128, 128, 0, s>>>(g);
 }
 
-void launch_stop_group(EventSlot* slots, int nev, cudaStream_t s) { k_stop_group<<<nev, 256, 0, s>>>(slots); }
+void launch_stop_group(const GroupArgs& g, cudaStream_t s) { k_stop_group<<<g.nev, 256, 0, s>>>(g); }
 
 }  // namespace ccake

@@ -8,8 +8,9 @@
 //   2. advances the resident events.
 //      Mixed-form events (precision 1, no hypersurface output) of the same
 //      dimension form a group: their particles are advanced together by
-//      grouped launches, one launch of each step kernel for every event of
-//      the group (the launch's blocks carry the event's slot, EventSlot).
+//      grouped launches, one launch of each step kernel for every
+//      kGroupMax events of the group (GroupArgs: the events' descriptors in
+//      the launch's parameters, their stop-rule state in device memory).
 //      One CUDA graph holds a candidate-list period of RK2 steps for the
 //      whole group: before every step the device applies each event's stop
 //      rule (every particle frozen out with particlization, tau_max, or a
@@ -73,13 +74,12 @@ struct Event {
 struct Group {
   int dim = 2;
   int period = 0;                  // RK2 steps a graph launch advances (a list period)
-  std::vector<Event*> members;     // order of the slot table
+  std::vector<Event*> members;     // order of the state table
   std::vector<Event*> joining;     // admitted, join at the next period
-  ccake::EventSlot* d_slots = nullptr;
-  ccake::EventSlot* h_slots = nullptr;   // pinned: the table after a period
-  int slot_cap = 0;
-  int2* d_map = nullptr;
-  int map_cap = 0, nblocks = 0;
+  ccake::EventState* d_state = nullptr;
+  ccake::EventState* h_state = nullptr;   // pinned: the states after a period
+  int state_cap = 0;
+  std::vector<ccake::GroupArgs> chunks;   // launch arguments, kGroupMax events each
   int32_t* h_cand = nullptr;       // pinned: largest candidate count of each event's build
   int cand_cap = 0;
   cudaStream_t stream = nullptr;
@@ -123,9 +123,8 @@ void free_group(Group& g) {
   if (g.stream) cudaStreamSynchronize(g.stream);
   if (g.exec) cudaGraphExecDestroy(g.exec);
   if (g.graph) cudaGraphDestroy(g.graph);
-  if (g.d_slots) cudaFree(g.d_slots);
-  if (g.h_slots) cudaFreeHost(g.h_slots);
-  if (g.d_map) cudaFree(g.d_map);
+  if (g.d_state) cudaFree(g.d_state);
+  if (g.h_state) cudaFreeHost(g.h_state);
   if (g.h_cand) cudaFreeHost(g.h_cand);
   if (g.mark) cudaEventDestroy(g.mark);
   if (g.stream) cudaStreamDestroy(g.stream);
@@ -200,31 +199,38 @@ bool ensure_pinned(T*& p, int& cap, int need) {
   return true;
 }
 
-// Slot table, block map and period graph of the group's current members.
+// State table, launch arguments and period graph of the group's members.
 ccake_status_t rebuild_group(Group& g) {
   const int nev = (int)g.members.size();
-  int pinned_cap = g.slot_cap;   // the pinned copy grows with the device table
-  if (!ensure_pinned(g.h_slots, pinned_cap, nev)) return CCAKE_ERR_NOMEM;
-  if (!ensure_device(g.d_slots, g.slot_cap, nev)) return CCAKE_ERR_NOMEM;
-  std::vector<ccake::EventSlot> slots((size_t)nev);
-  std::vector<int2> map;
+  int pinned_cap = g.state_cap;   // the pinned copy grows with the device table
+  if (!ensure_pinned(g.h_state, pinned_cap, nev)) return CCAKE_ERR_NOMEM;
+  if (!ensure_device(g.d_state, g.state_cap, nev)) return CCAKE_ERR_NOMEM;
+  std::vector<ccake::EventState> st((size_t)nev);
+  g.chunks.clear();
   bool freeze = false;
   for (int k = 0; k < nev; k++) {
     Event* e = g.members[(size_t)k];
-    ccake_internal::fill_slot(e->ctx, &slots[(size_t)k]);
-    slots[(size_t)k].tau_max = e->tau_max;
-    slots[(size_t)k].tau = e->tau;
-    slots[(size_t)k].steps = e->steps;
+    ccake::EventState& x = st[(size_t)k];
+    std::memset(&x, 0, sizeof(x));
+    x.tau_max = e->tau_max;
+    x.tau = e->tau;
+    x.steps = e->steps;
+    x.active = 1;
     freeze = freeze || e->cfg.particlization;
+    if (k % ccake::kGroupMax == 0) {
+      g.chunks.emplace_back();
+      ccake::GroupArgs& a = g.chunks.back();
+      std::memset(&a, 0, sizeof(a));
+      a.state = g.d_state + k;
+    }
+    ccake::GroupArgs& a = g.chunks.back();
+    ccake_internal::group_desc(e->ctx, &a.ev[a.nev]);
     const int nb = (int)((e->n + ccake::kBlock - 1) / ccake::kBlock);
-    for (int b = 0; b < nb; b++) map.push_back(make_int2(k, b * ccake::kBlock));
+    a.first_block[a.nev + 1] = a.first_block[a.nev] + nb;
+    a.nev++;
   }
-  g.nblocks = (int)map.size();
-  if (!ensure_device(g.d_map, g.map_cap, g.nblocks)) return CCAKE_ERR_NOMEM;
-  if (cudaMemcpyAsync(g.d_slots, slots.data(), (size_t)nev * sizeof(ccake::EventSlot), cudaMemcpyHostToDevice,
+  if (cudaMemcpyAsync(g.d_state, st.data(), (size_t)nev * sizeof(ccake::EventState), cudaMemcpyHostToDevice,
                       g.stream) != cudaSuccess ||
-      cudaMemcpyAsync(g.d_map, map.data(), map.size() * sizeof(int2), cudaMemcpyHostToDevice, g.stream) !=
-          cudaSuccess ||
       cudaStreamSynchronize(g.stream) != cudaSuccess)
     return CCAKE_ERR_CUDA;
   if (g.exec) cudaGraphExecDestroy(g.exec);
@@ -233,17 +239,19 @@ ccake_status_t rebuild_group(Group& g) {
   g.graph = nullptr;
   if (cudaStreamBeginCapture(g.stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return CCAKE_ERR_CUDA;
   for (int k = 0; k < g.period; k++) {
-    ccake::launch_stop_group(g.d_slots, nev, g.stream);
+    for (const ccake::GroupArgs& a : g.chunks) ccake::launch_stop_group(a, g.stream);
     for (int sub = 1; sub <= 2; sub++) {
-      ccake::launch_passA_mixed(g.d_slots, g.d_map, g.nblocks, g.dim, g.stream);
-      ccake::launch_passB_mixed(g.d_slots, g.d_map, g.nblocks, g.dim,
-                                ccake::B_EOM | ccake::B_UPDATE | (sub == 2 ? ccake::B_WRITE_Y0 : 0), sub, g.stream);
-      ccake::launch_clock_group(g.d_slots, nev, sub, g.stream);
+      for (const ccake::GroupArgs& a : g.chunks) ccake::launch_passA_mixed(a, g.dim, g.stream);
+      for (const ccake::GroupArgs& a : g.chunks)
+        ccake::launch_passB_mixed(a, g.dim, ccake::B_EOM | ccake::B_UPDATE | (sub == 2 ? ccake::B_WRITE_Y0 : 0),
+                                  sub, g.stream);
+      for (const ccake::GroupArgs& a : g.chunks) ccake::launch_clock_group(a, sub, g.stream);
     }
-    if (freeze) ccake::launch_freeze_group(g.d_slots, g.d_map, g.nblocks, nev, g.stream);
+    if (freeze)
+      for (const ccake::GroupArgs& a : g.chunks) ccake::launch_freeze_group(a, g.stream);
   }
-  ccake::launch_stop_group(g.d_slots, nev, g.stream);
-  cudaMemcpyAsync(g.h_slots, g.d_slots, (size_t)nev * sizeof(ccake::EventSlot), cudaMemcpyDeviceToHost, g.stream);
+  for (const ccake::GroupArgs& a : g.chunks) ccake::launch_stop_group(a, g.stream);
+  cudaMemcpyAsync(g.h_state, g.d_state, (size_t)nev * sizeof(ccake::EventState), cudaMemcpyDeviceToHost, g.stream);
   if (cudaStreamEndCapture(g.stream, &g.graph) != cudaSuccess ||
       cudaGraphInstantiate(&g.exec, g.graph, 0) != cudaSuccess)
     return CCAKE_ERR_CUDA;
@@ -256,7 +264,7 @@ void collect_group(ccake_server* srv, Group& g) {
   std::vector<Event*> keep;
   for (size_t k = 0; k < g.members.size(); k++) {
     Event* e = g.members[k];
-    const ccake::EventSlot& h = g.h_slots[k];
+    const ccake::EventState& h = g.h_state[k];
     {
       std::lock_guard<std::mutex> lk(srv->mu);
       e->steps = h.steps;
