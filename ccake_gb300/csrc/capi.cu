@@ -910,6 +910,10 @@ ccake_status_t ccake_initialize(ccake_ctx* ctx) {
   } else {
     launch_init_invert(ctx->rc, ctx->eos, ctx->p, nullptr, ctx->stream);
   }
+  // a particle without a solution even at zero charge ends the
+  // initialisation here, as the reference throws (src/sph_workstation.cpp:
+  // 1840-1846); its eos_id (-1) stays for the caller to read
+  if ((s = check_errors(ctx))) return s;
   // candidate-list capacity: 1.5x the largest count + 16 (a build flags an
   // overflow, reported as CCAKE_ERR_CAPACITY)
   {
