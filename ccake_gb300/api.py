@@ -132,6 +132,7 @@ def lib():
         L.ccake_eos_thermo_batch.argtypes = [P, _i32, _i64, _dp, _dp]
         L.ccake_set_eos_table_file.argtypes = [P, ctypes.c_char_p, _i32, _dp, _dp]
         L.ccake_eos_table_fallback_scales.argtypes = [_ip, _dp, _dp, _dp, _f64, _dp, _dp]
+        L.ccake_sph_kernel.argtypes = [_i32, _f64, _i64, _dp, _dp, _dp]
         _fp = ctypes.POINTER(ctypes.c_float)
         L.ccake_mlp_train.argtypes = [P, _i64, _i32, _i32, ctypes.c_double, ctypes.c_uint64, _dp]
         L.ccake_mlp_get_params.argtypes = [P, _fp, _fp]
@@ -163,6 +164,18 @@ def _d(a):
 
 def _i(a):
     return a.ctypes.data_as(_ip) if a is not None else None
+
+
+def sph_kernel(dim, h, r2):
+    """(W, fg) of the cubic spline at squared distances r2, evaluated on the
+    GPU by the device function of the FP64 pair loops (ccake_sph_kernel):
+    W = SPHkernel<dim>::kernel(sqrt(r2), h), grad W = fg * rel."""
+    r2 = np.ascontiguousarray(r2, dtype=np.float64)
+    w, fg = np.zeros_like(r2), np.zeros_like(r2)
+    code = lib().ccake_sph_kernel(int(dim), float(h), r2.size, _d(r2), _d(w), _d(fg))
+    if code:
+        raise CcakeError(code, "sph_kernel")
+    return w, fg
 
 
 def table_fallback_scales(n, lo, d, fields, freeze_out_T):

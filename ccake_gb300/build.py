@@ -15,7 +15,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libccake_gpu.so")
-SOURCES = ["kernels.cu", "mixed.cu", "mlp.cu", "capi.cu", "server.cu", "noalloc.cu", "io.cu", "preinv.cu"]
+SOURCES = ["kernels.cu", "thermo.cu", "mixed.cu", "mlp.cu", "capi.cu", "server.cu", "noalloc.cu", "io.cu", "preinv.cu"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 

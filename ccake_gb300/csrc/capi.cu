@@ -650,26 +650,13 @@ ccake_status_t ccake_ctx_create(const ccake_config* cfg, ccake_ctx** out) {
   rc.cfg = *cfg;
   const int D = cfg->dim;
   const double h = cfg->hT;
-  rc.cut2 = (2.0 * h) * (2.0 * h);
+  set_kernel_constants(rc, D, h);
   // skin: at least one RK2 step of travel at the largest coordinate speed
   // (tau only grows from t0), so that a list lasts a step or more
   const double vmax0 = (D == 3 && cfg->coord == 0) ? std::max(1.0, 1.0 / cfg->t0) : 1.0;
   ctx->skin = std::max((cfg->skin_frac > 0.0 ? cfg->skin_frac : 0.1) * 2.0 * h, 2.0 * cfg->dt * vmax0 * (1.0 + 1e-6));
   rc.cutc2 = (2.0 * h + ctx->skin) * (2.0 * h + ctx->skin);
-  rc.inv_h = 1.0 / h;
-  rc.wn = knorm(D) / std::pow(h, D);
-  rc.wn2 = knorm2(D) / std::pow(h, D);
-  rc.gn = kgrad(D) / std::pow(h, D + 1);
-  rc.gn2 = kgrad2(D) / std::pow(h, D + 1);
-  rc.k0 = rc.wn;   // W(0)
-  rc.fcut2 = (float)rc.cut2;
   rc.fcutc2 = (float)rc.cutc2;
-  rc.finv_h = (float)rc.inv_h;
-  rc.fwn = (float)rc.wn;
-  rc.fwn2 = (float)rc.wn2;
-  rc.fgn = (float)rc.gn;
-  rc.fgn2 = (float)rc.gn2;
-  rc.fk0 = (float)rc.k0;
   EosDev& e = ctx->eos;
   e.kind = cfg->eos_kind;
   e.thermo_mode = cfg->thermo_mode;
@@ -1409,6 +1396,27 @@ ccake_status_t ccake_set_eos_table_file(ccake_ctx* ctx, const char* eos_path, in
     }
   }
   return ccake_set_eos_table(ctx, n, lo, d, fields.data(), conf5, cdiag5);
+}
+
+ccake_status_t ccake_sph_kernel(int32_t dim, double h, int64_t n, const double* r2, double* w, double* fg) {
+  if ((dim != 2 && dim != 3) || !(h > 0.0) || !std::isfinite(h) || n < 0) return CCAKE_ERR_INVALID;
+  if (n == 0) return CCAKE_OK;
+  if (!r2 || !w || !fg) return CCAKE_ERR_INVALID;
+  for (int64_t i = 0; i < n; i++)
+    if (!(r2[i] >= 0.0) || !std::isfinite(r2[i])) return CCAKE_ERR_INVALID;
+  RunConst rc{};
+  set_kernel_constants(rc, dim, h);
+  double* d = nullptr;
+  if (cudaMalloc(&d, n * 3 * sizeof(double)) != cudaSuccess) return CCAKE_ERR_NOMEM;
+  cudaError_t err = cudaMemcpy(d, r2, n * sizeof(double), cudaMemcpyHostToDevice);
+  if (err == cudaSuccess) {
+    launch_sph_kernel(rc, n, d, d + n, d + 2 * n, 0);
+    err = cudaGetLastError();
+  }
+  if (err == cudaSuccess) err = cudaMemcpy(w, d + n, n * sizeof(double), cudaMemcpyDeviceToHost);
+  if (err == cudaSuccess) err = cudaMemcpy(fg, d + 2 * n, n * sizeof(double), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  return err == cudaSuccess ? CCAKE_OK : CCAKE_ERR_CUDA;
 }
 
 ccake_status_t ccake_eos_thermo_batch(ccake_ctx* ctx, int32_t chain_index, int64_t n, const double* tbqs,

@@ -1,7 +1,9 @@
 // Shared device definitions for the GB300 SPH hot path: state layout in HBM,
 // the cubic-spline kernel, the neighbour-cell grid and run constants.
 #pragma once
+#include <cmath>
 #include <cstdint>
+#include <cstring>
 #include <cuda_runtime.h>
 
 #include "ccake_gpu.h"
@@ -96,6 +98,11 @@ struct RunConst {
   double wn, wn2;        // W normalisations knorm/h^D, knorm2/h^D
   double gn, gn2;        // grad W normalisations kgrad/h^(D+1), kgrad2/h^(D+1)
   double k0;             // W(0)
+  // the cubic spline in the forms the FP64 pair loop evaluates:
+  // W(q < 1) = wn + q^2 (win_c1 + win_c2 q), the grad-W factor for q < 1 is
+  // fin_a q + fin_b
+  double win_c1, win_c2, fin_a, fin_b;
+  unsigned long long cut2_bits;   // IEEE bits of cut2 (for the integer-pipe predicate)
   double efreeze;        // e(T_FO, 0, 0, 0)
   // FP32 copies for the FP32 pair loops, rounded once on the host (a
   // conversion in a kernel is an FP64-pipe instruction, and the compiler may
@@ -144,6 +151,29 @@ __host__ __device__ inline double knorm(int D) { return D == 1 ? 2. / 3. : D == 
 __host__ __device__ inline double knorm2(int D) { return D == 1 ? 1. / 6. : D == 2 ? 5. / (14. * M_PI) : 1. / (4 * M_PI); }
 __host__ __device__ inline double kgrad(int D) { return D == 1 ? -1. / 2. : D == 2 ? -15. / (14. * M_PI) : -3. / (4. * M_PI); }
 __host__ __device__ inline double kgrad2(int D) { return D == 1 ? 1. : D == 2 ? 15. / (7. * M_PI) : 3. / (2. * M_PI); }
+
+// Kernel constants of a run with smoothing length h in D dimensions (host).
+inline void set_kernel_constants(RunConst& rc, int D, double h) {
+  rc.cut2 = (2.0 * h) * (2.0 * h);
+  std::memcpy(&rc.cut2_bits, &rc.cut2, sizeof(double));
+  rc.inv_h = 1.0 / h;
+  rc.wn = knorm(D) / std::pow(h, D);
+  rc.wn2 = knorm2(D) / std::pow(h, D);
+  rc.gn = kgrad(D) / std::pow(h, D + 1);
+  rc.gn2 = kgrad2(D) / std::pow(h, D + 1);
+  rc.k0 = rc.wn;   // W(0)
+  rc.win_c1 = -1.5 * rc.wn;
+  rc.win_c2 = 0.75 * rc.wn;
+  rc.fin_a = 1.5 * rc.gn2 * rc.inv_h;
+  rc.fin_b = -2.0 * rc.gn2 * rc.inv_h;
+  rc.fcut2 = (float)rc.cut2;
+  rc.finv_h = (float)rc.inv_h;
+  rc.fwn = (float)rc.wn;
+  rc.fwn2 = (float)rc.wn2;
+  rc.fgn = (float)rc.gn;
+  rc.fgn2 = (float)rc.gn2;
+  rc.fk0 = (float)rc.k0;
+}
 
 // Exact squared distance of the neighbour predicate (reference Cabana
 // VerletList, cutoff 2h): products and sums rounded separately, no FMA.

@@ -1,9 +1,10 @@
 // Kernels of the GB300 SPH hot path.
 //
-// One RK2 substep is four small cell-list kernels plus two fused passes:
-//   pass A  (per particle a): smoothing sums over the 3^D neighbour cells,
-//           LRF densities, EoS Newton inversion, pi^{mu nu} constraints;
-//           writes neighbour record B.
+// One RK2 substep is two passes over each particle's neighbours:
+//   pass A  (per particle a): smoothing sums over the candidate list, the
+//           exact 2h neighbour list with its grad-W factors, LRF densities;
+//           then (thermo.cu) the EoS Newton inversion, pi^{mu nu}
+//           constraints and neighbour record B.
 //   pass B  (per particle a): gradient sums in separable form, the MRF
 //           equations of motion and the RK2 update of the state; writes
 //           neighbour record A for the next substep.
@@ -252,8 +253,12 @@ __device__ __forceinline__ void for_candidates(const RunConst& rc, const Ptrs& p
 // ---------------------------------------------------------------------------
 // pass A
 // ---------------------------------------------------------------------------
-template <int D, bool DIFF>
-__global__ void __launch_bounds__(kBlock) k_passA(RunConst rc, EosDev eos, Ptrs p, int mode) {
+// The smoothing kernel carries no EoS code: the inversion's ~255 registers
+// would cap it at 8 warps an SM, and its pair loop, bound by the FP64 pipe,
+// runs better with more warps to draw FP64 instructions from; k_thermo runs
+// the inversion right after it.
+template <int D>
+__global__ void __launch_bounds__(kBlock) k_passA(RunConst rc, Ptrs p) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= p.n) return;
   const int n = p.n;
@@ -296,19 +301,12 @@ __global__ void __launch_bounds__(kBlock) k_passA(RunConst rc, EosDev eos, Ptrs 
       const double2 b01 = __ldg(&ra[(size_t)b * 4 + 0]), b23 = __ldg(&ra[(size_t)b * 4 + 1]);
       double d[3] = {xa[0] - b01.x, xa[1] - b01.y, (D == 3) ? xa[2] - b23.x : 0.0};
       const double d2 = dist2_exact<D>(d);
-      if (!(d2 <= rc.cut2)) continue;
-      // W (src/kernel.cpp:34-48) and the radial factor of grad W (:95-118):
-      // grad_a W = fg (r_a - r_b), fg = kgrad/h^(D+1) (2-q)^2 / r for
-      // 1 <= q < 2 and kgrad2/h^(D+1) (1.5 q - 2) / h for q < 1. One rsqrt
-      // gives r and 1/r; both branches are evaluated and selected.
-      const double rs = d2 > 0.0 ? rsqrt(d2) : 0.0;
-      const double rr = d2 * rs;
-      const double q = rr * rc.inv_h;
-      const double z = 2.0 - q, qq = q * q;
-      const double Win = rc.wn * (1.0 - 1.5 * qq + 0.75 * q * qq), Wout = rc.wn2 * z * z * z;
-      const double fin = rc.gn2 * (1.5 * q - 2) * rc.inv_h, fout = rc.gn * rs * z * z;
-      const double W = q < 1.0 ? Win : (q < 2.0 ? Wout : 0.0);
-      const double fg = q < 1.0 ? fin : (q < 2.0 ? fout : 0.0);
+      // d2 <= (2h)^2 on the integer pipe: d2 is a sum of squares (+0 or
+      // more), whose IEEE bits read as an unsigned integer order like the
+      // value, and a NaN of either sign compares above the cut
+      if ((unsigned long long)__double_as_longlong(d2) > rc.cut2_bits) continue;
+      double W, fg;
+      pair_kernel(rc, d2, W, fg);
       if (nn < K) {
         p.nbr_idx[(size_t)nn * n + i] = b;
         p.nbr_f[(size_t)nn * n + i] = fg;
@@ -347,14 +345,6 @@ __global__ void __launch_bounds__(kBlock) k_passA(RunConst rc, EosDev eos, Ptrs 
     p.th[T_RQ * n + i] = s3 / g / t;
   }
   p.btrack[i] = nn;
-  if (mode == A_WITH_THERMO) thermo_tail<D, false, DIFF>(rc, eos, p, i, t);
-}
-
-template <int D, bool DIFF>
-__global__ void __launch_bounds__(kBlock) k_thermo(RunConst rc, EosDev eos, Ptrs p) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= p.n) return;
-  thermo_tail<D, false, DIFF>(rc, eos, p, i, p.clock->t);
 }
 
 // Diffusion sums of src/sph_workstation.cpp:909-967 over the list pass A
@@ -488,10 +478,9 @@ __global__ void __launch_bounds__(kBlock) k_passB(RunConst rc, Ptrs p, int mode,
         for (int k = 0; k < D; k++) {
 #pragma unroll
           for (int l = 0; l < D; l++) S0[k][l] += p0[l] * gm[k];
-          double acc = 0.0;
+          // one FMA a term into the sum (the FP64 pipe bounds this loop)
 #pragma unroll
-          for (int l = 0; l < D; l++) acc += PJ(k, l) * gm[l];
-          SD[k] += acc;
+          for (int l = 0; l < D; l++) SD[k] = fma(PJ(k, l), gm[l], SD[k]);
         }
       }
     }
@@ -573,41 +562,6 @@ __global__ void k_init_state(RunConst rc, Ptrs p) {
                           D == 3 ? (float)p.y[Y_X2 * n + i] : 0.0f, 0.0f);
   ra[2] = make_double2(1.0, 1.0);
   ra[3] = make_double2(1.0, 1.0);
-}
-
-// seeds (n rows of T, muB, muQ, muS, or null): the learned seed of every
-// particle, tried first on the first model of the chain
-__global__ void k_init_invert(RunConst rc, EosDev eos, Ptrs p, const double* seeds) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= p.n) return;
-  const int n = p.n;
-  const int entropy = rc.cfg.input_as_entropy;
-  double x[4] = {p.th[T_T * n + i], 0.0, 0.0, 0.0};
-  if (seeds)
-    for (int q = 0; q < 4; q++) x[q] = seeds[(size_t)4 * i + q];
-  double tgt[4] = {p.in_e[i], p.in_rho[i], p.in_rho[n + i], p.in_rho[2 * n + i]};
-  int iters = 0;
-  int k = eos_invert(eos, entropy, tgt, 0, x, &iters, seeds ? 2 : 0);
-  if (k < 0 && !entropy) {
-    // freeze the particle and retry at zero charge (src/sph_workstation.cpp:1825-1848)
-    p.freeze[i] = 4;
-    x[0] = p.th[T_T * n + i]; x[1] = x[2] = x[3] = 0.0;
-    const double tz[4] = {tgt[0], 0.0, 0.0, 0.0};
-    k = eos_invert(eos, 0, tz, 0, x, &iters);
-  }
-  if (k < 0) {   // per-particle status: no EoS solution
-    p.eos_id[i] = -1;
-    flag_error(p.err, E_EOS);
-    return;
-  }
-  double th[NTH];
-  set_thermo(eos, k, x, th);
-  for (int q = 0; q < NTH; q++) p.th[q * n + i] = th[q];
-  p.eos_id[i] = k;
-  p.eos_iters[i] = iters;
-  if (entropy) { p.in_s[i] = p.in_e[i]; p.in_e[i] = th[T_E]; }
-  else p.in_s[i] = th[T_S];
-  if (!(p.in_e[i] > rc.efreeze && p.freeze[i] != 4)) p.freeze[i] = 4;
 }
 
 // ext = input/sigma after the initial sigma (src/sph_workstation.cpp:338-364)
@@ -738,68 +692,6 @@ __global__ void k_nbr_fill(RunConst rc, Ptrs p, const int32_t* off, int32_t* idx
                    D == 3 ? xa[2] - p.y[Y_X2 * p.n + b] : 0.0};
     if (dist2_exact<D>(d) <= rc.cut2) idx[c++] = b;
   });
-}
-
-__global__ void k_eos_thermo(EosDev eos, int model, int64_t n, const double* tbqs, double* out17) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  model_thermo(eos, model, tbqs + 4 * i, out17 + 17 * i);
-}
-
-// Pass 1 of the two-pass batch inversion: the first attempt of each row
-// with a Newton budget; rows it does not settle are appended to `list` (an
-// atomic append: rows are independent, so the order does not matter).
-__global__ void k_eos_first(EosDev eos, int entropy, int seed_mode, int max_it, int64_t n, const double* in4,
-                            double* tbqs, double* th16, int32_t* status, int32_t* iters, int32_t* list,
-                            int32_t* count) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  double x[4] = {tbqs[4 * i], tbqs[4 * i + 1], tbqs[4 * i + 2], tbqs[4 * i + 3]};
-  int it = 0;
-  double o[17];
-  const int k = eos_invert_first(eos, entropy, in4 + 4 * i, 0, x, &it, seed_mode, max_it, o);
-  if (k == -2) {
-    list[atomicAdd(count, 1)] = (int32_t)i;
-    return;
-  }
-  status[i] = k;
-  if (iters) iters[i] = it;
-  for (int q = 0; q < 4; q++) tbqs[4 * i + q] = x[q];
-  if (th16) set_thermo_o(eos, k, x, o, th16 + 16 * i);
-}
-
-// Pass 2: the full inversion of the listed rows.
-__global__ void k_eos_rest(EosDev eos, int entropy, int seed_mode, const int32_t* list, const int32_t* count,
-                           const double* in4, double* tbqs, double* th16, int32_t* status, int32_t* iters) {
-  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= *count) return;
-  const int64_t i = list[j];
-  double x[4] = {tbqs[4 * i], tbqs[4 * i + 1], tbqs[4 * i + 2], tbqs[4 * i + 3]};
-  int it = 0;
-  double o[17];
-  const int k = eos_invert(eos, entropy, in4 + 4 * i, 0, x, &it, seed_mode, o);
-  status[i] = k;
-  if (iters) iters[i] = it;
-  if (k >= 0) {
-    for (int q = 0; q < 4; q++) tbqs[4 * i + q] = x[q];
-    if (th16) set_thermo_o(eos, k, x, o, th16 + 16 * i);
-  }
-}
-
-__global__ void k_eos_batch(EosDev eos, int entropy, int seed_mode, int64_t n, const double* in4, double* tbqs,
-                            double* th16, int32_t* status, int32_t* iters) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  double x[4] = {tbqs[4 * i], tbqs[4 * i + 1], tbqs[4 * i + 2], tbqs[4 * i + 3]};
-  int it = 0;
-  double o[17];
-  const int k = eos_invert(eos, entropy, in4 + 4 * i, 0, x, &it, seed_mode, o);
-  status[i] = k;
-  if (iters) iters[i] = it;
-  if (k >= 0) {
-    for (int q = 0; q < 4; q++) tbqs[4 * i + q] = x[q];
-    if (th16) set_thermo_o(eos, k, x, o, th16 + 16 * i);
-  }
 }
 
 // One block: the largest T and the number of frozen particles, tau and the
@@ -1231,26 +1123,9 @@ void launch_candidates(const RunConst& rc, const Ptrs& p, cudaStream_t s) {
 
 void launch_passA(const RunConst& rc, const EosDev& eos, const Ptrs& p, int mode, cudaStream_t s) {
   const int nb = (p.n + kBlock - 1) / kBlock;
-  const bool dif = rc.cfg.using_diffusion && p.dif;
-  if (rc.cfg.dim == 3) {
-    if (dif) k_passA<3, true><<<nb, kBlock, 0, s>>>(rc, eos, p, mode);
-    else k_passA<3, false><<<nb, kBlock, 0, s>>>(rc, eos, p, mode);
-  } else {
-    if (dif) k_passA<2, true><<<nb, kBlock, 0, s>>>(rc, eos, p, mode);
-    else k_passA<2, false><<<nb, kBlock, 0, s>>>(rc, eos, p, mode);
-  }
-}
-
-void launch_thermo(const RunConst& rc, const EosDev& eos, const Ptrs& p, cudaStream_t s) {
-  const int nb = (p.n + kBlock - 1) / kBlock;
-  const bool dif = rc.cfg.using_diffusion && p.dif;
-  if (rc.cfg.dim == 3) {
-    if (dif) k_thermo<3, true><<<nb, kBlock, 0, s>>>(rc, eos, p);
-    else k_thermo<3, false><<<nb, kBlock, 0, s>>>(rc, eos, p);
-  } else {
-    if (dif) k_thermo<2, true><<<nb, kBlock, 0, s>>>(rc, eos, p);
-    else k_thermo<2, false><<<nb, kBlock, 0, s>>>(rc, eos, p);
-  }
+  if (rc.cfg.dim == 3) k_passA<3><<<nb, kBlock, 0, s>>>(rc, p);
+  else k_passA<2><<<nb, kBlock, 0, s>>>(rc, p);
+  if (mode == A_WITH_THERMO) launch_thermo(rc, eos, p, s);
 }
 
 // With the diffusion sector, its gradient sums run first (they read the
@@ -1287,10 +1162,6 @@ void launch_init_state(const RunConst& rc, const Ptrs& p, cudaStream_t s) {
   else k_init_state<2><<<nb, kBlock, 0, s>>>(rc, p);
 }
 
-void launch_init_invert(const RunConst& rc, const EosDev& eos, const Ptrs& p, const double* seeds, cudaStream_t s) {
-  k_init_invert<<<(p.n + kBlock - 1) / kBlock, kBlock, 0, s>>>(rc, eos, p, seeds);
-}
-
 // The input densities as rows (e|s, rhoB, rhoS, rhoQ), for the seed network.
 __global__ void k_pack_inputs(Ptrs p, double* in4) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1298,6 +1169,20 @@ __global__ void k_pack_inputs(Ptrs p, double* in4) {
   const int n = p.n;
   in4[(size_t)4 * i] = p.in_e[i];
   for (int c = 0; c < 3; c++) in4[(size_t)4 * i + 1 + c] = p.in_rho[(size_t)c * n + i];
+}
+
+__global__ void k_sph_kernel(RunConst rc, int64_t n, const double* r2, double* w, double* fg) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double d2 = r2[i];
+  double W = 0.0, f = 0.0;
+  if ((unsigned long long)__double_as_longlong(d2) <= rc.cut2_bits) pair_kernel(rc, d2, W, f);
+  w[i] = W;
+  fg[i] = f;
+}
+
+void launch_sph_kernel(const RunConst& rc, int64_t n, const double* r2, double* w, double* fg, cudaStream_t s) {
+  k_sph_kernel<<<(unsigned)((n + kBlock - 1) / kBlock), kBlock, 0, s>>>(rc, n, r2, w, fg);
 }
 
 void launch_pack_inputs(const Ptrs& p, double* in4, cudaStream_t s) {
@@ -1371,30 +1256,6 @@ void launch_neighbour_fill(const RunConst& rc, const Ptrs& p, const int32_t* off
   const int nb = (p.n + kBlock - 1) / kBlock;
   if (rc.cfg.dim == 3) k_nbr_fill<3><<<nb, kBlock, 0, s>>>(rc, p, offsets, idx);
   else k_nbr_fill<2><<<nb, kBlock, 0, s>>>(rc, p, offsets, idx);
-}
-
-void launch_eos_thermo(const EosDev& eos, int chain_index, int64_t n, const double* tbqs, double* out17,
-                       cudaStream_t s) {
-  const int nb = (int)((n + kBlock - 1) / kBlock);
-  k_eos_thermo<<<nb, kBlock, 0, s>>>(eos, chain_model(eos.kind, chain_index), n, tbqs, out17);
-}
-
-void launch_eos_batch(const EosDev& eos, int entropy, int seed_mode, int64_t n, const double* in4, double* tbqs,
-                      double* th16, int32_t* status, int32_t* iters, int32_t* scratch, cudaStream_t s) {
-  const int nb = (int)((n + kBlock - 1) / kBlock);
-  if (seed_mode == 1 || !scratch) {
-    k_eos_batch<<<nb, kBlock, 0, s>>>(eos, entropy, seed_mode, n, in4, tbqs, th16, status, iters);
-    return;
-  }
-  // two passes: a warp of the single-pass kernel runs as long as its slowest
-  // row; the capped first pass settles most rows in a few Newton steps and
-  // the compacted second pass gives the hard rows warps of their own
-  int32_t* count = scratch;
-  int32_t* list = scratch + 1;
-  cudaMemsetAsync(count, 0, sizeof(int32_t), s);
-  k_eos_first<<<nb, kBlock, 0, s>>>(eos, entropy, seed_mode, kEosFirstIters, n, in4, tbqs, th16, status, iters, list,
-                                    count);
-  k_eos_rest<<<nb, kBlock, 0, s>>>(eos, entropy, seed_mode, list, count, in4, tbqs, th16, status, iters);
 }
 
 }  // namespace ccake

@@ -131,6 +131,7 @@ void launch_init_state(const RunConst& rc, const Ptrs& p, cudaStream_t s);
 // seeds: n rows (T, muB, muQ, muS) of learned seeds, or null for the reference's
 void launch_init_invert(const RunConst& rc, const EosDev& eos, const Ptrs& p, const double* seeds, cudaStream_t s);
 void launch_pack_inputs(const Ptrs& p, double* in4, cudaStream_t s);
+void launch_sph_kernel(const RunConst& rc, int64_t n, const double* r2, double* w, double* fg, cudaStream_t s);
 void launch_init_ext(const RunConst& rc, const Ptrs& p, cudaStream_t s);
 void launch_init_diffusion(const Ptrs& p, const double* iq, cudaStream_t s);
 void launch_init_viscous(const Ptrs& p, const double* iv, int bulk, int shear, cudaStream_t s);

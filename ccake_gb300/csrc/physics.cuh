@@ -230,7 +230,15 @@ __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, cons
   for (int i = 0; i < D; i++) divV += in.gradV[i * D + i];
   const R uD = u[D - 1];
   const R geo = (D == 3 && !cart) ? uD * uD * t * ig : R(0.0);
-  const R expn = g * divV + g * itc + geo;
+  // In 2-D the geometric term geo, every eta delta dEta(i) and the eta
+  // velocity vanish. A product with a constant zero is still an FP64
+  // instruction (IEEE arithmetic keeps NaN and the sign of zero), and the
+  // FP64 pipe bounds this function, so those terms are left out at compile
+  // time (if (D == 3) / if (e3) below): the results are the same up to the
+  // sign of zero.
+  constexpr bool e3 = (D == 3);
+  R expn = g * divV + g * itc;
+  if (e3) expn = expn + geo;
   auto dEta = [cart](int i) { return (!cart && D == 3 && i == 2) ? R(1.0) : R(0.0); };
 
   // ---- shear MRFs --------------------------------------------------------
@@ -239,7 +247,7 @@ __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, cons
   R ss = R(0.0);   // pi^{mu nu} pi_{mu nu}
   if (cfg.using_shear) {
     const R cmd[4] = {R(1.0), -R(1.0), -R(1.0), -R(1.0) * itm * itm};
-    const R eta = k.eta, phi6 = k.phi6, phi7 = k.phi7, lpP = k.lambda_piPi;
+    const R eta = k.eta, phi7 = k.phi7, lpP = k.lambda_piPi;
     const R tpp = k.tau_pipi, dpp = k.delta_pipi, tpi = k.tau_pi;
     const R tdelta = dpp - tpi;
     const R itg = R(1.0) / (tpi * g), istg = R(1.0) / (sig * tpi * g);
@@ -312,19 +320,27 @@ __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, cons
 #pragma unroll
     for (int i = 0; i < D; i++) {
       const R di = dEta(i);
-      R Fs = -(guv[i] - gu0c[i]) / R(2.) + u[i] * g * expn * k13 - g * geo * u[i] / R(2.);
-      R FD = g * (u[i] * hy[0][0] + g * hy[i + 1][0]) * geo + t * uD * pi[3][i + 1] * di;
-      R Fds = -(vgs[i] - ggs[i] - R(4.) * g * u[i] * sgu_s * k13 - sgu[i] + vsg[i]) / R(4.) +
-                   (hy[i + 1][0] - g * g * hy[i + 1][0] - g * u[i] * hy[0][0] + pi[0][i + 1] +
-                    R(4.) * u[i] * g * hy[0][0] * k13) * geo / R(4.) +
-                   ch * ((g * cmd[i + 1] * hy[0][3] * di * it + g * pi[3][0] * di * it + R(4.) * g * u[i] * (g * hy[3][3] * it) * k13) / R(4.)) -
-                   pi[0][i + 1] * (g * itc + geo + g * divV) * k13;
-      R Fdo = -(vgs[i] - ggs[i] + sgu[i] - vsg[i]) / R(4.) +
-                   (hy[i + 1][0] - g * g * hy[i + 1][0] - g * u[i] * hy[0][0] - pi[0][i + 1]) * geo / R(4.) +
-                   (g * cmd[i + 1] * hy[0][3] * di * it - g * pi[3][0] * di * it) / R(4.);
+      R Fs, FD = R(0.0), Fds, Fdo;
+      if (e3) {
+        Fs = -(guv[i] - gu0c[i]) / R(2.) + u[i] * g * expn * k13 - g * geo * u[i] / R(2.);
+        FD = g * (u[i] * hy[0][0] + g * hy[i + 1][0]) * geo + t * uD * pi[3][i + 1] * di;
+        Fds = -(vgs[i] - ggs[i] - R(4.) * g * u[i] * sgu_s * k13 - sgu[i] + vsg[i]) / R(4.) +
+              (hy[i + 1][0] - g * g * hy[i + 1][0] - g * u[i] * hy[0][0] + pi[0][i + 1] +
+               R(4.) * u[i] * g * hy[0][0] * k13) * geo / R(4.) +
+              ch * ((g * cmd[i + 1] * hy[0][3] * di * it + g * pi[3][0] * di * it + R(4.) * g * u[i] * (g * hy[3][3] * it) * k13) / R(4.)) -
+              pi[0][i + 1] * (g * itc + geo + g * divV) * k13;
+        Fdo = -(vgs[i] - ggs[i] + sgu[i] - vsg[i]) / R(4.) +
+              (hy[i + 1][0] - g * g * hy[i + 1][0] - g * u[i] * hy[0][0] - pi[0][i + 1]) * geo / R(4.) +
+              (g * cmd[i + 1] * hy[0][3] * di * it - g * pi[3][0] * di * it) / R(4.);
+        Fs += di * (-(-uD * t - uD * it + g * uD * uD * t + R(2.) * g * g * uD * it) / R(2.));
+        FD += di * (uD * pi[0][0] * it + g * pi[3][0] * it);
+      } else {
+        Fs = -(guv[i] - gu0c[i]) / R(2.) + u[i] * g * expn * k13;
+        Fds = -(vgs[i] - ggs[i] - R(4.) * g * u[i] * sgu_s * k13 - sgu[i] + vsg[i]) / R(4.) +
+              ch * ((R(4.) * g * u[i] * (g * hy[3][3] * it) * k13) / R(4.)) - pi[0][i + 1] * (g * itc + g * divV) * k13;
+        Fdo = -(vgs[i] - ggs[i] + sgu[i] - vsg[i]) / R(4.);
+      }
       const R Fdd = pi[i + 1][0] * expn;
-      Fs += di * (-(-uD * t - uD * it + g * uD * uD * t + R(2.) * g * g * uD * it) / R(2.));
-      FD += di * (uD * pi[0][0] * it + g * pi[3][0] * it);
       if (D == 3 && !cart) {
         Fds += (t * uD * di * cmd[i + 1] * hy[0][0] + uD * hy[i + 1][3] * g * it / R(4.) + hy[i + 1][3] * t * uD +
                 pi[0][0] * di * uD * it + t * uD * uD * (g * hy[i + 1][0] + u[i] * hy[0][0]) +
@@ -334,8 +350,12 @@ __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, cons
                 pi[0][0] * di * uD * it + t * uD * uD * (g * hy[i + 1][0] + u[i] * hy[0][0]) +
                 R(2.) * g * uD * (g * hy[i + 1][3] + u[i] * pi[0][3]) * it) / R(4.);
       }
-      F0i[i] = (-pi[i + 1][0] - tpi * FD - dpp * Fdd + R(2.) * tpi * Fdo * uv - tpp * Fds + (R(2.) * eta + lpP * Pi) * Fs +
-                phi6 * Pi * pi[i + 1][0] + phi7 * (sl0[i] + g * u[i] * ss * k13)) * itg;
+      // phi6 (and phi1, phi3 below) are zero in every coefficient mode:
+      // their terms are left out
+      R f0 = -pi[i + 1][0];
+      if (e3) f0 = f0 - tpi * FD;
+      F0i[i] = (f0 - dpp * Fdd + R(2.) * tpi * Fdo * uv - tpp * Fds + (R(2.) * eta + lpP * Pi) * Fs +
+                phi7 * (sl0[i] + g * u[i] * ss * k13)) * itg;
 #pragma unroll
       for (int j = 0; j < D; j++) {
         R Ms = u[i] * uc[j] * k16;
@@ -363,7 +383,8 @@ __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, cons
       for (int j = 0; j < D; j++) Fnab += (hy[i + 1][j + 1] - v[i] * hy[0][j + 1]) * gu[i][j];
       Fnab += (hy[i + 1][0] - v[i] * hy[0][0]) * gu0[i];
     }
-    Fnab += +ch * (hy[3][3] * g * it) + hy[0][0] * geo + (t * hy[3][0] + hy[0][3] * it) * uD * dEta(D - 1);
+    if (e3) Fnab += +ch * (hy[3][3] * g * it) + hy[0][0] * geo + (t * hy[3][0] + hy[0][3] * it) * uD * dEta(D - 1);
+    else Fnab += ch * (hy[3][3] * g * it);
     // shear-tensor evolution MRFs on the (i <= j) entries of the 2x3 block
     const R f2 = fu[2];
 #pragma unroll
@@ -383,51 +404,79 @@ __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, cons
         }
 #pragma unroll
         for (int kk = 0; kk < 4; kk++) sml += (pi[i + 1][kk] * hy[j + 1][kk] + pi[j + 1][kk] * hy[i + 1][kk]) / R(2.);
-        R FD2 = g * geo * (fu[i] * hy[j + 1][0] + fu[j] * hy[i + 1][0]);
+        // in 2-D the eta row (j = 2) has fu[j] = 0
+        const bool fj0 = (D == 2 && j == 2);
+        R FD2 = R(0.0);
+        if (e3) FD2 = g * geo * (fu[i] * hy[j + 1][0] + fu[j] * hy[i + 1][0]);
         const R cg_ij = (i < D && j < D) ? cgu[i][j] : R(0.0), cg_ji = (i < D && j < D) ? cgu[j][i] : R(0.0);
-        R Fsg = cg_ij / R(2.) + cg_ji / R(2.) + fu[i] * fu[j] * expn * k13;
+        R Fsg = R(0.0);
+        if (!fj0) Fsg = cg_ij / R(2.) + cg_ji / R(2.) + fu[i] * fu[j] * expn * k13;
         const R Fdl = pi[i + 1][j + 1] * expn;
-        const R common = ch * (t * f2 * (cmd[i + 1] * hy[j + 1][0] * di + cmd[j + 1] * hy[i + 1][0] * dj) +
-                              g * (cmd[i + 1] * hy[j + 1][3] * di + cmd[j + 1] * hy[i + 1][3] * dj) * it +
-                              f2 * f2 * t * (fu[i] * hy[j + 1][0] + fu[j] * hy[i + 1][0]) +
-                              R(2.) * g * f2 * (fu[i] * hy[j + 1][3] + fu[j] * hy[i + 1][3]) * it);
-        const R cross = ch * (g * (pi[3][i + 1] * dj + pi[3][j + 1] * di) * it + f2 * (pi[0][i + 1] * dj + pi[0][j + 1] * di) * it);
-        const R Fdo2 = -(-gugjs + sigu - vsig) / R(4.) + (-fu[i] * g * hy[j + 1][0] - fu[j] * g * hy[i + 1][0]) * geo / R(4.) +
-                            (common - cross) / R(4.);
-        R Fds2 = -(-gugjs - sigu + vsig - R(4.) * (fu[i] * fu[j]) * sgu_s * k13) / R(4.) +
-                      (-fu[i] * g * hy[j + 1][0] - fu[j] * g * hy[i + 1][0] + R(4.) * fu[i] * fu[j] * hy[0][0] * k13) * geo / R(4.) +
-                      (common + cross + ch * (R(4.) * fu[i] * fu[j] * (hy[3][0] * f2 * t + g * hy[3][3] * it + f2 * hy[0][3] * it) * k13)) / R(4.) -
-                      pi[i + 1][j + 1] * (g * itc + geo + g * divV) * k13;
+        R Fdo2, Fds2;
+        if (e3) {
+          const R common = ch * (t * f2 * (cmd[i + 1] * hy[j + 1][0] * di + cmd[j + 1] * hy[i + 1][0] * dj) +
+                                g * (cmd[i + 1] * hy[j + 1][3] * di + cmd[j + 1] * hy[i + 1][3] * dj) * it +
+                                f2 * f2 * t * (fu[i] * hy[j + 1][0] + fu[j] * hy[i + 1][0]) +
+                                R(2.) * g * f2 * (fu[i] * hy[j + 1][3] + fu[j] * hy[i + 1][3]) * it);
+          const R cross = ch * (g * (pi[3][i + 1] * dj + pi[3][j + 1] * di) * it + f2 * (pi[0][i + 1] * dj + pi[0][j + 1] * di) * it);
+          Fdo2 = -(-gugjs + sigu - vsig) / R(4.) + (-fu[i] * g * hy[j + 1][0] - fu[j] * g * hy[i + 1][0]) * geo / R(4.) +
+                 (common - cross) / R(4.);
+          Fds2 = -(-gugjs - sigu + vsig - R(4.) * (fu[i] * fu[j]) * sgu_s * k13) / R(4.) +
+                 (-fu[i] * g * hy[j + 1][0] - fu[j] * g * hy[i + 1][0] + R(4.) * fu[i] * fu[j] * hy[0][0] * k13) * geo / R(4.) +
+                 (common + cross + ch * (R(4.) * fu[i] * fu[j] * (hy[3][0] * f2 * t + g * hy[3][3] * it + f2 * hy[0][3] * it) * k13)) / R(4.) -
+                 pi[i + 1][j + 1] * (g * itc + geo + g * divV) * k13;
+        } else {
+          Fdo2 = -(-gugjs + sigu - vsig) / R(4.);
+          if (fj0) Fds2 = -(-gugjs - sigu + vsig) / R(4.);
+          else Fds2 = -(-gugjs - sigu + vsig - R(4.) * (fu[i] * fu[j]) * sgu_s * k13) / R(4.) +
+                      (ch * (R(4.) * fu[i] * fu[j] * (g * hy[3][3] * it) * k13)) / R(4.);
+          Fds2 = Fds2 - pi[i + 1][j + 1] * (g * itc + g * divV) * k13;
+        }
         if (j == 2 && !cart) {
-          FD2 += g * pi[3][i + 1] * it + f2 * pi[0][i + 1] * it;
-          Fsg += -fu[i] * f2 * f2 * t / R(2.) - fu[i] * f2 * g * it;
+          if (e3) {
+            FD2 += g * pi[3][i + 1] * it + f2 * pi[0][i + 1] * it;
+            Fsg += -fu[i] * f2 * f2 * t / R(2.) - fu[i] * f2 * g * it;
+          } else {
+            FD2 += g * pi[3][i + 1] * it;
+          }
         }
         if (i == j) {
           Fsg += -cmd[i + 1] * expn * k13;
-          Fds2 += -cmd[i + 1] * sgu_s * k13 - cmd[i + 1] * hy[0][0] * geo * k13 -
-                  ch * (cmd[i + 1] * (hy[3][0] * f2 * t + g * hy[3][3] * it + f2 * hy[0][3] * it) * k13);
+          if (e3) Fds2 += -cmd[i + 1] * sgu_s * k13 - cmd[i + 1] * hy[0][0] * geo * k13 -
+                          ch * (cmd[i + 1] * (hy[3][0] * f2 * t + g * hy[3][3] * it + f2 * hy[0][3] * it) * k13);
+          else Fds2 += -cmd[i + 1] * sgu_s * k13 - ch * (cmd[i + 1] * (g * hy[3][3] * it) * k13);
         }
         if (diag) sigF[slot] = Fsg;
-        R F = (-pi[i + 1][j + 1] - tdelta * Fdl - tpi * FD2 + R(2.) * tpi * Fdo2 * uv - tpp * Fds2 +
-                    (R(2.) * eta + lpP * Pi) * Fsg + phi6 * Pi * pi[i + 1][j + 1] + phi7 * (sml + fu[i] * fu[j] * ss * k13)) *
-                   istg;
+        R F = -pi[i + 1][j + 1] - tdelta * Fdl;
+        if (e3 || j == 2) F = F - tpi * FD2;   // FD2 vanishes in 2-D off the eta row
+        F = F + R(2.) * tpi * Fdo2 * uv - tpp * Fds2;
+        if (!fj0) F = F + (R(2.) * eta + lpP * Pi) * Fsg;
+        F = (F + phi7 * (fj0 ? sml : sml + fu[i] * fu[j] * ss * k13)) * istg;
         if (i == j) F += phi7 * (-cmd[i + 1] * ss) * (k13 * istg);
         Fext[slot] = F;
 #pragma unroll
         for (int kk = 0; kk < D; kk++) {
-          const R MD2 = g * (fu[i] * hy[j + 1][kk + 1] - fu[i] * hy[j + 1][0] * fuc[kk] * ig + fu[j] * hy[i + 1][kk + 1] -
-                                  fu[j] * hy[i + 1][0] * fuc[kk] * ig);
-          R Msg = -fu[i] * fu[j] * fuc[kk] * (k13 * ig);
+          R MD2, Msg = R(0.0), Mdo2, Mds2;
           const R Mdl = -pi[i + 1][j + 1] * fuc[kk] * ig;
-          R Mdo2 = (-fu[i] * hy[j + 1][kk + 1] * g - fu[j] * hy[i + 1][kk + 1] * g + fuc[kk] * fu[i] * hy[j + 1][0] +
-                         fuc[kk] * fu[j] * hy[i + 1][0]) / R(4.);
-          R Mds2 = (-fu[i] * hy[j + 1][kk + 1] * g - fu[j] * hy[i + 1][kk + 1] * g + fuc[kk] * fu[i] * hy[j + 1][0] +
-                         fuc[kk] * fu[j] * hy[i + 1][0] + R(4.) * fu[i] * fu[j] * (hy[0][kk + 1] - hy[0][0] * fuc[kk] * ig) * k13 +
-                         R(4.) * pi[i + 1][j + 1] * fuc[kk] * k13 * ig) / R(4.);
+          if (!fj0) {
+            MD2 = g * (fu[i] * hy[j + 1][kk + 1] - fu[i] * hy[j + 1][0] * fuc[kk] * ig + fu[j] * hy[i + 1][kk + 1] -
+                       fu[j] * hy[i + 1][0] * fuc[kk] * ig);
+            Msg = -fu[i] * fu[j] * fuc[kk] * (k13 * ig);
+            Mdo2 = (-fu[i] * hy[j + 1][kk + 1] * g - fu[j] * hy[i + 1][kk + 1] * g + fuc[kk] * fu[i] * hy[j + 1][0] +
+                    fuc[kk] * fu[j] * hy[i + 1][0]) / R(4.);
+            Mds2 = (-fu[i] * hy[j + 1][kk + 1] * g - fu[j] * hy[i + 1][kk + 1] * g + fuc[kk] * fu[i] * hy[j + 1][0] +
+                    fuc[kk] * fu[j] * hy[i + 1][0] + R(4.) * fu[i] * fu[j] * (hy[0][kk + 1] - hy[0][0] * fuc[kk] * ig) * k13 +
+                    R(4.) * pi[i + 1][j + 1] * fuc[kk] * k13 * ig) / R(4.);
+          } else {
+            MD2 = g * (fu[i] * hy[j + 1][kk + 1] - fu[i] * hy[j + 1][0] * fuc[kk] * ig);
+            Mdo2 = (-fu[i] * hy[j + 1][kk + 1] * g + fuc[kk] * fu[i] * hy[j + 1][0]) / R(4.);
+            Mds2 = (-fu[i] * hy[j + 1][kk + 1] * g + fuc[kk] * fu[i] * hy[j + 1][0] +
+                    R(4.) * pi[i + 1][j + 1] * fuc[kk] * k13 * ig) / R(4.);
+          }
           if (kk == i) {            // i = k terms
             Mds2 += pi[0][j + 1] / R(4.);
             Mdo2 += -pi[0][j + 1] / R(4.);
-            Msg += -g * fu[j] / R(2.);
+            if (!fj0) Msg += -g * fu[j] / R(2.);
           }
           if (kk == j && j < D) {   // j = k terms
             Msg += -g * fu[i] / R(2.);
@@ -439,8 +488,9 @@ __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, cons
             Mds2 += -cmd[i + 1] * (hy[0][kk + 1] - hy[0][0] * fuc[kk] * ig) * k13;
           }
           if (diag) sigM[slot][kk] = Msg;
-          Mext[slot][kk] = (-tpi * MD2 - tdelta * Mdl + R(2.) * tpi * Mdo2 * uv - tpp * Mds2 + (R(2.) * eta + lpP * Pi) * Msg) *
-                           istg;
+          R mx = -tpi * MD2 - tdelta * Mdl + R(2.) * tpi * Mdo2 * uv - tpp * Mds2;
+          if (!fj0) mx = mx + (R(2.) * eta + lpP * Pi) * Msg;
+          Mext[slot][kk] = mx * istg;
         }
       }
     }
@@ -455,11 +505,11 @@ __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, cons
     Mb[i] = (ztil * uc[i] * ig) * isgP;
     Ms[i] = (Pi * uc[i] * ig) * isgT;
   }
-  R Fb = -(ztil * expn + Pi - k.phi1 * Pi * Pi) * isgP;
+  R Fb = -(ztil * expn + Pi) * isgP;
   R Fs = (-Pi * expn) * isgT;
   if (cfg.using_shear) {
     Fs += Fnab * isgT;
-    Fb += -(k.lambda_Pipi * Fnab - k.phi3 * ss) * isgP;
+    Fb += -(k.lambda_Pipi * Fnab) * isgP;
 #pragma unroll
     for (int i = 0; i < D; i++) {
       Mb[i] += -k.lambda_Pipi * Mnab[i] * isgP;
@@ -478,17 +528,20 @@ __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, cons
   R Mw[3];
 #pragma unroll
   for (int i = 0; i < D; i++) Mw[i] = X * uc[i] * ig + sig * dwds * Ms[i];
-  const R Fw = -X * (geo + g * itc + g * divV) + sig * dwds * Fs;
-  const R Fbulk = sig * Fb - Pi * (g * divV + g * itc + geo) * ig;
+  const R Fw = -X * (e3 ? geo + g * itc + g * divV : g * itc + g * divV) + sig * dwds * Fs;
+  const R Fbulk = sig * Fb - Pi * (e3 ? g * divV + g * itc + geo : g * divV + g * itc) * ig;
   R Mu[9], Fu[3];
 #pragma unroll
   for (int i = 0; i < D; i++) {
 #pragma unroll
     for (int j = 0; j < D; j++) Mu[i * D + j] = u[i] * g * (Mb[j] + Mw[j]) - u[i] * uc[j] * (w + Pi) * ig + M0i[i * D + j];
     Mu[i * D + i] += g * (w + Pi);
-    Fu[i] = (gP[i] + gB[i]) - g * (Fw + Fbulk) * u[i] - (w + Pi) * expn * u[i] - R(2.) * (w + Pi) * g * uD * dEta(i) * it;
-    if (cfg.using_shear)
-      Fu[i] += -P(i + 1, 0) * itc - R(2.) * dEta(i) * P(0, 3) * it - in.divshear[i] + in.gradshear[i] - F0i[i];
+    Fu[i] = (gP[i] + gB[i]) - g * (Fw + Fbulk) * u[i] - (w + Pi) * expn * u[i];
+    if (e3) Fu[i] = Fu[i] - R(2.) * (w + Pi) * g * uD * dEta(i) * it;
+    if (cfg.using_shear) {
+      if (e3) Fu[i] += -P(i + 1, 0) * itc - R(2.) * dEta(i) * P(0, 3) * it - in.divshear[i] + in.gradshear[i] - F0i[i];
+      else Fu[i] += -P(i + 1, 0) * itc - in.divshear[i] + in.gradshear[i] - F0i[i];
+    }
   }
   // ---- diffusion sector: time components of the q MRFs and the charge
   // MRFs, coupled into the four-acceleration -----------------------------------

@@ -408,6 +408,16 @@ ccake_status_t ccake_eos_invert_device(ccake_ctx* ctx, int32_t entropy_mode, int
                                        const double* d_in4, double* d_tbqs, double* d_th16, int32_t* d_status,
                                        int32_t* d_iters, void* stream);
 
+/* The SPH cubic-spline kernel the FP64 pair loops evaluate, on the GPU: for
+ * each squared distance r2[i] (finite, >= 0) in a run of dim (2 or 3)
+ * dimensions with smoothing length h, w[i] = W(sqrt(r2[i]), h) and fg[i] the
+ * radial factor of its gradient, grad_a W = fg (r_a - r_b); both 0 beyond
+ * r = 2h. Host arrays of n values; synchronous. Replaces
+ * SPHkernel<D>::kernel(distance, hT) and SPHkernel<D>::gradKernel(rel,
+ * distance, hT) (include/kernel.h:22-30, src/kernel.cpp:36-118) for a batch
+ * of pairs. */
+ccake_status_t ccake_sph_kernel(int32_t dim, double h, int64_t n, const double* r2, double* w, double* fg);
+
 /* ------------------------------------------------------------------------
  * Event server: continuous batching of independent hydro events on one GPU.
  * No reference counterpart (the reference runs one event per process).
