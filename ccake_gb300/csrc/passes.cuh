@@ -74,17 +74,18 @@ __device__ __forceinline__ float rsqrt_hw(float x) {
 // factor fg of grad_a W = fg (r_a - r_b) (:95-118), fg = gn (2 - q)^2 / r for
 // 1 <= q < 2 and gn2 (1.5 q - 2) / h for q < 1, q = r / h. The FP64 pipe
 // bounds the FP64 passes, so this spends as few FP64 instructions as it can
-// (15 a pair):
-//  * 1/r: the FP32 hardware estimate y0 (rsqrt_hw) refined by one
-//    Newton-Raphson step for the inverse square root, y = y0 + (y0 / 2)
-//    (1 - d2 y0^2). The step squares the relative error: with e0 <= 2^-22.9
-//    (estimate) + 2^-24 (the truncated input), |y r - 1| <= 1.5 e0^2 + a few
-//    FP64 roundings, below 1e-13.
+// (17 a pair):
+//  * 1/r: the FP32 hardware estimate y0 (rsqrt_hw, relative error d <=
+//    2^-22.9 + 2^-24 for the truncated input) refined by the third-order
+//    step of the binomial series y = y0 (1 - e)^(-1/2) = y0 (1 + e/2 +
+//    3 e^2/8 + ...), e = 1 - d2 y0^2 (Householder's method of order 2 for
+//    x^(-1/2)): the truncation error is about 5 |e|^3 / 16 = 2.5 d^3 < 1e-19,
+//    so y is 1/r to within the few roundings of the step (~2 ulp).
 //  * the FP64 <-> FP32 moves of the estimate are done on the IEEE bit
 //    patterns by integer instructions (a hardware conversion is an FP64-pipe
 //    instruction): d2 truncated to FP32, inputs below the smallest normal
 //    FP32 number lifted to it (a zero distance still gives q = 0, W = wn);
-//    the normal FP32 estimate and its half widened exactly.
+//    the normal FP32 estimate widened exactly.
 //  * both polynomial branches are evaluated and selected; q >= 0, so the
 //    branch tests compare the high word of q on the integer pipe.
 // The result is symmetric in the pair (it depends on d2 alone), so the pair
@@ -94,9 +95,8 @@ __device__ __forceinline__ void pair_kernel(const RunConst& rc, double d2, doubl
   const unsigned xf = __funnelshift_l((unsigned)__double2loint(d2), (unsigned)(hi - (896 << 20)), 3);
   const unsigned yb = __float_as_uint(rsqrt_hw(__uint_as_float(xf)));
   const double y0 = __hiloint2double((int)((yb >> 3) + (896u << 20)), (int)(yb << 29));
-  const double hy0 = __hiloint2double((int)((yb >> 3) + (895u << 20)), (int)(yb << 29));
   const double e = fma(-(d2 * y0), y0, 1.0);
-  const double y = fma(hy0, e, y0);   // 1/r
+  const double y = fma(y0, e * fma(0.375, e, 0.5), y0);   // 1/r
   const double q = (d2 * y) * rc.inv_h;
   const double Win = fma(q * q, fma(rc.win_c2, q, rc.win_c1), rc.wn);
   const double z = 2.0 - q, z2 = z * z;

@@ -3,7 +3,7 @@ SPHkernel<D>::kernel / gradKernel (src/kernel.cpp:36-118) and against an
 independent numpy evaluation with a correctly rounded square root.
 
 The device function takes 1/r from the FP32 hardware estimate and one
-Newton-Raphson step; its error bound (relative error of 1/r below 1e-13) is
+third-order correction step; its error bound (1/r to within a few ulp) is
 what these checks hold it to, at every lattice distance of the benchmark
 grids (q = 1 and q = 2 exactly among them), at random distances and at zero.
 """
@@ -11,7 +11,7 @@ import numpy as np
 import pytest
 
 from ccake_gb300 import api
-from oracle import oracle_py as O
+import oracle_py as O
 
 pytestmark = pytest.mark.gpu
 
@@ -60,14 +60,14 @@ def test_pair_kernel_matches_oracle_and_bound(D, h, dx):
     wscale = np.max(np.abs(Wo))
     inside = r2 < (2 * h) ** 2 * (1 - 1e-12)
     for ref in (Wo, Wn):
-        assert np.max(np.abs(W - ref)) <= 1e-13 * wscale
+        assert np.max(np.abs(W - ref)) <= 2e-15 * wscale
         # relative to the value itself away from the cut, where W -> 0
         far = inside & (np.abs(ref) > 1e-3 * wscale)
-        assert np.max(np.abs(W[far] / ref[far] - 1)) < 1e-12
+        assert np.max(np.abs(W[far] / ref[far] - 1)) < 1e-13
     nz = r2 > 0
     fscale = np.max(np.abs(fo[nz]))
     for ref in (fo, fn):
-        assert np.max(np.abs(fg[nz] - ref[nz])) <= 1e-13 * fscale
+        assert np.max(np.abs(fg[nz] - ref[nz])) <= 2e-15 * fscale
     # beyond 2h both vanish; at 0 the value of the q < 1 branch (its product
     # with the zero separation is the zero gradient)
     assert np.all(W[r2 > (2 * h) ** 2] == 0) and np.all(fg[r2 > (2 * h) ** 2] == 0)
