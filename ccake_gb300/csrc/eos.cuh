@@ -746,6 +746,33 @@ __host__ __device__ inline int eos_invert_first(const EosDev& e, int entropy, co
   return k;
 }
 
+// The first attempt of eos_invert in seed mode 1 (entropy mode) when the
+// analytic inverse settles it: the model tried first is conformal or
+// conformal-diagonal and its exact inverse passes the residual and c_s^2
+// tests. Returns the chain index with x and o_out as eos_invert gives them
+// then (no Newton steps), or -2 (the caller runs eos_invert). Only the two
+// analytic models are compiled in, so a kernel built on it stays small.
+__host__ __device__ inline int eos_analytic_first(const EosDev& e, const double* target, int start, double* x,
+                                                  double* o_out) {
+  const double tgt[4] = {target[0], target[1], target[3], target[2]};  // (s, B, Q, S)
+  const int k = start > 0 ? start : 0;
+  if (k >= chain_len(e.kind)) return -2;
+  const int model = chain_model(e.kind, k);
+  if (model != M_CONF && model != M_CDIAG) return -2;
+  double y[4];
+  if (!analytic_seed(e, model, tgt, y)) return -2;
+  const Scales sc = model_scales(e, model);
+  double o[17];
+  if (model == M_CONF) conformal_thermo(sc, y, o);
+  else confdiag_thermo(sc, y, o);
+  const double fres = fmax(fmax(fabs(o[1] - tgt[0]), fabs(o[2] - tgt[1])),
+                           fmax(fabs(o[4] - tgt[2]), fabs(o[3] - tgt[3])));
+  if (!(fres < 1e-10 && o[6] >= 0.0 && o[6] <= 1.0)) return -2;
+  for (int i = 0; i < 4; i++) x[i] = y[i];
+  for (int i = 0; i < 17; i++) o_out[i] = o[i];
+  return k;
+}
+
 // a^T m^-1 b with the reference's guard on m11, m22 (src/eos_derivatives.cpp:457-560).
 __host__ __device__ inline double aTmb(const double* a, double m[3][3], const double* b) {
   const double EPS = 1e-3;

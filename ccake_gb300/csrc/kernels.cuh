@@ -75,6 +75,8 @@ struct Ptrs {
 // by value, read as __grid_constant__), as the single-event kernels' did;
 // what the kernels change between steps lives in device memory (EventState).
 constexpr int kGroupMax = 16;
+// eos_iters of a particle the analytic EoS pass left to the full inversion
+constexpr int32_t kEosPending = -1;
 
 struct EventDesc {
   RunConst rc;

@@ -177,10 +177,10 @@ __device__ __forceinline__ void passA_mixed_body(const RunConst& rc, const Ptrs&
   const double tm = rc.cfg.coord == 1 ? 1.0 : t;   // the metric's tau (1 in Cartesian coordinates)
   const double g = gamma_milne<D>(u3, tm * tm);
   p.gam[i] = g;
+  const double ig = 1.0 / g, igt = 1.0 / (g * tm);
 #pragma unroll
-  for (int q = 0; q < 3; q++) p.v[q * n + i] = (q < D) ? u3[q] / g : 0.0;
+  for (int q = 0; q < 3; q++) p.v[q * n + i] = (q < D) ? u3[q] * ig : 0.0;
   const double slab = sl.value64();
-  const double igt = 1.0 / (g * tm);
   p.slab[i] = slab;
   p.sig[i] = slab * igt;
   p.th[T_S * n + i] = s0.value64() * igt;
@@ -194,9 +194,38 @@ __device__ __forceinline__ void passA_mixed_body(const RunConst& rc, const Ptrs&
 // FP64 Newton solve needs ~255 registers a thread, which would cap the
 // occupancy of the gather loop above at 8 warps an SM.
 template <int D>
-__device__ __forceinline__ void thermo_mixed_body(const RunConst& rc, const EosDev& eos, const Ptrs& p, const int i) {
+__device__ __forceinline__ void thermo_mixed_body(const RunConst& rc, const EosDev& eos, const Ptrs& p, const int i,
+                                                  bool pending_only) {
   if (i >= p.n) return;
+  if (pending_only && p.eos_iters[i] != kEosPending) return;
   thermo_tail<D, true>(rc, eos, p, i, p.clock->t);
+}
+
+// The EoS pass of the mixed form for the analytic models (conformal and
+// conformal-diagonal, no pre-inverted tables): eos_invert's first attempt in
+// seed mode 1 -- the exact inverse, accepted by the reference's residual
+// test -- settles every particle it can, in a kernel a fraction of the full
+// inverter's size (more warps an SM for the FP64 pipe to draw on). The
+// particles it does not settle, and every particle of a table EoS, are
+// marked pending for the full inversion (k_thermo_mixed with pending_only),
+// which starts over from the same state: the results are eos_invert's.
+template <int D>
+__device__ __forceinline__ void thermo_fast_body(const RunConst& rc, const EosDev& eos, const Ptrs& p, const int i) {
+  if (i >= p.n) return;
+  const int n = p.n;
+  double x[4], o[17];
+  int k = -2;
+  if (!eos.pre) {
+    const double tgt[4] = {p.th[T_S * n + i], p.th[T_RB * n + i], p.th[T_RS * n + i], p.th[T_RQ * n + i]};
+    k = eos_analytic_first(eos, tgt, p.eos_id[i], x, o);
+  }
+  if (k < 0) {
+    p.eos_iters[i] = kEosPending;
+    return;
+  }
+  double th[NTH];
+  set_thermo_o(eos, k, x, o, th, true);
+  thermo_store<D, true, false>(rc, p, i, p.clock->t, th, k, 0);
 }
 
 // Pass B, mixed form, part 1: separable gradient sums over the list pass A
@@ -397,11 +426,19 @@ __global__ void __launch_bounds__(kBlock) k_passA_mixed(const __grid_constant__ 
 }
 
 template <int D>
-__global__ void __launch_bounds__(kBlock) k_thermo_mixed(const __grid_constant__ GroupArgs g) {
+__global__ void __launch_bounds__(kBlock) k_thermo_fast(const __grid_constant__ GroupArgs g) {
   int first;
   const int e = group_event(g, first);
   if (e < 0) return;
-  thermo_mixed_body<D>(g.ev[e].rc, g.ev[e].eos, g.ev[e].p, first + threadIdx.x);
+  thermo_fast_body<D>(g.ev[e].rc, g.ev[e].eos, g.ev[e].p, first + threadIdx.x);
+}
+
+template <int D>
+__global__ void __launch_bounds__(kBlock) k_thermo_mixed(const __grid_constant__ GroupArgs g, int pending_only) {
+  int first;
+  const int e = group_event(g, first);
+  if (e < 0) return;
+  thermo_mixed_body<D>(g.ev[e].rc, g.ev[e].eos, g.ev[e].p, first + threadIdx.x, pending_only != 0);
 }
 
 template <int D>
@@ -485,14 +522,28 @@ void launch_pack_mixed(const RunConst& rc, const Ptrs& p, cudaStream_t s) {
   else k_pack_mixed<2><<<nb, kBlock, 0, s>>>(p);
 }
 
+// The analytic EoS pass runs when an event of the group has an analytic
+// model first in its chain (conformal, conformal-diagonal; no pre-inverted
+// tables); the full inversion then takes only the particles it left.
+static bool group_has_analytic(const GroupArgs& g) {
+  for (int e = 0; e < g.nev; e++) {
+    const EosDev& q = g.ev[e].eos;
+    if (!q.pre && q.kind != 2) return true;
+  }
+  return false;
+}
+
 void launch_passA_mixed(const GroupArgs& g, int dim, cudaStream_t s) {
   const int nb = g.first_block[g.nev];
+  const int fast = group_has_analytic(g) ? 1 : 0;
   if (dim == 3) {
     k_passA_mixed<3><<<nb, kBlock, 0, s>>>(g);
-    k_thermo_mixed<3><<<nb, kBlock, 0, s>>>(g);
+    if (fast) k_thermo_fast<3><<<nb, kBlock, 0, s>>>(g);
+    k_thermo_mixed<3><<<nb, kBlock, 0, s>>>(g, fast);
   } else {
     k_passA_mixed<2><<<nb, kBlock, 0, s>>>(g);
-    k_thermo_mixed<2><<<nb, kBlock, 0, s>>>(g);
+    if (fast) k_thermo_fast<2><<<nb, kBlock, 0, s>>>(g);
+    k_thermo_mixed<2><<<nb, kBlock, 0, s>>>(g, fast);
   }
 }
 

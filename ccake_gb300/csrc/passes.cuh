@@ -168,10 +168,13 @@ __device__ __forceinline__ void write_recAf(const Ptrs& p, int i, const double* 
 // DIFF: the diffusion sector (FP64 form): the alpha derivatives at the
 // solution, q^mu from the extensive current (src/eom_default.cpp:140-165),
 // the regulator (src/sph_workstation.cpp:132-218) and the diffusion record.
+template <int D, bool MIX, bool DIFF>
+__device__ __forceinline__ void thermo_store(const RunConst& rc, const Ptrs& p, int i, double t, const double* th,
+                                             int k, int iters);
+
 template <int D, bool MIX, bool DIFF = false>
 __device__ __forceinline__ void thermo_tail(const RunConst& rc, const EosDev& eos, const Ptrs& p, int i, double t) {
   const int n = p.n;
-  const double t2 = rc.cfg.coord == 1 ? 1.0 : t * t;   // the metric's tau^2 (1 in Cartesian coordinates)
   double th[NTH];
   double x[4] = {p.th[T_T * n + i], p.th[T_MUB * n + i], p.th[T_MUQ * n + i], p.th[T_MUS * n + i]};
   const double tgt[4] = {p.th[T_S * n + i], p.th[T_RB * n + i], p.th[T_RS * n + i], p.th[T_RQ * n + i]};
@@ -213,6 +216,18 @@ __device__ __forceinline__ void thermo_tail(const RunConst& rc, const EosDev& eo
       for (int q = 0; q < 12; q++) p.dif[(size_t)(F_DA + q) * n + i] = da[q];
     }
   }
+  thermo_store<D, MIX, DIFF>(rc, p, i, t, th, k, iters);
+}
+
+// Everything of the EoS pass after the inversion, for particle i with the
+// thermodynamics th (chain index k, iters Newton steps): the stored
+// thermodynamics, pi^{mu nu} and Pi from the extensive forms, and the
+// gradient record (FP64 or mixed form; DIFF: the diffusion record).
+template <int D, bool MIX, bool DIFF>
+__device__ __forceinline__ void thermo_store(const RunConst& rc, const Ptrs& p, int i, double t, const double* th,
+                                             int k, int iters) {
+  const int n = p.n;
+  const double t2 = rc.cfg.coord == 1 ? 1.0 : t * t;   // the metric's tau^2 (1 in Cartesian coordinates)
 #pragma unroll
   for (int q = 0; q < NTH; q++) p.th[q * n + i] = th[q];
   p.eos_id[i] = k;
@@ -224,7 +239,7 @@ __device__ __forceinline__ void thermo_tail(const RunConst& rc, const EosDev& eo
 #pragma unroll
   for (int q = 0; q < 5; q++) es[q] = p.y[(Y_SHV0 + q) * n + i];
   double pi[NPI];
-  reset_pi(es, sig, g, u3, t2, pi);
+  reset_pi<D>(es, sig, g, u3, t2, pi);
   const double Pi = p.y[Y_EBULK * n + i] * sig;
   p.bulk[i] = Pi;
 #pragma unroll

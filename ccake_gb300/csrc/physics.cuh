@@ -157,6 +157,9 @@ __device__ __forceinline__ double gamma_milne(const double* u, double t2) {
 
 // pi^{mu nu} from the extensive spatial components, tracelessness and
 // orthogonality (reference src/eom_default.cpp:56-172). pi[] uses PiSlot.
+// In 2-D the eta velocity is zero and its terms are left out (the same
+// values; a product with a constant zero would still cost FP64 instructions).
+template <int D>
 __device__ inline void reset_pi(const double* ext_shv, double sigma, double g, const double* u3, double t2,
                                 double* pi) {
   const double f0 = -u3[0], f1 = -u3[1], f2 = -t2 * u3[2];   // covariant u_i
@@ -164,13 +167,23 @@ __device__ inline void reset_pi(const double* ext_shv, double sigma, double g, c
   const double p22 = ext_shv[3] * sigma, p23 = ext_shv[4] * sigma;
   // one division each for 1/t^2 and 1/g (FP64 division is a long sequence)
   const double it2 = 1.0 / t2, ig = 1.0 / g;
-  const double p00 = (f0 * f0 * p11 + f1 * f1 * p22 + 2. * f1 * f0 * p12 + 2. * f2 * f0 * p13 + 2. * f2 * f1 * p23 -
-                      f2 * f2 * (p11 + p22) * it2) / (g * g - f2 * f2 * it2);
+  double p00;
+  if (D == 3)
+    p00 = (f0 * f0 * p11 + f1 * f1 * p22 + 2. * f1 * f0 * p12 + 2. * f2 * f0 * p13 + 2. * f2 * f1 * p23 -
+           f2 * f2 * (p11 + p22) * it2) / (g * g - f2 * f2 * it2);
+  else
+    p00 = (f0 * f0 * p11 + f1 * f1 * p22 + 2. * f1 * f0 * p12) / (g * g);
   const double p33 = (p00 - p11 - p22) * it2;
   pi[P00] = p00; pi[P11] = p11; pi[P12] = p12; pi[P13] = p13; pi[P22] = p22; pi[P23] = p23; pi[P33] = p33;
-  pi[P01] = -(p11 * f0 + p12 * f1 + p13 * f2) * ig;
-  pi[P02] = -(p12 * f0 + p22 * f1 + p23 * f2) * ig;
-  pi[P03] = -(p13 * f0 + p23 * f1 + p33 * f2) * ig;
+  if (D == 3) {
+    pi[P01] = -(p11 * f0 + p12 * f1 + p13 * f2) * ig;
+    pi[P02] = -(p12 * f0 + p22 * f1 + p23 * f2) * ig;
+    pi[P03] = -(p13 * f0 + p23 * f1 + p33 * f2) * ig;
+  } else {
+    pi[P01] = -(p11 * f0 + p12 * f1) * ig;
+    pi[P02] = -(p12 * f0 + p22 * f1) * ig;
+    pi[P03] = -(p13 * f0 + p23 * f1) * ig;
+  }
 }
 
 // Inputs of the equations of motion for one particle.
