@@ -152,6 +152,67 @@ __host__ __device__ inline double knorm2(int D) { return D == 1 ? 1. / 6. : D ==
 __host__ __device__ inline double kgrad(int D) { return D == 1 ? -1. / 2. : D == 2 ? -15. / (14. * M_PI) : -3. / (4. * M_PI); }
 __host__ __device__ inline double kgrad2(int D) { return D == 1 ? 1. : D == 2 ? 15. / (7. * M_PI) : 3. / (2. * M_PI); }
 
+// FP64 <-> FP32 conversions and the FP64 finiteness test on the integer pipe
+// (device; plain casts on the host). A hardware conversion issues to the
+// FP64 pipe, the narrowest unit of this GPU -- in the mixed-form kernels the
+// conversions kept it busier than their FP64 arithmetic did -- while the
+// integer pipe has room to spare. Both follow the IEEE 754 binary32 and
+// binary64 formats: narrowing rounds to nearest, ties to even, for
+// magnitudes in the normal FP32 range (the bits a hardware conversion gives
+// there), gives signed zero below that range and infinity above it, and
+// keeps NaN; widening is exact for normal FP32 values, zeros, infinities and
+// NaN, and flushes FP32 subnormals to signed zero.
+__host__ __device__ __forceinline__ float f32_rn(double x) {
+#ifdef __CUDA_ARCH__
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned s = (unsigned)(b >> 32) & 0x80000000u;
+  const unsigned long long m = b & 0x7FFFFFFFFFFFFFFFull;
+  const unsigned long long t = m - (896ull << 52);   // exponent bias 1023 -> 127
+  const unsigned long long r = (t + 0x0FFFFFFFull + ((t >> 29) & 1ull)) >> 29;
+  unsigned f = r >= 0x7F800000ull ? 0x7F800000u : (unsigned)r;
+  if (m < (897ull << 52)) f = 0u;
+  if (m >= 0x7FF0000000000000ull) f = m == 0x7FF0000000000000ull ? 0x7F800000u : 0x7FC00000u;
+  return __uint_as_float(s | f);
+#else
+  return (float)x;
+#endif
+}
+
+__host__ __device__ __forceinline__ double f64_of(float v) {
+#ifdef __CUDA_ARCH__
+  const unsigned b = __float_as_uint(v);
+  const unsigned s = b & 0x80000000u, m = b & 0x7FFFFFFFu;
+  unsigned hi = s | ((m >> 3) + (896u << 20));   // exponent bias 127 -> 1023
+  if (m >= 0x7F800000u) hi = s | 0x7FF00000u | ((m & 0x007FFFFFu) >> 3);
+  if (m < 0x00800000u) hi = s;
+  const unsigned lo = m < 0x00800000u ? 0u : (m << 29);
+  return __hiloint2double((int)hi, (int)lo);
+#else
+  return (double)v;
+#endif
+}
+
+__host__ __device__ __forceinline__ bool finite64(double x) {
+#ifdef __CUDA_ARCH__
+  return (__double2hiint(x) & 0x7FF00000) != 0x7FF00000;
+#else
+  return std::isfinite(x);
+#endif
+}
+
+// R(x) for the arithmetic type R of a templated kernel body (FP64 or FP32),
+// and back, by the conversions above.
+template <typename R>
+__host__ __device__ __forceinline__ R narrow(double x) {
+  if constexpr (sizeof(R) == sizeof(float)) return f32_rn(x);
+  else return x;
+}
+template <typename R>
+__host__ __device__ __forceinline__ double widen(R x) {
+  if constexpr (sizeof(R) == sizeof(float)) return f64_of(x);
+  else return x;
+}
+
 // Kernel constants of a run with smoothing length h in D dimensions (host).
 inline void set_kernel_constants(RunConst& rc, int D, double h) {
   rc.cut2 = (2.0 * h) * (2.0 * h);

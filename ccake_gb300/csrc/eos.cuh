@@ -594,7 +594,7 @@ __host__ __device__ inline double cbrt_halley(double x) {
   const double ax = fabs(x);
   if (ax == 0.0) return x;   // a zero density (no strangeness, say) is its own cube root
   if (!(ax > 1e-30 && ax < 1e30)) return cbrt(x);
-  const double y = (double)cbrtf((float)x);
+  const double y = f64_of(cbrtf(f32_rn(x)));
   const double y3 = y * y * y;
   return y * (y3 + 2.0 * x) / (2.0 * y3 + x);
 }
@@ -904,8 +904,8 @@ __host__ __device__ inline void set_thermo_o(const EosDev& e, int k, const doubl
       for (int a = 0; a < 4; a++) {
         const double Haa = H[a][a];
         if (fp32_derivs) {
-          const float G = Haa != 0.0 ? 1.0f / (float)Haa : 0.0f;
-          th[T_DWDS + a] = (a == 0 || act[a]) ? (double)((float)mu[a] + (float)(a == 0 ? s : rho[a]) * G) : mu[a];
+          const float G = Haa != 0.0 ? 1.0f / f32_rn(Haa) : 0.0f;
+          th[T_DWDS + a] = (a == 0 || act[a]) ? f64_of(f32_rn(mu[a]) + f32_rn(a == 0 ? s : rho[a]) * G) : mu[a];
         } else {
           const double G = Haa != 0.0 ? 1.0 / Haa : 0.0;
           th[T_DWDS + a] = (a == 0 || act[a]) ? mu[a] + (a == 0 ? s : rho[a]) * G : mu[a];

@@ -332,7 +332,7 @@ __device__ __forceinline__ void passB_mixed_body(const RunConst& rc, const Ptrs&
   }
   // own values from the same FP32 record as the neighbours', so that a
   // uniform field gives a zero gradient up to the compensated sums' error
-  const float sla = (float)p.slab[i], isla = 1.0f / sla;
+  const float sla = f32_rn(p.slab[i]), isla = 1.0f / sla;
   const float ea = A2.x, Pa = A1.w, Pia = A2.y;
   const float va[3] = {A2.z, A2.w, D == 3 ? A3.x : 0.0f};
   const float pi0a[3] = {A3.y, A3.z, A3.w};

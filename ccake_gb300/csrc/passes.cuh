@@ -56,7 +56,7 @@ struct KSum {
     s = t;
   }
   __device__ __forceinline__ float value() const { return s - c; }
-  __device__ __forceinline__ double value64() const { return (double)s - (double)c; }
+  __device__ __forceinline__ double value64() const { return f64_of(s) - f64_of(c); }
 };
 
 // 1/sqrt(x) for normal x > 0 by the hardware approximation
@@ -134,8 +134,8 @@ __device__ __forceinline__ void ldg256(const float4* p, float4& a, float4& b) {
 
 // x = hi + lo with hi = fl32(x): the pair carries x to ~2^-48 relative.
 __device__ __forceinline__ void split2(double x, float& hi, float& lo) {
-  hi = (float)x;
-  lo = (float)(x - (double)hi);
+  hi = f32_rn(x);
+  lo = f32_rn(x - f64_of(hi));
 }
 
 // Smoothing record of particle i (FP64 form, plus the FP32 screen copy).
@@ -146,7 +146,7 @@ __device__ __forceinline__ void write_recA(const Ptrs& p, int i, const double* x
   ra[1] = make_double2(D == 3 ? x[2] : 0.0, m);
   ra[2] = make_double2(m * ext[0], m * ext[1]);
   ra[3] = make_double2(m * ext[2], m * ext[3]);
-  p.posf[i] = make_float4((float)x[0], (float)x[1], D == 3 ? (float)x[2] : 0.0f, 0.0f);
+  p.posf[i] = make_float4(f32_rn(x[0]), f32_rn(x[1]), D == 3 ? f32_rn(x[2]) : 0.0f, 0.0f);
 }
 
 // Smoothing record of particle i (mixed form).
@@ -156,9 +156,9 @@ __device__ __forceinline__ void write_recAf(const Ptrs& p, int i, const double* 
 #pragma unroll
   for (int k = 0; k < 3; k++) split2(k < D ? x[k] : 0.0, hi[k], lo[k]);
   float4* ra = reinterpret_cast<float4*>(p.recAf) + (size_t)i * (raf_stride<D>() / 4);
-  ra[0] = make_float4(hi[0], hi[1], hi[2], (float)m);
+  ra[0] = make_float4(hi[0], hi[1], hi[2], f32_rn(m));
   ra[1] = make_float4(lo[0], lo[1], lo[2], 0.0f);
-  ra[2] = make_float4((float)(m * ext[0]), (float)(m * ext[1]), (float)(m * ext[2]), (float)(m * ext[3]));
+  ra[2] = make_float4(f32_rn(m * ext[0]), f32_rn(m * ext[1]), f32_rn(m * ext[2]), f32_rn(m * ext[3]));
   if (D == 3) ra[3] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   p.posf[i] = make_float4(hi[0], hi[1], hi[2], 0.0f);
 }
@@ -297,15 +297,15 @@ __device__ __forceinline__ void thermo_store(const RunConst& rc, const Ptrs& p, 
     float hi[3], lo[3];
 #pragma unroll
     for (int k = 0; k < 3; k++) split2(k < D ? p.y[(Y_X0 + k) * n + i] : 0.0, hi[k], lo[k]);
-    const float f = (float)isl2;
+    const float f = f32_rn(isl2);
     float4* rb = reinterpret_cast<float4*>(p.recBf) + (size_t)i * (RBF / 4);
-    rb[0] = make_float4(hi[0], hi[1], hi[2], (float)p.m[i]);
-    rb[1] = make_float4(lo[0], lo[1], lo[2], (float)(th[T_P] * isl2));
-    rb[2] = make_float4((float)th[T_E], (float)(Pi * isl2), (float)p.v[i], (float)p.v[n + i]);
-    rb[3] = make_float4((float)p.v[2 * n + i], (float)pi[pi_slot(0, 1)] * f, (float)pi[pi_slot(0, 2)] * f,
-                        (float)pi[pi_slot(0, 3)] * f);
-    rb[4] = make_float4((float)pi[P11] * f, (float)pi[P12] * f, (float)pi[P13] * f, (float)pi[P22] * f);
-    rb[5] = make_float4((float)pi[P23] * f, (float)pi[P33] * f, 0.0f, 0.0f);
+    rb[0] = make_float4(hi[0], hi[1], hi[2], f32_rn(p.m[i]));
+    rb[1] = make_float4(lo[0], lo[1], lo[2], f32_rn(th[T_P] * isl2));
+    rb[2] = make_float4(f32_rn(th[T_E]), f32_rn(Pi * isl2), f32_rn(p.v[i]), f32_rn(p.v[n + i]));
+    rb[3] = make_float4(f32_rn(p.v[2 * n + i]), f32_rn(pi[pi_slot(0, 1)]) * f, f32_rn(pi[pi_slot(0, 2)]) * f,
+                        f32_rn(pi[pi_slot(0, 3)]) * f);
+    rb[4] = make_float4(f32_rn(pi[P11]) * f, f32_rn(pi[P12]) * f, f32_rn(pi[P13]) * f, f32_rn(pi[P22]) * f);
+    rb[5] = make_float4(f32_rn(pi[P23]) * f, f32_rn(pi[P33]) * f, 0.0f, 0.0f);
   } else {
     double* rb = p.recB + (size_t)i * RB;
     rb[B_X0] = p.y[Y_X0 * n + i];
@@ -381,7 +381,7 @@ __device__ __forceinline__ void finish_particle(const RunConst& rc, const Ptrs& 
   in.th = th;
 #pragma unroll
   for (int q = 0; q < 3; q++) {
-    in.u[q] = (q < D) ? R(p.y[(Y_U0 + q) * n + i]) : R(0);
+    in.u[q] = (q < D) ? narrow<R>(p.y[(Y_U0 + q) * n + i]) : R(0);
     in.v[q] = va[q];
     in.gradP[q] = gP[q];
     in.gradBulk[q] = gB[q];
@@ -390,13 +390,13 @@ __device__ __forceinline__ void finish_particle(const RunConst& rc, const Ptrs& 
   }
 #pragma unroll
   for (int q = 0; q < 9; q++) in.gradV[q] = gV[q];
-  in.g = R(p.gam[i]);
-  in.sigma = R(p.sig[i]);
-  in.sigma_lab = R(p.slab[i]);
-  in.m = R(p.m[i]);
-  in.Pi = R(p.bulk[i]);
+  in.g = narrow<R>(p.gam[i]);
+  in.sigma = narrow<R>(p.sig[i]);
+  in.sigma_lab = narrow<R>(p.slab[i]);
+  in.m = narrow<R>(p.m[i]);
+  in.Pi = narrow<R>(p.bulk[i]);
 #pragma unroll
-  for (int q = 0; q < NPI; q++) in.pi[q] = R(p.pi[q * n + i]);
+  for (int q = 0; q < NPI; q++) in.pi[q] = narrow<R>(p.pi[q * n + i]);
   const TransportT<R> k = transport<R>(rc.cfg, th);
   EomOut<R> o;
   DiffOut dout;
@@ -434,13 +434,13 @@ __device__ __forceinline__ void finish_particle(const RunConst& rc, const Ptrs& 
 #pragma unroll
   for (int q = 0; q < D; q++) {
     ynew[Y_X0 + q] += dt_sub * p.v[q * n + i];
-    ynew[Y_U0 + q] += dt_sub * double(o.du[q]);
+    ynew[Y_U0 + q] += dt_sub * widen<R>(o.du[q]);
   }
-  double es = ynew[Y_ES] + dt_sub * double(o.dS);
-  ynew[Y_EBULK] += dt_sub * double(o.dBulk);
+  double es = ynew[Y_ES] + dt_sub * widen<R>(o.dS);
+  ynew[Y_EBULK] += dt_sub * widen<R>(o.dBulk);
 #pragma unroll
-  for (int q = 0; q < 5; q++) ynew[Y_SHV0 + q] += dt_sub * double(o.dShv[q]);
-  ynew[Y_EZ] += dt_sub * double(o.dEz);
+  for (int q = 0; q < 5; q++) ynew[Y_SHV0 + q] += dt_sub * widen<R>(o.dShv[q]);
+  ynew[Y_EZ] += dt_sub * widen<R>(o.dEz);
   double yq[9];
   if constexpr (DIFF) {
 #pragma unroll
@@ -455,10 +455,10 @@ __device__ __forceinline__ void finish_particle(const RunConst& rc, const Ptrs& 
   ynew[Y_ES] = es;
   bool finite = true;
 #pragma unroll
-  for (int q = 0; q < NY; q++) finite = finite && isfinite(ynew[q]);
+  for (int q = 0; q < NY; q++) finite = finite && finite64(ynew[q]);
   if constexpr (DIFF) {
 #pragma unroll
-    for (int q = 0; q < 9; q++) finite = finite && isfinite(yq[q]);
+    for (int q = 0; q < 9; q++) finite = finite && finite64(yq[q]);
   }
   if (!finite) flag_error(p.err, E_NONFINITE);
 #pragma unroll

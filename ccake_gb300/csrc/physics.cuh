@@ -35,7 +35,7 @@ __device__ __forceinline__ R powi_or_pow(R x, R p) {
 template <typename R = double>
 __device__ inline TransportT<R> transport(const ccake_config& c, const double* th) {
   TransportT<R> k;
-  const R T = R(th[T_T]), w = R(th[T_W]), cs2 = R(th[T_CS2]), p = R(th[T_P]);
+  const R T = narrow<R>(th[T_T]), w = narrow<R>(th[T_W]), cs2 = narrow<R>(th[T_CS2]), p = narrow<R>(th[T_P]);
   const R eos = R(c.eta_over_s), zos = R(c.zeta_over_s), zp = R(c.zeta_cs2_p);
   const R k13 = R(1.0) / R(3.0);
   k.eta = (T <= R(0)) ? R(0) : eos * (w / T);
@@ -216,7 +216,7 @@ template <int D, typename R = double>
 __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, const EomIn<D, R>& in, double td,
                            EomOut<R>& o, R* diag = nullptr, const DiffIn* dif = nullptr, DiffOut* dout = nullptr) {
   R sigF[5] = {0, 0, 0, 0, 0}, sigM[5][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-  const R t = R(td);
+  const R t = narrow<R>(td);
   // Cartesian coordinates (coord = 1, src/eom_cartesian.cpp:210-1400): the
   // metric without tau (tm = 1) and none of the Milne connection terms (1/tau
   // sources, the geometric factor, the eta deltas; ch = 0, itc = 0)
@@ -230,9 +230,9 @@ __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, cons
   const R itc = cart ? R(0.0) : it, itm = cart ? R(1.0) : it;
   const R k13 = R(1.0) / R(3.0), k16 = R(1.0) / R(6.0);
   const double* th = in.th;
-  const R T = R(th[T_T]), w = R(th[T_W]), sden = R(th[T_S]), dwds = R(th[T_DWDS]);
-  const R rho[3] = {R(th[T_RB]), R(th[T_RS]), R(th[T_RQ])};
-  const R dwdr[3] = {R(th[T_DWDB]), R(th[T_DWDSS]), R(th[T_DWDQ])};
+  const R T = narrow<R>(th[T_T]), w = narrow<R>(th[T_W]), sden = narrow<R>(th[T_S]), dwds = narrow<R>(th[T_DWDS]);
+  const R rho[3] = {narrow<R>(th[T_RB]), narrow<R>(th[T_RS]), narrow<R>(th[T_RQ])};
+  const R dwdr[3] = {narrow<R>(th[T_DWDB]), narrow<R>(th[T_DWDSS]), narrow<R>(th[T_DWDQ])};
   const R Pi = in.Pi;
   auto P = [&](int i, int j) { return in.pi[pi_slot(i, j)]; };
   // covariant spatial velocity (Vector<D>::make_covariant)
@@ -795,7 +795,8 @@ __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, cons
   }
   // ---- dEz (reference :827-862) ---------------------------------------------
   const R u3 = (D == 3) ? u[2] : R(0.0);
-  o.dEz = ((R(th[T_E]) + R(th[T_P]) + Pi) * u3 * u3 + (R(th[T_P]) + Pi) * it2 + P(3, 3)) * in.m * t2 / in.sigma_lab;
+  o.dEz = ((narrow<R>(th[T_E]) + narrow<R>(th[T_P]) + Pi) * u3 * u3 + (narrow<R>(th[T_P]) + Pi) * it2 + P(3, 3)) * in.m * t2 /
+          in.sigma_lab;
 }
 
 }  // namespace ccake
