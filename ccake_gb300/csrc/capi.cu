@@ -841,7 +841,8 @@ ccake_status_t ccake_initialize(ccake_ctx* ctx) {
   if (!ctx) return CCAKE_ERR_INVALID;
   if (!ctx->loaded) return fail(ctx, CCAKE_ERR_STATE, "load particles first");
   if (ctx->eos.kind == 2 && !ctx->d_table) return fail(ctx, CCAKE_ERR_STATE, "set the EoS table first");
-  Clock c{ctx->cfg.t0, ctx->cfg.t0, ctx->cfg.t0, 0, 0, 0.0, 0.0};
+  const double t0 = ctx->cfg.t0;
+  Clock c{t0, t0, t0, 0, 0, 0.0, 0.0, 1.0 / t0, 1.0 / (t0 * t0)};
   CK(cudaMemcpyAsync(ctx->p.clock, &c, sizeof(Clock), cudaMemcpyHostToDevice, ctx->stream));
   ccake_status_t s = reset_errors(ctx);
   if (s) return s;

@@ -118,6 +118,7 @@ struct Clock {
   int32_t frzc;   // steps seen by the freeze-out status machine (0, 1, 2 = third and later)
   int32_t nstep;  // steps seen by the freeze-out stage (the step of a hypersurface row)
   double taup, taupp;   // times of the last two freeze-out snapshots (FreezeOut::taup, taupp)
+  double it, it2;       // 1/t and 1/t^2 of the current t: one FP64 division a substep, not one a particle
 };
 
 // Freeze-out snapshot fields (FreezeOut::freeze_array, include/freeze_out.h):

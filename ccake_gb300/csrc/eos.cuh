@@ -12,9 +12,11 @@ namespace ccake {
 struct Scales {
   double c, T0, muB0, muQ0, muS0;
   double iT0, iB0, iQ0, iS0;
+  double ic4;   // 1 / (4 c T0^4), of the analytic inverses
 };
 __host__ __device__ inline Scales make_scales(double c, double T0, double muB0, double muQ0, double muS0) {
-  return Scales{c, T0, muB0, muQ0, muS0, 1.0 / T0, 1.0 / muB0, 1.0 / muQ0, 1.0 / muS0};
+  return Scales{c, T0, muB0, muQ0, muS0, 1.0 / T0, 1.0 / muB0, 1.0 / muQ0, 1.0 / muS0,
+                1.0 / (4.0 * c * T0 * T0 * T0 * T0)};
 }
 
 // Tabulated EoS in device memory: uniform (T, muB, muQ, muS) grid, muS
@@ -586,28 +588,32 @@ __host__ __device__ inline void confdiag_seed(const Scales& k, int entropy, cons
 //   conformal: p = c T0^4 x^2 with x = sum_k (X_k/X0_k)^2, so
 //     d_k = 4 c T0^4 x X_k / X0_k^2; with a_k = X_k/X0_k and
 //     d'_k = d_k X0_k / (4 c T0^4) = a_k x, x^3 = sum_k d'_k^2 and a_k = d'_k / x.
-// Real cube root: FP32 cbrtf seed, then one Halley step in FP64,
-// y <- y (y^3 + 2x) / (2 y^3 + x), which triples the seed's ~2^-23 relative
-// accuracy to beyond FP64 precision (Halley's method on y^3 - x = 0). Inputs
+// Real cube root without an FP64 division: the FP32 estimate r0 of x^(-1/3)
+// (rcbrtf of the rounded input, relative error d ~ 2^-23) refined by the
+// third-order step of the binomial series r = r0 (1 - e)^(-1/3) =
+// r0 (1 + e/3 + 2 e^2/9 + ...), e = 1 - x r0^3 (Householder's method of
+// order 2 for x^(-1/3)); the truncation error, about 14 |e|^3 / 81 ~ 5 d^3,
+// is far below FP64 precision, and cbrt(x) = x r^2 to a few ulp. Inputs
 // outside the FP32 normal range go to cbrt.
-__host__ __device__ inline double cbrt_halley(double x) {
+__host__ __device__ inline double cbrt_refined(double x) {
   const double ax = fabs(x);
   if (ax == 0.0) return x;   // a zero density (no strangeness, say) is its own cube root
   if (!(ax > 1e-30 && ax < 1e30)) return cbrt(x);
-  const double y = f64_of(cbrtf(f32_rn(x)));
-  const double y3 = y * y * y;
-  return y * (y3 + 2.0 * x) / (2.0 * y3 + x);
+  const double r0 = f64_of(rcbrtf(f32_rn(x)));
+  const double e = fma(-(x * r0), r0 * r0, 1.0);
+  const double r = fma(r0, e * fma(2.0 / 9.0, e, 1.0 / 3.0), r0);
+  return x * (r * r);
 }
 
 __host__ __device__ inline bool analytic_seed(const EosDev& e, int model, const double* tgt, double* y) {
   if (model == M_TABLE || model == M_TANH) return false;
   const Scales k = model_scales(e, model);
   const double X0[4] = {k.T0, k.muB0, k.muQ0, k.muS0};
-  const double ic4 = 1.0 / (4.0 * k.c * k.T0 * k.T0 * k.T0 * k.T0);
+  const double ic4 = k.ic4;
   if (model == M_CDIAG) {
     for (int i = 0; i < 4; i++) {
       const double q = X0[i] * X0[i];
-      y[i] = cbrt_halley(tgt[i] * q * q * ic4);
+      y[i] = cbrt_refined(tgt[i] * q * q * ic4);
     }
     return y[0] > 0.0;
   }
@@ -616,7 +622,7 @@ __host__ __device__ inline bool analytic_seed(const EosDev& e, int model, const 
     d[i] = tgt[i] * X0[i] * ic4;
     x3 += d[i] * d[i];
   }
-  const double xx = cbrt_halley(x3);
+  const double xx = cbrt_refined(x3);
   if (!(xx > 0.0)) return false;
   const double ix = 1.0 / xx;
   for (int i = 0; i < 4; i++) y[i] = d[i] * ix * X0[i];

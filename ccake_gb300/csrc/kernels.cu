@@ -970,6 +970,8 @@ __global__ void k_diag(RunConst rc, Ptrs p, int grads_f32) {
   auto G = [&](int slot) { return grads_f32 ? double(gf[(size_t)slot * n + i]) : p.grads[(size_t)slot * n + i]; };
   EomIn<D, double> in;
   in.th = th;
+  in.it = 1.0 / t;
+  in.it2 = 1.0 / (t * t);
   in.g = p.gam[i];
 #pragma unroll
   for (int q = 0; q < 3; q++) {

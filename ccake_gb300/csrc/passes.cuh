@@ -239,7 +239,7 @@ __device__ __forceinline__ void thermo_store(const RunConst& rc, const Ptrs& p, 
 #pragma unroll
   for (int q = 0; q < 5; q++) es[q] = p.y[(Y_SHV0 + q) * n + i];
   double pi[NPI];
-  reset_pi<D>(es, sig, g, u3, t2, pi);
+  reset_pi<D>(es, sig, g, u3, t2, rc.cfg.coord == 1 ? 1.0 : p.clock->it2, pi);
   const double Pi = p.y[Y_EBULK * n + i] * sig;
   p.bulk[i] = Pi;
 #pragma unroll
@@ -379,6 +379,8 @@ __device__ __forceinline__ void finish_particle(const RunConst& rc, const Ptrs& 
   for (int q = 0; q < NTH; q++) th[q] = p.th[q * n + i];
   EomIn<D, R> in;
   in.th = th;
+  in.it = p.clock->it;
+  in.it2 = p.clock->it2;
 #pragma unroll
   for (int q = 0; q < 3; q++) {
     in.u[q] = (q < D) ? narrow<R>(p.y[(Y_U0 + q) * n + i]) : R(0);
@@ -487,6 +489,8 @@ __device__ __forceinline__ void finish_particle(const RunConst& rc, const Ptrs& 
 __device__ __forceinline__ void advance_clock(Clock* c, int substep, double dt) {
   if (substep == 1) c->t = c->teval = c->t0 + 0.5 * dt;
   else { c->t = c->t0 + dt; c->t0 = c->t; }
+  c->it = 1.0 / c->t;
+  c->it2 = 1.0 / (c->t * c->t);
 }
 
 // The freeze-out status machine of one particle after a step

@@ -161,12 +161,12 @@ __device__ __forceinline__ double gamma_milne(const double* u, double t2) {
 // values; a product with a constant zero would still cost FP64 instructions).
 template <int D>
 __device__ inline void reset_pi(const double* ext_shv, double sigma, double g, const double* u3, double t2,
-                                double* pi) {
+                                double it2, double* pi) {
   const double f0 = -u3[0], f1 = -u3[1], f2 = -t2 * u3[2];   // covariant u_i
   const double p11 = ext_shv[0] * sigma, p12 = ext_shv[1] * sigma, p13 = ext_shv[2] * sigma;
   const double p22 = ext_shv[3] * sigma, p23 = ext_shv[4] * sigma;
-  // one division each for 1/t^2 and 1/g (FP64 division is a long sequence)
-  const double it2 = 1.0 / t2, ig = 1.0 / g;
+  // one division for 1/g (FP64 division is a long sequence); it2 = 1/t^2
+  const double ig = 1.0 / g;
   double p00;
   if (D == 3)
     p00 = (f0 * f0 * p11 + f1 * f1 * p22 + 2. * f1 * f0 * p12 + 2. * f2 * f0 * p13 + 2. * f2 * f1 * p23 -
@@ -191,6 +191,7 @@ template <int D, typename R = double>
 struct EomIn {
   R u[3], v[3];
   R g, sigma, sigma_lab, m;
+  double it, it2;            // 1/t and 1/t^2 at the evaluation time (FP64)
   const double* th;          // NTH thermo values (FP64, from the EoS)
   R Pi;                      // bulk pressure
   R pi[NPI];                 // pi^{mu nu}
@@ -226,7 +227,11 @@ __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, cons
   const R g = in.g, sig = in.sigma;
   // reciprocals: FP64 division is a long instruction sequence on the scarce
   // FP64 pipe, so each divisor is inverted once
-  const R ig = R(1.0) / g, it = R(1.0) / t, it2 = R(1.0) / t2;
+  // the FP64 form takes 1/t and 1/t^2 from the clock (the same values; one
+  // division a substep instead of two a particle)
+  constexpr bool f64 = sizeof(R) == sizeof(double);
+  const R ig = R(1.0) / g, it = f64 ? R(in.it) : R(1.0) / t;
+  const R it2 = cart ? R(1.0) : (f64 ? R(in.it2) : R(1.0) / t2);
   const R itc = cart ? R(0.0) : it, itm = cart ? R(1.0) : it;
   const R k13 = R(1.0) / R(3.0), k16 = R(1.0) / R(6.0);
   const double* th = in.th;

@@ -194,8 +194,9 @@ def test_eos_batch_inversion_parity(eos_kind, entropy, thermo_mode):
 
 @pytest.mark.parametrize("eos_kind,thermo_mode", [(0, 0), (1, 1)])
 def test_eos_batch_analytic_seed(eos_kind, thermo_mode):
-    # exact inverses of the conformal models (cube roots by an FP32 seed and
-    # one FP64 Halley step): accepted without Newton steps. They recover the
+    # exact inverses of the conformal models (cube roots from an FP32
+    # reciprocal-cube-root estimate and one third-order FP64 refinement):
+    # accepted without Newton steps. They recover the
     # states the targets were made from; the oracle's Newton (reference
     # stopping rule, absolute residual 1e-10) can stop short on a potential
     # whose density is below that residual, so the roots are compared with
