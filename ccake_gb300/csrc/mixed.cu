@@ -417,66 +417,45 @@ __device__ __forceinline__ int group_event(const GroupArgs& g, int& first) {
   return g.state[e].active ? e : -1;
 }
 
-// The event of a block of the step kernels. ONE (a group of one event: the
-// standalone path, and a group the server runs alone) fixes it at event 0 at
-// compile time, so the descriptor's fields sit at fixed offsets of the
-// parameter space and are read as a single-event kernel reads its arguments;
-// with a runtime index every field is a load. The arithmetic is the same
-// code either way.
-template <bool ONE>
-__device__ __forceinline__ int block_event(const GroupArgs& g, int& first) {
-  if constexpr (ONE) {
-    first = (int)blockIdx.x * kBlock;
-    return g.state[0].active ? 0 : -1;
-  } else {
-    return group_event(g, first);
-  }
-}
-
-template <int D, bool ONE>
+template <int D>
 __global__ void __launch_bounds__(kBlock) k_passA_mixed(const __grid_constant__ GroupArgs g) {
   int first;
-  const int e = block_event<ONE>(g, first);
+  const int e = group_event(g, first);
   if (e < 0) return;
-  const EventDesc& ev = g.ev[ONE ? 0 : e];
-  passA_mixed_body<D>(ev.rc, ev.p, first + threadIdx.x);
+  passA_mixed_body<D>(g.ev[e].rc, g.ev[e].p, first + threadIdx.x);
 }
 
-template <int D, bool ONE>
+template <int D>
 __global__ void __launch_bounds__(kBlock) k_thermo_fast(const __grid_constant__ GroupArgs g) {
   int first;
-  const int e = block_event<ONE>(g, first);
+  const int e = group_event(g, first);
   if (e < 0) return;
-  const EventDesc& ev = g.ev[ONE ? 0 : e];
-  thermo_fast_body<D>(ev.rc, ev.eos, ev.p, first + threadIdx.x);
+  thermo_fast_body<D>(g.ev[e].rc, g.ev[e].eos, g.ev[e].p, first + threadIdx.x);
 }
 
-template <int D, bool ONE>
+template <int D>
 __global__ void __launch_bounds__(kBlock) k_thermo_mixed(const __grid_constant__ GroupArgs g, int pending_only) {
   int first;
-  const int e = block_event<ONE>(g, first);
+  const int e = group_event(g, first);
   if (e < 0) return;
-  const EventDesc& ev = g.ev[ONE ? 0 : e];
-  thermo_mixed_body<D>(ev.rc, ev.eos, ev.p, first + threadIdx.x, pending_only != 0);
+  thermo_mixed_body<D>(g.ev[e].rc, g.ev[e].eos, g.ev[e].p, first + threadIdx.x, pending_only != 0);
 }
 
-template <int D, bool ONE>
+template <int D>
 __global__ void __launch_bounds__(kBlock) k_passB_mixed(const __grid_constant__ GroupArgs g) {
   int first;
-  const int e = block_event<ONE>(g, first);
+  const int e = group_event(g, first);
   if (e < 0) return;
-  const EventDesc& ev = g.ev[ONE ? 0 : e];
-  passB_mixed_body<D>(ev.rc, ev.p, first + threadIdx.x);
+  passB_mixed_body<D>(g.ev[e].rc, g.ev[e].p, first + threadIdx.x);
 }
 
-template <int D, bool ONE>
+template <int D>
 __global__ void __launch_bounds__(kBlock) k_eom_mixed(const __grid_constant__ GroupArgs g, int mode, int sub) {
   int first;
-  const int e = block_event<ONE>(g, first);
+  const int e = group_event(g, first);
   if (e < 0) return;
-  const EventDesc& ev = g.ev[ONE ? 0 : e];
-  const double dt = ev.rc.cfg.dt;
-  eom_mixed_body<D>(ev.rc, ev.p, first + threadIdx.x, mode, sub == 1 ? 0.5 * dt : dt);
+  const double dt = g.ev[e].rc.cfg.dt;
+  eom_mixed_body<D>(g.ev[e].rc, g.ev[e].p, first + threadIdx.x, mode, sub == 1 ? 0.5 * dt : dt);
 }
 
 __global__ void k_clock_group(const __grid_constant__ GroupArgs g, int sub) {
@@ -554,44 +533,35 @@ static bool group_has_analytic(const GroupArgs& g) {
   return false;
 }
 
-template <int D, bool ONE>
-void launch_passA_mixed_t(const GroupArgs& g, cudaStream_t s) {
+void launch_passA_mixed(const GroupArgs& g, int dim, cudaStream_t s) {
   const int nb = g.first_block[g.nev];
   const int fast = group_has_analytic(g) ? 1 : 0;
-  k_passA_mixed<D, ONE><<<nb, kBlock, 0, s>>>(g);
-  if (fast) k_thermo_fast<D, ONE><<<nb, kBlock, 0, s>>>(g);
-  k_thermo_mixed<D, ONE><<<nb, kBlock, 0, s>>>(g, fast);
-}
-
-template <int D, bool ONE>
-void launch_passB_mixed_t(const GroupArgs& g, int mode, int sub, cudaStream_t s) {
-  const int nb = g.first_block[g.nev];
-  k_passB_mixed<D, ONE><<<nb, kBlock, 0, s>>>(g);
-  k_eom_mixed<D, ONE><<<nb, kBlock, 0, s>>>(g, mode, sub);
-}
-
-void launch_passA_mixed(const GroupArgs& g, int dim, cudaStream_t s) {
-  const bool one = g.nev == 1;
-  if (dim == 3) one ? launch_passA_mixed_t<3, true>(g, s) : launch_passA_mixed_t<3, false>(g, s);
-  else one ? launch_passA_mixed_t<2, true>(g, s) : launch_passA_mixed_t<2, false>(g, s);
+  if (dim == 3) {
+    k_passA_mixed<3><<<nb, kBlock, 0, s>>>(g);
+    if (fast) k_thermo_fast<3><<<nb, kBlock, 0, s>>>(g);
+    k_thermo_mixed<3><<<nb, kBlock, 0, s>>>(g, fast);
+  } else {
+    k_passA_mixed<2><<<nb, kBlock, 0, s>>>(g);
+    if (fast) k_thermo_fast<2><<<nb, kBlock, 0, s>>>(g);
+    k_thermo_mixed<2><<<nb, kBlock, 0, s>>>(g, fast);
+  }
 }
 
 void launch_passB_mixed(const GroupArgs& g, int dim, int mode, int sub, cudaStream_t s) {
-  const bool one = g.nev == 1;
-  if (dim == 3) one ? launch_passB_mixed_t<3, true>(g, mode, sub, s) : launch_passB_mixed_t<3, false>(g, mode, sub, s);
-  else one ? launch_passB_mixed_t<2, true>(g, mode, sub, s) : launch_passB_mixed_t<2, false>(g, mode, sub, s);
+  const int nb = g.first_block[g.nev];
+  if (dim == 3) {
+    k_passB_mixed<3><<<nb, kBlock, 0, s>>>(g);
+    k_eom_mixed<3><<<nb, kBlock, 0, s>>>(g, mode, sub);
+  } else {
+    k_passB_mixed<2><<<nb, kBlock, 0, s>>>(g);
+    k_eom_mixed<2><<<nb, kBlock, 0, s>>>(g, mode, sub);
+  }
 }
 
 void launch_gradients_mixed(const GroupArgs& g, int dim, cudaStream_t s) {
   const int nb = g.first_block[g.nev];
-  const bool one = g.nev == 1;
-  if (dim == 3) {
-    if (one) k_passB_mixed<3, true><<<nb, kBlock, 0, s>>>(g);
-    else k_passB_mixed<3, false><<<nb, kBlock, 0, s>>>(g);
-  } else {
-    if (one) k_passB_mixed<2, true><<<nb, kBlock, 0, s>>>(g);
-    else k_passB_mixed<2, false><<<nb, kBlock, 0, s>>>(g);
-  }
+  if (dim == 3) k_passB_mixed<3><<<nb, kBlock, 0, s>>>(g);
+  else k_passB_mixed<2><<<nb, kBlock, 0, s>>>(g);
 }
 
 void launch_clock_group(const GroupArgs& g, int sub, cudaStream_t s) {
