@@ -441,8 +441,11 @@ __global__ void __launch_bounds__(kBlock) k_thermo_mixed(const __grid_constant__
   thermo_mixed_body<D>(g.ev[e].rc, g.ev[e].eos, g.ev[e].p, first + threadIdx.x, pending_only != 0);
 }
 
+// In 3-D the gather loop holds ~140 registers a thread, 3 blocks an SM; at
+// 128 it keeps 4 blocks (16 warps) in flight, which the L1-bound gathers
+// use (the same code with the event index fixed at compile time fits in 127).
 template <int D>
-__global__ void __launch_bounds__(kBlock) k_passB_mixed(const __grid_constant__ GroupArgs g) {
+__global__ void __launch_bounds__(kBlock, D == 3 ? 4 : 1) k_passB_mixed(const __grid_constant__ GroupArgs g) {
   int first;
   const int e = group_event(g, first);
   if (e < 0) return;
