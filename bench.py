@@ -164,7 +164,7 @@ def read_traffic(kernel):
 def read_mixed_traffic():
     """DRAM bytes per launch of the mixed-form kernels from the committed ncu summary."""
     out = {}
-    for k in ("passA_mixed", "thermo_mixed", "passB_mixed", "eom_mixed"):
+    for k in ("passA_mixed", "thermo_fast", "thermo_mixed", "passB_mixed", "eom_mixed"):
         v = read_traffic(k)
         if v is not None:
             out[k] = v

@@ -441,11 +441,20 @@ __global__ void __launch_bounds__(kBlock) k_thermo_mixed(const __grid_constant__
   thermo_mixed_body<D>(g.ev[e].rc, g.ev[e].eos, g.ev[e].p, first + threadIdx.x, pending_only != 0);
 }
 
-// In 3-D the gather loop holds ~140 registers a thread, 3 blocks an SM; at
-// 128 it keeps 4 blocks (16 warps) in flight, which the L1-bound gathers
-// use (the same code with the event index fixed at compile time fits in 127).
 template <int D>
-__global__ void __launch_bounds__(kBlock, D == 3 ? 4 : 1) k_passB_mixed(const __grid_constant__ GroupArgs g) {
+__global__ void __launch_bounds__(kBlock) k_passB_mixed(const __grid_constant__ GroupArgs g) {
+  int first;
+  const int e = group_event(g, first);
+  if (e < 0) return;
+  passB_mixed_body<D>(g.ev[e].rc, g.ev[e].p, first + threadIdx.x);
+}
+
+// The 3-D launch: its gather loop holds ~140 registers a thread, 3 blocks an
+// SM; held to 128 it keeps 4 blocks (16 warps) in flight for the L1-bound
+// gathers (3-D pass B 7.6 -> 6.5 ms at 1.44M particles). The 2-D loop runs
+// slower under the same bound, so it keeps the plain one.
+template <int D>
+__global__ void __launch_bounds__(kBlock, 4) k_passB_mixed_r128(const __grid_constant__ GroupArgs g) {
   int first;
   const int e = group_event(g, first);
   if (e < 0) return;
@@ -553,7 +562,7 @@ void launch_passA_mixed(const GroupArgs& g, int dim, cudaStream_t s) {
 void launch_passB_mixed(const GroupArgs& g, int dim, int mode, int sub, cudaStream_t s) {
   const int nb = g.first_block[g.nev];
   if (dim == 3) {
-    k_passB_mixed<3><<<nb, kBlock, 0, s>>>(g);
+    k_passB_mixed_r128<3><<<nb, kBlock, 0, s>>>(g);
     k_eom_mixed<3><<<nb, kBlock, 0, s>>>(g, mode, sub);
   } else {
     k_passB_mixed<2><<<nb, kBlock, 0, s>>>(g);
@@ -563,7 +572,7 @@ void launch_passB_mixed(const GroupArgs& g, int dim, int mode, int sub, cudaStre
 
 void launch_gradients_mixed(const GroupArgs& g, int dim, cudaStream_t s) {
   const int nb = g.first_block[g.nev];
-  if (dim == 3) k_passB_mixed<3><<<nb, kBlock, 0, s>>>(g);
+  if (dim == 3) k_passB_mixed_r128<3><<<nb, kBlock, 0, s>>>(g);
   else k_passB_mixed<2><<<nb, kBlock, 0, s>>>(g);
 }
 

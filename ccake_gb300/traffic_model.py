@@ -49,12 +49,22 @@ FIELDS = {
     },
 }
 
-# FP64 operations per particle per RK2 step (2 substeps), FP64 form:
-# pairs x (W + smoothing sums ~25, gradient sums incl. shear ~60) + EoM + EoS
+# FP64 operations (an FMA counts 2) of the FP64 form per particle and launch.
+# C2 (the bench event) from the kernels' FP64 instructions, counted in the
+# source and checked against ncu (2 DFMA + DMUL + DADD per launch over the
+# 160k particles: pass A smoothing 1797, EoS 490, pass B 3886):
+#   pair_A  38 = displacement 2 + exact |d|^2 3 + kernel values 23 (1/r by
+#                the refined FP32 estimate, W and grad-W branches) + 5 sums 10
+#   pair_B  43 = m fg 1 + displacement 2 + m grad W 2 + 9 separable sums with
+#                shear (S1, SP, SE, SB, SV, S0, SD) 38
+#   particle_A  gamma, v and the LRF densities; eos the inversion and the
+#   records; eom the transport, MRF equations of motion and RK2 update.
+# C1 and C4 are estimates of the same kind (no shear and charges in C1; 3-D,
+# table EoS and bulk in C4).
 FLOPS = {
-    "C1": {"neighbours": 48, "per_pair": 50, "eom": 800, "eos": 200},
-    "C2": {"neighbours": 48, "per_pair": 85, "eom": 1500, "eos": 400},
-    "C4": {"neighbours": 447, "per_pair": 120, "eom": 2500, "eos": 1200},
+    "C1": {"neighbours": 48, "pair_A": 38, "pair_B": 27, "particle_A": 60, "eos": 250, "eom": 700},
+    "C2": {"neighbours": 46, "pair_A": 38, "pair_B": 43, "particle_A": 60, "eos": 490, "eom": 1910},
+    "C4": {"neighbours": 447, "pair_A": 40, "pair_B": 60, "particle_A": 80, "eos": 1200, "eom": 2500},
 }
 
 # 3-D: +1 position, +1 velocity, +2 shear components per state copy
@@ -81,18 +91,17 @@ def bytes_per_particle_step(config: str) -> int:
 
 def flops_per_particle_step(config: str) -> int:
     c = FLOPS[config]
-    return 2 * (c["neighbours"] * c["per_pair"] + c["eom"] + c["eos"])
+    return 2 * (c["neighbours"] * (c["pair_A"] + c["pair_B"]) + c["particle_A"] + c["eos"] + c["eom"])
 
 
 def flops_per_launch(config: str, kernel: str, n: int) -> float:
-    """FP64 operations of one pass launch: pass A carries the smoothing part
-    of the pair work (~30 %) and the EoS, pass B the gradient part and the EoM."""
+    """FP64 operations of one pass launch over n particles: pass A (the
+    smoothing kernel and the EoS kernel) and pass B (gradients, EoM, RK2)."""
     c = FLOPS[config]
-    pair = c["neighbours"] * c["per_pair"]
     if kernel == "passA":
-        return n * (0.3 * pair + c["eos"])
+        return n * (c["neighbours"] * c["pair_A"] + c["particle_A"] + c["eos"])
     if kernel == "passB":
-        return n * (0.7 * pair + c["eom"])
+        return n * (c["neighbours"] * c["pair_B"] + c["eom"])
     return 0.0
 
 
