@@ -846,7 +846,8 @@ def run_form_only(args, form):
         g.step(1)
     torch.cuda.synchronize()
     ms = g.step_timed(args.steps)
-    line = {"partial": True, "form": form, "diffusion": bool(args.diffusion), "metric": METRIC, "unit": UNIT,
+    metric = METRIC if form == "fp64" else METRIC.replace("plain FP64", "mixed precision")
+    line = {"partial": True, "form": form, "diffusion": bool(args.diffusion), "metric": metric, "unit": UNIT,
             "steps": args.steps, "ms_per_step": ms / args.steps, "value": p.n * args.steps / (ms * 1e-3)}
     if args.diffusion and not args.no_cpu:
         steps = max(1, args.ref_steps)
