@@ -116,20 +116,22 @@ __device__ inline void diffusion_coefs(const ccake_config& c, const double* th, 
   for (int i = 0; i < 3; i++) tq[4 * i] += 0.2 / T;
 }
 
-// 3x3 inverse by cofactors over the determinant (include/milne.hpp:788-834).
+// 3x3 inverse by cofactors over the determinant (include/milne.hpp:788-834),
+// the cofactors times one reciprocal of the determinant.
 __device__ inline void inverse3(const double* A, double* Ai) {
 #define M3(i, j) A[(i) * 3 + (j)]
   const double det = M3(0, 0) * M3(1, 1) * M3(2, 2) + M3(0, 1) * M3(1, 2) * M3(2, 0) + M3(0, 2) * M3(1, 0) * M3(2, 1) -
                      M3(0, 2) * M3(1, 1) * M3(2, 0) - M3(0, 1) * M3(1, 0) * M3(2, 2) - M3(0, 0) * M3(1, 2) * M3(2, 1);
-  Ai[0] = (M3(1, 1) * M3(2, 2) - M3(1, 2) * M3(2, 1)) / det;
-  Ai[1] = (M3(0, 2) * M3(2, 1) - M3(0, 1) * M3(2, 2)) / det;
-  Ai[2] = (M3(0, 1) * M3(1, 2) - M3(0, 2) * M3(1, 1)) / det;
-  Ai[3] = (M3(1, 2) * M3(2, 0) - M3(1, 0) * M3(2, 2)) / det;
-  Ai[4] = (M3(0, 0) * M3(2, 2) - M3(0, 2) * M3(2, 0)) / det;
-  Ai[5] = (M3(0, 2) * M3(1, 0) - M3(0, 0) * M3(1, 2)) / det;
-  Ai[6] = (M3(1, 0) * M3(2, 1) - M3(1, 1) * M3(2, 0)) / det;
-  Ai[7] = (M3(0, 1) * M3(2, 0) - M3(0, 0) * M3(2, 1)) / det;
-  Ai[8] = (M3(0, 0) * M3(1, 1) - M3(0, 1) * M3(1, 0)) / det;
+  const double id = 1.0 / det;
+  Ai[0] = (M3(1, 1) * M3(2, 2) - M3(1, 2) * M3(2, 1)) * id;
+  Ai[1] = (M3(0, 2) * M3(2, 1) - M3(0, 1) * M3(2, 2)) * id;
+  Ai[2] = (M3(0, 1) * M3(1, 2) - M3(0, 2) * M3(1, 1)) * id;
+  Ai[3] = (M3(1, 2) * M3(2, 0) - M3(1, 0) * M3(2, 2)) * id;
+  Ai[4] = (M3(0, 0) * M3(2, 2) - M3(0, 2) * M3(2, 0)) * id;
+  Ai[5] = (M3(0, 2) * M3(1, 0) - M3(0, 0) * M3(1, 2)) * id;
+  Ai[6] = (M3(1, 0) * M3(2, 1) - M3(1, 1) * M3(2, 0)) * id;
+  Ai[7] = (M3(0, 1) * M3(2, 0) - M3(0, 0) * M3(2, 1)) * id;
+  Ai[8] = (M3(0, 0) * M3(1, 1) - M3(0, 1) * M3(1, 0)) * id;
 #undef M3
 }
 
@@ -567,9 +569,12 @@ __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, cons
   if constexpr (std::is_same<R, double>::value) {
     if (dif) {
       const double sig_ = sig, g_ = g;
+      // reciprocals once (an FP64 division is a long sequence on the FP64
+      // pipe): 1/gamma, 1/t and 1/T
+      const double ig_ = ig, it_ = it, iT = 1.0 / T;
       const double mu[3] = {th[T_MUB], th[T_MUS], th[T_MUQ]};
       double RS[3], MS[3] = {0, 0, 0};
-      for (int c = 0; c < 3; c++) RS[c] = -mu[c] / T;
+      for (int c = 0; c < 3; c++) RS[c] = -mu[c] * iT;
       for (int i = 0; i < D; i++) MS[i] = Ms[i];
       double itq[9], itt[9], itk[9];
       inverse3(dif->tq, itq);
@@ -585,7 +590,7 @@ __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, cons
         }
       // Cartesian twin (src/eom_cartesian.cpp:1327-1722): no F_D terms, the
       // expansion rate gamma div v alone, metric without tau
-      const double X_ = cart ? g_ * divV : g_ * divV + geo + g_ / t;
+      const double X_ = cart ? g_ * divV : g_ * divV + geo + g_ * it_;
       const double omg = 1. - g_ * g_;
       double qc[3][4];
       for (int c = 0; c < 3; c++) {
@@ -598,18 +603,18 @@ __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, cons
       for (int c = 0; c < 3; c++) {
         const double q0 = dif->q[4 * c];
         F0D[c] = cart ? 0.0
-                      : g_ * g_ * geo * q0 + 2. * g_ * g_ * qc[c][3] * u[2] / t + t * g_ * qc[c][0] * u[2] * u[2] +
+                      : g_ * g_ * geo * q0 + 2. * g_ * g_ * qc[c][3] * u[2] * it_ + t * g_ * qc[c][0] * u[2] * u[2] +
                             t * u[2] * dif->q[4 * c + 3];
         F0a[c] = omg * sig_ * dif->da[c] * Fs;
-        A0a[c] = -omg * dif->da[c] * double(sden) / g_;
+        A0a[c] = -omg * dif->da[c] * double(sden) * ig_;
         for (int i = 0; i < D; i++) {
-          M0D[c][i] = g_ * g_ * (qc[c][i + 1] - qc[c][0] * uc[i] / g_);
+          M0D[c][i] = g_ * g_ * (qc[c][i + 1] - qc[c][0] * uc[i] * ig_);
           M0a[c][i] = omg * sig_ * dif->da[c] * MS[i];
-          F0a[c] += -dif->ga[3 * i + c] * u[i] / g_;
+          F0a[c] += -dif->ga[3 * i + c] * u[i] * ig_;
         }
         for (int d = 0; d < 3; d++) {
           R0a[c][d] = omg * sig_ * (dif->da[c] * RS[d] + dif->da[3 + 3 * c + d]);
-          A0a[c] += -omg * dif->da[3 + 3 * c + d] * rho[d] / g_;
+          A0a[c] += -omg * dif->da[3 + 3 * c + d] * rho[d] * ig_;
         }
       }
       // charge MRFs: R_N = gamma sigma 1 - R_0q, M_N = -M_0q, F_N = -F_0q +
@@ -621,25 +626,25 @@ __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, cons
         double F0q = 0.0;
         for (int d = 0; d < 3; d++)
           F0q += (-itt[3 * c + d] * F0D[d] - itq[3 * c + d] * dif->q[4 * d] + itk[3 * c + d] * F0a[d] +
-                  itk[3 * c + d] * A0a[d] * X_) / (g_) -
-                 itt[3 * c + d] * dif->q[4 * d] * X_ / g_;
+                  itk[3 * c + d] * A0a[d] * X_) * ig_ -
+                 itt[3 * c + d] * dif->q[4 * d] * X_ * ig_;
         for (int i = 0; i < 3; i++) MN[i][c] = 0.0;
         for (int i = 0; i < D; i++) {
           double acc = 0.0;
           for (int d = 0; d < 3; d++)
-            acc += (-itt[3 * c + d] * M0D[d][i] + itk[3 * c + d] * M0a[d][i] - itk[3 * c + d] * A0a[d] * uc[i] / g_) /
-                       (g_) +
-                   itt[3 * c + d] * dif->q[4 * d] * uc[i] / g_ / g_;
+            acc += (-itt[3 * c + d] * M0D[d][i] + itk[3 * c + d] * M0a[d][i] - itk[3 * c + d] * A0a[d] * uc[i] * ig_) *
+                       ig_ +
+                   itt[3 * c + d] * dif->q[4 * d] * uc[i] * ig_ * ig_;
           MN[i][c] = 0.0 + -acc;
         }
         for (int d = 0; d < 3; d++) {
           double acc = 0.0;
-          for (int kk = 0; kk < 3; kk++) acc += itk[3 * c + kk] * R0a[kk][d] / (g_);
+          for (int kk = 0; kk < 3; kk++) acc += itk[3 * c + kk] * R0a[kk][d] * ig_;
           RN[3 * c + d] += -acc;
         }
         FN[c] = 0.0;
         if (cart) FN[c] += -F0q + dif->gq[c] - dif->dq[c];
-        else FN[c] += -F0q + dif->gq[c] - dif->dq[c] - dif->q[4 * c] / t;
+        else FN[c] += -F0q + dif->gq[c] - dif->dq[c] - dif->q[4 * c] * it_;
       }
       inverse3(RN, RI);
       // R_u = -u gamma (R_w + R_bulk sigma), R_w = sigma dw/drho + sigma dw/ds R_S
@@ -706,7 +711,8 @@ __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, cons
       }
       const double mu[3] = {th[T_MUB], th[T_MUS], th[T_MUQ]};
       double RS[3], MS[3] = {0, 0, 0};
-      for (int c = 0; c < 3; c++) RS[c] = -mu[c] / T;
+      const double iT = 1.0 / T;
+      for (int c = 0; c < 3; c++) RS[c] = -mu[c] * iT;
       for (int i = 0; i < D; i++) MS[i] = Ms[i];
       double rdn = 0.0;
       for (int c = 0; c < 3; c++) rdn += RS[c] * dN[c];
@@ -723,9 +729,9 @@ __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, cons
           itt[3 * c + d] = a1;
           itk[3 * c + d] = a2;
         }
-      const double X_ = cart ? g * divV : g * divV + geo + g / t;
-      const double gs = g * sig;
-      const double cmd[4] = {1., -1., -1., cart ? -1. : -1. / t / t};
+      const double X_ = cart ? g * divV : g * divV + geo + g * it;
+      const double gs = g * sig, igs = 1.0 / gs;
+      const double cmd[4] = {1., -1., -1., cart ? -1. : -it * it};
       const double fuc[3] = {-u[0], -u[1], -t2 * u[2]};
       double qc[3][4];
       for (int c = 0; c < 3; c++) {
@@ -740,11 +746,11 @@ __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, cons
                                i < D ? dif->ga[3 * i + 2] : 0.0};
         double FD[3], Fa[3], Aa[3], MD[3][3], Ma[3][3], Ra[3][3];
         for (int c = 0; c < 3; c++) {
-          FD[c] = cart ? 0.0 : fui * g * dif->q[4 * c] * geo + 2. * fui * qc[c][3] * u[2] * g / t;
+          FD[c] = cart ? 0.0 : fui * g * dif->q[4 * c] * geo + 2. * fui * qc[c][3] * u[2] * g * it;
           Fa[c] = -fui * g * sig * dif->da[c] * Fs + cmd[i + 1] * gai[c];
           Aa[c] = fui * dif->da[c] * double(sden);
           for (int j = 0; j < 3; j++) {
-            MD[c][j] = fui * g * (qc[c][j + 1] - qc[c][0] * fuc[j] / g);
+            MD[c][j] = fui * g * (qc[c][j + 1] - qc[c][0] * fuc[j] * ig);
             Ma[c][j] = -fui * g * sig * dif->da[c] * MS[j];
           }
           for (int d = 0; d < 3; d++) {
@@ -756,16 +762,16 @@ __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, cons
           double F = 0.0, Rq[3];
           for (int d = 0; d < 3; d++) {
             F += (-itt[3 * c + d] * FD[d] - itq[3 * c + d] * dif->q[4 * d + i + 1] + itk[3 * c + d] * Fa[d] +
-                  itk[3 * c + d] * Aa[d] * X_) / (gs);
+                  itk[3 * c + d] * Aa[d] * X_) * igs;
             double R_ = 0.0;
-            for (int kk = 0; kk < 3; kk++) R_ += itk[3 * c + kk] * Ra[kk][d] / (gs);
+            for (int kk = 0; kk < 3; kk++) R_ += itk[3 * c + kk] * Ra[kk][d] * igs;
             Rq[d] = R_;
           }
           double v = F;
           for (int j = 0; j < D; j++) {
             double M = 0.0;
             for (int d = 0; d < 3; d++)
-              M += (-itt[3 * c + d] * MD[d][j] + itk[3 * c + d] * Ma[d][j] - itk[3 * c + d] * Aa[d] * fuc[j] / g) / (gs);
+              M += (-itt[3 * c + d] * MD[d][j] + itk[3 * c + d] * Ma[d][j] - itk[3 * c + d] * Aa[d] * fuc[j] * ig) * igs;
             v += M * du[j];
           }
           for (int d = 0; d < 3; d++) v += Rq[d] * dN[d];
