@@ -636,9 +636,9 @@ ccake_status_t ccake_ctx_create(const ccake_config* cfg, ccake_ctx** out) {
     if (m != CCAKE_COEF_DEFAULT && m != CCAKE_COEF_DISABLED) return CCAKE_ERR_INVALID;
   for (int32_t m : {cfg->delta_pipi_mode, cfg->delta_PiPi_mode})
     if (m < CCAKE_COEF_DEFAULT || m > CCAKE_COEF_DISABLED) return CCAKE_ERR_INVALID;
-  // the diffusion sector runs in the FP64 form with the constant_over_T2 or
+  // the diffusion sector (both forms) with the constant_over_T2 or
   // kappaB_coth coefficients
-  if (cfg->using_diffusion && (cfg->precision != 0 || (cfg->diffusion_mode != 0 && cfg->diffusion_mode != 2)))
+  if (cfg->using_diffusion && cfg->diffusion_mode != 0 && cfg->diffusion_mode != 2)
     return CCAKE_ERR_INVALID;
   ccake_ctx* ctx = new ccake_ctx;
   ctx->cfg = *cfg;

@@ -193,12 +193,12 @@ __device__ __forceinline__ void passA_mixed_body(const RunConst& rc, const Ptrs&
 // EoS inversion and the mixed gradient record, as a kernel of its own: the
 // FP64 Newton solve needs ~255 registers a thread, which would cap the
 // occupancy of the gather loop above at 8 warps an SM.
-template <int D>
+template <int D, bool DIFF>
 __device__ __forceinline__ void thermo_mixed_body(const RunConst& rc, const EosDev& eos, const Ptrs& p, const int i,
                                                   bool pending_only) {
   if (i >= p.n) return;
   if (pending_only && p.eos_iters[i] != kEosPending) return;
-  thermo_tail<D, true>(rc, eos, p, i, p.clock->t);
+  thermo_tail<D, true, DIFF>(rc, eos, p, i, p.clock->t);
 }
 
 // The EoS pass of the mixed form for the analytic models (conformal and
@@ -226,6 +226,95 @@ __device__ __forceinline__ void thermo_fast_body(const RunConst& rc, const EosDe
   double th[NTH];
   set_thermo_o(eos, k, x, o, th, true);
   thermo_store<D, true, false>(rc, p, i, p.clock->t, th, k, 0);
+}
+
+// Diffusion sums of the mixed form, for particle i: the separable sums of
+// k_diffgrad (src/sph_workstation.cpp:909-967 of the reference: v.grad q^0,
+// div q and grad alpha of each charge) in FP32 with Kahan compensation over
+// the FP32 list, from the FP32 records: positions as (hi, lo) pairs and the
+// mass from record B, the diffusion record in the first half of its slot.
+// The particle's own values come from the same records as its neighbours'.
+// Written to the FP64 diffusion slabs the equations of motion read.
+template <int D>
+__device__ __forceinline__ void diffgrad_mixed_body(const Ptrs& p, const int i) {
+  if (i >= p.n) return;
+  const int n = p.n;
+  constexpr int SB = RBF / 4;
+  const float4* rbf = reinterpret_cast<const float4*>(p.recBf);
+  const float4 A0 = rbf[(size_t)i * SB], A1 = rbf[(size_t)i * SB + 1], A2 = rbf[(size_t)i * SB + 2];
+  const float va[3] = {A2.z, A2.w, D == 3 ? rbf[(size_t)i * SB + 3].x : 0.0f};
+  auto rec = [&](int b, float* f) {
+    const float4* rq = reinterpret_cast<const float4*>(p.recQ + (size_t)b * RQ);
+#pragma unroll
+    for (int k2 = 0; k2 < 4; k2++) {
+      const float4 v = __ldg(rq + k2);
+      f[4 * k2] = v.x; f[4 * k2 + 1] = v.y; f[4 * k2 + 2] = v.z; f[4 * k2 + 3] = v.w;
+    }
+  };
+  KSum S1[D], SQ0[3][D], SA[3][D], SQI[3];
+#pragma unroll
+  for (int k = 0; k < D; k++) {
+    S1[k].init(0.0f);
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      SQ0[c][k].init(0.0f);
+      SA[c][k].init(0.0f);
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 3; c++) SQI[c].init(0.0f);
+  const float* nf = reinterpret_cast<const float*>(p.nbr_f);
+  const int cnt = min(p.btrack[i], p.K);
+  for (int kk = 0; kk < cnt; kk++) {
+    const int b = p.nbr_idx[(size_t)kk * n + i];
+    const float fg = nf[(size_t)kk * n + i];
+    const float4 B0 = __ldg(rbf + (size_t)b * SB), B1 = __ldg(rbf + (size_t)b * SB + 1);
+    const float d[3] = {(A0.x - B0.x) + (A1.x - B1.x), (A0.y - B0.y) + (A1.y - B1.y),
+                        (D == 3) ? (A0.z - B0.z) + (A1.z - B1.z) : 0.0f};
+    const float mf = B0.w * fg;
+    float gm[D];
+#pragma unroll
+    for (int k = 0; k < D; k++) gm[k] = mf * d[k];
+    float f[16];
+    rec(b, f);
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      float acc = 0.0f;
+#pragma unroll
+      for (int k = 0; k < D; k++) {
+        SQ0[c][k].add(f[c] * gm[k]);
+        SA[c][k].add(f[3 + c] * gm[k]);
+        acc += f[6 + 3 * k + c] * gm[k];
+      }
+      SQI[c].add(acc);
+    }
+#pragma unroll
+    for (int k = 0; k < D; k++) S1[k].add(gm[k]);
+  }
+  float fa[16];
+  rec(i, fa);
+  const float sla = f32_rn(p.slab[i]), isla = 1.0f / sla;
+  float s1[D], vS1 = 0.0f;
+#pragma unroll
+  for (int k = 0; k < D; k++) {
+    s1[k] = S1[k].value();
+    vS1 += va[k] * s1[k];
+  }
+  double* df = p.dif;
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    float vq = 0.0f, qs = 0.0f;
+#pragma unroll
+    for (int k = 0; k < D; k++) {
+      vq += va[k] * SQ0[c][k].value();
+      qs += fa[6 + 3 * k + c] * s1[k];
+    }
+    df[(size_t)(F_GQ + c) * n + i] = f64_of(sla * (vq + fa[c] * vS1));
+    df[(size_t)(F_DQ + c) * n + i] = f64_of(sla * (SQI[c].value() + qs));
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+      df[(size_t)(F_GA + 3 * k + c) * n + i] = (k < D) ? f64_of((SA[c][k].value() - fa[3 + c] * s1[k]) * isla) : 0.0;
+  }
 }
 
 // Pass B, mixed form, part 1: separable gradient sums over the list pass A
@@ -381,7 +470,7 @@ __device__ __forceinline__ void passB_mixed_body(const RunConst& rc, const Ptrs&
 
 // Pass B, mixed form, part 2: FP32 equations of motion from the gradients of
 // part 1, FP64 RK2 update, mixed smoothing record for the next substep.
-template <int D>
+template <int D, bool DIFF>
 __device__ __forceinline__ void eom_mixed_body(const RunConst& rc, const Ptrs& p, const int i, const int mode,
                                                const double dt_sub) {
   if (i >= p.n) return;
@@ -401,7 +490,7 @@ __device__ __forceinline__ void eom_mixed_body(const RunConst& rc, const Ptrs& p
   }
 #pragma unroll
   for (int k = 0; k < D * D; k++) gV[k] = gf[(G_V + k) * n + i];
-  finish_particle<D, float, true>(rc, p, i, mode & ~B_GRADS, p.clock->t, dt_sub, va, gP, gE, gB, gS, dS, gV);
+  finish_particle<D, float, true, DIFF>(rc, p, i, mode & ~B_GRADS, p.clock->t, dt_sub, va, gP, gE, gB, gS, dS, gV);
 }
 
 // ---------------------------------------------------------------------------
@@ -433,12 +522,20 @@ __global__ void __launch_bounds__(kBlock) k_thermo_fast(const __grid_constant__ 
   thermo_fast_body<D>(g.ev[e].rc, g.ev[e].eos, g.ev[e].p, first + threadIdx.x);
 }
 
-template <int D>
+template <int D, bool DIFF>
 __global__ void __launch_bounds__(kBlock) k_thermo_mixed(const __grid_constant__ GroupArgs g, int pending_only) {
   int first;
   const int e = group_event(g, first);
   if (e < 0) return;
-  thermo_mixed_body<D>(g.ev[e].rc, g.ev[e].eos, g.ev[e].p, first + threadIdx.x, pending_only != 0);
+  thermo_mixed_body<D, DIFF>(g.ev[e].rc, g.ev[e].eos, g.ev[e].p, first + threadIdx.x, pending_only != 0);
+}
+
+template <int D>
+__global__ void __launch_bounds__(kBlock) k_diffgrad_mixed(const __grid_constant__ GroupArgs g) {
+  int first;
+  const int e = group_event(g, first);
+  if (e < 0) return;
+  diffgrad_mixed_body<D>(g.ev[e].p, first + threadIdx.x);
 }
 
 template <int D>
@@ -461,13 +558,13 @@ __global__ void __launch_bounds__(kBlock, 4) k_passB_mixed_r128(const __grid_con
   passB_mixed_body<D>(g.ev[e].rc, g.ev[e].p, first + threadIdx.x);
 }
 
-template <int D>
+template <int D, bool DIFF>
 __global__ void __launch_bounds__(kBlock) k_eom_mixed(const __grid_constant__ GroupArgs g, int mode, int sub) {
   int first;
   const int e = group_event(g, first);
   if (e < 0) return;
   const double dt = g.ev[e].rc.cfg.dt;
-  eom_mixed_body<D>(g.ev[e].rc, g.ev[e].p, first + threadIdx.x, mode, sub == 1 ? 0.5 * dt : dt);
+  eom_mixed_body<D, DIFF>(g.ev[e].rc, g.ev[e].p, first + threadIdx.x, mode, sub == 1 ? 0.5 * dt : dt);
 }
 
 __global__ void k_clock_group(const __grid_constant__ GroupArgs g, int sub) {
@@ -545,28 +642,48 @@ static bool group_has_analytic(const GroupArgs& g) {
   return false;
 }
 
+// A group with the diffusion sector (the server groups none; an event with
+// it runs alone): every member has it on.
+static bool group_has_diffusion(const GroupArgs& g) {
+  for (int e = 0; e < g.nev; e++)
+    if (g.ev[e].rc.cfg.using_diffusion && g.ev[e].p.dif) return true;
+  return false;
+}
+
 void launch_passA_mixed(const GroupArgs& g, int dim, cudaStream_t s) {
   const int nb = g.first_block[g.nev];
-  const int fast = group_has_analytic(g) ? 1 : 0;
+  const bool dif = group_has_diffusion(g);
+  // the analytic pass carries no diffusion record: with the sector on, the
+  // full inversion takes every particle
+  const int fast = (!dif && group_has_analytic(g)) ? 1 : 0;
   if (dim == 3) {
     k_passA_mixed<3><<<nb, kBlock, 0, s>>>(g);
     if (fast) k_thermo_fast<3><<<nb, kBlock, 0, s>>>(g);
-    k_thermo_mixed<3><<<nb, kBlock, 0, s>>>(g, fast);
+    if (dif) k_thermo_mixed<3, true><<<nb, kBlock, 0, s>>>(g, 0);
+    else k_thermo_mixed<3, false><<<nb, kBlock, 0, s>>>(g, fast);
   } else {
     k_passA_mixed<2><<<nb, kBlock, 0, s>>>(g);
     if (fast) k_thermo_fast<2><<<nb, kBlock, 0, s>>>(g);
-    k_thermo_mixed<2><<<nb, kBlock, 0, s>>>(g, fast);
+    if (dif) k_thermo_mixed<2, true><<<nb, kBlock, 0, s>>>(g, 0);
+    else k_thermo_mixed<2, false><<<nb, kBlock, 0, s>>>(g, fast);
   }
 }
 
+// With the diffusion sector its sums run first (they read the diffusion
+// records of the neighbours, complete after the EoS kernel).
 void launch_passB_mixed(const GroupArgs& g, int dim, int mode, int sub, cudaStream_t s) {
   const int nb = g.first_block[g.nev];
+  const bool dif = group_has_diffusion(g);
   if (dim == 3) {
+    if (dif) k_diffgrad_mixed<3><<<nb, kBlock, 0, s>>>(g);
     k_passB_mixed_r128<3><<<nb, kBlock, 0, s>>>(g);
-    k_eom_mixed<3><<<nb, kBlock, 0, s>>>(g, mode, sub);
+    if (dif) k_eom_mixed<3, true><<<nb, kBlock, 0, s>>>(g, mode, sub);
+    else k_eom_mixed<3, false><<<nb, kBlock, 0, s>>>(g, mode, sub);
   } else {
+    if (dif) k_diffgrad_mixed<2><<<nb, kBlock, 0, s>>>(g);
     k_passB_mixed<2><<<nb, kBlock, 0, s>>>(g);
-    k_eom_mixed<2><<<nb, kBlock, 0, s>>>(g, mode, sub);
+    if (dif) k_eom_mixed<2, true><<<nb, kBlock, 0, s>>>(g, mode, sub);
+    else k_eom_mixed<2, false><<<nb, kBlock, 0, s>>>(g, mode, sub);
   }
 }
 

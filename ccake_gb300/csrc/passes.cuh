@@ -279,19 +279,33 @@ __device__ __forceinline__ void thermo_store(const RunConst& rc, const Ptrs& p, 
         for (int m = 0; m < 4; m++) q[4 * c + m] = q[4 * c + m] * scale;
       }
     }
-    double* rq = p.recQ + (size_t)i * RQ;
+    // the diffusion record of the neighbour sums: q^0/sl^2 (3), alpha = mu/T
+    // (3), q^k/sl^2 (9); FP64, or FP32 in the first half of the same slot
+    // (mixed form)
+    double rv[16];
+    const double iT = 1.0 / th[T_T];
 #pragma unroll
     for (int c = 0; c < 3; c++) {
 #pragma unroll
       for (int m = 0; m < 4; m++) p.dif[(size_t)(F_Q + 4 * c + m) * n + i] = q[4 * c + m];
-      rq[c] = q[4 * c] * isl2;
+      rv[c] = q[4 * c] * isl2;
 #pragma unroll
-      for (int k2 = 0; k2 < 3; k2++) rq[6 + 3 * k2 + c] = q[4 * c + k2 + 1] * isl2;
+      for (int k2 = 0; k2 < 3; k2++) rv[6 + 3 * k2 + c] = q[4 * c + k2 + 1] * isl2;
     }
-    rq[3] = th[T_MUB] / th[T_T];
-    rq[4] = th[T_MUS] / th[T_T];
-    rq[5] = th[T_MUQ] / th[T_T];
-    rq[15] = 0.0;
+    rv[3] = th[T_MUB] * iT;
+    rv[4] = th[T_MUS] * iT;
+    rv[5] = th[T_MUQ] * iT;
+    rv[15] = 0.0;
+    if constexpr (MIX) {
+      float4* rq = reinterpret_cast<float4*>(p.recQ + (size_t)i * RQ);
+#pragma unroll
+      for (int k2 = 0; k2 < 4; k2++)
+        rq[k2] = make_float4(f32_rn(rv[4 * k2]), f32_rn(rv[4 * k2 + 1]), f32_rn(rv[4 * k2 + 2]), f32_rn(rv[4 * k2 + 3]));
+    } else {
+      double* rq = p.recQ + (size_t)i * RQ;
+#pragma unroll
+      for (int k2 = 0; k2 < 16; k2++) rq[k2] = rv[k2];
+    }
   }
   if constexpr (MIX) {
     float hi[3], lo[3];

@@ -118,11 +118,12 @@ __device__ inline void diffusion_coefs(const ccake_config& c, const double* th, 
 
 // 3x3 inverse by cofactors over the determinant (include/milne.hpp:788-834),
 // the cofactors times one reciprocal of the determinant.
-__device__ inline void inverse3(const double* A, double* Ai) {
+template <typename R>
+__device__ inline void inverse3(const R* A, R* Ai) {
 #define M3(i, j) A[(i) * 3 + (j)]
-  const double det = M3(0, 0) * M3(1, 1) * M3(2, 2) + M3(0, 1) * M3(1, 2) * M3(2, 0) + M3(0, 2) * M3(1, 0) * M3(2, 1) -
-                     M3(0, 2) * M3(1, 1) * M3(2, 0) - M3(0, 1) * M3(1, 0) * M3(2, 2) - M3(0, 0) * M3(1, 2) * M3(2, 1);
-  const double id = 1.0 / det;
+  const R det = M3(0, 0) * M3(1, 1) * M3(2, 2) + M3(0, 1) * M3(1, 2) * M3(2, 0) + M3(0, 2) * M3(1, 0) * M3(2, 1) -
+                M3(0, 2) * M3(1, 1) * M3(2, 0) - M3(0, 1) * M3(1, 0) * M3(2, 2) - M3(0, 0) * M3(1, 2) * M3(2, 1);
+  const R id = R(1.0) / det;
   Ai[0] = (M3(1, 1) * M3(2, 2) - M3(1, 2) * M3(2, 1)) * id;
   Ai[1] = (M3(0, 2) * M3(2, 1) - M3(0, 1) * M3(2, 2)) * id;
   Ai[2] = (M3(0, 1) * M3(1, 2) - M3(0, 2) * M3(1, 1)) * id;
@@ -565,99 +566,100 @@ __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, cons
   }
   // ---- diffusion sector: time components of the q MRFs and the charge
   // MRFs, coupled into the four-acceleration -----------------------------------
-  double RI[9], MN[3][3], FN[3];
-  if constexpr (std::is_same<R, double>::value) {
+  R RI[9], MN[3][3], FN[3];
+  {   // FP64 form: R = double; mixed form: R = float
     if (dif) {
-      const double sig_ = sig, g_ = g;
+      const R sig_ = sig, g_ = g;
       // reciprocals once (an FP64 division is a long sequence on the FP64
       // pipe): 1/gamma, 1/t and 1/T
-      const double ig_ = ig, it_ = it, iT = 1.0 / T;
-      const double mu[3] = {th[T_MUB], th[T_MUS], th[T_MUQ]};
-      double RS[3], MS[3] = {0, 0, 0};
+      const R ig_ = ig, it_ = it, iT = R(1.0) / T;
+      const R mu[3] = {narrow<R>(th[T_MUB]), narrow<R>(th[T_MUS]), narrow<R>(th[T_MUQ])};
+      R RS[3], MS[3] = {0, 0, 0};
       for (int c = 0; c < 3; c++) RS[c] = -mu[c] * iT;
       for (int i = 0; i < D; i++) MS[i] = Ms[i];
-      double itq[9], itt[9], itk[9];
-      inverse3(dif->tq, itq);
+      R itq[9], itt[9], itk[9], tqr[9];
+      for (int k2 = 0; k2 < 9; k2++) tqr[k2] = narrow<R>(dif->tq[k2]);
+      inverse3<R>(tqr, itq);
       for (int c = 0; c < 3; c++)
         for (int d = 0; d < 3; d++) {
-          double a1 = 0.0, a2 = 0.0;
+          R a1 = R(0.0), a2 = R(0.0);
           for (int kk = 0; kk < 3; kk++) {
-            a1 += itq[3 * c + kk] * dif->tq[3 * kk + d];
-            a2 += itq[3 * c + kk] * dif->kq[3 * kk + d];
+            a1 += itq[3 * c + kk] * narrow<R>(dif->tq[3 * kk + d]);
+            a2 += itq[3 * c + kk] * narrow<R>(dif->kq[3 * kk + d]);
           }
           itt[3 * c + d] = a1;
           itk[3 * c + d] = a2;
         }
       // Cartesian twin (src/eom_cartesian.cpp:1327-1722): no F_D terms, the
       // expansion rate gamma div v alone, metric without tau
-      const double X_ = cart ? g_ * divV : g_ * divV + geo + g_ * it_;
-      const double omg = 1. - g_ * g_;
-      double qc[3][4];
+      const R X_ = cart ? g_ * divV : g_ * divV + geo + g_ * it_;
+      const R omg = R(1.) - g_ * g_;
+      R qc[3][4];
       for (int c = 0; c < 3; c++) {
-        qc[c][0] = dif->q[4 * c];
-        qc[c][1] = -dif->q[4 * c + 1];
-        qc[c][2] = -dif->q[4 * c + 2];
-        qc[c][3] = -t2 * dif->q[4 * c + 3];
+        qc[c][0] = narrow<R>(dif->q[4 * c]);
+        qc[c][1] = -narrow<R>(dif->q[4 * c + 1]);
+        qc[c][2] = -narrow<R>(dif->q[4 * c + 2]);
+        qc[c][3] = -t2 * narrow<R>(dif->q[4 * c + 3]);
       }
-      double F0D[3], F0a[3], A0a[3], R0a[3][3], M0a[3][3], M0D[3][3];
+      R F0D[3], F0a[3], A0a[3], R0a[3][3], M0a[3][3], M0D[3][3];
       for (int c = 0; c < 3; c++) {
-        const double q0 = dif->q[4 * c];
-        F0D[c] = cart ? 0.0
-                      : g_ * g_ * geo * q0 + 2. * g_ * g_ * qc[c][3] * u[2] * it_ + t * g_ * qc[c][0] * u[2] * u[2] +
-                            t * u[2] * dif->q[4 * c + 3];
-        F0a[c] = omg * sig_ * dif->da[c] * Fs;
-        A0a[c] = -omg * dif->da[c] * double(sden) * ig_;
+        const R q0 = narrow<R>(dif->q[4 * c]);
+        F0D[c] = cart ? R(0.0)
+                      : g_ * g_ * geo * q0 + R(2.) * g_ * g_ * qc[c][3] * u[2] * it_ + t * g_ * qc[c][0] * u[2] * u[2] +
+                            t * u[2] * narrow<R>(dif->q[4 * c + 3]);
+        F0a[c] = omg * sig_ * narrow<R>(dif->da[c]) * Fs;
+        A0a[c] = -omg * narrow<R>(dif->da[c]) * sden * ig_;
         for (int i = 0; i < D; i++) {
           M0D[c][i] = g_ * g_ * (qc[c][i + 1] - qc[c][0] * uc[i] * ig_);
-          M0a[c][i] = omg * sig_ * dif->da[c] * MS[i];
-          F0a[c] += -dif->ga[3 * i + c] * u[i] * ig_;
+          M0a[c][i] = omg * sig_ * narrow<R>(dif->da[c]) * MS[i];
+          F0a[c] += -narrow<R>(dif->ga[3 * i + c]) * u[i] * ig_;
         }
         for (int d = 0; d < 3; d++) {
-          R0a[c][d] = omg * sig_ * (dif->da[c] * RS[d] + dif->da[3 + 3 * c + d]);
-          A0a[c] += -omg * dif->da[3 + 3 * c + d] * rho[d] * ig_;
+          R0a[c][d] = omg * sig_ * (narrow<R>(dif->da[c]) * RS[d] + narrow<R>(dif->da[3 + 3 * c + d]));
+          A0a[c] += -omg * narrow<R>(dif->da[3 + 3 * c + d]) * rho[d] * ig_;
         }
       }
       // charge MRFs: R_N = gamma sigma 1 - R_0q, M_N = -M_0q, F_N = -F_0q +
       // grad q - div q - q^0 / t (no external sources)
-      double RN[9];
-      for (int c = 0; c < 9; c++) RN[c] = 0.0;
+      R RN[9];
+      for (int c = 0; c < 9; c++) RN[c] = R(0.0);
       for (int c = 0; c < 3; c++) RN[4 * c] += g_ * sig_;
       for (int c = 0; c < 3; c++) {
-        double F0q = 0.0;
+        R F0q = R(0.0);
         for (int d = 0; d < 3; d++)
-          F0q += (-itt[3 * c + d] * F0D[d] - itq[3 * c + d] * dif->q[4 * d] + itk[3 * c + d] * F0a[d] +
+          F0q += (-itt[3 * c + d] * F0D[d] - itq[3 * c + d] * narrow<R>(dif->q[4 * d]) + itk[3 * c + d] * F0a[d] +
                   itk[3 * c + d] * A0a[d] * X_) * ig_ -
-                 itt[3 * c + d] * dif->q[4 * d] * X_ * ig_;
-        for (int i = 0; i < 3; i++) MN[i][c] = 0.0;
+                 itt[3 * c + d] * narrow<R>(dif->q[4 * d]) * X_ * ig_;
+        for (int i = 0; i < 3; i++) MN[i][c] = R(0.0);
         for (int i = 0; i < D; i++) {
-          double acc = 0.0;
+          R acc = R(0.0);
           for (int d = 0; d < 3; d++)
             acc += (-itt[3 * c + d] * M0D[d][i] + itk[3 * c + d] * M0a[d][i] - itk[3 * c + d] * A0a[d] * uc[i] * ig_) *
                        ig_ +
-                   itt[3 * c + d] * dif->q[4 * d] * uc[i] * ig_ * ig_;
-          MN[i][c] = 0.0 + -acc;
+                   itt[3 * c + d] * narrow<R>(dif->q[4 * d]) * uc[i] * ig_ * ig_;
+          MN[i][c] = R(0.0) + -acc;
         }
         for (int d = 0; d < 3; d++) {
-          double acc = 0.0;
+          R acc = R(0.0);
           for (int kk = 0; kk < 3; kk++) acc += itk[3 * c + kk] * R0a[kk][d] * ig_;
           RN[3 * c + d] += -acc;
         }
-        FN[c] = 0.0;
-        if (cart) FN[c] += -F0q + dif->gq[c] - dif->dq[c];
-        else FN[c] += -F0q + dif->gq[c] - dif->dq[c] - dif->q[4 * c] * it_;
+        FN[c] = R(0.0);
+        if (cart) FN[c] += -F0q + narrow<R>(dif->gq[c]) - narrow<R>(dif->dq[c]);
+        else FN[c] += -F0q + narrow<R>(dif->gq[c]) - narrow<R>(dif->dq[c]) - narrow<R>(dif->q[4 * c]) * it_;
       }
       inverse3(RN, RI);
       // R_u = -u gamma (R_w + R_bulk sigma), R_w = sigma dw/drho + sigma dw/ds R_S
-      double Ru[3][3];
+      R Ru[3][3];
       for (int i = 0; i < D; i++)
         for (int c = 0; c < 3; c++) {
-          const double Rw = sig_ * dwdr[c] + sig_ * dwds * RS[c];
-          Ru[i][c] = -u[i] * g_ * (Rw + 0.0 * sig_);
+          const R Rw = sig_ * dwdr[c] + sig_ * dwds * RS[c];
+          Ru[i][c] = -u[i] * g_ * (Rw + R(0.0) * sig_);
         }
       for (int i = 0; i < D; i++) {
-        double FR = 0.0;
+        R FR = R(0.0);
         for (int j = 0; j < D; j++) {
-          double MR = 0.0;
+          R MR = R(0.0);
           for (int c = 0; c < 3; c++)
             for (int d = 0; d < 3; d++) MR += Ru[i][c] * RI[3 * c + d] * MN[j][d];
           Mu[i * D + j] = Mu[i * D + j] - MR;
@@ -695,87 +697,88 @@ __device__ inline void eom(const ccake_config& cfg, const TransportT<R>& k, cons
   for (int i = 0; i < D; i++) { m1 += Ms[i] * du[i]; m2 += Mb[i] * du[i]; o.du[i] = du[i]; }
   o.dS = m1 + Fs;
   o.dBulk = m2 + Fb;
-  if constexpr (std::is_same<R, double>::value) {
+  {   // FP64 form: R = double; mixed form: R = float
     if (dif) {
       // dN/dt = R_N^-1 (F_N + M_N du/dt); the entropy picks up R_S dN/dt;
       // d(ext q)/dt = F_q + M_q du/dt + R_q dN/dt over all three directions
-      double MU[3], dN[3];
+      R MU[3], dN[3];
       for (int c = 0; c < 3; c++) {
-        MU[c] = 0.;
+        MU[c] = R(0.);
         for (int i = 0; i < D; i++) MU[c] += MN[i][c] * du[i];
       }
       for (int c = 0; c < 3; c++) {
-        dN[c] = 0.;
+        dN[c] = R(0.);
         for (int d = 0; d < 3; d++) dN[c] += RI[3 * c + d] * (FN[d] + MU[d]);
-        dout->dN[c] = dN[c];
+        dout->dN[c] = widen<R>(dN[c]);
       }
-      const double mu[3] = {th[T_MUB], th[T_MUS], th[T_MUQ]};
-      double RS[3], MS[3] = {0, 0, 0};
-      const double iT = 1.0 / T;
+      const R mu[3] = {narrow<R>(th[T_MUB]), narrow<R>(th[T_MUS]), narrow<R>(th[T_MUQ])};
+      R RS[3], MS[3] = {0, 0, 0};
+      const R iT = R(1.0) / T;
       for (int c = 0; c < 3; c++) RS[c] = -mu[c] * iT;
       for (int i = 0; i < D; i++) MS[i] = Ms[i];
-      double rdn = 0.0;
+      R rdn = R(0.0);
       for (int c = 0; c < 3; c++) rdn += RS[c] * dN[c];
       o.dS = m1 + Fs + rdn;
-      double itq[9], itt[9], itk[9];
-      inverse3(dif->tq, itq);
+      R itq[9], itt[9], itk[9], tqr[9];
+      for (int k2 = 0; k2 < 9; k2++) tqr[k2] = narrow<R>(dif->tq[k2]);
+      inverse3<R>(tqr, itq);
       for (int c = 0; c < 3; c++)
         for (int d = 0; d < 3; d++) {
-          double a1 = 0.0, a2 = 0.0;
+          R a1 = R(0.0), a2 = R(0.0);
           for (int kk = 0; kk < 3; kk++) {
-            a1 += itq[3 * c + kk] * dif->tq[3 * kk + d];
-            a2 += itq[3 * c + kk] * dif->kq[3 * kk + d];
+            a1 += itq[3 * c + kk] * narrow<R>(dif->tq[3 * kk + d]);
+            a2 += itq[3 * c + kk] * narrow<R>(dif->kq[3 * kk + d]);
           }
           itt[3 * c + d] = a1;
           itk[3 * c + d] = a2;
         }
-      const double X_ = cart ? g * divV : g * divV + geo + g * it;
-      const double gs = g * sig, igs = 1.0 / gs;
-      const double cmd[4] = {1., -1., -1., cart ? -1. : -it * it};
-      const double fuc[3] = {-u[0], -u[1], -t2 * u[2]};
-      double qc[3][4];
+      const R X_ = cart ? g * divV : g * divV + geo + g * it;
+      const R gs = g * sig, igs = R(1.0) / gs;
+      const R cmd[4] = {R(1.), -R(1.), -R(1.), cart ? -R(1.) : -it * it};
+      const R fuc[3] = {-u[0], -u[1], -t2 * u[2]};
+      R qc[3][4];
       for (int c = 0; c < 3; c++) {
-        qc[c][0] = dif->q[4 * c];
-        qc[c][1] = -dif->q[4 * c + 1];
-        qc[c][2] = -dif->q[4 * c + 2];
-        qc[c][3] = -t2 * dif->q[4 * c + 3];
+        qc[c][0] = narrow<R>(dif->q[4 * c]);
+        qc[c][1] = -narrow<R>(dif->q[4 * c + 1]);
+        qc[c][2] = -narrow<R>(dif->q[4 * c + 2]);
+        qc[c][3] = -t2 * narrow<R>(dif->q[4 * c + 3]);
       }
       for (int i = 0; i < 3; i++) {
-        const double fui = u[i];
-        const double gai[3] = {i < D ? dif->ga[3 * i] : 0.0, i < D ? dif->ga[3 * i + 1] : 0.0,
-                               i < D ? dif->ga[3 * i + 2] : 0.0};
-        double FD[3], Fa[3], Aa[3], MD[3][3], Ma[3][3], Ra[3][3];
+        const R fui = u[i];
+        const R gai[3] = {i < D ? narrow<R>(dif->ga[3 * i]) : R(0.0), i < D ? narrow<R>(dif->ga[3 * i + 1]) : R(0.0),
+                               i < D ? narrow<R>(dif->ga[3 * i + 2]) : R(0.0)};
+        R FD[3], Fa[3], Aa[3], MD[3][3], Ma[3][3], Ra[3][3];
         for (int c = 0; c < 3; c++) {
-          FD[c] = cart ? 0.0 : fui * g * dif->q[4 * c] * geo + 2. * fui * qc[c][3] * u[2] * g * it;
-          Fa[c] = -fui * g * sig * dif->da[c] * Fs + cmd[i + 1] * gai[c];
-          Aa[c] = fui * dif->da[c] * double(sden);
+          FD[c] = cart ? R(0.0) : fui * g * narrow<R>(dif->q[4 * c]) * geo + R(2.) * fui * qc[c][3] * u[2] * g * it;
+          Fa[c] = -fui * g * sig * narrow<R>(dif->da[c]) * Fs + cmd[i + 1] * gai[c];
+          Aa[c] = fui * narrow<R>(dif->da[c]) * sden;
           for (int j = 0; j < 3; j++) {
             MD[c][j] = fui * g * (qc[c][j + 1] - qc[c][0] * fuc[j] * ig);
-            Ma[c][j] = -fui * g * sig * dif->da[c] * MS[j];
+            Ma[c][j] = -fui * g * sig * narrow<R>(dif->da[c]) * MS[j];
           }
           for (int d = 0; d < 3; d++) {
-            Ra[c][d] = -fui * g * sig * (dif->da[c] * RS[d] + dif->da[3 + 3 * c + d]);
-            Aa[c] += fui * dif->da[3 + 3 * c + d] * rho[d];
+            Ra[c][d] = -fui * g * sig * (narrow<R>(dif->da[c]) * RS[d] + narrow<R>(dif->da[3 + 3 * c + d]));
+            Aa[c] += fui * narrow<R>(dif->da[3 + 3 * c + d]) * rho[d];
           }
         }
         for (int c = 0; c < 3; c++) {
-          double F = 0.0, Rq[3];
+          R F = R(0.0), Rq[3];
           for (int d = 0; d < 3; d++) {
-            F += (-itt[3 * c + d] * FD[d] - itq[3 * c + d] * dif->q[4 * d + i + 1] + itk[3 * c + d] * Fa[d] +
+            F += (-itt[3 * c + d] * FD[d] - itq[3 * c + d] * narrow<R>(dif->q[4 * d + i + 1]) + itk[3 * c + d] * Fa[d] +
                   itk[3 * c + d] * Aa[d] * X_) * igs;
-            double R_ = 0.0;
+            R R_ = R(0.0);
             for (int kk = 0; kk < 3; kk++) R_ += itk[3 * c + kk] * Ra[kk][d] * igs;
             Rq[d] = R_;
           }
-          double v = F;
+          R v = F;
           for (int j = 0; j < D; j++) {
-            double M = 0.0;
+            R M = R(0.0);
             for (int d = 0; d < 3; d++)
               M += (-itt[3 * c + d] * MD[d][j] + itk[3 * c + d] * Ma[d][j] - itk[3 * c + d] * Aa[d] * fuc[j] * ig) * igs;
             v += M * du[j];
           }
           for (int d = 0; d < 3; d++) v += Rq[d] * dN[d];
-          dout->dQ[3 * c + i] = v;
+          dout->dQ[3 * c + i] = widen<R>(v);
         }
       }
     }

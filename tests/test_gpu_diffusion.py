@@ -163,7 +163,7 @@ def test_diffusion_numbers_and_system_state(tmp_path):
 
 def test_diffusion_off_matches_plain_and_rejects_unsupported():
     # with kappa = 0 and no initial current the sector leaves the evolution as
-    # it is without it; the mixed form and the DNMR mode reject it
+    # it is without it; the DNMR mode is rejected
     p, rc = ics.hotspots_2d(n_side=32, n_hot=4, seed=5)
     plain = api.GpuHydro(rc)
     plain.load(p)
@@ -175,9 +175,8 @@ def test_diffusion_off_matches_plain_and_rejects_unsupported():
     zero.step(5)
     for f in ("x", "u0", "e", "ext_B"):
         assert relerr(zero.get(f), plain.get(f), 1e-5) < 1e-12, f
-    for bad in (dict(precision=1), dict(diffusion_mode=1)):
-        with pytest.raises(api.CcakeError):
-            api.GpuHydro(dataclasses.replace(rc, using_diffusion=1, **bad))
+    with pytest.raises(api.CcakeError):
+        api.GpuHydro(dataclasses.replace(rc, using_diffusion=1, diffusion_mode=1))
 
 
 def test_diffusion_freeze_out_rows():
