@@ -81,9 +81,11 @@ __device__ __forceinline__ void passA_mixed_body(const RunConst& rc, const Ptrs&
   const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
   // stores row r of the ring for every lane that has an entry there
   int nn = 0, base = 0;
+  int32_t* const nidx = p.nbr_idx;
+  const int32_t* const cand = p.cand_idx;
   auto flush_row = [&](int r) {
     if (nn > r && r < K) {
-      p.nbr_idx[(size_t)r * n + i] = ring_b[wq][r % kRing][lane];
+      nidx[(size_t)r * n + i] = ring_b[wq][r % kRing][lane];
       nf[(size_t)r * n + i] = ring_f[wq][r % kRing][lane];
     }
   };
@@ -92,8 +94,8 @@ __device__ __forceinline__ void passA_mixed_body(const RunConst& rc, const Ptrs&
   const int nc = live ? min(p.cand_cnt[i], p.Kc) : 0;
   const int wnc = kStage ? __reduce_max_sync(0xffffffffu, nc) : nc;
   int bq0 = 0, bq1 = 0;
-  if (nc > 0) bq0 = p.cand_idx[i];
-  if (nc > 1) bq1 = p.cand_idx[(size_t)n + i];
+  if (nc > 0) bq0 = cand[i];
+  if (nc > 1) bq1 = cand[(size_t)n + i];
   for (int kk = 0; kk < wnc; kk++) {
     const bool act = kk < nc;
     if (kStage && (kk % kCheck) == 0) {
@@ -112,7 +114,7 @@ __device__ __forceinline__ void passA_mixed_body(const RunConst& rc, const Ptrs&
     }
     const int b = bq0;
     bq0 = bq1;
-    if (kk + 2 < nc) bq1 = p.cand_idx[(size_t)(kk + 2) * n + i];
+    if (kk + 2 < nc) bq1 = cand[(size_t)(kk + 2) * n + i];
     bool in = false;
     float fg = 0.0f;
     if (act) {
@@ -147,7 +149,7 @@ __device__ __forceinline__ void passA_mixed_body(const RunConst& rc, const Ptrs&
       if (in) {
         if (nn < base) {
           if (nn < K) {
-            p.nbr_idx[(size_t)nn * n + i] = b;
+            nidx[(size_t)nn * n + i] = b;
             nf[(size_t)nn * n + i] = fg;
           }
         } else {
@@ -158,7 +160,7 @@ __device__ __forceinline__ void passA_mixed_body(const RunConst& rc, const Ptrs&
       }
     } else if (in) {
       if (nn < K) {
-        p.nbr_idx[(size_t)nn * n + i] = b;
+        nidx[(size_t)nn * n + i] = b;
         nf[(size_t)nn * n + i] = fg;
       }
       nn++;
@@ -209,7 +211,7 @@ __device__ __forceinline__ void thermo_mixed_body(const RunConst& rc, const EosD
 // particles it does not settle, and every particle of a table EoS, are
 // marked pending for the full inversion (k_thermo_mixed with pending_only),
 // which starts over from the same state: the results are eos_invert's.
-template <int D>
+template <int D, bool DIFF>
 __device__ __forceinline__ void thermo_fast_body(const RunConst& rc, const EosDev& eos, const Ptrs& p, const int i) {
   if (i >= p.n) return;
   const int n = p.n;
@@ -225,7 +227,13 @@ __device__ __forceinline__ void thermo_fast_body(const RunConst& rc, const EosDe
   }
   double th[NTH];
   set_thermo_o(eos, k, x, o, th, true);
-  thermo_store<D, true, false>(rc, p, i, p.clock->t, th, k, 0);
+  if constexpr (DIFF) {
+    double da[12];
+    alpha_derivs_o(eos, k, x, o, da);
+#pragma unroll
+    for (int q = 0; q < 12; q++) p.dif[(size_t)(F_DA + q) * n + i] = da[q];
+  }
+  thermo_store<D, true, DIFF>(rc, p, i, p.clock->t, th, k, 0);
 }
 
 // Diffusion sums of the mixed form, for particle i: the separable sums of
@@ -243,12 +251,15 @@ __device__ __forceinline__ void diffgrad_mixed_body(const Ptrs& p, const int i) 
   const float4* rbf = reinterpret_cast<const float4*>(p.recBf);
   const float4 A0 = rbf[(size_t)i * SB], A1 = rbf[(size_t)i * SB + 1], A2 = rbf[(size_t)i * SB + 2];
   const float va[3] = {A2.z, A2.w, D == 3 ? rbf[(size_t)i * SB + 3].x : 0.0f};
+  // the diffusion record: two 32-byte loads (the slot is 128-byte aligned)
   auto rec = [&](int b, float* f) {
     const float4* rq = reinterpret_cast<const float4*>(p.recQ + (size_t)b * RQ);
+    float4 v[4];
+    ldg256(rq, v[0], v[1]);
+    ldg256(rq + 2, v[2], v[3]);
 #pragma unroll
     for (int k2 = 0; k2 < 4; k2++) {
-      const float4 v = __ldg(rq + k2);
-      f[4 * k2] = v.x; f[4 * k2 + 1] = v.y; f[4 * k2 + 2] = v.z; f[4 * k2 + 3] = v.w;
+      f[4 * k2] = v[k2].x; f[4 * k2 + 1] = v[k2].y; f[4 * k2 + 2] = v[k2].z; f[4 * k2 + 3] = v[k2].w;
     }
   };
   KSum S1[D], SQ0[3][D], SA[3][D], SQI[3];
@@ -264,11 +275,20 @@ __device__ __forceinline__ void diffgrad_mixed_body(const Ptrs& p, const int i) 
 #pragma unroll
   for (int c = 0; c < 3; c++) SQI[c].init(0.0f);
   const float* nf = reinterpret_cast<const float*>(p.nbr_f);
+  const int32_t* nidx = p.nbr_idx;
   const int cnt = min(p.btrack[i], p.K);
+  // list entries streamed one iteration ahead of use
+  int bq = cnt > 0 ? nidx[i] : 0;
+  float fq = cnt > 0 ? nf[i] : 0.0f;
   for (int kk = 0; kk < cnt; kk++) {
-    const int b = p.nbr_idx[(size_t)kk * n + i];
-    const float fg = nf[(size_t)kk * n + i];
-    const float4 B0 = __ldg(rbf + (size_t)b * SB), B1 = __ldg(rbf + (size_t)b * SB + 1);
+    const int b = bq;
+    const float fg = fq;
+    if (kk + 1 < cnt) {
+      bq = nidx[(size_t)(kk + 1) * n + i];
+      fq = nf[(size_t)(kk + 1) * n + i];
+    }
+    float4 B0, B1;
+    ldg256(rbf + (size_t)b * SB, B0, B1);
     const float d[3] = {(A0.x - B0.x) + (A1.x - B1.x), (A0.y - B0.y) + (A1.y - B1.y),
                         (D == 3) ? (A0.z - B0.z) + (A1.z - B1.z) : 0.0f};
     const float mf = B0.w * fg;
@@ -514,12 +534,12 @@ __global__ void __launch_bounds__(kBlock) k_passA_mixed(const __grid_constant__ 
   passA_mixed_body<D>(g.ev[e].rc, g.ev[e].p, first + threadIdx.x);
 }
 
-template <int D>
+template <int D, bool DIFF>
 __global__ void __launch_bounds__(kBlock) k_thermo_fast(const __grid_constant__ GroupArgs g) {
   int first;
   const int e = group_event(g, first);
   if (e < 0) return;
-  thermo_fast_body<D>(g.ev[e].rc, g.ev[e].eos, g.ev[e].p, first + threadIdx.x);
+  thermo_fast_body<D, DIFF>(g.ev[e].rc, g.ev[e].eos, g.ev[e].p, first + threadIdx.x);
 }
 
 template <int D, bool DIFF>
@@ -653,19 +673,25 @@ static bool group_has_diffusion(const GroupArgs& g) {
 void launch_passA_mixed(const GroupArgs& g, int dim, cudaStream_t s) {
   const int nb = g.first_block[g.nev];
   const bool dif = group_has_diffusion(g);
-  // the analytic pass carries no diffusion record: with the sector on, the
-  // full inversion takes every particle
-  const int fast = (!dif && group_has_analytic(g)) ? 1 : 0;
+  const int fast = group_has_analytic(g) ? 1 : 0;
   if (dim == 3) {
     k_passA_mixed<3><<<nb, kBlock, 0, s>>>(g);
-    if (fast) k_thermo_fast<3><<<nb, kBlock, 0, s>>>(g);
-    if (dif) k_thermo_mixed<3, true><<<nb, kBlock, 0, s>>>(g, 0);
-    else k_thermo_mixed<3, false><<<nb, kBlock, 0, s>>>(g, fast);
+    if (dif) {
+      if (fast) k_thermo_fast<3, true><<<nb, kBlock, 0, s>>>(g);
+      k_thermo_mixed<3, true><<<nb, kBlock, 0, s>>>(g, fast);
+    } else {
+      if (fast) k_thermo_fast<3, false><<<nb, kBlock, 0, s>>>(g);
+      k_thermo_mixed<3, false><<<nb, kBlock, 0, s>>>(g, fast);
+    }
   } else {
     k_passA_mixed<2><<<nb, kBlock, 0, s>>>(g);
-    if (fast) k_thermo_fast<2><<<nb, kBlock, 0, s>>>(g);
-    if (dif) k_thermo_mixed<2, true><<<nb, kBlock, 0, s>>>(g, 0);
-    else k_thermo_mixed<2, false><<<nb, kBlock, 0, s>>>(g, fast);
+    if (dif) {
+      if (fast) k_thermo_fast<2, true><<<nb, kBlock, 0, s>>>(g);
+      k_thermo_mixed<2, true><<<nb, kBlock, 0, s>>>(g, fast);
+    } else {
+      if (fast) k_thermo_fast<2, false><<<nb, kBlock, 0, s>>>(g);
+      k_thermo_mixed<2, false><<<nb, kBlock, 0, s>>>(g, fast);
+    }
   }
 }
 
