@@ -511,7 +511,7 @@ static int32_t* eos_scratch(ccake_ctx* ctx, int64_t n) {
     if (ctx->eos_scratch) cudaFree(ctx->eos_scratch);
     ctx->eos_scratch = nullptr;
     ctx->eos_scratch_cap = 0;
-    if (cudaMalloc(&ctx->eos_scratch, (size_t)(2 * n + 2) * sizeof(int32_t)) != cudaSuccess) {
+    if (cudaMalloc(&ctx->eos_scratch, (size_t)(n + 1) * sizeof(int32_t)) != cudaSuccess) {
       cudaGetLastError();
       ctx->eos_scratch = nullptr;
       return nullptr;

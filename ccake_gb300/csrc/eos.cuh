@@ -528,10 +528,8 @@ __host__ __device__ inline double sgnd(double v) { return (0.0 < v) - (v < 0.0);
 
 // Seed sanitising and the perturbed-restart ladder of the reference
 // (src/rootfinder.cpp:421-715).
-// budget: the caller's iteration count above which the ladder stops early
-// (the caller then abandons the whole inversion, see eos_invert).
 __host__ __device__ inline bool find_root(const EosDev& e, int model, int entropy, const double* tgt, double* x,
-                                          int* iters, int budget = 0x7fffffff) {
+                                          int* iters) {
   double lo[4], hi[4];
   model_box(e, model, lo, hi);
   double pos[4] = {x[0], x[1], x[2], x[3]};
@@ -556,7 +554,6 @@ __host__ __device__ inline bool find_root(const EosDev& e, int model, int entrop
                                fmin(0.5 * hi[3], 1.0) * sg[3]}};
   (void)seeds;
   for (int a = 0; a < 10; a++) {
-    if (*iters > budget) return false;
     double y[4] = {list[a][0], list[a][1], list[a][2], list[a][3]};
     if (newton_attempt(e, model, entropy, tgt, lo, hi, y, iters)) {
       for (int i = 0; i < 4; i++) x[i] = y[i];
@@ -638,12 +635,9 @@ __host__ __device__ inline bool analytic_seed(const EosDev& e, int model, const 
 // exact inverse, seed_mode 2 from the given x (a learned seed) on the first
 // model tried; then the reference's seeds. o_out, if given, receives the
 // model thermodynamics at the solution (17 values). Returns the chain index
-// used, or -1. With a budget, an inversion that has spent more Newton
-// iterations than the budget stops and returns -2, leaving x as it was: the
-// caller runs it again without one and gets what a single run would give.
+// used, or -1.
 __host__ __device__ inline int eos_invert(const EosDev& e, int entropy, const double* target, int start, double* x,
-                                          int* iters, int seed_mode = 0, double* o_out = nullptr,
-                                          int budget = 0x7fffffff) {
+                                          int* iters, int seed_mode = 0, double* o_out = nullptr) {
   const double tgt[4] = {target[0], target[1], target[3], target[2]};  // (e|s, B, Q, S)
   const int n = chain_len(e.kind);
   const Scales cdk = model_scales(e, M_CDIAG);
@@ -659,7 +653,6 @@ __host__ __device__ inline int eos_invert(const EosDev& e, int entropy, const do
       model_box(e, model, lo, hi);
       for (int i = 0; i < 4; i++) y[i] = fmin(fmax(prev[i], lo[i]), hi[i]);
       ok = y[0] > 0.0 && newton_attempt(e, model, entropy, tgt, lo, hi, y, &it);
-      if (it > budget) { *iters = it; return -2; }
       if (ok) {   // a root the c_s^2 guard rejects leaves this model to the reference seeds
         double o[17];
         model_thermo(e, model, y, o);
@@ -684,24 +677,22 @@ __host__ __device__ inline int eos_invert(const EosDev& e, int entropy, const do
       double lo[4], hi[4];
       model_box(e, model, lo, hi);
       ok = newton_attempt(e, model, 1, tgt, lo, hi, y, &it);
-      if (it > budget) { *iters = it; return -2; }
     }
     if (ok) {
     } else if (entropy) {
       for (int i = 0; i < 4; i++) y[i] = prev[i];
-      ok = find_root(e, model, 1, tgt, y, &it, budget);
-      if (!ok) { y[0] = prev[0]; y[1] = y[2] = y[3] = 0.0; ok = find_root(e, model, 1, tgt, y, &it, budget); }
+      ok = find_root(e, model, 1, tgt, y, &it);
+      if (!ok) { y[0] = prev[0]; y[1] = y[2] = y[3] = 0.0; ok = find_root(e, model, 1, tgt, y, &it); }
       if (!ok) {
         y[0] = 580.0 / kHbarcMeVfm; y[1] = sgnd(tgt[1]); y[2] = sgnd(tgt[2]); y[3] = sgnd(tgt[3]);
-        ok = find_root(e, model, 1, tgt, y, &it, budget);
+        ok = find_root(e, model, 1, tgt, y, &it);
       }
-      if (!ok) { confdiag_seed(cdk, 1, target, y); ok = find_root(e, model, 1, tgt, y, &it, budget); }
+      if (!ok) { confdiag_seed(cdk, 1, target, y); ok = find_root(e, model, 1, tgt, y, &it); }
     } else {
       y[0] = 580.0 / kHbarcMeVfm; y[1] = sgnd(tgt[1]); y[2] = sgnd(tgt[2]); y[3] = sgnd(tgt[3]);
-      ok = find_root(e, model, 0, tgt, y, &it, budget);
-      if (!ok) { confdiag_seed(cdk, 0, target, y); ok = find_root(e, model, 0, tgt, y, &it, budget); }
+      ok = find_root(e, model, 0, tgt, y, &it);
+      if (!ok) { confdiag_seed(cdk, 0, target, y); ok = find_root(e, model, 0, tgt, y, &it); }
     }
-    if (it > budget) { *iters = it; return -2; }
     // a solution is a finite point with T > 0
     ok = ok && y[0] > 0.0 && y[0] <= 1e300 && fabs(y[1]) <= 1e300 && fabs(y[2]) <= 1e300 && fabs(y[3]) <= 1e300;
     if (ok) {

@@ -157,13 +157,11 @@ void launch_freeze_group(const GroupArgs& g, cudaStream_t s);
 void launch_stop_group(const GroupArgs& g, cudaStream_t s);
 void launch_eos_thermo(const EosDev& eos, int chain_index, int64_t n, const double* tbqs, double* out17,
                        cudaStream_t s);
-// Batch inversion. With scratch (2 n + 2 int32, device) and seed_mode 0 or
-// 2, three passes: the first attempt of every row with a Newton budget of
-// kEosFirstIters, the full inversion of the rows it left with a budget of
-// kEosRestIters, then the full inversion of the rows still left, each pass
-// compacting its rows into warps of their own (same results as one pass).
+// Batch inversion. With scratch (n + 1 int32, device) and seed_mode 0 or 2,
+// two passes: the first attempt of every row with a Newton budget of
+// kEosFirstIters, then the full inversion of the rows it left (same results
+// as one pass).
 constexpr int kEosFirstIters = 8;
-constexpr int kEosRestIters = 200;
 void launch_table_f32(const double* f, float* fd, int64_t nodes, cudaStream_t s);
 void launch_preinv_grid(const PreinvView& P, int64_t tile0, int64_t count, double* in4, double* tbqs, cudaStream_t s);
 void launch_preinv_pack(int64_t count, const double* th16, const int32_t* status, double* out, int32_t* nfail,

@@ -84,25 +84,16 @@ __global__ void k_eos_first(EosDev eos, int entropy, int seed_mode, int max_it, 
   if (th16) set_thermo_o(eos, k, x, o, th16 + 16 * i);
 }
 
-// Passes 2 and 3: the full inversion of the listed rows. Pass 2 stops a row
-// after `budget` Newton iterations and appends it to list2 (the rows that
-// exhaust the reference's restart ladder on a model they leave, ~2000
-// iterations, would otherwise hold a warp of rows that settle in tens);
-// pass 3 (budget < 0, no list2) runs those rows again without one.
+// Pass 2: the full inversion of the listed rows.
 __global__ void k_eos_rest(EosDev eos, int entropy, int seed_mode, const int32_t* list, const int32_t* count,
-                           const double* in4, double* tbqs, double* th16, int32_t* status, int32_t* iters,
-                           int budget, int32_t* list2, int32_t* count2) {
+                           const double* in4, double* tbqs, double* th16, int32_t* status, int32_t* iters) {
   const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= *count) return;
   const int64_t i = list[j];
   double x[4] = {tbqs[4 * i], tbqs[4 * i + 1], tbqs[4 * i + 2], tbqs[4 * i + 3]};
   int it = 0;
   double o[17];
-  const int k = eos_invert(eos, entropy, in4 + 4 * i, 0, x, &it, seed_mode, o, budget >= 0 ? budget : 0x7fffffff);
-  if (k == -2) {
-    list2[atomicAdd(count2, 1)] = (int32_t)i;
-    return;
-  }
+  const int k = eos_invert(eos, entropy, in4 + 4 * i, 0, x, &it, seed_mode, o);
   status[i] = k;
   if (iters) iters[i] = it;
   if (k >= 0) {
@@ -163,16 +154,10 @@ void launch_eos_batch(const EosDev& eos, int entropy, int seed_mode, int64_t n, 
   // the compacted second pass gives the hard rows warps of their own
   int32_t* count = scratch;
   int32_t* list = scratch + 1;
-  int32_t* count2 = scratch + 1 + n;
-  int32_t* list2 = scratch + 2 + n;
   cudaMemsetAsync(count, 0, sizeof(int32_t), s);
-  cudaMemsetAsync(count2, 0, sizeof(int32_t), s);
   k_eos_first<<<nb, kBlock, 0, s>>>(eos, entropy, seed_mode, kEosFirstIters, n, in4, tbqs, th16, status, iters, list,
                                     count);
-  k_eos_rest<<<nb, kBlock, 0, s>>>(eos, entropy, seed_mode, list, count, in4, tbqs, th16, status, iters,
-                                   kEosRestIters, list2, count2);
-  k_eos_rest<<<nb, kBlock, 0, s>>>(eos, entropy, seed_mode, list2, count2, in4, tbqs, th16, status, iters, -1,
-                                   nullptr, nullptr);
+  k_eos_rest<<<nb, kBlock, 0, s>>>(eos, entropy, seed_mode, list, count, in4, tbqs, th16, status, iters);
 }
 
 }  // namespace ccake
