@@ -146,7 +146,9 @@ constexpr double kTanhTc = 220.0 / kHbarcMeVfm, kTanhTs = 120.0 / kHbarcMeVfm;
 template <class R>
 __host__ __device__ inline void solve4(R A[4][4], R* b, R* x);
 
-__host__ __device__ inline void tanh_conformal_thermo(const Scales& k, const double* x4, double* o) {
+// cs2 = false leaves o[6] unset (the Newton iterations read the densities
+// and the susceptibilities only; the 4x4 solve is for c_s^2).
+__host__ __device__ inline void tanh_conformal_thermo(const Scales& k, const double* x4, double* o, bool cs2 = true) {
   double c[17];
   conformal_thermo(k, x4, c);
   const double T = x4[0], mB = x4[1], mQ = x4[2], mS = x4[3];
@@ -164,6 +166,7 @@ __host__ __device__ inline void tanh_conformal_thermo(const Scales& k, const dou
   o[14] = t * c[14] + tp * c[4];
   o[15] = t * c[15] + tp * c[3];
   o[16] = t * c[16] + 2.0 * tp * c[1] + tpp * c[0];
+  if (!cs2) return;
   // c_s^2 = n . chi^-1 n / w, n and chi in (T, muB, muQ, muS) order
   double H[4][4] = {{o[16], o[13], o[14], o[15]},
                     {o[13], o[7], o[10], o[11]},
@@ -354,7 +357,8 @@ __host__ __device__ inline void dens_jac(const EosDev& e, int model, int entropy
     }
     return;
   }
-  model_thermo(e, model, x, o);
+  if (model == M_TANH) tanh_conformal_thermo(model_scales(e, model), x, o, false);
+  else model_thermo(e, model, x, o);
   double H[4][4];
   if (model == M_CDIAG) {
     for (int i = 0; i < 4; i++) for (int j = 0; j < 4; j++) H[i][j] = 0.0;
