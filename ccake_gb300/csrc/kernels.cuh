@@ -115,15 +115,6 @@ struct GroupArgs {
 constexpr int RAF = 16;   // slab floats a particle (the 3-D stride)
 template <int D>
 constexpr int raf_stride() { return D == 3 ? 16 : 12; }
-// The mixed form's gradient record of a particle (floats; the slot is RBF
-// floats). 3-D: 24 floats as six float4, (hi xyz, m) (lo xyz, P/sl^2)
-// (e, Pi/sl^2, v0, v1) (v2, pi^0k/sl^2) (pi^11 pi^12 pi^13 pi^22 /sl^2)
-// (pi^23 pi^33 /sl^2, 0, 0). 2-D: the 16 floats the 2-D sums read, at a
-// 64-byte stride (two 32-byte loads a neighbour instead of two and a half):
-// (hi.x hi.y lo.x lo.y) (m, P/sl^2, e, Pi/sl^2) (v0 v1 pi^01 pi^02 /sl^2)
-// (pi^11 pi^12 pi^22 /sl^2, 0).
-template <int D>
-constexpr int rbf_stride() { return D == 3 ? 24 : 16; }
 constexpr int RBF = 24;
 
 // Pass A modes

@@ -247,34 +247,10 @@ template <int D>
 __device__ __forceinline__ void diffgrad_mixed_body(const Ptrs& p, const int i) {
   if (i >= p.n) return;
   const int n = p.n;
-  constexpr int SB = rbf_stride<D>() / 4;
+  constexpr int SB = RBF / 4;
   const float4* rbf = reinterpret_cast<const float4*>(p.recBf);
-  // positions (hi, lo) as (A0, A1) x y z, the velocity as va, by layout
-  auto pos = [&](int b, float4& H, float4& L, float& m) {
-    float4 R0, R1;
-    ldg256(rbf + (size_t)b * SB, R0, R1);
-    if constexpr (D == 2) {
-      H = make_float4(R0.x, R0.y, 0.0f, 0.0f);
-      L = make_float4(R0.z, R0.w, 0.0f, 0.0f);
-      m = R1.x;
-    } else {
-      H = R0;
-      L = R1;
-      m = R0.w;
-    }
-  };
-  float4 A0, A1;
-  float ma;
-  pos(i, A0, A1, ma);
-  (void)ma;
-  float va[3];
-  if constexpr (D == 2) {
-    const float4 R2 = rbf[(size_t)i * SB + 2];
-    va[0] = R2.x; va[1] = R2.y; va[2] = 0.0f;
-  } else {
-    const float4 R2 = rbf[(size_t)i * SB + 2];
-    va[0] = R2.z; va[1] = R2.w; va[2] = rbf[(size_t)i * SB + 3].x;
-  }
+  const float4 A0 = rbf[(size_t)i * SB], A1 = rbf[(size_t)i * SB + 1], A2 = rbf[(size_t)i * SB + 2];
+  const float va[3] = {A2.z, A2.w, D == 3 ? rbf[(size_t)i * SB + 3].x : 0.0f};
   // the diffusion record: two 32-byte loads (the slot is 128-byte aligned)
   auto rec = [&](int b, float* f) {
     const float4* rq = reinterpret_cast<const float4*>(p.recQ + (size_t)b * RQ);
@@ -312,11 +288,10 @@ __device__ __forceinline__ void diffgrad_mixed_body(const Ptrs& p, const int i) 
       fq = nf[(size_t)(kk + 1) * n + i];
     }
     float4 B0, B1;
-    float mb;
-    pos(b, B0, B1, mb);
+    ldg256(rbf + (size_t)b * SB, B0, B1);
     const float d[3] = {(A0.x - B0.x) + (A1.x - B1.x), (A0.y - B0.y) + (A1.y - B1.y),
                         (D == 3) ? (A0.z - B0.z) + (A1.z - B1.z) : 0.0f};
-    const float mf = mb * fg;
+    const float mf = B0.w * fg;
     float gm[D];
 #pragma unroll
     for (int k = 0; k < D; k++) gm[k] = mf * d[k];
@@ -374,23 +349,10 @@ __device__ __forceinline__ void passB_mixed_body(const RunConst& rc, const Ptrs&
   if (i >= p.n) return;
   const int n = p.n;
   const bool shear = rc.cfg.using_shear;
-  constexpr int SB = rbf_stride<D>() / 4;
+  constexpr int SB = RBF / 4;
   const float4* rbf = reinterpret_cast<const float4*>(p.recBf);
-  // the fields below are named by the 3-D layout; in 2-D they are read from
-  // the compact record (zeros where the 2-D sums read nothing)
-  float4 A0, A1, A2, A3, A4, A5 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-  if constexpr (D == 2) {
-    const float4 R0 = rbf[(size_t)i * SB], R1 = rbf[(size_t)i * SB + 1];
-    const float4 R2 = rbf[(size_t)i * SB + 2], R3 = rbf[(size_t)i * SB + 3];
-    A0 = make_float4(R0.x, R0.y, 0.0f, R1.x);
-    A1 = make_float4(R0.z, R0.w, 0.0f, R1.y);
-    A2 = make_float4(R1.z, R1.w, R2.x, R2.y);
-    A3 = make_float4(0.0f, R2.z, R2.w, 0.0f);
-    A4 = make_float4(R3.x, R3.y, 0.0f, R3.z);
-  } else {
-    A0 = rbf[(size_t)i * SB]; A1 = rbf[(size_t)i * SB + 1]; A2 = rbf[(size_t)i * SB + 2];
-    A3 = rbf[(size_t)i * SB + 3]; A4 = rbf[(size_t)i * SB + 4]; A5 = rbf[(size_t)i * SB + 5];
-  }
+  const float4 A0 = rbf[(size_t)i * SB], A1 = rbf[(size_t)i * SB + 1], A2 = rbf[(size_t)i * SB + 2];
+  const float4 A3 = rbf[(size_t)i * SB + 3], A4 = rbf[(size_t)i * SB + 4], A5 = rbf[(size_t)i * SB + 5];
   KSum S1[D], SP[D], SE[D], SB_[D], SV[D][D], S0[D][D], SD[D];
 #pragma unroll
   for (int k = 0; k < D; k++) {
@@ -436,20 +398,9 @@ __device__ __forceinline__ void passB_mixed_body(const RunConst& rc, const Ptrs&
       fq1 = nf[(size_t)(kk + 2) * n + i];
     }
     const float4* rb = rbf + (size_t)b * SB;
-    float4 B2, B3 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), B4 = B3;
-    if constexpr (D == 2) {
-      // compact record: B0/B1 hold its first 32 bytes, the second 32 follow
-      float4 R2, R3;
-      ldg256(rb + 2, R2, R3);
-      const float4 R0 = B0, R1 = B1;
-      B0 = make_float4(R0.x, R0.y, 0.0f, R1.x);
-      B1 = make_float4(R0.z, R0.w, 0.0f, R1.y);
-      B2 = make_float4(R1.z, R1.w, R2.x, R2.y);
-      B3 = make_float4(0.0f, R2.z, R2.w, 0.0f);
-      B4 = make_float4(R3.x, R3.y, 0.0f, R3.z);
-    } else {
-      ldg256(rb + 2, B2, B3);
-    }
+    float4 B2, B3 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (D == 3 || shear) ldg256(rb + 2, B2, B3);
+    else B2 = __ldg(rb + 2);
     const float d[3] = {(A0.x - B0.x) + (A1.x - B1.x), (A0.y - B0.y) + (A1.y - B1.y),
                         (D == 3) ? (A0.z - B0.z) + (A1.z - B1.z) : 0.0f};
     const float mf = B0.w * fg;
@@ -468,8 +419,9 @@ __device__ __forceinline__ void passB_mixed_body(const RunConst& rc, const Ptrs&
       for (int l = 0; l < D; l++) SV[k][l].add(vb[l] * gm[k]);
     }
     if (shear) {
-      float4 B5 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      float4 B4, B5 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
       if (D == 3) ldg256(rb + 4, B4, B5);
+      else B4 = __ldg(rb + 4);
       const float p0[3] = {B3.y, B3.z, B3.w};
       // pi^{ij}/sl^2 packed (11 12 13 22 23 33)
       const float pij[6] = {B4.x, B4.y, B4.z, B4.w, B5.x, B5.y};
@@ -544,13 +496,8 @@ __device__ __forceinline__ void eom_mixed_body(const RunConst& rc, const Ptrs& p
   if (i >= p.n) return;
   const int n = p.n;
   const float* gf = reinterpret_cast<const float*>(p.grads);
-  const float4 A2 = reinterpret_cast<const float4*>(p.recBf)[(size_t)i * (rbf_stride<D>() / 4) + 2];
-  float va[3];
-  if constexpr (D == 2) {
-    va[0] = A2.x; va[1] = A2.y; va[2] = 0.0f;
-  } else {
-    va[0] = A2.z; va[1] = A2.w; va[2] = p.recBf[(size_t)i * rbf_stride<D>() + 12];
-  }
+  const float4 A2 = reinterpret_cast<const float4*>(p.recBf)[(size_t)i * (RBF / 4) + 2];
+  const float va[3] = {A2.z, A2.w, D == 3 ? p.recBf[(size_t)i * RBF + 12] : 0.0f};
   float gP[3] = {0, 0, 0}, gE[3] = {0, 0, 0}, gB[3] = {0, 0, 0}, gS[3] = {0, 0, 0}, dS[3] = {0, 0, 0};
   float gV[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
 #pragma unroll

@@ -312,22 +312,14 @@ __device__ __forceinline__ void thermo_store(const RunConst& rc, const Ptrs& p, 
 #pragma unroll
     for (int k = 0; k < 3; k++) split2(k < D ? p.y[(Y_X0 + k) * n + i] : 0.0, hi[k], lo[k]);
     const float f = f32_rn(isl2);
-    float4* rb = reinterpret_cast<float4*>(p.recBf) + (size_t)i * (rbf_stride<D>() / 4);
-    if constexpr (D == 2) {
-      rb[0] = make_float4(hi[0], hi[1], lo[0], lo[1]);
-      rb[1] = make_float4(f32_rn(p.m[i]), f32_rn(th[T_P] * isl2), f32_rn(th[T_E]), f32_rn(Pi * isl2));
-      rb[2] = make_float4(f32_rn(p.v[i]), f32_rn(p.v[n + i]), f32_rn(pi[pi_slot(0, 1)]) * f,
-                          f32_rn(pi[pi_slot(0, 2)]) * f);
-      rb[3] = make_float4(f32_rn(pi[P11]) * f, f32_rn(pi[P12]) * f, f32_rn(pi[P22]) * f, 0.0f);
-    } else {
-      rb[0] = make_float4(hi[0], hi[1], hi[2], f32_rn(p.m[i]));
-      rb[1] = make_float4(lo[0], lo[1], lo[2], f32_rn(th[T_P] * isl2));
-      rb[2] = make_float4(f32_rn(th[T_E]), f32_rn(Pi * isl2), f32_rn(p.v[i]), f32_rn(p.v[n + i]));
-      rb[3] = make_float4(f32_rn(p.v[2 * n + i]), f32_rn(pi[pi_slot(0, 1)]) * f, f32_rn(pi[pi_slot(0, 2)]) * f,
-                          f32_rn(pi[pi_slot(0, 3)]) * f);
-      rb[4] = make_float4(f32_rn(pi[P11]) * f, f32_rn(pi[P12]) * f, f32_rn(pi[P13]) * f, f32_rn(pi[P22]) * f);
-      rb[5] = make_float4(f32_rn(pi[P23]) * f, f32_rn(pi[P33]) * f, 0.0f, 0.0f);
-    }
+    float4* rb = reinterpret_cast<float4*>(p.recBf) + (size_t)i * (RBF / 4);
+    rb[0] = make_float4(hi[0], hi[1], hi[2], f32_rn(p.m[i]));
+    rb[1] = make_float4(lo[0], lo[1], lo[2], f32_rn(th[T_P] * isl2));
+    rb[2] = make_float4(f32_rn(th[T_E]), f32_rn(Pi * isl2), f32_rn(p.v[i]), f32_rn(p.v[n + i]));
+    rb[3] = make_float4(f32_rn(p.v[2 * n + i]), f32_rn(pi[pi_slot(0, 1)]) * f, f32_rn(pi[pi_slot(0, 2)]) * f,
+                        f32_rn(pi[pi_slot(0, 3)]) * f);
+    rb[4] = make_float4(f32_rn(pi[P11]) * f, f32_rn(pi[P12]) * f, f32_rn(pi[P13]) * f, f32_rn(pi[P22]) * f);
+    rb[5] = make_float4(f32_rn(pi[P23]) * f, f32_rn(pi[P33]) * f, 0.0f, 0.0f);
   } else {
     double* rb = p.recB + (size_t)i * RB;
     rb[B_X0] = p.y[Y_X0 * n + i];
