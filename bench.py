@@ -371,7 +371,7 @@ def accuracy_vs_oracle(p, rc, orc, O):
     out["with_strangeness"] = {name: errors(gpu_state(ps, rcs, prec), o2.get, o2_tot)
                                for prec, name in ((0, "fp64"), (1, "mixed"))}
     out["note"] = ("max over particles of |gpu - oracle| / |oracle| where |oracle| >= 1e-3 of the field's "
-                   "largest magnitude; the north-star bar is 1e-5 in e and rhoB, rhoS, rhoQ for the mixed form")
+                   "largest magnitude; the mixed form's bar is 1e-5 in e and rhoB, rhoS, rhoQ")
     return out
 
 

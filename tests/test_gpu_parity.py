@@ -1,7 +1,7 @@
 """CUDA path against the CPU oracle, through the C ABI.
 
 Tolerances: neighbour sets bit-exact; fields within 1e-10 relative per
-comparison (the spec FP64 bar), measured as |gpu - oracle| /
+comparison (the FP64 form's bar), measured as |gpu - oracle| /
 (|oracle| + 1e-6 * max|oracle|) so that fields crossing zero are judged
 against their own scale.
 """
