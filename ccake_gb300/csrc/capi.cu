@@ -118,9 +118,24 @@ void drop_graph(ccake_ctx* ctx) {
 void free_lists(ccake_ctx* ctx) {
   if (ctx->p.nbr_idx) cudaFree(ctx->p.nbr_idx);
   if (ctx->p.nbr_f) cudaFree(ctx->p.nbr_f);
+  if (ctx->p.nbr_fe) cudaFree(ctx->p.nbr_fe);
   ctx->p.nbr_idx = nullptr;
   ctx->p.nbr_f = nullptr;
+  ctx->p.nbr_fe = nullptr;
   ctx->p.K = 0;
+}
+
+// The neighbour list of capacity K (with the factorised kernel's second
+// gradient factor when it is on).
+static bool alloc_lists(ccake_ctx* ctx, int K) {
+  const size_t m = (size_t)K * ctx->n;
+  if (cudaMalloc(&ctx->p.nbr_idx, m * sizeof(int32_t)) != cudaSuccess ||
+      cudaMalloc(&ctx->p.nbr_f, m * sizeof(double)) != cudaSuccess)
+    return false;
+  if (ctx->rc.cfg.dim == 3 && ctx->rc.cfg.factorized_kernel &&
+      cudaMalloc(&ctx->p.nbr_fe, m * sizeof(double)) != cudaSuccess)
+    return false;
+  return true;
 }
 
 void free_candidates(ccake_ctx* ctx) {
@@ -294,9 +309,7 @@ ccake_status_t grow_lists(ccake_ctx* ctx) {
     if (mx > ctx->p.K) {
       const int K = capacity_for(mx);
       free_lists(ctx);
-      if (cudaMalloc(&ctx->p.nbr_idx, (size_t)K * ctx->n * sizeof(int32_t)) != cudaSuccess ||
-          cudaMalloc(&ctx->p.nbr_f, (size_t)K * ctx->n * sizeof(double)) != cudaSuccess)
-        return fail(ctx, CCAKE_ERR_NOMEM, "neighbour list allocation");
+      if (!alloc_lists(ctx, K)) return fail(ctx, CCAKE_ERR_NOMEM, "neighbour list allocation");
       ctx->p.K = K;
     }
     enqueue_build(ctx);
@@ -625,7 +638,9 @@ ccake_status_t ccake_ctx_create(const ccake_config* cfg, ccake_ctx** out) {
   if (cfg->precision != 0 && cfg->precision != 1) return CCAKE_ERR_INVALID;
   if (!(cfg->skin_frac >= 0.0)) return CCAKE_ERR_INVALID;
   if (!(cfg->hT > 0) || !(cfg->t0 > 0) || !(cfg->dt > 0)) return CCAKE_ERR_INVALID;
-  if (cfg->dim == 3 && cfg->factorized_kernel) return CCAKE_ERR_INVALID;
+  // the factorised 3-D kernel runs in the FP64 form
+  if (cfg->dim == 3 && cfg->factorized_kernel && (cfg->precision != 0 || !(cfg->hEta > 0.0)))
+    return CCAKE_ERR_INVALID;
   // initial inversion seed: the reference's, or the learned one (table EoS)
   if (cfg->seed_mode != CCAKE_SEED_REFERENCE &&
       !(cfg->seed_mode == CCAKE_SEED_LEARNED && cfg->eos_kind == 2 && !cfg->input_as_entropy))
@@ -651,6 +666,13 @@ ccake_status_t ccake_ctx_create(const ccake_config* cfg, ccake_ctx** out) {
   const int D = cfg->dim;
   const double h = cfg->hT;
   set_kernel_constants(rc, D, h);
+  if (D == 3 && cfg->factorized_kernel) {
+    // W_2D(r_perp, hT) W_1D(|d eta|, hEta); the list keeps the reference's
+    // 2 hT sphere (src/system_state.cpp:650-719)
+    rc.kperp = kernel_const(2, h);
+    rc.keta = kernel_const(1, cfg->hEta);
+    rc.k0 = rc.kperp.wn * rc.keta.wn;
+  }
   // skin: at least one RK2 step of travel at the largest coordinate speed
   // (tau only grows from t0), so that a list lasts a step or more
   const double vmax0 = (D == 3 && cfg->coord == 0) ? std::max(1.0, 1.0 / cfg->t0) : 1.0;
@@ -871,9 +893,7 @@ ccake_status_t ccake_initialize(ccake_ctx* ctx) {
     if (K != ctx->p.K) {
       drop_graph(ctx);
       free_lists(ctx);
-      if (cudaMalloc(&ctx->p.nbr_idx, (size_t)K * ctx->n * sizeof(int32_t)) != cudaSuccess ||
-          cudaMalloc(&ctx->p.nbr_f, (size_t)K * ctx->n * sizeof(double)) != cudaSuccess)
-        return fail(ctx, CCAKE_ERR_NOMEM, "neighbour list allocation");
+      if (!alloc_lists(ctx, K)) return fail(ctx, CCAKE_ERR_NOMEM, "neighbour list allocation");
       ctx->p.K = K;
     }
   }

@@ -89,6 +89,12 @@ struct Grid {
 };
 
 // Run constants passed by value to every kernel.
+// The cubic spline of one dimensionality and smoothing length in the forms
+// the FP64 pair loop evaluates (the same member names as RunConst's own).
+struct KernelConst {
+  double inv_h, wn, wn2, gn, win_c1, win_c2, fin_a, fin_b;
+};
+
 struct RunConst {
   ccake_config cfg;
   Grid grid;
@@ -103,6 +109,9 @@ struct RunConst {
   // fin_a q + fin_b
   double win_c1, win_c2, fin_a, fin_b;
   unsigned long long cut2_bits;   // IEEE bits of cut2 (for the integer-pipe predicate)
+  // 3-D with the factorised kernel (src/kernel.cpp:129-170 of the reference):
+  // W = W_2D(r_perp, hT) W_1D(|d eta|, hEta), the two factors' constants
+  KernelConst kperp, keta;
   double efreeze;        // e(T_FO, 0, 0, 0)
   // FP32 copies for the FP32 pair loops, rounded once on the host (a
   // conversion in a kernel is an FP64-pipe instruction, and the compiler may
@@ -212,6 +221,21 @@ template <typename R>
 __host__ __device__ __forceinline__ double widen(R x) {
   if constexpr (sizeof(R) == sizeof(float)) return f64_of(x);
   else return x;
+}
+
+// Constants of the D-dimensional spline with smoothing length h (host).
+inline KernelConst kernel_const(int D, double h) {
+  KernelConst k;
+  k.inv_h = 1.0 / h;
+  k.wn = knorm(D) / std::pow(h, D);
+  k.wn2 = knorm2(D) / std::pow(h, D);
+  k.gn = kgrad(D) / std::pow(h, D + 1);
+  const double gn2 = kgrad2(D) / std::pow(h, D + 1);
+  k.win_c1 = -1.5 * k.wn;
+  k.win_c2 = 0.75 * k.wn;
+  k.fin_a = 1.5 * gn2 * k.inv_h;
+  k.fin_b = -2.0 * gn2 * k.inv_h;
+  return k;
 }
 
 // Kernel constants of a run with smoothing length h in D dimensions (host).

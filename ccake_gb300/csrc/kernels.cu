@@ -283,6 +283,8 @@ __global__ void __launch_bounds__(kBlock) k_passA(RunConst rc, Ptrs p) {
   // the candidate list of the last build holds every b that can be within
   // 2h now
   const int nc = min(p.cand_cnt[i], p.Kc);
+  // the factorised 3-D kernel (the reference's factorized_kernel option)
+  const bool fact = (D == 3) && rc.cfg.factorized_kernel;
   int kk = 0;
   while (kk < nc) {
     int ns = 0;
@@ -305,11 +307,24 @@ __global__ void __launch_bounds__(kBlock) k_passA(RunConst rc, Ptrs p) {
       // more), whose IEEE bits read as an unsigned integer order like the
       // value, and a NaN of either sign compares above the cut
       if ((unsigned long long)__double_as_longlong(d2) > rc.cut2_bits) continue;
-      double W, fg;
-      pair_kernel(rc, d2, W, fg);
+      double W, fg, fe = 0.0;
+      if (fact) {
+        // W_2D(r_perp, hT) W_1D(|d eta|, hEta) and its gradient
+        // (src/kernel.cpp:129-170): (dW_2D W_1D along d_perp, W_2D dW_1D
+        // along d eta)
+        double W2, g2, W1, g1;
+        pair_kernel(rc.kperp, d[0] * d[0] + d[1] * d[1], W2, g2);
+        pair_kernel(rc.keta, d[2] * d[2], W1, g1);
+        W = W2 * W1;
+        fg = g2 * W1;
+        fe = W2 * g1;
+      } else {
+        pair_kernel(rc, d2, W, fg);
+      }
       if (nn < K) {
         p.nbr_idx[(size_t)nn * n + i] = b;
         p.nbr_f[(size_t)nn * n + i] = fg;
+        if (fact) p.nbr_fe[(size_t)nn * n + i] = fe;
       }
       nn++;
       const double2 b45 = __ldg(&ra[(size_t)b * 4 + 2]);
@@ -372,6 +387,7 @@ __global__ void __launch_bounds__(kBlock) k_diffgrad(Ptrs p) {
     double gm[D];
 #pragma unroll
     for (int k = 0; k < D; k++) gm[k] = mf * d[k];
+    if (D == 3 && p.nbr_fe) gm[D - 1] = (__ldg(rb + B_M) * p.nbr_fe[(size_t)kk * n + i]) * d[D - 1];
 #pragma unroll
     for (int c = 0; c < 3; c++) {
       const double q0 = __ldg(rq + c), al = __ldg(rq + 3 + c);
@@ -445,6 +461,7 @@ __global__ void __launch_bounds__(kBlock) k_passB(RunConst rc, Ptrs p, int mode,
       double gm[D];
 #pragma unroll
       for (int k = 0; k < D; k++) gm[k] = mf * d[k];
+      if (D == 3 && p.nbr_fe) gm[D - 1] = (b23.y * p.nbr_fe[(size_t)kk * n + i]) * d[D - 1];   // factorised kernel
       const double2 b45 = __ldg(reinterpret_cast<const double2*>(rb + 4));
       const double2 b67 = __ldg(reinterpret_cast<const double2*>(rb + 6));
       const double2 v01 = __ldg(reinterpret_cast<const double2*>(rb + B_V0));

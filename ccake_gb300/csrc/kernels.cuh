@@ -51,6 +51,9 @@ struct Ptrs {
   float4* posf;          // FP32 copy of the positions (candidate prefilter)
   int32_t* nbr_idx;      // K * n
   double* nbr_f;         // K * n
+  // factorised 3-D kernel only (else null): grad_a W = (nbr_f dx, nbr_f dy,
+  // nbr_fe d eta), nbr_f = dW_2D factor x W_1D, nbr_fe = W_2D x dW_1D factor
+  double* nbr_fe;        // K * n
   int K;                 // list capacity per particle
   // candidate (Verlet) list: every b within 2h + skin of a at the last
   // build, k-major like the neighbour list; rebuilt every few steps

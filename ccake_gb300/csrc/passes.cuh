@@ -90,7 +90,10 @@ __device__ __forceinline__ float rsqrt_hw(float x) {
 //    branch tests compare the high word of q on the integer pipe.
 // The result is symmetric in the pair (it depends on d2 alone), so the pair
 // sums keep the antisymmetry the conservation laws rest on.
-__device__ __forceinline__ void pair_kernel(const RunConst& rc, double d2, double& W, double& fg) {
+// K: RunConst (the run's kernel) or KernelConst (a factor of the factorised
+// 3-D kernel); the same member names.
+template <class K>
+__device__ __forceinline__ void pair_kernel(const K& rc, double d2, double& W, double& fg) {
   const int hi = max(__double2hiint(d2), 897 << 20);
   const unsigned xf = __funnelshift_l((unsigned)__double2loint(d2), (unsigned)(hi - (896 << 20)), 3);
   const unsigned yb = __float_as_uint(rsqrt_hw(__uint_as_float(xf)));
