@@ -44,7 +44,8 @@ typedef struct ccake_config {
   int32_t using_vorticity;
   int32_t shear_relax_mode;  /* 0 default max(5 eta/w, 0.005), 1 "Gubser" 5 eta/w, 2 minVal */
   int32_t zeta_mode;         /* 0 default 0.005 w/T, 1 constant, 2 cs2-dependent, 3 peaked */
-  int32_t factorized_kernel; /* D=3 W2D(r_perp)*W1D(deta) (src/kernel.cpp:130-170) */
+  int32_t factorized_kernel; /* D=3 W2D(r_perp, hT)*W1D(deta, hEta) (src/kernel.cpp:130-170); FP64
+                                form (precision 0) only, CCAKE_ERR_INVALID otherwise */
   int32_t input_as_entropy;  /* input column is s instead of e */
   int32_t modulate_zeta_with_tanh;
   int32_t thermo_mode;       /* 0 reference dw/ds chain (src/eos.cpp:276-344), 1 exact Hessian inverse */
