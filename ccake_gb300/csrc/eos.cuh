@@ -324,8 +324,29 @@ __host__ __device__ inline void model_box(const EosDev& e, int model, double* lo
 // differentiates it by finite differences), not the interpolated
 // susceptibilities.
 // Jf (mixed form, table model): the Jacobian in FP32 instead of J.
+// Reduced modes of the reference for a model whose chemical-potential axes
+// are frozen (a table with one node along them). Derivatives
+// (src/eos.cpp:129-141): 2 every mu frozen (T-only), 1 muQ and muS frozen
+// (baryon-only), else 0. Root finder (src/rootfinder.cpp:447-491): the same,
+// and only with zero target charges (T-only: B, Q, S; baryon-only: Q, S).
+__host__ __device__ inline int frozen_mode(const EosDev& e, int model) {
+  if (model != M_TABLE) return 0;
+  const bool fb = e.tab.n[1] <= 1, fq = e.tab.n[2] <= 1, fs = e.tab.n[3] <= 1;
+  if (fb && fq && fs) return 2;
+  return (fq && fs) ? 1 : 0;
+}
+__host__ __device__ inline int root_mode(const EosDev& e, int model, const double* tgt) {   // (e|s, B, Q, S)
+  if (model != M_TABLE) return 0;
+  const bool fb = e.tab.n[1] <= 1, fq = e.tab.n[2] <= 1, fs = e.tab.n[3] <= 1;
+  const bool zb = fabs(tgt[1]) < 1e-30, zq = fabs(tgt[2]) < 1e-30, zs = fabs(tgt[3]) < 1e-30;
+  if (fb && fq && fs && zb && zq && zs) return 2;
+  return (fq && fs && zq && zs) ? 1 : 0;
+}
+
+// rmode: in a reduced mode the equations of the frozen chemical potentials
+// are mu = 0 (src/rootfinder.cpp:119-140; their targets are 0).
 __host__ __device__ inline void dens_jac(const EosDev& e, int model, int entropy, const double* x, double* f,
-                                         double J[4][4], float (*Jf)[4] = nullptr) {
+                                         double J[4][4], float (*Jf)[4] = nullptr, int rmode = 0) {
   double o[17];
   if (model == M_TABLE && Jf) {
     float jac[5][4];
@@ -339,6 +360,10 @@ __host__ __device__ inline void dens_jac(const EosDev& e, int model, int entropy
       Jf[1][j] = jac[1][j];
       Jf[2][j] = jac[3][j];
       Jf[3][j] = jac[2][j];
+    }
+    for (int i = (rmode == 2 ? 1 : 2); rmode && i < 4; i++) {
+      f[i] = x[i];
+      for (int j = 0; j < 4; j++) Jf[i][j] = (i == j) ? 1.0f : 0.0f;
     }
     return;
   }
@@ -354,6 +379,10 @@ __host__ __device__ inline void dens_jac(const EosDev& e, int model, int entropy
       J[1][j] = jac[1][j];
       J[2][j] = jac[3][j];
       J[3][j] = jac[2][j];
+    }
+    for (int i = (rmode == 2 ? 1 : 2); rmode && i < 4; i++) {
+      f[i] = x[i];
+      for (int j = 0; j < 4; j++) J[i][j] = (i == j) ? 1.0 : 0.0;
     }
     return;
   }
@@ -418,7 +447,7 @@ __host__ __device__ inline void solve4(R A[4][4], R* b, R* x) {
 // halving; leaving the model box fails.
 __host__ __device__ inline bool newton_attempt(const EosDev& e, int model, int entropy, const double* tgt,
                                                const double* lo, const double* hi, double* x, int* iters,
-                                               int max_it = 100) {
+                                               int max_it = 100, int rmode = 0) {
   // f, J at the current x are carried over from the accepted trial point of
   // the previous iteration (the same values a fresh evaluation would give),
   // so an undamped iteration costs one density/Jacobian evaluation.
@@ -431,7 +460,7 @@ __host__ __device__ inline bool newton_attempt(const EosDev& e, int model, int e
   bool have = false;
   const bool diag = (model == M_CDIAG);
   for (int it = 0; it < max_it; it++) {
-    if (!have) dens_jac(e, model, entropy, x, f, J, f32 ? Jf : nullptr);
+    if (!have) dens_jac(e, model, entropy, x, f, J, f32 ? Jf : nullptr, rmode);
     have = false;
     // the largest |F_i|, NaN if any is NaN: a non-finite residual fails the
     // attempt, as GSL_EBADFUNC fails the reference's solver
@@ -491,7 +520,7 @@ __host__ __device__ inline bool newton_attempt(const EosDev& e, int model, int e
     for (int h = 0; h < 7; h++) {
       for (int i = 0; i < 4; i++) y[i] = x[i] + lam * dx[i];
       if (y[0] > 0) {
-        dens_jac(e, model, entropy, y, f, J, f32 ? Jf : nullptr);
+        dens_jac(e, model, entropy, y, f, J, f32 ? Jf : nullptr, rmode);
         double gmax = 0.0;
         for (int i = 0; i < 4; i++) {
           const double r = fabs(f[i] - tgt[i]);
@@ -537,6 +566,9 @@ __host__ __device__ inline bool find_root(const EosDev& e, int model, int entrop
   double lo[4], hi[4];
   model_box(e, model, lo, hi);
   double pos[4] = {x[0], x[1], x[2], x[3]};
+  // the reduced modes start the frozen potentials at zero
+  const int rmode = root_mode(e, model, tgt);
+  for (int i = (rmode == 2 ? 1 : 2); rmode && i < 4; i++) pos[i] = 0.0;
   const double sg[4] = {1.0, sgnd(tgt[1]), sgnd(tgt[2]), sgnd(tgt[3])};
   for (int i = 0; i < 4; i++)
     if (pos[i] * pos[i] < 1e-10) pos[i] = fmin(0.5 * hi[i], 1.0) * sg[i];
@@ -559,7 +591,7 @@ __host__ __device__ inline bool find_root(const EosDev& e, int model, int entrop
   (void)seeds;
   for (int a = 0; a < 10; a++) {
     double y[4] = {list[a][0], list[a][1], list[a][2], list[a][3]};
-    if (newton_attempt(e, model, entropy, tgt, lo, hi, y, iters)) {
+    if (newton_attempt(e, model, entropy, tgt, lo, hi, y, iters, 100, rmode)) {
       for (int i = 0; i < 4; i++) x[i] = y[i];
       return true;
     }
@@ -656,7 +688,7 @@ __host__ __device__ inline int eos_invert(const EosDev& e, int entropy, const do
       double lo[4], hi[4];
       model_box(e, model, lo, hi);
       for (int i = 0; i < 4; i++) y[i] = fmin(fmax(prev[i], lo[i]), hi[i]);
-      ok = y[0] > 0.0 && newton_attempt(e, model, entropy, tgt, lo, hi, y, &it);
+      ok = y[0] > 0.0 && newton_attempt(e, model, entropy, tgt, lo, hi, y, &it, 100, root_mode(e, model, tgt));
       if (ok) {   // a root the c_s^2 guard rejects leaves this model to the reference seeds
         double o[17];
         model_thermo(e, model, y, o);
@@ -728,6 +760,7 @@ __host__ __device__ inline int eos_invert_first(const EosDev& e, int entropy, co
   double lo[4], hi[4];
   model_box(e, model, lo, hi);
   double y[4];
+  const int rmode = root_mode(e, model, tgt);
   if (seed_mode == 2) {
     for (int i = 0; i < 4; i++) y[i] = fmin(fmax(x[i], lo[i]), hi[i]);
     if (!(y[0] > 0.0)) return -2;
@@ -737,13 +770,14 @@ __host__ __device__ inline int eos_invert_first(const EosDev& e, int entropy, co
     } else {
       y[0] = 580.0 / kHbarcMeVfm; y[1] = sgnd(tgt[1]); y[2] = sgnd(tgt[2]); y[3] = sgnd(tgt[3]);
     }
-    // find_root's seed sanitising
+    // find_root's seed sanitising (and its zeroing of frozen potentials)
+    for (int i = (rmode == 2 ? 1 : 2); rmode && i < 4; i++) y[i] = 0.0;
     const double sg[4] = {1.0, sgnd(tgt[1]), sgnd(tgt[2]), sgnd(tgt[3])};
     for (int i = 0; i < 4; i++)
       if (y[i] * y[i] < 1e-10) y[i] = fmin(0.5 * hi[i], 1.0) * sg[i];
   }
   int it = 0;
-  if (!newton_attempt(e, model, entropy, tgt, lo, hi, y, &it, max_it)) return -2;
+  if (!newton_attempt(e, model, entropy, tgt, lo, hi, y, &it, max_it, rmode)) return -2;
   if (!(y[0] > 0.0 && y[0] <= 1e300 && fabs(y[1]) <= 1e300 && fabs(y[2]) <= 1e300 && fabs(y[3]) <= 1e300))
     return -2;
   double o[17];
@@ -815,7 +849,19 @@ struct Chi { double t2, tb, tq, ts, b2, q2, s2, bq, bs, sq; };
 
 // Schur-complement terms of the reference (src/eos_derivatives.cpp:33-455).
 // which: 0 term1; 1..3 term2(B,S,Q); 4..6 term3(B,S,Q); 7 + 3*j + i term4(j,i).
-__host__ __device__ inline double schur_term(const Chi& x, int which) {
+// rm: the reduced modes (2 T-only, 1 baryon-only; src/eos_derivatives.cpp:
+// 33-45, :74-90, :160-172, :240-254): the Schur complements over the active
+// rows only, with the reference's 1e-30 guards. which: 0 term1, 1..3
+// term2(B, S, Q), 4..6 term3(B, S, Q), 7 + 3j + i term4(j, i).
+__host__ __device__ inline double schur_term(const Chi& x, int which, int rm = 0) {
+  if (rm == 2) return which == 0 ? x.t2 : 0.0;
+  if (rm == 1) {
+    if (which == 0) return x.t2 - (x.tb * x.tb) / (x.b2 + 1e-30);
+    if (which == 1) return x.tb - (x.t2 * x.b2) / (x.tb + 1e-30);
+    if (which == 4) return x.tb - (x.b2 * x.t2) / (x.tb + 1e-30);
+    if (which == 7) return x.b2 - (x.tb * x.tb) / (x.t2 + 1e-30);
+    return 0.0;
+  }
   double a[3], b[3], m[3][3], base;
 #define SET3(v, p, q, r) { v[0] = (p); v[1] = (q); v[2] = (r); }
 #define SETM(a0, a1, a2, b0, b1, b2, c0, c1, c2) \
@@ -894,6 +940,7 @@ __host__ __device__ inline void hessian_inverse(const double H[4][4], const int*
 __host__ __device__ inline void set_thermo_o(const EosDev& e, int k, const double* x, const double* o, double* th,
                                              bool fp32_derivs = false) {
   const int model = chain_model(e.kind, k);
+  const int rm = frozen_mode(e, model);
   const double T = x[0], mB = x[1], mQ = x[2], mS = x[3];
   const double s = o[1], B = o[2], S = o[3], Q = o[4];
   th[T_T] = T; th[T_MUB] = mB; th[T_MUS] = mS; th[T_MUQ] = mQ;
@@ -943,29 +990,29 @@ __host__ __device__ inline void set_thermo_o(const EosDev& e, int k, const doubl
     return;
   }
   double ct = 0.0;
-  if (hB) ct += B / schur_term(X, 1);
-  if (hQ) ct += Q / schur_term(X, 3);
-  if (hS) ct += S / schur_term(X, 2);
-  th[T_DWDS] = T + s / schur_term(X, 0) + ct;
+  if (hB) ct += B / schur_term(X, 1, rm);
+  if (hQ) ct += Q / schur_term(X, 3, rm);
+  if (hS) ct += S / schur_term(X, 2, rm);
+  th[T_DWDS] = T + s / schur_term(X, 0, rm) + ct;
   ct = 0.0;
   if (hB) {
-    ct += s / schur_term(X, 4) + B / schur_term(X, 7 + 0);
-    if (hQ) ct += Q / schur_term(X, 7 + 0 * 3 + 2);
-    if (hS) ct += S / schur_term(X, 7 + 0 * 3 + 1);
+    ct += s / schur_term(X, 4, rm) + B / schur_term(X, 7 + 0, rm);
+    if (hQ) ct += Q / schur_term(X, 7 + 0 * 3 + 2, rm);
+    if (hS) ct += S / schur_term(X, 7 + 0 * 3 + 1, rm);
   }
   th[T_DWDB] = mB + ct;
   ct = 0.0;
   if (hS) {
-    ct += s / schur_term(X, 5) + S / schur_term(X, 7 + 1 * 3 + 1);
-    if (hB) ct += B / schur_term(X, 7 + 1 * 3 + 0);
-    if (hQ) ct += Q / schur_term(X, 7 + 1 * 3 + 2);
+    ct += s / schur_term(X, 5, rm) + S / schur_term(X, 7 + 1 * 3 + 1, rm);
+    if (hB) ct += B / schur_term(X, 7 + 1 * 3 + 0, rm);
+    if (hQ) ct += Q / schur_term(X, 7 + 1 * 3 + 2, rm);
   }
   th[T_DWDSS] = mS + ct;
   ct = 0.0;
   if (hQ) {
-    ct += s / schur_term(X, 6) + Q / schur_term(X, 7 + 2 * 3 + 2);
-    if (hB) ct += B / schur_term(X, 7 + 2 * 3 + 0);
-    if (hS) ct += S / schur_term(X, 7 + 2 * 3 + 1);
+    ct += s / schur_term(X, 6, rm) + Q / schur_term(X, 7 + 2 * 3 + 2, rm);
+    if (hB) ct += B / schur_term(X, 7 + 2 * 3 + 0, rm);
+    if (hS) ct += S / schur_term(X, 7 + 2 * 3 + 1, rm);
   }
   th[T_DWDQ] = mQ + ct;
 }
@@ -980,6 +1027,7 @@ __host__ __device__ inline void set_thermo_o(const EosDev& e, int k, const doubl
 // first. thermo_mode 1: the same with the entries of H^-1 for 1/term.
 __host__ __device__ inline void alpha_derivs_o(const EosDev& e, int k, const double* x, const double* o,
                                                double* out) {
+  const int rm = frozen_mode(e, chain_model(e.kind, k));
   const double T = x[0];
   const double mu[3] = {x[1], x[3], x[2]};
   const double rho[3] = {o[2], o[3], o[4]};
@@ -1016,10 +1064,10 @@ __host__ __device__ inline void alpha_derivs_o(const EosDev& e, int k, const dou
     }
     return;
   }
-  const double t1 = schur_term(X, 0);
+  const double t1 = schur_term(X, 0, rm);
   for (int a = 0; a < 3; a++) {
     double ct = 0.0;
-    if (h[a]) ct += iT / schur_term(X, 1 + a);
+    if (h[a]) ct += iT / schur_term(X, 1 + a, rm);
     out[a] = -mu[a] / T / T / t1 + ct;
   }
   for (int b = 0; b < 3; b++) {
@@ -1027,14 +1075,14 @@ __host__ __device__ inline void alpha_derivs_o(const EosDev& e, int k, const dou
       for (int a = 0; a < 3; a++) out[3 + 3 * a + b] = 0.0;
       continue;
     }
-    const double t3 = schur_term(X, 4 + b);
+    const double t3 = schur_term(X, 4 + b, rm);
     for (int a = 0; a < 3; a++) {
       double v = 0.0;
       if (a == 0 && b == 0) {
-        v += iT / schur_term(X, 7) - mu[0] / T / T / t3;
+        v += iT / schur_term(X, 7, rm) - mu[0] / T / T / t3;
       } else {
         v += -mu[a] / T / T / t3;
-        if (h[a]) v += iT / schur_term(X, 7 + 3 * b + a);
+        if (h[a]) v += iT / schur_term(X, 7 + 3 * b + a, rm);
       }
       out[3 + 3 * a + b] = v;
     }

@@ -139,8 +139,39 @@ void model_thermo(const Config& c, const Table* tab, int model, const double* x4
 // function the solver zeroes; the reference's GSL hybrids solver
 // differentiates it by finite differences), not the interpolated
 // susceptibilities.
+// Reduced modes of the reference for a model whose chemical-potential axes
+// are frozen (a table with one node along them). Derivatives
+// (src/eos.cpp:129-141): 2 every mu frozen (T-only), 1 muQ and muS frozen
+// (baryon-only), else 0. Root finder (src/rootfinder.cpp:447-491): the same,
+// and only with zero target charges (T-only: B, Q, S; baryon-only: Q, S).
+int frozen_mode(const Table* tab, int model) {
+  if (model != mTable || !tab) return 0;
+  const bool fb = tab->n[1] <= 1, fq = tab->n[2] <= 1, fs = tab->n[3] <= 1;
+  if (fb && fq && fs) return 2;
+  return (fq && fs) ? 1 : 0;
+}
+int root_mode(const Table* tab, int model, const double* tgt) {   // tgt order (e|s, B, Q, S)
+  if (model != mTable || !tab) return 0;
+  const bool fb = tab->n[1] <= 1, fq = tab->n[2] <= 1, fs = tab->n[3] <= 1;
+  const bool zb = std::fabs(tgt[1]) < 1e-30, zq = std::fabs(tgt[2]) < 1e-30, zs = std::fabs(tgt[3]) < 1e-30;
+  if (fb && fq && fs && zb && zq && zs) return 2;
+  return (fq && fs && zq && zs) ? 1 : 0;
+}
+
 void densities_and_jacobian(const Config& c, const Table* tab, int model, int entropy,
-                            const double* x, double* f, double J[4][4]) {
+                            const double* x, double* f, double J[4][4], int rmode = 0);
+
+// In a reduced mode the equations of the frozen chemical potentials are
+// mu = 0 (src/rootfinder.cpp:119-140), with the targets of those charges 0.
+void reduce_rows(int rmode, const double* x, double* f, double J[4][4]) {
+  for (int i = (rmode == 2 ? 1 : 2); rmode && i < 4; i++) {
+    f[i] = x[i];
+    for (int j = 0; j < 4; j++) J[i][j] = (i == j) ? 1.0 : 0.0;
+  }
+}
+
+void densities_and_jacobian(const Config& c, const Table* tab, int model, int entropy,
+                            const double* x, double* f, double J[4][4], int rmode) {
   double o[17];
   if (model == mTable) {
     double jac[5][4];
@@ -155,6 +186,7 @@ void densities_and_jacobian(const Config& c, const Table* tab, int model, int en
       J[2][j] = jac[3][j];
       J[3][j] = jac[2][j];
     }
+    reduce_rows(rmode, x, f, J);
     return;
   }
   model_thermo(c, tab, model, x, o);
@@ -222,13 +254,13 @@ inline double nan_max(double a, double b) { return (b > a || b != b) ? b : a; }
 // not depend on where the absolute rule happened to trigger. At most 100
 // iterations; leaving the model's (T, mu) box fails the attempt.
 bool newton_attempt(const Config& c, const Table* tab, int model, int entropy,
-                    const double* tgt, const double* lo, const double* hi, double* x, int* iters) {
+                    const double* tgt, const double* lo, const double* hi, double* x, int* iters, int rmode = 0) {
   const double tol = 1e-10;
   int extra = -1, nslow1 = 0, nslow2 = 0;
   double xgood[4] = {0, 0, 0, 0};
   for (int it = 0; it < 100; it++) {
     double f[4], J[4][4];
-    densities_and_jacobian(c, tab, model, entropy, x, f, J);
+    densities_and_jacobian(c, tab, model, entropy, x, f, J, rmode);
     double F[4] = {f[0] - tgt[0], f[1] - tgt[1], f[2] - tgt[2], f[3] - tgt[3]};
     // maxima propagate NaN (std::max(a, NaN) would return a): a NaN residual
     // fails the iterate, as GSL_EBADFUNC fails the reference's solver
@@ -275,7 +307,7 @@ bool newton_attempt(const Config& c, const Table* tab, int model, int entropy,
       for (int i = 0; i < 4; i++) y[i] = x[i] + lam * dx[i];
       if (y[0] > 0) {
         double fy[4], Jy[4][4];
-        densities_and_jacobian(c, tab, model, entropy, y, fy, Jy);
+        densities_and_jacobian(c, tab, model, entropy, y, fy, Jy, rmode);
         double gmax = 0;
         for (int i = 0; i < 4; i++) gmax = nan_max(gmax, std::fabs(fy[i] - tgt[i]));
         if (gmax <= fmax || h == 6) break;
@@ -289,7 +321,7 @@ bool newton_attempt(const Config& c, const Table* tab, int model, int entropy,
     // five iterations below 0.1 or ten below 0.001 fail the attempt
     if (have) {
       double fy[4], Jy[4][4];
-      densities_and_jacobian(c, tab, model, entropy, y, fy, Jy);
+      densities_and_jacobian(c, tab, model, entropy, y, fy, Jy, rmode);
       double n0 = 0.0, n1 = 0.0;
       for (int i = 0; i < 4; i++) {
         n0 += F[i] * F[i];
@@ -329,12 +361,15 @@ bool find_root(const Config& c, const Table* tab, int model, int entropy, const 
   model_box(c, tab, model, lo, hi);
   const double TOL = 1e-10;
   double pos[4] = {x[0], x[1], x[2], x[3]};
+  // the reduced modes start the frozen potentials at zero
+  const int rmode = root_mode(tab, model, tgt);
+  for (int i = (rmode == 2 ? 1 : 2); rmode && i < 4; i++) pos[i] = 0.0;
   const double sg[4] = {1.0, sgn(tgt[1]), sgn(tgt[2]), sgn(tgt[3])};
   for (int i = 0; i < 4; i++)
     if (pos[i] * pos[i] < TOL) pos[i] = std::min(0.5 * hi[i], 1.0) * sg[i];
   auto attempt = [&](double a, double b, double q, double s_) {
     double y[4] = {a, b, q, s_};
-    if (newton_attempt(c, tab, model, entropy, tgt, lo, hi, y, iters)) {
+    if (newton_attempt(c, tab, model, entropy, tgt, lo, hi, y, iters, rmode)) {
       for (int i = 0; i < 4; i++) x[i] = y[i];
       return true;
     }
@@ -474,14 +509,20 @@ double aTmb(const double a[3], double m[3][3], const double b[3]) {
 
 struct Chi { double t2, tb, tq, ts, b2, q2, s2, bq, bs, sq; };
 
-// src/eos_derivatives.cpp:33-73 (calc_term_1)
-double term1(const Chi& x) {
+// The reduced modes of the terms (rm: 2 T-only, 1 baryon-only; src/
+// eos_derivatives.cpp:33-45, :74-90, :160-172, :240-254): the Schur
+// complements over the active rows only, with the reference's 1e-30 guards.
+double term1(const Chi& x, int rm = 0) {
+  if (rm == 2) return x.t2;
+  if (rm == 1) return x.t2 - (x.tb * x.tb) / (x.b2 + 1e-30);
   double a[3] = {x.tb, x.ts, x.tq};
   double m[3][3] = {{x.b2, x.bs, x.bq}, {x.bs, x.s2, x.sq}, {x.bq, x.sq, x.q2}};
   return x.t2 - aTmb(a, m, a);
 }
 // :75-155 (calc_term_2), i = 0 B, 1 S, 2 Q
-double term2(const Chi& x, int i) {
+double term2(const Chi& x, int i, int rm = 0) {
+  if (rm == 2) return 0.0;
+  if (rm == 1) return i == 0 ? x.tb - (x.t2 * x.b2) / (x.tb + 1e-30) : 0.0;
   if (i == 0) {
     double a[3] = {x.t2, x.ts, x.tq}, b[3] = {x.b2, x.bs, x.bq};
     double m[3][3] = {{x.tb, x.bs, x.bq}, {x.ts, x.s2, x.sq}, {x.tq, x.sq, x.q2}};
@@ -496,7 +537,9 @@ double term2(const Chi& x, int i) {
   return x.tq - aTmb(a, m, b);
 }
 // :157-233 (calc_term_3)
-double term3(const Chi& x, int i) {
+double term3(const Chi& x, int i, int rm = 0) {
+  if (rm == 2) return 0.0;
+  if (rm == 1) return i == 0 ? x.tb - (x.b2 * x.t2) / (x.tb + 1e-30) : 0.0;
   if (i == 0) {
     double a[3] = {x.b2, x.bs, x.bq}, b[3] = {x.t2, x.ts, x.tq};
     double m[3][3] = {{x.tb, x.ts, x.tq}, {x.bs, x.s2, x.sq}, {x.bq, x.sq, x.q2}};
@@ -511,7 +554,9 @@ double term3(const Chi& x, int i) {
   return x.tq - aTmb(a, m, b);
 }
 // :235-455 (calc_term_4(j, i)), indices 0 B, 1 S, 2 Q
-double term4(const Chi& x, int j, int i) {
+double term4(const Chi& x, int j, int i, int rm = 0) {
+  if (rm == 2) return 0.0;
+  if (rm == 1) return (i == 0 && j == 0) ? x.b2 - (x.tb * x.tb) / (x.t2 + 1e-30) : 0.0;
   double a[3], b[3], m[3][3], base;
   auto set = [](double* v, double p, double q, double r) { v[0] = p; v[1] = q; v[2] = r; };
   auto setm = [](double m[3][3], double a0, double a1, double a2, double b0, double b1, double b2,
@@ -584,6 +629,7 @@ void exact_hessian_inverse(const Chi& X, bool diag, double G[4][4]) {
 void eos_set_thermo(const Config& c, const Table* tab, int k, const double x[4], double th[16]) {
   double o[17];
   model_thermo(c, tab, chain_model(c, k), x, o);
+  const int rm = frozen_mode(tab, chain_model(c, k));
   const double T = x[0], mB = x[1], mQ = x[2], mS = x[3];
   const double p = o[0], s = o[1], B = o[2], S = o[3], Q = o[4], e = o[5];
   Chi X{o[16], o[13], o[14], o[15], o[7], o[8], o[9], o[10], o[11], o[12]};
@@ -613,29 +659,29 @@ void eos_set_thermo(const Config& c, const Table* tab, int k, const double x[4],
     return;
   }
   double ct = 0.0;
-  if (hB) ct += B / term2(X, 0);
-  if (hQ) ct += Q / term2(X, 2);
-  if (hS) ct += S / term2(X, 1);
-  th[kDwds] = T + s / term1(X) + ct;
+  if (hB) ct += B / term2(X, 0, rm);
+  if (hQ) ct += Q / term2(X, 2, rm);
+  if (hS) ct += S / term2(X, 1, rm);
+  th[kDwds] = T + s / term1(X, rm) + ct;
   ct = 0.0;
   if (hB) {
-    ct += s / term3(X, 0) + B / term4(X, 0, 0);
-    if (hQ) ct += Q / term4(X, 0, 2);
-    if (hS) ct += S / term4(X, 0, 1);
+    ct += s / term3(X, 0, rm) + B / term4(X, 0, 0, rm);
+    if (hQ) ct += Q / term4(X, 0, 2, rm);
+    if (hS) ct += S / term4(X, 0, 1, rm);
   }
   th[kDwdB] = mB + ct;
   ct = 0.0;
   if (hS) {
-    ct += s / term3(X, 1) + S / term4(X, 1, 1);
-    if (hB) ct += B / term4(X, 1, 0);
-    if (hQ) ct += Q / term4(X, 1, 2);
+    ct += s / term3(X, 1, rm) + S / term4(X, 1, 1, rm);
+    if (hB) ct += B / term4(X, 1, 0, rm);
+    if (hQ) ct += Q / term4(X, 1, 2, rm);
   }
   th[kDwdS] = mS + ct;
   ct = 0.0;
   if (hQ) {
-    ct += s / term3(X, 2) + Q / term4(X, 2, 2);
-    if (hB) ct += B / term4(X, 2, 0);
-    if (hS) ct += S / term4(X, 2, 1);
+    ct += s / term3(X, 2, rm) + Q / term4(X, 2, 2, rm);
+    if (hB) ct += B / term4(X, 2, 0, rm);
+    if (hS) ct += S / term4(X, 2, 1, rm);
   }
   th[kDwdQ] = mQ + ct;
 }
@@ -652,6 +698,7 @@ void eos_set_thermo(const Config& c, const Table* tab, int k, const double x[4],
 void eos_alpha_derivs(const Config& c, const Table* tab, int k, const double x[4], double out[12]) {
   double o[17];
   model_thermo(c, tab, chain_model(c, k), x, o);
+  const int rm = frozen_mode(tab, chain_model(c, k));
   const double T = x[0];
   const double mu[3] = {x[1], x[3], x[2]};            // muB, muS, muQ
   const double rho[3] = {o[2], o[3], o[4]};           // B, S, Q
@@ -679,16 +726,16 @@ void eos_alpha_derivs(const Config& c, const Table* tab, int k, const double x[4
   }
   for (int a = 0; a < 3; a++) {
     double ct = 0.0;
-    if (h[a]) ct += 1 / T / term2(X, a);
-    out[a] = -mu[a] / T / T / term1(X) + ct;
+    if (h[a]) ct += 1 / T / term2(X, a, rm);
+    out[a] = -mu[a] / T / T / term1(X, rm) + ct;
     for (int b = 0; b < 3; b++) {
       double v = 0.0;
       if (h[b]) {
         if (a == b && a == 0) {
-          v += 1 / T / term4(X, b, a) - mu[a] / T / T / term3(X, b);
+          v += 1 / T / term4(X, b, a, rm) - mu[a] / T / T / term3(X, b, rm);
         } else {
-          v += -mu[a] / T / T / term3(X, b);
-          if (h[a]) v += 1 / T / term4(X, b, a);
+          v += -mu[a] / T / T / term3(X, b, rm);
+          if (h[a]) v += 1 / T / term4(X, b, a, rm);
         }
       }
       out[3 + 3 * a + b] = v;
