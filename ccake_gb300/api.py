@@ -33,7 +33,7 @@ class CcakeConfig(ctypes.Structure):
                              "crit_wmuB")] + \
         [(n, _i32) for n in ("delta_pipi_mode", "tau_pipi_mode", "lambda_piPi_mode", "phi6_mode", "phi7_mode",
                              "delta_PiPi_mode", "lambda_Pipi_mode", "phi1_mode", "phi3_mode", "pad3",
-                             "seed_mode", "pad4")]
+                             "seed_mode", "restrict_mu_T_ratios")]
 
 
 class ParticlesSoA(ctypes.Structure):

@@ -682,6 +682,7 @@ ccake_status_t ccake_ctx_create(const ccake_config* cfg, ccake_ctx** out) {
   EosDev& e = ctx->eos;
   e.kind = cfg->eos_kind;
   e.thermo_mode = cfg->thermo_mode;
+  e.restrict_mu_T = cfg->restrict_mu_T_ratios ? 1 : 0;
   e.own = make_scales(cfg->eos_c, cfg->eos_T0, cfg->eos_muB0, cfg->eos_muQ0, cfg->eos_muS0);
   e.conf = e.cdiag = e.own;
   if (e.kind != 2) {   // a table kind sets it with the table

@@ -58,6 +58,9 @@ struct EosDev {
   TableView tab;
   // 1: Newton Jacobians of the table in FP32 (residuals stay FP64)
   int jac32 = 0;
+  // restrict_mu_T_ratios: table solutions with a chemical potential above
+  // 3.5 T are refused (src/eos.cpp:781-786)
+  int restrict_mu_T = 0;
   // device copy of the pre-inverted tables' description; non-null: the step's
   // thermodynamics come from the tables instead of the inversion
   const PreinvView* pre = nullptr;
@@ -665,6 +668,12 @@ __host__ __device__ inline bool analytic_seed(const EosDev& e, int model, const 
   return y[0] > 0.0;
 }
 
+// restrict_mu_T_ratios (src/eos.cpp:781-786): a table solution x = (T, muB,
+// muQ, muS) with max |mu| > 3.5 T is refused.
+__host__ __device__ inline bool mu_T_refused(const EosDev& e, int model, const double* x) {
+  return e.restrict_mu_T && model == M_TABLE && fmax(fmax(fabs(x[1]), fabs(x[3])), fabs(x[2])) > 3.5 * x[0];
+}
+
 // (e|s, B, S, Q) -> (T, muB, muQ, muS) through the EoS chain with the
 // reference's seeds (src/eos.cpp:629-804 entropy mode, :813-975 energy mode).
 // seed_mode 1 (entropy mode) first tries Newton from the analytic model's
@@ -735,6 +744,7 @@ __host__ __device__ inline int eos_invert(const EosDev& e, int entropy, const do
       double o[17];
       model_thermo(e, model, y, o);
       if (!(o[6] >= 0.0 && o[6] <= 1.0)) continue;   // prohibit unstable / acausal cs2
+      if (mu_T_refused(e, model, y)) continue;
       for (int i = 0; i < 4; i++) x[i] = y[i];
       if (o_out)
         for (int i = 0; i < 17; i++) o_out[i] = o[i];
@@ -782,7 +792,7 @@ __host__ __device__ inline int eos_invert_first(const EosDev& e, int entropy, co
     return -2;
   double o[17];
   model_thermo(e, model, y, o);
-  if (!(o[6] >= 0.0 && o[6] <= 1.0)) return -2;
+  if (!(o[6] >= 0.0 && o[6] <= 1.0) || mu_T_refused(e, model, y)) return -2;
   for (int i = 0; i < 4; i++) x[i] = y[i];
   if (o_out)
     for (int i = 0; i < 17; i++) o_out[i] = o[i];

@@ -93,6 +93,8 @@ class RunConfig:
     # initial e -> (T, mu) inversion: 0 the reference's seeds, 2 the learned
     # seed (trained network, table EoS) first
     seed_mode: int = 0
+    # refuse table solutions with a chemical potential above 3.5 T
+    restrict_mu_T_ratios: int = 0
 
 
 @dataclasses.dataclass

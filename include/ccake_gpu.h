@@ -98,7 +98,10 @@ typedef struct ccake_config {
    * step's entropy-mode inversions always start from each particle's
    * previous (T, mu), as the reference's do. */
   int32_t seed_mode;
-  int32_t pad4;
+  /* restrict_mu_T_ratios (src/eos.cpp:781-786; off by default): a table
+   * solution with max(|muB|, |muS|, |muQ|) > 3.5 T is refused and the row
+   * goes down the EoS chain */
+  int32_t restrict_mu_T_ratios;
 } ccake_config;
 
 enum { CCAKE_COEF_DEFAULT = 0, CCAKE_COEF_IS = 1, CCAKE_COEF_DISABLED = 2 };

@@ -469,6 +469,11 @@ int eos_invert(const Config& c, const Table* tab, int entropy, const double targ
       model_thermo(c, tab, model, y, o);
       // prohibit_unstable_cs2 / prohibit_acausal_cs2 default true (include/settings.h:145-147)
       if (!(o[6] >= 0.0 && o[6] <= 1.0)) continue;
+      // restrict_mu_T_ratios (src/eos.cpp:781-786): a table solution with a
+      // chemical potential above 3.5 T is refused
+      if (c.restrict_mu_T_ratios && model == mTable &&
+          std::max(std::max(std::fabs(y[1]), std::fabs(y[3])), std::fabs(y[2])) > 3.5 * y[0])
+        continue;
       for (int i = 0; i < 4; i++) x[i] = y[i];
       if (iterations) *iterations = it;
       return k;

@@ -67,7 +67,7 @@ struct Config {
   // 0 the *_DEFAULT function, 1 israel-stewart (the two deltas), 2 disabled
   int32_t delta_pipi_mode, tau_pipi_mode, lambda_piPi_mode, phi6_mode, phi7_mode;
   int32_t delta_PiPi_mode, lambda_Pipi_mode, phi1_mode, phi3_mode;
-  int32_t pad3;
+  int32_t restrict_mu_T_ratios;           // src/eos.cpp:781-786 (settings, off by default)
 };
 
 // Freeze-out snapshot of one step (FreezeOut::freeze_array,

@@ -30,7 +30,7 @@ class Config(ctypes.Structure):
         "C_B", "reg_chi0", "reg_e0", "reg_xi0", "reg_rq_max", "crit_T", "crit_muB", "crit_wT", "crit_wmuB")] + [
         (n, ctypes.c_int32) for n in ("delta_pipi_mode", "tau_pipi_mode", "lambda_piPi_mode", "phi6_mode",
                                       "phi7_mode", "delta_PiPi_mode", "lambda_Pipi_mode", "phi1_mode",
-                                      "phi3_mode", "pad3")]
+                                      "phi3_mode", "restrict_mu_T_ratios")]
 
 
 def make_config(rc) -> Config:

@@ -65,3 +65,27 @@ def test_zero_charge_event_on_the_T_only_table():
     for f in ("x", "u0", "u1", "ext_s", "T", "e", "ext_shv0"):
         floor = 1e-5 if f[0] == "u" else 1e-6
         assert relerr(gpu.get(f), orc.get(f), floor) < 1e-10, f
+
+
+def test_restrict_mu_T_ratios_parity():
+    # the same rows refused by the GPU inverter and the oracle
+    import fallback_scales as FS
+    from ccake_gb300 import eos_table
+    tab = eos_table.synthetic_table(nT=40, nmu=11)
+    c5, d5 = FS.reference_fallback_scales(*tab, ics.RunConfig().freeze_out_T)
+    rng = np.random.default_rng(4)
+    n = 2000
+    x = np.column_stack([rng.uniform(0.055, 0.3, n), rng.uniform(-0.44, 0.44, n), np.zeros(n), np.zeros(n)])
+    x /= eos_table.HBARC
+    rc = ics.RunConfig(eos_kind=2, thermo_mode=1, restrict_mu_T_ratios=1)
+    g = api.GpuHydro(rc)
+    g.set_eos_table(*tab, c5, d5)
+    ot = O.OracleTable(*tab, c5, d5)
+    fw = g.eos_thermo(0, x)
+    tgt = np.column_stack([fw[:, 1], fw[:, 2], fw[:, 3], fw[:, 4]])
+    xo, _, sto, _ = O.eos_invert_batch(rc, 1, tgt, seeds=x.copy(), table=ot)
+    xg, _, stg, _ = g.eos_invert(1, tgt, x.copy())
+    assert np.mean(stg == sto) > 0.995
+    ratio = np.abs(x[:, 1]) / x[:, 0]
+    assert np.all(stg[ratio > 3.6] != 0)       # no table root above the bound
+    assert np.mean(stg[ratio < 3.0] == 0) > 0.9

@@ -81,3 +81,23 @@ def test_reduced_mode_derivatives(kind):
         want_b = mB + np.where(hB, s / term3 + B / term4, 0.0)
     assert np.allclose(th[ok][:, 12], want_s, rtol=1e-12, atol=0)
     assert np.allclose(th[ok][:, 13], want_b, rtol=1e-12, atol=1e-14)
+
+
+def test_restrict_mu_T_ratios_refuses_table_roots():
+    # src/eos.cpp:781-786: with restrict_mu_T_ratios a table root with
+    # max |mu| > 3.5 T goes down the chain; without it the table keeps it
+    import fallback_scales as FS
+    from ccake_gb300 import eos_table
+    tab = eos_table.synthetic_table(nT=40, nmu=11)
+    c5, d5 = FS.reference_fallback_scales(*tab, ics.RunConfig().freeze_out_T)
+    ot = O.OracleTable(*tab, c5, d5)
+    # (T, muB) in GeV: muB / T = 3.75, 6.7 (refused); 3.0, 1.33 (kept)
+    x = np.array([[0.08, 0.3, 0, 0], [0.06, 0.4, 0, 0], [0.1, 0.3, 0, 0], [0.3, 0.4, 0, 0]]) / eos_table.HBARC
+    rc = ics.RunConfig(eos_kind=2, thermo_mode=1)
+    fw = table_thermo(O.make_config(rc), ot, x)
+    tgt = np.column_stack([fw[:, 1], fw[:, 2], fw[:, 3], fw[:, 4]])
+    _, _, st0, _ = O.eos_invert_batch(rc, 1, tgt, seeds=x.copy(), table=ot)
+    rr = ics.RunConfig(eos_kind=2, thermo_mode=1, restrict_mu_T_ratios=1)
+    _, _, st1, _ = O.eos_invert_batch(rr, 1, tgt, seeds=x.copy(), table=ot)
+    assert list(st0) == [0, 0, 0, 0]
+    assert st1[0] > 0 and st1[1] > 0 and st1[2] == 0 and st1[3] == 0
