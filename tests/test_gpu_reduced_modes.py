@@ -86,6 +86,9 @@ def test_restrict_mu_T_ratios_parity():
     xo, _, sto, _ = O.eos_invert_batch(rc, 1, tgt, seeds=x.copy(), table=ot)
     xg, _, stg, _ = g.eos_invert(1, tgt, x.copy())
     assert np.mean(stg == sto) > 0.995
+    # no table root above the bound; rows drawn well below it stay on the table
+    tab_rows = stg == 0
+    assert np.all(np.max(np.abs(xg[tab_rows][:, 1:]), axis=1) <= 3.5 * xg[tab_rows][:, 0])
     ratio = np.abs(x[:, 1]) / x[:, 0]
-    assert np.all(stg[ratio > 3.6] != 0)       # no table root above the bound
     assert np.mean(stg[ratio < 3.0] == 0) > 0.9
+    assert np.mean(stg[ratio > 3.6] != 0) > 0.9
