@@ -86,9 +86,17 @@ def test_restrict_mu_T_ratios_parity():
     xo, _, sto, _ = O.eos_invert_batch(rc, 1, tgt, seeds=x.copy(), table=ot)
     xg, _, stg, _ = g.eos_invert(1, tgt, x.copy())
     assert np.mean(stg == sto) > 0.995
-    # no table root above the bound; rows drawn well below it stay on the table
+    # no table root above the bound
     tab_rows = stg == 0
     assert np.all(np.max(np.abs(xg[tab_rows][:, 1:]), axis=1) <= 3.5 * xg[tab_rows][:, 0])
-    ratio = np.abs(x[:, 1]) / x[:, 0]
-    assert np.mean(stg[ratio < 3.0] == 0) > 0.9
-    assert np.mean(stg[ratio > 3.6] != 0) > 0.9
+    # against the unrestricted inversion: exactly the table roots above the
+    # bound leave the table, every other row keeps its status and root
+    g0 = api.GpuHydro(ics.RunConfig(eos_kind=2, thermo_mode=1))
+    g0.set_eos_table(*tab, c5, d5)
+    xu, _, stu, _ = g0.eos_invert(1, tgt, x.copy())
+    over = (stu == 0) & (np.max(np.abs(xu[:, 1:]), axis=1) > 3.5 * xu[:, 0])
+    assert over.sum() > 50
+    assert np.all(stg[over] != 0)
+    keep = ~over
+    assert np.array_equal(stg[keep], stu[keep])
+    assert np.array_equal(xg[keep & (stu == 0)], xu[keep & (stu == 0)])
