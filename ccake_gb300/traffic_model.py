@@ -11,7 +11,8 @@ per build. The field lists are the ones the passes of this library touch:
                              the state and the step-start cache, write the state.
 
 `python -m ccake_gb300.traffic_model` writes traffic_model.json beside this
-file (the committed copy).
+file (the committed copy), with the pair-slot counts of `pair_slots` on the
+benchmark lattices.
 """
 from __future__ import annotations
 
@@ -105,16 +106,97 @@ def flops_per_launch(config: str, kernel: str, n: int) -> float:
     return 0.0
 
 
-def as_dict():
-    return {"rule": "compulsory FP64 scalars x 8 B per particle per launch; neighbour reads 0; keys 8 B",
-            "fields": FIELDS, "flops": FLOPS,
-            "bytes_per_particle_step": {c: bytes_per_particle_step(c) for c in ("C1", "C2", "C4")},
-            "flops_per_particle_step": {c: flops_per_particle_step(c) for c in ("C1", "C2", "C4")}}
+def pair_slots(pts, h, skin_frac=0.1, warp=32, icl=8, jcl=4, sample=37):
+    """Pair slots a lane walks per particle under four pair-loop designs, on
+    the particle positions `pts` (n x D) with smoothing length h, for interior
+    particles (at least the median count within 2h):
+
+      in_2h        pairs within 2h (the useful work)
+      candidates   the candidate list within 2h + skin (this library)
+      stencil      the 3^D cells of edge >= 2h + skin around the particle's cell
+      warp_union   the union of the stencils of a warp of 32 consecutive
+                   cell-sorted particles (a warp-uniform loop over staged tiles)
+      cluster      i-clusters of 8 x j-clusters of 4 consecutive cell-sorted
+                   particles whose bounding boxes lie within 2h + skin, per
+                   i-particle (a lane per (i, j) pair, sums reduced by shuffles)
+
+    Counted with a k-d tree (scipy); warps and clusters are sampled."""
+    import numpy as np
+    from scipy.spatial import cKDTree
+    n, D = pts.shape
+    cut, cutc = 2 * h, 2 * h * (1 + skin_frac)
+    tree = cKDTree(pts)
+    nin = np.array([len(l) - 1 for l in tree.query_ball_point(pts, cut * (1 + 1e-12))])
+    ncand = np.array([len(l) - 1 for l in tree.query_ball_point(pts, cutc)])
+    lo = pts.min(0)
+    span = pts.max(0) - lo
+    ncell = np.maximum(np.floor(span / cutc).astype(int), 1)
+    c = np.minimum(np.floor((pts - lo) / (span / ncell)).astype(int), ncell - 1)
+    lin = np.ravel_multi_index(c.T[::-1], ncell[::-1])
+    order = np.argsort(lin, kind="stable")
+    counts = np.bincount(lin, minlength=int(np.prod(ncell))).reshape(ncell[::-1])
+    pad = np.pad(counts, 1)
+    st = np.zeros_like(counts)
+    for off in np.ndindex(*([3] * D)):
+        st += pad[tuple(slice(o, o + s) for o, s in zip(off, counts.shape))]
+    stencil = st.ravel()[lin]
+    cidx = np.array(np.unravel_index(lin[order], ncell[::-1])).T
+    wu = []
+    for w0 in range(0, n, warp * sample):
+        nb = set()
+        for x in {tuple(v) for v in cidx[w0:w0 + warp]}:
+            for off in np.ndindex(*([3] * D)):
+                y = tuple(a + o - 1 for a, o in zip(x, off))
+                if all(0 <= a < s for a, s in zip(y, counts.shape)):
+                    nb.add(y)
+        wu.append(sum(int(counts[y]) for y in nb))
+    ps = pts[order]
+
+    def boxes(k):
+        b = ps[:(n // k) * k].reshape(-1, k, D)
+        return b.min(1), b.max(1)
+    ilo, ihi = boxes(icl)
+    jlo, jhi = boxes(jcl)
+    jt = cKDTree((jlo + jhi) / 2)
+    reach = cutc + (np.max(np.linalg.norm(ihi - ilo, axis=1)) + np.max(np.linalg.norm(jhi - jlo, axis=1))) / 2
+    slots = []
+    for a in range(0, len(ilo), sample):
+        cand = jt.query_ball_point((ilo[a] + ihi[a]) / 2, reach)
+        gap = np.maximum(0, np.maximum(jlo[cand] - ihi[a], ilo[a] - jhi[cand]))
+        slots.append(int(np.sum(np.sum(gap * gap, 1) <= cutc * cutc)) * jcl)
+    inner = nin >= np.percentile(nin, 50)
+    return {"in_2h": float(nin[inner].mean()), "candidates": float(ncand[inner].mean()),
+            "stencil": float(stencil[inner].mean()), "warp_union": float(np.mean(wu)),
+            "cluster": float(np.mean(slots)), "particles_per_cell": float(n / np.prod(ncell))}
+
+
+def bench_lattices():
+    """The 2-D hot-spot lattice (400 x 400, dx 0.05 fm, h 0.1 fm) and the 3-D
+    Milne lattice (120 x 120 x 100, dx 0.1 fm, d eta 0.06, h 0.2)."""
+    import numpy as np
+    xs = -10 + 0.05 * np.arange(400)
+    X, Y = np.meshgrid(xs, xs, indexing="ij")
+    xs3 = -6 + 0.1 * np.arange(120)
+    es = -3 + 0.06 * np.arange(100)
+    E, Y3, X3 = np.meshgrid(es, xs3, xs3, indexing="ij")
+    return {"C2": (np.column_stack([X.ravel(), Y.ravel()]), 0.1),
+            "C4": (np.column_stack([X3.ravel(), Y3.ravel(), E.ravel()]), 0.2)}
+
+
+def as_dict(with_slots=False):
+    d = {"rule": "compulsory FP64 scalars x 8 B per particle per launch; neighbour reads 0; keys 8 B",
+         "fields": FIELDS, "flops": FLOPS,
+         "bytes_per_particle_step": {c: bytes_per_particle_step(c) for c in ("C1", "C2", "C4")},
+         "flops_per_particle_step": {c: flops_per_particle_step(c) for c in ("C1", "C2", "C4")}}
+    if with_slots:
+        d["pair_slots"] = {k: {a: round(b, 1) for a, b in pair_slots(*v).items()}
+                           for k, v in bench_lattices().items()}
+    return d
 
 
 if __name__ == "__main__":
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "traffic_model.json")
     with open(path, "w") as fh:
-        json.dump(as_dict(), fh, indent=1)
+        json.dump(as_dict(with_slots=True), fh, indent=1)
         fh.write("\n")
     print(path)
