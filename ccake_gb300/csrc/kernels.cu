@@ -196,10 +196,13 @@ __global__ void k_sort_cells(Ptrs p, int ncell) {
 
 // Candidate (Verlet) list of particle i: every b != i in the 3^D cells around
 // it whose FP32 squared distance is not above (2h + skin)^2 by more than its
-// error bound (so no pair within 2h + skin in FP64 is dropped), in cell order.
-// With Kc = 0 it only counts. The largest count goes to cand_max (zeroed
-// before the build): the host grows the capacities when it exceeds them and
-// builds again, so no entry past Kc is ever used.
+// error bound (so no pair within 2h + skin in FP64 is dropped). The pairs
+// closer than h (by the FP32 distance) come first, then the rest, each part in
+// cell order: the lanes of a warp then mostly reach the pairs of one kernel
+// branch together in the FP64 pair loop. With Kc = 0 it only counts. The
+// largest count goes to cand_max (zeroed before the build): the host grows
+// the capacities when it exceeds them and builds again, so no entry past Kc is
+// ever used.
 template <int D>
 __global__ void __launch_bounds__(kBlock) k_candidates(RunConst rc, Ptrs p) {
   const int i_ = blockIdx.x * blockDim.x + threadIdx.x;
@@ -209,19 +212,23 @@ __global__ void __launch_bounds__(kBlock) k_candidates(RunConst rc, Ptrs p) {
   const double xa[3] = {p.y[Y_X0 * n + i], p.y[Y_X1 * n + i], D == 3 ? p.y[Y_X2 * n + i] : 0.0};
   const float4 pa = p.posf[i];
   const float cut2f = rc.fcutc2 * 1.000001f;
+  const float h2f = 0.25f * rc.fcut2;   // h^2 = (2h)^2 / 4
   int rlo[D == 3 ? 9 : 3], rhi[D == 3 ? 9 : 3];
   const int nr = live ? neighbour_ranges<D>(rc.grid, p.cell_start, xa, rlo, rhi) : 0;
   const int Kc = p.Kc;
   int c = 0;
-  for (int r = 0; r < nr; r++)
-    for (int j = rlo[r]; j < rhi[r]; j++) {
-      const int b = p.cell_idx[j];
-      if (b == i) continue;
-      float d2f, bound;
-      if (!maybe_neighbour<D>(pa, __ldg(&p.posf[b]), cut2f, d2f, bound)) continue;
-      if (c < Kc) p.cand_idx[(size_t)c * n + i] = b;
-      c++;
-    }
+#pragma unroll 1
+  for (int part = 0; part < 2; part++)
+    for (int r = 0; r < nr; r++)
+      for (int j = rlo[r]; j < rhi[r]; j++) {
+        const int b = p.cell_idx[j];
+        if (b == i) continue;
+        float d2f, bound;
+        if (!maybe_neighbour<D>(pa, __ldg(&p.posf[b]), cut2f, d2f, bound)) continue;
+        if ((d2f < h2f) != (part == 0)) continue;
+        if (c < Kc) p.cand_idx[(size_t)c * n + i] = b;
+        c++;
+      }
   // every lane reaches the warp reduction; lanes past the end count 0
   if (!live) c = 0;
   const int wmax = __reduce_max_sync(0xffffffffu, c);
@@ -319,7 +326,7 @@ __global__ void __launch_bounds__(kBlock) k_passA(RunConst rc, Ptrs p) {
         fg = g2 * W1;
         fe = W2 * g1;
       } else {
-        pair_kernel(rc, d2, W, fg);
+        pair_kernel_warp(rc, d2, W, fg);
       }
       if (nn < K) {
         p.nbr_idx[(size_t)nn * n + i] = b;
@@ -1190,7 +1197,7 @@ __global__ void k_sph_kernel(RunConst rc, int64_t n, const double* r2, double* w
   if (i >= n) return;
   const double d2 = r2[i];
   double W = 0.0, f = 0.0;
-  if ((unsigned long long)__double_as_longlong(d2) <= rc.cut2_bits) pair_kernel(rc, d2, W, f);
+  if ((unsigned long long)__double_as_longlong(d2) <= rc.cut2_bits) pair_kernel_warp(rc, d2, W, f);
   w[i] = W;
   fg[i] = f;
 }

@@ -88,27 +88,77 @@ __device__ __forceinline__ float rsqrt_hw(float x) {
 //    the normal FP32 estimate widened exactly.
 //  * both polynomial branches are evaluated and selected; q >= 0, so the
 //    branch tests compare the high word of q on the integer pipe.
+//  * every product and difference is rounded on its own (_rn intrinsics,
+//    never contracted), so each branch's value does not depend on how the
+//    caller reaches it (pair_kernel_warp below).
 // The result is symmetric in the pair (it depends on d2 alone), so the pair
 // sums keep the antisymmetry the conservation laws rest on.
 // K: RunConst (the run's kernel) or KernelConst (a factor of the factorised
 // 3-D kernel); the same member names.
 template <class K>
-__device__ __forceinline__ void pair_kernel(const K& rc, double d2, double& W, double& fg) {
+__device__ __forceinline__ void pair_q(const K& rc, double d2, double& y, double& q) {
   const int hi = max(__double2hiint(d2), 897 << 20);
   const unsigned xf = __funnelshift_l((unsigned)__double2loint(d2), (unsigned)(hi - (896 << 20)), 3);
   const unsigned yb = __float_as_uint(rsqrt_hw(__uint_as_float(xf)));
   const double y0 = __hiloint2double((int)((yb >> 3) + (896u << 20)), (int)(yb << 29));
-  const double e = fma(-(d2 * y0), y0, 1.0);
-  const double y = fma(y0, e * fma(0.375, e, 0.5), y0);   // 1/r
-  const double q = (d2 * y) * rc.inv_h;
-  const double Win = fma(q * q, fma(rc.win_c2, q, rc.win_c1), rc.wn);
-  const double z = 2.0 - q, z2 = z * z;
-  const double Wout = (rc.wn2 * z) * z2;
-  const double fin = fma(rc.fin_a, q, rc.fin_b), fout = (rc.gn * y) * z2;
+  const double e = fma(-__dmul_rn(d2, y0), y0, 1.0);
+  y = fma(y0, __dmul_rn(e, fma(0.375, e, 0.5)), y0);   // 1/r
+  q = __dmul_rn(__dmul_rn(d2, y), rc.inv_h);
+}
+
+// q < 1 (src/kernel.cpp:40-44, :103-106)
+template <class K>
+__device__ __forceinline__ void pair_inner(const K& rc, double q, double& W, double& fg) {
+  W = fma(__dmul_rn(q, q), fma(rc.win_c2, q, rc.win_c1), rc.wn);
+  fg = fma(rc.fin_a, q, rc.fin_b);
+}
+
+// 1 <= q < 2 (src/kernel.cpp:45-47, :107-112)
+template <class K>
+__device__ __forceinline__ void pair_outer(const K& rc, double q, double y, double& W, double& fg) {
+  const double z = __dsub_rn(2.0, q), z2 = __dmul_rn(z, z);
+  W = __dmul_rn(__dmul_rn(rc.wn2, z), z2);
+  fg = __dmul_rn(__dmul_rn(rc.gn, y), z2);
+}
+
+template <class K>
+__device__ __forceinline__ void pair_kernel(const K& rc, double d2, double& W, double& fg) {
+  double y, q, Win, fin, Wout, fout;
+  pair_q(rc, d2, y, q);
+  pair_inner(rc, q, Win, fin);
+  pair_outer(rc, q, y, Wout, fout);
   const int qh = __double2hiint(q);
   const bool in1 = qh < 0x3FF00000, in2 = qh < 0x40000000;   // q < 1, q < 2
   W = in1 ? Win : (in2 ? Wout : 0.0);
   fg = in1 ? fin : (in2 ? fout : 0.0);
+}
+
+// pair_kernel for a warp: when every active lane is on the same side of
+// q = 1, only that side's polynomial runs (6 or 4 FP64 instructions fewer a
+// pair; the candidate lists put the pairs within h first, so on a lattice
+// the lanes of a warp mostly agree). The same operations as pair_kernel on
+// each side, hence the same bits whichever path a lane takes.
+template <class K>
+__device__ __forceinline__ void pair_kernel_warp(const K& rc, double d2, double& W, double& fg) {
+  double y, q;
+  pair_q(rc, d2, y, q);
+  const int qh = __double2hiint(q);
+  const bool in1 = qh < 0x3FF00000, in2 = qh < 0x40000000;   // q < 1, q < 2
+  const unsigned act = __activemask();
+  if (__all_sync(act, in1)) {
+    pair_inner(rc, q, W, fg);
+  } else if (__all_sync(act, !in1)) {
+    double Wo, fo;
+    pair_outer(rc, q, y, Wo, fo);
+    W = in2 ? Wo : 0.0;
+    fg = in2 ? fo : 0.0;
+  } else {
+    double Win, fin, Wout, fout;
+    pair_inner(rc, q, Win, fin);
+    pair_outer(rc, q, y, Wout, fout);
+    W = in1 ? Win : (in2 ? Wout : 0.0);
+    fg = in1 ? fin : (in2 ? fout : 0.0);
+  }
 }
 
 // Squared FP32 pair distance and the radial factor fg of grad_a W =
