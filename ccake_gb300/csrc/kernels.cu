@@ -436,8 +436,13 @@ __global__ void __launch_bounds__(kBlock) k_diffgrad(Ptrs p) {
 // ---------------------------------------------------------------------------
 // pass B
 // ---------------------------------------------------------------------------
+// The 2-D launch is held to 168 registers (3 blocks, 12 warps an SM instead of
+// 8): its loop and equations of motion are bound by the FP64 pipe, which more
+// warps keep busier, at the cost of a few hundred bytes of spills (the FP64
+// step 3.04 -> 2.94 ms at 160k particles; 128 registers was no better). The
+// 3-D instantiations, with larger live sets, keep the plain bound.
 template <int D, bool DIFF>
-__global__ void __launch_bounds__(kBlock) k_passB(RunConst rc, Ptrs p, int mode, double dt_sub) {
+__global__ void __launch_bounds__(kBlock, (D == 2) ? 3 : 1) k_passB(RunConst rc, Ptrs p, int mode, double dt_sub) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= p.n) return;
   const int n = p.n;
