@@ -6,6 +6,9 @@ The device function takes 1/r from the FP32 hardware estimate and one
 third-order correction step; its error bound (1/r to within a few ulp) is
 what these checks hold it to, at every lattice distance of the benchmark
 grids (q = 1 and q = 2 exactly among them), at random distances and at zero.
+It runs one branch's polynomial for a warp whose lanes agree on q < 1 and
+both otherwise; the values must not depend on which, so the same inputs in
+other orders give the same bits.
 """
 import numpy as np
 import pytest
@@ -75,6 +78,14 @@ def test_pair_kernel_matches_oracle_and_bound(D, h, dx):
     # symmetric by construction: the same d2 gives the same bits
     W2, fg2 = api.sph_kernel(D, h, r2[::-1].copy())
     assert np.array_equal(W2[::-1], W) and np.array_equal(fg2[::-1], fg)
+    # whatever the other lanes of its warp hold: sorted inputs put whole warps
+    # on one side of q = 1 (one polynomial runs), a shuffle mixes them (both run)
+    perm = rng.permutation(len(r2))
+    W3, fg3 = api.sph_kernel(D, h, r2[perm].copy())
+    assert np.array_equal(W3, W[perm]) and np.array_equal(fg3, fg[perm])
+    srt = np.argsort(r2, kind="stable")
+    W4, fg4 = api.sph_kernel(D, h, r2[srt].copy())
+    assert np.array_equal(W4, W[srt]) and np.array_equal(fg4, fg[srt])
 
 
 def test_pair_kernel_rejects_bad_input():
