@@ -196,10 +196,15 @@ __global__ void k_sort_cells(Ptrs p, int ncell) {
 
 // Candidate (Verlet) list of particle i: every b != i in the 3^D cells around
 // it whose FP32 squared distance is not above (2h + skin)^2 by more than its
-// error bound (so no pair within 2h + skin in FP64 is dropped). The pairs
-// closer than h (by the FP32 distance) come first, then the rest, each part in
-// cell order: the lanes of a warp then mostly reach the pairs of one kernel
-// branch together in the FP64 pair loop. With Kc = 0 it only counts. The
+// error bound (so no pair within 2h + skin in FP64 is dropped). In the FP64
+// form the list is in three parts by the FP32 distance at the build, each in
+// cell order: the pairs with r < 0.9 h, those with 0.9 h <= r < 1.1 h, then
+// the rest. The lanes of a warp then mostly reach pairs on the same side of
+// r = h together in the FP64 pair loop (on a lattice with h = 2 dx, r = h
+// exactly is a lattice distance: those pairs, on either side as the
+// particles move, are kept together in the middle part). The mixed form's
+// FP32 loops gain nothing from it and gather better in plain cell order,
+// which they keep. With Kc = 0 it only counts. The
 // largest count goes to cand_max (zeroed before the build): the host grows
 // the capacities when it exceeds them and builds again, so no entry past Kc is
 // ever used.
@@ -212,20 +217,21 @@ __global__ void __launch_bounds__(kBlock) k_candidates(RunConst rc, Ptrs p) {
   const double xa[3] = {p.y[Y_X0 * n + i], p.y[Y_X1 * n + i], D == 3 ? p.y[Y_X2 * n + i] : 0.0};
   const float4 pa = p.posf[i];
   const float cut2f = rc.fcutc2 * 1.000001f;
-  const float h2f = 0.25f * rc.fcut2;   // h^2 = (2h)^2 / 4
+  const float h2lo = 0.2025f * rc.fcut2, h2hi = 0.3025f * rc.fcut2;   // (0.9 h)^2, (1.1 h)^2
   int rlo[D == 3 ? 9 : 3], rhi[D == 3 ? 9 : 3];
   const int nr = live ? neighbour_ranges<D>(rc.grid, p.cell_start, xa, rlo, rhi) : 0;
   const int Kc = p.Kc;
   int c = 0;
+  const int nparts = rc.cfg.precision == 0 ? 3 : 1;
 #pragma unroll 1
-  for (int part = 0; part < 2; part++)
+  for (int part = 0; part < nparts; part++)
     for (int r = 0; r < nr; r++)
       for (int j = rlo[r]; j < rhi[r]; j++) {
         const int b = p.cell_idx[j];
         if (b == i) continue;
         float d2f, bound;
         if (!maybe_neighbour<D>(pa, __ldg(&p.posf[b]), cut2f, d2f, bound)) continue;
-        if ((d2f < h2f) != (part == 0)) continue;
+        if (nparts > 1 && (d2f < h2lo ? 0 : (d2f < h2hi ? 1 : 2)) != part) continue;
         if (c < Kc) p.cand_idx[(size_t)c * n + i] = b;
         c++;
       }
