@@ -53,9 +53,13 @@ FIELDS = {
 # FP64 operations (an FMA counts 2) of the FP64 form per particle and launch.
 # C2 (the bench event) from the kernels' FP64 instructions, counted in the
 # source and checked against ncu (2 DFMA + DMUL + DADD per launch over the
-# 160k particles: pass A smoothing 1797, EoS 490, pass B 3886):
-#   pair_A  38 = displacement 2 + exact |d|^2 3 + kernel values 23 (1/r by
-#                the refined FP32 estimate, W and grad-W branches) + 5 sums 10
+# 160k particles: pass A smoothing 1511, EoS 481, pass B 3873):
+#   pair_A  31 = displacement 2 + exact |d|^2 3 + kernel values + 5 sums 10;
+#                the kernel values cost 23 with both branches (1/r by the
+#                refined FP32 estimate, W and grad-W of q < 1 and q >= 1)
+#                and 13 or 15 when the warp's lanes agree on one branch,
+#                which the ordered candidate lists make the common case
+#                (31 is the measured mean)
 #   pair_B  43 = m fg 1 + displacement 2 + m grad W 2 + 9 separable sums with
 #                shear (S1, SP, SE, SB, SV, S0, SD) 38
 #   particle_A  gamma, v and the LRF densities; eos the inversion and the
@@ -64,7 +68,7 @@ FIELDS = {
 # table EoS and bulk in C4).
 FLOPS = {
     "C1": {"neighbours": 48, "pair_A": 38, "pair_B": 27, "particle_A": 60, "eos": 250, "eom": 700},
-    "C2": {"neighbours": 46, "pair_A": 38, "pair_B": 43, "particle_A": 60, "eos": 490, "eom": 1910},
+    "C2": {"neighbours": 46, "pair_A": 31, "pair_B": 43, "particle_A": 60, "eos": 490, "eom": 1910},
     "C4": {"neighbours": 447, "pair_A": 40, "pair_B": 60, "particle_A": 80, "eos": 1200, "eom": 2500},
 }
 
