@@ -21,6 +21,20 @@ __global__ void __launch_bounds__(kBlock) k_thermo(RunConst rc, EosDev eos, Ptrs
   thermo_tail<D, false, DIFF>(rc, eos, p, i, p.clock->t);
 }
 
+// The same for an EoS of kind KIND known at launch (an analytic model, no
+// pre-inverted tables): the kind in a local copy is a constant, so the
+// chain's table and tanh-conformal code drops out of the kernel and the
+// inversion of the same model runs in fewer registers.
+template <int D, bool DIFF, int KIND>
+__global__ void __launch_bounds__(kBlock) k_thermo_kind(RunConst rc, EosDev eos, Ptrs p) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.n) return;
+  EosDev e = eos;
+  e.kind = KIND;
+  e.pre = nullptr;
+  thermo_tail<D, false, DIFF>(rc, e, p, i, p.clock->t);
+}
+
 // seeds (n rows of T, muB, muQ, muS, or null): the learned seed of every
 // particle, tried first on the first model of the chain
 __global__ void k_init_invert(RunConst rc, EosDev eos, Ptrs p, const double* seeds) {
@@ -126,6 +140,9 @@ void launch_thermo(const RunConst& rc, const EosDev& eos, const Ptrs& p, cudaStr
   if (rc.cfg.dim == 3) {
     if (dif) k_thermo<3, true><<<nb, kBlock, 0, s>>>(rc, eos, p);
     else k_thermo<3, false><<<nb, kBlock, 0, s>>>(rc, eos, p);
+  } else if (eos.kind == 1 && !eos.pre) {
+    if (dif) k_thermo_kind<2, true, 1><<<nb, kBlock, 0, s>>>(rc, eos, p);
+    else k_thermo_kind<2, false, 1><<<nb, kBlock, 0, s>>>(rc, eos, p);
   } else {
     if (dif) k_thermo<2, true><<<nb, kBlock, 0, s>>>(rc, eos, p);
     else k_thermo<2, false><<<nb, kBlock, 0, s>>>(rc, eos, p);
