@@ -331,7 +331,7 @@ def accuracy_vs_oracle(p, rc, orc, O):
     RK2 steps against the oracle's state after the same steps (plain
     relative error of e and the densities; velocities against their range),
     on the 160k event and on the same event with strangeness (rhoS = 0.2
-    rhoB cos x), so that all four densities are judged."""
+    rhoB cos x), so that all four densities are checked."""
     import dataclasses
     from ccake_gb300 import api, ics
     fields = ("e", "rhoB", "rhoS", "rhoQ", "s", "T")

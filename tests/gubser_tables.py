@@ -31,7 +31,7 @@ def sph_fields(get, tau):
 
 def line_errors(table, line, x, y, fields, dx, xlim):
     """Max |SPH - table| over the table's points with |x| <= xlim, per field,
-    divided by the field's largest magnitude in the table (T is judged
+    divided by the field's largest magnitude in the table (T is checked
     relative to the local value)."""
     sel = np.abs(y) < 0.25 * dx if line == "y=0" else np.abs(x - y) < 0.25 * dx
     xs = x[sel]

@@ -5,7 +5,7 @@ workloads, through the C ABI.
   conformal constant, 100 RK2 steps.
 * The viscous BSQ hot-spot event, 400 x 400 lattice (160,000 particles),
   200 RK2 steps; and the same event with strangeness (rhoS != 0), so that
-  all four densities are judged.
+  all four densities are checked.
 
 Bars: neighbour sets bit-exact at step 0 and at the last step (the oracle is
 given the GPU's positions there, so the two searches see the same inputs);

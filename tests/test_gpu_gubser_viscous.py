@@ -46,7 +46,7 @@ def test_viscous_gubser_gpu_matches_oracle():
     for f in ("x", "y", "u0", "u1", "ext_s", "T", "e", "sigma_lab", "ext_shv0", "ext_shv1", "ext_shv3", "shv11",
               "shv22", "shv12", "shv33", "Ez"):
         a, b = g.get(f), orc.get(f)
-        # u^y, u^x and pi^xy vanish on the axes: judged against 1e-5 of their range
+        # u^y, u^x and pi^xy vanish on the axes: checked against 1e-5 of their range
         floor = 1e-5 if f in ("u0", "u1", "ext_shv1", "shv12") else 1e-6
         scale = np.abs(b) + floor * np.max(np.abs(b)) + 1e-300
         assert np.max(np.abs(a - b) / scale) < 1e-10, f

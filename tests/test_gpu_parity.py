@@ -2,7 +2,7 @@
 
 Tolerances: neighbour sets bit-exact; fields within 1e-10 relative per
 comparison (the FP64 form's bar), measured as |gpu - oracle| /
-(|oracle| + 1e-6 * max|oracle|) so that fields crossing zero are judged
+(|oracle| + 1e-6 * max|oracle|) so that fields crossing zero are checked
 against their own scale.
 """
 import dataclasses
@@ -406,7 +406,7 @@ def test_cartesian_parity(dim):
     gpu.step(steps)
     assert orc.step(steps) == 0
     for f in fields:
-        # velocities cross zero: judged against 1e-5 of their range
+        # velocities cross zero: checked against 1e-5 of their range
         floor = 1e-5 if f in ("u0", "u1", "u2") else 1e-6
         assert relerr(gpu.get(f), orc.get(f), floor) < RTOL, f
     tg, to = gpu.totals(), orc.totals()

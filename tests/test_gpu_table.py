@@ -196,7 +196,7 @@ def test_table_eos_hydro_parity(table, precision):
     tol = 1e-10 if precision == 0 else 1e-5
     for f in ("T", "muB", "e", "ext_s"):
         assert relerr(g.get(f), orc.get(f), floor=1e-3) < tol, f
-    # velocities and shear start at zero: judged against 1e-2 of their range
+    # velocities and shear start at zero: checked against 1e-2 of their range
     for f in ("u0", "shv11"):
         assert relerr(g.get(f), orc.get(f), floor=1e-2) < tol, f
     assert np.array_equal(g.get_int("eos_id"), orc.get_int("eos_id"))
